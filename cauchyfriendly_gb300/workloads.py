@@ -1,0 +1,159 @@
+"""Seeded synthetic estimation problems.
+
+The reference publishes no dataset for this path; its demos feed fixed or
+simulated measurement sequences into ``CauchyEstimator::step``
+(src/cauchy_estimator.cpp:57-433).  These generators build linear systems of
+the documented shapes and simulate Cauchy-noise measurement histories with
+numpy's PCG64 so every consumer (tests, bench, the CPU baseline) sees the same
+inputs for a given seed.
+
+A problem is a plain dict:
+  d, pncc, cmcc, p       state dim, process-noise columns, control columns,
+                         scalar measurements per step
+  Phi (d,d)  Gamma (d,pncc)  beta (pncc,)  H (p,d)  gamma (p,)
+  B (d,cmcc) or None
+  A0 (d,d)  p0 (d,)  b0 (d,)
+  steps                  estimation steps (the reference's ``steps`` argument)
+  msmts (steps, p)       measurement history; row k is fed at step k
+"""
+from __future__ import annotations
+
+import numpy as np
+
+__all__ = [
+    "simulate", "three_state_lti", "random_stable", "batched_three_state",
+    "four_state_lti", "two_state_lti", "five_state_two_msmt",
+]
+
+
+def _cauchy(rng, scale, size=None):
+    return rng.standard_cauchy(size) * scale
+
+
+def simulate(prob, rng, outlier_frac=0.0, outlier_scale=1.0):
+    """Simulates x_{k+1} = Phi x_k + Gamma w_k, z_k = H x_k + v_k with Cauchy w, v.
+
+    The first measurement is taken at the initial state, matching the
+    reference's first step, which is a measurement update only
+    (include/cauchy_estimator.hpp:1179).
+    """
+    d, p, pncc = prob["d"], prob["p"], prob["pncc"]
+    Phi, Gamma, H = prob["Phi"], prob["Gamma"], prob["H"]
+    beta, gamma = np.asarray(prob["beta"]), np.asarray(prob["gamma"])
+    A0, p0, b0 = prob["A0"], prob["p0"], prob["b0"]
+    # initial state: b0 + A0^{-1} (Cauchy(p0)) -- scales act along the rows of A0
+    x = b0 + np.linalg.solve(A0, _cauchy(rng, p0, d))
+    zs = np.zeros((prob["steps"], p))
+    for k in range(prob["steps"]):
+        if k > 0:
+            w = _cauchy(rng, beta, pncc)
+            x = Phi @ x + Gamma @ w
+        v = _cauchy(rng, gamma, p)
+        if outlier_frac > 0:
+            mask = rng.random(p) < outlier_frac
+            v = np.where(mask, v * outlier_scale, v)
+        zs[k] = H @ x + v
+    return zs
+
+
+def _base(d, pncc, p, Phi, Gamma, beta, H, gamma, p0, steps):
+    return {
+        "d": d, "pncc": pncc, "cmcc": 0, "p": p,
+        "Phi": np.asarray(Phi, dtype=np.float64).reshape(d, d),
+        "Gamma": np.asarray(Gamma, dtype=np.float64).reshape(d, pncc),
+        "beta": np.asarray(beta, dtype=np.float64).reshape(pncc),
+        "H": np.asarray(H, dtype=np.float64).reshape(p, d),
+        "gamma": np.asarray(gamma, dtype=np.float64).reshape(p),
+        "B": None,
+        "A0": np.eye(d), "p0": np.asarray(p0, dtype=np.float64).reshape(d),
+        "b0": np.zeros(d), "steps": int(steps),
+    }
+
+
+def three_state_lti(seed=0, steps=8):
+    """Plain 3-state LTI problem: Phi=[[1,.1,0],[0,1,.1],[0,0,.95]],
+    Gamma=[0,0,1]^T, H=[1,0,0], beta=0.1, gamma=0.2, p0=[.1,.08,.05]."""
+    prob = _base(3, 1, 1,
+                 [[1.0, 0.1, 0.0], [0.0, 1.0, 0.1], [0.0, 0.0, 0.95]],
+                 [0.0, 0.0, 1.0], [0.1], [1.0, 0.0, 0.0], [0.2], [0.1, 0.08, 0.05], steps)
+    prob["msmts"] = simulate(prob, np.random.Generator(np.random.PCG64(seed)))
+    return prob
+
+
+def random_stable(rng, d, rho_lo, rho_hi):
+    """Random real matrix with eigenvalue moduli uniform in [rho_lo, rho_hi]:
+    a block-diagonal real-Schur-like matrix (2x2 rotation-scale blocks plus a
+    1x1 block for odd d) under a random orthogonal similarity."""
+    blocks = np.zeros((d, d))
+    i = 0
+    while i < d:
+        r = rng.uniform(rho_lo, rho_hi)
+        if i + 1 < d and rng.random() < 0.5:
+            th = rng.uniform(0.05, np.pi - 0.05)
+            c, s = np.cos(th), np.sin(th)
+            blocks[i:i + 2, i:i + 2] = r * np.array([[c, -s], [s, c]])
+            i += 2
+        else:
+            blocks[i, i] = r * (1.0 if rng.random() < 0.8 else -1.0)
+            i += 1
+    Q, R = np.linalg.qr(rng.standard_normal((d, d)))
+    Q = Q * np.sign(np.diag(R))
+    return Q @ blocks @ Q.T
+
+
+def _log_uniform(rng, lo, hi, size=None):
+    return np.exp(rng.uniform(np.log(lo), np.log(hi), size))
+
+
+def batched_three_state(n, seed=0, steps_lo=4, steps_hi=9, outlier_frac=0.05, outlier_scale=100.0):
+    """Batch of independent 3-state LTI estimators: random stable Phi with
+    eigenvalue moduli in [0.8, 1.0], Gamma=[0,0,1]^T, H=[1,0,0], beta, gamma
+    and p0 log-uniform in [0.02, 0.5], steps uniform in [steps_lo, steps_hi],
+    measurement histories with 5% impulsive outliers at 100x scale."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    probs = []
+    for _ in range(n):
+        Phi = random_stable(rng, 3, 0.8, 1.0)
+        beta = _log_uniform(rng, 0.02, 0.5, 1)
+        gamma = _log_uniform(rng, 0.02, 0.5, 1)
+        p0 = _log_uniform(rng, 0.02, 0.5, 3)
+        steps = int(rng.integers(steps_lo, steps_hi + 1))
+        prob = _base(3, 1, 1, Phi, [0.0, 0.0, 1.0], beta, [1.0, 0.0, 0.0], gamma, p0, steps)
+        prob["msmts"] = simulate(prob, rng, outlier_frac, outlier_scale)
+        probs.append(prob)
+    return probs
+
+
+def four_state_lti(seed=0, steps=7):
+    """4-state LTI problem: Phi random with spectral radius 0.95, Gamma 4x1 and
+    H 1x4 with N(0,1) entries, beta=0.1, gamma=0.2."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    M = rng.standard_normal((4, 4))
+    Phi = 0.95 * M / np.max(np.abs(np.linalg.eigvals(M)))
+    Gamma = rng.standard_normal((4, 1))
+    H = rng.standard_normal((1, 4))
+    prob = _base(4, 1, 1, Phi, Gamma, [0.1], H, [0.2], [0.1, 0.1, 0.1, 0.1], steps)
+    prob["msmts"] = simulate(prob, rng)
+    return prob
+
+
+def two_state_lti(seed=0, steps=10):
+    """2-state LTI problem with a non-trivial H.Gamma (well-defined moments)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    Phi = random_stable(rng, 2, 0.85, 1.0)
+    prob = _base(2, 1, 1, Phi, [1.0, 0.3], [0.1], [1.0, 1.0], [0.2], [0.1, 0.05], steps)
+    prob["msmts"] = simulate(prob, rng)
+    return prob
+
+
+def five_state_two_msmt(seed=0, steps=3):
+    """5-state problem with two process-noise columns and two scalar
+    measurements per step (Phi = expm(0.1 A), A ~ N(0, 0.3^2))."""
+    from scipy.linalg import expm
+    rng = np.random.Generator(np.random.PCG64(seed))
+    Phi = expm(0.1 * rng.normal(0.0, 0.3, (5, 5)))
+    Gamma = 0.1 * rng.standard_normal((5, 2))
+    H = rng.standard_normal((2, 5))
+    prob = _base(5, 2, 2, Phi, Gamma, [0.05, 0.05], H, [0.1, 0.1], 0.1 * np.ones(5), steps)
+    prob["msmts"] = simulate(prob, rng)
+    return prob

@@ -1,0 +1,311 @@
+"""Test infrastructure: the CPU oracle for the MCE step path.
+
+Two checkers live here, and only tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline legs may use them:
+
+* ``Oracle`` — ``mce_oracle.cpp``, a serial C++ restatement of the reference's
+  ``CauchyEstimator::step`` (include/cauchy_estimator.hpp:1211-1245), built
+  into ``oracle/_build`` by :func:`build`.
+* ``Reference`` — ``ref_harness.cpp`` compiled from the reference's own headers
+  where they lie (only when the reference sources are present), built into
+  ``oracle/_ref``.  Used to generate the golden fixtures and to pin the oracle.
+
+Both expose the same stepping interface so tests can run either on a problem
+dict from :mod:`cauchyfriendly_gb300.workloads`.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REF_OUT = os.path.join(HERE, "_ref")
+REFERENCE_INCLUDE = "/root/reference/include"
+ORACLE_SO = os.path.join(BUILD, "libmce_oracle.so")
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+def _ptr(a, kind=_dp):
+    if a is None:
+        return None
+    return a.ctypes.data_as(kind)
+
+
+def build(force=False, with_reference=True, verbose=False):
+    """Compiles the oracle (always) and the reference harness (when the
+    reference headers are present).  -ffp-contract=off keeps a*b+c unfused on
+    every host so results match across x86 and aarch64."""
+    os.makedirs(BUILD, exist_ok=True)
+    jobs = []
+    src = os.path.join(HERE, "mce_oracle.cpp")
+    if force or not os.path.exists(ORACLE_SO) or os.path.getmtime(ORACLE_SO) < os.path.getmtime(src):
+        jobs.append(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-std=c++17", src,
+                     "-o", ORACLE_SO, "-lpthread"])
+    if with_reference and os.path.isdir(REFERENCE_INCLUDE):
+        os.makedirs(REF_OUT, exist_ok=True)
+        hsrc = os.path.join(HERE, "ref_harness.cpp")
+        ncpu = 1
+        while ncpu * 2 <= (os.cpu_count() or 1):
+            ncpu *= 2
+        for name, n in (("libmce_ref_serial.so", 1), ("libmce_ref_threaded.so", ncpu)):
+            out = os.path.join(REF_OUT, name)
+            if force or not os.path.exists(out) or os.path.getmtime(out) < os.path.getmtime(hsrc):
+                jobs.append(["g++", "-O3", "-ffp-contract=off", "-fPIC", "-shared", "-w",
+                             "-I" + REFERENCE_INCLUDE, "-DHARNESS_NUM_CPUS=%d" % n, hsrc, "-o", out,
+                             "-lpthread"])
+    procs = [subprocess.Popen(j, stdout=subprocess.PIPE, stderr=subprocess.STDOUT) for j in jobs]
+    for j, p in zip(jobs, procs):
+        out, _ = p.communicate()
+        if p.returncode != 0:
+            raise RuntimeError("oracle build failed: %s\n%s" % (" ".join(j), out.decode()))
+        if verbose:
+            print(" ".join(j))
+
+
+def reference_available():
+    return os.path.exists(os.path.join(REF_OUT, "libmce_ref_serial.so"))
+
+
+_libc = ctypes.CDLL(None)
+
+
+def draw_reference_constants(seed, d, max_shape, num_cpus=8):
+    """Reproduces the reference constructor's libc rand() draws after
+    srand(seed): root_point[i] = 1 + U(0,1] (include/cauchy_estimator.hpp:127-128)
+    then num_cpus DCE helpers each draw b_pert[i] = 2 U(0,1] - 1
+    (include/cell_enumeration.hpp:467-470); helper 0's b_pert is returned."""
+    _libc.srand(ctypes.c_uint(seed))
+    rmax = 2147483647.0
+
+    def u():
+        return (float(_libc.rand()) + 1.0) / (rmax + 1.0)
+
+    root = np.array([1.0 + u() for _ in range(d)])
+    bpert = None
+    for h in range(num_cpus):
+        bp = np.array([2.0 * u() - 1.0 for _ in range(max_shape)])
+        if h == 0:
+            bpert = bp
+    return root, bpert
+
+
+def max_shape_of(prob):
+    d, pncc = prob["d"], prob["pncc"]
+    return (prob["steps"] - 1) * pncc + d if d > 1 else d + pncc
+
+
+class _Lib:
+    def __init__(self, path, prefix):
+        self.lib = ctypes.CDLL(path)
+        self.prefix = prefix
+        L = self.lib
+        f = lambda n: getattr(L, prefix + n)
+        f("step").restype = ctypes.c_int
+        f("step").argtypes = [ctypes.c_void_p, ctypes.c_double, _dp, _dp, _dp, _dp, ctypes.c_double, _dp, _dp]
+        f("destroy").argtypes = [ctypes.c_void_p]
+        f("num_terms").argtypes = [ctypes.c_void_p]
+        f("shape_range").argtypes = [ctypes.c_void_p]
+        f("terms_per_shape").argtypes = [ctypes.c_void_p, _ip]
+        f("get_moments").argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        f("total_cells").restype = ctypes.c_longlong
+        f("total_cells").argtypes = [ctypes.c_void_p]
+        f("dump_terms").argtypes = [ctypes.c_void_p, _ip, _dp, _dp, _dp, _ip, _ip, _dp]
+
+    def fn(self, name):
+        return getattr(self.lib, self.prefix + name)
+
+
+class _EstimatorBase:
+    """Common stepping/readout over the oracle or the reference harness."""
+
+    def __init__(self, lib, handle, prob):
+        self._l = lib
+        self.h = handle
+        self.prob = prob
+        self.d = prob["d"]
+
+    def step(self, k, sub=0):
+        """Feeds measurement ``sub`` of step ``k``; returns the error bitmask."""
+        prob = self.prob
+        Phi = np.ascontiguousarray(prob["Phi"] if prob["Phi"].ndim == 2 else prob["Phi"][k], dtype=np.float64)
+        Gamma = np.ascontiguousarray(prob["Gamma"], dtype=np.float64)
+        beta = np.ascontiguousarray(prob["beta"], dtype=np.float64)
+        H = np.ascontiguousarray(prob["H"][sub], dtype=np.float64)
+        B = None if prob.get("B") is None else np.ascontiguousarray(prob["B"], dtype=np.float64)
+        u = None
+        if B is not None:
+            u = np.ascontiguousarray(prob["u"][k], dtype=np.float64)
+        z = float(prob["msmts"][k, sub])
+        return self._l.fn("step")(self.h, z, _ptr(Phi), _ptr(Gamma), _ptr(beta), _ptr(H),
+                                  float(prob["gamma"][sub]), _ptr(B), _ptr(u))
+
+    def moments(self):
+        d = self.d
+        fz = np.zeros(2); mean = np.zeros(2 * d); cov = np.zeros(2 * d * d)
+        rfz = np.zeros(2); rmean = np.zeros(2 * d); rcov = np.zeros(2 * d * d)
+        gs = np.zeros(1)
+        self._l.fn("get_moments")(self.h, _ptr(fz), _ptr(mean), _ptr(cov), _ptr(rfz), _ptr(rmean),
+                                  _ptr(rcov), _ptr(gs))
+        c = lambda a: a[0::2] + 1j * a[1::2]
+        return {"fz": complex(fz[0], fz[1]), "mean": c(mean), "cov": c(cov).reshape(d, d),
+                "raw_fz": complex(rfz[0], rfz[1]), "raw_mean": c(rmean), "raw_cov": c(rcov).reshape(d, d),
+                "gscale": float(gs[0])}
+
+    def num_terms(self):
+        return int(self._l.fn("num_terms")(self.h))
+
+    def terms_per_shape(self):
+        n = int(self._l.fn("shape_range")(self.h))
+        out = np.zeros(n, dtype=np.int32)
+        self._l.fn("terms_per_shape")(self.h, _ptr(out, _ip))
+        return out
+
+    def dump_terms(self, max_shape):
+        nt = self.num_terms()
+        tc = int(self._l.fn("total_cells")(self.h))
+        d = self.d
+        shape = np.zeros(nt, dtype=np.int32)
+        A = np.zeros(nt * max_shape * d)
+        p = np.zeros(nt * max_shape)
+        b = np.zeros(nt * d)
+        cells = np.zeros(nt, dtype=np.int32)
+        keys = np.zeros(max(tc, 1), dtype=np.int32)
+        g = np.zeros(2 * max(tc, 1))
+        self._l.fn("dump_terms")(self.h, _ptr(shape, _ip), _ptr(A), _ptr(p), _ptr(b), _ptr(cells, _ip),
+                                 _ptr(keys, _ip), _ptr(g))
+        return {"shape": shape, "A": A.reshape(nt, max_shape, d), "p": p.reshape(nt, max_shape),
+                "b": b.reshape(nt, d), "cells": cells, "keys": keys[:tc],
+                "g": (g[0::2] + 1j * g[1::2])[:tc]}
+
+    def close(self):
+        if self.h:
+            self._l.fn("destroy")(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_oracle_lib = None
+_ref_libs = {}
+
+
+def _load_oracle():
+    global _oracle_lib
+    if _oracle_lib is None:
+        if not os.path.exists(ORACLE_SO):
+            build(with_reference=False)
+        lib = _Lib(ORACLE_SO, "orc_")
+        lib.lib.orc_create.restype = ctypes.c_void_p
+        lib.lib.orc_create.argtypes = [_dp, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, _dp, _dp]
+        lib.lib.orc_post_mu_terms.restype = ctypes.c_longlong
+        lib.lib.orc_post_mu_terms.argtypes = [ctypes.c_void_p]
+        _oracle_lib = lib
+    return _oracle_lib
+
+
+def _load_ref(threaded=False):
+    name = "libmce_ref_threaded.so" if threaded else "libmce_ref_serial.so"
+    if name not in _ref_libs:
+        path = os.path.join(REF_OUT, name)
+        if not os.path.exists(path):
+            raise FileNotFoundError(path + " (reference harness not built; needs the reference sources)")
+        lib = _Lib(path, "ref_")
+        lib.lib.ref_create.restype = ctypes.c_void_p
+        lib.lib.ref_create.argtypes = [_dp, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_uint]
+        lib.lib.ref_get_constants.argtypes = [ctypes.c_void_p, _dp, _dp, _ip]
+        lib.lib.ref_last_step_seconds.restype = ctypes.c_double
+        lib.lib.ref_last_step_seconds.argtypes = [ctypes.c_void_p]
+        _ref_libs[name] = lib
+    return _ref_libs[name]
+
+
+def _arr(x):
+    return np.ascontiguousarray(x, dtype=np.float64)
+
+
+class Oracle(_EstimatorBase):
+    def __init__(self, prob, root_point, b_pert):
+        lib = _load_oracle()
+        A0, p0, b0 = _arr(prob["A0"]), _arr(prob["p0"]), _arr(prob["b0"])
+        rp, bp = _arr(root_point), _arr(b_pert)
+        h = lib.lib.orc_create(_ptr(A0), _ptr(p0), _ptr(b0), prob["steps"], prob["d"], prob["cmcc"],
+                               prob["pncc"], prob["p"], _ptr(rp), _ptr(bp))
+        super().__init__(lib, h, prob)
+
+    def post_mu_terms(self):
+        return int(self._l.lib.orc_post_mu_terms(self.h))
+
+
+class Reference(_EstimatorBase):
+    def __init__(self, prob, seed=0, threaded=False):
+        lib = _load_ref(threaded)
+        A0, p0, b0 = _arr(prob["A0"]), _arr(prob["p0"]), _arr(prob["b0"])
+        h = lib.lib.ref_create(_ptr(A0), _ptr(p0), _ptr(b0), prob["steps"], prob["d"], prob["cmcc"],
+                               prob["pncc"], prob["p"], seed)
+        super().__init__(lib, h, prob)
+
+    def constants(self):
+        ms = max_shape_of(self.prob)
+        rp = np.zeros(self.d)
+        bp = np.zeros(ms)
+        n = ctypes.c_int(0)
+        self._l.lib.ref_get_constants(self.h, _ptr(rp), _ptr(bp), ctypes.byref(n))
+        return rp, bp
+
+    def last_step_seconds(self):
+        return float(self._l.lib.ref_last_step_seconds(self.h))
+
+
+def run(est, prob, record_terms_upto=0):
+    """Steps ``est`` through the whole problem; returns per-measurement records."""
+    recs = []
+    ms = max_shape_of(prob)
+    total = prob["steps"] * prob["p"]
+    n = 0
+    for k in range(prob["steps"]):
+        for s in range(prob["p"]):
+            err = est.step(k, s)
+            n += 1
+            rec = est.moments()
+            rec["err"] = int(err)
+            rec["Nt"] = est.num_terms()
+            rec["tps"] = est.terms_per_shape()
+            if n < total and rec["Nt"] <= record_terms_upto:
+                rec["terms"] = est.dump_terms(ms)
+            recs.append(rec)
+    return recs
+
+
+def run_oracle_batch(probs, constants, threads=None):
+    """Runs independent problems on a thread pool (each estimator serial).
+    Returns (total post-MU term count, wall seconds)."""
+    import time
+    threads = threads or (os.cpu_count() or 1)
+
+    def one(i):
+        est = Oracle(probs[i], *constants[i])
+        for k in range(probs[i]["steps"]):
+            for s in range(probs[i]["p"]):
+                est.step(k, s)
+        n = est.post_mu_terms()
+        est.close()
+        return n
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        counts = list(ex.map(one, range(len(probs))))
+    return int(sum(counts)), time.perf_counter() - t0

@@ -1,0 +1,1389 @@
+// ORACLE — test infrastructure only.
+//
+// A plain, serial CPU restatement of the reference's per-step term
+// propagation (natsnyder1/CauchyFriendly, CauchyEstimator::step,
+// include/cauchy_estimator.hpp:1211-1245), written from the reference's
+// algorithm, used only by tests/, __graft_entry__.smoke() and bench.py's
+// cpu_baseline / reference arm as the CHECKER.  The shipped product never
+// links or calls this file.
+//
+// Pinned against the compiled reference (oracle/ref_harness.cpp) through the
+// golden fixtures in tests/golden (tests/test_oracle_golden.py).
+//
+// Storage mode mirrored: binary-search g-tables with half storage (the
+// reference defaults, include/cauchy_types.hpp:22-35).  Term order mirrors the
+// serial path (NUM_CPUS == 1): parents in shape/index order, then children in
+// (parent, hyperplane) order (include/cauchy_estimator.hpp:741-780).
+//
+// Floating point: every sum is evaluated sequentially in the reference's
+// index order and complex numbers use the C99 complex type, so with
+// -ffp-contract=off the results are bit-identical to the reference build.
+#include <algorithm>
+#include <cmath>
+#include <complex.h>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <thread>
+#include <vector>
+#include <chrono>
+
+typedef double __complex__ cplx;
+
+static inline cplx mkc(double re, double im)
+{
+    cplx z;
+    __real__ z = re;
+    __imag__ z = im;
+    return z;
+}
+static inline cplx cconj(cplx z)
+{
+    __imag__ z = -__imag__ z;
+    return z;
+}
+
+// Constants: include/cauchy_constants.hpp:27-81
+static const double kTwoPiInv = 1.0 / (2.0 * M_PI);
+static const double kCoalignEps = 1e-8;   // COALIGN_TP_EPS / COALIGN_MU_EPS
+static const double kMuEps = 1e-10;       // MU_EPS
+static const double kTermApproxEps = 1e-15;
+static const double kPluEps = 1e-15;
+static const double kCondEps = 1e12;
+static const double kReductionEps = 1e-8;
+
+enum {
+    ERR_FZ_NEGATIVE = 9,
+    ERR_FZ_UNSTABLE = 8,
+    ERR_MEAN_DNE = 7,
+    ERR_MEAN_UNSTABLE_NOT_FINAL = 6,
+    ERR_MEAN_UNSTABLE_FINAL = 5,
+    ERR_MEAN_UNSTABLE_ANY = 4,
+    ERR_COV_DNE = 3,
+    ERR_COV_UNSTABLE_NOT_FINAL = 2,
+    ERR_COV_UNSTABLE_FINAL = 1,
+    ERR_COV_UNSTABLE_ANY = 0,
+};
+
+enum { ORC_OK = 0, ORC_ERR_BOTH_HORTHOG_NEG = 1, ORC_ERR_SHAPE = 2, ORC_ERR_DONE = 3 };
+
+// ----------------------------------------------------------------------------
+// Combinatorics: include/cell_enumeration.hpp:11-56, 71-119
+static long long binom(int n, int k)
+{
+    if (k < 0 || k > n) return 0;
+    long long r = 1;
+    if (k > n - k) k = n - k;
+    for (int i = 0; i < k; i++) {
+        r *= (n - i);
+        r /= (i + 1);
+    }
+    return r;
+}
+static int cells_central(int m, int d)
+{
+    if (m < d) return 1 << m;
+    long long s = 0;
+    for (int i = 0; i < d; i++) s += binom(m - 1, i);
+    return (int)(2 * s);
+}
+static int cells_general(int m, int d)
+{
+    if (m < d) return 1 << m;
+    long long s = 0;
+    for (int i = 0; i <= d; i++) s += binom(m, i);
+    return (int)s;
+}
+// d-subsets of {0..m-1} in lexicographic order (the order std::prev_permutation
+// on a leading-ones mask produces, cell_enumeration.hpp:71-92).
+static void lex_combos(int m, int d, std::vector<int>& out)
+{
+    out.clear();
+    if (d > m || d <= 0) return;
+    std::vector<int> c(d);
+    for (int i = 0; i < d; i++) c[i] = i;
+    while (true) {
+        out.insert(out.end(), c.begin(), c.end());
+        int i = d - 1;
+        while (i >= 0 && c[i] == m - d + i) i--;
+        if (i < 0) break;
+        c[i]++;
+        for (int j = i + 1; j < d; j++) c[j] = c[j - 1] + 1;
+    }
+}
+
+// ----------------------------------------------------------------------------
+// Small dense linear algebra with the reference's exact operation order.
+// PLU with partial pivoting: cauchy_linalg.hpp:1180-1231
+static int plu(double* A, int* P, int n, double tol)
+{
+    double tmp[32];
+    for (int j = 0; j < n; j++) {
+        double piv = tol;
+        int pi = -1;
+        for (int i = j; i < n; i++)
+            if (fabs(A[i * n + j]) > fabs(piv)) {
+                piv = A[i * n + j];
+                pi = i;
+            }
+        if (pi == -1) return 1;
+        if (pi != j) {
+            memcpy(tmp, A + j * n, n * sizeof(double));
+            memcpy(A + j * n, A + pi * n, n * sizeof(double));
+            memcpy(A + pi * n, tmp, n * sizeof(double));
+        }
+        P[j] = pi;
+        for (int k = j + 1; k < n; k++) {
+            A[k * n + j] /= A[j * n + j];
+            double t = A[k * n + j];
+            for (int q = j + 1; q < n; q++) A[k * n + q] -= t * A[j * n + q];
+        }
+    }
+    return 0;
+}
+// forward/back solves on a packed LU: cauchy_linalg.hpp:1234-1256
+static void lu_forward(const double* LU, double* b, int n)
+{
+    for (int i = 0; i < n; i++) {
+        double s = b[i];
+        for (int j = 0; j < i; j++) s -= LU[i * n + j] * b[j];
+        b[i] = s;
+    }
+}
+static void lu_back(const double* LU, double* b, int n)
+{
+    for (int i = n - 1; i >= 0; i--) {
+        double s = b[i];
+        for (int j = n - 1; j > i; j--) s -= LU[i * n + j] * b[j];
+        b[i] = s / LU[i * n + i];
+    }
+}
+// Inverse row permutation of the pivot list: cauchy_linalg.hpp:1258-1277
+static void pivots_to_inverse_perm(const int* P, int* PT, int n)
+{
+    int Preg[32];
+    for (int i = 0; i < n; i++) Preg[i] = i;
+    for (int i = 0; i < n; i++) {
+        int t = Preg[i];
+        Preg[i] = Preg[P[i]];
+        Preg[P[i]] = t;
+    }
+    for (int i = 0; i < n; i++) PT[Preg[i]] = i;
+}
+// 1-norm condition number through an explicit inverse: cauchy_linalg.hpp:1337-1390
+static double cond1(double* A, int* P, int n)
+{
+    double nrm = -1;
+    for (int c = 0; c < n; c++) {
+        double s = 0;
+        for (int r = 0; r < n; r++) s += fabs(A[r * n + c]);
+        if (s > nrm) nrm = s;
+    }
+    if (plu(A, P, n, kPluEps)) return 1.79769313486231570815e+308;
+    int PT[32];
+    pivots_to_inverse_perm(P, PT, n);
+    double W[32 * 32];
+    memset(W, 0, sizeof(double) * n * n);
+    for (int i = 0; i < n; i++) {
+        W[i * n + PT[i]] = 1;
+        lu_forward(A, W + i * n, n);
+        lu_back(A, W + i * n, n);
+    }
+    // The reference transposes W and takes column sums; that equals row sums of W.
+    double inrm = -1;
+    for (int i = 0; i < n; i++) {
+        double s = 0;
+        for (int j = 0; j < n; j++) s += fabs(W[i * n + j]);
+        if (s > inrm) inrm = s;
+    }
+    return nrm * inrm;
+}
+// solve_trf: cauchy_linalg.hpp:1280-1299
+static void solve_lu(const double* LU, const int* P, const double* b, double* x, int n)
+{
+    int PT[32];
+    pivots_to_inverse_perm(P, PT, n);
+    for (int i = 0; i < n; i++) x[PT[i]] = b[i];
+    lu_forward(LU, x, n);
+    lu_back(LU, x, n);
+}
+
+// Symmetric eigenvalues (Jacobi rotations) for the covariance check.  The
+// reference uses tred2/tqli (eig_solve.hpp:404); only the sign test against
+// -1e-5 consumes the result.
+static void sym_eigvals(const double* S, double* ev, int n)
+{
+    double a[64];
+    memcpy(a, S, sizeof(double) * n * n);
+    for (int sweep = 0; sweep < 100; sweep++) {
+        double off = 0;
+        for (int i = 0; i < n; i++)
+            for (int j = i + 1; j < n; j++) off += a[i * n + j] * a[i * n + j];
+        if (off < 1e-300) break;
+        for (int p = 0; p < n; p++)
+            for (int q = p + 1; q < n; q++) {
+                double apq = a[p * n + q];
+                if (apq == 0) continue;
+                double th = (a[q * n + q] - a[p * n + p]) / (2 * apq);
+                double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1));
+                double c = 1 / sqrt(t * t + 1), s = t * c;
+                for (int k = 0; k < n; k++) {
+                    double akp = a[k * n + p], akq = a[k * n + q];
+                    a[k * n + p] = c * akp - s * akq;
+                    a[k * n + q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < n; k++) {
+                    double apk = a[p * n + k], aqk = a[q * n + k];
+                    a[p * n + k] = c * apk - s * aqk;
+                    a[q * n + k] = s * apk + c * aqk;
+                }
+            }
+    }
+    for (int i = 0; i < n; i++) ev[i] = a[i * n + i];
+}
+
+// covariance_checker: cauchy_util.hpp:1882-2004
+static int covariance_flags(const cplx* cov, int d)
+{
+    int flags = 0;
+    double re[64], im[64], ev[8];
+    for (int i = 0; i < d * d; i++) {
+        re[i] = __real__ cov[i];
+        im[i] = __imag__ cov[i];
+    }
+    sym_eigvals(re, ev, d);
+    for (int i = 0; i < d; i++)
+        if (ev[i] < -1e-5) flags |= 1;
+    for (int i = 0; i < d - 1; i++) {
+        double sii = sqrt(re[i * d + i]);
+        for (int j = i + 1; j < d; j++) {
+            double sjj = sqrt(re[j * d + j]);
+            double c = re[i * d + j] / (sii * sjj);
+            if (fabs(c) > 1) flags |= 2;
+        }
+    }
+    for (int i = 0; i < d; i++)
+        for (int j = i; j < d; j++) {
+            double r = fabs(im[i * d + j]) / (fabs(re[i * d + j]) + 1e-15);
+            if (r > 10) flags |= 4;
+        }
+    for (int i = 0; i < d * d; i++)
+        if (fabs(im[i]) > 2000) flags |= 8;
+    return flags;
+}
+
+// ----------------------------------------------------------------------------
+// g-table: sorted keys with complex values (half storage).
+struct GTable {
+    std::vector<int> keys;
+    std::vector<cplx> vals;
+    int find(int key) const
+    {
+        // binsearch: gtable.hpp:283-301
+        int lo = 0, hi = (int)keys.size() - 1;
+        while (lo <= hi) {
+            int mid = (lo + hi) / 2;
+            int mk = keys[mid];
+            if (mk == key) return mid;
+            if ((unsigned)mk > (unsigned)key) hi = mid - 1;
+            else lo = mid + 1;
+        }
+        return -1;
+    }
+};
+
+// g numerator lookup in the parent table with half storage: eval_gs.hpp:94-153
+static inline cplx lookup_num(const GTable* gp, int enc, int phc)
+{
+    const int top = 1 << (phc - 1);
+    const int rev = (1 << phc) - 1;
+    if (enc & top) {
+        int idx = gp->find(rev ^ enc);
+        if (idx < 0) return mkc(0, 0);
+        return cconj(gp->vals[idx]);
+    }
+    int idx = gp->find(enc);
+    if (idx < 0) return mkc(0, 0);
+    return gp->vals[idx];
+}
+
+struct Term {
+    int m = 0;
+    std::vector<double> A, p, q, b;
+    double c_val = 0, d_val = 0;
+    unsigned horthog = 0;
+    int phc = 0, pbc = 0, z = 0, enc_lhp = 0;
+    bool is_new_child = false;
+    bool has_cmap = false;
+    std::vector<int> cmap, csmap;
+    std::shared_ptr<GTable> gp;             // parent table (keys in phc-bit space)
+    std::shared_ptr<std::vector<int>> encB;  // own B (parents) or shared B_mu (new children)
+    std::vector<int> own_B;                  // B built for this term in make_gtables
+    GTable g;                                // table built at this step
+};
+
+struct Estimator {
+    int d, cmcc, pncc, p, num_steps, shape_range;
+    int master_step = 0;
+    std::vector<double> A0, p0, b0, root, bpert;
+    std::vector<Term> terms;  // ordered by shape then index
+    int Nt = 1;
+    std::vector<int> terms_per_shape;
+    cplx fz, last_fz;
+    std::vector<cplx> mean, cov, last_mean, last_cov;
+    cplx raw_fz;
+    std::vector<cplx> raw_mean, raw_cov;
+    double gscale = 0;
+    int errors = 0;
+    bool skip_post_mu = false;
+    std::vector<std::vector<int>> combos;  // per shape
+    long long post_mu_terms = 0;           // sum over steps of terms after MU
+};
+
+// ----------------------------------------------------------------------------
+// Term operations (include/cauchy_term.hpp)
+
+// time_prop: cauchy_term.hpp:435-456
+static void time_prop(Term& t, int d, const double* Phi, const double* B, const double* u, int cmcc)
+{
+    std::vector<double> w(t.A.begin(), t.A.begin() + t.m * d);
+    for (int i = 0; i < t.m; i++)
+        for (int j = 0; j < d; j++) {
+            double s = 0.0;
+            for (int k = 0; k < d; k++) s += w[i * d + k] * Phi[k + j * d];
+            t.A[i * d + j] = s;
+        }
+    double wb[16];
+    memcpy(wb, t.b.data(), d * sizeof(double));
+    for (int i = 0; i < d; i++) {
+        double s = 0.0;
+        for (int j = 0; j < d; j++) s += Phi[i * d + j] * wb[j];
+        t.b[i] = s;
+    }
+    if (cmcc > 0) {
+        for (int i = 0; i < d; i++) {
+            double s = 0.0;
+            for (int j = 0; j < cmcc; j++) s += B[i * cmcc + j] * u[j];
+            wb[i] = s;
+        }
+        for (int i = 0; i < d; i++) t.b[i] += 1.0 * wb[i];
+    }
+}
+
+// normalize_hps: cauchy_term.hpp:458-472
+static void normalize_rows(Term& t, int d, bool set_q)
+{
+    if (set_q) t.q.assign(t.p.begin(), t.p.begin() + t.m);
+    for (int i = 0; i < t.m; i++) {
+        double n1 = 0;
+        for (int j = 0; j < d; j++) n1 += fabs(t.A[i * d + j]);
+        t.p[i] *= n1;
+        for (int j = 0; j < d; j++) t.A[i * d + j] /= n1;
+    }
+}
+
+// row-vs-row coalignment gate used by TP and MU coalignment
+// (cauchy_term.hpp:494-504, 565-576): returns +1 (same), -1 (opposite), 0.
+static inline int coalign_gate(const double* r, const double* c, int d)
+{
+    bool pos = true, neg = true;
+    for (int l = 0; l < d; l++) {
+        if (pos) pos &= fabs(r[l] - c[l]) < kCoalignEps;
+        if (neg) neg &= fabs(r[l] + c[l]) < kCoalignEps;
+        if (!(pos || neg)) break;
+    }
+    if (pos) return 1;
+    if (neg) return -1;
+    return 0;
+}
+
+// tp_coalign: cauchy_term.hpp:475-531
+static void tp_coalign(Term& t, int d, const double* Gt, const double* bt, int cnt)
+{
+    normalize_rows(t, d, false);
+    bool F[32];
+    for (int j = 0; j < cnt; j++) F[j] = true;
+    for (int j = 0; j < cnt; j++)
+        for (int k = 0; k < t.m; k++)
+            if (F[j] && coalign_gate(Gt + j * d, t.A.data() + k * d, d) != 0) {
+                F[j] = false;
+                t.p[k] += bt[j];
+            }
+    for (int j = 0; j < cnt; j++)
+        if (F[j]) {
+            t.A.resize((t.m + 1) * d);
+            t.p.resize(t.m + 1);
+            memcpy(t.A.data() + t.m * d, Gt + j * d, d * sizeof(double));
+            t.p[t.m] = bt[j];
+            t.m++;
+        }
+}
+
+// precoalign_Gamma_beta: cauchy_util.hpp:128-210
+static int precoalign_gamma(const double* Gamma, const double* beta, int pncc, int d, double* Gt, double* bt)
+{
+    for (int i = 0; i < pncc; i++) {
+        for (int j = 0; j < d; j++) Gt[i * d + j] = Gamma[j * pncc + i];
+        bt[i] = beta[i];
+    }
+    for (int i = 0; i < pncc; i++) {
+        double nf = 0;
+        for (int j = 0; j < d; j++) nf += fabs(Gt[i * d + j]);
+        for (int j = 0; j < d; j++) Gt[i * d + j] /= nf;
+        bt[i] *= nf;
+    }
+    bool F[32];
+    for (int i = 0; i < pncc; i++) F[i] = true;
+    for (int i = 0; i < pncc - 1; i++)
+        if (F[i])
+            for (int j = i + 1; j < pncc; j++)
+                if (F[j] && coalign_gate(Gt + i * d, Gt + j * d, d) != 0) {
+                    F[j] = false;
+                    bt[i] += bt[j];
+                }
+    int cnt = 0;
+    for (int i = 0; i < pncc; i++) cnt += F[i];
+    if (cnt != pncc) {
+        int u = 1;
+        for (int j = 1; j < pncc; j++)
+            if (F[j]) {
+                if (u < j) {
+                    memcpy(Gt + u * d, Gt + j * d, d * sizeof(double));
+                    bt[u] = bt[j];
+                }
+                u++;
+            }
+    }
+    return cnt;
+}
+
+// make_time_prop_btable: cell_enumeration.hpp:676-855 (the FAST_TP_DCE=false path)
+static void tp_enumerate(Estimator& E, Term& t)
+{
+    const int m = t.m, d = E.d;
+    std::vector<int> out;
+    if (m < d) {
+        for (int i = 0; i < (1 << (m - 1)); i++) out.push_back(i);
+        t.encB = std::make_shared<std::vector<int>>(out);
+        return;
+    }
+    const int phc = t.phc;
+    const int gmask = (1 << phc) - 1, ptop = 1 << (phc - 1);
+    const int mtop = 1 << (m - 1), mrev = (1 << m) - 1;
+    const int cells_gen = cells_general(m, d);
+    std::vector<char> seen((size_t)1 << m, 0);
+    std::vector<int> found;
+    std::vector<char> in_set((size_t)1 << m, 0);
+    const std::vector<int>& cmb = E.combos[m];
+    const int ncomb = m > d ? (int)(cmb.size() / d) : 0;  // the reference has no combos for m == d
+    double Ac[64], bc[8], v[8];
+    int P[8];
+    for (int i = 0; i < ncomb; i++) {
+        const int* c = &cmb[i * d];
+        for (int j = 0; j < d; j++) {
+            memcpy(Ac + j * d, t.A.data() + c[j] * d, d * sizeof(double));
+            bc[j] = E.bpert[c[j]];
+        }
+        if (cond1(Ac, P, d) > kCondEps) continue;
+        solve_lu(Ac, P, bc, v, d);
+        int niv = 0;
+        for (int a = 0; a < m; a++) {
+            bool inc = false;
+            for (int j = 0; j < d; j++)
+                if (c[j] == a) inc = true;
+            if (inc) continue;
+            double s = 0.0;
+            for (int j = 0; j < d; j++) s += t.A[a * d + j] * v[j];
+            if (s - E.bpert[a] < 0) niv |= 1 << a;
+        }
+        for (int j = 0; j < (1 << d); j++) {
+            int sv = niv;
+            for (int k = 0; k < d; k++)
+                if ((j >> k) & 1) sv |= 1 << c[k];
+            if (seen[sv]) continue;
+            seen[sv] = 1;
+            int psv = sv & gmask;
+            if (psv & ptop) psv ^= gmask;
+            if (t.gp->find(psv) >= 0) {
+                found.push_back(sv);
+                in_set[sv] = 1;
+            }
+        }
+        if ((int)found.size() == cells_gen) break;
+    }
+    std::vector<char> used(found.size(), 0);
+    for (size_t i = 0; i < found.size(); i++) {
+        if (used[i]) continue;
+        int b = found[i], br = b ^ mrev;
+        if (in_set[br]) {
+            used[i] = 1;
+            // mark the partner as consumed
+            for (size_t k = i + 1; k < found.size(); k++)
+                if (found[k] == br) {
+                    used[k] = 1;
+                    break;
+                }
+            out.push_back((b & mtop) ? br : b);
+        }
+    }
+    t.encB = std::make_shared<std::vector<int>>(out);
+}
+
+// msmt_update: cauchy_term.hpp:84-310.  `t` is the parent; integrable children
+// are appended to `kids`.  Returns the number of children.
+static int msmt_update(Term& t, int d, std::vector<Term>& kids, double msmt, const double* H, double gamma,
+                       bool first, bool last)
+{
+    const int m = t.m;
+    std::vector<double> mu((m + 1) * d), rho(m + 1);
+    std::vector<int> sgn(m);
+    std::vector<char> Fi(m + 1);
+    memcpy(mu.data(), t.A.data(), m * d * sizeof(double));
+    memcpy(rho.data(), t.p.data(), m * sizeof(double));
+    rho[m] = gamma;
+    for (int j = 0; j < d; j++) mu[m * d + j] = 0;
+    Fi[m] = 1;
+    for (int l = 0; l < m; l++) {
+        double h = 0.0;
+        for (int j = 0; j < d; j++) h += H[j] * mu[l * d + j];
+        double ah = fabs(h);
+        if (ah < kMuEps) {
+            rho[l] = t.p[l];
+            sgn[l] = 1;
+            Fi[l] = 0;
+        } else {
+            double r = 1.0 / h;
+            for (int j = 0; j < d; j++) mu[l * d + j] *= r;
+            rho[l] = t.p[l] * ah;
+            sgn[l] = h > 0 ? 1 : -1;
+            Fi[l] = 1;
+        }
+    }
+    double hb = 0.0;
+    for (int j = 0; j < d; j++) hb += H[j] * t.b[j];
+    const double zeta = msmt - hb;
+    const size_t kid0 = kids.size();
+    std::vector<double> b_old(t.b);
+    for (int tt = 0; tt <= m; tt++) {
+        if (!Fi[tt]) continue;
+        Term* c;
+        Term tmp;
+        if (tt == m) c = &t;
+        else c = &tmp;
+        if (!first) {
+            c->gp = t.gp;
+            c->phc = t.phc;
+            c->pbc = m;
+            c->z = tt;
+        }
+        c->c_val = zeta;
+        c->d_val = rho[tt];
+        c->m = m;
+        std::vector<double> nb(d), nA(m * d), np(m);
+        for (int j = 0; j < d; j++) nb[j] = b_old[j] + zeta * mu[tt * d + j];
+        int l = 0;
+        unsigned hof = 0;
+        for (int ll = 0; ll <= m; ll++) {
+            if (ll == tt) continue;
+            np[l] = rho[ll];
+            if (Fi[ll])
+                for (int j = 0; j < d; j++) nA[l * d + j] = mu[ll * d + j] - mu[tt * d + j];
+            else {
+                for (int j = 0; j < d; j++) nA[l * d + j] = mu[ll * d + j];
+                hof |= 1u << l;
+            }
+            l++;
+        }
+        c->A = nA;
+        c->p = np;
+        c->b = nb;
+        c->horthog = hof;
+        if (tt != m) kids.push_back(std::move(tmp));
+    }
+    t.is_new_child = false;
+    if (!first) {
+        int esg = 0;
+        for (int l = 0; l < m; l++)
+            if (sgn[l] == -1) esg |= 1 << l;
+        int lhp = esg;
+        if (t.phc < m) lhp &= (1 << t.phc) - 1;
+        t.enc_lhp = lhp;
+        if (esg & (1 << (m - 1))) esg ^= (1 << m) - 1;
+        for (size_t i = kid0; i < kids.size(); i++) {
+            kids[i].enc_lhp = lhp;
+            kids[i].is_new_child = true;
+            kids[i].encB = t.encB;  // shared: sees the parent's XOR below (B_mu)
+        }
+        if (!last)
+            for (auto& k : *t.encB) k ^= esg;
+    }
+    return (int)(kids.size() - kid0);
+}
+
+// eval_g_yei: cauchy_term.hpp:312-401
+static cplx eval_g_yei(const Term& t, int d, const double* root, cplx* yei, bool first)
+{
+    const int m = t.m;
+    double sA[32], ty[16];
+    for (int j = 0; j < d; j++) ty[j] = 0;
+    double ygi = 0;
+    for (int l = 0; l < m; l++) {
+        double s = 0.0;
+        for (int j = 0; j < d; j++) s += t.A[l * d + j] * root[j];
+        sA[l] = s > 0 ? 1 : -1;
+        double sc = t.p[l] * sA[l];
+        for (int j = 0; j < d; j++) ty[j] += sc * t.A[l * d + j];
+    }
+    if (t.horthog) {
+        for (int l = 0; l < m; l++)
+            if (!(t.horthog & (1u << l))) ygi += t.p[l] * sA[l];
+    } else {
+        double z = 0.0;
+        for (int l = 0; l < m; l++) z += t.p[l] * sA[l];
+        ygi = z;
+    }
+    cplx gp, gm;
+    if (first) {
+        gp = mkc(1, 0);
+        gm = mkc(1, 0);
+    } else {
+        int lp = 0, lm = 0, k = 0;
+        for (int l = 0; l < m; l++) {
+            if (k < t.phc) {
+                if (k == t.z) {
+                    lm |= 1 << k;
+                    k++;
+                    if (k == t.phc) continue;
+                }
+                if (sA[l] < 0) {
+                    lp |= 1 << k;
+                    lm |= 1 << k;
+                }
+                k++;
+            }
+        }
+        gp = lookup_num(t.gp.get(), lp ^ t.enc_lhp, t.phc);
+        gm = lookup_num(t.gp.get(), lm ^ t.enc_lhp, t.phc);
+    }
+    cplx g = gp / mkc(ygi + t.d_val, t.c_val) - gm / mkc(ygi - t.d_val, t.c_val);
+    g *= kTwoPiInv;
+    for (int j = 0; j < d; j++) yei[j] = mkc(-ty[j], t.b[j]);
+    return g;
+}
+
+// mu_coalign: cauchy_term.hpp:533-745.  Returns the new shape or -1 on the
+// reference's fatal condition (two H-orthogonal rows anti-coaligned).
+static int mu_coalign(Term& t, int d)
+{
+    normalize_rows(t, d, true);
+    const int m = t.m;
+    std::vector<char> F(m, 1);
+    std::vector<char> hflag(m, 0);
+    t.cmap.assign(m, 255);
+    t.csmap.assign(m, 1);
+    if (t.horthog)
+        for (int j = 0; j < m; j++) hflag[j] = (t.horthog >> j) & 1;
+    int uc = 0;
+    for (int j = 0; j < m - 1; j++) {
+        if (!F[j]) continue;
+        t.cmap[j] = uc;
+        for (int k = j + 1; k < m; k++) {
+            if (!F[k]) continue;
+            int g = coalign_gate(t.A.data() + j * d, t.A.data() + k * d, d);
+            if (g == 1) {
+                if (t.horthog) {
+                    bool hj = hflag[j], hk = hflag[k];
+                    if (!hj && !hk) t.q[j] += t.q[k];
+                    else if (hj && !hk) {
+                        t.q[j] = t.q[k];
+                        hflag[j] = 0;
+                    } else if (!hj && hk) hflag[k] = 0;
+                    else {
+                        hflag[k] = 0;
+                        t.q[j] += t.q[k];
+                    }
+                } else
+                    t.q[j] += t.q[k];
+                F[k] = 0;
+                t.p[j] += t.p[k];
+                t.cmap[k] = uc;
+                t.csmap[k] = 1;
+            } else if (g == -1) {
+                if (t.horthog) {
+                    bool hj = hflag[j], hk = hflag[k];
+                    if (!hj && !hk) t.q[j] -= t.q[k];
+                    else if (hj && !hk) {
+                        t.q[j] = -t.q[k];
+                        hflag[j] = 0;
+                    } else if (!hj && hk) hflag[k] = 0;
+                    else return -1;
+                } else
+                    t.q[j] -= t.q[k];
+                F[k] = 0;
+                t.p[j] += t.p[k];
+                t.cmap[k] = uc;
+                t.csmap[k] = -1;
+            }
+        }
+        uc++;
+    }
+    if (F[m - 1]) t.cmap[m - 1] = uc;
+    int ns = 0;
+    for (int i = 0; i < m; i++) ns += F[i];
+    if (ns != m) {
+        int u = 1;
+        for (int j = 1; j < m; j++)
+            if (F[j]) {
+                if (u < j) {
+                    memcpy(t.A.data() + u * d, t.A.data() + j * d, d * sizeof(double));
+                    t.p[u] = t.p[j];
+                    t.q[u] = t.q[j];
+                }
+                u++;
+            }
+        if (t.horthog) {
+            unsigned nh = 0;
+            int c = 0;
+            for (int j = 0; j < m; j++)
+                if (F[j]) nh |= (unsigned)hflag[j] << c++;
+            t.horthog = nh;
+        }
+        t.m = ns;
+        t.A.resize(ns * d);
+        t.p.resize(ns);
+        t.q.resize(ns);
+    }
+    return t.m;
+}
+
+// make_new_child_btable: cell_enumeration.hpp:206-371 (the MU-side DCE)
+static void new_child_btable(Term& t, int d)
+{
+    const int m = t.m;
+    std::vector<int> out;
+    if (m <= d) {
+        for (int i = 0; i < (1 << (m - 1)); i++) out.push_back(i);
+        t.own_B = out;
+        return;
+    }
+    const std::vector<int>& Bmu = *t.encB;
+    const int pbc = t.pbc, z = t.z;
+    const int mz = 1 << z, hb = 1 << (pbc - 1), rev = (1 << pbc) - 1, low = mz - 1;
+    std::vector<int> pos((size_t)1 << pbc, -1);
+    for (size_t j = 0; j < Bmu.size(); j++) pos[Bmu[j]] = (int)j;
+    std::vector<char> F(Bmu.size(), 1);
+    std::vector<int> buc;
+    for (size_t j = 0; j < Bmu.size(); j++) {
+        if (!F[j]) continue;
+        int b = Bmu[j];
+        int bq = b ^ mz;
+        if (bq & hb) bq ^= rev;
+        int k = pos[bq];
+        if (k < 0) continue;
+        F[j] = 0;
+        F[k] = 0;
+        int zb = (b & mz) >> z;
+        int c1 = ((b >> (z + 1)) << z) | (b & low) | (zb << (pbc - 1));
+        int c2 = c1 ^ hb;
+        buc.push_back((c1 & hb) ? (c1 ^ rev) : c1);
+        buc.push_back((c2 & hb) ? (c2 ^ rev) : c2);
+    }
+    if (m < pbc) {
+        // projection through the coalignment map, first occurrence kept
+        std::vector<int> bitmask;
+        std::vector<char> Fc(pbc, 1);
+        for (int j = 0; j < pbc; j++) {
+            int ci = t.cmap[j];
+            if (Fc[ci]) {
+                Fc[ci] = 0;
+                bitmask.push_back(1 << j);
+            }
+        }
+        std::vector<char> seen((size_t)1 << bitmask.size(), 0);
+        for (int b : buc) {
+            int bc = 0;
+            for (size_t l = 0; l < bitmask.size(); l++)
+                if (b & bitmask[l]) bc |= 1 << l;
+            if (!seen[bc]) {
+                seen[bc] = 1;
+                out.push_back(bc);
+            }
+        }
+    } else
+        out = buc;
+    t.own_B = out;
+}
+
+// Orientation mask between two equal arrangements (first component that is
+// significant in both rows decides): cell_enumeration.hpp:630-640 and
+// flattening.hpp:279-288.
+static int orientation_mask(const double* Ai, const double* Aj, int m, int d)
+{
+    int s = 0;
+    for (int k = 0; k < m; k++) {
+        int l = 0;
+        while (l < d - 1 && ((fabs(Ai[k * d + l]) < kReductionEps) || (fabs(Aj[k * d + l]) < kReductionEps))) l++;
+        if (Ai[k * d + l] * Aj[k * d + l] < 0) s |= 1 << k;
+    }
+    return s;
+}
+// update_btable: cell_enumeration.hpp:584-625
+static std::vector<int> reorient(const double* Ai, const std::vector<int>& Bi, const double* Aj, int n, int m, int d)
+{
+    int s = orientation_mask(Ai, Aj, m, d);
+    if (s & (1 << (m - 1))) s ^= (1 << m) - 1;
+    std::vector<int> out(Bi.begin(), Bi.begin() + n);
+    if (s)
+        for (auto& k : out) k ^= s;
+    return out;
+}
+
+// make_gtable: flattening.hpp:77-255.  Returns true when the term is negligible.
+static bool make_gtable(Term& t, const std::vector<int>& B, double gscale)
+{
+    const int m = t.m, phc = t.phc;
+    double ps = 0;
+    for (int i = 0; i < m; i++) ps += t.p[i];
+    ps *= ps;
+    bool negl = true;
+    std::vector<std::pair<int, cplx>> kv;
+    kv.reserve(B.size());
+    int sb[32];
+    for (int be : B) {
+        double ygi = 0;
+        if (t.horthog) {
+            for (int k = 0; k < m; k++) {
+                sb[k] = ((be >> k) & 1) ? -1 : 1;
+                if (!(t.horthog & (1u << k))) ygi += t.q[k] * sb[k];
+            }
+        } else
+            for (int k = 0; k < m; k++) {
+                sb[k] = ((be >> k) & 1) ? -1 : 1;
+                ygi += t.q[k] * sb[k];
+            }
+        int lp = 0, lm = 0;
+        if (!t.is_new_child) {
+            lp = be & ((1 << phc) - 1);
+            lm = lp;
+        } else {
+            int k = 0, l = 0;
+            while (k < phc) {
+                if (k == t.z) {
+                    lm |= 1 << k;
+                    k++;
+                    if (k == phc) break;
+                }
+                int bv = t.has_cmap ? sb[t.cmap[l]] * t.csmap[l] : sb[l];
+                if (bv < 0) {
+                    lp |= 1 << k;
+                    lm |= 1 << k;
+                }
+                k++;
+                l++;
+            }
+        }
+        cplx gp = lookup_num(t.gp.get(), lp ^ t.enc_lhp, phc);
+        cplx gm = lookup_num(t.gp.get(), lm ^ t.enc_lhp, phc);
+        cplx v = gp / mkc(ygi + t.d_val, t.c_val) - gm / mkc(ygi - t.d_val, t.c_val);
+        v *= gscale;
+        kv.push_back({be, v});
+        if (negl && ps * cabs(v) > kTermApproxEps) negl = false;
+    }
+    std::stable_sort(kv.begin(), kv.end(), [](const std::pair<int, cplx>& a, const std::pair<int, cplx>& b) {
+        return a.first < b.first;
+    });
+    t.g.keys.resize(kv.size());
+    t.g.vals.resize(kv.size());
+    for (size_t i = 0; i < kv.size(); i++) {
+        t.g.keys[i] = kv[i].first;
+        t.g.vals[i] = kv[i].second;
+    }
+    return negl;
+}
+
+// add_gtables: flattening.hpp:259-315
+static void add_gtables(Term& ti, const std::vector<int>& Bi, const Term& tj, int d)
+{
+    const int m = ti.m;
+    int s = orientation_mask(ti.A.data(), tj.A.data(), m, d);
+    const int top = 1 << (m - 1), rev = (1 << m) - 1;
+    for (int bi : Bi) {
+        int bj = bi ^ s;
+        bool cj = false;
+        if (bj & top) {
+            cj = true;
+            bj ^= rev;
+        }
+        int ii = ti.g.find(bi), jj = tj.g.find(bj);
+        if (ii >= 0 && jj >= 0) ti.g.vals[ii] += cj ? cconj(tj.g.vals[jj]) : tj.g.vals[jj];
+    }
+}
+
+static void become_parent(Term& t)
+{
+    t.phc = t.m;
+    t.gp = std::make_shared<GTable>(std::move(t.g));
+    t.g = GTable();
+    t.is_new_child = false;
+    t.has_cmap = false;
+    t.encB.reset();
+    t.own_B.clear();
+}
+
+// ----------------------------------------------------------------------------
+// Fast term reduction: term_reduction.hpp:159-276 (serial path).  The window
+// test on every axis is the value test qp-eps < v <= qp+eps that the
+// reference's sorted-axis binary searches implement.  The hyperplane check
+// compares the first m entries of the row-major A arrays, as the reference
+// does (it indexes Ai[k] / Aj[k] inside the per-component loop).
+static void ftr(const std::vector<Term*>& T, int d, std::vector<int>& F)
+{
+    const int n = (int)T.size();
+    F.resize(n);
+    for (int i = 0; i < n; i++) F[i] = i;
+    if (n == 0) return;
+    const int m = T[0]->m;
+    const double ep = kReductionEps;
+    // index sorted along axis 0 for the candidate window
+    std::vector<int> ord(n);
+    for (int i = 0; i < n; i++) ord[i] = i;
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return T[a]->b[0] < T[b]->b[0]; });
+    std::vector<double> v0(n);
+    for (int i = 0; i < n; i++) v0[i] = T[ord[i]]->b[0];
+    for (int i = 0; i < n; i++) {
+        if (F[i] != i) continue;
+        const double* bi = T[i]->b.data();
+        double lo = bi[0] - ep, hi = bi[0] + ep;
+        int s = (int)(std::upper_bound(v0.begin(), v0.end(), lo) - v0.begin());
+        int e = (int)(std::upper_bound(v0.begin(), v0.end(), hi) - v0.begin());
+        for (int w = s; w < e; w++) {
+            int j = ord[w];
+            if (j <= i || F[j] != j) continue;
+            const double* bj = T[j]->b.data();
+            bool ok = true;
+            for (int a = 1; a < d && ok; a++) {
+                double l2 = bi[a] - ep, h2 = bi[a] + ep;
+                if (!(bj[a] > l2 && bj[a] <= h2)) ok = false;
+            }
+            if (!ok) continue;
+            for (int k = 0; k < m && ok; k++)
+                if (fabs(T[j]->p[k] - T[i]->p[k]) > ep) ok = false;
+            if (!ok) continue;
+            for (int k = 0; k < m && ok; k++) {
+                double r = T[i]->A[k], c = T[j]->A[k];
+                if (!(fabs(r - c) < ep || fabs(r + c) < ep)) ok = false;
+            }
+            if (ok) F[j] = i;
+        }
+    }
+}
+
+// make_gtables for one shape: flattening.hpp:318-568.
+static void make_gtables_shape(std::vector<Term*>& T, const std::vector<int>& F, int d, double gscale,
+                               std::vector<Term*>& out)
+{
+    const int n = (int)T.size();
+    std::vector<std::vector<int>> members(n);
+    for (int j = 0; j < n; j++)
+        if (F[j] != j) members[F[j]].push_back(j);
+    for (int j = 0; j < n; j++) {
+        if (F[j] != j) continue;
+        Term* root = T[j];
+        bool have_root = true;
+        std::vector<int> rootB;
+        if (root->is_new_child) {
+            new_child_btable(*root, d);
+            rootB = root->own_B;
+        } else
+            rootB = *root->encB;
+        if (make_gtable(*root, rootB, gscale)) have_root = false;
+        size_t k = 0;
+        const std::vector<int>& mem = members[j];
+        if (!have_root) {
+            // the root approximated out: the next member that survives becomes root
+            std::vector<int> grpB = rootB;
+            const double* Alfr = root->A.data();
+            while (k < mem.size()) {
+                Term* c = T[mem[k++]];
+                std::vector<int> cB;
+                if (c->is_new_child) {
+                    grpB = reorient(Alfr, grpB, c->A.data(), (int)grpB.size(), c->m, d);
+                    cB = grpB;
+                } else {
+                    // a parent keeps its own B; the group's cell list becomes its list
+                    grpB = *c->encB;
+                    cB = grpB;
+                }
+                if (!make_gtable(*c, cB, gscale)) {
+                    root = c;
+                    rootB = cB;
+                    have_root = true;
+                    break;
+                } else
+                    Alfr = c->A.data();
+            }
+        }
+        while (k < mem.size()) {
+            Term* c = T[mem[k++]];
+            std::vector<int> cB;
+            if (c->is_new_child)
+                cB = reorient(root->A.data(), rootB, c->A.data(), (int)rootB.size(), c->m, d);
+            else {
+                if (c->encB->size() != rootB.size())
+                    cB = reorient(root->A.data(), rootB, c->A.data(), (int)rootB.size(), c->m, d);
+                else
+                    cB = *c->encB;
+            }
+            if (!make_gtable(*c, cB, gscale)) add_gtables(*root, rootB, *c, d);
+        }
+        if (have_root) {
+            become_parent(*root);
+            out.push_back(root);
+        }
+    }
+}
+
+// ----------------------------------------------------------------------------
+// Estimator (include/cauchy_estimator.hpp)
+
+static void numeric_check(Estimator& E)
+{
+    // moments_numerical_check: cauchy_estimator.hpp:359-461
+    const int d = E.d;
+    const int ph = E.master_step % E.p;
+    const bool first = ph == 0, not_last = ph != E.p - 1, last = ph == E.p - 1;
+    if (first) {
+        E.errors |= (1 << ERR_MEAN_DNE) | (1 << ERR_COV_DNE);
+        E.errors &= ~((1 << ERR_MEAN_UNSTABLE_FINAL) | (1 << ERR_MEAN_UNSTABLE_NOT_FINAL) |
+                      (1 << ERR_COV_UNSTABLE_NOT_FINAL) | (1 << ERR_COV_UNSTABLE_FINAL));
+    }
+    int ne = 0;
+    if (__real__ E.fz <= 0) ne |= 1 << ERR_FZ_NEGATIVE;
+    if (fabs(__imag__ E.fz / (1e-15 + __real__ E.fz)) > 1e-3) ne |= 1 << ERR_FZ_UNSTABLE;
+    bool mean_ok = true;
+    for (int i = 0; i < d; i++) {
+        double re = fabs(__real__ E.mean[i]), im = fabs(__imag__ E.mean[i]);
+        double r = im / (1e-15 + re);
+        if (r > 1e-1 || im > 0.001) {
+            ne |= 1 << ERR_MEAN_UNSTABLE_ANY;
+            if (not_last) ne |= 1 << ERR_MEAN_UNSTABLE_NOT_FINAL;
+            if (last) ne |= 1 << ERR_MEAN_UNSTABLE_FINAL;
+            mean_ok = false;
+        }
+    }
+    bool cov_ok = true;
+    if (covariance_flags(E.cov.data(), d)) {
+        ne |= 1 << ERR_COV_UNSTABLE_ANY;
+        if (not_last) ne |= 1 << ERR_COV_UNSTABLE_NOT_FINAL;
+        if (last) ne |= 1 << ERR_COV_UNSTABLE_FINAL;
+        cov_ok = false;
+    }
+    E.errors |= ne;
+    if (mean_ok) E.errors &= ~(1 << ERR_MEAN_DNE);
+    if (cov_ok) E.errors &= ~(1 << ERR_COV_DNE);
+    if (mean_ok) E.last_mean = E.mean;
+    else E.mean = E.last_mean;
+    if (cov_ok) E.last_cov = E.cov;
+    else E.cov = E.last_cov;
+    if (!mean_ok && !cov_ok) E.fz = E.last_fz;
+    else E.last_fz = E.fz;
+}
+
+static void accumulate(Estimator& E, cplx g, const cplx* y)
+{
+    // cache_moments: cauchy_estimator.hpp:307-338
+    const int d = E.d;
+    E.fz += g;
+    for (int j = 0; j < d; j++) {
+        cplx yy = y[j];
+        E.mean[j] += g * yy;
+        for (int k = 0; k < d; k++) E.cov[j * d + k] -= g * yy * y[k];
+    }
+}
+
+static void finalize_moments(Estimator& E)
+{
+    // finalize_cached_moments: cauchy_estimator.hpp:340-357
+    const int d = E.d;
+    E.gscale = kTwoPiInv / __real__ E.fz;
+    cplx ifz = mkc(0, __real__ E.fz);
+    for (int i = 0; i < d; i++) E.mean[i] /= ifz;
+    for (int i = 0; i < d; i++)
+        for (int j = 0; j < d; j++) E.cov[i * d + j] = (E.cov[i * d + j] / E.fz) - E.mean[i] * E.mean[j];
+    E.raw_fz = E.fz;
+    E.raw_mean = E.mean;
+    E.raw_cov = E.cov;
+    numeric_check(E);
+}
+
+static void reset_terms(Estimator& E)
+{
+    E.terms.clear();
+    Term t;
+    t.m = E.d;
+    t.A = E.A0;
+    t.p = E.p0;
+    t.b = E.b0;
+    E.terms.push_back(t);
+    E.Nt = 1;
+    E.terms_per_shape.assign(E.shape_range, 0);
+    E.terms_per_shape[E.d] = 1;
+    E.master_step = 0;
+    E.errors = 0;
+}
+
+// step_first: cauchy_estimator.hpp:1179-1208 with make_gtable_first flattening.hpp:14-67
+static void step_first(Estimator& E, double msmt, const double* H, double gamma)
+{
+    const int d = E.d;
+    std::vector<Term> kids;
+    Term parent = E.terms[0];
+    msmt_update(parent, d, kids, msmt, H, gamma, true, false);
+    std::vector<Term> all;
+    all.push_back(parent);
+    for (auto& k : kids) all.push_back(std::move(k));
+    E.fz = mkc(0, 0);
+    E.mean.assign(d, mkc(0, 0));
+    E.cov.assign(d * d, mkc(0, 0));
+    cplx y[16];
+    for (auto& t : all) {
+        cplx g = eval_g_yei(t, d, E.root.data(), y, true);
+        accumulate(E, g, y);
+    }
+    E.gscale = kTwoPiInv / __real__ E.fz;
+    cplx ifz = mkc(0, __real__ E.fz);
+    for (int i = 0; i < d; i++) E.mean[i] /= ifz;
+    for (int i = 0; i < d; i++)
+        for (int j = 0; j < d; j++) E.cov[i * d + j] = (E.cov[i * d + j] / E.fz) - E.mean[i] * E.mean[j];
+    E.raw_fz = E.fz;
+    E.raw_mean = E.mean;
+    E.raw_cov = E.cov;
+    const int cells = cells_central(d, d) / 2;
+    for (auto& t : all) {
+        t.g = GTable();
+        for (int j = 0; j < cells; j++) {
+            double ygi = 0;
+            for (int k = 0; k < d; k++)
+                if (!(t.horthog & (1u << k))) ygi += t.p[k] * (((j >> k) & 1) == 0 ? 1.0 : -1.0);
+            cplx v = 1.0 / mkc(ygi + t.d_val, t.c_val) - 1.0 / mkc(ygi - t.d_val, t.c_val);
+            v *= E.gscale;
+            t.g.keys.push_back(j);
+            t.g.vals.push_back(v);
+        }
+        become_parent(t);
+    }
+    E.terms = std::move(all);
+    E.Nt = (int)E.terms.size();
+    E.terms_per_shape.assign(E.shape_range, 0);
+    E.terms_per_shape[d] = E.Nt;
+    E.post_mu_terms += E.Nt;
+    E.fz = mkc(1, 0);
+    E.last_mean = E.mean;
+    E.last_cov = E.cov;
+    E.last_fz = E.fz;
+}
+
+// step_tp_to_muc (serial): cauchy_estimator.hpp:604-832, then
+// fast_term_reduction_and_create_gtables: cauchy_estimator.hpp:981-1177.
+static void step_rest(Estimator& E, double msmt, const double* Phi, const double* Gamma, const double* beta,
+                      const double* H, double gamma, const double* B, const double* u)
+{
+    const int d = E.d;
+    const bool with_tp = (E.master_step % E.p) == 0;
+    const bool skip = E.skip_post_mu;
+    double Gt[8 * 32], bt[32];
+    int gcnt = 0;
+    if (with_tp) gcnt = precoalign_gamma(Gamma, beta, E.pncc, d, Gt, bt);
+    E.fz = mkc(0, 0);
+    E.mean.assign(d, mkc(0, 0));
+    E.cov.assign(d * d, mkc(0, 0));
+    std::vector<Term> kids;
+    std::vector<Term>& P = E.terms;
+    cplx y[16];
+    long long skip_children = 0;
+    std::vector<int> skip_tps(E.shape_range, 0);
+    for (auto& t : P) {
+        if (with_tp) {
+            time_prop(t, d, Phi, B, u, E.cmcc);
+            tp_coalign(t, d, Gt, bt, gcnt);
+            if (!skip) {
+                if (t.m == t.phc) t.encB = std::make_shared<std::vector<int>>(t.gp->keys);
+                else tp_enumerate(E, t);
+            }
+        } else if (!skip) {
+            t.encB = std::make_shared<std::vector<int>>(t.gp->keys);
+        }
+        size_t k0 = kids.size();
+        msmt_update(t, d, kids, msmt, H, gamma, false, skip);
+        cplx g = eval_g_yei(t, d, E.root.data(), y, false);
+        accumulate(E, g, y);
+        for (size_t k = k0; k < kids.size(); k++) {
+            g = eval_g_yei(kids[k], d, E.root.data(), y, false);
+            accumulate(E, g, y);
+        }
+        if (!skip) {
+            normalize_rows(t, d, true);
+            t.has_cmap = false;
+            for (size_t k = k0; k < kids.size(); k++) {
+                int pre = kids[k].m;
+                int ns = mu_coalign(kids[k], d);
+                if (ns < 0) {
+                    fprintf(stderr, "oracle: anti-coaligned H-orthogonal hyperplanes\n");
+                    ns = kids[k].m;
+                }
+                kids[k].has_cmap = ns < pre;
+            }
+        } else {
+            // the final MU keeps only the counts (cauchy_estimator.hpp:749-751, 806-812)
+            const long long nk = (long long)(kids.size() - k0);
+            skip_children += nk;
+            skip_tps[t.m] += (int)nk + 1;
+            kids.resize(k0);
+        }
+    }
+    const long long n_after = (long long)P.size() + (long long)kids.size() + skip_children;
+    finalize_moments(E);
+    E.post_mu_terms += n_after;
+    if (skip) {
+        E.Nt = (int)n_after;
+        E.terms_per_shape = skip_tps;
+        return;
+    }
+    // regroup by shape: parents then children (cauchy_estimator.hpp:741-780)
+    std::vector<std::vector<Term*>> byshape(E.shape_range);
+    for (auto& t : P) byshape[t.m].push_back(&t);
+    for (auto& t : kids) byshape[t.m].push_back(&t);
+    std::vector<Term> next;
+    std::vector<Term*> survivors;
+    std::vector<int> tps(E.shape_range, 0);
+    for (int m = 0; m < E.shape_range; m++) {
+        if (byshape[m].empty()) continue;
+        std::vector<int> F;
+        ftr(byshape[m], d, F);
+        std::vector<Term*> outm;
+        make_gtables_shape(byshape[m], F, d, E.gscale, outm);
+        tps[m] = (int)outm.size();
+        for (auto* t : outm) survivors.push_back(t);
+    }
+    next.reserve(survivors.size());
+    for (auto* t : survivors) next.push_back(std::move(*t));
+    E.terms = std::move(next);
+    E.Nt = (int)E.terms.size();
+    E.terms_per_shape = tps;
+    E.fz = mkc(1, 0);
+}
+
+// ----------------------------------------------------------------------------
+// C ABI
+extern "C" {
+
+void* orc_create(const double* A0, const double* p0, const double* b0, int steps, int d, int cmcc, int pncc,
+                 int p, const double* root_point, const double* b_pert)
+{
+    Estimator* E = new Estimator();
+    E->d = d;
+    E->cmcc = cmcc;
+    E->pncc = pncc;
+    E->p = p;
+    E->num_steps = p * steps;
+    int max_shape = d > 1 ? (steps - 1) * pncc + d : d + pncc;
+    E->shape_range = max_shape + 1;
+    E->A0.assign(A0, A0 + d * d);
+    E->p0.assign(p0, p0 + d);
+    E->b0.assign(b0, b0 + d);
+    E->root.assign(root_point, root_point + d);
+    E->bpert.assign(b_pert, b_pert + max_shape);
+    E->combos.resize(E->shape_range);
+    for (int m = d + 1; m < E->shape_range; m++) lex_combos(m, d, E->combos[m]);
+    E->mean.assign(d, mkc(0, 0));
+    E->cov.assign(d * d, mkc(0, 0));
+    E->last_mean = E->mean;
+    E->last_cov = E->cov;
+    E->fz = E->last_fz = mkc(0, 0);
+    reset_terms(*E);
+    return E;
+}
+
+void orc_destroy(void* h) { delete (Estimator*)h; }
+
+int orc_step(void* h, double msmt, const double* Phi, const double* Gamma, const double* beta, const double* H,
+             double gamma, const double* B, const double* u)
+{
+    Estimator& E = *(Estimator*)h;
+    if (E.errors & (1 << ERR_FZ_NEGATIVE)) return E.errors;
+    if (E.master_step == E.num_steps) return -1;
+    E.skip_post_mu = E.master_step == E.num_steps - 1;
+    if (E.master_step == 0) step_first(E, msmt, H, gamma);
+    else step_rest(E, msmt, Phi, Gamma, beta, H, gamma, B, u);
+    E.master_step++;
+    return E.errors;
+}
+
+int orc_num_terms(void* h) { return ((Estimator*)h)->Nt; }
+long long orc_post_mu_terms(void* h) { return ((Estimator*)h)->post_mu_terms; }
+int orc_shape_range(void* h) { return ((Estimator*)h)->shape_range; }
+void orc_terms_per_shape(void* h, int* out)
+{
+    Estimator& E = *(Estimator*)h;
+    for (int i = 0; i < E.shape_range; i++) out[i] = E.terms_per_shape[i];
+}
+
+void orc_get_moments(void* h, double* fz, double* mean, double* cov, double* raw_fz, double* raw_mean,
+                     double* raw_cov, double* gscale)
+{
+    Estimator& E = *(Estimator*)h;
+    const int d = E.d;
+    fz[0] = __real__ E.fz;
+    fz[1] = __imag__ E.fz;
+    raw_fz[0] = __real__ E.raw_fz;
+    raw_fz[1] = __imag__ E.raw_fz;
+    for (int i = 0; i < d; i++) {
+        mean[2 * i] = __real__ E.mean[i];
+        mean[2 * i + 1] = __imag__ E.mean[i];
+        raw_mean[2 * i] = __real__ E.raw_mean[i];
+        raw_mean[2 * i + 1] = __imag__ E.raw_mean[i];
+    }
+    for (int i = 0; i < d * d; i++) {
+        cov[2 * i] = __real__ E.cov[i];
+        cov[2 * i + 1] = __imag__ E.cov[i];
+        raw_cov[2 * i] = __real__ E.raw_cov[i];
+        raw_cov[2 * i + 1] = __imag__ E.raw_cov[i];
+    }
+    *gscale = E.gscale;
+}
+
+long long orc_total_cells(void* h)
+{
+    Estimator& E = *(Estimator*)h;
+    long long s = 0;
+    for (auto& t : E.terms) s += t.gp ? (long long)t.gp->keys.size() : 0;
+    return s;
+}
+
+void orc_dump_terms(void* h, int* shape, double* A, double* p, double* b, int* cells, int* keys, double* gvals)
+{
+    Estimator& E = *(Estimator*)h;
+    const int d = E.d, M = E.shape_range - 1;
+    long long c = 0;
+    for (size_t t = 0; t < E.terms.size(); t++) {
+        const Term& T = E.terms[t];
+        shape[t] = T.m;
+        memset(A + t * M * d, 0, sizeof(double) * M * d);
+        memset(p + t * M, 0, sizeof(double) * M);
+        memcpy(A + t * M * d, T.A.data(), sizeof(double) * T.m * d);
+        memcpy(p + t * M, T.p.data(), sizeof(double) * T.m);
+        memcpy(b + t * d, T.b.data(), sizeof(double) * d);
+        int nc = T.gp ? (int)T.gp->keys.size() : 0;
+        cells[t] = nc;
+        for (int k = 0; k < nc; k++) {
+            keys[c] = T.gp->keys[k];
+            gvals[2 * c] = __real__ T.gp->vals[k];
+            gvals[2 * c + 1] = __imag__ T.gp->vals[k];
+            c++;
+        }
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,68 @@
+"""Loads the golden fixtures (made by tests/golden/make_golden.py from the
+reference itself) and compares estimator records against them."""
+import glob
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+# fz, mean and covariance tolerance (relative to the largest magnitude of the
+# quantity at that update); integer structure is compared exactly.
+REL_TOL = 1e-9
+
+
+def names():
+    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    prob = {k: z[k] for k in ("Phi", "Gamma", "beta", "H", "gamma", "A0", "p0", "b0", "msmts")}
+    for k in ("d", "pncc", "cmcc", "p", "steps"):
+        prob[k] = int(z[k])
+    prob["B"] = None
+    recs = []
+    for i in range(int(z["n_updates"])):
+        pre = "u%d_" % i
+        r = {k: z[pre + k] for k in ("err", "Nt", "tps", "fz", "raw_fz", "mean", "raw_mean", "cov", "raw_cov",
+                                      "gscale")}
+        r["err"] = int(r["err"]); r["Nt"] = int(r["Nt"])
+        if (pre + "T_shape") in z:
+            r["terms"] = {k: z[pre + "T_" + k] for k in ("shape", "A", "p", "b", "cells", "keys", "g")}
+        recs.append(r)
+    return prob, (z["root_point"], z["b_pert"]), recs
+
+
+def relerr(a, b):
+    a = np.asarray(a); b = np.asarray(b)
+    scale = max(np.max(np.abs(a)), 1e-300)
+    return float(np.max(np.abs(a - b)) / scale)
+
+
+def compare_records(got, want, rel_tol=REL_TOL, check_terms=True, first_raw_from_reported=True):
+    """Asserts a run's per-update records equal the golden ones: exact term
+    counts, shapes, error bits and g-table keys; moments within rel_tol."""
+    assert len(got) == len(want), (len(got), len(want))
+    for i, (g, w) in enumerate(zip(got, want)):
+        ctx = "update %d" % i
+        assert g["Nt"] == w["Nt"], (ctx, "Nt", g["Nt"], w["Nt"])
+        assert np.array_equal(np.asarray(g["tps"])[:len(w["tps"])], w["tps"]), (ctx, "terms per shape")
+        assert g["err"] == w["err"], (ctx, "error bits", g["err"], w["err"])
+        # update 0 never reaches the numeric check, so the raw copy is the reported one
+        if i == 0:
+            pairs = (("fz", "fz"), ("mean", "mean"), ("cov", "cov"))
+        else:
+            pairs = (("raw_fz", "raw_fz"), ("raw_mean", "raw_mean"), ("raw_cov", "raw_cov"), ("fz", "fz"),
+                     ("mean", "mean"), ("cov", "cov"))
+        for a, b in pairs:
+            assert relerr(g[a], w[b]) <= rel_tol, (ctx, a, relerr(g[a], w[b]))
+        assert abs(g["gscale"] - float(w["gscale"])) <= rel_tol * abs(float(w["gscale"])), (ctx, "gscale")
+        if check_terms and "terms" in w:
+            gt, wt = g["terms"], w["terms"]
+            assert np.array_equal(gt["shape"], wt["shape"]), (ctx, "term shapes")
+            assert np.array_equal(gt["cells"], wt["cells"]), (ctx, "cell counts")
+            assert np.array_equal(gt["keys"], wt["keys"]), (ctx, "g-table keys")
+            for k in ("A", "p", "b"):
+                assert relerr(gt[k], wt[k]) <= 1e-12, (ctx, k, relerr(gt[k], wt[k]))
+            assert relerr(gt["g"], wt["g"]) <= rel_tol, (ctx, "g values", relerr(gt["g"], wt["g"]))

@@ -1,0 +1,39 @@
+"""The oracle (oracle/mce_oracle.cpp) against the golden fixtures generated by
+the reference itself: bit-exact integer structure, 1e-9 relative moments."""
+import numpy as np
+import pytest
+
+import oracle
+from tests import golden_cases as G
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _build():
+    oracle.build(with_reference=False)
+
+
+@pytest.mark.parametrize("name", G.names())
+def test_oracle_matches_reference_golden(name):
+    prob, (rp, bp), want = G.load(name)
+    est = oracle.Oracle(prob, rp, bp)
+    got = oracle.run(est, prob, record_terms_upto=10**9)
+    est.close()
+    G.compare_records(got, want)
+
+
+def test_rand_constants_reproduce_reference_draws():
+    # root_point and b_pert come from libc rand() in the reference constructor
+    for name in G.names():
+        prob, (rp, bp), _ = G.load(name)
+        import numpy as _np
+        z = _np.load(G.GOLDEN + "/" + name + ".npz")
+        rp2, bp2 = oracle.draw_reference_constants(int(z["srand_seed"]), prob["d"], oracle.max_shape_of(prob))
+        assert np.array_equal(rp, rp2) and np.array_equal(bp, bp2)
+
+
+def test_cell_count_invariant_first_tables():
+    # after the first update every term holds 2^(d-1) cells (the central count / 2)
+    for name in G.names():
+        prob, _, want = G.load(name)
+        t = want[0]["terms"]
+        assert np.all(t["cells"] == 2 ** (prob["d"] - 1))
