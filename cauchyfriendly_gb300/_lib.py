@@ -1,0 +1,91 @@
+"""ctypes binding of libmce_gb300.so (the C ABI in include/mce_c_api.h).
+
+There is no fallback: if the library is not built, or no CUDA device is
+visible when an estimator is created, the call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+from . import build as _build
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_lp = ctypes.POINTER(ctypes.c_longlong)
+_vp = ctypes.c_void_p
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "mce_c_api.h")
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "mce_last_error": (ctypes.c_char_p, []),
+    "mce_draw_reference_constants": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                     _dp, _dp]),
+    "mce_batch_create": (_vp, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _ip, _dp, _dp,
+                               _dp, _dp, _dp, ctypes.c_int, _ip]),
+    "mce_batch_step": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int, _ip]),
+    "mce_batch_run": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int, _dp,
+                                     _dp, _dp, _ip, _lp]),
+    "mce_create": (_vp, [_dp, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp,
+                         _dp, _ip]),
+    "mce_step": (ctypes.c_int, [_vp, ctypes.c_double, _dp, _dp, _dp, _dp, ctypes.c_double, _dp, _dp]),
+    "mce_get_moments": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp]),
+    "mce_get_raw_moments": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp, _dp]),
+    "mce_get_errors": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "mce_num_terms": (ctypes.c_longlong, [_vp, ctypes.c_int]),
+    "mce_terms_per_shape": (ctypes.c_int, [_vp, ctypes.c_int, _ip, ctypes.c_int]),
+    "mce_post_mu_terms": (ctypes.c_longlong, [_vp]),
+    "mce_master_step": (ctypes.c_int, [_vp]),
+    "mce_device_errors": (ctypes.c_int, [_vp]),
+    "mce_total_cells": (ctypes.c_longlong, [_vp, ctypes.c_int]),
+    "mce_dump_terms": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _ip, _dp, _dp, _dp, _ip, _ip, _dp]),
+    "mce_reset": (ctypes.c_int, [_vp]),
+    "mce_reinitialize_start_statistics": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp]),
+    "mce_set_master_step": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "mce_set_window_number": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "mce_last_step_ms": (ctypes.c_double, [_vp]),
+    "mce_destroy": (None, [_vp]),
+}
+
+_LIB = None
+
+
+def header_functions():
+    """Function names declared in include/mce_c_api.h."""
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(mce_[a-z_]+)\s*\(", txt)))
+
+
+def load(build_if_missing=True):
+    """Loads the in-tree library, building it first when it is missing."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(_build.LIB):
+        if not build_if_missing:
+            raise OSError("libmce_gb300.so is not built (run cauchyfriendly_gb300.build.build())")
+        _build.build()
+    lib = ctypes.CDLL(_build.LIB)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def last_error():
+    return load().mce_last_error().decode(errors="replace")
+
+
+class MceError(RuntimeError):
+    pass
+
+
+def check(status, what):
+    if status < 0:
+        raise MceError("%s failed (%d): %s" % (what, status, last_error()))
+    return status

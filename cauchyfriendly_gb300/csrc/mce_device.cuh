@@ -1,0 +1,312 @@
+// Device-side building blocks of the MCE step path (sm_103a, FP64).
+//
+// Every arithmetic helper here evaluates in the same operation order as the
+// reference's C++ (natsnyder1/CauchyFriendly include/*.hpp) and the kernels are
+// compiled with --fmad=false, so the floating-point decisions that fix the
+// integer structure (coalignment, MU orthogonality, cond() vertex skipping,
+// term reduction, term approximation) take the same branches as the reference.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mce {
+
+constexpr int kMaxRows = 31;    // keys are 32-bit sign masks (cauchy_estimator.hpp:231-235)
+constexpr int kMaxDim = 8;
+constexpr int kMaxGamma = 8;   // process-noise columns per step
+constexpr double kTwoPiInv = 1.0 / (2.0 * 3.14159265358979323846);  // RECIPRICAL_TWO_PI
+constexpr double kCoalignEps = 1e-8;   // COALIGN_TP_EPS == COALIGN_MU_EPS
+constexpr double kMuEps = 1e-10;       // MU_EPS
+constexpr double kTermApproxEps = 1e-15;
+constexpr double kPluEps = 1e-15;
+constexpr double kCondEps = 1e12;
+constexpr double kReductionEps = 1e-8;
+
+// term flags
+constexpr int kFlagNewChild = 1;
+constexpr int kFlagHasCmap = 2;
+
+// device error bits (reported through the engine's status word)
+constexpr int kErrAntiCoalignedHorthog = 1;  // cauchy_term.hpp:673-687 exits the process
+constexpr int kErrTableOverflow = 2;
+constexpr int kErrShapeTooLarge = 4;
+constexpr int kErrResolveStalled = 8;
+constexpr int kErrDceOverflow = 16;
+
+struct cd {
+    double re, im;
+};
+__host__ __device__ inline cd mkcd(double r, double i) { return cd{r, i}; }
+__device__ inline cd cadd(cd a, cd b) { return cd{a.re + b.re, a.im + b.im}; }
+__device__ inline cd csub(cd a, cd b) { return cd{a.re - b.re, a.im - b.im}; }
+__device__ inline cd cconj(cd a) { return cd{a.re, -a.im}; }
+__device__ inline cd cscale(cd a, double s) { return cd{a.re * s, a.im * s}; }
+// (a+bi)(c+di) = (ac - bd) + (ad + bc)i, the textbook product.
+__device__ inline cd cmul(cd x, cd y)
+{
+    double ac = x.re * y.re, bd = x.im * y.im, ad = x.re * y.im, bc = x.im * y.re;
+    return cd{ac - bd, ad + bc};
+}
+// Complex division by R. L. Smith, "Algorithm 116: Complex division",
+// CACM 5(8), 1962: divide through by the larger of |c|, |d| to avoid overflow.
+__device__ inline cd cdiv(cd x, cd y)
+{
+    const double a = x.re, b = x.im, c = y.re, d = y.im;
+    if (fabs(c) < fabs(d)) {
+        const double r = c / d;
+        const double den = c * r + d;
+        return cd{(a * r + b) / den, (b * r - a) / den};
+    }
+    const double r = d / c;
+    const double den = d * r + c;
+    return cd{(b * r + a) / den, (b - a * r) / den};
+}
+
+// Binary search over ascending keys (gtable.hpp:283-301 semantics).
+__device__ inline int bsearch_key(const int* __restrict__ keys, int n, int key)
+{
+    int lo = 0, hi = n - 1;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        const int mk = keys[mid];
+        if (mk == key) return mid;
+        if (mk > key) hi = mid - 1;
+        else lo = mid + 1;
+    }
+    return -1;
+}
+
+// g numerator from the parent table with half storage: a key whose bit phc-1
+// is set is looked up reversed and conjugated (eval_gs.hpp:94-153).
+__device__ inline cd lookup_num(const int* __restrict__ keys, const cd* __restrict__ vals, int n, int enc, int phc)
+{
+    const int top = 1 << (phc - 1);
+    const int rev = (1 << phc) - 1;
+    if (enc & top) {
+        const int idx = bsearch_key(keys, n, rev ^ enc);
+        return idx < 0 ? mkcd(0, 0) : cconj(vals[idx]);
+    }
+    const int idx = bsearch_key(keys, n, enc);
+    return idx < 0 ? mkcd(0, 0) : vals[idx];
+}
+
+// Central-arrangement cell count (cell_enumeration.hpp:34-44).
+__host__ __device__ inline long long binom_ll(int n, int k)
+{
+    if (k < 0 || k > n) return 0;
+    if (k > n - k) k = n - k;
+    long long r = 1;
+    for (int i = 0; i < k; i++) {
+        r *= (n - i);
+        r /= (i + 1);
+    }
+    return r;
+}
+__host__ __device__ inline int cells_central(int m, int d)
+{
+    if (m < d) return 1 << m;
+    long long s = 0;
+    for (int i = 0; i < d; i++) s += binom_ll(m - 1, i);
+    return (int)(2 * s);
+}
+__host__ __device__ inline int half_cells_cap(int m, int d)
+{
+    int c = cells_central(m, d) / 2;
+    return c < 1 ? 1 : c;
+}
+
+// Row-vs-row coalignment gate (cauchy_term.hpp:494-504): +1 same, -1 opposite, 0 none.
+template <int D>
+__device__ inline int coalign_gate(const double* r, const double* c)
+{
+    bool pos = true, neg = true;
+#pragma unroll
+    for (int l = 0; l < D; l++) {
+        if (pos) pos &= fabs(r[l] - c[l]) < kCoalignEps;
+        if (neg) neg &= fabs(r[l] + c[l]) < kCoalignEps;
+        if (!(pos || neg)) break;
+    }
+    return pos ? 1 : (neg ? -1 : 0);
+}
+
+// Orientation mask of two equal arrangements: for each row, the first
+// component significant in both decides (cell_enumeration.hpp:630-640).
+template <int D>
+__device__ inline int orientation_mask(const double* Ai, const double* Aj, int m)
+{
+    int s = 0;
+    for (int k = 0; k < m; k++) {
+        int l = 0;
+        while (l < D - 1 && (fabs(Ai[k * D + l]) < kReductionEps || fabs(Aj[k * D + l]) < kReductionEps)) l++;
+        if (Ai[k * D + l] * Aj[k * D + l] < 0) s |= 1 << k;
+    }
+    return s;
+}
+
+// ---------------------------------------------------------------------------
+// Dense D x D linear algebra in the reference's operation order
+// (cauchy_linalg.hpp:1180-1390).
+template <int D>
+__device__ inline bool plu(double* A, int* P)
+{
+    for (int j = 0; j < D; j++) {
+        double piv = kPluEps;
+        int pi = -1;
+        for (int i = j; i < D; i++)
+            if (fabs(A[i * D + j]) > fabs(piv)) {
+                piv = A[i * D + j];
+                pi = i;
+            }
+        if (pi == -1) return false;
+        if (pi != j)
+            for (int c = 0; c < D; c++) {
+                const double t = A[j * D + c];
+                A[j * D + c] = A[pi * D + c];
+                A[pi * D + c] = t;
+            }
+        P[j] = pi;
+        for (int k = j + 1; k < D; k++) {
+            A[k * D + j] /= A[j * D + j];
+            const double t = A[k * D + j];
+            for (int q = j + 1; q < D; q++) A[k * D + q] -= t * A[j * D + q];
+        }
+    }
+    return true;
+}
+
+// Row permutation applied by the pivot list, inverted (cauchy_linalg.hpp:1258-1277).
+template <int D>
+__device__ inline void inverse_perm(const int* P, int* PT)
+{
+    int Preg[D];
+    for (int i = 0; i < D; i++) Preg[i] = i;
+    for (int i = 0; i < D; i++) {
+        const int t = Preg[i];
+        Preg[i] = Preg[P[i]];
+        Preg[P[i]] = t;
+    }
+    for (int i = 0; i < D; i++) PT[Preg[i]] = i;
+}
+
+template <int D>
+__device__ inline void lu_solve_inplace(const double* LU, double* x)
+{
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+        double s = x[i];
+#pragma unroll
+        for (int j = 0; j < i; j++) s -= LU[i * D + j] * x[j];
+        x[i] = s;
+    }
+#pragma unroll
+    for (int i = D - 1; i >= 0; i--) {
+        double s = x[i];
+#pragma unroll
+        for (int j = D - 1; j > i; j--) s -= LU[i * D + j] * x[j];
+        x[i] = s / LU[i * D + i];
+    }
+}
+
+// 1-norm condition number through the explicit inverse; on success A holds
+// the packed LU factors and P the pivots.  Returns +inf when PLU fails.
+template <int D>
+__device__ inline double cond1(double* A, int* P)
+{
+    double nrm = -1;
+#pragma unroll
+    for (int c = 0; c < D; c++) {
+        double s = 0;
+#pragma unroll
+        for (int r = 0; r < D; r++) s += fabs(A[r * D + c]);
+        if (s > nrm) nrm = s;
+    }
+    if (!plu<D>(A, P)) return 1.79769313486231570815e+308;
+    int PT[D];
+    inverse_perm<D>(P, PT);
+    double inrm = -1;
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+        double w[D];
+#pragma unroll
+        for (int j = 0; j < D; j++) w[j] = (j == PT[i]) ? 1.0 : 0.0;
+        lu_solve_inplace<D>(A, w);
+        double s = 0;
+#pragma unroll
+        for (int j = 0; j < D; j++) s += fabs(w[j]);
+        if (s > inrm) inrm = s;
+    }
+    return nrm * inrm;
+}
+
+template <int D>
+__device__ inline void solve_lu(const double* LU, const int* P, const double* b, double* x)
+{
+    int PT[D];
+    inverse_perm<D>(P, PT);
+    for (int i = 0; i < D; i++) x[PT[i]] = b[i];
+    lu_solve_inplace<D>(LU, x);
+}
+
+// ---------------------------------------------------------------------------
+// Post-MU term records (structure of arrays, one slot per term; rows padded
+// to the run's row capacity MC).
+struct TermRecs {
+    int* est;
+    int* m;       // rows after MU coalignment
+    int* pbc;     // rows at the MU (before MU coalignment)
+    int* phc;     // rows of the parent table's arrangement
+    int* z;       // index of the MU hyperplane (== pbc for the parent itself)
+    int* lhp;     // enc_lhp
+    int* fam;     // parent index (row of the parent list) of this term's family
+    int* flags;   // kFlagNewChild | kFlagHasCmap
+    unsigned* horthog;
+    double* A;    // [n][MC][D]
+    double* p;    // [n][MC]
+    double* q;    // [n][MC]
+    double* b;    // [n][D]
+    double* cval;
+    double* dval;
+    signed char* cmap;   // [n][MC]
+    signed char* csmap;  // [n][MC]
+};
+
+// Parent list at the start of a step (one slot per term, ordered by
+// estimator, shape, index).
+struct ParentList {
+    int* est;
+    int* m;          // rows (updated in place by time propagation)
+    int* m_old;      // rows before time propagation (the table's bit count)
+    double* A;       // [n][MC][D]
+    double* p;       // [n][MC]
+    double* b;       // [n][D]
+    long long* tab_off;  // g-table slice in the table arena
+    int* tab_cnt;
+    long long* B_off;    // this step's B (then B_mu) slice in the B arena
+    int* B_cnt;
+    int* nkids;      // integrable children written as records
+    int* nkids_all;  // integrable children (moments are taken over them even on the final MU)
+    long long* kscan;  // exclusive scan of nkids
+};
+
+struct Tables {
+    int* keys;
+    cd* vals;
+};
+
+// Per-estimator step inputs, packed by the host each step.
+template <int D>
+struct EstStep {
+    double msmt;
+    double gamma;
+    double Phi[D * D];
+    double H[D];
+    double Bu[D];     // B @ u (control shift), zero when there is no control
+    double Gt[kMaxGamma * D];  // pre-coaligned Gamma rows
+    double bt[kMaxGamma];
+    int gcnt;
+    int has_control;
+    int active;   // stepping this measurement
+    int skip;     // final measurement update of this estimator: moments only
+};
+
+}  // namespace mce

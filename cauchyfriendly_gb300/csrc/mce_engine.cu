@@ -1,0 +1,1303 @@
+// Host engine of the MCE step path and the C ABI declared in include/mce_c_api.h.
+//
+// One engine owns a batch of independent estimators that step in lock-step
+// (a single estimator is a batch of one).  All term state stays in device
+// arenas that only grow; a step issues the kernel sequence of
+// mce_kernels.cu on one stream and synchronises only where the host must
+// size the next allocation or read the moments the API returns.
+//
+// Host-side work per step is limited to per-estimator scalars: packing each
+// estimator's (Phi, Gamma, beta, H, gamma, B u) and pre-coaligning Gamma
+// (cauchy_util.hpp:128-210), and the numeric checks of the returned moments
+// (cauchy_estimator.hpp:359-461), both O(d^3) per estimator.
+#include "mce_kernels.cuh"
+#include "../../include/mce_c_api.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#ifndef MCE_ONLY_DIM
+#define MCE_ONLY_DIM -1  // every dimension and the C ABI in one unit
+#endif
+
+namespace mce {
+
+extern thread_local std::string g_last_error;
+#if MCE_ONLY_DIM <= 0
+thread_local std::string g_last_error;
+#endif
+
+static void set_error(const std::string& s) { g_last_error = s; }
+
+#define MCE_CUDA(call)                                                                     \
+    do {                                                                                   \
+        cudaError_t _e = (call);                                                           \
+        if (_e != cudaSuccess) {                                                           \
+            set_error(std::string(#call) + ": " + cudaGetErrorString(_e));                 \
+            return MCE_ERR_CUDA;                                                           \
+        }                                                                                  \
+    } while (0)
+
+// Grow-only device buffer.
+template <typename T>
+struct DevBuf {
+    T* ptr = nullptr;
+    size_t cap = 0;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        cap = 0;
+    }
+    int ensure(size_t n)
+    {
+        if (n <= cap && ptr) return MCE_OK;
+        size_t want = std::max<size_t>(n, cap + cap / 2);
+        want = std::max<size_t>(want, 64);
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(&ptr, want * sizeof(T));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            set_error(std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+            return MCE_ERR_NOMEM;
+        }
+        cap = want;
+        return MCE_OK;
+    }
+};
+
+// Numeric checks of one estimator's raw moments (cauchy_estimator.hpp:359-461,
+// covariance_checker cauchy_util.hpp:1882-2004).
+enum {
+    E_FZ_NEG = 9, E_FZ_UNST = 8, E_MEAN_DNE = 7, E_MEAN_NF = 6, E_MEAN_F = 5, E_MEAN_ANY = 4,
+    E_COV_DNE = 3, E_COV_NF = 2, E_COV_F = 1, E_COV_ANY = 0
+};
+
+static void jacobi_eigvals(const double* S, double* ev, int n)
+{
+    double a[64];
+    memcpy(a, S, sizeof(double) * n * n);
+    for (int sweep = 0; sweep < 100; sweep++) {
+        double off = 0;
+        for (int i = 0; i < n; i++)
+            for (int j = i + 1; j < n; j++) off += a[i * n + j] * a[i * n + j];
+        if (off < 1e-300) break;
+        for (int p = 0; p < n; p++)
+            for (int q = p + 1; q < n; q++) {
+                const double apq = a[p * n + q];
+                if (apq == 0) continue;
+                const double th = (a[q * n + q] - a[p * n + p]) / (2 * apq);
+                const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1));
+                const double c = 1 / sqrt(t * t + 1), s = t * c;
+                for (int k = 0; k < n; k++) {
+                    const double akp = a[k * n + p], akq = a[k * n + q];
+                    a[k * n + p] = c * akp - s * akq;
+                    a[k * n + q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < n; k++) {
+                    const double apk = a[p * n + k], aqk = a[q * n + k];
+                    a[p * n + k] = c * apk - s * aqk;
+                    a[q * n + k] = s * apk + c * aqk;
+                }
+            }
+    }
+    for (int i = 0; i < n; i++) ev[i] = a[i * n + i];
+}
+
+static int cov_flags(const double* cre, const double* cim, int d)
+{
+    int f = 0;
+    double ev[kMaxDim];
+    jacobi_eigvals(cre, ev, d);
+    for (int i = 0; i < d; i++)
+        if (ev[i] < -1e-5) f |= 1;
+    for (int i = 0; i < d - 1; i++) {
+        const double sii = sqrt(cre[i * d + i]);
+        for (int j = i + 1; j < d; j++) {
+            const double sjj = sqrt(cre[j * d + j]);
+            if (fabs(cre[i * d + j] / (sii * sjj)) > 1) f |= 2;
+        }
+    }
+    for (int i = 0; i < d; i++)
+        for (int j = i; j < d; j++)
+            if (fabs(cim[i * d + j]) / (fabs(cre[i * d + j]) + 1e-15) > 10) f |= 4;
+    for (int i = 0; i < d * d; i++)
+        if (fabs(cim[i]) > 2000) f |= 8;
+    return f;
+}
+
+struct EstHost {
+    int steps = 0;          // estimation steps
+    int num_updates = 0;    // p * steps
+    int max_shape = 0;
+    std::vector<double> A0, p0, b0;
+    int errors = 0;
+    // reported moments (after checks) and the last good ones
+    double fz[2] = {0, 0}, last_fz[2] = {0, 0};
+    std::vector<double> mean, cov, last_mean, last_cov;  // interleaved complex
+    // raw moments of the last update
+    double raw_fz[2] = {0, 0};
+    std::vector<double> raw_mean, raw_cov;
+    double gscale = 0;
+    long long nt = 1;
+    std::vector<int> tps;
+    int win_num = 0;
+};
+
+class EngineBase {
+public:
+    virtual ~EngineBase() {}
+    virtual int step(const double* msmt, const double* Phi, const double* Gamma, const double* beta,
+                     const double* H, const double* gamma, const double* B, const double* u, int shared,
+                     int* err_out) = 0;
+    virtual int dump_terms(int est, int max_shape, int* shape, double* A, double* p, double* b, int* cells,
+                           int* keys, double* g) = 0;
+    virtual long long total_cells(int est) = 0;
+    virtual int reset() = 0;
+
+    int E = 0, d = 0, cmcc = 0, pncc = 0, p = 0, MC = 0;
+    int master_step = 0;
+    int device_errors = 0;
+    long long post_mu_terms = 0;
+    double last_ms = 0;
+    std::vector<EstHost> est;
+    std::vector<double> roots, bpert;  // E*d, E*MC
+};
+
+template <int D>
+class Engine : public EngineBase {
+public:
+    LaunchCfg lc{};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // per-estimator device inputs
+    DevBuf<double> dA0, dp0, db0, droots, dbpert;
+    DevBuf<EstStep<D>> dsteps;
+    std::vector<EstStep<D>> hsteps;
+    DevBuf<long long> dpstart;
+    std::vector<long long> hpstart;  // E+1
+    // combos per shape (lexicographic d-subsets)
+    DevBuf<int> dcombo_off;
+    DevBuf<unsigned char> dcombos;
+    // parent lists (double-buffered) and tables
+    struct PBufs {
+        DevBuf<int> est, m, m_old, tab_cnt, B_cnt, nkids, nkids_all;
+        DevBuf<double> A, p, b;
+        DevBuf<long long> tab_off, B_off, kscan;
+        int ensure(long long n, int MC)
+        {
+            int s = MCE_OK;
+            s |= est.ensure(n + 1);
+            s |= m.ensure(n + 1);
+            s |= m_old.ensure(n + 1);
+            s |= tab_cnt.ensure(n + 1);
+            s |= B_cnt.ensure(n + 1);
+            s |= nkids.ensure(n + 1);
+            s |= nkids_all.ensure(n + 1);
+            s |= A.ensure((n + 1) * MC * D);
+            s |= p.ensure((n + 1) * MC);
+            s |= b.ensure((n + 1) * D);
+            s |= tab_off.ensure(n + 1);
+            s |= B_off.ensure(n + 1);
+            s |= kscan.ensure(n + 1);
+            return s;
+        }
+        ParentList view()
+        {
+            ParentList P;
+            P.est = est.ptr;
+            P.m = m.ptr;
+            P.m_old = m_old.ptr;
+            P.A = A.ptr;
+            P.p = p.ptr;
+            P.b = b.ptr;
+            P.tab_off = tab_off.ptr;
+            P.tab_cnt = tab_cnt.ptr;
+            P.B_off = B_off.ptr;
+            P.B_cnt = B_cnt.ptr;
+            P.nkids = nkids.ptr;
+            P.nkids_all = nkids_all.ptr;
+            P.kscan = kscan.ptr;
+            return P;
+        }
+    } Pb[2];
+    int cur = 0;
+    long long nP = 0;
+    struct TBufs {
+        DevBuf<int> keys;
+        DevBuf<cd> vals;
+    } Tb[2];
+    // per-step buffers
+    DevBuf<int> Bcap, Bkeys;
+    DevBuf<long long> kall_scan;
+    struct RBufs {
+        DevBuf<int> est, m, pbc, phc, z, lhp, fam, flags;
+        DevBuf<unsigned> horthog;
+        DevBuf<double> A, p, q, b, cval, dval;
+        DevBuf<signed char> cmap, csmap;
+        int ensure(long long n, int MC)
+        {
+            int s = MCE_OK;
+            s |= est.ensure(n + 1);
+            s |= m.ensure(n + 1);
+            s |= pbc.ensure(n + 1);
+            s |= phc.ensure(n + 1);
+            s |= z.ensure(n + 1);
+            s |= lhp.ensure(n + 1);
+            s |= fam.ensure(n + 1);
+            s |= flags.ensure(n + 1);
+            s |= horthog.ensure(n + 1);
+            s |= A.ensure((n + 1) * MC * D);
+            s |= p.ensure((n + 1) * MC);
+            s |= q.ensure((n + 1) * MC);
+            s |= b.ensure((n + 1) * D);
+            s |= cval.ensure(n + 1);
+            s |= dval.ensure(n + 1);
+            s |= cmap.ensure((n + 1) * MC);
+            s |= csmap.ensure((n + 1) * MC);
+            return s;
+        }
+        TermRecs view()
+        {
+            TermRecs R;
+            R.est = est.ptr;
+            R.m = m.ptr;
+            R.pbc = pbc.ptr;
+            R.phc = phc.ptr;
+            R.z = z.ptr;
+            R.lhp = lhp.ptr;
+            R.fam = fam.ptr;
+            R.flags = flags.ptr;
+            R.horthog = horthog.ptr;
+            R.A = A.ptr;
+            R.p = p.ptr;
+            R.q = q.ptr;
+            R.b = b.ptr;
+            R.cval = cval.ptr;
+            R.dval = dval.ptr;
+            R.cmap = cmap.ptr;
+            R.csmap = csmap.ptr;
+            return R;
+        }
+    } Rb;
+    DevBuf<cd> fam_mom, est_raw, scratch;
+    DevBuf<double> gscale;
+    DevBuf<long long> cellq, pred_off, goff, toff, rscan, bucket_off, rbase, scan_tmp, kall_est;
+    DevBuf<int> head, next, npred, preds, status, owner, gcnt, gfill, members, is_root, cap, roots_list, alive, src,
+        tcnt, hist, new_slot, counters, first_cnt;
+    std::vector<cd> h_raw;
+    std::vector<double> h_gscale;
+    std::vector<int> h_hist;
+    ScanScratch ss{};
+
+    int init(int E_, int cmcc_, int pncc_, int p_, const int* steps, const double* A0, const double* p0,
+             const double* b0, const double* root, const double* bp, int bp_stride)
+    {
+        E = E_;
+        d = D;
+        cmcc = cmcc_;
+        pncc = pncc_;
+        p = p_;
+        if (pncc > kMaxGamma || pncc < 0 || cmcc < 0 || p < 1) {
+            set_error("unsupported pncc/cmcc/p");
+            return MCE_ERR_ARG;
+        }
+        est.resize(E);
+        MC = 1;
+        for (int e = 0; e < E; e++) {
+            EstHost& h = est[e];
+            h.steps = steps[e];
+            if (h.steps < 1) {
+                set_error("steps must be >= 1");
+                return MCE_ERR_ARG;
+            }
+            h.num_updates = p * h.steps;
+            h.max_shape = D > 1 ? (h.steps - 1) * pncc + D : D + pncc;
+            MC = std::max(MC, h.max_shape);
+            h.A0.assign(A0 + (size_t)e * D * D, A0 + (size_t)(e + 1) * D * D);
+            h.p0.assign(p0 + (size_t)e * D, p0 + (size_t)(e + 1) * D);
+            h.b0.assign(b0 + (size_t)e * D, b0 + (size_t)(e + 1) * D);
+            h.mean.assign(2 * D, 0);
+            h.cov.assign(2 * D * D, 0);
+            h.last_mean = h.mean;
+            h.last_cov = h.cov;
+            h.raw_mean = h.mean;
+            h.raw_cov = h.cov;
+        }
+        if (MC > kMaxRows) {
+            set_error("max shape exceeds 31 hyperplanes (cauchy_estimator.hpp:231-235)");
+            return MCE_ERR_SHAPE;
+        }
+        // the shared-memory bitmaps of the cell enumeration hold 2^MC bits per warp
+        if (MC > 16) {
+            set_error("this build supports up to 16 hyperplanes per term");
+            return MCE_ERR_SHAPE;
+        }
+        if (bp && bp_stride < MC) {
+            for (int e = 0; e < E; e++)
+                if (bp_stride < est[e].max_shape) {
+                    set_error("b_pert stride smaller than an estimator's max shape");
+                    return MCE_ERR_ARG;
+                }
+        }
+        roots.assign((size_t)E * D, 0);
+        bpert.assign((size_t)E * MC, 0);
+        for (int e = 0; e < E; e++) {
+            if (root) memcpy(&roots[(size_t)e * D], root + (size_t)e * D, D * sizeof(double));
+            if (bp) memcpy(&bpert[(size_t)e * MC], bp + (size_t)e * bp_stride, est[e].max_shape * sizeof(double));
+        }
+        int dev = 0;
+        MCE_CUDA(cudaGetDevice(&dev));
+        MCE_CUDA(cudaDeviceGetAttribute(&lc.num_sms, cudaDevAttrMultiProcessorCount, dev));
+        MCE_CUDA(cudaStreamCreateWithFlags(&lc.stream, cudaStreamNonBlocking));
+        MCE_CUDA(cudaEventCreate(&ev0));
+        MCE_CUDA(cudaEventCreate(&ev1));
+        int s = MCE_OK;
+        s |= dA0.ensure((size_t)E * D * D);
+        s |= dp0.ensure((size_t)E * D);
+        s |= db0.ensure((size_t)E * D);
+        s |= droots.ensure((size_t)E * D);
+        s |= dbpert.ensure((size_t)E * MC);
+        s |= dsteps.ensure(E);
+        s |= dpstart.ensure(E + 1);
+        s |= est_raw.ensure((size_t)E * (1 + D + D * D));
+        s |= gscale.ensure(E);
+        s |= counters.ensure(8);
+        s |= first_cnt.ensure(E + 1);
+        s |= scan_tmp.ensure(1 << 16);
+        if (s) return MCE_ERR_NOMEM;
+        ss.block_sums = scan_tmp.ptr;
+        ss.cap = (long long)scan_tmp.cap;
+        MCE_CUDA(cudaMemcpy(droots.ptr, roots.data(), roots.size() * sizeof(double), cudaMemcpyHostToDevice));
+        MCE_CUDA(cudaMemcpy(dbpert.ptr, bpert.data(), bpert.size() * sizeof(double), cudaMemcpyHostToDevice));
+        // combination tables
+        std::vector<int> off(MC + 2, 0);
+        std::vector<unsigned char> cmb;
+        for (int m = 0; m <= MC; m++) {
+            off[m] = (int)cmb.size();
+            if (m > D) {
+                std::vector<int> c(D);
+                for (int i = 0; i < D; i++) c[i] = i;
+                while (true) {
+                    for (int i = 0; i < D; i++) cmb.push_back((unsigned char)c[i]);
+                    int i = D - 1;
+                    while (i >= 0 && c[i] == m - D + i) i--;
+                    if (i < 0) break;
+                    c[i]++;
+                    for (int j = i + 1; j < D; j++) c[j] = c[j - 1] + 1;
+                }
+            }
+        }
+        off[MC + 1] = (int)cmb.size();
+        if (cmb.empty()) cmb.push_back(0);
+        s |= dcombo_off.ensure(off.size());
+        s |= dcombos.ensure(cmb.size());
+        if (s) return MCE_ERR_NOMEM;
+        MCE_CUDA(cudaMemcpy(dcombo_off.ptr, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice));
+        MCE_CUDA(cudaMemcpy(dcombos.ptr, cmb.data(), cmb.size(), cudaMemcpyHostToDevice));
+        hsteps.resize(E);
+        return reset();
+    }
+
+    ~Engine() override
+    {
+        if (lc.stream) cudaStreamSynchronize(lc.stream);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (lc.stream) cudaStreamDestroy(lc.stream);
+    }
+
+    int reset() override
+    {
+        std::vector<double> A0((size_t)E * D * D), p0((size_t)E * D), b0((size_t)E * D);
+        for (int e = 0; e < E; e++) {
+            memcpy(&A0[(size_t)e * D * D], est[e].A0.data(), D * D * sizeof(double));
+            memcpy(&p0[(size_t)e * D], est[e].p0.data(), D * sizeof(double));
+            memcpy(&b0[(size_t)e * D], est[e].b0.data(), D * sizeof(double));
+            est[e].errors = 0;
+            est[e].nt = 1;
+            est[e].tps.assign(MC + 1, 0);
+            est[e].tps[D] = 1;
+        }
+        MCE_CUDA(cudaMemcpy(dA0.ptr, A0.data(), A0.size() * sizeof(double), cudaMemcpyHostToDevice));
+        MCE_CUDA(cudaMemcpy(dp0.ptr, p0.data(), p0.size() * sizeof(double), cudaMemcpyHostToDevice));
+        MCE_CUDA(cudaMemcpy(db0.ptr, b0.data(), b0.size() * sizeof(double), cudaMemcpyHostToDevice));
+        master_step = 0;
+        nP = 0;
+        post_mu_terms = 0;
+        device_errors = 0;
+        MCE_CUDA(cudaMemset(counters.ptr, 0, 8 * sizeof(int)));
+        return MCE_OK;
+    }
+
+    // Packs one estimator's step parameters; Gamma pre-coalignment follows
+    // precoalign_Gamma_beta (cauchy_util.hpp:128-210).
+    void pack(int e, double msmt, const double* Phi, const double* Gamma, const double* beta, const double* H,
+              double gamma, const double* B, const double* u, bool active, bool skip)
+    {
+        EstStep<D>& S = hsteps[e];
+        memset(&S, 0, sizeof(S));
+        S.msmt = msmt;
+        S.gamma = gamma;
+        S.active = active ? 1 : 0;
+        S.skip = skip ? 1 : 0;
+        memcpy(S.Phi, Phi, sizeof(double) * D * D);
+        memcpy(S.H, H, sizeof(double) * D);
+        if (cmcc > 0 && B && u) {
+            for (int i = 0; i < D; i++) {
+                double s = 0.0;
+                for (int j = 0; j < cmcc; j++) s += B[i * cmcc + j] * u[j];
+                S.Bu[i] = s;
+            }
+            S.has_control = 1;
+        }
+        const int n = pncc;
+        for (int i = 0; i < n; i++) {
+            for (int j = 0; j < D; j++) S.Gt[i * D + j] = Gamma[j * n + i];
+            S.bt[i] = beta[i];
+        }
+        for (int i = 0; i < n; i++) {
+            double nf = 0;
+            for (int j = 0; j < D; j++) nf += fabs(S.Gt[i * D + j]);
+            for (int j = 0; j < D; j++) S.Gt[i * D + j] /= nf;
+            S.bt[i] *= nf;
+        }
+        bool F[kMaxGamma];
+        for (int i = 0; i < n; i++) F[i] = true;
+        for (int i = 0; i < n - 1; i++)
+            if (F[i])
+                for (int j = i + 1; j < n; j++)
+                    if (F[j]) {
+                        bool pos = true, neg = true;
+                        for (int l = 0; l < D; l++) {
+                            const double r = S.Gt[i * D + l], c = S.Gt[j * D + l];
+                            if (pos) pos &= fabs(r - c) < kCoalignEps;
+                            if (neg) neg &= fabs(r + c) < kCoalignEps;
+                            if (!(pos || neg)) break;
+                        }
+                        if (pos || neg) {
+                            F[j] = false;
+                            S.bt[i] += S.bt[j];
+                        }
+                    }
+        int cnt = 0;
+        for (int i = 0; i < n; i++) cnt += F[i];
+        if (cnt != n) {
+            int uq = 1;
+            for (int j = 1; j < n; j++)
+                if (F[j]) {
+                    if (uq < j) {
+                        for (int l = 0; l < D; l++) S.Gt[uq * D + l] = S.Gt[j * D + l];
+                        S.bt[uq] = S.bt[j];
+                    }
+                    uq++;
+                }
+        }
+        S.gcnt = cnt;
+    }
+
+    int sync_and_check()
+    {
+        MCE_CUDA(cudaGetLastError());
+        MCE_CUDA(cudaStreamSynchronize(lc.stream));
+        int err = 0;
+        MCE_CUDA(cudaMemcpy(&err, counters.ptr, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err) {
+            device_errors |= err;
+            set_error("device error bits " + std::to_string(err));
+            return MCE_ERR_DEVICE;
+        }
+        return MCE_OK;
+    }
+
+    long long read_ll(const long long* p_)
+    {
+        long long v = 0;
+        cudaMemcpyAsync(&v, p_, sizeof(long long), cudaMemcpyDeviceToHost, lc.stream);
+        cudaStreamSynchronize(lc.stream);
+        return v;
+    }
+
+    int step(const double* msmt, const double* Phi, const double* Gamma, const double* beta, const double* H,
+             const double* gamma, const double* B, const double* u, int shared, int* err_out) override
+    {
+        const int ms = master_step;
+        const int sub = ms % p;
+        const bool with_tp = sub == 0;
+        bool any_active = false;
+        for (int e = 0; e < E; e++) {
+            const EstHost& h = est[e];
+            const bool done = ms >= h.num_updates;
+            const bool blocked = (h.errors >> E_FZ_NEG) & 1;
+            const bool active = !done && !blocked;
+            const bool skip = active && ms == h.num_updates - 1;
+            const size_t oe = shared ? 0 : (size_t)e;
+            pack(e, msmt[e], Phi + oe * D * D, Gamma + oe * D * pncc, beta + oe * pncc, H + (size_t)e * D, gamma[e],
+                 B ? B + oe * D * cmcc : nullptr, u ? u + (size_t)e * cmcc : nullptr, active, skip);
+            any_active |= active;
+        }
+        bool any_done_past = true;
+        for (int e = 0; e < E; e++)
+            if (ms < est[e].num_updates) any_done_past = false;
+        if (any_done_past) {
+            set_error("master_step == num_estimation_steps: the estimator must be reset");
+            return MCE_ERR_DONE;
+        }
+        MCE_CUDA(cudaMemcpyAsync(dsteps.ptr, hsteps.data(), sizeof(EstStep<D>) * E, cudaMemcpyHostToDevice,
+                                 lc.stream));
+        MCE_CUDA(cudaEventRecord(ev0, lc.stream));
+        int rc = any_active ? (ms == 0 ? step_first() : step_main(with_tp)) : MCE_OK;
+        if (rc != MCE_OK) return rc;
+        MCE_CUDA(cudaEventRecord(ev1, lc.stream));
+        rc = sync_and_check();
+        if (rc != MCE_OK) return rc;
+        float msf = 0;
+        cudaEventElapsedTime(&msf, ev0, ev1);
+        last_ms = msf;
+        // moments of every active estimator
+        finish_moments(ms);
+        master_step++;
+        if (err_out)
+            for (int e = 0; e < E; e++) err_out[e] = est[e].errors;
+        return MCE_OK;
+    }
+
+    void finish_moments(int ms)
+    {
+        const int NM = 1 + D + D * D;
+        for (int e = 0; e < E; e++) {
+            const EstStep<D>& S = hsteps[e];
+            if (!S.active) continue;
+            EstHost& h = est[e];
+            const cd* r = &h_raw[(size_t)e * NM];
+            h.raw_fz[0] = r[0].re;
+            h.raw_fz[1] = r[0].im;
+            for (int j = 0; j < D; j++) {
+                h.raw_mean[2 * j] = r[1 + j].re;
+                h.raw_mean[2 * j + 1] = r[1 + j].im;
+            }
+            for (int j = 0; j < D * D; j++) {
+                h.raw_cov[2 * j] = r[1 + D + j].re;
+                h.raw_cov[2 * j + 1] = r[1 + D + j].im;
+            }
+            h.gscale = h_gscale[e];
+            h.fz[0] = h.raw_fz[0];
+            h.fz[1] = h.raw_fz[1];
+            h.mean = h.raw_mean;
+            h.cov = h.raw_cov;
+            if (ms == 0) {
+                // step_first reports through compute_moments without the checks
+                h.last_mean = h.mean;
+                h.last_cov = h.cov;
+                h.fz[0] = 1;
+                h.fz[1] = 0;
+                h.last_fz[0] = 1;
+                h.last_fz[1] = 0;
+                continue;
+            }
+            numeric_check(h, ms);
+            if (!S.skip) {
+                // fz is set to 1 after the tables are rebuilt (cauchy_estimator.hpp:1172-1176)
+                h.fz[0] = 1;
+                h.fz[1] = 0;
+            }
+        }
+    }
+
+    void numeric_check(EstHost& h, int ms)
+    {
+        const int ph = ms % p;
+        const bool first = ph == 0, not_last = ph != p - 1, last = ph == p - 1;
+        if (first) {
+            h.errors |= (1 << E_MEAN_DNE) | (1 << E_COV_DNE);
+            h.errors &= ~((1 << E_MEAN_F) | (1 << E_MEAN_NF) | (1 << E_COV_NF) | (1 << E_COV_F));
+        }
+        int ne = 0;
+        if (h.fz[0] <= 0) ne |= 1 << E_FZ_NEG;
+        if (fabs(h.fz[1] / (1e-15 + h.fz[0])) > 1e-3) ne |= 1 << E_FZ_UNST;
+        bool mean_ok = true;
+        for (int i = 0; i < D; i++) {
+            const double re = fabs(h.mean[2 * i]), im = fabs(h.mean[2 * i + 1]);
+            if (im / (1e-15 + re) > 1e-1 || im > 0.001) {
+                ne |= 1 << E_MEAN_ANY;
+                if (not_last) ne |= 1 << E_MEAN_NF;
+                if (last) ne |= 1 << E_MEAN_F;
+                mean_ok = false;
+            }
+        }
+        double cre[kMaxDim * kMaxDim], cim[kMaxDim * kMaxDim];
+        for (int i = 0; i < D * D; i++) {
+            cre[i] = h.cov[2 * i];
+            cim[i] = h.cov[2 * i + 1];
+        }
+        bool cov_ok = true;
+        if (cov_flags(cre, cim, D)) {
+            ne |= 1 << E_COV_ANY;
+            if (not_last) ne |= 1 << E_COV_NF;
+            if (last) ne |= 1 << E_COV_F;
+            cov_ok = false;
+        }
+        h.errors |= ne;
+        if (mean_ok) h.errors &= ~(1 << E_MEAN_DNE);
+        if (cov_ok) h.errors &= ~(1 << E_COV_DNE);
+        if (mean_ok) h.last_mean = h.mean;
+        else h.mean = h.last_mean;
+        if (cov_ok) h.last_cov = h.cov;
+        else h.cov = h.last_cov;
+        if (!mean_ok && !cov_ok) {
+            h.fz[0] = h.last_fz[0];
+            h.fz[1] = h.last_fz[1];
+        } else {
+            h.last_fz[0] = h.fz[0];
+            h.last_fz[1] = h.fz[1];
+        }
+    }
+
+    int read_moments()
+    {
+        const int NM = 1 + D + D * D;
+        h_raw.resize((size_t)E * NM);
+        h_gscale.resize(E);
+        MCE_CUDA(cudaMemcpyAsync(h_raw.data(), est_raw.ptr, sizeof(cd) * E * NM, cudaMemcpyDeviceToHost, lc.stream));
+        MCE_CUDA(cudaMemcpyAsync(h_gscale.data(), gscale.ptr, sizeof(double) * E, cudaMemcpyDeviceToHost, lc.stream));
+        return MCE_OK;
+    }
+
+    int step_first()
+    {
+        int s = first_cnt.ensure(E + 1);
+        if (s) return s;
+        Kernels<D>::first_count(dA0.ptr, dsteps.ptr, E, first_cnt.ptr, lc);
+        std::vector<int> cnt(E);
+        MCE_CUDA(cudaMemcpyAsync(cnt.data(), first_cnt.ptr, sizeof(int) * E, cudaMemcpyDeviceToHost, lc.stream));
+        MCE_CUDA(cudaStreamSynchronize(lc.stream));
+        hpstart.assign(E + 1, 0);
+        for (int e = 0; e < E; e++) hpstart[e + 1] = hpstart[e] + cnt[e];
+        nP = hpstart[E];
+        PBufs& P = Pb[cur];
+        if ((s = P.ensure(nP, MC))) return s;
+        if ((s = Tb[cur].keys.ensure(nP << (D - 1)))) return s;
+        if ((s = Tb[cur].vals.ensure(nP << (D - 1)))) return s;
+        MCE_CUDA(cudaMemcpyAsync(dpstart.ptr, hpstart.data(), sizeof(long long) * (E + 1), cudaMemcpyHostToDevice,
+                                 lc.stream));
+        ParentList PV = P.view();
+        Kernels<D>::first_build(dA0.ptr, dp0.ptr, db0.ptr, dsteps.ptr, droots.ptr, E, dpstart.ptr, PV, MC,
+                                est_raw.ptr, lc);
+        // G_SCALE_FACTOR per estimator from the first moments
+        k_gscale_from_raw(E);
+        Kernels<D>::first_tables(PV, nP, reinterpret_cast<double*>(PV.kscan), reinterpret_cast<double*>(PV.B_off),
+                                 reinterpret_cast<unsigned*>(PV.nkids), gscale.ptr, Tables{Tb[cur].keys.ptr,
+                                 Tb[cur].vals.ptr}, MC, lc);
+        read_moments();
+        for (int e = 0; e < E; e++) {
+            est[e].nt = cnt[e];
+            est[e].tps.assign(MC + 1, 0);
+            est[e].tps[D] = cnt[e];
+            post_mu_terms += cnt[e];
+        }
+        return MCE_OK;
+    }
+
+    void k_gscale_from_raw(int E_);
+
+    int step_main(bool with_tp)
+    {
+        int s;
+        PBufs& P = Pb[cur];
+        PBufs& Pn = Pb[cur ^ 1];
+        ParentList PV = P.view();
+        Tables Told{Tb[cur].keys.ptr, Tb[cur].vals.ptr};
+        int* err = counters.ptr;
+        if ((s = Bcap.ensure(nP + 1))) return s;
+        if ((s = kall_scan.ensure(nP + 2))) return s;
+
+        if ((s = ensure_scan_scratch(nP + 1))) return s;
+        Kernels<D>::tp(PV, nP, dsteps.ptr, with_tp ? 1 : 0, MC, Bcap.ptr, err, lc);
+        scan_int_to_ll(PV.nkids, PV.kscan, nP, ss, lc);
+        scan_int_to_ll(Bcap.ptr, PV.B_off, nP, ss, lc);
+        scan_int_to_ll(PV.nkids_all, kall_scan.ptr, nP, ss, lc);
+        long long tot[3] = {0, 0, 0};
+        MCE_CUDA(cudaMemcpyAsync(&tot[0], PV.kscan + nP, sizeof(long long), cudaMemcpyDeviceToHost, lc.stream));
+        MCE_CUDA(cudaMemcpyAsync(&tot[1], PV.B_off + nP, sizeof(long long), cudaMemcpyDeviceToHost, lc.stream));
+        MCE_CUDA(cudaMemcpyAsync(&tot[2], kall_scan.ptr + nP, sizeof(long long), cudaMemcpyDeviceToHost, lc.stream));
+        // per-estimator post-MU counts for the un-reduced final MU
+        std::vector<long long> kall_at(E + 1, 0);
+        MCE_CUDA(cudaStreamSynchronize(lc.stream));
+        const long long K = tot[0], Btot = tot[1], Kall = tot[2];
+        const long long nR = nP + K;
+        post_mu_terms += nP + Kall;
+        if ((s = fam_mom.ensure((size_t)(nP + Kall + 1) * (1 + D + D * D)))) return s;
+        if ((s = Bkeys.ensure(Btot + 1))) return s;
+        if ((s = Rb.ensure(nR, MC))) return s;
+        Kernels<D>::build_B(PV, nP, dsteps.ptr, with_tp ? 1 : 0, Told, Bkeys.ptr, Btot, dbpert.ptr, MC,
+                            dcombo_off.ptr, dcombos.ptr, err, lc);
+        TermRecs R = Rb.view();
+        Kernels<D>::mu(PV, nP, dsteps.ptr, dpstart.ptr, droots.ptr, Told, Bkeys.ptr, R, nR, kall_scan.ptr,
+                       fam_mom.ptr, MC, err, lc);
+        Kernels<D>::moments(fam_mom.ptr, dpstart.ptr, kall_scan.ptr, E, dsteps.ptr, est_raw.ptr, gscale.ptr, lc);
+        read_moments();
+        // terms after the MU per estimator (un-reduced count, cauchy_estimator.hpp:749-751, 806-812)
+        if ((s = kall_est.ensure(E + 2))) return s;
+        k_gather_bounds(kall_scan.ptr, E);
+        MCE_CUDA(cudaMemcpyAsync(kall_at.data(), kall_est.ptr, sizeof(long long) * (E + 1), cudaMemcpyDeviceToHost,
+                                 lc.stream));
+        // shapes of the final-MU estimators (terms_per_shape of the parents' shapes)
+        std::vector<int> skip_hist;
+        bool any_skip = false, any_keep = false;
+        for (int e = 0; e < E; e++) {
+            if (hsteps[e].active && hsteps[e].skip) any_skip = true;
+            if (hsteps[e].active && !hsteps[e].skip) any_keep = true;
+        }
+        const int MCp = MC + 1;
+        if (any_skip) {
+            if ((s = hist.ensure((size_t)E * MCp))) return s;
+            MCE_CUDA(cudaMemsetAsync(hist.ptr, 0, sizeof(int) * E * MCp, lc.stream));
+            k_skip_hist(PV, nP, MCp);
+            skip_hist.resize((size_t)E * MCp);
+            MCE_CUDA(cudaMemcpyAsync(skip_hist.data(), hist.ptr, sizeof(int) * E * MCp, cudaMemcpyDeviceToHost,
+                                     lc.stream));
+        }
+        MCE_CUDA(cudaStreamSynchronize(lc.stream));
+        for (int e = 0; e < E; e++) {
+            if (!hsteps[e].active) continue;
+            if (hsteps[e].skip) {
+                est[e].nt = (hpstart[e + 1] - hpstart[e]) + (kall_at[e + 1] - kall_at[e]);
+                est[e].tps.assign(MCp, 0);
+                for (int m = 0; m < MCp; m++) est[e].tps[m] = skip_hist[(size_t)e * MCp + m];
+            }
+        }
+        if (!any_keep || nR == 0) {
+            // every estimator that stepped has now finished
+            nP = 0;
+            std::vector<long long> z(E + 1, 0);
+            hpstart = z;
+            return MCE_OK;
+        }
+        // ---- fast term reduction
+        long long H = 1;
+        while (H < 2 * nR) H <<= 1;
+        if ((s = head.ensure(H))) return s;
+        if ((s = next.ensure(nR + 1))) return s;
+        if ((s = cellq.ensure(nR + 1))) return s;
+        if ((s = npred.ensure(nR + 1))) return s;
+        if ((s = pred_off.ensure(nR + 2))) return s;
+        if ((s = status.ensure(nR + 1))) return s;
+        if ((s = owner.ensure(nR + 1))) return s;
+        if ((s = ensure_scan_scratch(nR + 1))) return s;
+        MCE_CUDA(cudaMemsetAsync(head.ptr, 0xff, sizeof(int) * H, lc.stream));
+        Kernels<D>::ftr_insert(R, nR, cellq.ptr, head.ptr, next.ptr, H - 1, lc);
+        Kernels<D>::ftr_preds(R, nR, cellq.ptr, head.ptr, next.ptr, H - 1, MC, nullptr, nullptr, npred.ptr, lc);
+        scan_int_to_ll(npred.ptr, pred_off.ptr, nR, ss, lc);
+        const long long npreds = read_ll(pred_off.ptr + nR);
+        if ((s = preds.ensure(npreds + 1))) return s;
+        Kernels<D>::ftr_preds(R, nR, cellq.ptr, head.ptr, next.ptr, H - 1, MC, pred_off.ptr, preds.ptr, npred.ptr, lc);
+        k_status_init(R, nR);
+        for (int round = 0;; round++) {
+            MCE_CUDA(cudaMemsetAsync(counters.ptr + 1, 0, sizeof(int), lc.stream));
+            ftr_resolve(pred_off.ptr, preds.ptr, nR, status.ptr, owner.ptr, counters.ptr + 1, lc);
+            int unk = 0;
+            MCE_CUDA(cudaMemcpyAsync(&unk, counters.ptr + 1, sizeof(int), cudaMemcpyDeviceToHost, lc.stream));
+            MCE_CUDA(cudaStreamSynchronize(lc.stream));
+            if (unk == 0) break;
+            if (round > 100000) {
+                set_error("term reduction did not converge");
+                device_errors |= kErrResolveStalled;
+                return MCE_ERR_DEVICE;
+            }
+        }
+        // ---- reduction groups
+        if ((s = gcnt.ensure(nR + 1))) return s;
+        if ((s = gfill.ensure(nR + 1))) return s;
+        if ((s = goff.ensure(nR + 2))) return s;
+        MCE_CUDA(cudaMemsetAsync(gcnt.ptr, 0, sizeof(int) * (nR + 1), lc.stream));
+        MCE_CUDA(cudaMemsetAsync(gfill.ptr, 0, sizeof(int) * (nR + 1), lc.stream));
+        group_count(status.ptr, owner.ptr, nR, gcnt.ptr, lc);
+        scan_int_to_ll(gcnt.ptr, goff.ptr, nR, ss, lc);
+        const long long nmembers = read_ll(goff.ptr + nR);
+        if ((s = members.ensure(nmembers + 1))) return s;
+        group_fill(status.ptr, owner.ptr, nR, goff.ptr, gfill.ptr, members.ptr, lc);
+        group_sort(gcnt.ptr, goff.ptr, nR, members.ptr, lc);
+        if ((s = is_root.ensure(nR + 1))) return s;
+        if ((s = cap.ensure(nR + 1))) return s;
+        if ((s = rscan.ensure(nR + 2))) return s;
+        if ((s = toff.ensure(nR + 2))) return s;
+        roots_flags(status.ptr, Rb.m.ptr, nR, D, is_root.ptr, cap.ptr, lc);
+        scan_int_to_ll(is_root.ptr, rscan.ptr, nR, ss, lc);
+        scan_int_to_ll(cap.ptr, toff.ptr, nR, ss, lc);
+        long long t2[2];
+        MCE_CUDA(cudaMemcpyAsync(&t2[0], rscan.ptr + nR, sizeof(long long), cudaMemcpyDeviceToHost, lc.stream));
+        MCE_CUDA(cudaMemcpyAsync(&t2[1], toff.ptr + nR, sizeof(long long), cudaMemcpyDeviceToHost, lc.stream));
+        MCE_CUDA(cudaStreamSynchronize(lc.stream));
+        const long long nroots = t2[0], ttot = t2[1];
+        if ((s = roots_list.ensure(nroots + 1))) return s;
+        mce::roots_list(is_root.ptr, rscan.ptr, nR, roots_list.ptr, lc);
+        TBufs& Tn = Tb[cur ^ 1];
+        if ((s = Tn.keys.ensure(ttot + 1))) return s;
+        if ((s = Tn.vals.ensure(ttot + 1))) return s;
+        if ((s = alive.ensure(nR + 1))) return s;
+        if ((s = src.ensure(nR + 1))) return s;
+        if ((s = tcnt.ensure(nR + 1))) return s;
+        MCE_CUDA(cudaMemsetAsync(alive.ptr, 0, sizeof(int) * (nR + 1), lc.stream));
+        const int capMC = half_cells_cap(MC, D);
+        const long long max_warps = (long long)lc.num_sms * 16 * 4;
+        if ((s = scratch.ensure((size_t)max_warps * capMC))) return s;
+        Kernels<D>::gtable(R, roots_list.ptr, nroots, gcnt.ptr, goff.ptr, members.ptr, PV, Told, Bkeys.ptr, gscale.ptr,
+                           toff.ptr, Tables{Tn.keys.ptr, Tn.vals.ptr}, tcnt.ptr, alive.ptr, src.ptr, scratch.ptr,
+                           capMC, MC, err, lc);
+        // ---- next parent list
+        if ((s = hist.ensure((size_t)E * MCp))) return s;
+        if ((s = bucket_off.ensure((size_t)E * MCp + 2))) return s;
+        if ((s = new_slot.ensure(nR + 1))) return s;
+        if ((s = rbase.ensure(E + 2))) return s;
+        MCE_CUDA(cudaMemsetAsync(hist.ptr, 0, sizeof(int) * E * MCp, lc.stream));
+        partition_count(alive.ptr, Rb.est.ptr, Rb.m.ptr, nR, MCp, hist.ptr, lc);
+        if ((s = ensure_scan_scratch((long long)E * MCp + 1))) return s;
+        scan_int_to_ll(hist.ptr, bucket_off.ptr, (long long)E * MCp, ss, lc);
+        rbase_kernel(dpstart.ptr, PV.kscan, E, rbase.ptr, lc);
+        partition_rank(alive.ptr, Rb.m.ptr, rbase.ptr, E, MCp, bucket_off.ptr, new_slot.ptr, lc);
+        h_hist.resize((size_t)E * MCp);
+        MCE_CUDA(cudaMemcpyAsync(h_hist.data(), hist.ptr, sizeof(int) * E * MCp, cudaMemcpyDeviceToHost, lc.stream));
+        MCE_CUDA(cudaStreamSynchronize(lc.stream));
+        std::vector<long long> np(E + 1, 0);
+        for (int e = 0; e < E; e++) {
+            long long c = 0;
+            for (int m = 0; m < MCp; m++) c += h_hist[(size_t)e * MCp + m];
+            np[e + 1] = np[e] + c;
+        }
+        const long long nPn = np[E];
+        if ((s = Pn.ensure(nPn, MC))) return s;
+        ParentList PnV = Pn.view();
+        Kernels<D>::compact(R, alive.ptr, src.ptr, nR, new_slot.ptr, toff.ptr, tcnt.ptr, PnV, MC, lc);
+        for (int e = 0; e < E; e++) {
+            if (!hsteps[e].active || hsteps[e].skip) continue;
+            est[e].nt = np[e + 1] - np[e];
+            est[e].tps.assign(MCp, 0);
+            for (int m = 0; m < MCp; m++) est[e].tps[m] = h_hist[(size_t)e * MCp + m];
+        }
+        hpstart = np;
+        MCE_CUDA(cudaMemcpyAsync(dpstart.ptr, hpstart.data(), sizeof(long long) * (E + 1), cudaMemcpyHostToDevice,
+                                 lc.stream));
+        nP = nPn;
+        cur ^= 1;
+        return MCE_OK;
+    }
+
+    int ensure_scan_scratch(long long n)
+    {
+        long long need = 4;
+        long long t = n;
+        while (t > 1) {
+            t = (t + 2047) / 2048;
+            need += t + 2;
+        }
+        int s = scan_tmp.ensure(need + 64);
+        if (s) return s;
+        ss.block_sums = scan_tmp.ptr;
+        ss.cap = (long long)scan_tmp.cap;
+        return MCE_OK;
+    }
+
+    void k_skip_hist(ParentList PV, long long n, int MCp);
+    void k_gather_bounds(const long long* scan, int E_);
+    void k_status_init(TermRecs R, long long nR);
+
+    long long total_cells(int e) override
+    {
+        if (e < 0 || e >= E || nP == 0) return 0;
+        const long long a = hpstart[e], bnd = hpstart[e + 1];
+        std::vector<int> c(bnd - a);
+        if (bnd > a)
+            cudaMemcpy(c.data(), Pb[cur].tab_cnt.ptr + a, sizeof(int) * (bnd - a), cudaMemcpyDeviceToHost);
+        long long t = 0;
+        for (int x : c) t += x;
+        return t;
+    }
+
+    int dump_terms(int e, int max_shape, int* shape, double* A, double* p_, double* b, int* cells, int* keys,
+                   double* g) override
+    {
+        if (e < 0 || e >= E) return MCE_ERR_ARG;
+        if (nP == 0) return MCE_OK;
+        const long long a = hpstart[e], bnd = hpstart[e + 1], n = bnd - a;
+        PBufs& P = Pb[cur];
+        std::vector<int> m(n), tc(n);
+        std::vector<double> hA(n * MC * D), hp(n * MC), hb(n * D);
+        std::vector<long long> to(n);
+        MCE_CUDA(cudaMemcpy(m.data(), P.m.ptr + a, sizeof(int) * n, cudaMemcpyDeviceToHost));
+        MCE_CUDA(cudaMemcpy(tc.data(), P.tab_cnt.ptr + a, sizeof(int) * n, cudaMemcpyDeviceToHost));
+        MCE_CUDA(cudaMemcpy(to.data(), P.tab_off.ptr + a, sizeof(long long) * n, cudaMemcpyDeviceToHost));
+        MCE_CUDA(cudaMemcpy(hA.data(), P.A.ptr + a * MC * D, sizeof(double) * n * MC * D, cudaMemcpyDeviceToHost));
+        MCE_CUDA(cudaMemcpy(hp.data(), P.p.ptr + a * MC, sizeof(double) * n * MC, cudaMemcpyDeviceToHost));
+        MCE_CUDA(cudaMemcpy(hb.data(), P.b.ptr + a * D, sizeof(double) * n * D, cudaMemcpyDeviceToHost));
+        long long c = 0;
+        for (long long t = 0; t < n; t++) {
+            shape[t] = m[t];
+            for (int k = 0; k < max_shape * D; k++) A[t * max_shape * D + k] = 0;
+            for (int k = 0; k < max_shape; k++) p_[t * max_shape + k] = 0;
+            for (int k = 0; k < m[t] * D && k < max_shape * D; k++) A[t * max_shape * D + k] = hA[t * MC * D + k];
+            for (int k = 0; k < m[t] && k < max_shape; k++) p_[t * max_shape + k] = hp[t * MC + k];
+            for (int k = 0; k < D; k++) b[t * D + k] = hb[t * D + k];
+            cells[t] = tc[t];
+            std::vector<int> kk(tc[t]);
+            std::vector<cd> vv(tc[t]);
+            if (tc[t] > 0) {
+                MCE_CUDA(cudaMemcpy(kk.data(), Tb[cur].keys.ptr + to[t], sizeof(int) * tc[t], cudaMemcpyDeviceToHost));
+                MCE_CUDA(cudaMemcpy(vv.data(), Tb[cur].vals.ptr + to[t], sizeof(cd) * tc[t], cudaMemcpyDeviceToHost));
+            }
+            for (int k = 0; k < tc[t]; k++) {
+                keys[c] = kk[k];
+                g[2 * c] = vv[k].re;
+                g[2 * c + 1] = vv[k].im;
+                c++;
+            }
+        }
+        return MCE_OK;
+    }
+};
+
+static __global__ void k_gscale_kernel(const cd* est_raw, int NM, int E, double* gscale)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < E) gscale[e] = kTwoPiInv / est_raw[(long long)e * NM].re;
+}
+
+template <int D>
+void Engine<D>::k_gscale_from_raw(int E_)
+{
+    k_gscale_kernel<<<(E_ + 127) / 128, 128, 0, lc.stream>>>(est_raw.ptr, 1 + D + D * D, E_, gscale.ptr);
+}
+
+template <int D>
+__global__ void k_skip_hist_kernel(ParentList P, long long n, const EstStep<D>* st, int MCp, int* hist)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int e = P.est[i];
+        if (!st[e].skip) continue;
+        atomicAdd(&hist[(long long)e * MCp + P.m[i]], 1 + P.nkids_all[i]);
+    }
+}
+
+template <int D>
+void Engine<D>::k_skip_hist(ParentList PV, long long n, int MCp)
+{
+    if (n == 0) return;
+    k_skip_hist_kernel<D><<<(int)std::min<long long>((n + 255) / 256, lc.num_sms * 16), 256, 0, lc.stream>>>(
+        PV, n, dsteps.ptr, MCp, hist.ptr);
+}
+
+static __global__ void k_gather_kernel(const long long* scan, const long long* pstart, int E, long long* out)
+{
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e <= E; e += gridDim.x * blockDim.x) out[e] = scan[pstart[e]];
+}
+
+template <int D>
+void Engine<D>::k_gather_bounds(const long long* scan, int E_)
+{
+    k_gather_kernel<<<(E_ + 256) / 256, 256, 0, lc.stream>>>(scan, dpstart.ptr, E_, kall_est.ptr);
+}
+
+static __global__ void k_status_init_kernel(const int* est, long long n, int* status)
+{
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x)
+        status[j] = est[j] < 0 ? -1 : 0;
+}
+
+template <int D>
+void Engine<D>::k_status_init(TermRecs R, long long nR)
+{
+    if (nR == 0) return;
+    k_status_init_kernel<<<(int)std::min<long long>((nR + 255) / 256, lc.num_sms * 16), 256, 0, lc.stream>>>(
+        R.est, nR, status.ptr);
+}
+
+// Per-dimension factories: each dimension's engine lives in its own unit.
+#define MCE_DECLARE_DIM(D)                                                                                     \
+    EngineBase* make_engine_##D();                                                                            \
+    int init_engine_##D(EngineBase* b, int E, int cmcc, int pncc, int p, const int* steps, const double* A0,   \
+                        const double* p0, const double* b0, const double* root, const double* bp, int bps);
+#define MCE_DEFINE_DIM(D)                                                                                      \
+    EngineBase* make_engine_##D() { return new Engine<D>(); }                                                  \
+    int init_engine_##D(EngineBase* b, int E, int cmcc, int pncc, int p, const int* steps, const double* A0,   \
+                        const double* p0, const double* b0, const double* root, const double* bp, int bps)      \
+    {                                                                                                          \
+        return static_cast<Engine<D>*>(b)->init(E, cmcc, pncc, p, steps, A0, p0, b0, root, bp, bps);          \
+    }
+MCE_DECLARE_DIM(1)
+MCE_DECLARE_DIM(2)
+MCE_DECLARE_DIM(3)
+MCE_DECLARE_DIM(4)
+MCE_DECLARE_DIM(5)
+MCE_DECLARE_DIM(6)
+MCE_DECLARE_DIM(7)
+MCE_DECLARE_DIM(8)
+#if MCE_ONLY_DIM == 1 || MCE_ONLY_DIM < 0
+MCE_DEFINE_DIM(1)
+#endif
+#if MCE_ONLY_DIM == 2 || MCE_ONLY_DIM < 0
+MCE_DEFINE_DIM(2)
+#endif
+#if MCE_ONLY_DIM == 3 || MCE_ONLY_DIM < 0
+MCE_DEFINE_DIM(3)
+#endif
+#if MCE_ONLY_DIM == 4 || MCE_ONLY_DIM < 0
+MCE_DEFINE_DIM(4)
+#endif
+#if MCE_ONLY_DIM == 5 || MCE_ONLY_DIM < 0
+MCE_DEFINE_DIM(5)
+#endif
+#if MCE_ONLY_DIM == 6 || MCE_ONLY_DIM < 0
+MCE_DEFINE_DIM(6)
+#endif
+#if MCE_ONLY_DIM == 7 || MCE_ONLY_DIM < 0
+MCE_DEFINE_DIM(7)
+#endif
+#if MCE_ONLY_DIM == 8 || MCE_ONLY_DIM < 0
+MCE_DEFINE_DIM(8)
+#endif
+
+}  // namespace mce
+
+#if MCE_ONLY_DIM <= 0
+using namespace mce;
+
+struct mce_handle {
+    EngineBase* eng;
+};
+
+extern "C" {
+
+const char* mce_last_error(void) { return g_last_error.c_str(); }
+
+int mce_draw_reference_constants(long long seed, int d, int max_shape, int num_cpus, double* root_point,
+                                 double* b_pert)
+{
+    if (d < 1 || max_shape < 1 || num_cpus < 1 || !root_point || !b_pert) return MCE_ERR_ARG;
+    if (seed >= 0) srand((unsigned)seed);
+    auto u = []() { return ((double)rand() + 1.0) / ((double)RAND_MAX + 1.0); };
+    for (int i = 0; i < d; i++) root_point[i] = 1.0 + u();
+    for (int h = 0; h < num_cpus; h++)
+        for (int i = 0; i < max_shape; i++) {
+            const double v = 2 * u() - 1;
+            if (h == 0) b_pert[i] = v;
+        }
+    return MCE_OK;
+}
+
+mce_handle* mce_batch_create(int n_est, int d, int cmcc, int pncc, int p, const int* steps, const double* A0,
+                             const double* p0, const double* b0, const double* root_point, const double* b_pert,
+                             int bpert_stride, int* status)
+{
+    int st = MCE_OK;
+    mce_handle* h = nullptr;
+    if (n_est < 1 || d < 1 || d > kMaxDim || !steps || !A0 || !p0 || !b0) {
+        set_error("invalid arguments to mce_batch_create");
+        if (status) *status = MCE_ERR_ARG;
+        return nullptr;
+    }
+    std::vector<double> roots, bps;
+    int stride = bpert_stride;
+    if (!root_point || !b_pert) {
+        // draw as the reference constructor does, estimator after estimator
+        int msmax = 1;
+        for (int e = 0; e < n_est; e++) msmax = std::max(msmax, d > 1 ? (steps[e] - 1) * pncc + d : d + pncc);
+        roots.resize((size_t)n_est * d);
+        bps.assign((size_t)n_est * msmax, 0);
+        for (int e = 0; e < n_est; e++) {
+            const int ms = d > 1 ? (steps[e] - 1) * pncc + d : d + pncc;
+            mce_draw_reference_constants(-1, d, ms, 8, &roots[(size_t)e * d], &bps[(size_t)e * msmax]);
+        }
+        if (root_point) memcpy(roots.data(), root_point, sizeof(double) * n_est * d);
+        if (b_pert) {
+            for (int e = 0; e < n_est; e++)
+                memcpy(&bps[(size_t)e * msmax], b_pert + (size_t)e * bpert_stride,
+                       sizeof(double) * std::min(bpert_stride, msmax));
+        }
+        root_point = roots.data();
+        b_pert = bps.data();
+        stride = msmax;
+    }
+    EngineBase* eng = nullptr;
+#define MCE_CASE(D)                                                                                    \
+    case D:                                                                                            \
+        eng = make_engine_##D();                                                                       \
+        st = init_engine_##D(eng, n_est, cmcc, pncc, p, steps, A0, p0, b0, root_point, b_pert, stride); \
+        break;
+    switch (d) {
+        MCE_CASE(1) MCE_CASE(2) MCE_CASE(3) MCE_CASE(4) MCE_CASE(5) MCE_CASE(6) MCE_CASE(7) MCE_CASE(8)
+    }
+#undef MCE_CASE
+    if (st != MCE_OK) {
+        delete eng;
+        if (status) *status = st;
+        return nullptr;
+    }
+    h = new mce_handle{eng};
+    if (status) *status = MCE_OK;
+    return h;
+}
+
+int mce_batch_step(mce_handle* h, const double* msmt, const double* Phi, const double* Gamma, const double* beta,
+                   const double* H, const double* gamma, const double* B, const double* u, int shared_model,
+                   int* err_out)
+{
+    if (!h || !msmt || !Phi || !H || !gamma) return MCE_ERR_ARG;
+    if (h->eng->pncc > 0 && (!Gamma || !beta)) return MCE_ERR_ARG;
+    static const double zero[kMaxGamma * kMaxDim] = {0};
+    const int E = h->eng->E, d = h->eng->d;
+    if (shared_model) {
+        // one model for every estimator: H and gamma are expanded per estimator
+        std::vector<double> Hs((size_t)E * d), gs(E);
+        for (int e = 0; e < E; e++) {
+            memcpy(&Hs[(size_t)e * d], H, sizeof(double) * d);
+            gs[e] = gamma[0];
+        }
+        return h->eng->step(msmt, Phi, Gamma ? Gamma : zero, beta ? beta : zero, Hs.data(), gs.data(), B, u, 1,
+                            err_out);
+    }
+    return h->eng->step(msmt, Phi, Gamma ? Gamma : zero, beta ? beta : zero, H, gamma, B, u, 0, err_out);
+}
+
+int mce_batch_run(mce_handle* h, const double* msmts, int max_steps, const double* Phi, const double* Gamma,
+                  const double* beta, const double* H, const double* gamma, const double* B, const double* u,
+                  int shared_model, double* fz, double* mean, double* cov, int* err, long long* nt)
+{
+    if (!h || !msmts || max_steps < 1) return MCE_ERR_ARG;
+    EngineBase* g = h->eng;
+    const int E = g->E, d = g->d, p = g->p;
+    int max_updates = 0;
+    for (auto& e : g->est) max_updates = std::max(max_updates, e.num_updates);
+    std::vector<double> z(E), gam(E), Hrow((size_t)E * d);
+    for (int k = 0; k < max_updates; k++) {
+        const int step = k / p, j = k % p;
+        for (int e = 0; e < E; e++) {
+            z[e] = (step < max_steps) ? msmts[((size_t)e * max_steps + step) * p + j] : 0.0;
+            const size_t oe = shared_model ? 0 : (size_t)e;
+            gam[e] = gamma[oe * p + j];
+            memcpy(&Hrow[(size_t)e * d], H + (oe * p + j) * d, sizeof(double) * d);
+        }
+        const double* uk = u ? u + (size_t)k * E * g->cmcc : nullptr;
+        static const double zero[kMaxGamma * kMaxDim] = {0};
+        int rc = g->step(z.data(), Phi, Gamma ? Gamma : zero, beta ? beta : zero, Hrow.data(), gam.data(), B, uk,
+                         shared_model ? 1 : 0, nullptr);
+        if (rc != MCE_OK) return rc;
+        for (int e = 0; e < E; e++) {
+            const EstHost& s = g->est[e];
+            const size_t o = (size_t)e * max_updates + k;
+            if (fz) {
+                fz[2 * o] = s.fz[0];
+                fz[2 * o + 1] = s.fz[1];
+            }
+            if (mean) memcpy(mean + o * 2 * d, s.mean.data(), sizeof(double) * 2 * d);
+            if (cov) memcpy(cov + o * 2 * d * d, s.cov.data(), sizeof(double) * 2 * d * d);
+            if (err) err[o] = s.errors;
+            if (nt) nt[o] = s.nt;
+        }
+    }
+    return MCE_OK;
+}
+
+mce_handle* mce_create(const double* A0, const double* p0, const double* b0, int steps, int d, int cmcc, int pncc,
+                       int p, const double* root_point, const double* b_pert, int* status)
+{
+    const int ms = d > 1 ? (steps - 1) * pncc + d : d + pncc;
+    return mce_batch_create(1, d, cmcc, pncc, p, &steps, A0, p0, b0, root_point, b_pert, ms, status);
+}
+
+int mce_step(mce_handle* h, double msmt, const double* Phi, const double* Gamma, const double* beta, const double* H,
+             double gamma, const double* B, const double* u)
+{
+    int err = 0;
+    int rc = mce_batch_step(h, &msmt, Phi, Gamma, beta, H, &gamma, B, u, 1, &err);
+    return rc == MCE_OK ? err : rc;
+}
+
+static bool bad(mce_handle* h, int e) { return !h || e < 0 || e >= h->eng->E; }
+
+int mce_get_moments(mce_handle* h, int e, double* fz, double* mean, double* cov)
+{
+    if (bad(h, e)) return MCE_ERR_ARG;
+    const EstHost& s = h->eng->est[e];
+    if (fz) {
+        fz[0] = s.fz[0];
+        fz[1] = s.fz[1];
+    }
+    if (mean) memcpy(mean, s.mean.data(), sizeof(double) * s.mean.size());
+    if (cov) memcpy(cov, s.cov.data(), sizeof(double) * s.cov.size());
+    return MCE_OK;
+}
+
+int mce_get_raw_moments(mce_handle* h, int e, double* fz, double* mean, double* cov, double* gsf)
+{
+    if (bad(h, e)) return MCE_ERR_ARG;
+    const EstHost& s = h->eng->est[e];
+    if (fz) {
+        fz[0] = s.raw_fz[0];
+        fz[1] = s.raw_fz[1];
+    }
+    if (mean) memcpy(mean, s.raw_mean.data(), sizeof(double) * s.raw_mean.size());
+    if (cov) memcpy(cov, s.raw_cov.data(), sizeof(double) * s.raw_cov.size());
+    if (gsf) *gsf = s.gscale;
+    return MCE_OK;
+}
+
+int mce_get_errors(mce_handle* h, int e) { return bad(h, e) ? MCE_ERR_ARG : h->eng->est[e].errors; }
+long long mce_num_terms(mce_handle* h, int e) { return bad(h, e) ? MCE_ERR_ARG : h->eng->est[e].nt; }
+int mce_terms_per_shape(mce_handle* h, int e, int* out, int n)
+{
+    if (bad(h, e) || !out) return MCE_ERR_ARG;
+    const auto& t = h->eng->est[e].tps;
+    for (int i = 0; i < n; i++) out[i] = i < (int)t.size() ? t[i] : 0;
+    return MCE_OK;
+}
+long long mce_post_mu_terms(mce_handle* h) { return h ? h->eng->post_mu_terms : MCE_ERR_ARG; }
+int mce_master_step(mce_handle* h) { return h ? h->eng->master_step : MCE_ERR_ARG; }
+int mce_device_errors(mce_handle* h) { return h ? h->eng->device_errors : MCE_ERR_ARG; }
+long long mce_total_cells(mce_handle* h, int e) { return bad(h, e) ? MCE_ERR_ARG : h->eng->total_cells(e); }
+int mce_dump_terms(mce_handle* h, int e, int max_shape, int* shape, double* A, double* p, double* b, int* cells,
+                   int* keys, double* g)
+{
+    if (bad(h, e)) return MCE_ERR_ARG;
+    return h->eng->dump_terms(e, max_shape, shape, A, p, b, cells, keys, g);
+}
+int mce_reset(mce_handle* h) { return h ? h->eng->reset() : MCE_ERR_ARG; }
+int mce_reinitialize_start_statistics(mce_handle* h, int e, const double* A0, const double* p0, const double* b0)
+{
+    if (bad(h, e) || !A0 || !p0 || !b0) return MCE_ERR_ARG;
+    EstHost& s = h->eng->est[e];
+    const int d = h->eng->d;
+    s.A0.assign(A0, A0 + d * d);
+    s.p0.assign(p0, p0 + d);
+    s.b0.assign(b0, b0 + d);
+    return MCE_OK;
+}
+int mce_set_master_step(mce_handle* h, int ms)
+{
+    if (!h || ms < 0) return MCE_ERR_ARG;
+    h->eng->master_step = ms;
+    return MCE_OK;
+}
+int mce_set_window_number(mce_handle* h, int w)
+{
+    if (!h) return MCE_ERR_ARG;
+    for (auto& e : h->eng->est) e.win_num = w;
+    return MCE_OK;
+}
+double mce_last_step_ms(mce_handle* h) { return h ? h->eng->last_ms : -1.0; }
+void mce_destroy(mce_handle* h)
+{
+    if (!h) return;
+    delete h->eng;
+    delete h;
+}
+
+}  // extern "C"
+
+#endif  // MCE_ONLY_DIM <= 0

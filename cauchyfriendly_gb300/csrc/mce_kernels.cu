@@ -1,0 +1,1699 @@
+// sm_103a kernels of the MCE step path (FP64).  See mce_kernels.cuh for the
+// launch interface and mce_device.cuh for the shared numerics.
+//
+// Term order inside one estimator follows the reference's serial path
+// (include/cauchy_estimator.hpp:741-780): parents in (shape, index) order,
+// then children in (parent, hyperplane) order.  Estimators of a batch are laid
+// out one after another, so every per-estimator rule (root = lowest index in a
+// reduction group, member order, next parent order) is a rule on positions.
+#include "mce_kernels.cuh"
+
+#include <climits>
+
+#ifndef MCE_ONLY_DIM
+#define MCE_ONLY_DIM -1  // every dimension and the shape-agnostic kernels in one unit
+#endif
+#define MCE_COMMON_UNIT (MCE_ONLY_DIM <= 0)
+
+namespace mce {
+
+static constexpr unsigned kFull = 0xffffffffu;
+
+__device__ inline void set_err(int* err, int bit)
+{
+    if (err) atomicOr(err, bit);
+}
+
+static inline int grid_for(long long items, int per_block, int num_sms, int blocks_per_sm = 16)
+{
+    long long g = (items + per_block - 1) / per_block;
+    long long cap = (long long)num_sms * blocks_per_sm;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+// ---------------------------------------------------------------------------
+// Device-wide exclusive scan (int counts -> long long offsets + total).
+static constexpr int kScanThreads = 256;
+static constexpr int kScanItems = 8;
+static constexpr int kScanTile = kScanThreads * kScanItems;
+
+template <typename T>
+__device__ inline long long block_exclusive_scan(long long v, long long* total)
+{
+    __shared__ long long warp_sums[kScanThreads / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    long long x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        long long y = __shfl_up_sync(kFull, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        long long s = lane < kScanThreads / 32 ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            long long y = __shfl_up_sync(kFull, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < kScanThreads / 32) warp_sums[lane] = s;
+    }
+    __syncthreads();
+    long long pre = (w > 0 ? warp_sums[w - 1] : 0) + x - v;
+    *total = warp_sums[kScanThreads / 32 - 1];
+    __syncthreads();
+    return pre;
+}
+
+template <typename TIn>
+__global__ void k_scan_tiles(const TIn* in, long long* out, long long n, long long* tile_sums)
+{
+    const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems;
+    long long v[kScanItems];
+    long long s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        long long idx = base + k;
+        v[k] = idx < n ? (long long)in[idx] : 0;
+        s += v[k];
+    }
+    long long tot;
+    long long pre = block_exclusive_scan<long long>(s, &tot);
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        long long idx = base + k;
+        if (idx < n) out[idx] = pre;
+        pre += v[k];
+    }
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = tot;
+}
+
+#if MCE_COMMON_UNIT
+__global__ void k_scan_add(long long* out, long long n, const long long* tile_off)
+{
+    const long long base = (long long)blockIdx.x * kScanTile;
+    const long long add = tile_off[blockIdx.x];
+    for (int k = threadIdx.x; k < kScanTile; k += blockDim.x) {
+        long long idx = base + k;
+        if (idx < n) out[idx] += add;
+    }
+}
+
+__global__ void k_write_total(long long* out, long long n, const long long* tile_off, long long ntiles)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) out[n] = tile_off[ntiles];
+}
+
+static void scan_ll_inplace(long long* data, long long n, long long* scratch, long long scratch_cap,
+                            const LaunchCfg& c);
+
+// Exclusive scan of long long values in place, total written at data[n].
+__global__ void k_copy_ll(const long long* a, long long* b, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = a[i];
+}
+
+static void scan_ll_inplace(long long* data, long long n, long long* scratch, long long scratch_cap,
+                            const LaunchCfg& c)
+{
+    // data has n+1 slots
+    const long long ntiles = (n + kScanTile - 1) / kScanTile;
+    if (ntiles <= 1) {
+        long long* ts = scratch;
+        k_scan_tiles<long long><<<1, kScanThreads, 0, c.stream>>>(data, data, n, ts);
+        // total: the single tile sum
+        k_copy_ll<<<1, 32, 0, c.stream>>>(ts, data + n, 1);
+        return;
+    }
+    long long* ts = scratch;  // ntiles + 1
+    k_scan_tiles<long long><<<(unsigned)ntiles, kScanThreads, 0, c.stream>>>(data, data, n, ts);
+    scan_ll_inplace(ts, ntiles, scratch + ntiles + 1, scratch_cap - (ntiles + 1), c);
+    k_scan_add<<<(unsigned)ntiles, kScanThreads, 0, c.stream>>>(data, n, ts);
+    k_write_total<<<1, 32, 0, c.stream>>>(data, n, ts, ntiles);
+}
+
+void scan_int_to_ll(const int* in, long long* out, long long n, ScanScratch& s, const LaunchCfg& c)
+{
+    const long long ntiles = (n + kScanTile - 1) / kScanTile;
+    if (n == 0) {
+        cudaMemsetAsync(out, 0, sizeof(long long), c.stream);
+        return;
+    }
+    long long* ts = s.block_sums;
+    k_scan_tiles<int><<<(unsigned)ntiles, kScanThreads, 0, c.stream>>>(in, out, n, ts);
+    if (ntiles == 1) {
+        k_copy_ll<<<1, 32, 0, c.stream>>>(ts, out + n, 1);
+        return;
+    }
+    scan_ll_inplace(ts, ntiles, s.block_sums + ntiles + 1, s.cap - (ntiles + 1), c);
+    k_scan_add<<<(unsigned)ntiles, kScanThreads, 0, c.stream>>>(out, n, ts);
+    k_write_total<<<1, 32, 0, c.stream>>>(out, n, ts, ntiles);
+}
+
+#endif  // MCE_COMMON_UNIT
+
+// ---------------------------------------------------------------------------
+// First measurement update: one thread per estimator (d+1 terms at most).
+
+template <int D>
+__global__ void k_first_count(const double* A0, const EstStep<D>* st, int E, int* cnt)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    const EstStep<D>& S = st[e];
+    if (!S.active) {
+        cnt[e] = 0;
+        return;
+    }
+    int c = 1;
+    for (int l = 0; l < D; l++) {
+        double h = 0.0;
+        for (int j = 0; j < D; j++) h += S.H[j] * A0[(long long)e * D * D + l * D + j];
+        if (!(fabs(h) < kMuEps)) c++;
+    }
+    cnt[e] = c;
+}
+
+// msmt_update with first_update=true (cauchy_term.hpp:84-310) followed by
+// compute_moments (cauchy_estimator.hpp:524-602): the d+1 terms are written
+// to the parent list in the reference's order and the moments are summed in
+// that same order.
+template <int D>
+__global__ void k_first_build(const double* A0, const double* p0, const double* b0, const EstStep<D>* st,
+                              const double* roots, int E, const long long* pstart, ParentList P, int MC,
+                              double* cval, double* dval, unsigned* hof_out, cd* est_raw)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    const EstStep<D>& S = st[e];
+    if (!S.active) return;
+    const double* A = A0 + (long long)e * D * D;
+    const double* p = p0 + (long long)e * D;
+    const double* b = b0 + (long long)e * D;
+    const double* root = roots + (long long)e * D;
+    double mu[(D + 1) * D];
+    double rho[D + 1];
+    bool Fi[D + 1];
+    for (int l = 0; l < D; l++) {
+        double h = 0.0;
+        for (int j = 0; j < D; j++) h += S.H[j] * A[l * D + j];
+        const double ah = fabs(h);
+        if (ah < kMuEps) {
+            for (int j = 0; j < D; j++) mu[l * D + j] = A[l * D + j];
+            rho[l] = p[l];
+            Fi[l] = false;
+        } else {
+            const double r = 1.0 / h;
+            for (int j = 0; j < D; j++) mu[l * D + j] = A[l * D + j] * r;
+            rho[l] = p[l] * ah;
+            Fi[l] = true;
+        }
+    }
+    for (int j = 0; j < D; j++) mu[D * D + j] = 0.0;
+    rho[D] = S.gamma;
+    Fi[D] = true;
+    double hb = 0.0;
+    for (int j = 0; j < D; j++) hb += S.H[j] * b[j];
+    const double zeta = S.msmt - hb;
+
+    cd fz = mkcd(0, 0);
+    cd mean[D];
+    cd cov[D * D];
+    for (int j = 0; j < D; j++) mean[j] = mkcd(0, 0);
+    for (int j = 0; j < D * D; j++) cov[j] = mkcd(0, 0);
+
+    long long slot = pstart[e];
+    // order: the parent (t == D) first, then the children t = 0..D-1
+    for (int n = 0; n <= D; n++) {
+        const int t = (n == 0) ? D : n - 1;
+        if (!Fi[t]) continue;
+        double* At = P.A + slot * MC * D;
+        double* pt = P.p + slot * MC;
+        double* bt = P.b + slot * D;
+        unsigned hof = 0;
+        double ty[D];
+        for (int j = 0; j < D; j++) ty[j] = 0;
+        double ygi = 0;
+        int l = 0;
+        for (int ll = 0; ll <= D; ll++) {
+            if (ll == t) continue;
+            double row[D];
+            if (Fi[ll])
+                for (int j = 0; j < D; j++) row[j] = mu[ll * D + j] - mu[t * D + j];
+            else {
+                for (int j = 0; j < D; j++) row[j] = mu[ll * D + j];
+                hof |= 1u << l;
+            }
+            for (int j = 0; j < D; j++) At[l * D + j] = row[j];
+            pt[l] = rho[ll];
+            double s = 0.0;
+            for (int j = 0; j < D; j++) s += row[j] * root[j];
+            const double sg = s > 0 ? 1.0 : -1.0;
+            const double sc = rho[ll] * sg;
+            for (int j = 0; j < D; j++) ty[j] += sc * row[j];
+            if (!(hof & (1u << l))) ygi += rho[ll] * sg;
+            l++;
+        }
+        for (int j = 0; j < D; j++) bt[j] = b[j] + zeta * mu[t * D + j];
+        P.est[slot] = e;
+        P.m[slot] = D;
+        P.m_old[slot] = D;
+        cval[slot] = zeta;
+        dval[slot] = rho[t];
+        hof_out[slot] = hof;
+        const cd one = mkcd(1, 0);
+        cd g = csub(cdiv(one, mkcd(ygi + rho[t], zeta)), cdiv(one, mkcd(ygi - rho[t], zeta)));
+        g = cscale(g, kTwoPiInv);
+        fz = cadd(fz, g);
+        for (int j = 0; j < D; j++) {
+            const cd y = mkcd(-ty[j], bt[j]);
+            const cd gy = cmul(g, y);
+            mean[j] = cadd(mean[j], gy);
+            for (int k = 0; k < D; k++) cov[j * D + k] = csub(cov[j * D + k], cmul(gy, mkcd(-ty[k], bt[k])));
+        }
+        slot++;
+    }
+    // compute_moments finalisation (cauchy_estimator.hpp:567-578)
+    const int NM = 1 + D + D * D;
+    cd* out = est_raw + (long long)e * NM;
+    const cd ifz = mkcd(0, fz.re);
+    cd mfin[D];
+    for (int j = 0; j < D; j++) mfin[j] = cdiv(mean[j], ifz);
+    out[0] = fz;
+    for (int j = 0; j < D; j++) out[1 + j] = mfin[j];
+    for (int j = 0; j < D; j++)
+        for (int k = 0; k < D; k++)
+            out[1 + D + j * D + k] = csub(cdiv(cov[j * D + k], fz), cmul(mfin[j], mfin[k]));
+}
+
+// make_gtable_first (flattening.hpp:14-67): 2^(d-1) cells with keys 0..2^(d-1)-1.
+template <int D>
+__global__ void k_first_tables(ParentList P, long long nP, const double* cval, const double* dval,
+                               const unsigned* hof, const double* gscale, Tables T, int MC)
+{
+    const int cells = 1 << (D - 1);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nP * cells;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long t = i / cells;
+        const int j = (int)(i % cells);
+        const double* p = P.p + t * MC;
+        const unsigned h = hof[t];
+        double ygi = 0;
+        for (int k = 0; k < D; k++)
+            if (!(h & (1u << k))) ygi += p[k] * (((j >> k) & 1) == 0 ? 1.0 : -1.0);
+        const cd one = mkcd(1, 0);
+        cd v = csub(cdiv(one, mkcd(ygi + dval[t], cval[t])), cdiv(one, mkcd(ygi - dval[t], cval[t])));
+        v = cscale(v, gscale[P.est[t]]);
+        const long long off = t * cells;
+        T.keys[off + j] = j;
+        T.vals[off + j] = v;
+        if (j == 0) {
+            P.tab_off[t] = off;
+            P.tab_cnt[t] = cells;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Time propagation + TP coalignment (cauchy_term.hpp:435-531) and the count
+// of hyperplanes the MU will integrate (cauchy_term.hpp:106-130).
+template <int D>
+__global__ void k_tp(ParentList P, long long nP, const EstStep<D>* st, int with_tp, int MC, int* Bcap, int* err)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nP; i += (long long)gridDim.x * blockDim.x) {
+        const int e = P.est[i];
+        const EstStep<D>& S = st[e];
+        int m = P.m[i];
+        P.m_old[i] = m;
+        double* A = P.A + i * MC * D;
+        double* p = P.p + i * MC;
+        double* b = P.b + i * D;
+        if (with_tp) {
+            for (int r = 0; r < m; r++) {
+                double w[D];
+                for (int k = 0; k < D; k++) w[k] = A[r * D + k];
+                for (int j = 0; j < D; j++) {
+                    double s = 0.0;
+                    for (int k = 0; k < D; k++) s += w[k] * S.Phi[j * D + k];
+                    A[r * D + j] = s;
+                }
+            }
+            double wb[D];
+            for (int j = 0; j < D; j++) wb[j] = b[j];
+            for (int r = 0; r < D; r++) {
+                double s = 0.0;
+                for (int j = 0; j < D; j++) s += S.Phi[r * D + j] * wb[j];
+                b[r] = s;
+            }
+            if (S.has_control)
+                for (int r = 0; r < D; r++) b[r] += 1.0 * S.Bu[r];
+            // normalize_hps(false)
+            for (int r = 0; r < m; r++) {
+                double n1 = 0;
+                for (int j = 0; j < D; j++) n1 += fabs(A[r * D + j]);
+                p[r] *= n1;
+                for (int j = 0; j < D; j++) A[r * D + j] /= n1;
+            }
+            bool F[kMaxGamma];
+            for (int j = 0; j < S.gcnt; j++) F[j] = true;
+            for (int j = 0; j < S.gcnt; j++)
+                for (int k = 0; k < m; k++)
+                    if (F[j] && coalign_gate<D>(S.Gt + j * D, A + k * D) != 0) {
+                        F[j] = false;
+                        p[k] += S.bt[j];
+                    }
+            for (int j = 0; j < S.gcnt; j++)
+                if (F[j]) {
+                    if (m >= MC) {
+                        set_err(err, kErrShapeTooLarge);
+                        break;
+                    }
+                    for (int l = 0; l < D; l++) A[m * D + l] = S.Gt[j * D + l];
+                    p[m] = S.bt[j];
+                    m++;
+                }
+            P.m[i] = m;
+        }
+        int cnt = 0;
+        for (int l = 0; l < m; l++) {
+            double h = 0.0;
+            for (int j = 0; j < D; j++) h += S.H[j] * A[l * D + j];
+            if (!(fabs(h) < kMuEps)) cnt++;
+        }
+        P.nkids_all[i] = cnt;
+        P.nkids[i] = S.skip ? 0 : cnt;
+        int cap;
+        if (S.skip) cap = 0;
+        else if (with_tp && m != P.m_old[i]) cap = m < D ? (1 << (m - 1)) : half_cells_cap(m, D);
+        else cap = P.tab_cnt[i];
+        Bcap[i] = cap;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// B tables.  A parent whose arrangement grew under TP gets its cells from the
+// vertex enumeration of make_time_prop_btable (cell_enumeration.hpp:676-855):
+// every non-degenerate d-subset of hyperplanes (cond <= 1e12) is solved for a
+// vertex of the perturbed arrangement A x = b_pert, the 2^d cells around the
+// vertex are formed, those whose parent part is a parent cell are kept, and a
+// sign vector is output (half storage) when its negation was found too.  The
+// sets are held as shared-memory bitmaps, so the output comes out sorted and
+// de-duplicated without hashing.  Other parents copy their table keys.
+template <int D>
+__global__ void k_build_B(ParentList P, long long nP, const EstStep<D>* st, int with_tp, Tables Told, int* Bkeys,
+                          const double* bpert_all, int MC, const int* combo_off, const unsigned char* combos,
+                          int* err)
+{
+    extern __shared__ unsigned long long smem_u64[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+    const int words = (1 << MC) > 32 ? (1 << MC) / 32 : 1;
+    const int per_warp_u32 = 2 * words + 2 * MC * D + 2;  // two bitmaps + A rows (as doubles)
+    unsigned* base = reinterpret_cast<unsigned*>(smem_u64) + (size_t)wib * ((per_warp_u32 + 1) & ~1);
+    double* As = reinterpret_cast<double*>(base);
+    unsigned* PB = base + 2 * MC * D;
+    unsigned* IS = PB + words;
+    for (long long i = (long long)blockIdx.x * nwb + wib; i < nP; i += (long long)gridDim.x * nwb) {
+        const int e = P.est[i];
+        const EstStep<D>& S = st[e];
+        if (S.skip) continue;
+        const int m = P.m[i], phc = P.m_old[i];
+        int* out = Bkeys + P.B_off[i];
+        const int cap = (int)(P.B_off[i + 1] - P.B_off[i]);
+        const int* pk = Told.keys + P.tab_off[i];
+        const int pcnt = P.tab_cnt[i];
+        const bool dce = with_tp && m != phc;
+        if (!dce) {
+            for (int k = lane; k < pcnt; k += 32)
+                if (k < cap) out[k] = pk[k];
+            if (lane == 0) {
+                P.B_cnt[i] = pcnt <= cap ? pcnt : cap;
+                if (pcnt > cap) set_err(err, kErrTableOverflow);
+            }
+            continue;
+        }
+        if (m < D) {
+            const int n = 1 << (m - 1);
+            for (int k = lane; k < n && k < cap; k += 32) out[k] = k;
+            if (lane == 0) P.B_cnt[i] = n;
+            continue;
+        }
+        const double* A = P.A + i * MC * D;
+        for (int k = lane; k < m * D; k += 32) As[k] = A[k];
+        const int mw = (1 << m) > 32 ? (1 << m) / 32 : 1;
+        const int pw = (1 << phc) > 32 ? (1 << phc) / 32 : 1;
+        for (int k = lane; k < mw; k += 32) IS[k] = 0;
+        for (int k = lane; k < pw; k += 32) PB[k] = 0;
+        __syncwarp();
+        for (int k = lane; k < pcnt; k += 32) {
+            const int key = pk[k];
+            if (key >= 0 && key < (1 << phc)) atomicOr(&PB[key >> 5], 1u << (key & 31));
+        }
+        __syncwarp();
+        const double* bp = bpert_all + (long long)e * MC;
+        const int gmask = (1 << phc) - 1, ptop = 1 << (phc - 1);
+        const int ncomb = m > D ? (int)binom_ll(m, D) : 0;
+        const unsigned char* cmb = combos + combo_off[m];
+        for (int ci = lane; ci < ncomb; ci += 32) {
+            const unsigned char* c = cmb + (long long)ci * D;
+            double Ac[D * D], bc[D], v[D];
+            int Pv[D];
+            for (int j = 0; j < D; j++) {
+                for (int l = 0; l < D; l++) Ac[j * D + l] = As[c[j] * D + l];
+                bc[j] = bp[c[j]];
+            }
+            if (cond1<D>(Ac, Pv) > kCondEps) continue;
+            solve_lu<D>(Ac, Pv, bc, v);
+            unsigned inmask = 0;
+            for (int j = 0; j < D; j++) inmask |= 1u << c[j];
+            int niv = 0;
+            for (int a = 0; a < m; a++) {
+                if (inmask & (1u << a)) continue;
+                double s = 0.0;
+                for (int j = 0; j < D; j++) s += As[a * D + j] * v[j];
+                if (s - bp[a] < 0) niv |= 1 << a;
+            }
+            for (int j = 0; j < (1 << D); j++) {
+                int sv = niv;
+                for (int k = 0; k < D; k++)
+                    if ((j >> k) & 1) sv |= 1 << c[k];
+                int psv = sv & gmask;
+                if (psv & ptop) psv ^= gmask;
+                if ((PB[psv >> 5] >> (psv & 31)) & 1u) atomicOr(&IS[sv >> 5], 1u << (sv & 31));
+            }
+        }
+        __syncwarp();
+        // pairs (b, ~b): output b with its top bit clear, ascending
+        int count = 0;
+        const int rev = (1 << m) - 1;
+        if (m <= 5) {
+            if (lane == 0) {
+                for (int sv = 0; sv < (1 << (m - 1)); sv++) {
+                    const int pr = sv ^ rev;
+                    if (((IS[sv >> 5] >> (sv & 31)) & 1u) && ((IS[pr >> 5] >> (pr & 31)) & 1u)) {
+                        if (count < cap) out[count] = sv;
+                        count++;
+                    }
+                }
+            }
+            count = __shfl_sync(kFull, count, 0);
+        } else {
+            const int half = mw / 2;
+            for (int w0 = 0; w0 < half; w0 += 32) {
+                const int w = w0 + lane;
+                unsigned bits = 0;
+                if (w < half) bits = IS[w] & __brev(IS[mw - 1 - w]);
+                const int c = __popc(bits);
+                int pre = c;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(kFull, pre, o);
+                    if (lane >= o) pre += y;
+                }
+                const int tot = __shfl_sync(kFull, pre, 31);
+                int pos = count + pre - c;
+                while (bits) {
+                    const int bt = __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    if (pos < cap) out[pos] = w * 32 + bt;
+                    pos++;
+                }
+                count += tot;
+            }
+        }
+        if (lane == 0) {
+            P.B_cnt[i] = count <= cap ? count : cap;
+            if (count > cap) set_err(err, kErrDceOverflow);
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// MU coalignment of one child record (cauchy_term.hpp:533-745), in place.
+template <int D>
+__device__ inline int mu_coalign_rec(TermRecs R, long long s, int MC, int* err)
+{
+    const int m = R.m[s];
+    double* A = R.A + s * MC * D;
+    double* p = R.p + s * MC;
+    double* q = R.q + s * MC;
+    signed char* cmap = R.cmap + s * MC;
+    signed char* csmap = R.csmap + s * MC;
+    unsigned hof = R.horthog[s];
+    // normalize_hps(true): q keeps the un-normalised scales
+    for (int i = 0; i < m; i++) {
+        q[i] = p[i];
+        double n1 = 0;
+        for (int j = 0; j < D; j++) n1 += fabs(A[i * D + j]);
+        p[i] *= n1;
+        for (int j = 0; j < D; j++) A[i * D + j] /= n1;
+    }
+    unsigned F = (m >= 32) ? kFull : ((1u << m) - 1);
+    unsigned hf = hof;
+    for (int j = 0; j < m; j++) {
+        cmap[j] = -1;  // 255 as uint8
+        csmap[j] = 1;
+    }
+    int uc = 0;
+    for (int j = 0; j < m - 1; j++) {
+        if (!((F >> j) & 1u)) continue;
+        cmap[j] = (signed char)uc;
+        for (int k = j + 1; k < m; k++) {
+            if (!((F >> k) & 1u)) continue;
+            const int g = coalign_gate<D>(A + j * D, A + k * D);
+            if (g == 0) continue;
+            const bool hj = (hf >> j) & 1u, hk = (hf >> k) & 1u;
+            if (g == 1) {
+                if (hof) {
+                    if (!hj && !hk) q[j] += q[k];
+                    else if (hj && !hk) {
+                        q[j] = q[k];
+                        hf &= ~(1u << j);
+                    } else if (!hj && hk) hf &= ~(1u << k);
+                    else {
+                        hf &= ~(1u << k);
+                        q[j] += q[k];
+                    }
+                } else
+                    q[j] += q[k];
+                csmap[k] = 1;
+            } else {
+                if (hof) {
+                    if (!hj && !hk) q[j] -= q[k];
+                    else if (hj && !hk) {
+                        q[j] = -q[k];
+                        hf &= ~(1u << j);
+                    } else if (!hj && hk) hf &= ~(1u << k);
+                    else set_err(err, kErrAntiCoalignedHorthog);
+                } else
+                    q[j] -= q[k];
+                csmap[k] = -1;
+            }
+            F &= ~(1u << k);
+            p[j] += p[k];
+            cmap[k] = (signed char)uc;
+        }
+        uc++;
+    }
+    if ((F >> (m - 1)) & 1u) cmap[m - 1] = (signed char)uc;
+    const int ns = __popc(F);
+    if (ns != m) {
+        int u = 1;
+        for (int j = 1; j < m; j++)
+            if ((F >> j) & 1u) {
+                if (u < j) {
+                    for (int l = 0; l < D; l++) A[u * D + l] = A[j * D + l];
+                    p[u] = p[j];
+                    q[u] = q[j];
+                }
+                u++;
+            }
+        if (hof) {
+            unsigned nh = 0;
+            int c = 0;
+            for (int j = 0; j < m; j++)
+                if ((F >> j) & 1u) nh |= ((hf >> j) & 1u) << c++;
+            R.horthog[s] = nh;
+        }
+        R.m[s] = ns;
+        R.flags[s] |= kFlagHasCmap;
+    }
+    return ns;
+}
+
+// Measurement update of every parent (cauchy_term.hpp:84-310), fused with the
+// g/yei evaluation of the parent and its children (cauchy_term.hpp:312-401),
+// the family's moment partial sums (cache_moments, cauchy_estimator.hpp:307),
+// the parent's re-normalisation and the children's MU coalignment.  One warp
+// per parent: lane l < m owns hyperplane l during the update, then lane t
+// owns child t (lane m owns the parent) for evaluation and coalignment.
+template <int D>
+__global__ void k_mu(ParentList P, long long nP, const EstStep<D>* st, const long long* pstart,
+                     const double* roots, Tables Told, int* Bkeys, TermRecs R, long long nR,
+                     const long long* kall_scan, cd* contrib, int MC, int* err)
+{
+    extern __shared__ double smem_d[];
+    constexpr int NM = 1 + D + D * D;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+    double* mu = smem_d + (size_t)wib * ((MC + 1) * D + (MC + 1));
+    double* rho = mu + (MC + 1) * D;
+    for (long long i = (long long)blockIdx.x * nwb + wib; i < nP; i += (long long)gridDim.x * nwb) {
+        const int e = P.est[i];
+        const EstStep<D>& S = st[e];
+        const int m = P.m[i], phc = P.m_old[i];
+        const double* A = P.A + i * MC * D;
+        const double* p = P.p + i * MC;
+        const double* b = P.b + i * D;
+        const double* root = roots + (long long)e * D;
+        bool integ = false, neg = false;
+        if (lane < m) {
+            double h = 0.0;
+            for (int j = 0; j < D; j++) h += S.H[j] * A[lane * D + j];
+            const double ah = fabs(h);
+            if (ah < kMuEps) {
+                for (int j = 0; j < D; j++) mu[lane * D + j] = A[lane * D + j];
+                rho[lane] = p[lane];
+            } else {
+                const double r = 1.0 / h;
+                for (int j = 0; j < D; j++) mu[lane * D + j] = A[lane * D + j] * r;
+                rho[lane] = p[lane] * ah;
+                integ = true;
+                neg = !(h > 0);
+            }
+        } else if (lane == m) {
+            for (int j = 0; j < D; j++) mu[m * D + j] = 0.0;
+            rho[m] = S.gamma;
+        }
+        const unsigned integ_mask = __ballot_sync(kFull, integ);
+        const int esg = (int)__ballot_sync(kFull, neg);
+        double zeta = 0;
+        if (lane == 0) {
+            double hb = 0.0;
+            for (int j = 0; j < D; j++) hb += S.H[j] * b[j];
+            zeta = S.msmt - hb;
+        }
+        zeta = __shfl_sync(kFull, zeta, 0);
+        __syncwarp();
+        int lhp = esg;
+        if (phc < m) lhp &= (1 << phc) - 1;
+        const int esg_c = (esg & (1 << (m - 1))) ? (esg ^ ((1 << m) - 1)) : esg;
+        const bool write = !S.skip;
+        const long long kbase = P.kscan[pstart[e]];
+        const bool mine = (lane < m) ? ((integ_mask >> lane) & 1u) : (lane == m);
+        cd acc[NM];
+        for (int k = 0; k < NM; k++) acc[k] = mkcd(0, 0);
+        if (mine) {
+            const int t = lane;
+            long long slot;
+            if (t == m) slot = i + kbase;
+            else slot = pstart[e + 1] + P.kscan[i] + __popc(integ_mask & ((1u << t) - 1));
+            if (write && slot >= nR) {
+                set_err(err, kErrTableOverflow);
+            } else {
+                double bt[D], ty[D];
+                for (int j = 0; j < D; j++) {
+                    bt[j] = b[j] + zeta * mu[t * D + j];
+                    ty[j] = 0;
+                }
+                double* Ao = write ? R.A + slot * MC * D : nullptr;
+                double* po = write ? R.p + slot * MC : nullptr;
+                unsigned hof = 0;
+                int sneg = 0;
+                double ygi = 0;
+                int l = 0;
+                for (int ll = 0; ll <= m; ll++) {
+                    if (ll == t) continue;
+                    const bool fi = (ll < m) ? ((integ_mask >> ll) & 1u) : true;
+                    double row[D];
+                    if (fi)
+                        for (int j = 0; j < D; j++) row[j] = mu[ll * D + j] - mu[t * D + j];
+                    else {
+                        for (int j = 0; j < D; j++) row[j] = mu[ll * D + j];
+                        hof |= 1u << l;
+                    }
+                    const double pl = rho[ll];
+                    double s = 0.0;
+                    for (int j = 0; j < D; j++) s += row[j] * root[j];
+                    const double sg = s > 0 ? 1.0 : -1.0;
+                    if (sg < 0) sneg |= 1 << l;
+                    const double sc = pl * sg;
+                    for (int j = 0; j < D; j++) ty[j] += sc * row[j];
+                    if (!(hof & (1u << l))) ygi += pl * sg;
+                    if (write) {
+                        for (int j = 0; j < D; j++) Ao[l * D + j] = row[j];
+                        po[l] = pl;
+                    }
+                    l++;
+                }
+                // lambda keys into the parent table (cauchy_term.hpp:357-381)
+                int lp = 0, lm = 0, k = 0;
+                for (int l2 = 0; l2 < m; l2++) {
+                    if (k < phc) {
+                        if (k == t) {
+                            lm |= 1 << k;
+                            k++;
+                            if (k == phc) continue;
+                        }
+                        if ((sneg >> l2) & 1) {
+                            lp |= 1 << k;
+                            lm |= 1 << k;
+                        }
+                        k++;
+                    }
+                }
+                const int* pk = Told.keys + P.tab_off[i];
+                const cd* pv = Told.vals + P.tab_off[i];
+                const int pcnt = P.tab_cnt[i];
+                const cd gp = lookup_num(pk, pv, pcnt, lp ^ lhp, phc);
+                const cd gm = lookup_num(pk, pv, pcnt, lm ^ lhp, phc);
+                const double dv = rho[t];
+                cd g = csub(cdiv(gp, mkcd(ygi + dv, zeta)), cdiv(gm, mkcd(ygi - dv, zeta)));
+                g = cscale(g, kTwoPiInv);
+                acc[0] = g;
+                for (int j = 0; j < D; j++) {
+                    const cd y = mkcd(-ty[j], bt[j]);
+                    const cd gy = cmul(g, y);
+                    acc[1 + j] = gy;
+                    for (int kk = 0; kk < D; kk++) acc[1 + D + j * D + kk] = cmul(gy, mkcd(-ty[kk], bt[kk]));
+                }
+                if (write) {
+                    for (int j = 0; j < D; j++) R.b[slot * D + j] = bt[j];
+                    R.est[slot] = e;
+                    R.m[slot] = m;
+                    R.pbc[slot] = m;
+                    R.phc[slot] = phc;
+                    R.z[slot] = t;
+                    R.lhp[slot] = lhp;
+                    R.fam[slot] = (int)i;
+                    R.horthog[slot] = hof;
+                    R.cval[slot] = zeta;
+                    R.dval[slot] = dv;
+                    R.flags[slot] = (t == m) ? 0 : kFlagNewChild;
+                    if (t == m) {
+                        // parent: normalize_hps(true), no coalignment
+                        double* q = R.q + slot * MC;
+                        for (int r = 0; r < m; r++) {
+                            q[r] = po[r];
+                            double n1 = 0;
+                            for (int j = 0; j < D; j++) n1 += fabs(Ao[r * D + j]);
+                            po[r] *= n1;
+                            for (int j = 0; j < D; j++) Ao[r * D + j] /= n1;
+                        }
+                    } else {
+                        mu_coalign_rec<D>(R, slot, MC, err);
+                    }
+                }
+            }
+        }
+        if (!write && lane == 0) {
+            // a final MU keeps no records; mark the parent's slot empty
+            const long long slot = i + kbase;
+            if (slot < nR) R.est[slot] = -1;
+        }
+        // this term's moment contribution, in the reference's summation order:
+        // the parent first, then its children by hyperplane (cache_moments)
+        if (mine) {
+            const long long pos = i + kall_scan[i] + (lane == m ? 0 : 1 + __popc(integ_mask & ((1u << lane) - 1)));
+            cd* out = contrib + pos * NM;
+            for (int k = 0; k < NM; k++) out[k] = acc[k];
+        }
+        // parent B -> B_mu (cauchy_term.hpp:245-250)
+        if (write) {
+            int* B = Bkeys + P.B_off[i];
+            const int n = P.B_cnt[i];
+            for (int k = lane; k < n; k += 32) B[k] ^= esg_c;
+        }
+        __syncwarp();
+    }
+}
+
+// Per-estimator moment sums, then finalize_cached_moments
+// (cauchy_estimator.hpp:340-357).  The reference accumulates fz, the mean and
+// the covariance in one sequential pass over the terms (parents in order, each
+// followed by its children); the same chain is summed here, one warp per
+// estimator with the lanes over the moment components, so the moments come
+// out bit-identical to the serial reference.
+template <int D>
+__global__ void k_moments(const cd* contrib, const long long* pstart, const long long* kall_scan, int E,
+                          const EstStep<D>* st, cd* est_raw, double* gscale)
+{
+    constexpr int NM = 1 + D + D * D;
+    constexpr int ND = 2 * NM;               // doubles per term
+    constexpr int PER = (ND + 31) / 32;      // doubles per lane
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+    for (int e = blockIdx.x * nwb + wib; e < E; e += gridDim.x * nwb) {
+        if (!st[e].active) continue;
+        const long long a = pstart[e] + kall_scan[pstart[e]];
+        const long long bnd = pstart[e + 1] + kall_scan[pstart[e + 1]];
+        const double* c = reinterpret_cast<const double*>(contrib);
+        double s[PER];
+#pragma unroll
+        for (int u = 0; u < PER; u++) s[u] = 0;
+        for (long long j = a; j < bnd; j++) {
+#pragma unroll
+            for (int u = 0; u < PER; u++) {
+                const int comp = lane + 32 * u;
+                if (comp < ND) s[u] += c[j * ND + comp];
+            }
+        }
+        // gather the totals to lane 0's view through shared memory
+        __shared__ double tot_s[8][ND > 0 ? ND : 1];
+#pragma unroll
+        for (int u = 0; u < PER; u++) {
+            const int comp = lane + 32 * u;
+            if (comp < ND) tot_s[wib][comp] = s[u];
+        }
+        __syncwarp();
+        if (lane == 0) {
+            const double* t = tot_s[wib];
+            const cd fz = mkcd(t[0], t[1]);
+            gscale[e] = kTwoPiInv / fz.re;
+            const cd ifz = mkcd(0, fz.re);
+            cd* out = est_raw + (long long)e * NM;
+            out[0] = fz;
+            cd mfin[D];
+            for (int j = 0; j < D; j++) {
+                mfin[j] = cdiv(mkcd(t[2 * (1 + j)], t[2 * (1 + j) + 1]), ifz);
+                out[1 + j] = mfin[j];
+            }
+            // the covariance is accumulated as cov -= (g y_j) y_k, i.e. minus the chain
+            for (int j = 0; j < D; j++)
+                for (int k = 0; k < D; k++) {
+                    const int q = 2 * (1 + D + j * D + k);
+                    const cd cv = mkcd(-t[q], -t[q + 1]);
+                    out[1 + D + j * D + k] = csub(cdiv(cv, fz), cmul(mfin[j], mfin[k]));
+                }
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Fast term reduction.  The reference sorts b along each axis and, for each
+// not-yet-reduced term i in index order, takes every later unreduced term j
+// with qp-eps < b_j <= qp+eps on all axes (qp = b_i), |p_j - p_i| <= eps and
+// the hyperplane test, and reduces it into i (term_reduction.hpp:159-276).
+// Here candidate pairs come from a hash grid over (estimator, shape, cell of
+// b[0] at width 2 eps); the greedy index-order resolution is reproduced by
+// ftr_resolve.
+__device__ inline unsigned long long mix64(unsigned long long x)
+{
+    x ^= x >> 30;
+    x *= 0xbf58476d1ce4e5b9ull;
+    x ^= x >> 27;
+    x *= 0x94d049bb133111ebull;
+    x ^= x >> 31;
+    return x;
+}
+__device__ inline long long cell_of(double v)
+{
+    double q = floor(v / (2.0 * kReductionEps));
+    if (!(q > -4.0e18)) q = -4.0e18;  // also catches NaN
+    if (q > 4.0e18) q = 4.0e18;
+    return (long long)q;
+}
+__device__ inline long long cell_slot(int e, int m, long long q, long long hmask)
+{
+    unsigned long long h = mix64((unsigned long long)q * 0x9e3779b97f4a7c15ull ^ ((unsigned long long)e << 8) ^
+                                 (unsigned long long)m);
+    return (long long)(h & (unsigned long long)hmask);
+}
+
+template <int D>
+__global__ void k_ftr_insert(TermRecs R, long long nR, long long* cellq, int* head, int* next, long long hmask)
+{
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nR; j += (long long)gridDim.x * blockDim.x) {
+        const int e = R.est[j];
+        if (e < 0) {
+            next[j] = -1;
+            continue;
+        }
+        const long long q = cell_of(R.b[j * D]);
+        cellq[j] = q;
+        const long long s = cell_slot(e, R.m[j], q, hmask);
+        next[j] = atomicExch(&head[s], (int)j);
+    }
+}
+
+template <int D>
+__device__ inline bool ftr_near(const TermRecs& R, long long i, long long j, int m, int MC)
+{
+    const double* bi = R.b + i * D;
+    const double* bj = R.b + j * D;
+    for (int a = 0; a < D; a++) {
+        const double lo = bi[a] - kReductionEps, hi = bi[a] + kReductionEps;
+        if (!(bj[a] > lo && bj[a] <= hi)) return false;
+    }
+    const double* pi = R.p + i * MC;
+    const double* pj = R.p + j * MC;
+    for (int k = 0; k < m; k++)
+        if (fabs(pj[k] - pi[k]) > kReductionEps) return false;
+    // the reference compares Ai[k] with Aj[k] for k < m inside its per-component
+    // loop (term_reduction.hpp:237-244), i.e. the first m entries of row-major A
+    const double* Ai = R.A + i * MC * D;
+    const double* Aj = R.A + j * MC * D;
+    for (int k = 0; k < m; k++) {
+        const double r = Ai[k], c = Aj[k];
+        if (!(fabs(r - c) < kReductionEps || fabs(r + c) < kReductionEps)) return false;
+    }
+    return true;
+}
+
+template <int D>
+__global__ void k_ftr_preds(TermRecs R, long long nR, const long long* cellq, const int* head, const int* next,
+                            long long hmask, int MC, const long long* pred_off, int* preds, int* npred)
+{
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nR; j += (long long)gridDim.x * blockDim.x) {
+        const int e = R.est[j];
+        int c = 0;
+        if (e >= 0) {
+            const int m = R.m[j];
+            const long long qj = cellq[j];
+            for (int dq = -1; dq <= 1; dq++) {
+                const long long qq = qj + dq;
+                const long long s = cell_slot(e, m, qq, hmask);
+                long long guard = 0;
+                for (int i = head[s]; i >= 0 && guard <= nR; i = next[i], guard++) {
+                    if (i >= j) continue;
+                    if (cellq[i] != qq || R.est[i] != e || R.m[i] != m) continue;
+                    if (!ftr_near<D>(R, i, j, m, MC)) continue;
+                    if (preds) preds[pred_off[j] + c] = i;
+                    c++;
+                }
+            }
+        }
+        if (!preds) npred[j] = c;
+    }
+}
+
+#if MCE_COMMON_UNIT
+__global__ void k_ftr_resolve(const long long* pred_off, const int* preds, long long nR, int* status, int* owner,
+                              int* unknown)
+{
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nR; j += (long long)gridDim.x * blockDim.x) {
+        if (status[j] != 0) continue;
+        int best = INT_MAX, minu = INT_MAX;
+        for (long long k = pred_off[j]; k < pred_off[j + 1]; k++) {
+            const int i = preds[k];
+            const int s = ((volatile int*)status)[i];
+            if (s == 1) best = i < best ? i : best;
+            else if (s == 0) minu = i < minu ? i : minu;
+        }
+        if (best < minu) {
+            owner[j] = best;
+            ((volatile int*)status)[j] = 2;
+        } else if (minu == INT_MAX) {
+            owner[j] = (int)j;
+            ((volatile int*)status)[j] = 1;
+        } else
+            atomicAdd(unknown, 1);
+    }
+}
+
+__global__ void k_group_count(const int* status, const int* owner, long long nR, int* gcnt)
+{
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nR; j += (long long)gridDim.x * blockDim.x)
+        if (status[j] == 2) atomicAdd(&gcnt[owner[j]], 1);
+}
+
+__global__ void k_group_fill(const int* status, const int* owner, long long nR, const long long* goff, int* gfill,
+                             int* members)
+{
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nR; j += (long long)gridDim.x * blockDim.x)
+        if (status[j] == 2) {
+            const int r = owner[j];
+            const int k = atomicAdd(&gfill[r], 1);
+            members[goff[r] + k] = (int)j;
+        }
+}
+
+__global__ void k_group_sort(const int* gcnt, const long long* goff, long long nR, int* members)
+{
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < nR; r += (long long)gridDim.x * blockDim.x) {
+        const int n = gcnt[r];
+        if (n < 2) continue;
+        int* a = members + goff[r];
+        for (int x = 1; x < n; x++) {
+            const int v = a[x];
+            int y = x - 1;
+            while (y >= 0 && a[y] > v) {
+                a[y + 1] = a[y];
+                y--;
+            }
+            a[y + 1] = v;
+        }
+    }
+}
+
+__global__ void k_roots_flags(const int* status, const int* m, long long nR, int D, int* is_root, int* cap)
+{
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nR; j += (long long)gridDim.x * blockDim.x) {
+        const bool r = status[j] == 1;
+        is_root[j] = r ? 1 : 0;
+        cap[j] = r ? half_cells_cap(m[j], D) : 0;
+    }
+}
+
+__global__ void k_roots_list(const int* is_root, const long long* rscan, long long nR, int* list)
+{
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nR; j += (long long)gridDim.x * blockDim.x)
+        if (is_root[j]) list[rscan[j]] = (int)j;
+}
+
+#endif  // MCE_COMMON_UNIT
+
+// ---------------------------------------------------------------------------
+// g-table construction per reduction group (flattening.hpp:77-568).
+
+struct GCtx {
+    TermRecs R;
+    ParentList P;
+    Tables Told;
+    const int* Bkeys;
+    int MC;
+};
+
+// One cell of make_gtable (flattening.hpp:105-224) for record s at `key`.
+template <int D>
+__device__ inline cd g_cell(const GCtx& c, long long s, int key, double gscale)
+{
+    const TermRecs& R = c.R;
+    const int MC = c.MC;
+    const int m = R.m[s], phc = R.phc[s], flags = R.flags[s];
+    const unsigned hof = R.horthog[s];
+    const double* q = R.q + s * MC;
+    double ygi = 0;
+    for (int k = 0; k < m; k++) {
+        const double sk = ((key >> k) & 1) ? -1.0 : 1.0;
+        if (!(hof & (1u << k))) ygi += q[k] * sk;
+    }
+    int lp = 0, lm = 0;
+    if (!(flags & kFlagNewChild)) {
+        lp = key & ((1 << phc) - 1);
+        lm = lp;
+    } else {
+        const int z = R.z[s];
+        const signed char* cmap = R.cmap + s * MC;
+        const signed char* csmap = R.csmap + s * MC;
+        const bool hc = flags & kFlagHasCmap;
+        int k = 0, l = 0;
+        while (k < phc) {
+            if (k == z) {
+                lm |= 1 << k;
+                k++;
+                if (k == phc) break;
+            }
+            int neg;
+            if (hc) {
+                const int ci = (unsigned char)cmap[l];
+                const int bv = (((key >> ci) & 1) ? -1 : 1) * (int)csmap[l];
+                neg = bv < 0;
+            } else
+                neg = (key >> l) & 1;
+            if (neg) {
+                lp |= 1 << k;
+                lm |= 1 << k;
+            }
+            k++;
+            l++;
+        }
+    }
+    const int fam = R.fam[s];
+    const int* pk = c.Told.keys + c.P.tab_off[fam];
+    const cd* pv = c.Told.vals + c.P.tab_off[fam];
+    const int pcnt = c.P.tab_cnt[fam];
+    const int lhp = R.lhp[s];
+    const cd gp = lookup_num(pk, pv, pcnt, lp ^ lhp, phc);
+    const cd gm = lookup_num(pk, pv, pcnt, lm ^ lhp, phc);
+    const double dv = R.dval[s], cv = R.cval[s];
+    cd v = csub(cdiv(gp, mkcd(ygi + dv, cv)), cdiv(gm, mkcd(ygi - dv, cv)));
+    return cscale(v, gscale);
+}
+
+__device__ inline bool bm_get(const unsigned* bm, int k) { return (bm[k >> 5] >> (k & 31)) & 1u; }
+
+// Extracts the set bits of a 2^m-bit bitmap in ascending order into out[]; returns the count.
+__device__ inline int bm_extract(const unsigned* bm, int m, int* out, int cap, int lane)
+{
+    const int nb = 1 << m;
+    const int words = nb > 32 ? nb / 32 : 1;
+    int count = 0;
+    for (int w0 = 0; w0 < words; w0 += 32) {
+        const int w = w0 + lane;
+        unsigned bits = w < words ? bm[w] : 0u;
+        if (nb < 32) bits &= (1u << nb) - 1;
+        const int c = __popc(bits);
+        int pre = c;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(kFull, pre, o);
+            if (lane >= o) pre += y;
+        }
+        const int tot = __shfl_sync(kFull, pre, 31);
+        int pos = count + pre - c;
+        while (bits) {
+            const int b = __ffs(bits) - 1;
+            bits &= bits - 1;
+            if (pos < cap) out[pos] = w * 32 + b;
+            pos++;
+        }
+        count += tot;
+    }
+    return count;
+}
+
+__device__ inline double p_sum_sq(const double* p, int m)
+{
+    double s = 0;
+    for (int k = 0; k < m; k++) s += p[k];
+    return s * s;
+}
+
+// Root cells of a new child: make_new_child_btable (cell_enumeration.hpp:206-371)
+// into the bitmap RK (2^m bits).  PB receives the parent's B_mu as a bitmap.
+template <int D>
+__device__ inline void new_child_cells(const GCtx& c, long long s, unsigned* RK, unsigned* PB, int* bmk, int lane)
+{
+    const TermRecs& R = c.R;
+    const int m = R.m[s];
+    const int words_m = (1 << m) > 32 ? (1 << m) / 32 : 1;
+    for (int k = lane; k < words_m; k += 32) RK[k] = 0;
+    if (m <= D) {
+        __syncwarp();
+        for (int k = lane; k < (1 << (m - 1)); k += 32) atomicOr(&RK[k >> 5], 1u << (k & 31));
+        __syncwarp();
+        return;
+    }
+    const int fam = R.fam[s];
+    const int* Bmu = c.Bkeys + c.P.B_off[fam];
+    const int nB = c.P.B_cnt[fam];
+    const int pbc = R.pbc[s], z = R.z[s];
+    const int words_p = (1 << pbc) > 32 ? (1 << pbc) / 32 : 1;
+    for (int k = lane; k < words_p; k += 32) PB[k] = 0;
+    const bool coal = m < pbc;
+    if (coal && lane == 0) {
+        // first original row of every coaligned group (cell_enumeration.hpp:318-331)
+        unsigned seen = 0;
+        int cnt = 0;
+        const signed char* cmap = R.cmap + s * c.MC;
+        for (int j = 0; j < pbc; j++) {
+            const int ci = (unsigned char)cmap[j];
+            if (ci < 32 && !((seen >> ci) & 1u)) {
+                seen |= 1u << ci;
+                bmk[cnt++] = j;
+            }
+        }
+        bmk[31] = cnt;
+    }
+    __syncwarp();
+    for (int k = lane; k < nB; k += 32) {
+        const int key = Bmu[k];
+        if (key >= 0 && key < (1 << pbc)) atomicOr(&PB[key >> 5], 1u << (key & 31));
+    }
+    __syncwarp();
+    const int ncoal = coal ? bmk[31] : 0;
+    const int mz = 1 << z, hb = 1 << (pbc - 1), rev = (1 << pbc) - 1;
+    for (int k = lane; k < nB; k += 32) {
+        const int b = Bmu[k];
+        int bq = b ^ mz;
+        if (bq & hb) bq ^= rev;
+        if (bq < 0 || bq >= (1 << pbc) || !bm_get(PB, bq)) continue;
+        const int zb = (b & mz) >> z;
+        const int c1 = ((b >> (z + 1)) << z) | (b & (mz - 1)) | (zb << (pbc - 1));
+        const int c2 = c1 ^ hb;
+        int out[2] = {(c1 & hb) ? (c1 ^ rev) : c1, (c2 & hb) ? (c2 ^ rev) : c2};
+        for (int u = 0; u < 2; u++) {
+            int key = out[u];
+            if (coal) {
+                int bc = 0;
+                for (int l = 0; l < ncoal; l++)
+                    if (key & (1 << bmk[l])) bc |= 1 << l;
+                key = bc;
+            }
+            if (key >= 0 && key < (1 << m)) atomicOr(&RK[key >> 5], 1u << (key & 31));
+        }
+    }
+    __syncwarp();
+}
+
+template <int D>
+__device__ inline void own_cells(const GCtx& c, long long s, unsigned* bm, int lane)
+{
+    const int m = c.R.m[s];
+    const int words_m = (1 << m) > 32 ? (1 << m) / 32 : 1;
+    for (int k = lane; k < words_m; k += 32) bm[k] = 0;
+    __syncwarp();
+    const int fam = c.R.fam[s];
+    const int* B = c.Bkeys + c.P.B_off[fam];
+    const int n = c.P.B_cnt[fam];
+    for (int k = lane; k < n; k += 32) {
+        const int key = B[k];
+        if (key >= 0 && key < (1 << m)) atomicOr(&bm[key >> 5], 1u << (key & 31));
+    }
+    __syncwarp();
+}
+
+template <int D>
+__global__ void k_gtable(GCtx c, const int* roots_list, long long nroots, const int* gcnt, const long long* goff,
+                         const int* members, const double* gscale_e, const long long* toff, Tables Tnew, int* tcnt,
+                         int* alive, int* src, cd* scratch, long long scratch_per_warp, int* err)
+{
+    extern __shared__ unsigned smem_g[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+    const int MC = c.MC;
+    const int words = (1 << MC) > 32 ? (1 << MC) / 32 : 1;
+    const int capMC = half_cells_cap(MC, D);
+    unsigned* PB = smem_g + (size_t)wib * (3 * words + 32 + capMC);
+    unsigned* RK = PB + words;
+    unsigned* OK = RK + words;
+    int* bmk = reinterpret_cast<int*>(OK + words);
+    int* RKL = bmk + 32;
+    const long long gw = (long long)blockIdx.x * nwb + wib;
+    cd* scr = scratch + gw * scratch_per_warp;
+    const TermRecs& R = c.R;
+    for (long long ri = gw; ri < nroots; ri += (long long)gridDim.x * nwb) {
+        const long long r = roots_list[ri];
+        const int m = R.m[r];
+        const int e = R.est[r];
+        const double gs = gscale_e[e];
+        const int top = 1 << (m - 1), rev = (1 << m) - 1;
+        const long long out_off = toff[r];
+        const int cap = (int)(toff[r + 1] - toff[r]);
+        int* okeys = Tnew.keys + out_off;
+        cd* ovals = Tnew.vals + out_off;
+        // ---- root cells
+        if (R.flags[r] & kFlagNewChild) new_child_cells<D>(c, r, RK, PB, bmk, lane);
+        else own_cells<D>(c, r, RK, lane);
+        int nR = bm_extract(RK, m, RKL, capMC, lane);
+        __syncwarp();
+        if (nR > cap || nR > capMC) {
+            if (lane == 0) set_err(err, kErrTableOverflow);
+            nR = cap < capMC ? cap : capMC;
+        }
+        long long root = r;
+        // ---- root values and the term-approximation test (flattening.hpp:242-247)
+        double ps2 = p_sum_sq(R.p + root * MC, m);
+        bool negl = true;
+        for (int k = lane; k < nR; k += 32) {
+            const cd v = g_cell<D>(c, root, RKL[k], gs);
+            okeys[k] = RKL[k];
+            ovals[k] = v;
+            if (ps2 * hypot(v.re, v.im) > kTermApproxEps) negl = false;
+        }
+        negl = __all_sync(kFull, negl);
+        const int nmem = gcnt[r];
+        const int* mem = members + goff[r];
+        int kidx = 0;
+        if (negl) {
+            // the root is approximated out: the first member that is not
+            // becomes the root, with the group's cells carried along
+            // (flattening.hpp:412-489)
+            root = -1;
+            long long alfr = r;
+            while (kidx < nmem) {
+                const long long cm = mem[kidx++];
+                if (R.flags[cm] & kFlagNewChild) {
+                    int sg = 0;
+                    if (lane == 0) {
+                        sg = orientation_mask<D>(R.A + alfr * MC * D, R.A + cm * MC * D, m);
+                        if (sg & top) sg ^= rev;
+                    }
+                    sg = __shfl_sync(kFull, sg, 0);
+                    // re-orient the group's cell list into RK and re-sort
+                    for (int k = lane; k < words; k += 32) RK[k] = 0;
+                    __syncwarp();
+                    for (int k = lane; k < nR; k += 32) {
+                        const int key = RKL[k] ^ sg;
+                        if (key >= 0 && key < (1 << m)) atomicOr(&RK[key >> 5], 1u << (key & 31));
+                    }
+                    __syncwarp();
+                    nR = bm_extract(RK, m, RKL, capMC, lane);
+                } else {
+                    own_cells<D>(c, cm, RK, lane);
+                    nR = bm_extract(RK, m, RKL, capMC, lane);
+                }
+                __syncwarp();
+                if (nR > cap) {
+                    if (lane == 0) set_err(err, kErrTableOverflow);
+                    nR = cap;
+                }
+                const double ps2c = p_sum_sq(R.p + cm * MC, m);
+                bool ng = true;
+                for (int k = lane; k < nR; k += 32) {
+                    const cd v = g_cell<D>(c, cm, RKL[k], gs);
+                    okeys[k] = RKL[k];
+                    ovals[k] = v;
+                    if (ps2c * hypot(v.re, v.im) > kTermApproxEps) ng = false;
+                }
+                ng = __all_sync(kFull, ng);
+                if (!ng) {
+                    root = cm;
+                    break;
+                }
+                alfr = cm;
+            }
+        }
+        if (root < 0) {
+            if (lane == 0) {
+                alive[r] = 0;
+                tcnt[r] = 0;
+            }
+            __syncwarp();
+            continue;
+        }
+        // RK holds the root's cells as a bitmap, RKL as a sorted list
+        // ---- members: make_gtable + add_gtables (flattening.hpp:493-552)
+        for (; kidx < nmem; kidx++) {
+            const long long cm = mem[kidx];
+            const bool newc = R.flags[cm] & kFlagNewChild;
+            bool own = false;
+            if (!newc) own = c.P.B_cnt[R.fam[cm]] == nR;
+            int sig = 0;
+            if (lane == 0) sig = orientation_mask<D>(R.A + root * MC * D, R.A + cm * MC * D, m);
+            sig = __shfl_sync(kFull, sig, 0);
+            const int sigf = (sig & top) ? (sig ^ rev) : sig;
+            const double ps2c = p_sum_sq(R.p + cm * MC, m);
+            bool ng = true;
+            if (!own) {
+                for (int k = lane; k < nR; k += 32) {
+                    const cd v = g_cell<D>(c, cm, RKL[k] ^ sigf, gs);
+                    scr[k] = v;
+                    if (ps2c * hypot(v.re, v.im) > kTermApproxEps) ng = false;
+                }
+                ng = __all_sync(kFull, ng);
+                if (!ng)
+                    for (int k = lane; k < nR; k += 32) {
+                        const int bi = RKL[k];
+                        const int t = bi ^ sig;
+                        const bool cj = t & top;
+                        const int bj = cj ? (t ^ rev) : t;
+                        cd v;
+                        if (bj == (bi ^ sigf)) v = scr[k];
+                        else if (bm_get(RK, bj ^ sigf)) v = g_cell<D>(c, cm, bj, gs);
+                        else continue;
+                        const cd a = ovals[k];
+                        ovals[k] = cadd(a, cj ? cconj(v) : v);
+                    }
+            } else {
+                own_cells<D>(c, cm, OK, lane);
+                const int fam = R.fam[cm];
+                const int* B = c.Bkeys + c.P.B_off[fam];
+                const int n = c.P.B_cnt[fam];
+                for (int k = lane; k < n; k += 32) {
+                    const cd v = g_cell<D>(c, cm, B[k], gs);
+                    if (ps2c * hypot(v.re, v.im) > kTermApproxEps) ng = false;
+                }
+                ng = __all_sync(kFull, ng);
+                if (!ng)
+                    for (int k = lane; k < nR; k += 32) {
+                        const int bi = RKL[k];
+                        const int t = bi ^ sig;
+                        const bool cj = t & top;
+                        const int bj = cj ? (t ^ rev) : t;
+                        if (bj < 0 || bj >= (1 << m) || !bm_get(OK, bj)) continue;
+                        const cd v = g_cell<D>(c, cm, bj, gs);
+                        const cd a = ovals[k];
+                        ovals[k] = cadd(a, cj ? cconj(v) : v);
+                    }
+            }
+            __syncwarp();
+        }
+        if (lane == 0) {
+            alive[r] = 1;
+            tcnt[r] = nR;
+            src[r] = (int)root;
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Next parent list: per estimator, surviving roots bucketed by shape in
+// position order (cauchy_estimator.hpp:1059-1101 keeps roots in index order
+// within each shape; shapes ascend).
+
+#if MCE_COMMON_UNIT
+__global__ void k_partition_count(const int* alive, const int* est, const int* m, long long nR, int MCp, int* hist)
+{
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nR; j += (long long)gridDim.x * blockDim.x)
+        if (alive[j]) atomicAdd(&hist[(long long)est[j] * MCp + m[j]], 1);
+}
+
+__global__ void k_partition_rank(const int* alive, const int* m, const long long* rbase, int E, int MCp,
+                                 const long long* bucket_off, int* new_slot)
+{
+    __shared__ long long running[33];
+    __shared__ int wcnt[8][33];
+    __shared__ int total[33];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int e = blockIdx.x; e < E; e += gridDim.x) {
+        if (threadIdx.x < MCp) running[threadIdx.x] = bucket_off[(long long)e * MCp + threadIdx.x];
+        for (int k = threadIdx.x; k < 8 * 33; k += blockDim.x) wcnt[k / 33][k % 33] = 0;
+        __syncthreads();
+        const long long a = rbase[e], bnd = rbase[e + 1];
+        for (long long base = a; base < bnd; base += blockDim.x) {
+            const long long j = base + threadIdx.x;
+            const int key = (j < bnd && alive[j]) ? m[j] : -1;
+            const unsigned mask = __match_any_sync(kFull, key);
+            const int rank = __popc(mask & ((1u << lane) - 1));
+            const int leader = __ffs(mask) - 1;
+            if (key >= 0 && lane == leader) wcnt[w][key] = __popc(mask);
+            __syncthreads();
+            if (threadIdx.x < MCp) {
+                int acc = 0;
+                for (int ww = 0; ww < (int)(blockDim.x >> 5); ww++) {
+                    const int t = wcnt[ww][threadIdx.x];
+                    wcnt[ww][threadIdx.x] = acc;
+                    acc += t;
+                }
+                total[threadIdx.x] = acc;
+            }
+            __syncthreads();
+            if (key >= 0) new_slot[j] = (int)(running[key] + wcnt[w][key] + rank);
+            __syncthreads();
+            if (threadIdx.x < MCp) {
+                running[threadIdx.x] += total[threadIdx.x];
+                for (int ww = 0; ww < (int)(blockDim.x >> 5); ww++) wcnt[ww][threadIdx.x] = 0;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+#endif  // MCE_COMMON_UNIT
+
+template <int D>
+__global__ void k_compact(TermRecs R, const int* alive, const int* src, long long nR, const int* new_slot,
+                          const long long* toff, const int* tcnt, ParentList Pn, int MC)
+{
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nR; j += (long long)gridDim.x * blockDim.x) {
+        if (!alive[j]) continue;
+        const long long s = src[j];
+        const long long o = new_slot[j];
+        const int m = R.m[s];
+        Pn.est[o] = R.est[s];
+        Pn.m[o] = m;
+        for (int k = 0; k < m * D; k++) Pn.A[o * MC * D + k] = R.A[s * MC * D + k];
+        for (int k = 0; k < m; k++) Pn.p[o * MC + k] = R.p[s * MC + k];
+        for (int k = 0; k < D; k++) Pn.b[o * D + k] = R.b[s * D + k];
+        Pn.tab_off[o] = toff[j];
+        Pn.tab_cnt[o] = tcnt[j];
+    }
+}
+
+#if MCE_COMMON_UNIT
+__global__ void k_rbase(const long long* pstart, const long long* kscan, int E, long long* rbase)
+{
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e <= E; e += gridDim.x * blockDim.x)
+        rbase[e] = pstart[e] + kscan[pstart[e]];
+}
+
+#endif  // MCE_COMMON_UNIT
+
+// ---------------------------------------------------------------------------
+// Launchers
+
+template <int D>
+void Kernels<D>::first_count(const double* A0, const EstStep<D>* st, int E, int* cnt, const LaunchCfg& c)
+{
+    k_first_count<D><<<(E + 127) / 128, 128, 0, c.stream>>>(A0, st, E, cnt);
+}
+
+template <int D>
+void Kernels<D>::first_build(const double* A0, const double* p0, const double* b0, const EstStep<D>* st,
+                             const double* roots, int E, const long long* pstart, ParentList P, int MC, cd* est_raw,
+                             const LaunchCfg& c)
+{
+    // c_val, d_val and the H-orthogonal flags of the first terms ride in
+    // spare parent-list arrays until the first tables are built.
+    k_first_build<D><<<(E + 63) / 64, 64, 0, c.stream>>>(A0, p0, b0, st, roots, E, pstart, P, MC,
+                                                         reinterpret_cast<double*>(P.kscan),
+                                                         reinterpret_cast<double*>(P.B_off),
+                                                         reinterpret_cast<unsigned*>(P.nkids), est_raw);
+}
+
+template <int D>
+void Kernels<D>::first_tables(ParentList P, long long nP, const double* cval, const double* dval, const unsigned* hof,
+                              const double* gscale, Tables T, int MC, const LaunchCfg& c)
+{
+    const long long n = nP << (D - 1);
+    k_first_tables<D><<<grid_for(n, 256, c.num_sms), 256, 0, c.stream>>>(P, nP, cval, dval, hof, gscale, T, MC);
+}
+
+template <int D>
+void Kernels<D>::tp(ParentList P, long long nP, const EstStep<D>* st, int with_tp, int MC, int* Bcap, int* err,
+                    const LaunchCfg& c)
+{
+    if (nP == 0) return;
+    k_tp<D><<<grid_for(nP, 128, c.num_sms), 128, 0, c.stream>>>(P, nP, st, with_tp, MC, Bcap, err);
+}
+
+static inline size_t build_B_smem_per_warp(int MC, int D)
+{
+    const int words = (1 << MC) > 32 ? (1 << MC) / 32 : 1;
+    const int u32 = 2 * words + 2 * MC * D + 2;
+    return (size_t)((u32 + 1) & ~1) * 4;
+}
+
+template <int D>
+void Kernels<D>::build_B(ParentList P, long long nP, const EstStep<D>* st, int with_tp, Tables Told, int* Bkeys,
+                         long long Bcap_total, const double* bpert, int MC, const int* combo_off,
+                         const unsigned char* combos, int* err, const LaunchCfg& c)
+{
+    (void)Bcap_total;
+    if (nP == 0) return;
+    const size_t pw = build_B_smem_per_warp(MC, D);
+    int warps = (int)(96 * 1024 / pw);
+    if (warps > 8) warps = 8;
+    if (warps < 1) warps = 1;
+    const size_t sm = pw * warps;
+    cudaFuncSetAttribute(k_build_B<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_build_B<D><<<grid_for(nP, warps, c.num_sms, 8), warps * 32, sm, c.stream>>>(
+        P, nP, st, with_tp, Told, Bkeys, bpert, MC, combo_off, combos, err);
+}
+
+template <int D>
+void Kernels<D>::mu(ParentList P, long long nP, const EstStep<D>* st, const long long* pstart, const double* roots,
+                    Tables Told, int* Bkeys, TermRecs R, long long nR, const long long* kall_scan, cd* contrib,
+                    int MC, int* err, const LaunchCfg& c)
+{
+    if (nP == 0) return;
+    const int warps = 4;
+    const size_t sm = (size_t)warps * ((MC + 1) * D + (MC + 1)) * sizeof(double);
+    k_mu<D><<<grid_for(nP, warps, c.num_sms, 16), warps * 32, sm, c.stream>>>(P, nP, st, pstart, roots, Told,
+                                                                              Bkeys, R, nR, kall_scan, contrib, MC,
+                                                                              err);
+}
+
+template <int D>
+void Kernels<D>::moments(const cd* contrib, const long long* pstart, const long long* kall_scan, int E,
+                         const EstStep<D>* st, cd* est_raw, double* gscale, const LaunchCfg& c)
+{
+    const int warps = 8;
+    int g = (E + warps - 1) / warps;
+    if (g > c.num_sms * 8) g = c.num_sms * 8;
+    if (g < 1) g = 1;
+    k_moments<D><<<g, warps * 32, 0, c.stream>>>(contrib, pstart, kall_scan, E, st, est_raw, gscale);
+}
+
+template <int D>
+void Kernels<D>::ftr_insert(TermRecs R, long long nR, long long* cellq, int* head, int* next, long long hmask,
+                            const LaunchCfg& c)
+{
+    if (nR == 0) return;
+    k_ftr_insert<D><<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(R, nR, cellq, head, next, hmask);
+}
+
+template <int D>
+void Kernels<D>::ftr_preds(TermRecs R, long long nR, const long long* cellq, const int* head, const int* next,
+                           long long hmask, int MC, const long long* pred_off, int* preds, int* npred,
+                           const LaunchCfg& c)
+{
+    if (nR == 0) return;
+    k_ftr_preds<D><<<grid_for(nR, 128, c.num_sms), 128, 0, c.stream>>>(R, nR, cellq, head, next, hmask, MC,
+                                                                       pred_off, preds, npred);
+}
+
+static inline size_t gtable_smem_per_warp(int MC, int D)
+{
+    const int words = (1 << MC) > 32 ? (1 << MC) / 32 : 1;
+    const int capMC = half_cells_cap(MC, D);
+    return (size_t)(3 * words + 32 + capMC) * 4;
+}
+
+template <int D>
+void Kernels<D>::gtable(TermRecs R, const int* roots_list, long long nroots, const int* gcnt, const long long* goff,
+                        const int* members, ParentList P, Tables Told, const int* Bkeys, const double* gscale,
+                        const long long* toff, Tables Tnew, int* tcnt, int* alive, int* src, cd* scratch,
+                        long long scratch_per_warp, int MC, int* err, const LaunchCfg& c)
+{
+    if (nroots == 0) return;
+    GCtx ctx{R, P, Told, Bkeys, MC};
+    const size_t pw = gtable_smem_per_warp(MC, D);
+    int warps = (int)(96 * 1024 / pw);
+    if (warps > 4) warps = 4;
+    if (warps < 1) warps = 1;
+    const size_t sm = pw * warps;
+    cudaFuncSetAttribute(k_gtable<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    const int grid = grid_for(nroots, warps, c.num_sms, 16);
+    k_gtable<D><<<grid, warps * 32, sm, c.stream>>>(ctx, roots_list, nroots, gcnt, goff, members, gscale, toff, Tnew,
+                                                    tcnt, alive, src, scratch, scratch_per_warp, err);
+}
+
+template <int D>
+void Kernels<D>::compact(TermRecs R, const int* alive, const int* src, long long nR, const int* new_slot,
+                         const long long* toff, const int* tcnt, ParentList Pn, int MC, const LaunchCfg& c)
+{
+    if (nR == 0) return;
+    k_compact<D><<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(R, alive, src, nR, new_slot, toff, tcnt, Pn, MC);
+}
+
+#if MCE_COMMON_UNIT
+void ftr_resolve(const long long* pred_off, const int* preds, long long nR, int* status, int* owner, int* unknown,
+                 const LaunchCfg& c)
+{
+    if (nR == 0) return;
+    k_ftr_resolve<<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(pred_off, preds, nR, status, owner, unknown);
+}
+void group_count(const int* status, const int* owner, long long nR, int* gcnt, const LaunchCfg& c)
+{
+    if (nR == 0) return;
+    k_group_count<<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(status, owner, nR, gcnt);
+}
+void group_fill(const int* status, const int* owner, long long nR, const long long* goff, int* gfill, int* members,
+                const LaunchCfg& c)
+{
+    if (nR == 0) return;
+    k_group_fill<<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(status, owner, nR, goff, gfill, members);
+}
+void group_sort(const int* gcnt, const long long* goff, long long nR, int* members, const LaunchCfg& c)
+{
+    if (nR == 0) return;
+    k_group_sort<<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(gcnt, goff, nR, members);
+}
+void roots_flags(const int* status, const int* m, long long nR, int D, int* is_root, int* cap, const LaunchCfg& c)
+{
+    if (nR == 0) return;
+    k_roots_flags<<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(status, m, nR, D, is_root, cap);
+}
+void roots_list(const int* is_root, const long long* rscan, long long nR, int* list, const LaunchCfg& c)
+{
+    if (nR == 0) return;
+    k_roots_list<<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(is_root, rscan, nR, list);
+}
+void partition_count(const int* alive, const int* est, const int* m, long long nR, int MCp, int* hist,
+                     const LaunchCfg& c)
+{
+    if (nR == 0) return;
+    k_partition_count<<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(alive, est, m, nR, MCp, hist);
+}
+void partition_rank(const int* alive, const int* m, const long long* rbase, int E, int MCp,
+                    const long long* bucket_off, int* new_slot, const LaunchCfg& c)
+{
+    int g = E < c.num_sms * 8 ? E : c.num_sms * 8;
+    if (g < 1) g = 1;
+    k_partition_rank<<<g, 256, 0, c.stream>>>(alive, m, rbase, E, MCp, bucket_off, new_slot);
+}
+void rbase_kernel(const long long* pstart, const long long* kscan, int E, long long* rbase, const LaunchCfg& c)
+{
+    k_rbase<<<(E + 1 + 255) / 256, 256, 0, c.stream>>>(pstart, kscan, E, rbase);
+}
+
+#endif  // MCE_COMMON_UNIT
+
+#if MCE_ONLY_DIM > 0
+template struct Kernels<MCE_ONLY_DIM>;
+#elif MCE_ONLY_DIM < 0
+template struct Kernels<1>;
+template struct Kernels<2>;
+template struct Kernels<3>;
+template struct Kernels<4>;
+template struct Kernels<5>;
+template struct Kernels<6>;
+template struct Kernels<7>;
+template struct Kernels<8>;
+#endif
+
+}  // namespace mce

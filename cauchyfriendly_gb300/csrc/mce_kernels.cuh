@@ -1,0 +1,83 @@
+// Kernel launch interface of the MCE step path.  The kernels themselves live
+// in mce_kernels.cu (templated on the state dimension D, instantiated for
+// D = 1..8); the engine (mce_engine.cu) calls these launchers.
+#pragma once
+#include "mce_device.cuh"
+
+namespace mce {
+
+struct LaunchCfg {
+    cudaStream_t stream;
+    int num_sms;
+};
+
+// Scratch for the device-wide scans.
+struct ScanScratch {
+    long long* block_sums;  // capacity >= ceil(n / 2048) + 1 at every level
+    long long cap;
+};
+
+// out[i] = sum_{k<i} in[k] for i in [0, n]; out[n] holds the total.
+void scan_int_to_ll(const int* in, long long* out, long long n, ScanScratch& s, const LaunchCfg& c);
+
+template <int D>
+struct Kernels {
+    // First measurement update (cauchy_estimator.hpp:1179-1208).
+    static void first_count(const double* A0, const EstStep<D>* st, int E, int* cnt, const LaunchCfg& c);
+    static void first_build(const double* A0, const double* p0, const double* b0, const EstStep<D>* st,
+                            const double* roots, int E, const long long* pstart, ParentList P, int MC,
+                            cd* est_raw, const LaunchCfg& c);
+    static void first_tables(ParentList P, long long nP, const double* cval, const double* dval,
+                             const unsigned* hof, const double* gscale, Tables T, int MC, const LaunchCfg& c);
+
+    // Time propagation, TP coalignment and child counting (cauchy_term.hpp:84-145, 435-531).
+    static void tp(ParentList P, long long nP, const EstStep<D>* st, int with_tp, int MC, int* Bcap,
+                   int* err, const LaunchCfg& c);
+    // B tables: TP enumeration (cell_enumeration.hpp:676-855) or a copy of the parent keys.
+    static void build_B(ParentList P, long long nP, const EstStep<D>* st, int with_tp, Tables Told,
+                        int* Bkeys, long long Bcap_total, const double* bpert, int MC, const int* combo_off,
+                        const unsigned char* combos, int* err, const LaunchCfg& c);
+    // Measurement update, g/yei evaluation, moment partials, MU coalignment.
+    static void mu(ParentList P, long long nP, const EstStep<D>* st, const long long* pstart,
+                   const double* roots, Tables Told, int* Bkeys, TermRecs R, long long nR,
+                   const long long* kall_scan, cd* contrib, int MC, int* err, const LaunchCfg& c);
+    // Per-estimator moment sums in the reference's order and finalisation
+    // (cauchy_estimator.hpp:307-357).
+    static void moments(const cd* contrib, const long long* pstart, const long long* kall_scan, int E,
+                        const EstStep<D>* st, cd* est_raw, double* gscale, const LaunchCfg& c);
+    // Fast term reduction (term_reduction.hpp:159-276) over the post-MU records.
+    static void ftr_insert(TermRecs R, long long nR, long long* cellq, int* head, int* next, long long hmask,
+                           const LaunchCfg& c);
+    static void ftr_preds(TermRecs R, long long nR, const long long* cellq, const int* head, const int* next,
+                          long long hmask, int MC, const long long* pred_off, int* preds, int* npred,
+                          const LaunchCfg& c);
+    // g-tables of every reduction group (flattening.hpp:318-568).
+    static void gtable(TermRecs R, const int* roots_list, long long nroots, const int* gcnt,
+                       const long long* goff, const int* members, ParentList P, Tables Told, const int* Bkeys,
+                       const double* gscale, const long long* toff, Tables Tnew, int* tcnt, int* alive,
+                       int* src, cd* scratch, long long scratch_per_warp, int MC, int* err,
+                       const LaunchCfg& c);
+    // Next parent list (shape-bucketed, stable) from the surviving roots.
+    static void compact(TermRecs R, const int* alive, const int* src, long long nR, const int* new_slot,
+                        const long long* toff, const int* tcnt, ParentList Pn, int MC, const LaunchCfg& c);
+};
+
+// Shape-agnostic kernels.
+void ftr_resolve(const long long* pred_off, const int* preds, long long nR, int* status, int* owner,
+                 int* unknown, const LaunchCfg& c);
+void group_count(const int* status, const int* owner, long long nR, int* gcnt, const LaunchCfg& c);
+void group_fill(const int* status, const int* owner, long long nR, const long long* goff, int* gfill,
+                int* members, const LaunchCfg& c);
+void group_sort(const int* gcnt, const long long* goff, long long nR, int* members, const LaunchCfg& c);
+void roots_flags(const int* status, const int* m, long long nR, int D, int* is_root, int* cap,
+                 const LaunchCfg& c);
+void roots_list(const int* is_root, const long long* rscan, long long nR, int* list, const LaunchCfg& c);
+// Stable partition of alive roots of each estimator by shape.
+void partition_count(const int* alive, const int* est, const int* m, long long nR, int MCp, int* hist,
+                     const LaunchCfg& c);
+void partition_rank(const int* alive, const int* m, const long long* rbase, int E, int MCp,
+                    const long long* bucket_off, int* new_slot, const LaunchCfg& c);
+void rbase_kernel(const long long* pstart, const long long* kscan, int E, long long* rbase,
+                  const LaunchCfg& c);
+
+}  // namespace mce

@@ -1,0 +1,223 @@
+"""Host-side mirror of the reference's C++ estimator interface.
+
+``CauchyEstimator`` follows ``struct CauchyEstimator``
+(include/cauchy_estimator.hpp:47-1432): same constructor arguments, ``step``
+semantics (one scalar measurement, returns the numeric-moment error bitmask)
+and public fields (``fz``, ``conditional_mean``, ``conditional_variance``,
+``Nt``, ``master_step``, ``terms_per_shape``, ``G_SCALE_FACTOR``).
+``BatchedCauchyEstimator`` steps many independent estimators in lock-step on
+one GPU.  All compute runs in libmce_gb300.so.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_lp = ctypes.POINTER(ctypes.c_longlong)
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _p(a, kind=_dp):
+    return None if a is None else a.ctypes.data_as(kind)
+
+
+def max_shape(steps, d, pncc):
+    """Largest hyperplane count a term can reach (cauchy_estimator.hpp:96)."""
+    return (steps - 1) * pncc + d if d > 1 else d + pncc
+
+
+class BatchedCauchyEstimator:
+    """n_est independent estimators stepped together.
+
+    A0 (n_est,d,d), p0 (n_est,d), b0 (n_est,d), steps (n_est,); root_point
+    (n_est,d) and b_pert (n_est, stride) default to the reference's libc
+    rand() draws."""
+
+    def __init__(self, A0, p0, b0, steps, d, cmcc, pncc, p, root_point=None, b_pert=None):
+        self._lib = _lib.load()
+        self.d, self.cmcc, self.pncc, self.p = int(d), int(cmcc), int(pncc), int(p)
+        self.steps = np.ascontiguousarray(steps, dtype=np.int32).reshape(-1)
+        self.n_est = int(self.steps.size)
+        A0, p0, b0 = _f64(A0), _f64(p0), _f64(b0)
+        rp, bp = _f64(root_point), _f64(b_pert)
+        stride = 0 if bp is None else int(bp.reshape(self.n_est, -1).shape[1])
+        st = ctypes.c_int(0)
+        self._h = self._lib.mce_batch_create(self.n_est, self.d, self.cmcc, self.pncc, self.p,
+                                             _p(self.steps, _ip), _p(A0), _p(p0), _p(b0), _p(rp), _p(bp), stride,
+                                             ctypes.byref(st))
+        if not self._h:
+            raise _lib.MceError("mce_batch_create failed (%d): %s" % (st.value, _lib.last_error()))
+        self.max_shape = max_shape(int(self.steps.max()), self.d, self.pncc)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.mce_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- stepping ------------------------------------------------------------
+    def step(self, msmts, Phi, Gamma, beta, H, gamma, B=None, u=None, shared_model=None):
+        """One measurement update for every estimator.  With shared_model the
+        model arrays hold one copy; otherwise they are stacked per estimator."""
+        msmts = _f64(msmts).reshape(self.n_est)
+        Phi, Gamma, beta, H, gamma, B, u = map(_f64, (Phi, Gamma, beta, H, gamma, B, u))
+        if shared_model is None:
+            shared_model = Phi.ndim == 2
+        err = np.zeros(self.n_est, dtype=np.int32)
+        rc = self._lib.mce_batch_step(self._h, _p(msmts), _p(Phi), _p(Gamma), _p(beta), _p(H), _p(gamma), _p(B),
+                                      _p(u), 1 if shared_model else 0, _p(err, _ip))
+        _lib.check(rc, "mce_batch_step")
+        return err
+
+    def run(self, msmts, Phi, Gamma, beta, H, gamma, B=None, u=None, shared_model=False, outputs=True):
+        """Whole measurement histories msmts (n_est, max_steps, p)."""
+        msmts = _f64(msmts)
+        max_steps = msmts.shape[1]
+        Phi, Gamma, beta, H, gamma, B, u = map(_f64, (Phi, Gamma, beta, H, gamma, B, u))
+        nu = int(self.p * self.steps.max())
+        out = None
+        if outputs:
+            d = self.d
+            out = {"fz": np.zeros((self.n_est, nu, 2)), "mean": np.zeros((self.n_est, nu, 2 * d)),
+                   "cov": np.zeros((self.n_est, nu, 2 * d * d)), "err": np.zeros((self.n_est, nu), np.int32),
+                   "nt": np.zeros((self.n_est, nu), np.int64)}
+        rc = self._lib.mce_batch_run(self._h, _p(msmts), max_steps, _p(Phi), _p(Gamma), _p(beta), _p(H), _p(gamma),
+                                     _p(B), _p(u), 1 if shared_model else 0,
+                                     _p(out["fz"]) if out else None, _p(out["mean"]) if out else None,
+                                     _p(out["cov"]) if out else None, _p(out["err"], _ip) if out else None,
+                                     _p(out["nt"], _lp) if out else None)
+        _lib.check(rc, "mce_batch_run")
+        return out
+
+    # -- read-out ------------------------------------------------------------
+    def moments(self, e=0):
+        d = self.d
+        fz, mean, cov = np.zeros(2), np.zeros(2 * d), np.zeros(2 * d * d)
+        rfz, rmean, rcov, gs = np.zeros(2), np.zeros(2 * d), np.zeros(2 * d * d), np.zeros(1)
+        _lib.check(self._lib.mce_get_moments(self._h, e, _p(fz), _p(mean), _p(cov)), "mce_get_moments")
+        _lib.check(self._lib.mce_get_raw_moments(self._h, e, _p(rfz), _p(rmean), _p(rcov), _p(gs)),
+                   "mce_get_raw_moments")
+        c = lambda a: a[0::2] + 1j * a[1::2]
+        return {"fz": complex(*fz), "mean": c(mean), "cov": c(cov).reshape(d, d), "raw_fz": complex(*rfz),
+                "raw_mean": c(rmean), "raw_cov": c(rcov).reshape(d, d), "gscale": float(gs[0])}
+
+    def errors(self, e=0):
+        return int(self._lib.mce_get_errors(self._h, e))
+
+    def num_terms(self, e=0):
+        return int(self._lib.mce_num_terms(self._h, e))
+
+    def terms_per_shape(self, e=0):
+        out = np.zeros(self.max_shape + 1, dtype=np.int32)
+        _lib.check(self._lib.mce_terms_per_shape(self._h, e, _p(out, _ip), out.size), "mce_terms_per_shape")
+        return out
+
+    def post_mu_terms(self):
+        return int(self._lib.mce_post_mu_terms(self._h))
+
+    def master_step(self):
+        return int(self._lib.mce_master_step(self._h))
+
+    def device_errors(self):
+        return int(self._lib.mce_device_errors(self._h))
+
+    def last_step_ms(self):
+        return float(self._lib.mce_last_step_ms(self._h))
+
+    def dump_terms(self, e=0, max_shape=None):
+        """Terms of estimator e in (shape, index) order with their g-tables."""
+        ms = max_shape or self.max_shape
+        nt = self.num_terms(e)
+        tc = int(self._lib.mce_total_cells(self._h, e))
+        d = self.d
+        shape = np.zeros(nt, np.int32)
+        A = np.zeros(nt * ms * d)
+        p = np.zeros(nt * ms)
+        b = np.zeros(nt * d)
+        cells = np.zeros(nt, np.int32)
+        keys = np.zeros(max(tc, 1), np.int32)
+        g = np.zeros(2 * max(tc, 1))
+        _lib.check(self._lib.mce_dump_terms(self._h, e, ms, _p(shape, _ip), _p(A), _p(p), _p(b), _p(cells, _ip),
+                                            _p(keys, _ip), _p(g)), "mce_dump_terms")
+        return {"shape": shape, "A": A.reshape(nt, ms, d), "p": p.reshape(nt, ms), "b": b.reshape(nt, d),
+                "cells": cells, "keys": keys[:tc], "g": (g[0::2] + 1j * g[1::2])[:tc]}
+
+    def reset(self):
+        _lib.check(self._lib.mce_reset(self._h), "mce_reset")
+
+    def reinitialize_start_statistics(self, A0, p0, b0, e=0):
+        A0, p0, b0 = _f64(A0), _f64(p0), _f64(b0)
+        _lib.check(self._lib.mce_reinitialize_start_statistics(self._h, e, _p(A0), _p(p0), _p(b0)),
+                   "mce_reinitialize_start_statistics")
+
+    def set_master_step(self, ms):
+        _lib.check(self._lib.mce_set_master_step(self._h, int(ms)), "mce_set_master_step")
+
+    def set_win_num(self, w):
+        _lib.check(self._lib.mce_set_window_number(self._h, int(w)), "mce_set_window_number")
+
+
+class CauchyEstimator(BatchedCauchyEstimator):
+    """CauchyEstimator(A0, p0, b0, steps, d, cmcc, pncc, p, print_basic_info)
+    (include/cauchy_estimator.hpp:87): a batch of one."""
+
+    def __init__(self, A0, p0, b0, steps, d, cmcc, pncc, p, print_basic_info=False, root_point=None,
+                 b_pert=None):
+        d = int(d)
+        A0 = _f64(A0).reshape(1, d, d)
+        p0 = _f64(p0).reshape(1, d)
+        b0 = _f64(b0).reshape(1, d)
+        rp = None if root_point is None else _f64(root_point).reshape(1, d)
+        bp = None if b_pert is None else _f64(b_pert).reshape(1, -1)
+        super().__init__(A0, p0, b0, [int(steps)], d, cmcc, pncc, p, rp, bp)
+        self.print_basic_info = bool(print_basic_info)
+
+    def step(self, msmt, Phi, Gamma, beta, H, gamma, B=None, u=None):
+        """CauchyEstimator::step (include/cauchy_estimator.hpp:1211): returns
+        numeric_moment_errors."""
+        d = self.d
+        Phi = _f64(Phi).reshape(d, d)
+        Gamma = None if Gamma is None else _f64(Gamma).reshape(d, -1)
+        beta = None if beta is None else _f64(beta).reshape(-1)
+        H = _f64(H).reshape(d)
+        B = None if B is None else _f64(B).reshape(d, -1)
+        u = None if u is None else _f64(u).reshape(-1)
+        rc = self._lib.mce_step(self._h, float(msmt), _p(Phi), _p(Gamma), _p(beta), _p(H), float(gamma), _p(B), _p(u))
+        return _lib.check(rc, "mce_step")
+
+    @property
+    def fz(self):
+        return self.moments()["fz"]
+
+    @property
+    def conditional_mean(self):
+        return self.moments()["mean"]
+
+    @property
+    def conditional_variance(self):
+        return self.moments()["cov"]
+
+    @property
+    def G_SCALE_FACTOR(self):
+        return self.moments()["gscale"]
+
+    @property
+    def Nt(self):
+        return self.num_terms()
+
+    @property
+    def numeric_moment_errors(self):
+        return self.errors()

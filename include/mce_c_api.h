@@ -1,0 +1,124 @@
+/*
+ * C ABI of the GB300 MCE step path (libmce_gb300.so).
+ *
+ * Drop-in boundary for the reference's CauchyEstimator::step path
+ * (natsnyder1/CauchyFriendly).  Plain pointers and sizes only; all device
+ * state (terms, cell tables, arenas) stays inside the library.  Every entry
+ * point returns a status instead of exiting the process.
+ *
+ * Arrays follow the reference's layouts: Phi is d x d row-major, Gamma is
+ * d x pncc row-major, H is one measurement row (d), B is d x cmcc row-major,
+ * complex outputs are interleaved (re, im) pairs.
+ */
+#ifndef MCE_C_API_H
+#define MCE_C_API_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mce_handle mce_handle;
+
+/* status codes */
+#define MCE_OK 0
+#define MCE_ERR_ARG (-1)       /* invalid argument */
+#define MCE_ERR_CUDA (-2)      /* CUDA runtime failure (message via mce_last_error) */
+#define MCE_ERR_SHAPE (-3)     /* hyperplane count beyond what the build supports */
+#define MCE_ERR_DEVICE (-4)    /* a kernel reported an error bit (see mce_device_errors) */
+#define MCE_ERR_DONE (-5)      /* stepped past the last step; the reference calls exit(1) here */
+#define MCE_ERR_NOMEM (-6)     /* device allocation failed */
+
+/* Last error message of the calling thread (static storage). */
+const char* mce_last_error(void);
+
+/* Reproduces the reference constructor's libc rand() draws
+ * (include/cauchy_estimator.hpp:127-128 root point, then num_cpus DCE helpers
+ * drawing b_pert, include/cell_enumeration.hpp:467-470); helper 0's b_pert is
+ * returned.  seed < 0 keeps the current rand() state (the reference never
+ * seeds), otherwise srand(seed) is called first. */
+int mce_draw_reference_constants(long long seed, int d, int max_shape, int num_cpus, double* root_point,
+                                 double* b_pert);
+
+/* Batch of independent estimators stepped in lock-step.  Replaces
+ * CauchyEstimator::CauchyEstimator (include/cauchy_estimator.hpp:87-185) for
+ * n_est estimators at once.
+ *   steps[n_est]            estimation steps per estimator
+ *   A0 [n_est*d*d], p0 [n_est*d], b0 [n_est*d]
+ *   root_point [n_est*d]    or NULL: drawn with rand() as the reference does
+ *   b_pert [n_est*bpert_stride] or NULL: drawn with rand()
+ * bpert_stride must be >= each estimator's max shape ((steps-1)*pncc + d). */
+mce_handle* mce_batch_create(int n_est, int d, int cmcc, int pncc, int p, const int* steps, const double* A0,
+                             const double* p0, const double* b0, const double* root_point, const double* b_pert,
+                             int bpert_stride, int* status);
+
+/* One measurement update for every estimator (CauchyEstimator::step,
+ * include/cauchy_estimator.hpp:1211-1245).  shared_model != 0 means Phi,
+ * Gamma, beta, H, gamma, B hold a single copy used by all estimators;
+ * otherwise each is stacked per estimator.  msmt[n_est], u[n_est*cmcc].
+ * err_out[n_est] receives each estimator's error bitmask (may be NULL). */
+int mce_batch_step(mce_handle* h, const double* msmt, const double* Phi, const double* Gamma, const double* beta,
+                   const double* H, const double* gamma, const double* B, const double* u, int shared_model,
+                   int* err_out);
+
+/* Runs every estimator through its whole measurement history
+ * msmts[n_est * max_steps * p] (row e*max_steps*p + k*p + j), with a shared
+ * model or per-estimator models as in mce_batch_step.  Per-update outputs are
+ * optional (NULL): fz[n_est*max_updates*2], mean[...*2d], cov[...*2d*d],
+ * err[n_est*max_updates], nt[n_est*max_updates]. */
+int mce_batch_run(mce_handle* h, const double* msmts, int max_steps, const double* Phi, const double* Gamma,
+                  const double* beta, const double* H, const double* gamma, const double* B, const double* u,
+                  int shared_model, double* fz, double* mean, double* cov, int* err, long long* nt);
+
+/* Single estimator, the CauchyEstimator constructor
+ * (include/cauchy_estimator.hpp:87): a batch of one. */
+mce_handle* mce_create(const double* A0, const double* p0, const double* b0, int steps, int d, int cmcc, int pncc,
+                       int p, const double* root_point, const double* b_pert, int* status);
+
+/* CauchyEstimator::step (include/cauchy_estimator.hpp:1211): returns the
+ * error bitmask (>= 0) or a negative MCE_ERR_* status. */
+int mce_step(mce_handle* h, double msmt, const double* Phi, const double* Gamma, const double* beta, const double* H,
+             double gamma, const double* B, const double* u);
+
+/* Reported moments after the numeric checks (the fields fz,
+ * conditional_mean, conditional_variance the reference exposes,
+ * include/cauchy_estimator.hpp:66-68): fz[2], mean[2d], cov[2d*d]. */
+int mce_get_moments(mce_handle* h, int est, double* fz, double* mean, double* cov);
+/* Raw moments of the last update before the checks, and G_SCALE_FACTOR. */
+int mce_get_raw_moments(mce_handle* h, int est, double* fz, double* mean, double* cov, double* g_scale_factor);
+/* numeric_moment_errors of one estimator. */
+int mce_get_errors(mce_handle* h, int est);
+/* Nt after the last update (post-reduction, or un-reduced after the final MU). */
+long long mce_num_terms(mce_handle* h, int est);
+/* terms_per_shape (n entries, shape index = hyperplane count). */
+int mce_terms_per_shape(mce_handle* h, int est, int* out, int n);
+/* Sum over all updates and estimators of the terms present after each MU. */
+long long mce_post_mu_terms(mce_handle* h);
+int mce_master_step(mce_handle* h);
+/* Device error bits accumulated by the kernels (0 when healthy). */
+int mce_device_errors(mce_handle* h);
+
+/* Parity hooks: terms of one estimator in (shape, index) order.  Sizes:
+ * shape[nt], A[nt*max_shape*d], p[nt*max_shape], b[nt*d], cells[nt],
+ * keys[total_cells], g[2*total_cells]. */
+long long mce_total_cells(mce_handle* h, int est);
+int mce_dump_terms(mce_handle* h, int est, int max_shape, int* shape, double* A, double* p, double* b, int* cells,
+                   int* keys, double* g);
+
+/* CauchyEstimator::reset (include/cauchy_estimator.hpp:1247) for every estimator. */
+int mce_reset(mce_handle* h);
+/* reinitialize_start_statistics (include/cauchy_estimator.hpp:1302). */
+int mce_reinitialize_start_statistics(mce_handle* h, int est, const double* A0, const double* p0, const double* b0);
+/* master_step setter used by the window manager (pycauchy.hpp:776). */
+int mce_set_master_step(mce_handle* h, int master_step);
+int mce_set_window_number(mce_handle* h, int win_num);
+
+/* Wall time of the device work of the last step (CUDA events), ms. */
+double mce_last_step_ms(mce_handle* h);
+
+void mce_destroy(mce_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MCE_C_API_H */

@@ -44,6 +44,22 @@ static inline cplx cconj(cplx z)
     __imag__ z = -__imag__ z;
     return z;
 }
+// Complex division by Smith's method (CACM 5(8), 1962), evaluated here
+// unfused.  On x86-64 this is bit-identical to the compiler runtime's
+// division the reference uses; spelling it out keeps the oracle identical on
+// hosts whose runtime division is built with fused multiply-adds (aarch64).
+static inline cplx cdiv(cplx x, cplx y)
+{
+    const double a = __real__ x, b = __imag__ x, c = __real__ y, d = __imag__ y;
+    if (fabs(c) < fabs(d)) {
+        const double r = c / d;
+        const double den = c * r + d;
+        return mkc((a * r + b) / den, (b * r - a) / den);
+    }
+    const double r = d / c;
+    const double den = d * r + c;
+    return mkc((b * r + a) / den, (b - a * r) / den);
+}
 
 // Constants: include/cauchy_constants.hpp:27-81
 static const double kTwoPiInv = 1.0 / (2.0 * M_PI);
@@ -667,7 +683,7 @@ static cplx eval_g_yei(const Term& t, int d, const double* root, cplx* yei, bool
         gp = lookup_num(t.gp.get(), lp ^ t.enc_lhp, t.phc);
         gm = lookup_num(t.gp.get(), lm ^ t.enc_lhp, t.phc);
     }
-    cplx g = gp / mkc(ygi + t.d_val, t.c_val) - gm / mkc(ygi - t.d_val, t.c_val);
+    cplx g = cdiv(gp, mkc(ygi + t.d_val, t.c_val)) - cdiv(gm, mkc(ygi - t.d_val, t.c_val));
     g *= kTwoPiInv;
     for (int j = 0; j < d; j++) yei[j] = mkc(-ty[j], t.b[j]);
     return g;
@@ -886,10 +902,10 @@ static bool make_gtable(Term& t, const std::vector<int>& B, double gscale)
         }
         cplx gp = lookup_num(t.gp.get(), lp ^ t.enc_lhp, phc);
         cplx gm = lookup_num(t.gp.get(), lm ^ t.enc_lhp, phc);
-        cplx v = gp / mkc(ygi + t.d_val, t.c_val) - gm / mkc(ygi - t.d_val, t.c_val);
+        cplx v = cdiv(gp, mkc(ygi + t.d_val, t.c_val)) - cdiv(gm, mkc(ygi - t.d_val, t.c_val));
         v *= gscale;
         kv.push_back({be, v});
-        if (negl && ps * cabs(v) > kTermApproxEps) negl = false;
+        if (negl && ps * hypot(__real__ v, __imag__ v) > kTermApproxEps) negl = false;  // cabs == hypot
     }
     std::stable_sort(kv.begin(), kv.end(), [](const std::pair<int, cplx>& a, const std::pair<int, cplx>& b) {
         return a.first < b.first;
@@ -1109,9 +1125,9 @@ static void finalize_moments(Estimator& E)
     const int d = E.d;
     E.gscale = kTwoPiInv / __real__ E.fz;
     cplx ifz = mkc(0, __real__ E.fz);
-    for (int i = 0; i < d; i++) E.mean[i] /= ifz;
+    for (int i = 0; i < d; i++) E.mean[i] = cdiv(E.mean[i], ifz);
     for (int i = 0; i < d; i++)
-        for (int j = 0; j < d; j++) E.cov[i * d + j] = (E.cov[i * d + j] / E.fz) - E.mean[i] * E.mean[j];
+        for (int j = 0; j < d; j++) E.cov[i * d + j] = cdiv(E.cov[i * d + j], E.fz) - E.mean[i] * E.mean[j];
     E.raw_fz = E.fz;
     E.raw_mean = E.mean;
     E.raw_cov = E.cov;
@@ -1154,9 +1170,9 @@ static void step_first(Estimator& E, double msmt, const double* H, double gamma)
     }
     E.gscale = kTwoPiInv / __real__ E.fz;
     cplx ifz = mkc(0, __real__ E.fz);
-    for (int i = 0; i < d; i++) E.mean[i] /= ifz;
+    for (int i = 0; i < d; i++) E.mean[i] = cdiv(E.mean[i], ifz);
     for (int i = 0; i < d; i++)
-        for (int j = 0; j < d; j++) E.cov[i * d + j] = (E.cov[i * d + j] / E.fz) - E.mean[i] * E.mean[j];
+        for (int j = 0; j < d; j++) E.cov[i * d + j] = cdiv(E.cov[i * d + j], E.fz) - E.mean[i] * E.mean[j];
     E.raw_fz = E.fz;
     E.raw_mean = E.mean;
     E.raw_cov = E.cov;
@@ -1167,7 +1183,7 @@ static void step_first(Estimator& E, double msmt, const double* H, double gamma)
             double ygi = 0;
             for (int k = 0; k < d; k++)
                 if (!(t.horthog & (1u << k))) ygi += t.p[k] * (((j >> k) & 1) == 0 ? 1.0 : -1.0);
-            cplx v = 1.0 / mkc(ygi + t.d_val, t.c_val) - 1.0 / mkc(ygi - t.d_val, t.c_val);
+            cplx v = cdiv(mkc(1, 0), mkc(ygi + t.d_val, t.c_val)) - cdiv(mkc(1, 0), mkc(ygi - t.d_val, t.c_val));
             v *= E.gscale;
             t.g.keys.push_back(j);
             t.g.vals.push_back(v);

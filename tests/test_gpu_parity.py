@@ -1,0 +1,149 @@
+"""Parity of the GPU path (through the C ABI) with the reference.
+
+* golden fixtures made by the reference itself: integer structure (term
+  counts, terms per shape, error bits, g-table keys) bit-exact; fz, mean,
+  covariance and g values within 1e-9 relative (REL_TOL in golden_cases);
+* larger seeded problems against the oracle (oracle/mce_oracle.cpp), the
+  batched path against per-estimator oracle runs.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from tests import golden_cases as G
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from cauchyfriendly_gb300 import BatchedCauchyEstimator, CauchyEstimator
+    return CauchyEstimator, BatchedCauchyEstimator
+
+
+class _GpuAdapter:
+    """Gives a GPU CauchyEstimator the stepping interface oracle.run uses."""
+
+    def __init__(self, prob, root_point, b_pert):
+        CE, _ = _gpu()
+        self.prob = prob
+        self.est = CE(prob["A0"], prob["p0"], prob["b0"], prob["steps"], prob["d"], prob["cmcc"], prob["pncc"],
+                      prob["p"], root_point=root_point, b_pert=b_pert)
+
+    def step(self, k, sub=0):
+        pr = self.prob
+        Phi = pr["Phi"] if pr["Phi"].ndim == 2 else pr["Phi"][k]
+        return self.est.step(pr["msmts"][k, sub], Phi, pr["Gamma"], pr["beta"], pr["H"][sub], pr["gamma"][sub])
+
+    def moments(self):
+        return self.est.moments()
+
+    def num_terms(self):
+        return self.est.num_terms()
+
+    def terms_per_shape(self):
+        return self.est.terms_per_shape()
+
+    def dump_terms(self, max_shape):
+        return self.est.dump_terms(0, max_shape)
+
+    def close(self):
+        self.est.close()
+
+
+@pytest.mark.parametrize("name", G.names())
+def test_gpu_matches_reference_golden(name):
+    prob, (rp, bp), want = G.load(name)
+    est = _GpuAdapter(prob, rp, bp)
+    got = oracle.run(est, prob, record_terms_upto=10**9)
+    assert est.est.device_errors() == 0
+    est.close()
+    G.compare_records(got, want)
+
+
+def _batch_run_compare(probs, consts, check_terms=False):
+    _, BCE = _gpu()
+    n = len(probs)
+    d = probs[0]["d"]
+    steps = np.array([p["steps"] for p in probs], np.int32)
+    A0 = np.stack([p["A0"] for p in probs])
+    p0 = np.stack([p["p0"] for p in probs])
+    b0 = np.stack([p["b0"] for p in probs])
+    ms = oracle.max_shape_of({"steps": int(steps.max()), "d": d, "pncc": probs[0]["pncc"]})
+    rp = np.stack([c[0] for c in consts])
+    bp = np.zeros((n, ms))
+    for i, c in enumerate(consts):
+        bp[i, :len(c[1])] = c[1]
+    bat = BCE(A0, p0, b0, steps, d, probs[0]["cmcc"], probs[0]["pncc"], probs[0]["p"], rp, bp)
+    maxs = int(steps.max())
+    msm = np.zeros((n, maxs, probs[0]["p"]))
+    for i, p in enumerate(probs):
+        msm[i, :p["steps"]] = p["msmts"]
+    Phi = np.stack([p["Phi"] for p in probs])
+    Gam = np.stack([p["Gamma"] for p in probs])
+    beta = np.stack([p["beta"] for p in probs])
+    H = np.stack([p["H"] for p in probs])
+    gam = np.stack([p["gamma"] for p in probs])
+    # step by step so per-estimator term dumps can be compared too
+    recs = [[] for _ in range(n)]
+    for k in range(maxs):
+        for s in range(probs[0]["p"]):
+            bat.step(msm[:, k, s], Phi, Gam, beta, H[:, s, :], gam[:, s], shared_model=False)
+            for i, p in enumerate(probs):
+                if k < p["steps"]:
+                    r = bat.moments(i)
+                    r["err"] = bat.errors(i)
+                    r["Nt"] = bat.num_terms(i)
+                    r["tps"] = bat.terms_per_shape(i)
+                    if check_terms and k < p["steps"] - 1:
+                        r["terms"] = bat.dump_terms(i, oracle.max_shape_of(p))
+                    recs[i].append(r)
+    assert bat.device_errors() == 0
+    total = bat.post_mu_terms()
+    bat.close()
+    return recs, total
+
+
+def test_batched_matches_golden_per_estimator():
+    names = [n for n in G.names() if n.startswith("batched_three_state")]
+    loaded = [G.load(n) for n in names]
+    probs = [l[0] for l in loaded]
+    consts = [l[1] for l in loaded]
+    recs, _ = _batch_run_compare(probs, consts, check_terms=True)
+    for (prob, _, want), got in zip(loaded, recs):
+        G.compare_records(got, want)
+
+
+def _oracle_records(prob, rp, bp):
+    est = oracle.Oracle(prob, rp, bp)
+    r = oracle.run(est, prob, 0)
+    n = est.post_mu_terms()
+    est.close()
+    return r, n
+
+
+def test_batched_random_three_state_against_oracle():
+    from cauchyfriendly_gb300 import workloads as W
+    probs = W.batched_three_state(48, seed=11, steps_lo=4, steps_hi=8)
+    consts = [oracle.draw_reference_constants(100 + i, 3, oracle.max_shape_of(p)) for i, p in enumerate(probs)]
+    recs, total = _batch_run_compare(probs, consts)
+    want_total = 0
+    for prob, c, got in zip(probs, consts, recs):
+        want, n = _oracle_records(prob, *c)
+        want_total += n
+        G.compare_records(got, want, check_terms=False)
+    assert total == want_total
+
+
+@pytest.mark.parametrize("steps", [10])
+def test_three_state_longer_against_oracle(steps):
+    from cauchyfriendly_gb300 import workloads as W
+    prob = W.three_state_lti(seed=5, steps=steps)
+    rp, bp = oracle.draw_reference_constants(3, 3, oracle.max_shape_of(prob))
+    est = _GpuAdapter(prob, rp, bp)
+    got = oracle.run(est, prob, 0)
+    est.close()
+    want, _ = _oracle_records(prob, rp, bp)
+    G.compare_records(got, want, check_terms=False)
