@@ -1,0 +1,371 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 MCE step path.
+
+Workload: the batched plain-MCE configuration -- 4096 independent 3-state LTI
+estimators (random stable Phi with eigenvalue moduli in [0.8, 1.0],
+Gamma=[0,0,1]^T, H=[1,0,0], beta/gamma/p0 log-uniform in [0.02, 0.5], step
+counts uniform in 4..9, Cauchy measurement histories with 5% outliers at
+100x), seeded synthetic data.  One bench step = one pass of the whole batch
+through every measurement update.
+
+metric: MCE terms updated per second = sum over updates of the terms present
+after each measurement update (the reference's "Total Terms after MU(C)"
+counter) / time.
+
+  value   device time (CUDA events on the library's stream, summed over the
+          updates of the pass; inputs are per-update scalars already on the
+          host-side engine, the term state lives in HBM)
+  e2e     the same through the public C ABI call mce_batch_run with host
+          measurement buffers, wall clock around the call
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MCE terms updated/sec (1 GB300, FP64) at rel err <=1e-9; batched/adjoint vs plain"
+UNIT = "terms/s"
+WORKLOAD = "batched plain MCE: 4096 x 3-state LTI, steps U{4..9}, 5% outliers at 100x"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n-est", type=int, default=4096)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of the CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def batch_arrays(probs):
+    n = len(probs)
+    d = probs[0]["d"]
+    steps = np.array([p["steps"] for p in probs], np.int32)
+    maxs = int(steps.max())
+    msm = np.zeros((n, maxs, 1))
+    for i, p in enumerate(probs):
+        msm[i, :p["steps"]] = p["msmts"]
+    return {
+        "steps": steps, "A0": np.stack([p["A0"] for p in probs]), "p0": np.stack([p["p0"] for p in probs]),
+        "b0": np.stack([p["b0"] for p in probs]), "Phi": np.stack([p["Phi"] for p in probs]),
+        "Gamma": np.stack([p["Gamma"] for p in probs]), "beta": np.stack([p["beta"] for p in probs]),
+        "H": np.stack([p["H"] for p in probs]), "gamma": np.stack([p["gamma"] for p in probs]), "msmts": msm, "d": d,
+    }
+
+
+def constants(probs, seed):
+    import ctypes
+    from cauchyfriendly_gb300 import _lib, max_shape
+    lib = _lib.load()
+    ms = max(max_shape(p["steps"], p["d"], p["pncc"]) for p in probs)
+    rp = np.zeros((len(probs), probs[0]["d"]))
+    bp = np.zeros((len(probs), ms))
+    dp = ctypes.POINTER(ctypes.c_double)
+    for i, p in enumerate(probs):
+        m = max_shape(p["steps"], p["d"], p["pncc"])
+        r = np.zeros(p["d"])
+        b = np.zeros(m)
+        lib.mce_draw_reference_constants(seed * 100003 + i, p["d"], m, 8, r.ctypes.data_as(dp), b.ctypes.data_as(dp))
+        rp[i] = r
+        bp[i, :m] = b
+    return rp, bp
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                          "-i", "0", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (a line 'traffic_per_term <group> <bytes>' scaled by terms)."""
+    path = os.path.join(ROOT, "profiles", "ncu_gtable_batched_three_state.md")
+    out = {}
+    try:
+        for ln in open(path):
+            if ln.startswith("traffic_bytes_per_alg_byte"):
+                _, grp, v = ln.split()
+                out[grp] = float(v)
+    except OSError:
+        pass
+    return out
+
+
+def cpu_sample(probs, consts, target_seconds):
+    """Bounded sample of the same workload for the CPU baseline: every k-th
+    estimator, k chosen so the oracle port needs about target_seconds."""
+    import oracle
+    oracle.build(with_reference=False)
+    threads = os.cpu_count() or 1
+    # calibrate on a small stride sample
+    k = 64
+    sub = probs[::k]
+    sc = [consts[i] for i in range(0, len(probs), k)]
+    n, t = oracle.run_oracle_batch(sub, sc, threads)
+    if t < target_seconds * 0.3 and k > 1:
+        k = max(1, int(k * t / (target_seconds * 0.5)))
+        sub = probs[::k]
+        sc = [consts[i] for i in range(0, len(probs), k)]
+        n, t = oracle.run_oracle_batch(sub, sc, threads)
+    return {"value": n / t, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "every %d-th estimator of the batch (%d estimators, %d post-MU terms, %.1f s)"
+                      % (k, len(sub), n, t)}
+
+
+def run_reference(args):
+    """Reference arm: the CPU implementation of the path on this host's cores,
+    over a bounded sample of the same batch (every 32nd estimator) per step.
+    Uses the reference's own C++ (oracle/_ref, compiled from its headers) when
+    it is built on this host, otherwise the oracle port."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from cauchyfriendly_gb300 import workloads as W
+    import oracle
+    oracle.build(with_reference=True)
+    probs = W.batched_three_state(args.n_est, seed=args.seed)
+    stride = 32
+    idx = list(range(0, len(probs), stride))
+    sub = [probs[i] for i in idx]
+    seeds = [args.seed * 100003 + i for i in idx]
+    consts = [oracle.draw_reference_constants(s, p["d"], oracle.max_shape_of(p)) for s, p in zip(seeds, sub)]
+    threads = os.cpu_count() or 1
+    use_ref = oracle.reference_available()
+    # terms after each MU of the sample (identical for the reference and the port)
+    n_terms, _ = oracle.run_oracle_batch(sub, consts, threads)
+
+    def one_pass():
+        if use_ref:
+            return _ref_pass(sub, seeds, threads)
+        return oracle.run_oracle_batch(sub, consts, threads)[1]
+
+    for _ in range(args.warmup):
+        one_pass()
+    tot_t = 0.0
+    for _ in range(args.steps):
+        tot_t += one_pass()
+    v = n_terms * args.steps / tot_t
+    kind = "reference" if use_ref else "port"
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "sample_stride": stride},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
+                             "sample": "every %d-th estimator of the batch per step (%d estimators, %d terms)" %
+                                       (stride, len(sub), n_terms)},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def _ref_pass(probs, seeds, threads):
+    """The reference's own C++ (oracle/_ref) on a thread pool, one estimator per
+    task; each estimator is seeded so its rand()-drawn constants equal the GPU
+    run's.  Returns wall seconds."""
+    import oracle
+    from concurrent.futures import ThreadPoolExecutor
+
+    def one(i):
+        est = oracle.Reference(probs[i], seed=seeds[i])
+        for k in range(probs[i]["steps"]):
+            est.step(k, 0)
+        est.close()
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(one, range(len(probs))))
+    return time.perf_counter() - t0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from cauchyfriendly_gb300 import BatchedCauchyEstimator, workloads as W
+    from cauchyfriendly_gb300 import _lib
+    # each rank runs its own replica of the batch (independent estimators shard trivially)
+    probs = W.batched_three_state(args.n_est, seed=args.seed + rank)
+    consts = constants(probs, args.seed + rank)
+    B = batch_arrays(probs)
+    est = BatchedCauchyEstimator(B["A0"], B["p0"], B["b0"], B["steps"], 3, 0, 1, 1, consts[0], consts[1])
+    lib = _lib.load()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def one_pass():
+        est.reset()
+        t0 = time.perf_counter()
+        est.run(B["msmts"], B["Phi"], B["Gamma"], B["beta"], B["H"], B["gamma"], shared_model=False, outputs=False)
+        return time.perf_counter() - t0
+
+    # algorithmic bytes / flops per kernel group: one untimed pass
+    lib.mce_set_profiling(est._h, 2)
+    lib.mce_clear_profile(est._h)
+    one_pass()
+    groups = [lib.mce_kernel_group_name(k).decode() for k in range(lib.mce_num_kernel_groups())]
+    import ctypes
+    alg = {}
+    for k, g in enumerate(groups):
+        ms, nl, ab, af = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_double(), ctypes.c_double()
+        lib.mce_kernel_group_stats(est._h, k, ctypes.byref(ms), ctypes.byref(nl), ctypes.byref(ab), ctypes.byref(af))
+        alg[g] = (ab.value, af.value)
+    lib.mce_set_profiling(est._h, 1)
+    for _ in range(max(0, args.warmup - 1)):
+        one_pass()
+    terms_per_pass = est.post_mu_terms()
+    lib.mce_clear_profile(est._h)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler()
+    clk.start()
+    walls = []
+    dev_ms_total = 0.0
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        before = lib.mce_device_time_ms(est._h)
+        walls.append(one_pass())
+        dev_ms_total += lib.mce_device_time_ms(est._h) - before
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    launches = int(lib.mce_launch_count(est._h))
+    kstats = {}
+    for k, g in enumerate(groups):
+        ms, nl, ab, af = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_double(), ctypes.c_double()
+        lib.mce_kernel_group_stats(est._h, k, ctypes.byref(ms), ctypes.byref(nl), ctypes.byref(ab), ctypes.byref(af))
+        kstats[g] = (ms.value, nl.value)
+    dev_ms = dev_ms_total / args.steps
+    wall_s = sum(walls) / args.steps
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([dev_ms, wall_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_ms, wall_s = float(t[0]), float(t[1])
+    total_terms = terms_per_pass * world
+    value = total_terms / (dev_ms / 1e3)
+    e2e = total_terms / wall_s
+    # roofline of the dominant kernel group (largest device time)
+    top = max(kstats, key=lambda g: kstats[g][0])
+    top_ms, top_launches = kstats[top]
+    ab, af = alg.get(top, (0.0, 0.0))
+    secs = top_ms / 1e3 / args.steps  # per pass
+    peak, peak_kind = measured_peaks()
+    achieved = ab / secs / 1e9 if secs > 0 else 0.0
+    tr = profile_traffic().get(top)
+    roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": (tr * ab / max(1, top_launches / args.steps)) if tr else None,
+                "alg_bytes_per_launch": ab / max(1, top_launches / args.steps),
+                "launches_per_pass": top_launches / args.steps,
+                "fp64": {"achieved_tflops": af / secs / 1e12 if secs > 0 else 0.0, "peak_tflops": 1.25,
+                         "peak_source": "nominal GB300 FP64 (not measured)"}}
+    share = {g: round(kstats[g][0] / max(1e-9, sum(v[0] for v in kstats.values())), 4) for g in kstats}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dev_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_estimators": args.n_est, "seed": args.seed,
+                   "terms_per_step": terms_per_pass, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "256 MiB buffer written between passes; term state per pass is several GB"},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(B["msmts"].nbytes + B["Phi"].nbytes
+                                                                       + B["Gamma"].nbytes + B["beta"].nbytes
+                                                                       + B["H"].nbytes + B["gamma"].nbytes),
+                "d2h_bytes_per_step": int(B["steps"].sum() * (2 + 2 * 3 + 2 * 9) * 8), "wall_s_per_step": wall_s},
+        "gpu_launches": launches,
+        "kernel_time_share": share,
+        "roofline": roofline,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_sample(probs, list(zip(consts[0], consts[1])), args.cpu_seconds)
+    est.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

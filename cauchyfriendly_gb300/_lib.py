@@ -46,6 +46,13 @@ SIGNATURES = {
     "mce_set_master_step": (ctypes.c_int, [_vp, ctypes.c_int]),
     "mce_set_window_number": (ctypes.c_int, [_vp, ctypes.c_int]),
     "mce_last_step_ms": (ctypes.c_double, [_vp]),
+    "mce_device_time_ms": (ctypes.c_double, [_vp]),
+    "mce_launch_count": (ctypes.c_longlong, [_vp]),
+    "mce_set_profiling": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "mce_clear_profile": (ctypes.c_int, [_vp]),
+    "mce_num_kernel_groups": (ctypes.c_int, []),
+    "mce_kernel_group_name": (ctypes.c_char_p, [ctypes.c_int]),
+    "mce_kernel_group_stats": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _lp, _dp, _dp]),
     "mce_destroy": (None, [_vp]),
 }
 

@@ -135,6 +135,13 @@ static int cov_flags(const double* cre, const double* cim, int d)
     return f;
 }
 
+enum KernelGroup {
+    KID_FIRST = 0, KID_TP, KID_BUILD_B, KID_MU, KID_MOMENTS, KID_FTR, KID_GROUPS, KID_GTABLE, KID_PARTITION,
+    KID_SCAN, KID_COUNT
+};
+static const char* kKernelGroupNames[KID_COUNT] = {
+    "first_step", "tp", "build_B", "mu", "moments", "ftr", "groups", "gtable", "partition", "scan"};
+
 struct EstHost {
     int steps = 0;          // estimation steps
     int num_updates = 0;    // p * steps
@@ -169,6 +176,26 @@ public:
     int device_errors = 0;
     long long post_mu_terms = 0;
     double last_ms = 0;
+    // profiling: per-kernel-group device time (CUDA events on the engine's
+    // stream), launch counts and algorithmic bytes / FP64 flops
+    int prof_mode = 0;
+    double device_ms_total = 0;
+    long long launches = 0;
+    double kms[KID_COUNT] = {0};
+    long long klaunch[KID_COUNT] = {0};
+    double kbytes[KID_COUNT] = {0};
+    double kflops[KID_COUNT] = {0};
+    void clear_prof()
+    {
+        device_ms_total = 0;
+        launches = 0;
+        for (int k = 0; k < KID_COUNT; k++) {
+            kms[k] = 0;
+            klaunch[k] = 0;
+            kbytes[k] = 0;
+            kflops[k] = 0;
+        }
+    }
     std::vector<EstHost> est;
     std::vector<double> roots, bpert;  // E*d, E*MC
 };
@@ -297,6 +324,52 @@ public:
     std::vector<double> h_gscale;
     std::vector<int> h_hist;
     ScanScratch ss{};
+    // profiling events
+    std::vector<cudaEvent_t> evpool;
+    struct PEv {
+        int id, a, b;
+        long long launches;
+    };
+    std::vector<PEv> pevs;
+    int ev_used = 0, p_id = 0, p_a = 0;
+    long long p_l0 = 0;
+    DevBuf<double> alg;  // [KID_COUNT][2] bytes, flops
+
+    void pbeg(int id)
+    {
+        p_l0 = g_launches;
+        p_id = id;
+        if (!prof_mode) return;
+        if (ev_used + 2 > (int)evpool.size()) {
+            for (int k = 0; k < 256; k++) {
+                cudaEvent_t ev;
+                if (cudaEventCreate(&ev) != cudaSuccess) return;
+                evpool.push_back(ev);
+            }
+        }
+        p_a = ev_used++;
+        cudaEventRecord(evpool[p_a], lc.stream);
+    }
+    void pend()
+    {
+        const long long nl = g_launches - p_l0;
+        launches += nl;
+        if (!prof_mode || p_a >= ev_used) return;
+        const int b_ = ev_used++;
+        cudaEventRecord(evpool[b_], lc.stream);
+        pevs.push_back(PEv{p_id, p_a, b_, nl});
+    }
+    void collect_prof()
+    {
+        for (const PEv& pe : pevs) {
+            float ms = 0;
+            if (cudaEventElapsedTime(&ms, evpool[pe.a], evpool[pe.b]) == cudaSuccess) kms[pe.id] += ms;
+            klaunch[pe.id] += pe.launches;
+        }
+        pevs.clear();
+        ev_used = 0;
+    }
+    void alg_stats(bool with_tp, long long nR, bool tables_built);
 
     int init(int E_, int cmcc_, int pncc_, int p_, const int* steps, const double* A0, const double* p0,
              const double* b0, const double* root, const double* bp, int bp_stride)
@@ -412,6 +485,7 @@ public:
         if (lc.stream) cudaStreamSynchronize(lc.stream);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        for (cudaEvent_t ev : evpool) cudaEventDestroy(ev);
         if (lc.stream) cudaStreamDestroy(lc.stream);
     }
 
@@ -562,6 +636,8 @@ public:
         float msf = 0;
         cudaEventElapsedTime(&msf, ev0, ev1);
         last_ms = msf;
+        device_ms_total += msf;
+        collect_prof();
         // moments of every active estimator
         finish_moments(ms);
         master_step++;
@@ -675,7 +751,9 @@ public:
     {
         int s = first_cnt.ensure(E + 1);
         if (s) return s;
+        pbeg(KID_FIRST);
         Kernels<D>::first_count(dA0.ptr, dsteps.ptr, E, first_cnt.ptr, lc);
+        pend();
         std::vector<int> cnt(E);
         MCE_CUDA(cudaMemcpyAsync(cnt.data(), first_cnt.ptr, sizeof(int) * E, cudaMemcpyDeviceToHost, lc.stream));
         MCE_CUDA(cudaStreamSynchronize(lc.stream));
@@ -689,6 +767,7 @@ public:
         MCE_CUDA(cudaMemcpyAsync(dpstart.ptr, hpstart.data(), sizeof(long long) * (E + 1), cudaMemcpyHostToDevice,
                                  lc.stream));
         ParentList PV = P.view();
+        pbeg(KID_FIRST);
         Kernels<D>::first_build(dA0.ptr, dp0.ptr, db0.ptr, dsteps.ptr, droots.ptr, E, dpstart.ptr, PV, MC,
                                 est_raw.ptr, lc);
         // G_SCALE_FACTOR per estimator from the first moments
@@ -696,6 +775,7 @@ public:
         Kernels<D>::first_tables(PV, nP, reinterpret_cast<double*>(PV.kscan), reinterpret_cast<double*>(PV.B_off),
                                  reinterpret_cast<unsigned*>(PV.nkids), gscale.ptr, Tables{Tb[cur].keys.ptr,
                                  Tb[cur].vals.ptr}, MC, lc);
+        pend();
         read_moments();
         for (int e = 0; e < E; e++) {
             est[e].nt = cnt[e];
@@ -720,10 +800,14 @@ public:
         if ((s = kall_scan.ensure(nP + 2))) return s;
 
         if ((s = ensure_scan_scratch(nP + 1))) return s;
+        pbeg(KID_TP);
         Kernels<D>::tp(PV, nP, dsteps.ptr, with_tp ? 1 : 0, MC, Bcap.ptr, err, lc);
+        pend();
+        pbeg(KID_SCAN);
         scan_int_to_ll(PV.nkids, PV.kscan, nP, ss, lc);
         scan_int_to_ll(Bcap.ptr, PV.B_off, nP, ss, lc);
         scan_int_to_ll(PV.nkids_all, kall_scan.ptr, nP, ss, lc);
+        pend();
         long long tot[3] = {0, 0, 0};
         MCE_CUDA(cudaMemcpyAsync(&tot[0], PV.kscan + nP, sizeof(long long), cudaMemcpyDeviceToHost, lc.stream));
         MCE_CUDA(cudaMemcpyAsync(&tot[1], PV.B_off + nP, sizeof(long long), cudaMemcpyDeviceToHost, lc.stream));
@@ -737,16 +821,24 @@ public:
         if ((s = fam_mom.ensure((size_t)(nP + Kall + 1) * (1 + D + D * D)))) return s;
         if ((s = Bkeys.ensure(Btot + 1))) return s;
         if ((s = Rb.ensure(nR, MC))) return s;
+        pbeg(KID_BUILD_B);
         Kernels<D>::build_B(PV, nP, dsteps.ptr, with_tp ? 1 : 0, Told, Bkeys.ptr, Btot, dbpert.ptr, MC,
                             dcombo_off.ptr, dcombos.ptr, err, lc);
+        pend();
         TermRecs R = Rb.view();
+        pbeg(KID_MU);
         Kernels<D>::mu(PV, nP, dsteps.ptr, dpstart.ptr, droots.ptr, Told, Bkeys.ptr, R, nR, kall_scan.ptr,
                        fam_mom.ptr, MC, err, lc);
+        pend();
+        pbeg(KID_MOMENTS);
         Kernels<D>::moments(fam_mom.ptr, dpstart.ptr, kall_scan.ptr, E, dsteps.ptr, est_raw.ptr, gscale.ptr, lc);
+        pend();
         read_moments();
         // terms after the MU per estimator (un-reduced count, cauchy_estimator.hpp:749-751, 806-812)
         if ((s = kall_est.ensure(E + 2))) return s;
+        pbeg(KID_SCAN);
         k_gather_bounds(kall_scan.ptr, E);
+        pend();
         MCE_CUDA(cudaMemcpyAsync(kall_at.data(), kall_est.ptr, sizeof(long long) * (E + 1), cudaMemcpyDeviceToHost,
                                  lc.stream));
         // shapes of the final-MU estimators (terms_per_shape of the parents' shapes)
@@ -760,7 +852,9 @@ public:
         if (any_skip) {
             if ((s = hist.ensure((size_t)E * MCp))) return s;
             MCE_CUDA(cudaMemsetAsync(hist.ptr, 0, sizeof(int) * E * MCp, lc.stream));
+            pbeg(KID_PARTITION);
             k_skip_hist(PV, nP, MCp);
+            pend();
             skip_hist.resize((size_t)E * MCp);
             MCE_CUDA(cudaMemcpyAsync(skip_hist.data(), hist.ptr, sizeof(int) * E * MCp, cudaMemcpyDeviceToHost,
                                      lc.stream));
@@ -774,6 +868,7 @@ public:
                 for (int m = 0; m < MCp; m++) est[e].tps[m] = skip_hist[(size_t)e * MCp + m];
             }
         }
+        if (prof_mode >= 2) alg_stats(with_tp, nR, false);
         if (!any_keep || nR == 0) {
             // every estimator that stepped has now finished
             nP = 0;
@@ -793,16 +888,24 @@ public:
         if ((s = owner.ensure(nR + 1))) return s;
         if ((s = ensure_scan_scratch(nR + 1))) return s;
         MCE_CUDA(cudaMemsetAsync(head.ptr, 0xff, sizeof(int) * H, lc.stream));
+        pbeg(KID_FTR);
         Kernels<D>::ftr_insert(R, nR, cellq.ptr, head.ptr, next.ptr, H - 1, lc);
         Kernels<D>::ftr_preds(R, nR, cellq.ptr, head.ptr, next.ptr, H - 1, MC, nullptr, nullptr, npred.ptr, lc);
+        pend();
+        pbeg(KID_SCAN);
         scan_int_to_ll(npred.ptr, pred_off.ptr, nR, ss, lc);
+        pend();
         const long long npreds = read_ll(pred_off.ptr + nR);
         if ((s = preds.ensure(npreds + 1))) return s;
+        pbeg(KID_FTR);
         Kernels<D>::ftr_preds(R, nR, cellq.ptr, head.ptr, next.ptr, H - 1, MC, pred_off.ptr, preds.ptr, npred.ptr, lc);
         k_status_init(R, nR);
+        pend();
         for (int round = 0;; round++) {
             MCE_CUDA(cudaMemsetAsync(counters.ptr + 1, 0, sizeof(int), lc.stream));
+            pbeg(KID_FTR);
             ftr_resolve(pred_off.ptr, preds.ptr, nR, status.ptr, owner.ptr, counters.ptr + 1, lc);
+            pend();
             int unk = 0;
             MCE_CUDA(cudaMemcpyAsync(&unk, counters.ptr + 1, sizeof(int), cudaMemcpyDeviceToHost, lc.stream));
             MCE_CUDA(cudaStreamSynchronize(lc.stream));
@@ -819,26 +922,34 @@ public:
         if ((s = goff.ensure(nR + 2))) return s;
         MCE_CUDA(cudaMemsetAsync(gcnt.ptr, 0, sizeof(int) * (nR + 1), lc.stream));
         MCE_CUDA(cudaMemsetAsync(gfill.ptr, 0, sizeof(int) * (nR + 1), lc.stream));
+        pbeg(KID_GROUPS);
         group_count(status.ptr, owner.ptr, nR, gcnt.ptr, lc);
         scan_int_to_ll(gcnt.ptr, goff.ptr, nR, ss, lc);
+        pend();
         const long long nmembers = read_ll(goff.ptr + nR);
         if ((s = members.ensure(nmembers + 1))) return s;
+        pbeg(KID_GROUPS);
         group_fill(status.ptr, owner.ptr, nR, goff.ptr, gfill.ptr, members.ptr, lc);
         group_sort(gcnt.ptr, goff.ptr, nR, members.ptr, lc);
+        pend();
         if ((s = is_root.ensure(nR + 1))) return s;
         if ((s = cap.ensure(nR + 1))) return s;
         if ((s = rscan.ensure(nR + 2))) return s;
         if ((s = toff.ensure(nR + 2))) return s;
+        pbeg(KID_GROUPS);
         roots_flags(status.ptr, Rb.m.ptr, nR, D, is_root.ptr, cap.ptr, lc);
         scan_int_to_ll(is_root.ptr, rscan.ptr, nR, ss, lc);
         scan_int_to_ll(cap.ptr, toff.ptr, nR, ss, lc);
+        pend();
         long long t2[2];
         MCE_CUDA(cudaMemcpyAsync(&t2[0], rscan.ptr + nR, sizeof(long long), cudaMemcpyDeviceToHost, lc.stream));
         MCE_CUDA(cudaMemcpyAsync(&t2[1], toff.ptr + nR, sizeof(long long), cudaMemcpyDeviceToHost, lc.stream));
         MCE_CUDA(cudaStreamSynchronize(lc.stream));
         const long long nroots = t2[0], ttot = t2[1];
         if ((s = roots_list.ensure(nroots + 1))) return s;
+        pbeg(KID_GROUPS);
         mce::roots_list(is_root.ptr, rscan.ptr, nR, roots_list.ptr, lc);
+        pend();
         TBufs& Tn = Tb[cur ^ 1];
         if ((s = Tn.keys.ensure(ttot + 1))) return s;
         if ((s = Tn.vals.ensure(ttot + 1))) return s;
@@ -849,20 +960,25 @@ public:
         const int capMC = half_cells_cap(MC, D);
         const long long max_warps = (long long)lc.num_sms * 16 * 4;
         if ((s = scratch.ensure((size_t)max_warps * capMC))) return s;
+        pbeg(KID_GTABLE);
         Kernels<D>::gtable(R, roots_list.ptr, nroots, gcnt.ptr, goff.ptr, members.ptr, PV, Told, Bkeys.ptr, gscale.ptr,
                            toff.ptr, Tables{Tn.keys.ptr, Tn.vals.ptr}, tcnt.ptr, alive.ptr, src.ptr, scratch.ptr,
                            capMC, MC, err, lc);
+        pend();
+        if (prof_mode >= 2) alg_stats(with_tp, nR, true);
         // ---- next parent list
         if ((s = hist.ensure((size_t)E * MCp))) return s;
         if ((s = bucket_off.ensure((size_t)E * MCp + 2))) return s;
         if ((s = new_slot.ensure(nR + 1))) return s;
         if ((s = rbase.ensure(E + 2))) return s;
         MCE_CUDA(cudaMemsetAsync(hist.ptr, 0, sizeof(int) * E * MCp, lc.stream));
-        partition_count(alive.ptr, Rb.est.ptr, Rb.m.ptr, nR, MCp, hist.ptr, lc);
         if ((s = ensure_scan_scratch((long long)E * MCp + 1))) return s;
+        pbeg(KID_PARTITION);
+        partition_count(alive.ptr, Rb.est.ptr, Rb.m.ptr, nR, MCp, hist.ptr, lc);
         scan_int_to_ll(hist.ptr, bucket_off.ptr, (long long)E * MCp, ss, lc);
         rbase_kernel(dpstart.ptr, PV.kscan, E, rbase.ptr, lc);
         partition_rank(alive.ptr, Rb.m.ptr, rbase.ptr, E, MCp, bucket_off.ptr, new_slot.ptr, lc);
+        pend();
         h_hist.resize((size_t)E * MCp);
         MCE_CUDA(cudaMemcpyAsync(h_hist.data(), hist.ptr, sizeof(int) * E * MCp, cudaMemcpyDeviceToHost, lc.stream));
         MCE_CUDA(cudaStreamSynchronize(lc.stream));
@@ -875,7 +991,9 @@ public:
         const long long nPn = np[E];
         if ((s = Pn.ensure(nPn, MC))) return s;
         ParentList PnV = Pn.view();
+        pbeg(KID_PARTITION);
         Kernels<D>::compact(R, alive.ptr, src.ptr, nR, new_slot.ptr, toff.ptr, tcnt.ptr, PnV, MC, lc);
+        pend();
         for (int e = 0; e < E; e++) {
             if (!hsteps[e].active || hsteps[e].skip) continue;
             est[e].nt = np[e + 1] - np[e];
@@ -972,6 +1090,7 @@ static __global__ void k_gscale_kernel(const cd* est_raw, int NM, int E, double*
 template <int D>
 void Engine<D>::k_gscale_from_raw(int E_)
 {
+    ++g_launches;
     k_gscale_kernel<<<(E_ + 127) / 128, 128, 0, lc.stream>>>(est_raw.ptr, 1 + D + D * D, E_, gscale.ptr);
 }
 
@@ -989,6 +1108,7 @@ template <int D>
 void Engine<D>::k_skip_hist(ParentList PV, long long n, int MCp)
 {
     if (n == 0) return;
+    ++g_launches;
     k_skip_hist_kernel<D><<<(int)std::min<long long>((n + 255) / 256, lc.num_sms * 16), 256, 0, lc.stream>>>(
         PV, n, dsteps.ptr, MCp, hist.ptr);
 }
@@ -1001,7 +1121,93 @@ static __global__ void k_gather_kernel(const long long* scan, const long long* p
 template <int D>
 void Engine<D>::k_gather_bounds(const long long* scan, int E_)
 {
+    ++g_launches;
     k_gather_kernel<<<(E_ + 256) / 256, 256, 0, lc.stream>>>(scan, dpstart.ptr, E_, kall_est.ptr);
+}
+
+// Algorithmic traffic and FP64 work per kernel group (profiling mode 2).
+// Bytes count the data a kernel must move at least once (term records, table
+// cells, two parent-table lookups of one key and one complex value per g
+// evaluation); flops count FP64 operations of the formulas evaluated, with a
+// complex division as 11 and a complex product as 6.
+__device__ inline void acc_stat(double* alg, int kid, double bytes, double flops)
+{
+    atomicAdd(&alg[2 * kid], bytes);
+    atomicAdd(&alg[2 * kid + 1], flops);
+}
+
+template <int D>
+static __global__ void k_alg_parents(ParentList P, long long nP, const EstStep<D>* st, int with_tp,
+                                     const long long* kall_scan, double* alg)
+{
+    constexpr int NM = 1 + D + D * D;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nP; i += (long long)gridDim.x * blockDim.x) {
+        const EstStep<D>& S = st[P.est[i]];
+        const double m = P.m[i], phc = P.m_old[i], Cp = P.tab_cnt[i];
+        const double CB = S.skip ? 0.0 : (double)P.B_cnt[i];
+        const double K = (double)P.nkids_all[i];
+        const bool dce = with_tp && P.m[i] != P.m_old[i];
+        double f = 2 * m * D;
+        if (with_tp) f += 2 * phc * D * D + 2.0 * D * D + phc * (2 * D + 1);
+        acc_stat(alg, KID_TP, 8 * (phc * D + phc + D) + 8 * (m * D + m + D) + 16, f);
+        if (!S.skip) {
+            if (dce && P.m[i] > D) {
+                const double nc = (double)binom_ll(P.m[i], D);
+                acc_stat(alg, KID_BUILD_B, 8 * m * D + 4 * Cp + 4 * CB,
+                         nc * ((2.0 / 3.0) * D * D * D + 2.0 * D * D * D + 2.0 * D * D + 2 * (m - D) * D));
+            } else
+                acc_stat(alg, KID_BUILD_B, 8 * Cp, 0);
+        }
+        const double T = 1 + K;
+        double b = 8 * (m * D + m + D) + T * 2 * 20 + T * NM * 16;
+        double fl = m * (3 * D + 2) + T * (m * D + 4 * m * D + 8 * D + 14.0 * D * D + 22);
+        if (!S.skip) {
+            b += T * (8 * (m * D + 2 * m + D + 2) + 36 + 2 * m) + 8 * CB;
+            fl += K * (m * m * D + 3 * m * D);
+        }
+        acc_stat(alg, KID_MU, b, fl);
+        acc_stat(alg, KID_MOMENTS, T * NM * 16, T * 2 * NM);
+    }
+}
+
+template <int D>
+static __global__ void k_alg_roots(TermRecs R, long long nR, const int* status, const int* gcnt, const int* alive,
+                                   const int* tcnt, double* alg)
+{
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nR; j += (long long)gridDim.x * blockDim.x) {
+        if (R.est[j] < 0) continue;
+        const double m = R.m[j];
+        acc_stat(alg, KID_FTR, 8 * D + 16 * m + 16, 2 * D);
+        if (status[j] != 1) continue;
+        const double g = gcnt[j];
+        const double cells = alive[j] ? (double)tcnt[j] : 0.0;
+        acc_stat(alg, KID_GTABLE,
+                 (1 + g) * (8 * (m * D + 2 * m + D + 2) + 24) + cells * (1 + g) * 40 + cells * 20 + g * cells * 32,
+                 (1 + g) * cells * (2 * m + 22) + g * cells * 2);
+        if (alive[j]) acc_stat(alg, KID_PARTITION, 2 * (8 * (m * D + m + D) + 16), 0);
+    }
+}
+
+template <int D>
+void Engine<D>::alg_stats(bool with_tp, long long nR, bool tables_built)
+{
+    if (alg.ensure(2 * KID_COUNT)) return;
+    cudaMemsetAsync(alg.ptr, 0, sizeof(double) * 2 * KID_COUNT, lc.stream);
+    if (!tables_built) {
+        if (nP > 0)
+            k_alg_parents<D><<<(int)std::min<long long>((nP + 255) / 256, lc.num_sms * 8), 256, 0, lc.stream>>>(
+                Pb[cur].view(), nP, dsteps.ptr, with_tp ? 1 : 0, kall_scan.ptr, alg.ptr);
+    } else if (nR > 0) {
+        k_alg_roots<D><<<(int)std::min<long long>((nR + 255) / 256, lc.num_sms * 8), 256, 0, lc.stream>>>(
+            Rb.view(), nR, status.ptr, gcnt.ptr, alive.ptr, tcnt.ptr, alg.ptr);
+    }
+    double h[2 * KID_COUNT];
+    cudaMemcpyAsync(h, alg.ptr, sizeof(h), cudaMemcpyDeviceToHost, lc.stream);
+    cudaStreamSynchronize(lc.stream);
+    for (int k = 0; k < KID_COUNT; k++) {
+        kbytes[k] += h[2 * k];
+        kflops[k] += h[2 * k + 1];
+    }
 }
 
 static __global__ void k_status_init_kernel(const int* est, long long n, int* status)
@@ -1014,6 +1220,7 @@ template <int D>
 void Engine<D>::k_status_init(TermRecs R, long long nR)
 {
     if (nR == 0) return;
+    ++g_launches;
     k_status_init_kernel<<<(int)std::min<long long>((nR + 255) / 256, lc.num_sms * 16), 256, 0, lc.stream>>>(
         R.est, nR, status.ptr);
 }
@@ -1291,6 +1498,33 @@ int mce_set_window_number(mce_handle* h, int w)
     return MCE_OK;
 }
 double mce_last_step_ms(mce_handle* h) { return h ? h->eng->last_ms : -1.0; }
+double mce_device_time_ms(mce_handle* h) { return h ? h->eng->device_ms_total : -1.0; }
+long long mce_launch_count(mce_handle* h) { return h ? h->eng->launches : MCE_ERR_ARG; }
+int mce_set_profiling(mce_handle* h, int mode)
+{
+    if (!h || mode < 0 || mode > 2) return MCE_ERR_ARG;
+    h->eng->prof_mode = mode;
+    return MCE_OK;
+}
+int mce_clear_profile(mce_handle* h)
+{
+    if (!h) return MCE_ERR_ARG;
+    h->eng->clear_prof();
+    return MCE_OK;
+}
+int mce_num_kernel_groups(void) { return KID_COUNT; }
+const char* mce_kernel_group_name(int k) { return (k >= 0 && k < KID_COUNT) ? kKernelGroupNames[k] : ""; }
+int mce_kernel_group_stats(mce_handle* h, int k, double* ms, long long* launches, double* alg_bytes,
+                           double* alg_flops)
+{
+    if (!h || k < 0 || k >= KID_COUNT) return MCE_ERR_ARG;
+    EngineBase* g = h->eng;
+    if (ms) *ms = g->kms[k];
+    if (launches) *launches = g->klaunch[k];
+    if (alg_bytes) *alg_bytes = g->kbytes[k];
+    if (alg_flops) *alg_flops = g->kflops[k];
+    return MCE_OK;
+}
 void mce_destroy(mce_handle* h)
 {
     if (!h) return;

@@ -17,6 +17,10 @@
 
 namespace mce {
 
+#if MCE_COMMON_UNIT
+long long g_launches = 0;
+#endif
+
 static constexpr unsigned kFull = 0xffffffffu;
 
 __device__ inline void set_err(int* err, int bit)
@@ -124,15 +128,20 @@ static void scan_ll_inplace(long long* data, long long n, long long* scratch, lo
     const long long ntiles = (n + kScanTile - 1) / kScanTile;
     if (ntiles <= 1) {
         long long* ts = scratch;
+        ++g_launches;
         k_scan_tiles<long long><<<1, kScanThreads, 0, c.stream>>>(data, data, n, ts);
         // total: the single tile sum
+        ++g_launches;
         k_copy_ll<<<1, 32, 0, c.stream>>>(ts, data + n, 1);
         return;
     }
     long long* ts = scratch;  // ntiles + 1
+    ++g_launches;
     k_scan_tiles<long long><<<(unsigned)ntiles, kScanThreads, 0, c.stream>>>(data, data, n, ts);
     scan_ll_inplace(ts, ntiles, scratch + ntiles + 1, scratch_cap - (ntiles + 1), c);
+    ++g_launches;
     k_scan_add<<<(unsigned)ntiles, kScanThreads, 0, c.stream>>>(data, n, ts);
+    ++g_launches;
     k_write_total<<<1, 32, 0, c.stream>>>(data, n, ts, ntiles);
 }
 
@@ -144,13 +153,17 @@ void scan_int_to_ll(const int* in, long long* out, long long n, ScanScratch& s, 
         return;
     }
     long long* ts = s.block_sums;
+    ++g_launches;
     k_scan_tiles<int><<<(unsigned)ntiles, kScanThreads, 0, c.stream>>>(in, out, n, ts);
     if (ntiles == 1) {
+        ++g_launches;
         k_copy_ll<<<1, 32, 0, c.stream>>>(ts, out + n, 1);
         return;
     }
     scan_ll_inplace(ts, ntiles, s.block_sums + ntiles + 1, s.cap - (ntiles + 1), c);
+    ++g_launches;
     k_scan_add<<<(unsigned)ntiles, kScanThreads, 0, c.stream>>>(out, n, ts);
+    ++g_launches;
     k_write_total<<<1, 32, 0, c.stream>>>(out, n, ts, ntiles);
 }
 
@@ -1498,6 +1511,7 @@ __global__ void k_rbase(const long long* pstart, const long long* kscan, int E, 
 template <int D>
 void Kernels<D>::first_count(const double* A0, const EstStep<D>* st, int E, int* cnt, const LaunchCfg& c)
 {
+    ++g_launches;
     k_first_count<D><<<(E + 127) / 128, 128, 0, c.stream>>>(A0, st, E, cnt);
 }
 
@@ -1508,6 +1522,7 @@ void Kernels<D>::first_build(const double* A0, const double* p0, const double* b
 {
     // c_val, d_val and the H-orthogonal flags of the first terms ride in
     // spare parent-list arrays until the first tables are built.
+    ++g_launches;
     k_first_build<D><<<(E + 63) / 64, 64, 0, c.stream>>>(A0, p0, b0, st, roots, E, pstart, P, MC,
                                                          reinterpret_cast<double*>(P.kscan),
                                                          reinterpret_cast<double*>(P.B_off),
@@ -1519,6 +1534,7 @@ void Kernels<D>::first_tables(ParentList P, long long nP, const double* cval, co
                               const double* gscale, Tables T, int MC, const LaunchCfg& c)
 {
     const long long n = nP << (D - 1);
+    ++g_launches;
     k_first_tables<D><<<grid_for(n, 256, c.num_sms), 256, 0, c.stream>>>(P, nP, cval, dval, hof, gscale, T, MC);
 }
 
@@ -1527,6 +1543,7 @@ void Kernels<D>::tp(ParentList P, long long nP, const EstStep<D>* st, int with_t
                     const LaunchCfg& c)
 {
     if (nP == 0) return;
+    ++g_launches;
     k_tp<D><<<grid_for(nP, 128, c.num_sms), 128, 0, c.stream>>>(P, nP, st, with_tp, MC, Bcap, err);
 }
 
@@ -1562,6 +1579,7 @@ void Kernels<D>::mu(ParentList P, long long nP, const EstStep<D>* st, const long
     if (nP == 0) return;
     const int warps = 4;
     const size_t sm = (size_t)warps * ((MC + 1) * D + (MC + 1)) * sizeof(double);
+    ++g_launches;
     k_mu<D><<<grid_for(nP, warps, c.num_sms, 16), warps * 32, sm, c.stream>>>(P, nP, st, pstart, roots, Told,
                                                                               Bkeys, R, nR, kall_scan, contrib, MC,
                                                                               err);
@@ -1575,6 +1593,7 @@ void Kernels<D>::moments(const cd* contrib, const long long* pstart, const long 
     int g = (E + warps - 1) / warps;
     if (g > c.num_sms * 8) g = c.num_sms * 8;
     if (g < 1) g = 1;
+    ++g_launches;
     k_moments<D><<<g, warps * 32, 0, c.stream>>>(contrib, pstart, kall_scan, E, st, est_raw, gscale);
 }
 
@@ -1583,6 +1602,7 @@ void Kernels<D>::ftr_insert(TermRecs R, long long nR, long long* cellq, int* hea
                             const LaunchCfg& c)
 {
     if (nR == 0) return;
+    ++g_launches;
     k_ftr_insert<D><<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(R, nR, cellq, head, next, hmask);
 }
 
@@ -1592,6 +1612,7 @@ void Kernels<D>::ftr_preds(TermRecs R, long long nR, const long long* cellq, con
                            const LaunchCfg& c)
 {
     if (nR == 0) return;
+    ++g_launches;
     k_ftr_preds<D><<<grid_for(nR, 128, c.num_sms), 128, 0, c.stream>>>(R, nR, cellq, head, next, hmask, MC,
                                                                        pred_off, preds, npred);
 }
@@ -1618,6 +1639,7 @@ void Kernels<D>::gtable(TermRecs R, const int* roots_list, long long nroots, con
     const size_t sm = pw * warps;
     cudaFuncSetAttribute(k_gtable<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     const int grid = grid_for(nroots, warps, c.num_sms, 16);
+    ++g_launches;
     k_gtable<D><<<grid, warps * 32, sm, c.stream>>>(ctx, roots_list, nroots, gcnt, goff, members, gscale, toff, Tnew,
                                                     tcnt, alive, src, scratch, scratch_per_warp, err);
 }
@@ -1627,6 +1649,7 @@ void Kernels<D>::compact(TermRecs R, const int* alive, const int* src, long long
                          const long long* toff, const int* tcnt, ParentList Pn, int MC, const LaunchCfg& c)
 {
     if (nR == 0) return;
+    ++g_launches;
     k_compact<D><<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(R, alive, src, nR, new_slot, toff, tcnt, Pn, MC);
 }
 
@@ -1635,38 +1658,45 @@ void ftr_resolve(const long long* pred_off, const int* preds, long long nR, int*
                  const LaunchCfg& c)
 {
     if (nR == 0) return;
+    ++g_launches;
     k_ftr_resolve<<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(pred_off, preds, nR, status, owner, unknown);
 }
 void group_count(const int* status, const int* owner, long long nR, int* gcnt, const LaunchCfg& c)
 {
     if (nR == 0) return;
+    ++g_launches;
     k_group_count<<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(status, owner, nR, gcnt);
 }
 void group_fill(const int* status, const int* owner, long long nR, const long long* goff, int* gfill, int* members,
                 const LaunchCfg& c)
 {
     if (nR == 0) return;
+    ++g_launches;
     k_group_fill<<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(status, owner, nR, goff, gfill, members);
 }
 void group_sort(const int* gcnt, const long long* goff, long long nR, int* members, const LaunchCfg& c)
 {
     if (nR == 0) return;
+    ++g_launches;
     k_group_sort<<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(gcnt, goff, nR, members);
 }
 void roots_flags(const int* status, const int* m, long long nR, int D, int* is_root, int* cap, const LaunchCfg& c)
 {
     if (nR == 0) return;
+    ++g_launches;
     k_roots_flags<<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(status, m, nR, D, is_root, cap);
 }
 void roots_list(const int* is_root, const long long* rscan, long long nR, int* list, const LaunchCfg& c)
 {
     if (nR == 0) return;
+    ++g_launches;
     k_roots_list<<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(is_root, rscan, nR, list);
 }
 void partition_count(const int* alive, const int* est, const int* m, long long nR, int MCp, int* hist,
                      const LaunchCfg& c)
 {
     if (nR == 0) return;
+    ++g_launches;
     k_partition_count<<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(alive, est, m, nR, MCp, hist);
 }
 void partition_rank(const int* alive, const int* m, const long long* rbase, int E, int MCp,
@@ -1674,10 +1704,12 @@ void partition_rank(const int* alive, const int* m, const long long* rbase, int 
 {
     int g = E < c.num_sms * 8 ? E : c.num_sms * 8;
     if (g < 1) g = 1;
+    ++g_launches;
     k_partition_rank<<<g, 256, 0, c.stream>>>(alive, m, rbase, E, MCp, bucket_off, new_slot);
 }
 void rbase_kernel(const long long* pstart, const long long* kscan, int E, long long* rbase, const LaunchCfg& c)
 {
+    ++g_launches;
     k_rbase<<<(E + 1 + 255) / 256, 256, 0, c.stream>>>(pstart, kscan, E, rbase);
 }
 

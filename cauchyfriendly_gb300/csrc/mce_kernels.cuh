@@ -6,6 +6,9 @@
 
 namespace mce {
 
+// Kernels launched by this library since load (every launch site counts itself).
+extern long long g_launches;
+
 struct LaunchCfg {
     cudaStream_t stream;
     int num_sms;

@@ -112,8 +112,21 @@ int mce_reinitialize_start_statistics(mce_handle* h, int est, const double* A0, 
 int mce_set_master_step(mce_handle* h, int master_step);
 int mce_set_window_number(mce_handle* h, int win_num);
 
-/* Wall time of the device work of the last step (CUDA events), ms. */
+/* Device time of the last step and since creation / mce_clear_profile
+ * (CUDA events on the library's stream), ms. */
 double mce_last_step_ms(mce_handle* h);
+double mce_device_time_ms(mce_handle* h);
+/* Kernels launched by this handle since creation / mce_clear_profile. */
+long long mce_launch_count(mce_handle* h);
+/* Profiling: 0 off, 1 time each kernel group with CUDA events, 2 also
+ * accumulate each group's algorithmic bytes and FP64 flops (extra kernels and
+ * synchronisation; for an untimed pass). */
+int mce_set_profiling(mce_handle* h, int mode);
+int mce_clear_profile(mce_handle* h);
+int mce_num_kernel_groups(void);
+const char* mce_kernel_group_name(int group);
+int mce_kernel_group_stats(mce_handle* h, int group, double* ms, long long* launches, double* alg_bytes,
+                           double* alg_flops);
 
 void mce_destroy(mce_handle* h);
 
