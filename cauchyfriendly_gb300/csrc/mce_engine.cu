@@ -317,9 +317,11 @@ public:
     } Rb;
     DevBuf<cd> fam_mom, est_raw, scratch;
     DevBuf<double> gscale;
-    DevBuf<long long> cellq, pred_off, goff, toff, rscan, bucket_off, rbase, scan_tmp, kall_est;
-    DevBuf<int> head, next, npred, preds, status, owner, gcnt, gfill, members, is_root, cap, roots_list, alive, src,
-        tcnt, hist, new_slot, counters, first_cnt;
+    DevBuf<long long> pred_off, goff, toff, rscan, bucket_off, rbase, scan_tmp, kall_est;
+    DevBuf<int> npred, preds, status, owner, gcnt, gfill, members, members_tmp, is_root, cap, roots_list, alive, src,
+        tcnt, hist, new_slot, counters, first_cnt, bcount, bfill, slot_of;
+    DevBuf<long long> boff;
+    DevBuf<unsigned char> cell_ent;
     std::vector<cd> h_raw;
     std::vector<double> h_gscale;
     std::vector<int> h_hist;
@@ -878,19 +880,28 @@ public:
         }
         // ---- fast term reduction
         long long H = 1;
-        while (H < 2 * nR) H <<= 1;
-        if ((s = head.ensure(H))) return s;
-        if ((s = next.ensure(nR + 1))) return s;
-        if ((s = cellq.ensure(nR + 1))) return s;
+        while (H < nR) H <<= 1;
+        if ((s = bcount.ensure(H + 1))) return s;
+        if ((s = bfill.ensure(H + 1))) return s;
+        if ((s = boff.ensure(H + 2))) return s;
+        if ((s = slot_of.ensure(nR + 1))) return s;
+        if ((s = cell_ent.ensure((nR + 1) * Kernels<D>::cell_entry_bytes()))) return s;
         if ((s = npred.ensure(nR + 1))) return s;
         if ((s = pred_off.ensure(nR + 2))) return s;
         if ((s = status.ensure(nR + 1))) return s;
         if ((s = owner.ensure(nR + 1))) return s;
-        if ((s = ensure_scan_scratch(nR + 1))) return s;
-        MCE_CUDA(cudaMemsetAsync(head.ptr, 0xff, sizeof(int) * H, lc.stream));
+        if ((s = ensure_scan_scratch(std::max(nR, H) + 1))) return s;
+        MCE_CUDA(cudaMemsetAsync(bcount.ptr, 0, sizeof(int) * H, lc.stream));
+        MCE_CUDA(cudaMemsetAsync(bfill.ptr, 0, sizeof(int) * H, lc.stream));
         pbeg(KID_FTR);
-        Kernels<D>::ftr_insert(R, nR, cellq.ptr, head.ptr, next.ptr, H - 1, lc);
-        Kernels<D>::ftr_preds(R, nR, cellq.ptr, head.ptr, next.ptr, H - 1, MC, nullptr, nullptr, npred.ptr, lc);
+        Kernels<D>::ftr_cells(R, nR, H - 1, slot_of.ptr, bcount.ptr, lc);
+        pend();
+        pbeg(KID_SCAN);
+        scan_int_to_ll(bcount.ptr, boff.ptr, H, ss, lc);
+        pend();
+        pbeg(KID_FTR);
+        Kernels<D>::ftr_scatter(R, nR, slot_of.ptr, boff.ptr, bfill.ptr, cell_ent.ptr, lc);
+        Kernels<D>::ftr_preds(R, nR, cell_ent.ptr, boff.ptr, H - 1, MC, nullptr, nullptr, npred.ptr, lc);
         pend();
         pbeg(KID_SCAN);
         scan_int_to_ll(npred.ptr, pred_off.ptr, nR, ss, lc);
@@ -898,7 +909,7 @@ public:
         const long long npreds = read_ll(pred_off.ptr + nR);
         if ((s = preds.ensure(npreds + 1))) return s;
         pbeg(KID_FTR);
-        Kernels<D>::ftr_preds(R, nR, cellq.ptr, head.ptr, next.ptr, H - 1, MC, pred_off.ptr, preds.ptr, npred.ptr, lc);
+        Kernels<D>::ftr_preds(R, nR, cell_ent.ptr, boff.ptr, H - 1, MC, pred_off.ptr, preds.ptr, npred.ptr, lc);
         k_status_init(R, nR);
         pend();
         for (int round = 0;; round++) {
@@ -928,9 +939,10 @@ public:
         pend();
         const long long nmembers = read_ll(goff.ptr + nR);
         if ((s = members.ensure(nmembers + 1))) return s;
+        if ((s = members_tmp.ensure(nmembers + 1))) return s;
         pbeg(KID_GROUPS);
-        group_fill(status.ptr, owner.ptr, nR, goff.ptr, gfill.ptr, members.ptr, lc);
-        group_sort(gcnt.ptr, goff.ptr, nR, members.ptr, lc);
+        group_fill(status.ptr, owner.ptr, nR, goff.ptr, gfill.ptr, members_tmp.ptr, lc);
+        group_sort(gcnt.ptr, goff.ptr, nR, members_tmp.ptr, members.ptr, lc);
         pend();
         if ((s = is_root.ensure(nR + 1))) return s;
         if ((s = cap.ensure(nR + 1))) return s;

@@ -545,17 +545,12 @@ __global__ void k_build_B(ParentList P, long long nP, const EstStep<D>* st, int 
 }
 
 // ---------------------------------------------------------------------------
-// MU coalignment of one child record (cauchy_term.hpp:533-745), in place.
+// MU coalignment of one staged child (cauchy_term.hpp:533-745), in place on
+// the lane's shared-memory rows.  Returns the new row count.
 template <int D>
-__device__ inline int mu_coalign_rec(TermRecs R, long long s, int MC, int* err)
+__device__ inline int mu_coalign_smem(double* A, double* p, double* q, int m, unsigned& hof, signed char* cmap,
+                                      signed char* csmap, int* err)
 {
-    const int m = R.m[s];
-    double* A = R.A + s * MC * D;
-    double* p = R.p + s * MC;
-    double* q = R.q + s * MC;
-    signed char* cmap = R.cmap + s * MC;
-    signed char* csmap = R.csmap + s * MC;
-    unsigned hof = R.horthog[s];
     // normalize_hps(true): q keeps the un-normalised scales
     for (int i = 0; i < m; i++) {
         q[i] = p[i];
@@ -567,7 +562,7 @@ __device__ inline int mu_coalign_rec(TermRecs R, long long s, int MC, int* err)
     unsigned F = (m >= 32) ? kFull : ((1u << m) - 1);
     unsigned hf = hof;
     for (int j = 0; j < m; j++) {
-        cmap[j] = -1;  // 255 as uint8
+        cmap[j] = -1;  // 255 as uint8: no coalignment
         csmap[j] = 1;
     }
     int uc = 0;
@@ -629,30 +624,46 @@ __device__ inline int mu_coalign_rec(TermRecs R, long long s, int MC, int* err)
             int c = 0;
             for (int j = 0; j < m; j++)
                 if ((F >> j) & 1u) nh |= ((hf >> j) & 1u) << c++;
-            R.horthog[s] = nh;
+            hof = nh;
         }
-        R.m[s] = ns;
-        R.flags[s] |= kFlagHasCmap;
     }
     return ns;
 }
 
+// Shared memory of k_mu per warp, in doubles: MU rows and scales, then per
+// lane a staged term (A rows, p, q) and its moment contribution.
+__host__ __device__ inline int mu_warp_doubles(int MC, int D)
+{
+    const int NM = 1 + D + D * D;
+    return (MC + 1) * (D + 1) + 32 * (MC * D + 2 * MC) + 32 * 2 * NM + 16;
+}
+
 // Measurement update of every parent (cauchy_term.hpp:84-310), fused with the
 // g/yei evaluation of the parent and its children (cauchy_term.hpp:312-401),
-// the family's moment partial sums (cache_moments, cauchy_estimator.hpp:307),
-// the parent's re-normalisation and the children's MU coalignment.  One warp
-// per parent: lane l < m owns hyperplane l during the update, then lane t
-// owns child t (lane m owns the parent) for evaluation and coalignment.
+// the moment contributions (cache_moments, cauchy_estimator.hpp:307), the
+// parent's re-normalisation and the children's MU coalignment.  One warp per
+// parent: lane l < m owns hyperplane l during the update, then lane t stages
+// child t (lane m the parent) in shared memory for evaluation and
+// coalignment; the family's records and contributions leave with coalesced
+// warp-wide stores (children of a parent are contiguous in the records).
 template <int D>
-__global__ void k_mu(ParentList P, long long nP, const EstStep<D>* st, const long long* pstart,
-                     const double* roots, Tables Told, int* Bkeys, TermRecs R, long long nR,
-                     const long long* kall_scan, cd* contrib, int MC, int* err)
+__global__ void __launch_bounds__(128) k_mu(ParentList P, long long nP, const EstStep<D>* st, const long long* pstart,
+                                            const double* roots, Tables Told, int* Bkeys, TermRecs R, long long nR,
+                                            const long long* kall_scan, cd* contrib, int MC, int* err)
 {
     extern __shared__ double smem_d[];
     constexpr int NM = 1 + D + D * D;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
-    double* mu = smem_d + (size_t)wib * ((MC + 1) * D + (MC + 1));
+    const int RS = MC * D + 2 * MC;  // staged doubles per lane
+    double* wbase = smem_d + (size_t)wib * mu_warp_doubles(MC, D);
+    double* mu = wbase;
     double* rho = mu + (MC + 1) * D;
+    double* stage = rho + (MC + 1);
+    double* cstage = stage + 32 * RS;
+    int* rank2lane = reinterpret_cast<int*>(cstage + 32 * 2 * NM);  // child rank -> staging lane
+    double* At = stage + lane * RS;
+    double* pt = At + MC * D;
+    double* qt = pt + MC;
     for (long long i = (long long)blockIdx.x * nwb + wib; i < nP; i += (long long)gridDim.x * nwb) {
         const int e = P.est[i];
         const EstStep<D>& S = st[e];
@@ -695,87 +706,102 @@ __global__ void k_mu(ParentList P, long long nP, const EstStep<D>* st, const lon
         const int esg_c = (esg & (1 << (m - 1))) ? (esg ^ ((1 << m) - 1)) : esg;
         const bool write = !S.skip;
         const long long kbase = P.kscan[pstart[e]];
+        const long long pslot = i + kbase;                     // parent's record
+        const long long cslot0 = pstart[e + 1] + P.kscan[i];   // first child's record
+        const int nk = __popc(integ_mask);
         const bool mine = (lane < m) ? ((integ_mask >> lane) & 1u) : (lane == m);
-        cd acc[NM];
-        for (int k = 0; k < NM; k++) acc[k] = mkcd(0, 0);
+        // family order of this lane's term: parent 0, child c -> 1 + c
+        const int ford = (lane == m) ? 0 : 1 + __popc(integ_mask & ((1u << lane) - 1));
+        if (mine) rank2lane[ford] = lane;
+        int mfin = 0;
         if (mine) {
             const int t = lane;
-            long long slot;
-            if (t == m) slot = i + kbase;
-            else slot = pstart[e + 1] + P.kscan[i] + __popc(integ_mask & ((1u << t) - 1));
-            if (write && slot >= nR) {
-                set_err(err, kErrTableOverflow);
-            } else {
-                double bt[D], ty[D];
-                for (int j = 0; j < D; j++) {
-                    bt[j] = b[j] + zeta * mu[t * D + j];
-                    ty[j] = 0;
+            double bt[D], ty[D];
+            for (int j = 0; j < D; j++) {
+                bt[j] = b[j] + zeta * mu[t * D + j];
+                ty[j] = 0;
+            }
+            unsigned hof = 0;
+            int sneg = 0;
+            double ygi = 0;
+            int l = 0;
+            for (int ll = 0; ll <= m; ll++) {
+                if (ll == t) continue;
+                const bool fi = (ll < m) ? ((integ_mask >> ll) & 1u) : true;
+                double row[D];
+                if (fi)
+                    for (int j = 0; j < D; j++) row[j] = mu[ll * D + j] - mu[t * D + j];
+                else {
+                    for (int j = 0; j < D; j++) row[j] = mu[ll * D + j];
+                    hof |= 1u << l;
                 }
-                double* Ao = write ? R.A + slot * MC * D : nullptr;
-                double* po = write ? R.p + slot * MC : nullptr;
-                unsigned hof = 0;
-                int sneg = 0;
-                double ygi = 0;
-                int l = 0;
-                for (int ll = 0; ll <= m; ll++) {
-                    if (ll == t) continue;
-                    const bool fi = (ll < m) ? ((integ_mask >> ll) & 1u) : true;
-                    double row[D];
-                    if (fi)
-                        for (int j = 0; j < D; j++) row[j] = mu[ll * D + j] - mu[t * D + j];
-                    else {
-                        for (int j = 0; j < D; j++) row[j] = mu[ll * D + j];
-                        hof |= 1u << l;
-                    }
-                    const double pl = rho[ll];
-                    double s = 0.0;
-                    for (int j = 0; j < D; j++) s += row[j] * root[j];
-                    const double sg = s > 0 ? 1.0 : -1.0;
-                    if (sg < 0) sneg |= 1 << l;
-                    const double sc = pl * sg;
-                    for (int j = 0; j < D; j++) ty[j] += sc * row[j];
-                    if (!(hof & (1u << l))) ygi += pl * sg;
-                    if (write) {
-                        for (int j = 0; j < D; j++) Ao[l * D + j] = row[j];
-                        po[l] = pl;
-                    }
-                    l++;
-                }
-                // lambda keys into the parent table (cauchy_term.hpp:357-381)
-                int lp = 0, lm = 0, k = 0;
-                for (int l2 = 0; l2 < m; l2++) {
-                    if (k < phc) {
-                        if (k == t) {
-                            lm |= 1 << k;
-                            k++;
-                            if (k == phc) continue;
-                        }
-                        if ((sneg >> l2) & 1) {
-                            lp |= 1 << k;
-                            lm |= 1 << k;
-                        }
+                const double pl = rho[ll];
+                double s = 0.0;
+                for (int j = 0; j < D; j++) s += row[j] * root[j];
+                const double sg = s > 0 ? 1.0 : -1.0;
+                if (sg < 0) sneg |= 1 << l;
+                const double sc = pl * sg;
+                for (int j = 0; j < D; j++) ty[j] += sc * row[j];
+                if (!(hof & (1u << l))) ygi += pl * sg;
+                for (int j = 0; j < D; j++) At[l * D + j] = row[j];
+                pt[l] = pl;
+                l++;
+            }
+            // lambda keys into the parent table (cauchy_term.hpp:357-381)
+            int lp = 0, lm = 0, k = 0;
+            for (int l2 = 0; l2 < m; l2++) {
+                if (k < phc) {
+                    if (k == t) {
+                        lm |= 1 << k;
                         k++;
+                        if (k == phc) continue;
                     }
+                    if ((sneg >> l2) & 1) {
+                        lp |= 1 << k;
+                        lm |= 1 << k;
+                    }
+                    k++;
                 }
-                const int* pk = Told.keys + P.tab_off[i];
-                const cd* pv = Told.vals + P.tab_off[i];
-                const int pcnt = P.tab_cnt[i];
-                const cd gp = lookup_num(pk, pv, pcnt, lp ^ lhp, phc);
-                const cd gm = lookup_num(pk, pv, pcnt, lm ^ lhp, phc);
-                const double dv = rho[t];
-                cd g = csub(cdiv(gp, mkcd(ygi + dv, zeta)), cdiv(gm, mkcd(ygi - dv, zeta)));
-                g = cscale(g, kTwoPiInv);
-                acc[0] = g;
-                for (int j = 0; j < D; j++) {
-                    const cd y = mkcd(-ty[j], bt[j]);
-                    const cd gy = cmul(g, y);
-                    acc[1 + j] = gy;
-                    for (int kk = 0; kk < D; kk++) acc[1 + D + j * D + kk] = cmul(gy, mkcd(-ty[kk], bt[kk]));
-                }
-                if (write) {
+            }
+            const int* pk = Told.keys + P.tab_off[i];
+            const cd* pv = Told.vals + P.tab_off[i];
+            const int pcnt = P.tab_cnt[i];
+            const cd gp = lookup_num(pk, pv, pcnt, lp ^ lhp, phc);
+            const cd gm = lookup_num(pk, pv, pcnt, lm ^ lhp, phc);
+            const double dv = rho[t];
+            cd g = csub(cdiv(gp, mkcd(ygi + dv, zeta)), cdiv(gm, mkcd(ygi - dv, zeta)));
+            g = cscale(g, kTwoPiInv);
+            cd* cs = reinterpret_cast<cd*>(cstage) + lane * NM;
+            cs[0] = g;
+            for (int j = 0; j < D; j++) {
+                const cd y = mkcd(-ty[j], bt[j]);
+                const cd gy = cmul(g, y);
+                cs[1 + j] = gy;
+                for (int kk = 0; kk < D; kk++) cs[1 + D + j * D + kk] = cmul(gy, mkcd(-ty[kk], bt[kk]));
+            }
+            mfin = m;
+            if (write) {
+                const long long slot = (t == m) ? pslot : cslot0 + (ford - 1);
+                if (slot >= nR) {
+                    set_err(err, kErrTableOverflow);
+                } else {
+                    int flags = (t == m) ? 0 : kFlagNewChild;
+                    if (t == m) {
+                        // parent: normalize_hps(true), no coalignment
+                        for (int r = 0; r < m; r++) {
+                            qt[r] = pt[r];
+                            double n1 = 0;
+                            for (int j = 0; j < D; j++) n1 += fabs(At[r * D + j]);
+                            pt[r] *= n1;
+                            for (int j = 0; j < D; j++) At[r * D + j] /= n1;
+                        }
+                    } else {
+                        mfin = mu_coalign_smem<D>(At, pt, qt, m, hof, R.cmap + slot * MC, R.csmap + slot * MC, err);
+                        if (mfin != m) flags |= kFlagHasCmap;
+                    }
                     for (int j = 0; j < D; j++) R.b[slot * D + j] = bt[j];
                     R.est[slot] = e;
-                    R.m[slot] = m;
+                    R.m[slot] = mfin;
                     R.pbc[slot] = m;
                     R.phc[slot] = phc;
                     R.z[slot] = t;
@@ -784,34 +810,39 @@ __global__ void k_mu(ParentList P, long long nP, const EstStep<D>* st, const lon
                     R.horthog[slot] = hof;
                     R.cval[slot] = zeta;
                     R.dval[slot] = dv;
-                    R.flags[slot] = (t == m) ? 0 : kFlagNewChild;
-                    if (t == m) {
-                        // parent: normalize_hps(true), no coalignment
-                        double* q = R.q + slot * MC;
-                        for (int r = 0; r < m; r++) {
-                            q[r] = po[r];
-                            double n1 = 0;
-                            for (int j = 0; j < D; j++) n1 += fabs(Ao[r * D + j]);
-                            po[r] *= n1;
-                            for (int j = 0; j < D; j++) Ao[r * D + j] /= n1;
-                        }
-                    } else {
-                        mu_coalign_rec<D>(R, slot, MC, err);
-                    }
+                    R.flags[slot] = flags;
                 }
             }
         }
-        if (!write && lane == 0) {
-            // a final MU keeps no records; mark the parent's slot empty
-            const long long slot = i + kbase;
-            if (slot < nR) R.est[slot] = -1;
+        __syncwarp();
+        // moment contributions of the family in the reference's summation order
+        {
+            const long long fbase = i + kall_scan[i];
+            const int nterm = 1 + nk;
+            const double* cs = cstage;
+            double* out = reinterpret_cast<double*>(contrib + fbase * NM);
+            for (int x = lane; x < nterm * 2 * NM; x += 32) {
+                const int f = x / (2 * NM), o = x % (2 * NM);
+                // family position f -> staging lane
+                const int src_lane = rank2lane[f];
+                out[x] = cs[src_lane * 2 * NM + o];
+            }
         }
-        // this term's moment contribution, in the reference's summation order:
-        // the parent first, then its children by hyperplane (cache_moments)
-        if (mine) {
-            const long long pos = i + kall_scan[i] + (lane == m ? 0 : 1 + __popc(integ_mask & ((1u << lane) - 1)));
-            cd* out = contrib + pos * NM;
-            for (int k = 0; k < NM; k++) out[k] = acc[k];
+        if (write && pslot < nR && cslot0 + nk <= nR) {
+            // records: A, p, q rows of the family (rows padded to MC)
+            const int nterm = 1 + nk;
+            for (int x = lane; x < nterm * RS; x += 32) {
+                const int f = x / RS, o = x % RS;
+                const int src_lane = rank2lane[f];
+                const double v = stage[src_lane * RS + o];
+                const long long slot = (f == 0) ? pslot : cslot0 + (f - 1);
+                if (o < MC * D) R.A[slot * MC * D + o] = v;
+                else if (o < MC * D + MC) R.p[slot * MC + (o - MC * D)] = v;
+                else R.q[slot * MC + (o - MC * D - MC)] = v;
+            }
+        } else if (!write && lane == 0 && pslot < nR) {
+            // a final MU keeps no records; mark the parent's slot empty
+            R.est[pslot] = -1;
         }
         // parent B -> B_mu (cauchy_term.hpp:245-250)
         if (write) {
@@ -889,9 +920,16 @@ __global__ void k_moments(const cd* contrib, const long long* pstart, const long
 // not-yet-reduced term i in index order, takes every later unreduced term j
 // with qp-eps < b_j <= qp+eps on all axes (qp = b_i), |p_j - p_i| <= eps and
 // the hyperplane test, and reduces it into i (term_reduction.hpp:159-276).
-// Here candidate pairs come from a hash grid over (estimator, shape, cell of
-// b[0] at width 2 eps); the greedy index-order resolution is reproduced by
-// ftr_resolve.
+// Here candidates come from a grid over all coordinates of b with cells of
+// width 64 eps, keyed by (estimator, shape, cell): a near pair is at most one
+// cell apart per axis, and a term only probes the neighbour cell on an axis
+// when its +-3 eps window crosses the cell boundary (about 1.2 probes per term
+// in three dimensions).  Cells are counting-sorted into contiguous buckets
+// that carry b inline, so candidate scans read contiguous memory.  The greedy
+// index-order resolution of the reference is reproduced by ftr_resolve.
+constexpr double kCellWidth = 64.0 * kReductionEps;
+constexpr double kProbeHalfWidth = 3.0 * kReductionEps;
+
 __device__ inline unsigned long long mix64(unsigned long long x)
 {
     x ^= x >> 30;
@@ -903,43 +941,62 @@ __device__ inline unsigned long long mix64(unsigned long long x)
 }
 __device__ inline long long cell_of(double v)
 {
-    double q = floor(v / (2.0 * kReductionEps));
+    double q = floor(v / kCellWidth);
     if (!(q > -4.0e18)) q = -4.0e18;  // also catches NaN
     if (q > 4.0e18) q = 4.0e18;
     return (long long)q;
 }
-__device__ inline long long cell_slot(int e, int m, long long q, long long hmask)
+template <int D>
+__device__ inline long long cell_slot(int e, int m, const long long* c, long long hmask)
 {
-    unsigned long long h = mix64((unsigned long long)q * 0x9e3779b97f4a7c15ull ^ ((unsigned long long)e << 8) ^
-                                 (unsigned long long)m);
+    unsigned long long h = mix64(((unsigned long long)e << 8) ^ (unsigned long long)m);
+    for (int a = 0; a < D; a++) h = mix64(h ^ ((unsigned long long)c[a] * 0x9e3779b97f4a7c15ull));
     return (long long)(h & (unsigned long long)hmask);
 }
 
 template <int D>
-__global__ void k_ftr_insert(TermRecs R, long long nR, long long* cellq, int* head, int* next, long long hmask)
+struct CellEntry {
+    int idx;
+    int est_m;  // est << 5 | m
+    double b[D];
+};
+
+template <int D>
+__global__ void k_ftr_count_cells(TermRecs R, long long nR, long long hmask, int* slot_of, int* bcount)
 {
     for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nR; j += (long long)gridDim.x * blockDim.x) {
         const int e = R.est[j];
         if (e < 0) {
-            next[j] = -1;
+            slot_of[j] = -1;
             continue;
         }
-        const long long q = cell_of(R.b[j * D]);
-        cellq[j] = q;
-        const long long s = cell_slot(e, R.m[j], q, hmask);
-        next[j] = atomicExch(&head[s], (int)j);
+        long long c[D];
+        for (int a = 0; a < D; a++) c[a] = cell_of(R.b[j * D + a]);
+        const int s = (int)cell_slot<D>(e, R.m[j], c, hmask);
+        slot_of[j] = s;
+        atomicAdd(&bcount[s], 1);
     }
 }
 
 template <int D>
-__device__ inline bool ftr_near(const TermRecs& R, long long i, long long j, int m, int MC)
+__global__ void k_ftr_scatter(TermRecs R, long long nR, const int* slot_of, const long long* boff, int* bfill,
+                              CellEntry<D>* ent)
 {
-    const double* bi = R.b + i * D;
-    const double* bj = R.b + j * D;
-    for (int a = 0; a < D; a++) {
-        const double lo = bi[a] - kReductionEps, hi = bi[a] + kReductionEps;
-        if (!(bj[a] > lo && bj[a] <= hi)) return false;
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nR; j += (long long)gridDim.x * blockDim.x) {
+        const int s = slot_of[j];
+        if (s < 0) continue;
+        const long long pos = boff[s] + atomicAdd(&bfill[s], 1);
+        CellEntry<D> c;
+        c.idx = (int)j;
+        c.est_m = (R.est[j] << 5) | R.m[j];
+        for (int a = 0; a < D; a++) c.b[a] = R.b[j * D + a];
+        ent[pos] = c;
     }
+}
+
+template <int D>
+__device__ inline bool ftr_near_pm(const TermRecs& R, long long i, long long j, int m, int MC)
+{
     const double* pi = R.p + i * MC;
     const double* pj = R.p + j * MC;
     for (int k = 0; k < m; k++)
@@ -955,30 +1012,53 @@ __device__ inline bool ftr_near(const TermRecs& R, long long i, long long j, int
     return true;
 }
 
+// Near predecessors of every term: count pass (preds == nullptr) then fill pass.
 template <int D>
-__global__ void k_ftr_preds(TermRecs R, long long nR, const long long* cellq, const int* head, const int* next,
+__global__ void k_ftr_preds(TermRecs R, long long nR, const CellEntry<D>* ent, const long long* boff,
                             long long hmask, int MC, const long long* pred_off, int* preds, int* npred)
 {
     for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nR; j += (long long)gridDim.x * blockDim.x) {
         const int e = R.est[j];
-        int c = 0;
+        int cnt = 0;
         if (e >= 0) {
             const int m = R.m[j];
-            const long long qj = cellq[j];
-            for (int dq = -1; dq <= 1; dq++) {
-                const long long qq = qj + dq;
-                const long long s = cell_slot(e, m, qq, hmask);
-                long long guard = 0;
-                for (int i = head[s]; i >= 0 && guard <= nR; i = next[i], guard++) {
-                    if (i >= j) continue;
-                    if (cellq[i] != qq || R.est[i] != e || R.m[i] != m) continue;
-                    if (!ftr_near<D>(R, i, j, m, MC)) continue;
-                    if (preds) preds[pred_off[j] + c] = i;
-                    c++;
+            const int em = (e << 5) | m;
+            double bj[D];
+            long long lo[D], nc[D];
+            int nprobe = 1;
+            for (int a = 0; a < D; a++) {
+                bj[a] = R.b[j * D + a];
+                lo[a] = cell_of(bj[a] - kProbeHalfWidth);
+                const long long hi = cell_of(bj[a] + kProbeHalfWidth);
+                nc[a] = hi - lo[a] + 1;
+                if (nc[a] < 1) nc[a] = 1;
+                if (nc[a] > 2) nc[a] = 2;
+                nprobe *= (int)nc[a];
+            }
+            for (int pr = 0; pr < nprobe; pr++) {
+                long long c[D];
+                int rem = pr;
+                for (int a = 0; a < D; a++) {
+                    c[a] = lo[a] + (rem % nc[a]);
+                    rem /= (int)nc[a];
+                }
+                const long long s = cell_slot<D>(e, m, c, hmask);
+                for (long long k = boff[s]; k < boff[s + 1]; k++) {
+                    const CellEntry<D>& ce = ent[k];
+                    if (ce.idx >= j || ce.est_m != em) continue;
+                    bool ok = true;
+                    for (int a = 0; a < D && ok; a++) {
+                        if (cell_of(ce.b[a]) != c[a]) ok = false;
+                        const double lo_a = ce.b[a] - kReductionEps, hi_a = ce.b[a] + kReductionEps;
+                        if (!(bj[a] > lo_a && bj[a] <= hi_a)) ok = false;
+                    }
+                    if (!ok || !ftr_near_pm<D>(R, ce.idx, j, m, MC)) continue;
+                    if (preds) preds[pred_off[j] + cnt] = ce.idx;
+                    cnt++;
                 }
             }
         }
-        if (!preds) npred[j] = c;
+        if (!preds) npred[j] = cnt;
     }
 }
 
@@ -1023,20 +1103,23 @@ __global__ void k_group_fill(const int* status, const int* owner, long long nR, 
         }
 }
 
-__global__ void k_group_sort(const int* gcnt, const long long* goff, long long nR, int* members)
+// Member lists in ascending index order (the forward flag array's order,
+// cauchy_util.hpp:387-410): one warp per group ranks each member by counting
+// smaller ones.
+__global__ void k_group_sort(const int* gcnt, const long long* goff, long long nR, const int* members_in,
+                             int* members_out)
 {
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < nR; r += (long long)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+    for (long long r = (long long)blockIdx.x * nwb + wib; r < nR; r += (long long)gridDim.x * nwb) {
         const int n = gcnt[r];
-        if (n < 2) continue;
-        int* a = members + goff[r];
-        for (int x = 1; x < n; x++) {
+        if (n == 0) continue;
+        const int* a = members_in + goff[r];
+        int* o = members_out + goff[r];
+        for (int x = lane; x < n; x += 32) {
             const int v = a[x];
-            int y = x - 1;
-            while (y >= 0 && a[y] > v) {
-                a[y + 1] = a[y];
-                y--;
-            }
-            a[y + 1] = v;
+            int rank = 0;
+            for (int y = 0; y < n; y++) rank += a[y] < v;
+            o[rank] = v;
         }
     }
 }
@@ -1577,8 +1660,12 @@ void Kernels<D>::mu(ParentList P, long long nP, const EstStep<D>* st, const long
                     int MC, int* err, const LaunchCfg& c)
 {
     if (nP == 0) return;
-    const int warps = 4;
-    const size_t sm = (size_t)warps * ((MC + 1) * D + (MC + 1)) * sizeof(double);
+    const size_t pw = (size_t)mu_warp_doubles(MC, D) * sizeof(double);
+    int warps = (int)(200 * 1024 / pw);
+    if (warps > 4) warps = 4;
+    if (warps < 1) warps = 1;
+    const size_t sm = pw * warps;
+    cudaFuncSetAttribute(k_mu<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     ++g_launches;
     k_mu<D><<<grid_for(nP, warps, c.num_sms, 16), warps * 32, sm, c.stream>>>(P, nP, st, pstart, roots, Told,
                                                                               Bkeys, R, nR, kall_scan, contrib, MC,
@@ -1598,23 +1685,37 @@ void Kernels<D>::moments(const cd* contrib, const long long* pstart, const long 
 }
 
 template <int D>
-void Kernels<D>::ftr_insert(TermRecs R, long long nR, long long* cellq, int* head, int* next, long long hmask,
-                            const LaunchCfg& c)
+void Kernels<D>::ftr_cells(TermRecs R, long long nR, long long hmask, int* slot_of, int* bcount, const LaunchCfg& c)
 {
     if (nR == 0) return;
     ++g_launches;
-    k_ftr_insert<D><<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(R, nR, cellq, head, next, hmask);
+    k_ftr_count_cells<D><<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(R, nR, hmask, slot_of, bcount);
 }
 
 template <int D>
-void Kernels<D>::ftr_preds(TermRecs R, long long nR, const long long* cellq, const int* head, const int* next,
-                           long long hmask, int MC, const long long* pred_off, int* preds, int* npred,
-                           const LaunchCfg& c)
+void Kernels<D>::ftr_scatter(TermRecs R, long long nR, const int* slot_of, const long long* boff, int* bfill,
+                             void* ent, const LaunchCfg& c)
 {
     if (nR == 0) return;
     ++g_launches;
-    k_ftr_preds<D><<<grid_for(nR, 128, c.num_sms), 128, 0, c.stream>>>(R, nR, cellq, head, next, hmask, MC,
-                                                                       pred_off, preds, npred);
+    k_ftr_scatter<D><<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(R, nR, slot_of, boff, bfill,
+                                                                         static_cast<CellEntry<D>*>(ent));
+}
+
+template <int D>
+size_t Kernels<D>::cell_entry_bytes()
+{
+    return sizeof(CellEntry<D>);
+}
+
+template <int D>
+void Kernels<D>::ftr_preds(TermRecs R, long long nR, const void* ent, const long long* boff, long long hmask, int MC,
+                           const long long* pred_off, int* preds, int* npred, const LaunchCfg& c)
+{
+    if (nR == 0) return;
+    ++g_launches;
+    k_ftr_preds<D><<<grid_for(nR, 128, c.num_sms), 128, 0, c.stream>>>(
+        R, nR, static_cast<const CellEntry<D>*>(ent), boff, hmask, MC, pred_off, preds, npred);
 }
 
 static inline size_t gtable_smem_per_warp(int MC, int D)
@@ -1674,11 +1775,12 @@ void group_fill(const int* status, const int* owner, long long nR, const long lo
     ++g_launches;
     k_group_fill<<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(status, owner, nR, goff, gfill, members);
 }
-void group_sort(const int* gcnt, const long long* goff, long long nR, int* members, const LaunchCfg& c)
+void group_sort(const int* gcnt, const long long* goff, long long nR, const int* members_in, int* members_out,
+                const LaunchCfg& c)
 {
     if (nR == 0) return;
     ++g_launches;
-    k_group_sort<<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(gcnt, goff, nR, members);
+    k_group_sort<<<grid_for(nR, 8, c.num_sms), 256, 0, c.stream>>>(gcnt, goff, nR, members_in, members_out);
 }
 void roots_flags(const int* status, const int* m, long long nR, int D, int* is_root, int* cap, const LaunchCfg& c)
 {

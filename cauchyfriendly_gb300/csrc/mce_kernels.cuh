@@ -48,12 +48,14 @@ struct Kernels {
     // (cauchy_estimator.hpp:307-357).
     static void moments(const cd* contrib, const long long* pstart, const long long* kall_scan, int E,
                         const EstStep<D>* st, cd* est_raw, double* gscale, const LaunchCfg& c);
-    // Fast term reduction (term_reduction.hpp:159-276) over the post-MU records.
-    static void ftr_insert(TermRecs R, long long nR, long long* cellq, int* head, int* next, long long hmask,
-                           const LaunchCfg& c);
-    static void ftr_preds(TermRecs R, long long nR, const long long* cellq, const int* head, const int* next,
-                          long long hmask, int MC, const long long* pred_off, int* preds, int* npred,
-                          const LaunchCfg& c);
+    // Fast term reduction (term_reduction.hpp:159-276) over the post-MU records:
+    // grid cells of b, counting-sorted buckets, near predecessors.
+    static void ftr_cells(TermRecs R, long long nR, long long hmask, int* slot_of, int* bcount, const LaunchCfg& c);
+    static void ftr_scatter(TermRecs R, long long nR, const int* slot_of, const long long* boff, int* bfill,
+                            void* ent, const LaunchCfg& c);
+    static size_t cell_entry_bytes();
+    static void ftr_preds(TermRecs R, long long nR, const void* ent, const long long* boff, long long hmask, int MC,
+                          const long long* pred_off, int* preds, int* npred, const LaunchCfg& c);
     // g-tables of every reduction group (flattening.hpp:318-568).
     static void gtable(TermRecs R, const int* roots_list, long long nroots, const int* gcnt,
                        const long long* goff, const int* members, ParentList P, Tables Told, const int* Bkeys,
@@ -71,7 +73,8 @@ void ftr_resolve(const long long* pred_off, const int* preds, long long nR, int*
 void group_count(const int* status, const int* owner, long long nR, int* gcnt, const LaunchCfg& c);
 void group_fill(const int* status, const int* owner, long long nR, const long long* goff, int* gfill,
                 int* members, const LaunchCfg& c);
-void group_sort(const int* gcnt, const long long* goff, long long nR, int* members, const LaunchCfg& c);
+void group_sort(const int* gcnt, const long long* goff, long long nR, const int* members_in, int* members_out,
+                const LaunchCfg& c);
 void roots_flags(const int* status, const int* m, long long nR, int D, int* is_root, int* cap,
                  const LaunchCfg& c);
 void roots_list(const int* is_root, const long long* rscan, long long nR, int* list, const LaunchCfg& c);

@@ -1,0 +1,183 @@
+"""Drop-in replacement of the reference's SWIG module ``pycauchy`` for the
+single-estimator step path, backed by libmce_gb300.so.
+
+Same function names, argument order and return tuples as the SWIG wrappers in
+scripts/swig/cauchy/pycauchy.hpp / pycauchy.i, so the reference's
+``cauchy_estimator.PyCauchyEstimator`` runs on the GPU when this module is
+importable as ``pycauchy``.  Numpy arrays come in flattened (the numpy.i
+IN_ARRAY1 typemaps) and go out as float64 / int32 arrays (ARGOUTVIEWM_ARRAY1).
+
+Covered: pycauchy_initialize_lti / _ltv, pycauchy_single_step_ltiv,
+_get_number_of_terms, _set_master_step, _set_window_number, _get_duc, _reset,
+_shutdown, pycauchy_set_tr_search_idxs_ordering.  The window manager, the
+nonlinear (extended) mode, CPDF grids and relative-system functions of the
+SWIG module are not provided by this build.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+
+import numpy as np
+
+from .estimator import CauchyEstimator
+
+
+class C_CauchyDynamicsUpdateContainer(ct.Structure):
+    """Layout of CauchyDynamicsUpdateContainer (include/dynamic_models.hpp:62-80),
+    the struct LTV callbacks receive."""
+    _fields_ = [("x", ct.POINTER(ct.c_double)), ("u", ct.POINTER(ct.c_double)), ("dt", ct.c_double),
+                ("step", ct.c_int), ("n", ct.c_int), ("cmcc", ct.c_int), ("pncc", ct.c_int), ("p", ct.c_int),
+                ("Phi", ct.POINTER(ct.c_double)), ("Gamma", ct.POINTER(ct.c_double)), ("B", ct.POINTER(ct.c_double)),
+                ("H", ct.POINTER(ct.c_double)), ("beta", ct.POINTER(ct.c_double)), ("gamma", ct.POINTER(ct.c_double)),
+                ("is_xbar_set_for_ece", ct.c_bool), ("other_stuff", ct.c_void_p)]
+
+
+_CALLBACK = ct.CFUNCTYPE(None, ct.POINTER(C_CauchyDynamicsUpdateContainer))
+
+
+class _Handle:
+    """What pycauchy_initialize_* returns: the estimator plus the dynamics
+    container (pycauchy.hpp:240-280 PyCauchyDataHandler)."""
+
+    def __init__(self, num_steps, A0, p0, b0, Phi, Gamma, B, beta, H, gamma, dt, init_step, debug_print):
+        n = int(np.asarray(b0).size)
+        self.n = n
+        self.pncc = int(np.asarray(beta).size)
+        self.cmcc = int(np.asarray(B).size) // n
+        self.p = int(np.asarray(gamma).size)
+        f = lambda a, size: (np.zeros(size) if a is None or np.asarray(a).size == 0
+                             else np.array(a, dtype=np.float64).reshape(-1))
+        # dynamics container storage (owned here, pointed to by the C struct)
+        self.x = np.zeros(n)
+        self.u = np.zeros(max(self.cmcc, 1))
+        self.Phi = f(Phi, n * n)
+        self.Gamma = f(Gamma, n * self.pncc)
+        self.B = f(B, n * self.cmcc)
+        self.H = f(H, self.p * n)
+        self.beta = f(beta, self.pncc)
+        self.gamma = f(gamma, self.p)
+        self.duc = C_CauchyDynamicsUpdateContainer()
+        P = lambda a: a.ctypes.data_as(ct.POINTER(ct.c_double))
+        self.duc.x, self.duc.u = P(self.x), P(self.u)
+        self.duc.dt, self.duc.step = float(dt), int(init_step)
+        self.duc.n, self.duc.cmcc, self.duc.pncc, self.duc.p = n, self.cmcc, self.pncc, self.p
+        self.duc.Phi, self.duc.Gamma, self.duc.B = P(self.Phi), P(self.Gamma), P(self.B)
+        self.duc.H, self.duc.beta, self.duc.gamma = P(self.H), P(self.beta), P(self.gamma)
+        self.duc.is_xbar_set_for_ece = False
+        self.duc.other_stuff = None
+        self.callback = None
+        self.est = CauchyEstimator(np.asarray(A0, dtype=np.float64).reshape(n, n), p0, b0, int(num_steps), n,
+                                   self.cmcc, self.pncc, self.p, bool(debug_print))
+
+
+def pycauchy_initialize_lti(num_steps, A0, p0, b0, Phi, Gamma, B, beta, H, gamma, dt, init_step, debug_print):
+    """pycauchy.hpp:295-328"""
+    return _Handle(num_steps, A0, p0, b0, Phi, Gamma, B, beta, H, gamma, dt, init_step, debug_print)
+
+
+def pycauchy_initialize_ltv(num_steps, A0, p0, b0, Phi, Gamma, B, beta, H, gamma, f_dyn_update_callback, dt,
+                            init_step, debug_print):
+    """pycauchy.hpp:330-363; the callback is a raw C function pointer (int)."""
+    h = _Handle(num_steps, A0, p0, b0, Phi, Gamma, B, beta, H, gamma, dt, init_step, debug_print)
+    h.callback = _CALLBACK(int(f_dyn_update_callback))
+    return h
+
+
+def pycauchy_single_step_ltiv(h, msmts, controls):
+    """pycauchy.hpp:461-543: steps the estimator through len(msmts) scalar
+    measurements (the last len(msmts) of the p per step) and returns
+    (Phi, Gamma, B, H, beta, gamma, fz, xhat, Phat, cerr_fz, cerr_xhat,
+    cerr_Phat, err_code)."""
+    msmts = np.atleast_1d(np.asarray(msmts, dtype=np.float64)).reshape(-1)
+    controls = np.atleast_1d(np.asarray(controls, dtype=np.float64)).reshape(-1)
+    n, p, k = h.n, h.p, msmts.size
+    assert p >= k
+    if h.cmcc > 0:
+        h.u[:h.cmcc] = controls[:h.cmcc]
+    start = p - k
+    empty = np.array([], dtype=np.float64)
+    outs = [empty] * 6
+    if h.callback is not None:
+        h.x[:] = np.real(h.est.moments()["mean"]) if h.est.master_step() > 0 else h.x
+        h.callback(ct.pointer(h.duc))
+        outs = [h.Phi.copy(), h.Gamma.copy(), h.B.copy(), h.H[start * n:(start + k) * n].copy(), h.beta.copy(),
+                h.gamma[start:start + k].copy()]
+    fz = np.zeros(k)
+    xhat = np.zeros(k * n)
+    Phat = np.zeros(k * n * n)
+    cfz = np.zeros(k)
+    cx = np.zeros(k)
+    cP = np.zeros(k)
+    err = np.zeros(k, dtype=np.int32)
+    Phi = h.Phi.reshape(n, n)
+    Gamma = h.Gamma.reshape(n, h.pncc) if h.pncc else None
+    B = h.B.reshape(n, h.cmcc) if h.cmcc else None
+    u = h.u[:h.cmcc] if h.cmcc else None
+    for i in range(k):
+        idx = start + i
+        err[i] = h.est.step(msmts[i], Phi, Gamma, h.beta if h.pncc else None, h.H[idx * n:(idx + 1) * n],
+                            h.gamma[idx], B, u)
+        mo = h.est.moments()
+        fz[i] = mo["fz"].real
+        cfz[i] = mo["fz"].imag
+        xhat[i * n:(i + 1) * n] = mo["mean"].real
+        Phat[i * n * n:(i + 1) * n * n] = mo["cov"].real.reshape(-1)
+        cx[i] = np.max(np.abs(mo["mean"].imag))
+        cP[i] = np.max(np.abs(mo["cov"].imag))
+    return (*outs, fz, xhat, Phat, cfz, cx, cP, err)
+
+
+def pycauchy_single_step_get_number_of_terms(h):
+    """pycauchy.hpp:666"""
+    return h.est.num_terms()
+
+
+def pycauchy_single_step_set_master_step(h, step):
+    """pycauchy.hpp:767"""
+    h.est.set_master_step(int(step))
+
+
+def pycauchy_single_step_set_window_number(h, win_num):
+    """pycauchy.hpp:779"""
+    h.est.set_win_num(int(win_num))
+
+
+def pycauchy_single_step_get_duc(h):
+    """pycauchy.hpp:791: address of the dynamics container."""
+    return ct.addressof(h.duc)
+
+
+def pycauchy_single_step_reset(h, A0, p0, b0, xbar):
+    """pycauchy.hpp:798-819: new start statistics (empty arrays keep the old
+    ones), optional xbar into the container, then reset."""
+    n = h.n
+    A0 = np.asarray(A0, dtype=np.float64).reshape(-1)
+    p0 = np.asarray(p0, dtype=np.float64).reshape(-1)
+    b0 = np.asarray(b0, dtype=np.float64).reshape(-1)
+    xbar = np.asarray(xbar, dtype=np.float64).reshape(-1)
+    if A0.size or p0.size or b0.size:
+        cur = h.est
+        a = A0 if A0.size else None
+        pp = p0 if p0.size else None
+        bb = b0 if b0.size else None
+        if a is None or pp is None or bb is None:
+            raise ValueError("partial start statistics are not supported; pass A0, p0 and b0")
+        cur.reinitialize_start_statistics(a.reshape(n, n), pp, bb)
+    if xbar.size:
+        h.x[:] = xbar
+    h.est.reset()
+
+
+def pycauchy_single_step_shutdown(h):
+    """pycauchy.hpp:752"""
+    h.est.close()
+
+
+def pycauchy_set_tr_search_idxs_ordering(ordering):
+    """pycauchy.hpp:994.  The axis order only changes how the reference walks
+    its sorted candidate lists; the reduction groups are the same for every
+    order, so the ordering is accepted and has no effect here."""
+    ordering = np.asarray(ordering).reshape(-1)
+    if ordering.size > 12:
+        return 1
+    return 0
