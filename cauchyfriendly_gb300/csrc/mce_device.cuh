@@ -62,6 +62,38 @@ __device__ inline cd cdiv(cd x, cd y)
     return cd{(b * r + a) / den, (b - a * r) / den};
 }
 
+// Comparisons of doubles on their bit patterns (integer pipe).  IEEE doubles
+// order like sign-magnitude integers, so these give the same answers as the
+// floating-point comparisons for every non-NaN operand (-0 and +0 included).
+__device__ inline unsigned long long dabs_bits(double x)
+{
+    return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+}
+// |x| < c for c > 0
+__device__ inline bool abs_lt(double x, double c)
+{
+    return dabs_bits(x) < (unsigned long long)__double_as_longlong(c);
+}
+// |x| > |y|
+__device__ inline bool abs_gt(double x, double y) { return dabs_bits(x) > dabs_bits(y); }
+// x > 0
+__device__ inline bool pos(double x) { return __double_as_longlong(x) > 0; }
+// x < 0
+__device__ inline bool neg(double x)
+{
+    const long long b = __double_as_longlong(x);
+    return b < 0 && (b & 0x7fffffffffffffffLL) != 0;
+}
+// Order-preserving integer key: +x -> bits, -x -> -(magnitude bits).
+__device__ inline long long dkey(double x)
+{
+    const long long b = __double_as_longlong(x);
+    return (b >= 0) ? b : -(b & 0x7fffffffffffffffLL);
+}
+// a < b and a <= b (keys map -0 and +0 to the same value)
+__device__ inline bool dlt(double a, double b) { return dkey(a) < dkey(b); }
+__device__ inline bool dle(double a, double b) { return dkey(a) <= dkey(b); }
+
 // Binary search over ascending keys (gtable.hpp:283-301 semantics).
 __device__ inline int bsearch_key(const int* __restrict__ keys, int n, int key)
 {
@@ -119,14 +151,14 @@ __host__ __device__ inline int half_cells_cap(int m, int d)
 template <int D>
 __device__ inline int coalign_gate(const double* r, const double* c)
 {
-    bool pos = true, neg = true;
+    bool ps = true, ng = true;
 #pragma unroll
     for (int l = 0; l < D; l++) {
-        if (pos) pos &= fabs(r[l] - c[l]) < kCoalignEps;
-        if (neg) neg &= fabs(r[l] + c[l]) < kCoalignEps;
-        if (!(pos || neg)) break;
+        if (ps) ps &= abs_lt(r[l] - c[l], kCoalignEps);
+        if (ng) ng &= abs_lt(r[l] + c[l], kCoalignEps);
+        if (!(ps || ng)) break;
     }
-    return pos ? 1 : (neg ? -1 : 0);
+    return ps ? 1 : (ng ? -1 : 0);
 }
 
 // Orientation mask of two equal arrangements: for each row, the first
@@ -137,7 +169,7 @@ __device__ inline int orientation_mask(const double* Ai, const double* Aj, int m
     int s = 0;
     for (int k = 0; k < m; k++) {
         int l = 0;
-        while (l < D - 1 && (fabs(Ai[k * D + l]) < kReductionEps || fabs(Aj[k * D + l]) < kReductionEps)) l++;
+        while (l < D - 1 && (abs_lt(Ai[k * D + l], kReductionEps) || abs_lt(Aj[k * D + l], kReductionEps))) l++;
         if (Ai[k * D + l] * Aj[k * D + l] < 0) s |= 1 << k;
     }
     return s;
@@ -153,7 +185,7 @@ __device__ inline bool plu(double* A, int* P)
         double piv = kPluEps;
         int pi = -1;
         for (int i = j; i < D; i++)
-            if (fabs(A[i * D + j]) > fabs(piv)) {
+            if (abs_gt(A[i * D + j], piv)) {
                 piv = A[i * D + j];
                 pi = i;
             }
@@ -207,8 +239,41 @@ __device__ inline void lu_solve_inplace(const double* LU, double* x)
     }
 }
 
+template <int D>
+__device__ inline double cond1_from_lu(const double* A, const int* P, double nrm);
+
+// Upper bound on the 1-norm of (LU)^-1 from packed factors with partial
+// pivoting: ||A^-1|| <= ||M(U)^-1|| ||L^-1|| with M(U) the comparison matrix
+// of U (|u_ii| on the diagonal, -|u_ij| above) and ||L^-1||_1 <= 2^(D-1) since
+// |l_ij| <= 1.  M(U)^-1 is non-negative, so its column sums are computed by a
+// cancellation-free back substitution in single precision, then inflated by a
+// margin that covers the rounding.  Returns +inf when it cannot bound.
+template <int D>
+__device__ inline float inv_norm1_bound(const double* LU)
+{
+    float Ua[D * D];
+    for (int i = 0; i < D; i++)
+        for (int j = i; j < D; j++) Ua[i * D + j] = fabsf(__double2float_ru(fabs(LU[i * D + j])));
+    float best = 0.f;
+    for (int k = 0; k < D; k++) {
+        float x[D];
+        float colsum = 0.f;
+        for (int i = k; i >= 0; i--) {
+            float acc = (i == k) ? 1.f : 0.f;
+            for (int j = i + 1; j <= k; j++) acc += Ua[i * D + j] * x[j];
+            // a lower bound of |u_ii| keeps the quotient an upper bound
+            const float den = __double2float_rd(fabs(LU[i * D + i]));
+            x[i] = acc / den;
+            colsum += x[i];
+        }
+        best = fmaxf(best, colsum);
+    }
+    // row sums of |M(U)^-1| in 1-norm sense: column sums as computed above bound ||M(U)^-1||_1
+    return best * (float)(1 << (D - 1)) * 1.0001f;
+}
+
 // 1-norm condition number through the explicit inverse; on success A holds
-// the packed LU factors and P the pivots.  Returns +inf when PLU fails.
+// the packed LU factors and P the pivots.  Returns DBL_MAX when PLU fails.
 template <int D>
 __device__ inline double cond1(double* A, int* P)
 {
@@ -218,12 +283,21 @@ __device__ inline double cond1(double* A, int* P)
         double s = 0;
 #pragma unroll
         for (int r = 0; r < D; r++) s += fabs(A[r * D + c]);
-        if (s > nrm) nrm = s;
+        if (dlt(nrm, s)) nrm = s;
     }
     if (!plu<D>(A, P)) return 1.79769313486231570815e+308;
+    return cond1_from_lu<D>(A, P, nrm);
+}
+
+// The second half of cond1: 1-norm of the explicit inverse from the packed LU
+// factors, times the 1-norm of A (cauchy_linalg.hpp:1369-1389).
+template <int D>
+__device__ inline double cond1_from_lu(const double* A, const int* P, double nrm)
+{
     int PT[D];
     inverse_perm<D>(P, PT);
     double inrm = -1;
+    (void)A;
 #pragma unroll
     for (int i = 0; i < D; i++) {
         double w[D];
@@ -233,7 +307,7 @@ __device__ inline double cond1(double* A, int* P)
         double s = 0;
 #pragma unroll
         for (int j = 0; j < D; j++) s += fabs(w[j]);
-        if (s > inrm) inrm = s;
+        if (dlt(inrm, s)) inrm = s;
     }
     return nrm * inrm;
 }

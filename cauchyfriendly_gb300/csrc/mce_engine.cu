@@ -317,11 +317,13 @@ public:
     } Rb;
     DevBuf<cd> fam_mom, est_raw, scratch;
     DevBuf<double> gscale;
-    DevBuf<long long> pred_off, goff, toff, rscan, bucket_off, rbase, scan_tmp, kall_est;
-    DevBuf<int> npred, preds, status, owner, gcnt, gfill, members, members_tmp, is_root, cap, roots_list, alive, src,
+    DevBuf<long long> goff, toff, rscan, bucket_off, rbase, scan_tmp, kall_est;
+    DevBuf<int> status, owner, gcnt, gfill, members, members_tmp, is_root, cap, roots_list, alive, src,
         tcnt, hist, new_slot, counters, first_cnt, bcount, bfill, slot_of;
     DevBuf<long long> boff;
-    DevBuf<unsigned char> cell_ent;
+    DevBuf<unsigned char> cell_ent, cell_ent2;
+    // number of bucket entries (valid records), known after the bucket scan
+    long long nvalid_entries(long long H) { return read_ll(boff.ptr + H); }
     std::vector<cd> h_raw;
     std::vector<double> h_gscale;
     std::vector<int> h_hist;
@@ -886,8 +888,7 @@ public:
         if ((s = boff.ensure(H + 2))) return s;
         if ((s = slot_of.ensure(nR + 1))) return s;
         if ((s = cell_ent.ensure((nR + 1) * Kernels<D>::cell_entry_bytes()))) return s;
-        if ((s = npred.ensure(nR + 1))) return s;
-        if ((s = pred_off.ensure(nR + 2))) return s;
+        if ((s = cell_ent2.ensure((nR + 1) * Kernels<D>::cell_entry_bytes()))) return s;
         if ((s = status.ensure(nR + 1))) return s;
         if ((s = owner.ensure(nR + 1))) return s;
         if ((s = ensure_scan_scratch(std::max(nR, H) + 1))) return s;
@@ -899,23 +900,18 @@ public:
         pbeg(KID_SCAN);
         scan_int_to_ll(bcount.ptr, boff.ptr, H, ss, lc);
         pend();
+        const long long nent = nvalid_entries(H);  // bucket entries = valid records
         pbeg(KID_FTR);
         Kernels<D>::ftr_scatter(R, nR, slot_of.ptr, boff.ptr, bfill.ptr, cell_ent.ptr, lc);
-        Kernels<D>::ftr_preds(R, nR, cell_ent.ptr, boff.ptr, H - 1, MC, nullptr, nullptr, npred.ptr, lc);
-        pend();
-        pbeg(KID_SCAN);
-        scan_int_to_ll(npred.ptr, pred_off.ptr, nR, ss, lc);
-        pend();
-        const long long npreds = read_ll(pred_off.ptr + nR);
-        if ((s = preds.ensure(npreds + 1))) return s;
-        pbeg(KID_FTR);
-        Kernels<D>::ftr_preds(R, nR, cell_ent.ptr, boff.ptr, H - 1, MC, pred_off.ptr, preds.ptr, npred.ptr, lc);
+        // sort each bucket by term index
+        Kernels<D>::ftr_sort(cell_ent.ptr, nent, slot_of.ptr, boff.ptr, cell_ent2.ptr, lc);
         k_status_init(R, nR);
         pend();
         for (int round = 0;; round++) {
             MCE_CUDA(cudaMemsetAsync(counters.ptr + 1, 0, sizeof(int), lc.stream));
             pbeg(KID_FTR);
-            ftr_resolve(pred_off.ptr, preds.ptr, nR, status.ptr, owner.ptr, counters.ptr + 1, lc);
+            Kernels<D>::ftr_resolve(R, nR, cell_ent2.ptr, boff.ptr, H - 1, MC, status.ptr, owner.ptr, counters.ptr + 1,
+                                    lc);
             pend();
             int unk = 0;
             MCE_CUDA(cudaMemcpyAsync(&unk, counters.ptr + 1, sizeof(int), cudaMemcpyDeviceToHost, lc.stream));

@@ -478,7 +478,19 @@ __global__ void k_build_B(ParentList P, long long nP, const EstStep<D>* st, int 
                 for (int l = 0; l < D; l++) Ac[j * D + l] = As[c[j] * D + l];
                 bc[j] = bp[c[j]];
             }
-            if (cond1<D>(Ac, Pv) > kCondEps) continue;
+            // cond(A) > 1e12 skips the vertex (cell_enumeration.hpp:751-757).  A
+            // single-precision upper bound from the exact LU factors settles the
+            // well-conditioned subsets; the reference's explicit-inverse value is
+            // computed only when the bound is not at least ten times below 1e12.
+            double nrm = -1;
+            for (int cc = 0; cc < D; cc++) {
+                double sm = 0;
+                for (int r = 0; r < D; r++) sm += fabs(Ac[r * D + cc]);
+                if (dlt(nrm, sm)) nrm = sm;
+            }
+            if (!plu<D>(Ac, Pv)) continue;
+            const double bound = nrm * (double)inv_norm1_bound<D>(Ac);
+            if (!(bound <= 0.1 * kCondEps) && cond1_from_lu<D>(Ac, Pv, nrm) > kCondEps) continue;
             solve_lu<D>(Ac, Pv, bc, v);
             unsigned inmask = 0;
             for (int j = 0; j < D; j++) inmask |= 1u << c[j];
@@ -487,7 +499,7 @@ __global__ void k_build_B(ParentList P, long long nP, const EstStep<D>* st, int 
                 if (inmask & (1u << a)) continue;
                 double s = 0.0;
                 for (int j = 0; j < D; j++) s += As[a * D + j] * v[j];
-                if (s - bp[a] < 0) niv |= 1 << a;
+                if (neg(s - bp[a])) niv |= 1 << a;
             }
             for (int j = 0; j < (1 << D); j++) {
                 int sv = niv;
@@ -677,7 +689,7 @@ __global__ void __launch_bounds__(128) k_mu(ParentList P, long long nP, const Es
             double h = 0.0;
             for (int j = 0; j < D; j++) h += S.H[j] * A[lane * D + j];
             const double ah = fabs(h);
-            if (ah < kMuEps) {
+            if (abs_lt(h, kMuEps)) {
                 for (int j = 0; j < D; j++) mu[lane * D + j] = A[lane * D + j];
                 rho[lane] = p[lane];
             } else {
@@ -738,11 +750,11 @@ __global__ void __launch_bounds__(128) k_mu(ParentList P, long long nP, const Es
                 const double pl = rho[ll];
                 double s = 0.0;
                 for (int j = 0; j < D; j++) s += row[j] * root[j];
-                const double sg = s > 0 ? 1.0 : -1.0;
-                if (sg < 0) sneg |= 1 << l;
-                const double sc = pl * sg;
+                const bool sgp = pos(s);
+                if (!sgp) sneg |= 1 << l;
+                const double sc = sgp ? pl : -pl;  // p_l * sign, exact
                 for (int j = 0; j < D; j++) ty[j] += sc * row[j];
-                if (!(hof & (1u << l))) ygi += pl * sg;
+                if (!(hof & (1u << l))) ygi += sc;
                 for (int j = 0; j < D; j++) At[l * D + j] = row[j];
                 pt[l] = pl;
                 l++;
@@ -876,7 +888,24 @@ __global__ void k_moments(const cd* contrib, const long long* pstart, const long
         double s[PER];
 #pragma unroll
         for (int u = 0; u < PER; u++) s[u] = 0;
-        for (long long j = a; j < bnd; j++) {
+        // loads run ahead in batches of 8 rows; the additions stay in row order
+        long long j = a;
+        for (; j + 8 <= bnd; j += 8) {
+            double buf[8][PER];
+#pragma unroll
+            for (int r = 0; r < 8; r++)
+#pragma unroll
+                for (int u = 0; u < PER; u++) {
+                    const int comp = lane + 32 * u;
+                    buf[r][u] = comp < ND ? c[(j + r) * ND + comp] : 0.0;
+                }
+#pragma unroll
+            for (int r = 0; r < 8; r++)
+#pragma unroll
+                for (int u = 0; u < PER; u++)
+                    if (lane + 32 * u < ND) s[u] += buf[r][u];
+        }
+        for (; j < bnd; j++) {
 #pragma unroll
             for (int u = 0; u < PER; u++) {
                 const int comp = lane + 32 * u;
@@ -941,7 +970,8 @@ __device__ inline unsigned long long mix64(unsigned long long x)
 }
 __device__ inline long long cell_of(double v)
 {
-    double q = floor(v / kCellWidth);
+    // only a bucketing device: the same rounding on every side keeps it consistent
+    double q = floor(v * (1.0 / kCellWidth));
     if (!(q > -4.0e18)) q = -4.0e18;  // also catches NaN
     if (q > 4.0e18) q = 4.0e18;
     return (long long)q;
@@ -1000,80 +1030,91 @@ __device__ inline bool ftr_near_pm(const TermRecs& R, long long i, long long j, 
     const double* pi = R.p + i * MC;
     const double* pj = R.p + j * MC;
     for (int k = 0; k < m; k++)
-        if (fabs(pj[k] - pi[k]) > kReductionEps) return false;
+        if (!abs_lt(pj[k] - pi[k], kReductionEps) && dabs_bits(pj[k] - pi[k]) != dabs_bits(kReductionEps))
+            return false;  // |p_j - p_i| > eps
     // the reference compares Ai[k] with Aj[k] for k < m inside its per-component
     // loop (term_reduction.hpp:237-244), i.e. the first m entries of row-major A
     const double* Ai = R.A + i * MC * D;
     const double* Aj = R.A + j * MC * D;
     for (int k = 0; k < m; k++) {
         const double r = Ai[k], c = Aj[k];
-        if (!(fabs(r - c) < kReductionEps || fabs(r + c) < kReductionEps)) return false;
+        if (!(abs_lt(r - c, kReductionEps) || abs_lt(r + c, kReductionEps))) return false;
     }
     return true;
 }
 
-// Near predecessors of every term: count pass (preds == nullptr) then fill pass.
+// Buckets in ascending term order: every entry ranks itself inside its bucket.
 template <int D>
-__global__ void k_ftr_preds(TermRecs R, long long nR, const CellEntry<D>* ent, const long long* boff,
-                            long long hmask, int MC, const long long* pred_off, int* preds, int* npred)
+__global__ void k_ftr_sort_buckets(const CellEntry<D>* in, long long n, const int* slot_of, const long long* boff,
+                                   CellEntry<D>* out)
 {
-    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nR; j += (long long)gridDim.x * blockDim.x) {
-        const int e = R.est[j];
-        int cnt = 0;
-        if (e >= 0) {
-            const int m = R.m[j];
-            const int em = (e << 5) | m;
-            double bj[D];
-            long long lo[D], nc[D];
-            int nprobe = 1;
-            for (int a = 0; a < D; a++) {
-                bj[a] = R.b[j * D + a];
-                lo[a] = cell_of(bj[a] - kProbeHalfWidth);
-                const long long hi = cell_of(bj[a] + kProbeHalfWidth);
-                nc[a] = hi - lo[a] + 1;
-                if (nc[a] < 1) nc[a] = 1;
-                if (nc[a] > 2) nc[a] = 2;
-                nprobe *= (int)nc[a];
-            }
-            for (int pr = 0; pr < nprobe; pr++) {
-                long long c[D];
-                int rem = pr;
-                for (int a = 0; a < D; a++) {
-                    c[a] = lo[a] + (rem % nc[a]);
-                    rem /= (int)nc[a];
-                }
-                const long long s = cell_slot<D>(e, m, c, hmask);
-                for (long long k = boff[s]; k < boff[s + 1]; k++) {
-                    const CellEntry<D>& ce = ent[k];
-                    if (ce.idx >= j || ce.est_m != em) continue;
-                    bool ok = true;
-                    for (int a = 0; a < D && ok; a++) {
-                        if (cell_of(ce.b[a]) != c[a]) ok = false;
-                        const double lo_a = ce.b[a] - kReductionEps, hi_a = ce.b[a] + kReductionEps;
-                        if (!(bj[a] > lo_a && bj[a] <= hi_a)) ok = false;
-                    }
-                    if (!ok || !ftr_near_pm<D>(R, ce.idx, j, m, MC)) continue;
-                    if (preds) preds[pred_off[j] + cnt] = ce.idx;
-                    cnt++;
-                }
-            }
-        }
-        if (!preds) npred[j] = cnt;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const CellEntry<D> me = in[k];
+        const int s = slot_of[me.idx];
+        const long long a = boff[s], bnd = boff[s + 1];
+        long long rank = 0;
+        for (long long q = a; q < bnd; q++) rank += in[q].idx < me.idx;
+        out[a + rank] = me;
     }
 }
 
-#if MCE_COMMON_UNIT
-__global__ void k_ftr_resolve(const long long* pred_off, const int* preds, long long nR, int* status, int* owner,
-                              int* unknown)
+// One round of the greedy term reduction (term_reduction.hpp:186-270): a term
+// whose smallest not-yet-reduced near predecessor is a root joins it; a term
+// with no such predecessor is a root; otherwise it waits for the next round.
+// Near predecessors are found by scanning the sorted buckets of the cells
+// around b in ascending index, stopping at the first one that is not a member.
+template <int D>
+__global__ void k_ftr_resolve_scan(TermRecs R, long long nR, const CellEntry<D>* ent, const long long* boff,
+                                   long long hmask, int MC, int* status, int* owner, int* unknown)
 {
     for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nR; j += (long long)gridDim.x * blockDim.x) {
         if (status[j] != 0) continue;
+        const int e = R.est[j];
+        const int m = R.m[j];
+        const int em = (e << 5) | m;
+        double bj[D];
+        long long lo[D], nc[D];
+        int nprobe = 1;
+        for (int a = 0; a < D; a++) {
+            bj[a] = R.b[j * D + a];
+            lo[a] = cell_of(bj[a] - kProbeHalfWidth);
+            const long long hi = cell_of(bj[a] + kProbeHalfWidth);
+            nc[a] = hi - lo[a] + 1;
+            if (nc[a] < 1) nc[a] = 1;
+            if (nc[a] > 2) nc[a] = 2;
+            nprobe *= (int)nc[a];
+        }
         int best = INT_MAX, minu = INT_MAX;
-        for (long long k = pred_off[j]; k < pred_off[j + 1]; k++) {
-            const int i = preds[k];
-            const int s = ((volatile int*)status)[i];
-            if (s == 1) best = i < best ? i : best;
-            else if (s == 0) minu = i < minu ? i : minu;
+        long long seen[1 << (D < 5 ? D : 5)];
+        int nseen = 0;
+        for (int pr = 0; pr < nprobe; pr++) {
+            long long c[D];
+            int rem = pr;
+            for (int a = 0; a < D; a++) {
+                c[a] = lo[a] + (rem % nc[a]);
+                rem /= (int)nc[a];
+            }
+            const long long s = cell_slot<D>(e, m, c, hmask);
+            bool dup = false;
+            for (int q = 0; q < nseen; q++) dup |= seen[q] == s;
+            if (dup) continue;
+            if (nseen < (1 << (D < 5 ? D : 5))) seen[nseen++] = s;
+            for (long long k = boff[s]; k < boff[s + 1]; k++) {
+                const CellEntry<D>& ce = ent[k];
+                if (ce.idx >= j) break;  // ascending: no predecessors beyond
+                if (ce.est_m != em) continue;
+                bool ok = true;
+                for (int a = 0; a < D && ok; a++) {
+                    const double lo_a = ce.b[a] - kReductionEps, hi_a = ce.b[a] + kReductionEps;
+                    if (!(dlt(lo_a, bj[a]) && dle(bj[a], hi_a))) ok = false;
+                }
+                if (!ok || !ftr_near_pm<D>(R, ce.idx, j, m, MC)) continue;
+                const int st = ((volatile int*)status)[ce.idx];
+                if (st == 2) continue;  // a member: look further
+                if (st == 1) best = ce.idx < best ? ce.idx : best;
+                else minu = ce.idx < minu ? ce.idx : minu;
+                break;  // the first non-member near predecessor of this bucket decides it
+            }
         }
         if (best < minu) {
             owner[j] = best;
@@ -1086,6 +1127,7 @@ __global__ void k_ftr_resolve(const long long* pred_off, const int* preds, long 
     }
 }
 
+#if MCE_COMMON_UNIT
 __global__ void k_group_count(const int* status, const int* owner, long long nR, int* gcnt)
 {
     for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nR; j += (long long)gridDim.x * blockDim.x)
@@ -1162,10 +1204,8 @@ __device__ inline cd g_cell(const GCtx& c, long long s, int key, double gscale)
     const unsigned hof = R.horthog[s];
     const double* q = R.q + s * MC;
     double ygi = 0;
-    for (int k = 0; k < m; k++) {
-        const double sk = ((key >> k) & 1) ? -1.0 : 1.0;
-        if (!(hof & (1u << k))) ygi += q[k] * sk;
-    }
+    for (int k = 0; k < m; k++)
+        if (!(hof & (1u << k))) ygi += ((key >> k) & 1) ? -q[k] : q[k];  // q_k * s_k, exact
     int lp = 0, lm = 0;
     if (!(flags & kFlagNewChild)) {
         lp = key & ((1 << phc) - 1);
@@ -1709,13 +1749,23 @@ size_t Kernels<D>::cell_entry_bytes()
 }
 
 template <int D>
-void Kernels<D>::ftr_preds(TermRecs R, long long nR, const void* ent, const long long* boff, long long hmask, int MC,
-                           const long long* pred_off, int* preds, int* npred, const LaunchCfg& c)
+void Kernels<D>::ftr_sort(const void* in, long long n, const int* slot_of, const long long* boff, void* out,
+                          const LaunchCfg& c)
+{
+    if (n == 0) return;
+    ++g_launches;
+    k_ftr_sort_buckets<D><<<grid_for(n, 256, c.num_sms), 256, 0, c.stream>>>(
+        static_cast<const CellEntry<D>*>(in), n, slot_of, boff, static_cast<CellEntry<D>*>(out));
+}
+
+template <int D>
+void Kernels<D>::ftr_resolve(TermRecs R, long long nR, const void* ent, const long long* boff, long long hmask,
+                             int MC, int* status, int* owner, int* unknown, const LaunchCfg& c)
 {
     if (nR == 0) return;
     ++g_launches;
-    k_ftr_preds<D><<<grid_for(nR, 128, c.num_sms), 128, 0, c.stream>>>(
-        R, nR, static_cast<const CellEntry<D>*>(ent), boff, hmask, MC, pred_off, preds, npred);
+    k_ftr_resolve_scan<D><<<grid_for(nR, 128, c.num_sms), 128, 0, c.stream>>>(
+        R, nR, static_cast<const CellEntry<D>*>(ent), boff, hmask, MC, status, owner, unknown);
 }
 
 static inline size_t gtable_smem_per_warp(int MC, int D)
@@ -1755,13 +1805,6 @@ void Kernels<D>::compact(TermRecs R, const int* alive, const int* src, long long
 }
 
 #if MCE_COMMON_UNIT
-void ftr_resolve(const long long* pred_off, const int* preds, long long nR, int* status, int* owner, int* unknown,
-                 const LaunchCfg& c)
-{
-    if (nR == 0) return;
-    ++g_launches;
-    k_ftr_resolve<<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(pred_off, preds, nR, status, owner, unknown);
-}
 void group_count(const int* status, const int* owner, long long nR, int* gcnt, const LaunchCfg& c)
 {
     if (nR == 0) return;

@@ -54,8 +54,10 @@ struct Kernels {
     static void ftr_scatter(TermRecs R, long long nR, const int* slot_of, const long long* boff, int* bfill,
                             void* ent, const LaunchCfg& c);
     static size_t cell_entry_bytes();
-    static void ftr_preds(TermRecs R, long long nR, const void* ent, const long long* boff, long long hmask, int MC,
-                          const long long* pred_off, int* preds, int* npred, const LaunchCfg& c);
+    static void ftr_sort(const void* in, long long n, const int* slot_of, const long long* boff, void* out,
+                         const LaunchCfg& c);
+    static void ftr_resolve(TermRecs R, long long nR, const void* ent, const long long* boff, long long hmask, int MC,
+                            int* status, int* owner, int* unknown, const LaunchCfg& c);
     // g-tables of every reduction group (flattening.hpp:318-568).
     static void gtable(TermRecs R, const int* roots_list, long long nroots, const int* gcnt,
                        const long long* goff, const int* members, ParentList P, Tables Told, const int* Bkeys,
@@ -68,8 +70,6 @@ struct Kernels {
 };
 
 // Shape-agnostic kernels.
-void ftr_resolve(const long long* pred_off, const int* preds, long long nR, int* status, int* owner,
-                 int* unknown, const LaunchCfg& c);
 void group_count(const int* status, const int* owner, long long nR, int* gcnt, const LaunchCfg& c);
 void group_fill(const int* status, const int* owner, long long nR, const long long* goff, int* gfill,
                 int* members, const LaunchCfg& c);

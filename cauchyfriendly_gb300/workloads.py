@@ -157,3 +157,33 @@ def five_state_two_msmt(seed=0, steps=3):
     prob = _base(5, 2, 2, Phi, Gamma, [0.05, 0.05], H, [0.1, 0.1], 0.1 * np.ones(5), steps)
     prob["msmts"] = simulate(prob, rng)
     return prob
+
+
+def five_state_ltv_windows(seed=0, steps=200, dt=0.1, outlier_frac=0.02, outlier_scale=50.0):
+    """Sliding-window 5-state LTV problem: Phi_k = expm(A_k dt) with A_k a
+    seeded N(0, 0.3^2) 5x5 matrix plus a slow sinusoidal drift of amplitude
+    0.05 in each entry, Gamma 5x2 = 0.1 N(0,1), H 2x5 = N(0,1), beta = gamma =
+    [0.05, 0.05] / [0.1, 0.1], p0 = 0.1, two measurements per step, 2% of the
+    noise samples replaced by outliers at 50x.  Phi has shape (steps, 5, 5)."""
+    from scipy.linalg import expm
+    rng = np.random.Generator(np.random.PCG64(seed))
+    d = 5
+    A = rng.normal(0.0, 0.3, (d, d))
+    ph = rng.uniform(0, 2 * np.pi, (d, d))
+    Phis = np.stack([expm(dt * (A + 0.05 * np.sin(0.05 * k + ph))) for k in range(steps)])
+    Gamma = 0.1 * rng.standard_normal((d, 2))
+    H = rng.standard_normal((2, d))
+    prob = _base(d, 2, 2, Phis[0], Gamma, [0.05, 0.05], H, [0.1, 0.1], 0.1 * np.ones(d), steps)
+    prob["Phi"] = Phis
+    # simulate with the time-varying Phi
+    x = np.linalg.solve(prob["A0"], _cauchy(rng, prob["p0"], d))
+    zs = np.zeros((steps, 2))
+    for k in range(steps):
+        if k > 0:
+            w = _cauchy(rng, prob["beta"], 2)
+            x = Phis[k] @ x + Gamma @ w
+        v = _cauchy(rng, prob["gamma"], 2)
+        v = np.where(rng.random(2) < outlier_frac, v * outlier_scale, v)
+        zs[k] = H @ x + v
+    prob["msmts"] = zs
+    return prob

@@ -212,6 +212,10 @@ def _load_oracle():
                                        ctypes.c_int, _dp, _dp]
         lib.lib.orc_post_mu_terms.restype = ctypes.c_longlong
         lib.lib.orc_post_mu_terms.argtypes = [ctypes.c_void_p]
+        lib.lib.orc_reset.argtypes = [ctypes.c_void_p]
+        lib.lib.orc_reinit.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+        lib.lib.orc_set_master_step.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.lib.orc_errors.argtypes = [ctypes.c_void_p]
         _oracle_lib = lib
     return _oracle_lib
 
@@ -248,6 +252,70 @@ class Oracle(_EstimatorBase):
 
     def post_mu_terms(self):
         return int(self._l.lib.orc_post_mu_terms(self.h))
+
+    def step_with(self, msmt, Phi, Gamma, beta, H, gamma):
+        """One update with explicit model arrays (window-manager use)."""
+        a = lambda x: np.ascontiguousarray(x, dtype=np.float64)
+        Phi, Gamma, beta, H = a(Phi), a(Gamma), a(beta), a(H)
+        return self._l.fn("step")(self.h, float(msmt), _ptr(Phi), _ptr(Gamma), _ptr(beta), _ptr(H), float(gamma),
+                                  None, None)
+
+    def reset(self):
+        self._l.lib.orc_reset(self.h)
+
+    def reinit(self, A0, p0, b0):
+        a = lambda x: np.ascontiguousarray(x, dtype=np.float64)
+        A0, p0, b0 = a(A0), a(p0), a(b0)
+        self._l.lib.orc_reinit(self.h, _ptr(A0), _ptr(p0), _ptr(b0))
+
+    def set_master_step(self, ms):
+        self._l.lib.orc_set_master_step(self.h, int(ms))
+
+    def errors(self):
+        return int(self._l.lib.orc_errors(self.h))
+
+
+class OracleSlot:
+    """A window slot of n_mgr oracle estimators with the batch interface the
+    window manager drives (cauchyfriendly_gb300.windows)."""
+
+    def __init__(self, A0, p0, b0, steps, d, cmcc, pncc, p, consts):
+        self.ests = []
+        for m in range(A0.shape[0]):
+            prob = {"A0": A0[m], "p0": p0[m], "b0": b0[m], "steps": steps, "d": d, "cmcc": cmcc, "pncc": pncc,
+                    "p": p}
+            self.ests.append(Oracle(prob, *consts[m]))
+
+    def step(self, z, Phi, Gamma, beta, H, gamma):
+        return np.array([e.step_with(z[m], Phi[m], Gamma[m], beta[m], H[m], gamma[m])
+                         for m, e in enumerate(self.ests)], dtype=np.int32)
+
+    def moments(self, i):
+        return self.ests[i].moments()
+
+    def errors(self, i):
+        return self.ests[i].errors()
+
+    def num_terms(self, i):
+        return self.ests[i].num_terms()
+
+    def reset(self):
+        for e in self.ests:
+            e.reset()
+
+    def reinit(self, i, A0, p0, b0):
+        self.ests[i].reinit(A0, p0, b0)
+
+    def set_master_step(self, ms):
+        for e in self.ests:
+            e.set_master_step(ms)
+
+    def post_mu_terms(self):
+        return sum(e.post_mu_terms() for e in self.ests)
+
+    def close(self):
+        for e in self.ests:
+            e.close()
 
 
 class Reference(_EstimatorBase):

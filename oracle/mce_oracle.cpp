@@ -1337,6 +1337,19 @@ int orc_step(void* h, double msmt, const double* Phi, const double* Gamma, const
     return E.errors;
 }
 
+// reset (cauchy_estimator.hpp:1247), reinitialize_start_statistics (:1302),
+// and the master_step setter the window manager uses (pycauchy.hpp:767).
+void orc_reset(void* h) { reset_terms(*(Estimator*)h); }
+void orc_reinit(void* h, const double* A0, const double* p0, const double* b0)
+{
+    Estimator& E = *(Estimator*)h;
+    E.A0.assign(A0, A0 + E.d * E.d);
+    E.p0.assign(p0, p0 + E.d);
+    E.b0.assign(b0, b0 + E.d);
+}
+void orc_set_master_step(void* h, int ms) { ((Estimator*)h)->master_step = ms; }
+int orc_errors(void* h) { return ((Estimator*)h)->errors; }
+
 int orc_num_terms(void* h) { return ((Estimator*)h)->Nt; }
 long long orc_post_mu_terms(void* h) { return ((Estimator*)h)->post_mu_terms; }
 int orc_shape_range(void* h) { return ((Estimator*)h)->shape_range; }

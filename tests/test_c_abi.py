@@ -38,3 +38,26 @@ def test_create_without_gpu_fails_loudly():
     from cauchyfriendly_gb300 import CauchyEstimator
     with pytest.raises(_lib.MceError):
         CauchyEstimator(np.eye(3), np.ones(3) * 0.1, np.zeros(3), 5, 3, 0, 1, 1)
+
+
+def test_invalid_arguments_return_status_without_device():
+    import ctypes as ct
+    import numpy as np
+    lib = _lib.load()
+    st = ct.c_int(0)
+    dp = ct.POINTER(ct.c_double)
+    A0 = np.eye(3)
+    z = np.zeros(3)
+    steps = np.array([5], np.int32)
+    # d out of range
+    h = lib.mce_batch_create(1, 9, 0, 1, 1, steps.ctypes.data_as(ct.POINTER(ct.c_int)), A0.ctypes.data_as(dp),
+                             z.ctypes.data_as(dp), z.ctypes.data_as(dp), None, None, 0, ct.byref(st))
+    assert not h and st.value == -1
+    # more hyperplanes than the build supports (the reference caps at 31, this build at 16)
+    steps = np.array([40], np.int32)
+    h = lib.mce_batch_create(1, 3, 0, 1, 1, steps.ctypes.data_as(ct.POINTER(ct.c_int)), A0.ctypes.data_as(dp),
+                             z.ctypes.data_as(dp), z.ctypes.data_as(dp), None, None, 0, ct.byref(st))
+    assert not h and st.value == -3
+    assert "31" in _lib.last_error() or "16" in _lib.last_error()
+    # NULL handle
+    assert lib.mce_step(None, 0.0, None, None, None, None, 0.0, None, None) == -1

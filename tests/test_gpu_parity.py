@@ -147,3 +147,21 @@ def test_three_state_longer_against_oracle(steps):
     est.close()
     want, _ = _oracle_records(prob, rp, bp)
     G.compare_records(got, want, check_terms=False)
+
+
+def test_stepping_past_the_last_step_returns_status():
+    CE, _ = _gpu()
+    from cauchyfriendly_gb300 import _lib, workloads as W
+    prob = W.three_state_lti(seed=1, steps=3)
+    est = CE(prob["A0"], prob["p0"], prob["b0"], prob["steps"], 3, 0, 1, 1)
+    for k in range(3):
+        est.step(prob["msmts"][k, 0], prob["Phi"], prob["Gamma"], prob["beta"], prob["H"][0], prob["gamma"][0])
+    # the reference calls exit(1) here (cauchy_estimator.hpp:1220-1225)
+    with pytest.raises(_lib.MceError):
+        est.step(0.0, prob["Phi"], prob["Gamma"], prob["beta"], prob["H"][0], prob["gamma"][0])
+    # reset makes it usable again, with the same results
+    est.reset()
+    est.step(prob["msmts"][0, 0], prob["Phi"], prob["Gamma"], prob["beta"], prob["H"][0], prob["gamma"][0])
+    assert est.num_terms() >= 1
+    assert est.device_errors() == 0
+    est.close()
