@@ -51,6 +51,10 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="batched3", choices=["batched3", "windows5"],
+                    help="batched3: the batched 3-state configuration (default); windows5: the sliding-window "
+                         "5-state LTV configuration for --window-steps steps")
+    ap.add_argument("--window-steps", type=int, default=12)
     return ap.parse_args()
 
 
@@ -148,18 +152,24 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per launch of the dominant kernel from the committed ncu
-    summary (a line 'traffic_per_term <group> <bytes>' scaled by terms)."""
-    path = os.path.join(ROOT, "profiles", "ncu_gtable_batched_three_state.md")
+def profile_figures():
+    """Figures bench.py takes from the committed ncu summaries: lines
+    'bench: <name> <group> <value>' in profiles/*.md (DRAM traffic per
+    algorithmic byte and FP64-pipe activity of a kernel group)."""
     out = {}
+    pdir = os.path.join(ROOT, "profiles")
     try:
-        for ln in open(path):
-            if ln.startswith("traffic_bytes_per_alg_byte"):
-                _, grp, v = ln.split()
-                out[grp] = float(v)
+        names = sorted(os.listdir(pdir))
     except OSError:
-        pass
+        return out
+    for fn in names:
+        if not fn.endswith(".md"):
+            continue
+        for ln in open(os.path.join(pdir, fn)):
+            if ln.startswith("bench: "):
+                f = ln.split()
+                if len(f) == 4:
+                    out[(f[1], f[2])] = float(f[3])
     return out
 
 
@@ -248,10 +258,54 @@ def _ref_pass(probs, seeds, threads):
     return time.perf_counter() - t0
 
 
+def run_windows5(args):
+    """Sliding-window 5-state LTV MCE (window 6, 2 measurements per step),
+    run for --window-steps steps; terms/s over the device time of all window
+    updates (value) and the wall clock of the manager steps (e2e)."""
+    import torch
+    from cauchyfriendly_gb300 import windows, workloads as W
+    torch.cuda.set_device(0)
+    prob = W.five_state_ltv_windows(seed=args.seed, steps=args.window_steps)
+    Wn = 6
+    A0, p0, b0 = prob["A0"][None], prob["p0"][None], prob["b0"][None]
+
+    def one_pass():
+        mgr = windows.SlidingWindowManager(Wn, A0, p0, b0, 5, 2, 2)
+        t0 = time.perf_counter()
+        dev0 = [s.est._lib.mce_device_time_ms(s.est._h) for s in mgr.slots]
+        for k in range(prob["steps"]):
+            mgr.step(prob["msmts"][k][None], prob["Phi"][k][None], prob["Gamma"][None], prob["beta"][None],
+                     prob["H"][None], prob["gamma"][None])
+        wall = time.perf_counter() - t0
+        dev = sum(s.est._lib.mce_device_time_ms(s.est._h) for s in mgr.slots) - sum(dev0)
+        terms = mgr.total_post_mu_terms()
+        mgr.close()
+        return terms, dev / 1e3, wall
+
+    for _ in range(max(0, args.warmup - 2)):
+        one_pass()
+    tot_terms = tot_dev = tot_wall = 0.0
+    for _ in range(args.steps):
+        n, dv, wl = one_pass()
+        tot_terms += n
+        tot_dev += dv
+        tot_wall += wl
+    line = {"metric": METRIC, "value": tot_terms / tot_dev, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * tot_dev / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "sliding-window 5-state LTV MCE, window 6, 2 msmts/step, %d steps"
+                                   % args.window_steps, "terms_per_step": tot_terms / args.steps},
+            "e2e": {"value": tot_terms / tot_wall, "unit": UNIT, "wall_s_per_step": tot_wall / args.steps}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload == "windows5":
+        run_windows5(args)
         return
     import torch
     rank = int(os.environ.get("RANK", "0"))
@@ -332,14 +386,19 @@ def main():
     secs = top_ms / 1e3 / args.steps  # per pass
     peak, peak_kind = measured_peaks()
     achieved = ab / secs / 1e9 if secs > 0 else 0.0
-    tr = profile_traffic().get(top)
+    figs = profile_figures()
+    tr = figs.get(("traffic_bytes_per_alg_byte", top))
+    per_launch = ab / max(1, top_launches / args.steps)
     roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind,
-                "traffic": (tr * ab / max(1, top_launches / args.steps)) if tr else None,
-                "alg_bytes_per_launch": ab / max(1, top_launches / args.steps),
+                "traffic": tr * per_launch if tr else None,
+                "alg_bytes_per_launch": per_launch,
                 "launches_per_pass": top_launches / args.steps,
-                "fp64": {"achieved_tflops": af / secs / 1e12 if secs > 0 else 0.0, "peak_tflops": 1.25,
-                         "peak_source": "nominal GB300 FP64 (not measured)"}}
+                "note": "FP64-bound: the FP64 pipe, not HBM, limits this kernel (see fp64)",
+                "fp64": {"algorithmic_tflops": af / secs / 1e12 if secs > 0 else 0.0, "nominal_peak_tflops": 1.25,
+                         "pipe_active_pct_ncu": figs.get(("fp64_pipe_active_pct", top)),
+                         "peak_source": "nominal GB300 FP64; pipe activity from the committed ncu capture"}}
+    alg_per_pass = {g: {"bytes": alg[g][0], "flops": alg[g][1]} for g in alg}
     share = {g: round(kstats[g][0] / max(1e-9, sum(v[0] for v in kstats.values())), 4) for g in kstats}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -354,6 +413,7 @@ def main():
                 "d2h_bytes_per_step": int(B["steps"].sum() * (2 + 2 * 3 + 2 * 9) * 8), "wall_s_per_step": wall_s},
         "gpu_launches": launches,
         "kernel_time_share": share,
+        "alg_per_pass": alg_per_pass,
         "roofline": roofline,
         "clocks": clocks,
     }

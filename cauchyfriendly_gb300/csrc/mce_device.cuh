@@ -47,12 +47,14 @@ __device__ inline cd cmul(cd x, cd y)
     double ac = x.re * y.re, bd = x.im * y.im, ad = x.re * y.im, bc = x.im * y.re;
     return cd{ac - bd, ad + bc};
 }
+__device__ inline unsigned long long dabs_bits(double x);
+
 // Complex division by R. L. Smith, "Algorithm 116: Complex division",
 // CACM 5(8), 1962: divide through by the larger of |c|, |d| to avoid overflow.
 __device__ inline cd cdiv(cd x, cd y)
 {
     const double a = x.re, b = x.im, c = y.re, d = y.im;
-    if (fabs(c) < fabs(d)) {
+    if (dabs_bits(c) < dabs_bits(d)) {  // |c| < |d|
         const double r = c / d;
         const double den = c * r + d;
         return cd{(a * r + b) / den, (b * r - a) / den};
@@ -93,6 +95,19 @@ __device__ inline long long dkey(double x)
 // a < b and a <= b (keys map -0 and +0 to the same value)
 __device__ inline bool dlt(double a, double b) { return dkey(a) < dkey(b); }
 __device__ inline bool dle(double a, double b) { return dkey(a) <= dkey(b); }
+
+// The term-approximation test of make_gtable, ps2 * |v| > 1e-15 with
+// |v| = hypot(re, im) (flattening.hpp:242-247).  ps2^2 (re^2 + im^2) is
+// compared with the threshold first; only values within a relative 1e-9 of it
+// take the reference's exact expression.
+__device__ inline bool above_approx_threshold(double ps2, double re, double im)
+{
+    const double t = (ps2 * ps2) * (re * re + im * im);
+    const double thr = kTermApproxEps * kTermApproxEps;
+    if (t > thr * (1.0 + 1e-9)) return true;
+    if (t < thr * (1.0 - 1e-9)) return false;
+    return ps2 * hypot(re, im) > kTermApproxEps;
+}
 
 // Binary search over ascending keys (gtable.hpp:283-301 semantics).
 __device__ inline int bsearch_key(const int* __restrict__ keys, int n, int key)

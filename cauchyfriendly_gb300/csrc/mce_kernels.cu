@@ -1416,7 +1416,7 @@ __global__ void k_gtable(GCtx c, const int* roots_list, long long nroots, const 
             const cd v = g_cell<D>(c, root, RKL[k], gs);
             okeys[k] = RKL[k];
             ovals[k] = v;
-            if (ps2 * hypot(v.re, v.im) > kTermApproxEps) negl = false;
+            if (above_approx_threshold(ps2, v.re, v.im)) negl = false;
         }
         negl = __all_sync(kFull, negl);
         const int nmem = gcnt[r];
@@ -1461,7 +1461,7 @@ __global__ void k_gtable(GCtx c, const int* roots_list, long long nroots, const 
                     const cd v = g_cell<D>(c, cm, RKL[k], gs);
                     okeys[k] = RKL[k];
                     ovals[k] = v;
-                    if (ps2c * hypot(v.re, v.im) > kTermApproxEps) ng = false;
+                    if (above_approx_threshold(ps2c, v.re, v.im)) ng = false;
                 }
                 ng = __all_sync(kFull, ng);
                 if (!ng) {
@@ -1496,7 +1496,7 @@ __global__ void k_gtable(GCtx c, const int* roots_list, long long nroots, const 
                 for (int k = lane; k < nR; k += 32) {
                     const cd v = g_cell<D>(c, cm, RKL[k] ^ sigf, gs);
                     scr[k] = v;
-                    if (ps2c * hypot(v.re, v.im) > kTermApproxEps) ng = false;
+                    if (above_approx_threshold(ps2c, v.re, v.im)) ng = false;
                 }
                 ng = __all_sync(kFull, ng);
                 if (!ng)
@@ -1519,7 +1519,7 @@ __global__ void k_gtable(GCtx c, const int* roots_list, long long nroots, const 
                 const int n = c.P.B_cnt[fam];
                 for (int k = lane; k < n; k += 32) {
                     const cd v = g_cell<D>(c, cm, B[k], gs);
-                    if (ps2c * hypot(v.re, v.im) > kTermApproxEps) ng = false;
+                    if (above_approx_threshold(ps2c, v.re, v.im)) ng = false;
                 }
                 ng = __all_sync(kFull, ng);
                 if (!ng)
