@@ -26,6 +26,7 @@ SIGNATURES = {
     "mce_batch_create": (_vp, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _ip, _dp, _dp,
                                _dp, _dp, _dp, ctypes.c_int, _ip]),
     "mce_batch_step": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int, _ip]),
+    "mce_batch_step_noalloc": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int, _ip]),
     "mce_batch_run": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int, _dp,
                                      _dp, _dp, _ip, _lp]),
     "mce_create": (_vp, [_dp, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp,

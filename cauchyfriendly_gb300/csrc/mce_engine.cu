@@ -29,8 +29,12 @@
 namespace mce {
 
 extern thread_local std::string g_last_error;
+// Set by mce_batch_step_noalloc for the duration of its step: a DevBuf that
+// would have to grow fails with MCE_ERR_NOMEM instead of calling cudaMalloc.
+extern thread_local bool g_device_alloc_forbidden;
 #if MCE_ONLY_DIM <= 0
 thread_local std::string g_last_error;
+thread_local bool g_device_alloc_forbidden = false;
 #endif
 
 static void set_error(const std::string& s) { g_last_error = s; }
@@ -59,6 +63,12 @@ struct DevBuf {
     int ensure(size_t n)
     {
         if (n <= cap && ptr) return MCE_OK;
+        if (g_device_alloc_forbidden) {
+            set_error("mce_batch_step_noalloc: a device buffer of the handle is too small for this step (" +
+                      std::to_string(n * sizeof(T)) + " bytes needed, " + std::to_string(cap * sizeof(T)) +
+                      " held) and this call may not allocate; the handle must be reset");
+            return MCE_ERR_NOMEM;
+        }
         size_t want = std::max<size_t>(n, cap + cap / 2);
         want = std::max<size_t>(want, 64);
         if (ptr) cudaFree(ptr);
@@ -170,8 +180,17 @@ public:
                            int* keys, double* g) = 0;
     virtual long long total_cells(int est) = 0;
     virtual int reset() = 0;
+    // waits for the work the engine queued (after a step that stopped early)
+    virtual void drain() = 0;
 
     int E = 0, d = 0, cmcc = 0, pncc = 0, p = 0, MC = 0;
+    // When set (only by mce_batch_step_noalloc), the g-table kernel takes its
+    // per-warp scratch from this caller-owned region instead of the handle's
+    // own buffer, with as many warps as fit in it.
+    void* fixed_gtable_scratch = nullptr;
+    size_t fixed_gtable_scratch_bytes = 0;
+    // bytes of g-table scratch one warp needs: half the cells of a full-shape term
+    size_t gtable_scratch_bytes_per_warp() const { return sizeof(cd) * (size_t)half_cells_cap(MC, d); }
     int master_step = 0;
     int device_errors = 0;
     long long post_mu_terms = 0;
@@ -491,6 +510,11 @@ public:
         if (ev1) cudaEventDestroy(ev1);
         for (cudaEvent_t ev : evpool) cudaEventDestroy(ev);
         if (lc.stream) cudaStreamDestroy(lc.stream);
+    }
+
+    void drain() override
+    {
+        if (lc.stream) cudaStreamSynchronize(lc.stream);
     }
 
     int reset() override
@@ -966,12 +990,20 @@ public:
         if ((s = tcnt.ensure(nR + 1))) return s;
         MCE_CUDA(cudaMemsetAsync(alive.ptr, 0, sizeof(int) * (nR + 1), lc.stream));
         const int capMC = half_cells_cap(MC, D);
-        const long long max_warps = (long long)lc.num_sms * 16 * 4;
-        if ((s = scratch.ensure((size_t)max_warps * capMC))) return s;
+        cd* gscr = nullptr;
+        long long gscr_warps = 0;  // 0: the handle's buffer holds a warp slot for every launched warp
+        if (fixed_gtable_scratch) {
+            gscr = static_cast<cd*>(fixed_gtable_scratch);
+            gscr_warps = (long long)(fixed_gtable_scratch_bytes / (sizeof(cd) * capMC));
+        } else {
+            const long long max_warps = (long long)lc.num_sms * 16 * 4;
+            if ((s = scratch.ensure((size_t)max_warps * capMC))) return s;
+            gscr = scratch.ptr;
+        }
         pbeg(KID_GTABLE);
         Kernels<D>::gtable(R, roots_list.ptr, nroots, gcnt.ptr, goff.ptr, members.ptr, PV, Told, Bkeys.ptr, gscale.ptr,
-                           toff.ptr, Tables{Tn.keys.ptr, Tn.vals.ptr}, tcnt.ptr, alive.ptr, src.ptr, scratch.ptr,
-                           capMC, MC, err, lc);
+                           toff.ptr, Tables{Tn.keys.ptr, Tn.vals.ptr}, tcnt.ptr, alive.ptr, src.ptr, gscr, capMC, MC,
+                           err, lc, gscr_warps);
         pend();
         if (prof_mode >= 2) alg_stats(with_tp, nR, true);
         // ---- next parent list
@@ -1541,5 +1573,47 @@ void mce_destroy(mce_handle* h)
 }
 
 }  // extern "C"
+
+namespace mce {
+
+void report_error(const std::string& s) { set_error(s); }
+
+// mce_batch_step with the g-table kernel's per-warp scratch placed in
+// [scratch, scratch + bytes) and every device allocation refused; the
+// entry point mce_batch_step_noalloc (mce_no_alloc.cu) owns the region.
+int batch_step_in_fixed_scratch(mce_handle* h, void* scratch, size_t bytes, const double* msmt, const double* Phi,
+                                const double* Gamma, const double* beta, const double* H, const double* gamma,
+                                const double* B, const double* u, int shared_model, int* err_out)
+{
+    if (!h || !scratch) return MCE_ERR_ARG;
+    EngineBase* g = h->eng;
+    // the launcher puts up to 4 warps in a block: one block's slots must fit
+    const size_t need = 4 * g->gtable_scratch_bytes_per_warp();
+    if (need > bytes) {
+        set_error("mce_batch_step_noalloc: a term of up to " + std::to_string(g->MC) + " hyperplanes in " +
+                  std::to_string(g->d) + " dimensions needs " + std::to_string(need) +
+                  " bytes of g-table scratch, more than the " + std::to_string(bytes) + " bytes of the static array");
+        return MCE_ERR_SHAPE;
+    }
+    struct Restore {
+        EngineBase* g;
+        ~Restore()
+        {
+            g_device_alloc_forbidden = false;
+            g->fixed_gtable_scratch = nullptr;
+            g->fixed_gtable_scratch_bytes = 0;
+        }
+    } restore{g};
+    g->fixed_gtable_scratch = scratch;
+    g->fixed_gtable_scratch_bytes = bytes;
+    g_device_alloc_forbidden = true;
+    const int rc = mce_batch_step(h, msmt, Phi, Gamma, beta, H, gamma, B, u, shared_model, err_out);
+    // a step refused part-way may have kernels queued: let them finish so
+    // the reset that must follow does not race them
+    if (rc != MCE_OK) g->drain();
+    return rc;
+}
+
+}  // namespace mce
 
 #endif  // MCE_ONLY_DIM <= 0

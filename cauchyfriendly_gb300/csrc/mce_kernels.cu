@@ -1779,7 +1779,7 @@ template <int D>
 void Kernels<D>::gtable(TermRecs R, const int* roots_list, long long nroots, const int* gcnt, const long long* goff,
                         const int* members, ParentList P, Tables Told, const int* Bkeys, const double* gscale,
                         const long long* toff, Tables Tnew, int* tcnt, int* alive, int* src, cd* scratch,
-                        long long scratch_per_warp, int MC, int* err, const LaunchCfg& c)
+                        long long scratch_per_warp, int MC, int* err, const LaunchCfg& c, long long max_warps)
 {
     if (nroots == 0) return;
     GCtx ctx{R, P, Told, Bkeys, MC};
@@ -1789,7 +1789,11 @@ void Kernels<D>::gtable(TermRecs R, const int* roots_list, long long nroots, con
     if (warps < 1) warps = 1;
     const size_t sm = pw * warps;
     cudaFuncSetAttribute(k_gtable<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    const int grid = grid_for(nroots, warps, c.num_sms, 16);
+    int grid = grid_for(nroots, warps, c.num_sms, 16);
+    // a scratch region sized for max_warps warps (the caller guarantees
+    // max_warps >= 4 >= warps): the warps stride over the roots, so fewer of
+    // them give the same tables
+    if (max_warps > 0 && (long long)grid * warps > max_warps) grid = (int)(max_warps / warps);
     ++g_launches;
     k_gtable<D><<<grid, warps * 32, sm, c.stream>>>(ctx, roots_list, nroots, gcnt, goff, members, gscale, toff, Tnew,
                                                     tcnt, alive, src, scratch, scratch_per_warp, err);

@@ -63,7 +63,7 @@ struct Kernels {
                        const long long* goff, const int* members, ParentList P, Tables Told, const int* Bkeys,
                        const double* gscale, const long long* toff, Tables Tnew, int* tcnt, int* alive,
                        int* src, cd* scratch, long long scratch_per_warp, int MC, int* err,
-                       const LaunchCfg& c);
+                       const LaunchCfg& c, long long max_warps = 0);
     // Next parent list (shape-bucketed, stable) from the surviving roots.
     static void compact(TermRecs R, const int* alive, const int* src, long long nR, const int* new_slot,
                         const long long* toff, const int* tcnt, ParentList Pn, int MC, const LaunchCfg& c);

@@ -60,6 +60,31 @@ int mce_batch_step(mce_handle* h, const double* msmt, const double* Phi, const d
                    const double* H, const double* gamma, const double* B, const double* u, int shared_model,
                    int* err_out);
 
+/* No counterpart in the reference.  mce_batch_step for callers that may not
+ * allocate device memory while they estimate: a process whose device memory
+ * is already handed out (a framework's caching allocator, a real-time loop
+ * that sizes its memory at start-up), or one that cannot accept the
+ * device-wide synchronisation of cudaMalloc/cudaFree.  Same arguments and
+ * results as mce_batch_step; it calls no cudaMalloc, cudaFree or other
+ * allocating routine:
+ *  - the g-table kernel's scratch is a static 32 MiB device array of the
+ *    library, and the kernel runs as many warps as it has slots for; a
+ *    handle whose full-shape terms would need more than 4 warps' worth
+ *    (above 524,288 half-cells per term) is refused with MCE_ERR_SHAPE
+ *    before any work.  Under this build's limit of 16 hyperplanes per term
+ *    the largest need is 1 MiB (8 states), so every handle fits;
+ *  - the handle's own device buffers must already be large enough (they grow
+ *    only in the other calls: step the handle with mce_batch_step over a
+ *    representative history, then mce_reset); a buffer that would have to
+ *    grow stops the step with MCE_ERR_NOMEM, after which the handle must be
+ *    reset.
+ * The first call on a device looks the array up (cudaGetSymbolAddress); make
+ * it before any stream capture.  Every call on a device shares the array:
+ * calls that overlap on the GPU race, so serialise them. */
+int mce_batch_step_noalloc(mce_handle* h, const double* msmt, const double* Phi, const double* Gamma,
+                           const double* beta, const double* H, const double* gamma, const double* B, const double* u,
+                           int shared_model, int* err_out);
+
 /* Runs every estimator through its whole measurement history
  * msmts[n_est * max_steps * p] (row e*max_steps*p + k*p + j), with a shared
  * model or per-estimator models as in mce_batch_step.  Per-update outputs are
