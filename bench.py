@@ -269,33 +269,56 @@ def run_windows5(args):
     Wn = 6
     A0, p0, b0 = prob["A0"][None], prob["p0"][None], prob["b0"][None]
 
+    import ctypes
+    from cauchyfriendly_gb300 import _lib
+    lib = _lib.load()
+    groups = [lib.mce_kernel_group_name(k).decode() for k in range(lib.mce_num_kernel_groups())]
+    kms = {g: 0.0 for g in groups}
+
     def one_pass():
         mgr = windows.SlidingWindowManager(Wn, A0, p0, b0, 5, 2, 2)
+        for s in mgr.slots:
+            lib.mce_set_profiling(s.est._h, 1)
+            lib.mce_clear_profile(s.est._h)
         t0 = time.perf_counter()
-        dev0 = [s.est._lib.mce_device_time_ms(s.est._h) for s in mgr.slots]
+        dev0 = [lib.mce_device_time_ms(s.est._h) for s in mgr.slots]
         for k in range(prob["steps"]):
             mgr.step(prob["msmts"][k][None], prob["Phi"][k][None], prob["Gamma"][None], prob["beta"][None],
                      prob["H"][None], prob["gamma"][None])
         wall = time.perf_counter() - t0
-        dev = sum(s.est._lib.mce_device_time_ms(s.est._h) for s in mgr.slots) - sum(dev0)
+        dev = sum(lib.mce_device_time_ms(s.est._h) for s in mgr.slots) - sum(dev0)
         terms = mgr.total_post_mu_terms()
+        per = {}
+        for k, g in enumerate(groups):
+            tot = 0.0
+            for s in mgr.slots:
+                ms, nl, ab, af = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_double(), ctypes.c_double()
+                lib.mce_kernel_group_stats(s.est._h, k, ctypes.byref(ms), ctypes.byref(nl), ctypes.byref(ab),
+                                           ctypes.byref(af))
+                tot += ms.value
+            per[g] = tot
         mgr.close()
-        return terms, dev / 1e3, wall
+        return terms, dev / 1e3, wall, per
 
     for _ in range(max(0, args.warmup - 2)):
         one_pass()
     tot_terms = tot_dev = tot_wall = 0.0
     for _ in range(args.steps):
-        n, dv, wl = one_pass()
+        n, dv, wl, per = one_pass()
         tot_terms += n
         tot_dev += dv
         tot_wall += wl
+        for g in groups:
+            kms[g] += per[g]
+    ksum = sum(kms.values()) or 1.0
     line = {"metric": METRIC, "value": tot_terms / tot_dev, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * tot_dev / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "sliding-window 5-state LTV MCE, window 6, 2 msmts/step, %d steps"
                                    % args.window_steps, "terms_per_step": tot_terms / args.steps},
-            "e2e": {"value": tot_terms / tot_wall, "unit": UNIT, "wall_s_per_step": tot_wall / args.steps}}
+            "e2e": {"value": tot_terms / tot_wall, "unit": UNIT, "wall_s_per_step": tot_wall / args.steps},
+            "kernel_time_share": {g: round(kms[g] / ksum, 4) for g in groups},
+            "kernel_ms_per_step": {g: round(kms[g] / args.steps, 3) for g in groups}}
     print(json.dumps(line), flush=True)
 
 

@@ -642,227 +642,277 @@ __device__ inline int mu_coalign_smem(double* A, double* p, double* q, int m, un
     return ns;
 }
 
-// Shared memory of k_mu per warp, in doubles: MU rows and scales, then per
-// lane a staged term (A rows, p, q) and its moment contribution.
+// Shared memory of k_mu per warp, in doubles: per lane one MU row and its
+// scale, a staged term (A rows, p, q) and its moment contribution; then the
+// round's rank -> lane table, record slots and per-family scalars.
 __host__ __device__ inline int mu_warp_doubles(int MC, int D)
 {
     const int NM = 1 + D + D * D;
-    return (MC + 1) * (D + 1) + 32 * (MC * D + 2 * MC) + 32 * 2 * NM + 16;
+    return 32 * (D + 1) + 32 * (MC * D + 2 * MC) + 32 * 2 * NM + 16 + 32 + 32;
 }
 
 // Measurement update of every parent (cauchy_term.hpp:84-310), fused with the
 // g/yei evaluation of the parent and its children (cauchy_term.hpp:312-401),
 // the moment contributions (cache_moments, cauchy_estimator.hpp:307), the
-// parent's re-normalisation and the children's MU coalignment.  One warp per
-// parent: lane l < m owns hyperplane l during the update, then lane t stages
-// child t (lane m the parent) in shared memory for evaluation and
-// coalignment; the family's records and contributions leave with coalesced
-// warp-wide stores (children of a parent are contiguous in the records).
+// parent's re-normalisation and the children's MU coalignment.
+//
+// Lane packing: a family (parent of m hyperplanes and its children) needs
+// m + 1 lanes, lane t < m for hyperplane t / child t and lane m for the
+// measurement row / the parent itself.  Each warp walks a chunk of up to 32
+// consecutive parents in rounds; a round takes as many consecutive families
+// as fit in the 32 lanes (3-state terms have 4-12 lanes each), so the FP64
+// work, which the SM issues per warp instruction whatever the number of
+// active lanes, runs on nearly full warps.  The per-term arithmetic is the
+// same as with one family per warp.  Each round's contributions and records
+// leave with coalesced warp-wide stores (the families of consecutive parents
+// are contiguous in both).
 template <int D>
 __global__ void __launch_bounds__(128) k_mu(ParentList P, long long nP, const EstStep<D>* st, const long long* pstart,
                                             const double* roots, Tables Told, int* Bkeys, TermRecs R, long long nR,
-                                            const long long* kall_scan, cd* contrib, int MC, int* err)
+                                            const long long* kall_scan, cd* contrib, int MC, int chunk, int* err)
 {
     extern __shared__ double smem_d[];
     constexpr int NM = 1 + D + D * D;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
     const int RS = MC * D + 2 * MC;  // staged doubles per lane
     double* wbase = smem_d + (size_t)wib * mu_warp_doubles(MC, D);
-    double* mu = wbase;
-    double* rho = mu + (MC + 1) * D;
-    double* stage = rho + (MC + 1);
-    double* cstage = stage + 32 * RS;
-    int* rank2lane = reinterpret_cast<int*>(cstage + 32 * 2 * NM);  // child rank -> staging lane
+    double* mu = wbase;                // 32 x D: the row of lane L
+    double* rho = mu + 32 * D;         // 32
+    double* stage = rho + 32;          // 32 x RS
+    double* cstage = stage + 32 * RS;  // 32 x 2 NM
+    int* rank2lane = reinterpret_cast<int*>(cstage + 32 * 2 * NM);       // round rank -> staging lane
+    long long* slot_of = reinterpret_cast<long long*>(rank2lane + 32);  // round rank -> record slot (-1: none)
+    int* fam_esgc = reinterpret_cast<int*>(slot_of + 32);                // family -> B flip mask
+    int* fam_bok = fam_esgc + 32;                                        // family -> flips its B table
     double* At = stage + lane * RS;
     double* pt = At + MC * D;
     double* qt = pt + MC;
-    for (long long i = (long long)blockIdx.x * nwb + wib; i < nP; i += (long long)gridDim.x * nwb) {
-        const int e = P.est[i];
-        const EstStep<D>& S = st[e];
-        const int m = P.m[i], phc = P.m_old[i];
-        const double* A = P.A + i * MC * D;
-        const double* p = P.p + i * MC;
-        const double* b = P.b + i * D;
-        const double* root = roots + (long long)e * D;
-        bool integ = false, neg = false;
-        if (lane < m) {
-            double h = 0.0;
-            for (int j = 0; j < D; j++) h += S.H[j] * A[lane * D + j];
-            const double ah = fabs(h);
-            if (abs_lt(h, kMuEps)) {
-                for (int j = 0; j < D; j++) mu[lane * D + j] = A[lane * D + j];
-                rho[lane] = p[lane];
-            } else {
-                const double r = 1.0 / h;
-                for (int j = 0; j < D; j++) mu[lane * D + j] = A[lane * D + j] * r;
-                rho[lane] = p[lane] * ah;
-                integ = true;
-                neg = !(h > 0);
+    const long long nchunks = (nP + chunk - 1) / chunk;
+    for (long long ch = (long long)blockIdx.x * nwb + wib; ch < nchunks; ch += (long long)gridDim.x * nwb) {
+        const long long cend = (ch + 1) * chunk < nP ? (ch + 1) * chunk : nP;
+        long long cur = ch * chunk;
+        while (cur < cend) {
+            // ---- the round: consecutive families whose lanes fit in the warp
+            const int my_need = (cur + lane < cend) ? P.m[cur + lane] + 1 : 64;
+            int pre = my_need;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(kFull, pre, o);
+                if (lane >= o) pre += y;
             }
-        } else if (lane == m) {
-            for (int j = 0; j < D; j++) mu[m * D + j] = 0.0;
-            rho[m] = S.gamma;
-        }
-        const unsigned integ_mask = __ballot_sync(kFull, integ);
-        const int esg = (int)__ballot_sync(kFull, neg);
-        double zeta = 0;
-        if (lane == 0) {
-            double hb = 0.0;
-            for (int j = 0; j < D; j++) hb += S.H[j] * b[j];
-            zeta = S.msmt - hb;
-        }
-        zeta = __shfl_sync(kFull, zeta, 0);
-        __syncwarp();
-        int lhp = esg;
-        if (phc < m) lhp &= (1 << phc) - 1;
-        const int esg_c = (esg & (1 << (m - 1))) ? (esg ^ ((1 << m) - 1)) : esg;
-        const bool write = !S.skip;
-        const long long kbase = P.kscan[pstart[e]];
-        const long long pslot = i + kbase;                     // parent's record
-        const long long cslot0 = pstart[e + 1] + P.kscan[i];   // first child's record
-        const int nk = __popc(integ_mask);
-        const bool mine = (lane < m) ? ((integ_mask >> lane) & 1u) : (lane == m);
-        // family order of this lane's term: parent 0, child c -> 1 + c
-        const int ford = (lane == m) ? 0 : 1 + __popc(integ_mask & ((1u << lane) - 1));
-        if (mine) rank2lane[ford] = lane;
-        int mfin = 0;
-        if (mine) {
-            const int t = lane;
-            double bt[D], ty[D];
-            for (int j = 0; j < D; j++) {
-                bt[j] = b[j] + zeta * mu[t * D + j];
-                ty[j] = 0;
+            const int nfam = __popc(__ballot_sync(kFull, pre <= 32));  // >= 1: m + 1 <= 32
+            const unsigned starts = __reduce_or_sync(kFull, lane < nfam ? (1u << (pre - my_need)) : 0u);
+            const int used = __shfl_sync(kFull, pre, nfam - 1);
+            const unsigned le = starts & ((2u << lane) - 1u);  // family starts at or below this lane
+            const int f = __popc(le) - 1;
+            const int fb = 31 - __clz(le);  // first lane of this lane's family
+            const int t = lane - fb;
+            const bool active = lane < used;
+            const long long i = cur + f;
+            int e = 0, m = 0, phc = 0;
+            if (active) {
+                e = P.est[i];
+                m = P.m[i];
+                phc = P.m_old[i];
             }
-            unsigned hof = 0;
-            int sneg = 0;
-            double ygi = 0;
-            int l = 0;
-            for (int ll = 0; ll <= m; ll++) {
-                if (ll == t) continue;
-                const bool fi = (ll < m) ? ((integ_mask >> ll) & 1u) : true;
-                double row[D];
-                if (fi)
-                    for (int j = 0; j < D; j++) row[j] = mu[ll * D + j] - mu[t * D + j];
-                else {
-                    for (int j = 0; j < D; j++) row[j] = mu[ll * D + j];
-                    hof |= 1u << l;
-                }
-                const double pl = rho[ll];
-                double s = 0.0;
-                for (int j = 0; j < D; j++) s += row[j] * root[j];
-                const bool sgp = pos(s);
-                if (!sgp) sneg |= 1 << l;
-                const double sc = sgp ? pl : -pl;  // p_l * sign, exact
-                for (int j = 0; j < D; j++) ty[j] += sc * row[j];
-                if (!(hof & (1u << l))) ygi += sc;
-                for (int j = 0; j < D; j++) At[l * D + j] = row[j];
-                pt[l] = pl;
-                l++;
-            }
-            // lambda keys into the parent table (cauchy_term.hpp:357-381)
-            int lp = 0, lm = 0, k = 0;
-            for (int l2 = 0; l2 < m; l2++) {
-                if (k < phc) {
-                    if (k == t) {
-                        lm |= 1 << k;
-                        k++;
-                        if (k == phc) continue;
-                    }
-                    if ((sneg >> l2) & 1) {
-                        lp |= 1 << k;
-                        lm |= 1 << k;
-                    }
-                    k++;
-                }
-            }
-            const int* pk = Told.keys + P.tab_off[i];
-            const cd* pv = Told.vals + P.tab_off[i];
-            const int pcnt = P.tab_cnt[i];
-            const cd gp = lookup_num(pk, pv, pcnt, lp ^ lhp, phc);
-            const cd gm = lookup_num(pk, pv, pcnt, lm ^ lhp, phc);
-            const double dv = rho[t];
-            cd g = csub(cdiv(gp, mkcd(ygi + dv, zeta)), cdiv(gm, mkcd(ygi - dv, zeta)));
-            g = cscale(g, kTwoPiInv);
-            cd* cs = reinterpret_cast<cd*>(cstage) + lane * NM;
-            cs[0] = g;
-            for (int j = 0; j < D; j++) {
-                const cd y = mkcd(-ty[j], bt[j]);
-                const cd gy = cmul(g, y);
-                cs[1 + j] = gy;
-                for (int kk = 0; kk < D; kk++) cs[1 + D + j * D + kk] = cmul(gy, mkcd(-ty[kk], bt[kk]));
-            }
-            mfin = m;
-            if (write) {
-                const long long slot = (t == m) ? pslot : cslot0 + (ford - 1);
-                if (slot >= nR) {
-                    set_err(err, kErrTableOverflow);
-                } else {
-                    int flags = (t == m) ? 0 : kFlagNewChild;
-                    if (t == m) {
-                        // parent: normalize_hps(true), no coalignment
-                        for (int r = 0; r < m; r++) {
-                            qt[r] = pt[r];
-                            double n1 = 0;
-                            for (int j = 0; j < D; j++) n1 += fabs(At[r * D + j]);
-                            pt[r] *= n1;
-                            for (int j = 0; j < D; j++) At[r * D + j] /= n1;
-                        }
+            const EstStep<D>& S = st[e];
+            const double* A = P.A + i * MC * D;
+            const double* p = P.p + i * MC;
+            const double* b = P.b + i * D;
+            const double* root = roots + (long long)e * D;
+            // ---- MU rows: lane t < m hyperplane t, lane m the measurement row
+            bool integ = false, neg = false;
+            double zeta_l = 0;
+            if (active) {
+                if (t < m) {
+                    double h = 0.0;
+                    for (int j = 0; j < D; j++) h += S.H[j] * A[t * D + j];
+                    const double ah = fabs(h);
+                    if (abs_lt(h, kMuEps)) {
+                        for (int j = 0; j < D; j++) mu[lane * D + j] = A[t * D + j];
+                        rho[lane] = p[t];
                     } else {
-                        mfin = mu_coalign_smem<D>(At, pt, qt, m, hof, R.cmap + slot * MC, R.csmap + slot * MC, err);
-                        if (mfin != m) flags |= kFlagHasCmap;
+                        const double r = 1.0 / h;
+                        for (int j = 0; j < D; j++) mu[lane * D + j] = A[t * D + j] * r;
+                        rho[lane] = p[t] * ah;
+                        integ = true;
+                        neg = !(h > 0);
                     }
-                    for (int j = 0; j < D; j++) R.b[slot * D + j] = bt[j];
-                    R.est[slot] = e;
-                    R.m[slot] = mfin;
-                    R.pbc[slot] = m;
-                    R.phc[slot] = phc;
-                    R.z[slot] = t;
-                    R.lhp[slot] = lhp;
-                    R.fam[slot] = (int)i;
-                    R.horthog[slot] = hof;
-                    R.cval[slot] = zeta;
-                    R.dval[slot] = dv;
-                    R.flags[slot] = flags;
+                } else {
+                    for (int j = 0; j < D; j++) mu[lane * D + j] = 0.0;
+                    rho[lane] = S.gamma;
+                    double hb = 0.0;
+                    for (int j = 0; j < D; j++) hb += S.H[j] * b[j];
+                    zeta_l = S.msmt - hb;
                 }
             }
-        }
-        __syncwarp();
-        // moment contributions of the family in the reference's summation order
-        {
-            const long long fbase = i + kall_scan[i];
-            const int nterm = 1 + nk;
-            const double* cs = cstage;
-            double* out = reinterpret_cast<double*>(contrib + fbase * NM);
-            for (int x = lane; x < nterm * 2 * NM; x += 32) {
-                const int f = x / (2 * NM), o = x % (2 * NM);
-                // family position f -> staging lane
-                const int src_lane = rank2lane[f];
-                out[x] = cs[src_lane * 2 * NM + o];
+            const unsigned integ_all = __ballot_sync(kFull, integ);
+            const unsigned neg_all = __ballot_sync(kFull, neg);
+            const double zeta = __shfl_sync(kFull, zeta_l, (fb + m) & 31);
+            __syncwarp();
+            const unsigned fmask = m >= 32 ? kFull : ((1u << m) - 1u);
+            const unsigned integ_mask = (integ_all >> fb) & fmask;
+            const int esg = (int)((neg_all >> fb) & fmask);
+            int lhp = esg, esg_c = 0;
+            if (active) {
+                if (phc < m) lhp &= (1 << phc) - 1;
+                esg_c = (esg & (1 << (m - 1))) ? (esg ^ ((1 << m) - 1)) : esg;
             }
-        }
-        if (write && pslot < nR && cslot0 + nk <= nR) {
-            // records: A, p, q rows of the family (rows padded to MC)
-            const int nterm = 1 + nk;
-            for (int x = lane; x < nterm * RS; x += 32) {
-                const int f = x / RS, o = x % RS;
-                const int src_lane = rank2lane[f];
-                const double v = stage[src_lane * RS + o];
-                const long long slot = (f == 0) ? pslot : cslot0 + (f - 1);
+            const bool write = !S.skip;
+            const long long kbase = active ? P.kscan[pstart[e]] : 0;
+            const long long pslot = i + kbase;                              // parent's record
+            const long long cslot0 = active ? pstart[e + 1] + P.kscan[i] : 0;  // first child's record
+            const int nk = __popc(integ_mask);
+            const bool mine = active && (t < m ? ((integ_mask >> t) & 1u) != 0 : true);
+            // family order of this lane's term: parent 0, child c -> 1 + c
+            const int ford = (t == m) ? 0 : 1 + __popc(integ_mask & ((1u << t) - 1u));
+            const long long fbase0 = cur + kall_scan[cur];  // the round's first contribution row
+            if (mine) {
+                const int q = (int)(i + kall_scan[i] - fbase0) + ford;
+                const bool rec_ok = write && pslot < nR && cslot0 + nk <= nR;
+                rank2lane[q] = lane;
+                slot_of[q] = rec_ok ? ((t == m) ? pslot : cslot0 + (ford - 1)) : -1;
+            }
+            if (active && t == m) {
+                fam_esgc[f] = esg_c;
+                fam_bok[f] = write ? 1 : 0;
+            }
+            if (mine) {
+                double bt[D], ty[D];
+                for (int j = 0; j < D; j++) {
+                    bt[j] = b[j] + zeta * mu[lane * D + j];
+                    ty[j] = 0;
+                }
+                unsigned hof = 0;
+                int sneg = 0;
+                double ygi = 0;
+                int l = 0;
+                for (int ll = 0; ll <= m; ll++) {
+                    if (ll == t) continue;
+                    const bool fi = (ll < m) ? ((integ_mask >> ll) & 1u) : true;
+                    const double* mrow = mu + (fb + ll) * D;
+                    double row[D];
+                    if (fi)
+                        for (int j = 0; j < D; j++) row[j] = mrow[j] - mu[lane * D + j];
+                    else {
+                        for (int j = 0; j < D; j++) row[j] = mrow[j];
+                        hof |= 1u << l;
+                    }
+                    const double pl = rho[fb + ll];
+                    double s = 0.0;
+                    for (int j = 0; j < D; j++) s += row[j] * root[j];
+                    const bool sgp = pos(s);
+                    if (!sgp) sneg |= 1 << l;
+                    const double sc = sgp ? pl : -pl;  // p_l * sign, exact
+                    for (int j = 0; j < D; j++) ty[j] += sc * row[j];
+                    if (!(hof & (1u << l))) ygi += sc;
+                    for (int j = 0; j < D; j++) At[l * D + j] = row[j];
+                    pt[l] = pl;
+                    l++;
+                }
+                // lambda keys into the parent table (cauchy_term.hpp:357-381)
+                int lp = 0, lm = 0, k = 0;
+                for (int l2 = 0; l2 < m; l2++) {
+                    if (k < phc) {
+                        if (k == t) {
+                            lm |= 1 << k;
+                            k++;
+                            if (k == phc) continue;
+                        }
+                        if ((sneg >> l2) & 1) {
+                            lp |= 1 << k;
+                            lm |= 1 << k;
+                        }
+                        k++;
+                    }
+                }
+                const int* pk = Told.keys + P.tab_off[i];
+                const cd* pv = Told.vals + P.tab_off[i];
+                const int pcnt = P.tab_cnt[i];
+                const cd gp = lookup_num(pk, pv, pcnt, lp ^ lhp, phc);
+                const cd gm = lookup_num(pk, pv, pcnt, lm ^ lhp, phc);
+                const double dv = rho[lane];
+                cd g = csub(cdiv(gp, mkcd(ygi + dv, zeta)), cdiv(gm, mkcd(ygi - dv, zeta)));
+                g = cscale(g, kTwoPiInv);
+                cd* cs = reinterpret_cast<cd*>(cstage) + lane * NM;
+                cs[0] = g;
+                for (int j = 0; j < D; j++) {
+                    const cd y = mkcd(-ty[j], bt[j]);
+                    const cd gy = cmul(g, y);
+                    cs[1 + j] = gy;
+                    for (int kk = 0; kk < D; kk++) cs[1 + D + j * D + kk] = cmul(gy, mkcd(-ty[kk], bt[kk]));
+                }
+                if (write) {
+                    const long long slot = (t == m) ? pslot : cslot0 + (ford - 1);
+                    if (slot >= nR) {
+                        set_err(err, kErrTableOverflow);
+                    } else {
+                        int mfin = m;
+                        int flags = (t == m) ? 0 : kFlagNewChild;
+                        if (t == m) {
+                            // parent: normalize_hps(true), no coalignment
+                            for (int r = 0; r < m; r++) {
+                                qt[r] = pt[r];
+                                double n1 = 0;
+                                for (int j = 0; j < D; j++) n1 += fabs(At[r * D + j]);
+                                pt[r] *= n1;
+                                for (int j = 0; j < D; j++) At[r * D + j] /= n1;
+                            }
+                        } else {
+                            mfin = mu_coalign_smem<D>(At, pt, qt, m, hof, R.cmap + slot * MC, R.csmap + slot * MC,
+                                                      err);
+                            if (mfin != m) flags |= kFlagHasCmap;
+                        }
+                        for (int j = 0; j < D; j++) R.b[slot * D + j] = bt[j];
+                        R.est[slot] = e;
+                        R.m[slot] = mfin;
+                        R.pbc[slot] = m;
+                        R.phc[slot] = phc;
+                        R.z[slot] = t;
+                        R.lhp[slot] = lhp;
+                        R.fam[slot] = (int)i;
+                        R.horthog[slot] = hof;
+                        R.cval[slot] = zeta;
+                        R.dval[slot] = dv;
+                        R.flags[slot] = flags;
+                    }
+                } else if (t == m && pslot < nR) {
+                    // a final MU keeps no records; mark the parent's slot empty
+                    R.est[pslot] = -1;
+                }
+            }
+            const int T = __popc(__ballot_sync(kFull, mine));  // terms of the round
+            __syncwarp();
+            // moment contributions of the round's families in the reference's
+            // summation order (each parent followed by its children)
+            {
+                double* out = reinterpret_cast<double*>(contrib + fbase0 * NM);
+                for (int x = lane; x < T * 2 * NM; x += 32) {
+                    const int q = x / (2 * NM), o = x % (2 * NM);
+                    out[x] = cstage[rank2lane[q] * 2 * NM + o];
+                }
+            }
+            // records: A, p, q rows (padded to MC) of the families that keep them
+            for (int x = lane; x < T * RS; x += 32) {
+                const int q = x / RS, o = x % RS;
+                const long long slot = slot_of[q];
+                if (slot < 0) continue;
+                const double v = stage[rank2lane[q] * RS + o];
                 if (o < MC * D) R.A[slot * MC * D + o] = v;
                 else if (o < MC * D + MC) R.p[slot * MC + (o - MC * D)] = v;
                 else R.q[slot * MC + (o - MC * D - MC)] = v;
             }
-        } else if (!write && lane == 0 && pslot < nR) {
-            // a final MU keeps no records; mark the parent's slot empty
-            R.est[pslot] = -1;
+            // parent B -> B_mu (cauchy_term.hpp:245-250)
+            for (int ff = 0; ff < nfam; ff++) {
+                if (!fam_bok[ff]) continue;
+                const long long ip = cur + ff;
+                int* B = Bkeys + P.B_off[ip];
+                const int n = P.B_cnt[ip];
+                const int ec = fam_esgc[ff];
+                for (int k = lane; k < n; k += 32) B[k] ^= ec;
+            }
+            __syncwarp();
+            cur += nfam;
         }
-        // parent B -> B_mu (cauchy_term.hpp:245-250)
-        if (write) {
-            int* B = Bkeys + P.B_off[i];
-            const int n = P.B_cnt[i];
-            for (int k = lane; k < n; k += 32) B[k] ^= esg_c;
-        }
-        __syncwarp();
     }
 }
 
@@ -1707,9 +1757,16 @@ void Kernels<D>::mu(ParentList P, long long nP, const EstStep<D>* st, const long
     const size_t sm = pw * warps;
     cudaFuncSetAttribute(k_mu<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     ++g_launches;
-    k_mu<D><<<grid_for(nP, warps, c.num_sms, 16), warps * 32, sm, c.stream>>>(P, nP, st, pstart, roots, Told,
-                                                                              Bkeys, R, nR, kall_scan, contrib, MC,
-                                                                              err);
+    // parents per warp: up to 32, fewer when that would leave the GPU with
+    // less than 16 warps per SM
+    const long long want = (long long)c.num_sms * 16;
+    long long chunk = (nP + want - 1) / want;
+    if (chunk > 32) chunk = 32;
+    if (chunk < 1) chunk = 1;
+    const long long nchunks = (nP + chunk - 1) / chunk;
+    k_mu<D><<<grid_for(nchunks, warps, c.num_sms, 16), warps * 32, sm, c.stream>>>(P, nP, st, pstart, roots, Told,
+                                                                                   Bkeys, R, nR, kall_scan, contrib,
+                                                                                   MC, (int)chunk, err);
 }
 
 template <int D>
