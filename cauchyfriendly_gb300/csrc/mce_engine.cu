@@ -335,7 +335,7 @@ public:
         }
     } Rb;
     DevBuf<cd> fam_mom, est_raw, scratch;
-    DevBuf<double> gscale;
+    DevBuf<double> gscale, mom_tot;
     DevBuf<long long> goff, toff, rscan, bucket_off, rbase, scan_tmp, kall_est;
     DevBuf<int> status, owner, gcnt, gfill, members, members_tmp, is_root, cap, roots_list, alive, src,
         tcnt, hist, new_slot, counters, first_cnt, bcount, bfill, slot_of;
@@ -465,6 +465,7 @@ public:
         s |= dsteps.ensure(E);
         s |= dpstart.ensure(E + 1);
         s |= est_raw.ensure((size_t)E * (1 + D + D * D));
+        s |= mom_tot.ensure((size_t)E * 2 * (1 + D + D * D));
         s |= gscale.ensure(E);
         s |= counters.ensure(8);
         s |= first_cnt.ensure(E + 1);
@@ -859,7 +860,8 @@ public:
                        fam_mom.ptr, MC, err, lc);
         pend();
         pbeg(KID_MOMENTS);
-        Kernels<D>::moments(fam_mom.ptr, dpstart.ptr, kall_scan.ptr, E, dsteps.ptr, est_raw.ptr, gscale.ptr, lc);
+        Kernels<D>::moments(fam_mom.ptr, dpstart.ptr, kall_scan.ptr, E, dsteps.ptr, mom_tot.ptr, est_raw.ptr,
+                            gscale.ptr, lc);
         pend();
         read_moments();
         // terms after the MU per estimator (un-reduced count, cauchy_estimator.hpp:749-751, 806-812)

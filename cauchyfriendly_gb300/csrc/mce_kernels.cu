@@ -919,79 +919,98 @@ __global__ void __launch_bounds__(128) k_mu(ParentList P, long long nP, const Es
 // Per-estimator moment sums, then finalize_cached_moments
 // (cauchy_estimator.hpp:340-357).  The reference accumulates fz, the mean and
 // the covariance in one sequential pass over the terms (parents in order, each
-// followed by its children); the same chain is summed here, one warp per
-// estimator with the lanes over the moment components, so the moments come
-// out bit-identical to the serial reference.
+// followed by its children); the same chain is summed here, so the moments
+// come out bit-identical to the serial reference.
+//
+// The chains are independent per moment component: one warp per (estimator,
+// 32 components), each lane adding its component over the estimator's rows in
+// order.  A chain is a run of dependent additions, so the rows are streamed
+// into a shared-memory ring by cp.async ahead of the adder: with one active
+// estimator of 10^6 terms the chain runs at the FP64 add rate instead of
+// waiting on DRAM once every few rows.  Each lane copies and reads only its
+// own column, so its own cp.async.wait_group is the only synchronisation.
+constexpr int kMomStages = 8, kMomRows = 16;
+
+__device__ inline void cp_async8(double* smem_dst, const double* gmem_src)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem_src) : "memory");
+}
+__device__ inline void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ inline void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 template <int D>
-__global__ void k_moments(const cd* contrib, const long long* pstart, const long long* kall_scan, int E,
-                          const EstStep<D>* st, cd* est_raw, double* gscale)
+__global__ void __launch_bounds__(32) k_moments_chain(const cd* contrib, const long long* pstart,
+                                                      const long long* kall_scan, int E, const EstStep<D>* st,
+                                                      double* tot)
 {
     constexpr int NM = 1 + D + D * D;
-    constexpr int ND = 2 * NM;               // doubles per term
-    constexpr int PER = (ND + 31) / 32;      // doubles per lane
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
-    for (int e = blockIdx.x * nwb + wib; e < E; e += gridDim.x * nwb) {
-        if (!st[e].active) continue;
-        const long long a = pstart[e] + kall_scan[pstart[e]];
-        const long long bnd = pstart[e + 1] + kall_scan[pstart[e + 1]];
-        const double* c = reinterpret_cast<const double*>(contrib);
-        double s[PER];
-#pragma unroll
-        for (int u = 0; u < PER; u++) s[u] = 0;
-        // loads run ahead in batches of 8 rows; the additions stay in row order
-        long long j = a;
-        for (; j + 8 <= bnd; j += 8) {
-            double buf[8][PER];
-#pragma unroll
-            for (int r = 0; r < 8; r++)
-#pragma unroll
-                for (int u = 0; u < PER; u++) {
-                    const int comp = lane + 32 * u;
-                    buf[r][u] = comp < ND ? c[(j + r) * ND + comp] : 0.0;
-                }
-#pragma unroll
-            for (int r = 0; r < 8; r++)
-#pragma unroll
-                for (int u = 0; u < PER; u++)
-                    if (lane + 32 * u < ND) s[u] += buf[r][u];
+    constexpr int ND = 2 * NM;              // doubles per term
+    constexpr int NS = (ND + 31) / 32;      // 32-component slices
+    __shared__ double ring[kMomStages][kMomRows][32];
+    const int lane = threadIdx.x;
+    const int e = blockIdx.x / NS, slice = blockIdx.x - e * NS;
+    if (e >= E || !st[e].active) return;
+    const long long a = pstart[e] + kall_scan[pstart[e]];
+    const long long n = pstart[e + 1] + kall_scan[pstart[e + 1]] - a;
+    const int comp = slice * 32 + lane;
+    const bool valid = comp < ND;
+    const double* col = reinterpret_cast<const double*>(contrib) + a * ND + comp;
+    const long long nchunks = (n + kMomRows - 1) / kMomRows;
+    // chunk k of this lane's column into ring slot k % kMomStages (one commit group per chunk)
+    auto issue = [&](long long k) {
+        if (valid && k < nchunks) {
+            const long long r0 = k * kMomRows;
+            const int cnt = n - r0 < kMomRows ? (int)(n - r0) : kMomRows;
+            double(*slot)[32] = ring[k % kMomStages];
+            for (int r = 0; r < cnt; r++) cp_async8(&slot[r][lane], col + (r0 + r) * ND);
         }
-        for (; j < bnd; j++) {
-#pragma unroll
-            for (int u = 0; u < PER; u++) {
-                const int comp = lane + 32 * u;
-                if (comp < ND) s[u] += c[j * ND + comp];
-            }
+        cp_async_commit();
+    };
+    for (int k = 0; k < kMomStages - 1; k++) issue(k);
+    double sum = 0.0;
+    for (long long k = 0; k < nchunks; k++) {
+        cp_async_wait<kMomStages - 2>();  // chunk k has landed
+        // refill the slot of chunk k - 1, whose values were added last iteration
+        issue(k + kMomStages - 1);
+        if (valid) {
+            const long long r0 = k * kMomRows;
+            const int cnt = n - r0 < kMomRows ? (int)(n - r0) : kMomRows;
+            const double(*slot)[32] = ring[k % kMomStages];
+            for (int r = 0; r < cnt; r++) sum += slot[r][lane];
         }
-        // gather the totals to lane 0's view through shared memory
-        __shared__ double tot_s[8][ND > 0 ? ND : 1];
-#pragma unroll
-        for (int u = 0; u < PER; u++) {
-            const int comp = lane + 32 * u;
-            if (comp < ND) tot_s[wib][comp] = s[u];
-        }
-        __syncwarp();
-        if (lane == 0) {
-            const double* t = tot_s[wib];
-            const cd fz = mkcd(t[0], t[1]);
-            gscale[e] = kTwoPiInv / fz.re;
-            const cd ifz = mkcd(0, fz.re);
-            cd* out = est_raw + (long long)e * NM;
-            out[0] = fz;
-            cd mfin[D];
-            for (int j = 0; j < D; j++) {
-                mfin[j] = cdiv(mkcd(t[2 * (1 + j)], t[2 * (1 + j) + 1]), ifz);
-                out[1 + j] = mfin[j];
-            }
-            // the covariance is accumulated as cov -= (g y_j) y_k, i.e. minus the chain
-            for (int j = 0; j < D; j++)
-                for (int k = 0; k < D; k++) {
-                    const int q = 2 * (1 + D + j * D + k);
-                    const cd cv = mkcd(-t[q], -t[q + 1]);
-                    out[1 + D + j * D + k] = csub(cdiv(cv, fz), cmul(mfin[j], mfin[k]));
-                }
-        }
-        __syncwarp();
     }
+    cp_async_wait<0>();
+    if (valid) tot[(long long)e * ND + comp] = sum;
+}
+
+// finalize_cached_moments (cauchy_estimator.hpp:340-357) from the chain totals.
+template <int D>
+__global__ void k_moments_final(const double* tot, int E, const EstStep<D>* st, cd* est_raw, double* gscale)
+{
+    constexpr int NM = 1 + D + D * D;
+    constexpr int ND = 2 * NM;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E || !st[e].active) return;
+    const double* t = tot + (long long)e * ND;
+    const cd fz = mkcd(t[0], t[1]);
+    gscale[e] = kTwoPiInv / fz.re;
+    const cd ifz = mkcd(0, fz.re);
+    cd* out = est_raw + (long long)e * NM;
+    out[0] = fz;
+    cd mfin[D];
+    for (int j = 0; j < D; j++) {
+        mfin[j] = cdiv(mkcd(t[2 * (1 + j)], t[2 * (1 + j) + 1]), ifz);
+        out[1 + j] = mfin[j];
+    }
+    // the covariance is accumulated as cov -= (g y_j) y_k, i.e. minus the chain
+    for (int j = 0; j < D; j++)
+        for (int k = 0; k < D; k++) {
+            const int q = 2 * (1 + D + j * D + k);
+            const cd cv = mkcd(-t[q], -t[q + 1]);
+            out[1 + D + j * D + k] = csub(cdiv(cv, fz), cmul(mfin[j], mfin[k]));
+        }
 }
 
 // ---------------------------------------------------------------------------
@@ -1771,14 +1790,12 @@ void Kernels<D>::mu(ParentList P, long long nP, const EstStep<D>* st, const long
 
 template <int D>
 void Kernels<D>::moments(const cd* contrib, const long long* pstart, const long long* kall_scan, int E,
-                         const EstStep<D>* st, cd* est_raw, double* gscale, const LaunchCfg& c)
+                         const EstStep<D>* st, double* tot, cd* est_raw, double* gscale, const LaunchCfg& c)
 {
-    const int warps = 8;
-    int g = (E + warps - 1) / warps;
-    if (g > c.num_sms * 8) g = c.num_sms * 8;
-    if (g < 1) g = 1;
-    ++g_launches;
-    k_moments<D><<<g, warps * 32, 0, c.stream>>>(contrib, pstart, kall_scan, E, st, est_raw, gscale);
+    constexpr int NS = (2 * (1 + D + D * D) + 31) / 32;
+    g_launches += 2;
+    k_moments_chain<D><<<(unsigned)E * NS, 32, 0, c.stream>>>(contrib, pstart, kall_scan, E, st, tot);
+    k_moments_final<D><<<(E + 127) / 128, 128, 0, c.stream>>>(tot, E, st, est_raw, gscale);
 }
 
 template <int D>

@@ -47,7 +47,7 @@ struct Kernels {
     // Per-estimator moment sums in the reference's order and finalisation
     // (cauchy_estimator.hpp:307-357).
     static void moments(const cd* contrib, const long long* pstart, const long long* kall_scan, int E,
-                        const EstStep<D>* st, cd* est_raw, double* gscale, const LaunchCfg& c);
+                        const EstStep<D>* st, double* tot, cd* est_raw, double* gscale, const LaunchCfg& c);
     // Fast term reduction (term_reduction.hpp:159-276) over the post-MU records:
     // grid cells of b, counting-sorted buckets, near predecessors.
     static void ftr_cells(TermRecs R, long long nR, long long hmask, int* slot_of, int* bcount, const LaunchCfg& c);

@@ -170,11 +170,13 @@ class SlidingWindowManager:
                 xh, Ph = out[m][0], out[m][1]
                 A0, p0, b0 = speyers_window_init(xh, Ph, H[m, j], gamma[m, j], msmts[m, j])
                 slot.reinit(m, A0, p0, b0)
+            self.post_mu_terms += slot.post_mu_terms()  # a reset clears the slot's count
             slot.reset()  # pycauchy_single_step_reset: new start statistics, then reset
             slot.step(msmts[:, j], Phi, Gamma, beta, H[:, j, :], gamma[:, j])
             slot.set_master_step(self.p)
             self.win_counts[min_idx] += 1
             if self.win_counts[max_idx] == self.W:
+                self.post_mu_terms += self.slots[max_idx].post_mu_terms()
                 self.slots[max_idx].reset()
                 self.win_counts[max_idx] = 0
         self.step_idx += 1
@@ -182,7 +184,8 @@ class SlidingWindowManager:
         return out
 
     def total_post_mu_terms(self):
-        return sum(s.post_mu_terms() for s in self.slots)
+        """Terms present after every MU of every window since construction."""
+        return self.post_mu_terms + sum(s.post_mu_terms() for s in self.slots)
 
     def close(self):
         for s in self.slots:

@@ -1148,6 +1148,7 @@ static void reset_terms(Estimator& E)
     E.terms_per_shape[E.d] = 1;
     E.master_step = 0;
     E.errors = 0;
+    E.post_mu_terms = 0;  // counts since the last reset, as mce_post_mu_terms does
 }
 
 // step_first: cauchy_estimator.hpp:1179-1208 with make_gtable_first flattening.hpp:14-67

@@ -51,8 +51,9 @@ def _run(probs, W, backend):
         out = mgr.step(z, Phi, Gam, beta, H, gam)
         nts = [[mgr.slots[w].num_terms(m) for m in range(n)] for w in range(W)]
         recs.append((out, nts, mgr.win_counts.copy()))
+    total = mgr.total_post_mu_terms()
     mgr.close()
-    return recs
+    return recs, total
 
 
 @pytest.mark.parametrize("case", ["four_state", "five_state_two_msmt"])
@@ -65,8 +66,9 @@ def test_windows_gpu_matches_oracle_windows(case):
     else:
         probs = _managers(lambda s: W.five_state_two_msmt(seed=s, steps=6), 2, 3, 6)
         Wn = 3
-    got = _run(probs, Wn, "gpu")
-    want = _run(probs, Wn, "oracle")
+    got, total_got = _run(probs, Wn, "gpu")
+    want, total_want = _run(probs, Wn, "oracle")
+    assert total_got == total_want
     for k, ((og, ng, cg), (ow, nw, cw)) in enumerate(zip(got, want)):
         assert np.array_equal(cg, cw)
         assert ng == nw, (k, ng, nw)
