@@ -51,17 +51,23 @@ __device__ inline unsigned long long dabs_bits(double x);
 
 // Complex division by R. L. Smith, "Algorithm 116: Complex division",
 // CACM 5(8), 1962: divide through by the larger of |c|, |d| to avoid overflow.
+// The two branches are folded into one sequence with operand selects, each
+// select giving the branch's own expression (|c| >= |d|: r = d/c,
+// den = d r + c, (b r + a)/den, (b - a r)/den; |c| < |d|: r = c/d,
+// den = c r + d, (a r + b)/den, (b r - a)/den), so the results are the same
+// bits and lanes of a warp that would take different branches no longer
+// execute both.
 __device__ inline cd cdiv(cd x, cd y)
 {
     const double a = x.re, b = x.im, c = y.re, d = y.im;
-    if (dabs_bits(c) < dabs_bits(d)) {  // |c| < |d|
-        const double r = c / d;
-        const double den = c * r + d;
-        return cd{(a * r + b) / den, (b * r - a) / den};
-    }
-    const double r = d / c;
-    const double den = d * r + c;
-    return cd{(b * r + a) / den, (b - a * r) / den};
+    const bool big_c = !(dabs_bits(c) < dabs_bits(d));
+    const double p = big_c ? c : d, q = big_c ? d : c;
+    const double P = big_c ? a : b, Q = big_c ? b : a;
+    const double r = q / p;
+    const double den = q * r + p;
+    const double pr = P * r;
+    const double num = big_c ? (Q - pr) : (pr - Q);
+    return cd{(Q * r + P) / den, num / den};
 }
 
 // Comparisons of doubles on their bit patterns (integer pipe).  IEEE doubles

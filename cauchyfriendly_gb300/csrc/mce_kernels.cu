@@ -976,9 +976,18 @@ __global__ void __launch_bounds__(32) k_moments_chain(const cd* contrib, const l
         issue(k + kMomStages - 1);
         if (valid) {
             const long long r0 = k * kMomRows;
-            const int cnt = n - r0 < kMomRows ? (int)(n - r0) : kMomRows;
             const double(*slot)[32] = ring[k % kMomStages];
-            for (int r = 0; r < cnt; r++) sum += slot[r][lane];
+            if (n - r0 >= kMomRows) {
+                // all loads first, then the dependent additions back to back
+                double v[kMomRows];
+#pragma unroll
+                for (int r = 0; r < kMomRows; r++) v[r] = slot[r][lane];
+#pragma unroll
+                for (int r = 0; r < kMomRows; r++) sum += v[r];
+            } else {
+                const int cnt = (int)(n - r0);
+                for (int r = 0; r < cnt; r++) sum += slot[r][lane];
+            }
         }
     }
     cp_async_wait<0>();
