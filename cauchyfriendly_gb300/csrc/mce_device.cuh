@@ -129,6 +129,22 @@ __device__ inline int bsearch_key(const int* __restrict__ keys, int n, int key)
     return -1;
 }
 
+// Position of `key` in keys[] where keys[i] ^ x ascends (a sorted table whose
+// entries were all XORed with x), -1 if absent.
+__device__ inline int bsearch_key_xor(const int* __restrict__ keys, int n, int key, int x)
+{
+    const int target = key ^ x;
+    int lo = 0, hi = n - 1;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        const int mk = keys[mid] ^ x;
+        if (mk == target) return mid;
+        if (mk > target) hi = mid - 1;
+        else lo = mid + 1;
+    }
+    return -1;
+}
+
 // g numerator from the parent table with half storage: a key whose bit phc-1
 // is set is looked up reversed and conjugated (eval_gs.hpp:94-153).
 __device__ inline cd lookup_num(const int* __restrict__ keys, const cd* __restrict__ vals, int n, int enc, int phc)
@@ -381,11 +397,26 @@ struct ParentList {
     int* nkids;      // integrable children written as records
     int* nkids_all;  // integrable children (moments are taken over them even on the final MU)
     long long* kscan;  // exclusive scan of nkids
+    int* bflip;        // mask the MU XORed into the parent's (ascending) B table
 };
 
 struct Tables {
     int* keys;
     cd* vals;
+};
+
+// Flat g-table evaluation of one step: per group (root list index) its cell
+// count, item offset, root p-sum and kept flag; per member slot its info word,
+// p-sum and kept flag; the evaluated items.
+struct GFlat {
+    int* gnr;
+    long long* ioff;
+    double* rps2;
+    int* rflag;
+    int* minfo;
+    double* mps2;
+    int* mflag;
+    cd* gv;
 };
 
 // Per-estimator step inputs, packed by the host each step.

@@ -235,7 +235,7 @@ public:
     DevBuf<unsigned char> dcombos;
     // parent lists (double-buffered) and tables
     struct PBufs {
-        DevBuf<int> est, m, m_old, tab_cnt, B_cnt, nkids, nkids_all;
+        DevBuf<int> est, m, m_old, tab_cnt, B_cnt, nkids, nkids_all, bflip;
         DevBuf<double> A, p, b;
         DevBuf<long long> tab_off, B_off, kscan;
         int ensure(long long n, int MC)
@@ -248,6 +248,7 @@ public:
             s |= B_cnt.ensure(n + 1);
             s |= nkids.ensure(n + 1);
             s |= nkids_all.ensure(n + 1);
+            s |= bflip.ensure(n + 1);
             s |= A.ensure((n + 1) * MC * D);
             s |= p.ensure((n + 1) * MC);
             s |= b.ensure((n + 1) * D);
@@ -272,6 +273,7 @@ public:
             P.nkids = nkids.ptr;
             P.nkids_all = nkids_all.ptr;
             P.kscan = kscan.ptr;
+            P.bflip = bflip.ptr;
             return P;
         }
     } Pb[2];
@@ -334,7 +336,10 @@ public:
             return R;
         }
     } Rb;
-    DevBuf<cd> fam_mom, est_raw, scratch;
+    DevBuf<cd> fam_mom, est_raw, scratch, g_vals;
+    DevBuf<int> g_nr, g_items, g_cells, g_rflag, g_minfo, g_mflag;
+    DevBuf<long long> g_ioff, g_coff;
+    DevBuf<double> g_rps2, g_mps2;
     DevBuf<double> gscale, mom_tot;
     DevBuf<long long> goff, toff, rscan, bucket_off, rbase, scan_tmp, kall_est;
     DevBuf<int> status, owner, gcnt, gfill, members, members_tmp, is_root, cap, roots_list, alive, src,
@@ -1002,10 +1007,44 @@ public:
             if ((s = scratch.ensure((size_t)max_warps * capMC))) return s;
             gscr = scratch.ptr;
         }
+        // flat evaluation: cells and orientations, item offsets, the items
+        if ((s = g_nr.ensure(nroots + 1))) return s;
+        if ((s = g_items.ensure(nroots + 1))) return s;
+        if ((s = g_cells.ensure(nroots + 1))) return s;
+        if ((s = g_ioff.ensure(nroots + 2))) return s;
+        if ((s = g_coff.ensure(nroots + 2))) return s;
+        if ((s = g_rps2.ensure(nroots + 1))) return s;
+        if ((s = g_rflag.ensure(nroots + 1))) return s;
+        if ((s = g_minfo.ensure(nmembers + 1))) return s;
+        if ((s = g_mps2.ensure(nmembers + 1))) return s;
+        if ((s = g_mflag.ensure(nmembers + 1))) return s;
+        if ((s = ensure_scan_scratch(nroots + 1))) return s;
+        GFlat gf{g_nr.ptr, g_ioff.ptr, g_rps2.ptr, g_rflag.ptr, g_minfo.ptr, g_mps2.ptr, g_mflag.ptr, nullptr};
+        const Tables Tnv{Tn.keys.ptr, Tn.vals.ptr};
         pbeg(KID_GTABLE);
+        Kernels<D>::gtable_prep(R, roots_list.ptr, nroots, gcnt.ptr, goff.ptr, members.ptr, PV, Told, Bkeys.ptr,
+                                toff.ptr, Tnv, gf, g_items.ptr, g_cells.ptr, MC, err, lc);
+        scan_int_to_ll(g_items.ptr, g_ioff.ptr, nroots, ss, lc);
+        scan_int_to_ll(g_cells.ptr, g_coff.ptr, nroots, ss, lc);
+        pend();
+        long long gt[2] = {0, 0};
+        if (nroots > 0) {
+            MCE_CUDA(cudaMemcpyAsync(&gt[0], g_ioff.ptr + nroots, sizeof(long long), cudaMemcpyDeviceToHost,
+                                     lc.stream));
+            MCE_CUDA(cudaMemcpyAsync(&gt[1], g_coff.ptr + nroots, sizeof(long long), cudaMemcpyDeviceToHost,
+                                     lc.stream));
+            MCE_CUDA(cudaStreamSynchronize(lc.stream));
+        }
+        const long long nitems = gt[0], ncells = gt[1];
+        if ((s = g_vals.ensure(nitems + 1))) return s;
+        gf.gv = g_vals.ptr;
+        pbeg(KID_GTABLE);
+        Kernels<D>::gtable_eval(R, roots_list.ptr, nroots, nitems, goff.ptr, members.ptr, PV, Told, Bkeys.ptr,
+                                gscale.ptr, toff.ptr, Tnv, gf, MC, lc);
+        Kernels<D>::gtable_combine(R, roots_list.ptr, nroots, g_coff.ptr, ncells, gcnt.ptr, goff.ptr, members.ptr, PV,
+                                   Told, Bkeys.ptr, toff.ptr, Tnv, tcnt.ptr, alive.ptr, src.ptr, gf, MC, lc);
         Kernels<D>::gtable(R, roots_list.ptr, nroots, gcnt.ptr, goff.ptr, members.ptr, PV, Told, Bkeys.ptr, gscale.ptr,
-                           toff.ptr, Tables{Tn.keys.ptr, Tn.vals.ptr}, tcnt.ptr, alive.ptr, src.ptr, gscr, capMC, MC,
-                           err, lc, gscr_warps);
+                           toff.ptr, Tnv, tcnt.ptr, alive.ptr, src.ptr, gscr, capMC, gf, MC, err, lc, gscr_warps);
         pend();
         if (prof_mode >= 2) alg_stats(with_tp, nR, true);
         // ---- next parent list

@@ -775,6 +775,7 @@ __global__ void __launch_bounds__(128) k_mu(ParentList P, long long nP, const Es
             if (active && t == m) {
                 fam_esgc[f] = esg_c;
                 fam_bok[f] = write ? 1 : 0;
+                P.bflip[i] = esg_c;
             }
             if (mine) {
                 double bt[D], ty[D];
@@ -1449,10 +1450,207 @@ __device__ inline void own_cells(const GCtx& c, long long s, unsigned* bm, int l
     __syncwarp();
 }
 
+// ---------------------------------------------------------------------------
+// Flat g-table evaluation.  make_gtables (flattening.hpp:318-568) spends its
+// FP64 work in one cell evaluation per (term, cell) of every reduction group:
+// the root's cells, then each member's cells in the root's orientation.  Most
+// groups are small (a 3-state term of 4-6 hyperplanes has 7-16 cells, a group
+// holds one to three terms), so evaluating them a group per warp leaves most
+// lanes idle through every FP64 instruction.  Instead:
+//   k_gtable_prep  (a warp per group)  the root's cells into its output keys,
+//                  each member's orientation and mode, the p sums;
+//   k_gtable_eval  (a thread per (term, cell) of every group)  g_cell, and
+//                  the term-approximation flags;
+//   k_gtable       (a warp per group)  the sums in member order; a group whose
+//                  root is approximated out takes the serial path, which
+//                  re-derives everything in the reference's order.
+// Member info word: bits 0-15 the orientation mask relative to the root,
+// bit 30 the own-table mode.
+constexpr int kInfoOwn = 1 << 30;
+constexpr int kFlatMaxCells = 64;
+
+template <int D>
+__global__ void k_gtable_prep(GCtx c, const int* roots_list, long long nroots, const int* gcnt, const long long* goff,
+                              const int* members, const long long* toff, Tables Tnew, int* gnr, int* gitems,
+                              int* gcells, int* minfo, double* rps2, double* mps2, int* rflag, int* mflag,
+                              int* err)
+{
+    extern __shared__ unsigned smem_g[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+    const int MC = c.MC;
+    const int words = (1 << MC) > 32 ? (1 << MC) / 32 : 1;
+    const int capMC = half_cells_cap(MC, D);
+    unsigned* PB = smem_g + (size_t)wib * (2 * words + 32 + capMC);
+    unsigned* RK = PB + words;
+    int* bmk = reinterpret_cast<int*>(RK + words);
+    int* RKL = bmk + 32;
+    const TermRecs& R = c.R;
+    for (long long ri = (long long)blockIdx.x * nwb + wib; ri < nroots; ri += (long long)gridDim.x * nwb) {
+        const long long r = roots_list[ri];
+        const int m = R.m[r];
+        const int cap = (int)(toff[r + 1] - toff[r]);
+        int* okeys = Tnew.keys + toff[r];
+        if (R.flags[r] & kFlagNewChild) new_child_cells<D>(c, r, RK, PB, bmk, lane);
+        else own_cells<D>(c, r, RK, lane);
+        int nR = bm_extract(RK, m, RKL, capMC, lane);
+        __syncwarp();
+        if (nR > cap || nR > capMC) {
+            if (lane == 0) set_err(err, kErrTableOverflow);
+            nR = cap < capMC ? cap : capMC;
+        }
+        for (int k = lane; k < nR; k += 32) okeys[k] = RKL[k];
+        const int nmem = gcnt[r];
+        // groups of many cells fill warps on their own: they stay on the
+        // serial path, which keeps the items buffer small
+        const bool flat = nR > 0 && nR <= kFlatMaxCells;
+        if (lane == 0) {
+            gnr[ri] = nR;
+            gitems[ri] = flat ? (1 + nmem) * nR : 0;
+            gcells[ri] = flat ? nR : 0;
+            rps2[ri] = p_sum_sq(R.p + r * MC, m);
+            rflag[ri] = 0;
+        }
+        const long long mb = goff[r];
+        for (int j = lane; j < nmem; j += 32) {
+            const long long cm = members[mb + j];
+            const bool own = !(R.flags[cm] & kFlagNewChild) && c.P.B_cnt[R.fam[cm]] == nR;
+            const int sig = orientation_mask<D>(R.A + r * MC * D, R.A + cm * MC * D, m);
+            minfo[mb + j] = sig | (own ? kInfoOwn : 0);
+            mps2[mb + j] = p_sum_sq(R.p + cm * MC, m);
+            mflag[mb + j] = 0;
+        }
+        __syncwarp();
+    }
+}
+
+// Items of each group laid out root cells first, then each member's: item
+// (j, k) of group ri is ioff[ri] + j * nR + k.  The key of a member's item is
+// its k-th own-table key (own mode, make_gtable over the member's B) or the
+// root's k-th cell in the member's orientation.
+template <int D>
+__global__ void k_gtable_eval(GCtx c, const int* roots_list, long long nroots, const long long* ioff, long long nitems,
+                              const int* gnr, const long long* goff, const int* members, const int* minfo,
+                              const double* rps2, const double* mps2, const double* gscale_e, const long long* toff,
+                              Tables Tnew, cd* gv, int* rflag, int* mflag)
+{
+    const TermRecs& R = c.R;
+    for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < nitems;
+         x += (long long)gridDim.x * blockDim.x) {
+        // the group: the last ri with ioff[ri] <= x
+        long long lo = 0, hi = nroots;
+        while (hi - lo > 1) {
+            const long long mid = (lo + hi) >> 1;
+            if (ioff[mid] <= x) lo = mid;
+            else hi = mid;
+        }
+        const long long ri = lo;
+        const long long r = roots_list[ri];
+        const int nR = gnr[ri];
+        const long long loc = x - ioff[ri];
+        const int j = (int)(loc / nR), k = (int)(loc - (long long)j * nR);
+        const int* okeys = Tnew.keys + toff[r];
+        long long s;
+        int key;
+        double ps2;
+        int* flag;
+        if (j == 0) {
+            s = r;
+            key = okeys[k];
+            ps2 = rps2[ri];
+            flag = rflag + ri;
+        } else {
+            const long long mi = goff[r] + j - 1;
+            s = members[mi];
+            const int info = minfo[mi];
+            if (info & kInfoOwn) {
+                key = c.Bkeys[c.P.B_off[R.fam[s]] + k];
+            } else {
+                const int m = R.m[r];
+                const int top = 1 << (m - 1), rev = (1 << m) - 1;
+                const int sig = info & 0xffff;
+                key = okeys[k] ^ ((sig & top) ? (sig ^ rev) : sig);
+            }
+            ps2 = mps2[mi];
+            flag = mflag + mi;
+        }
+        const cd v = g_cell<D>(c, s, key, gscale_e[R.est[r]]);
+        gv[x] = v;
+        if (above_approx_threshold(ps2, v.re, v.im)) *flag = 1;
+    }
+}
+
+// The sums of kept groups, a thread per root cell (coff: the flat groups'
+// exclusive cell offsets): the root's value plus each member that is not
+// approximated out, in member order (flattening.hpp:493-552), from the
+// evaluated items.  A member's value for root cell bi is at the root cell
+// bj ^ sigf, bj the canonical form of bi ^ sig (own mode: at bj in the
+// member's own table).
+template <int D>
+__global__ void k_gtable_combine(GCtx c, const int* roots_list, long long nroots, const long long* coff,
+                                 long long ncells, const int* gcnt, const long long* goff, const int* members,
+                                 const long long* toff, Tables Tnew, int* tcnt, int* alive, int* src, const int* rflag,
+                                 const long long* ioff, const int* gnr, const int* minfo, const int* mflag,
+                                 const cd* gv)
+{
+    const TermRecs& R = c.R;
+    for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < ncells;
+         x += (long long)gridDim.x * blockDim.x) {
+        long long lo = 0, hi = nroots;
+        while (hi - lo > 1) {
+            const long long mid = (lo + hi) >> 1;
+            if (coff[mid] <= x) lo = mid;
+            else hi = mid;
+        }
+        const long long ri = lo;
+        if (!rflag[ri]) continue;  // the serial path takes this group
+        const long long r = roots_list[ri];
+        const int m = R.m[r];
+        const int top = 1 << (m - 1), rev = (1 << m) - 1;
+        const int nR = gnr[ri];
+        const int k = (int)(x - coff[ri]);
+        const long long base = ioff[ri];
+        const int* okeys = Tnew.keys + toff[r];
+        const int nmem = gcnt[r];
+        const long long mb = goff[r];
+        const int bi = okeys[k];
+        cd acc = gv[base + k];
+        for (int j = 0; j < nmem; j++) {
+            if (!mflag[mb + j]) continue;
+            const int info = minfo[mb + j];
+            const int sig = info & 0xffff;
+            const int sigf = (sig & top) ? (sig ^ rev) : sig;
+            const int t = bi ^ sig;
+            const bool cj = t & top;
+            const int bj = cj ? (t ^ rev) : t;
+            int idx;
+            if (info & kInfoOwn) {
+                if (bj < 0 || bj >= (1 << m)) continue;
+                // the member's table is its family's B_mu: ascending before
+                // the MU's XOR, so search through the XOR
+                const int fam = R.fam[members[mb + j]];
+                idx = bsearch_key_xor(c.Bkeys + c.P.B_off[fam], c.P.B_cnt[fam], bj, c.P.bflip[fam]);
+            } else {
+                idx = (bj == (bi ^ sigf)) ? k : bsearch_key(okeys, nR, bj ^ sigf);
+            }
+            if (idx < 0) continue;
+            const cd v = gv[base + (long long)(j + 1) * nR + idx];
+            acc = cadd(acc, cj ? cconj(v) : v);
+        }
+        Tnew.vals[toff[r] + k] = acc;
+        if (k == 0) {
+            alive[r] = 1;
+            tcnt[r] = nR;
+            src[r] = (int)r;
+        }
+    }
+}
+
 template <int D>
 __global__ void k_gtable(GCtx c, const int* roots_list, long long nroots, const int* gcnt, const long long* goff,
                          const int* members, const double* gscale_e, const long long* toff, Tables Tnew, int* tcnt,
-                         int* alive, int* src, cd* scratch, long long scratch_per_warp, int* err)
+                         int* alive, int* src, cd* scratch, long long scratch_per_warp, const int* rflag,
+                         const long long* ioff, const int* gnr, const int* minfo, const int* mflag, const cd* gv,
+                         int* err)
 {
     extern __shared__ unsigned smem_g[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
@@ -1468,6 +1666,8 @@ __global__ void k_gtable(GCtx c, const int* roots_list, long long nroots, const 
     cd* scr = scratch + gw * scratch_per_warp;
     const TermRecs& R = c.R;
     for (long long ri = gw; ri < nroots; ri += (long long)gridDim.x * nwb) {
+        if (rflag[ri]) continue;  // kept root: k_gtable_combine
+        // the root is approximated out (or has no cells): the serial path
         const long long r = roots_list[ri];
         const int m = R.m[r];
         const int e = R.est[r];
@@ -1862,7 +2062,8 @@ template <int D>
 void Kernels<D>::gtable(TermRecs R, const int* roots_list, long long nroots, const int* gcnt, const long long* goff,
                         const int* members, ParentList P, Tables Told, const int* Bkeys, const double* gscale,
                         const long long* toff, Tables Tnew, int* tcnt, int* alive, int* src, cd* scratch,
-                        long long scratch_per_warp, int MC, int* err, const LaunchCfg& c, long long max_warps)
+                        long long scratch_per_warp, const GFlat& f, int MC, int* err, const LaunchCfg& c,
+                        long long max_warps)
 {
     if (nroots == 0) return;
     GCtx ctx{R, P, Told, Bkeys, MC};
@@ -1879,7 +2080,57 @@ void Kernels<D>::gtable(TermRecs R, const int* roots_list, long long nroots, con
     if (max_warps > 0 && (long long)grid * warps > max_warps) grid = (int)(max_warps / warps);
     ++g_launches;
     k_gtable<D><<<grid, warps * 32, sm, c.stream>>>(ctx, roots_list, nroots, gcnt, goff, members, gscale, toff, Tnew,
-                                                    tcnt, alive, src, scratch, scratch_per_warp, err);
+                                                    tcnt, alive, src, scratch, scratch_per_warp, f.rflag, f.ioff,
+                                                    f.gnr, f.minfo, f.mflag, f.gv, err);
+}
+
+template <int D>
+void Kernels<D>::gtable_prep(TermRecs R, const int* roots_list, long long nroots, const int* gcnt,
+                             const long long* goff, const int* members, ParentList P, Tables Told, const int* Bkeys,
+                             const long long* toff, Tables Tnew, const GFlat& f, int* gitems, int* gcells, int MC,
+                             int* err, const LaunchCfg& c)
+{
+    if (nroots == 0) return;
+    GCtx ctx{R, P, Told, Bkeys, MC};
+    const int words = (1 << MC) > 32 ? (1 << MC) / 32 : 1;
+    const size_t pw = (size_t)(2 * words + 32 + half_cells_cap(MC, D)) * 4;
+    int warps = (int)(96 * 1024 / pw);
+    if (warps > 4) warps = 4;
+    if (warps < 1) warps = 1;
+    const size_t sm = pw * warps;
+    cudaFuncSetAttribute(k_gtable_prep<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    ++g_launches;
+    k_gtable_prep<D><<<grid_for(nroots, warps, c.num_sms, 16), warps * 32, sm, c.stream>>>(
+        ctx, roots_list, nroots, gcnt, goff, members, toff, Tnew, f.gnr, gitems, gcells, f.minfo, f.rps2, f.mps2,
+        f.rflag, f.mflag, err);
+}
+
+template <int D>
+void Kernels<D>::gtable_combine(TermRecs R, const int* roots_list, long long nroots, const long long* coff,
+                                long long ncells, const int* gcnt, const long long* goff, const int* members,
+                                ParentList P, Tables Told, const int* Bkeys, const long long* toff, Tables Tnew,
+                                int* tcnt, int* alive, int* src, const GFlat& f, int MC, const LaunchCfg& c)
+{
+    if (ncells == 0) return;
+    GCtx ctx{R, P, Told, Bkeys, MC};
+    ++g_launches;
+    k_gtable_combine<D><<<grid_for(ncells, 128, c.num_sms, 16), 128, 0, c.stream>>>(
+        ctx, roots_list, nroots, coff, ncells, gcnt, goff, members, toff, Tnew, tcnt, alive, src, f.rflag, f.ioff,
+        f.gnr, f.minfo, f.mflag, f.gv);
+}
+
+template <int D>
+void Kernels<D>::gtable_eval(TermRecs R, const int* roots_list, long long nroots, long long nitems,
+                             const long long* goff, const int* members, ParentList P, Tables Told, const int* Bkeys,
+                             const double* gscale, const long long* toff, Tables Tnew, const GFlat& f, int MC,
+                             const LaunchCfg& c)
+{
+    if (nitems == 0) return;
+    GCtx ctx{R, P, Told, Bkeys, MC};
+    ++g_launches;
+    k_gtable_eval<D><<<grid_for(nitems, 128, c.num_sms, 16), 128, 0, c.stream>>>(
+        ctx, roots_list, nroots, f.ioff, nitems, f.gnr, goff, members, f.minfo, f.rps2, f.mps2, gscale, toff, Tnew,
+        f.gv, f.rflag, f.mflag);
 }
 
 template <int D>

@@ -62,8 +62,20 @@ struct Kernels {
     static void gtable(TermRecs R, const int* roots_list, long long nroots, const int* gcnt,
                        const long long* goff, const int* members, ParentList P, Tables Told, const int* Bkeys,
                        const double* gscale, const long long* toff, Tables Tnew, int* tcnt, int* alive,
-                       int* src, cd* scratch, long long scratch_per_warp, int MC, int* err,
+                       int* src, cd* scratch, long long scratch_per_warp, const GFlat& f, int MC, int* err,
                        const LaunchCfg& c, long long max_warps = 0);
+    static void gtable_prep(TermRecs R, const int* roots_list, long long nroots, const int* gcnt,
+                            const long long* goff, const int* members, ParentList P, Tables Told, const int* Bkeys,
+                            const long long* toff, Tables Tnew, const GFlat& f, int* gitems, int* gcells, int MC,
+                            int* err, const LaunchCfg& c);
+    static void gtable_combine(TermRecs R, const int* roots_list, long long nroots, const long long* coff,
+                               long long ncells, const int* gcnt, const long long* goff, const int* members,
+                               ParentList P, Tables Told, const int* Bkeys, const long long* toff, Tables Tnew,
+                               int* tcnt, int* alive, int* src, const GFlat& f, int MC, const LaunchCfg& c);
+    static void gtable_eval(TermRecs R, const int* roots_list, long long nroots, long long nitems,
+                            const long long* goff, const int* members, ParentList P, Tables Told, const int* Bkeys,
+                            const double* gscale, const long long* toff, Tables Tnew, const GFlat& f, int MC,
+                            const LaunchCfg& c);
     // Next parent list (shape-bucketed, stable) from the surviving roots.
     static void compact(TermRecs R, const int* alive, const int* src, long long nR, const int* new_slot,
                         const long long* toff, const int* tcnt, ParentList Pn, int MC, const LaunchCfg& c);
