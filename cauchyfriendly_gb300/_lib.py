@@ -26,6 +26,9 @@ SIGNATURES = {
     "mce_batch_create": (_vp, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _ip, _dp, _dp,
                                _dp, _dp, _dp, ctypes.c_int, _ip]),
     "mce_batch_step": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int, _ip]),
+    "mce_cpdf_1d_grid": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_int, _dp, _dp]),
+    "mce_draw_bar_nu": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_int, _dp]),
     "mce_batch_step_noalloc": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int, _ip]),
     "mce_batch_run": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int, _dp,
                                      _dp, _dp, _ip, _lp]),
@@ -64,7 +67,7 @@ def header_functions():
     """Function names declared in include/mce_c_api.h."""
     txt = open(HEADER).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-    return sorted(set(re.findall(r"\b(mce_[a-z_]+)\s*\(", txt)))
+    return sorted(set(re.findall(r"\b(mce_[a-z0-9_]+)\s*\(", txt)))
 
 
 def load(build_if_missing=True):

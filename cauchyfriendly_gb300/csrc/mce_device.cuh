@@ -14,6 +14,7 @@ namespace mce {
 constexpr int kMaxRows = 31;    // keys are 32-bit sign masks (cauchy_estimator.hpp:231-235)
 constexpr int kMaxDim = 8;
 constexpr int kMaxGamma = 8;   // process-noise columns per step
+constexpr double kPi = 3.14159265358979323846;                      // PI (M_PI)
 constexpr double kTwoPiInv = 1.0 / (2.0 * 3.14159265358979323846);  // RECIPRICAL_TWO_PI
 constexpr double kCoalignEps = 1e-8;   // COALIGN_TP_EPS == COALIGN_MU_EPS
 constexpr double kMuEps = 1e-10;       // MU_EPS

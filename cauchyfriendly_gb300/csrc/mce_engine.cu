@@ -180,6 +180,8 @@ public:
                            int* keys, double* g) = 0;
     virtual long long total_cells(int est) = 0;
     virtual int reset() = 0;
+    virtual int cpdf_1d_grid(int est, int marg, const double* bar_nu, double low, double high, double res,
+                             int max_points, double* xs, double* ys) = 0;
     // waits for the work the engine queued (after a step that stopped early)
     virtual void drain() = 0;
 
@@ -541,6 +543,7 @@ public:
         master_step = 0;
         nP = 0;
         post_mu_terms = 0;
+        cpdf_step.assign(cpdf_step.size(), -1);  // the pdf cache belongs to the old terms
         device_errors = 0;
         MCE_CUDA(cudaMemset(counters.ptr, 0, 8 * sizeof(int)));
         return MCE_OK;
@@ -1108,6 +1111,79 @@ public:
     void k_gather_bounds(const long long* scan, int E_);
     void k_status_init(TermRecs R, long long nR);
 
+    // ---- marginal 1-D pdf: CauchyCPDFGridDispatcher1D (cpdf_ndim.hpp:2017-2139)
+    // over PointWiseNDimCauchyCPDF::evaluate_1D_marginal_cpdf (:1233-1352),
+    // with the reference's per-estimator cache of per-term constants, kept on
+    // the device and keyed by (master step, marginal index)
+    std::vector<int> cpdf_step, cpdf_marg;
+    std::vector<long long> cpdf_n;
+    std::vector<std::unique_ptr<DevBuf<double>>> cpdf_tt;
+    DevBuf<double> cpdf_nu, cpdf_x, cpdf_y;
+
+    int cpdf_1d_grid(int e, int marg, const double* bar_nu, double low, double high, double res, int max_points,
+                     double* xs, double* ys) override
+    {
+        if (e < 0 || e >= E || marg < 0 || marg >= D || !bar_nu) return MCE_ERR_ARG;
+        if (!(high > low) || !(res > 0)) return MCE_ERR_ARG;
+        const double span = (high - low + res - 1e-15) / res;
+        if (!(span < 1e8)) {
+            set_error("cpdf grid: too many points");
+            return MCE_ERR_ARG;
+        }
+        const int npts = (int)span + 1;  // reset_grid, cpdf_ndim.hpp:2055-2072
+        if (!xs || !ys) return npts;
+        if (npts > max_points) {
+            set_error("cpdf grid: " + std::to_string(npts) + " points do not fit in " + std::to_string(max_points));
+            return MCE_ERR_ARG;
+        }
+        if (master_step < 1) {
+            set_error("cpdf: the estimator has not been stepped");
+            return MCE_ERR_ARG;
+        }
+        if (master_step >= est[e].num_updates) {
+            // evaluate_point_grid refuses the last step: its g-tables are skipped
+            set_error("cpdf: the last step keeps no g-tables");
+            return MCE_ERR_DONE;
+        }
+        for (int i = 0; i < npts; i++) {
+            double x = low + i * res;
+            if (x > high) x = high;
+            xs[i] = x;
+        }
+        if ((int)cpdf_step.size() != E) {
+            cpdf_step.assign(E, -1);
+            cpdf_marg.assign(E, -1);
+            cpdf_n.assign(E, -1);
+            cpdf_tt.clear();
+            cpdf_tt.resize(E);
+        }
+        const long long a = hpstart[e], n = hpstart[e + 1] - a;
+        int exact = 0, s;
+        // the cache also keys on the term count: a reset cannot leave one
+        // whose size differs from the terms (the reference would read past it)
+        if (cpdf_step[e] != master_step || cpdf_marg[e] != marg || cpdf_n[e] != n) {
+            // the first evaluation at this step and index: the exact formula at
+            // the first point, and the per-term constants cached
+            if (!cpdf_tt[e]) cpdf_tt[e].reset(new DevBuf<double>());
+            if ((s = cpdf_tt[e]->ensure((size_t)(n + 1) * 8))) return s;
+            if ((s = cpdf_nu.ensure(D))) return s;
+            MCE_CUDA(cudaMemcpyAsync(cpdf_nu.ptr, bar_nu, sizeof(double) * D, cudaMemcpyHostToDevice, lc.stream));
+            Kernels<D>::cpdf1d_terms(Pb[cur].view(), a, n, marg, cpdf_nu.ptr,
+                                     Tables{Tb[cur].keys.ptr, Tb[cur].vals.ptr}, MC, cpdf_tt[e]->ptr, lc);
+            cpdf_step[e] = master_step;
+            cpdf_marg[e] = marg;
+            cpdf_n[e] = n;
+            exact = 1;
+        }
+        if ((s = cpdf_x.ensure(npts))) return s;
+        if ((s = cpdf_y.ensure(npts))) return s;
+        MCE_CUDA(cudaMemcpyAsync(cpdf_x.ptr, xs, sizeof(double) * npts, cudaMemcpyHostToDevice, lc.stream));
+        cpdf1d_points(cpdf_tt[e]->ptr, n, cpdf_x.ptr, npts, exact, est[e].fz[0], cpdf_y.ptr, lc);
+        MCE_CUDA(cudaMemcpyAsync(ys, cpdf_y.ptr, sizeof(double) * npts, cudaMemcpyDeviceToHost, lc.stream));
+        MCE_CUDA(cudaStreamSynchronize(lc.stream));
+        return npts;
+    }
+
     long long total_cells(int e) override
     {
         if (e < 0 || e >= E || nP == 0) return 0;
@@ -1543,6 +1619,20 @@ int mce_terms_per_shape(mce_handle* h, int e, int* out, int n)
     if (bad(h, e) || !out) return MCE_ERR_ARG;
     const auto& t = h->eng->est[e].tps;
     for (int i = 0; i < n; i++) out[i] = i < (int)t.size() ? t[i] : 0;
+    return MCE_OK;
+}
+int mce_cpdf_1d_grid(mce_handle* h, int e, int marg_idx, const double* bar_nu, double grid_low, double grid_high,
+                     double grid_res, int max_points, double* x, double* y)
+{
+    if (bad(h, e)) return MCE_ERR_ARG;
+    return h->eng->cpdf_1d_grid(e, marg_idx, bar_nu, grid_low, grid_high, grid_res, max_points, x, y);
+}
+int mce_draw_bar_nu(long long seed, int d, double* bar_nu)
+{
+    if (d < 1 || !bar_nu) return MCE_ERR_ARG;
+    if (seed >= 0) srand((unsigned)seed);
+    // random_uniform_open (random_variables.hpp:36-40), doubled
+    for (int i = 0; i < d; i++) bar_nu[i] = 2 * (((double)rand() + 1.0) / ((double)RAND_MAX + 2.0));
     return MCE_OK;
 }
 long long mce_post_mu_terms(mce_handle* h) { return h ? h->eng->post_mu_terms : MCE_ERR_ARG; }

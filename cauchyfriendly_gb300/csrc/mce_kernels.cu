@@ -2142,6 +2142,106 @@ void Kernels<D>::compact(TermRecs R, const int* alive, const int* src, long long
     k_compact<D><<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(R, alive, src, nR, new_slot, toff, tcnt, Pn, MC);
 }
 
+// ---------------------------------------------------------------------------
+// Marginal 1-D conditional pdf over the current terms
+// (PointWiseNDimCauchyCPDF::evaluate_1D_marginal_cpdf, cpdf_ndim.hpp:1233-1352).
+// k_cpdf1d_terms: per term, p_cc = sum_j p_j |A_j,marg|, the two sign
+// encodings (a row with |A_j,marg| <= 1e-15 takes the sign of A_j . bar_nu),
+// the two g numerators and the cache entry (a, b, w, s).  Each term's record
+// is 8 doubles: g_lhs, g_rhs, p_cc, s, a, b.
+template <int D>
+__global__ void k_cpdf1d_terms(ParentList P, long long a, long long n, int marg, const double* bar_nu, Tables T,
+                               int MC, double* tt)
+{
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
+        const long long i = a + j;
+        const int m = P.m[i];
+        const double* A = P.A + i * MC * D;
+        const double* p = P.p + i * MC;
+        double p_cc = 0;
+        int lhs = 0, rhs = 0;
+        for (int l = 0; l < m; l++) {
+            const double acj = A[l * D + marg];
+            const double fa = fabs(acj);
+            p_cc += p[l] * fa;
+            bool left;
+            if (fa > 1e-15) {
+                left = acj > 0;
+            } else {
+                double ip = 0.0;
+                for (int k = 0; k < D; k++) ip += A[l * D + k] * bar_nu[k];
+                left = ip > 0;
+            }
+            if (left) lhs |= 1 << l;
+            else rhs |= 1 << l;
+        }
+        const int* keys = T.keys + P.tab_off[i];
+        const cd* vals = T.vals + P.tab_off[i];
+        const int cnt = P.tab_cnt[i];
+        const cd gl = lookup_num(keys, vals, cnt, lhs, m);
+        const cd gr = lookup_num(keys, vals, cnt, rhs, m);
+        const double s = P.b[i * D + marg];
+        double* o = tt + j * 8;
+        o[0] = gl.re;
+        o[1] = gl.im;
+        o[2] = gr.re;
+        o[3] = gr.im;
+        o[4] = p_cc;
+        o[5] = s;
+        o[6] = gr.im / kPi;
+        o[7] = (gr.re * p_cc - gr.im * s) / kPi;
+    }
+}
+
+template <int D>
+void Kernels<D>::cpdf1d_terms(ParentList P, long long a, long long n, int marg, const double* bar_nu, Tables T, int MC,
+                              double* tt, const LaunchCfg& c)
+{
+    if (n == 0) return;
+    ++g_launches;
+    k_cpdf1d_terms<D><<<grid_for(n, 128, c.num_sms, 16), 128, 0, c.stream>>>(P, a, n, marg, bar_nu, T, MC, tt);
+}
+
+#if MCE_COMMON_UNIT
+// One thread per point, the terms summed in order.  Points below `exact`
+// take the complex formula (fx * 1/(2 pi) / fz), the others the cached one
+// (fx / fz).
+__global__ void k_cpdf1d_points(const double* tt, long long n, const double* xs, int npts, int exact, double fz,
+                                double* ys)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= npts) return;
+    const double x = xs[q];
+    double fx = 0;
+    if (q < exact) {
+        for (long long j = 0; j < n; j++) {
+            const double* t = tt + j * 8;
+            const double b_c = t[5] - x;
+            const cd g = csub(cdiv(mkcd(t[0], t[1]), mkcd(t[4], b_c)), cdiv(mkcd(t[2], t[3]), mkcd(-t[4], b_c)));
+            fx += g.re;
+        }
+        ys[q] = fx * kTwoPiInv / fz;
+    } else {
+        for (long long j = 0; j < n; j++) {
+            const double* t = tt + j * 8;
+            const double w2 = t[4] * t[4];
+            double xms = x - t[5];
+            xms *= xms;
+            fx += (t[6] * x + t[7]) / (w2 + xms);
+        }
+        ys[q] = fx / fz;
+    }
+}
+
+void cpdf1d_points(const double* tt, long long n, const double* xs, int npts, int exact, double fz, double* ys,
+                   const LaunchCfg& c)
+{
+    if (npts <= 0) return;
+    ++g_launches;
+    k_cpdf1d_points<<<(npts + 63) / 64, 64, 0, c.stream>>>(tt, n, xs, npts, exact, fz, ys);
+}
+#endif  // MCE_COMMON_UNIT
+
 #if MCE_COMMON_UNIT
 void group_count(const int* status, const int* owner, long long nR, int* gcnt, const LaunchCfg& c)
 {

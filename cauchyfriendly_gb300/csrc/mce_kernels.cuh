@@ -68,6 +68,8 @@ struct Kernels {
                             const long long* goff, const int* members, ParentList P, Tables Told, const int* Bkeys,
                             const long long* toff, Tables Tnew, const GFlat& f, int* gitems, int* gcells, int MC,
                             int* err, const LaunchCfg& c);
+    static void cpdf1d_terms(ParentList P, long long a, long long n, int marg, const double* bar_nu, Tables T,
+                             int MC, double* tt, const LaunchCfg& c);
     static void gtable_combine(TermRecs R, const int* roots_list, long long nroots, const long long* coff,
                                long long ncells, const int* gcnt, const long long* goff, const int* members,
                                ParentList P, Tables Told, const int* Bkeys, const long long* toff, Tables Tnew,
@@ -83,6 +85,9 @@ struct Kernels {
 
 // Shape-agnostic kernels.
 void group_count(const int* status, const int* owner, long long nR, int* gcnt, const LaunchCfg& c);
+// marginal 1-D pdf at npts points from the per-term records of k_cpdf1d_terms
+void cpdf1d_points(const double* tt, long long n, const double* xs, int npts, int exact, double fz, double* ys,
+                   const LaunchCfg& c);
 void group_fill(const int* status, const int* owner, long long nR, const long long* goff, int* gfill,
                 int* members, const LaunchCfg& c);
 void group_sort(const int* gcnt, const long long* goff, long long nR, const int* members_in, int* members_out,

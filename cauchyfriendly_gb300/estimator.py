@@ -169,6 +169,29 @@ class BatchedCauchyEstimator:
     def set_win_num(self, w):
         _lib.check(self._lib.mce_set_window_number(self._h, int(w)), "mce_set_window_number")
 
+    def cpdf_1d_grid(self, e, marg_idx, gridx_low, gridx_high, gridx_resolution, bar_nu):
+        """Marginal 1-D conditional pdf of estimator e on the grid
+        gridx_low..gridx_high step gridx_resolution
+        (CauchyCPDFGridDispatcher1D, include/cpdf_ndim.hpp:2017-2139);
+        returns (X, Y)."""
+        nu = _f64(bar_nu).reshape(self.d)
+        n = self._lib.mce_cpdf_1d_grid(self._h, int(e), int(marg_idx), _p(nu), float(gridx_low),
+                                       float(gridx_high), float(gridx_resolution), 0, None, None)
+        _lib.check(n, "mce_cpdf_1d_grid")
+        X, Y = np.zeros(n), np.zeros(n)
+        n = self._lib.mce_cpdf_1d_grid(self._h, int(e), int(marg_idx), _p(nu), float(gridx_low),
+                                       float(gridx_high), float(gridx_resolution), n, _p(X), _p(Y))
+        _lib.check(n, "mce_cpdf_1d_grid")
+        return X, Y
+
+
+def draw_bar_nu(d, seed=-1):
+    """The d draws of PointWiseNDimCauchyCPDF's constructor
+    (include/cpdf_ndim.hpp:385-389) from libc rand(); seed >= 0 seeds it first."""
+    out = np.zeros(int(d))
+    _lib.check(_lib.load().mce_draw_bar_nu(int(seed), int(d), _p(out)), "mce_draw_bar_nu")
+    return out
+
 
 class CauchyEstimator(BatchedCauchyEstimator):
     """CauchyEstimator(A0, p0, b0, steps, d, cmcc, pncc, p, print_basic_info)
@@ -221,3 +244,18 @@ class CauchyEstimator(BatchedCauchyEstimator):
     @property
     def numeric_moment_errors(self):
         return self.errors()
+
+    def get_marginal_1D_pointwise_cpdf(self, marg_idx, gridx_low, gridx_high, gridx_resolution, log_dir=None):
+        """CauchyEstimator.get_marginal_1D_pointwise_cpdf
+        (scripts/swig/cauchy/cauchy_estimator.py:1003-1031): (X, Y) on the
+        grid.  The pdf's random direction bar_nu is drawn from libc rand() on
+        the first call, as the reference's pdf object is."""
+        if getattr(self, "_bar_nu", None) is None:
+            self._bar_nu = draw_bar_nu(self.d)
+        return self.cpdf_1d_grid(0, marg_idx, gridx_low, gridx_high, gridx_resolution, self._bar_nu)
+
+    def get_1D_pointwise_cpdf(self, gridx_low, gridx_high, gridx_resolution, log_dir=None):
+        """The 1-state case of get_marginal_1D_pointwise_cpdf (cauchy_estimator.py:1033-1043)."""
+        if self.d != 1:
+            raise ValueError("get_1D_pointwise_cpdf needs a 1-state estimator")
+        return self.get_marginal_1D_pointwise_cpdf(0, gridx_low, gridx_high, gridx_resolution, log_dir)

@@ -168,6 +168,20 @@ def pycauchy_single_step_reset(h, A0, p0, b0, xbar):
     h.est.reset()
 
 
+def pycauchy_get_marginal_1D_pointwise_cpdf(h, marg_idx1, gridx_low, gridx_high, gridx_resolution, log_dir=None):
+    """pycauchy.hpp:890-931: the grid as (x, y) pairs, flattened, and its size.
+    The pdf object (and its rand() draws) is made on the first call."""
+    X, Y = h.est.get_marginal_1D_pointwise_cpdf(int(marg_idx1), gridx_low, gridx_high, gridx_resolution)
+    pts = np.empty(2 * X.size)
+    pts[0::2], pts[1::2] = X, Y
+    return pts, int(X.size)
+
+
+def pycauchy_get_1D_pointwise_cpdf(h, gridx_low, gridx_high, gridx_resolution, log_dir=None):
+    """pycauchy.hpp:934-944"""
+    return pycauchy_get_marginal_1D_pointwise_cpdf(h, 0, gridx_low, gridx_high, gridx_resolution, log_dir)
+
+
 def pycauchy_single_step_shutdown(h):
     """pycauchy.hpp:752"""
     h.est.close()

@@ -116,6 +116,27 @@ int mce_get_errors(mce_handle* h, int est);
 long long mce_num_terms(mce_handle* h, int est);
 /* terms_per_shape (n entries, shape index = hyperplane count). */
 int mce_terms_per_shape(mce_handle* h, int est, int* out, int n);
+/* Marginal 1-D conditional pdf of estimator `est` on the grid
+ * grid_low, grid_low + grid_res, ..., grid_high (the last point clamped), as
+ * CauchyCPDFGridDispatcher1D (include/cpdf_ndim.hpp:2017-2139) evaluates
+ * PointWiseNDimCauchyCPDF::evaluate_1D_marginal_cpdf (:1233-1352) and
+ * pycauchy_get_marginal_1D_pointwise_cpdf returns it
+ * (scripts/swig/cauchy/pycauchy.hpp:890-931).  bar_nu[d] is the pdf object's
+ * random direction for rows orthogonal to the marginal axis
+ * (mce_draw_bar_nu).  The first evaluation at a step and marginal index takes
+ * the exact formula at the first grid point and caches per-term constants;
+ * later evaluations at that step and index use the cache, as the reference
+ * does.  x, y receive the points; with x or y NULL only the point count is
+ * returned.  Returns the number of points or a negative status
+ * (MCE_ERR_DONE after the last step, whose g-tables are skipped). */
+int mce_cpdf_1d_grid(mce_handle* h, int est, int marg_idx, const double* bar_nu, double grid_low, double grid_high,
+                     double grid_res, int max_points, double* x, double* y);
+
+/* The draws of PointWiseNDimCauchyCPDF's constructor
+ * (include/cpdf_ndim.hpp:385-388): bar_nu[i] = 2 (rand() + 1)/(RAND_MAX + 2)
+ * for i < d.  seed >= 0 calls srand(seed) first. */
+int mce_draw_bar_nu(long long seed, int d, double* bar_nu);
+
 /* Sum over all updates and estimators of the terms present after each MU. */
 long long mce_post_mu_terms(mce_handle* h);
 int mce_master_step(mce_handle* h);

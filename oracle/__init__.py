@@ -274,6 +274,20 @@ class Oracle(_EstimatorBase):
     def errors(self):
         return int(self._l.lib.orc_errors(self.h))
 
+    def cpdf_1d_grid(self, marg, bar_nu, low, high, res, max_points=100000):
+        """Marginal 1-D pdf on the grid low..high step res (the reference's
+        CauchyCPDFGridDispatcher1D); returns (x, y) or raises with the status."""
+        f = self._l.lib.orc_cpdf_1d_grid
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                      ctypes.c_int, _dp, _dp]
+        nu = _arr(bar_nu)
+        xs, ys = np.zeros(max_points), np.zeros(max_points)
+        n = f(self.h, int(marg), _ptr(nu), float(low), float(high), float(res), max_points, _ptr(xs), _ptr(ys))
+        if n < 0:
+            raise RuntimeError("orc_cpdf_1d_grid returned %d" % n)
+        return xs[:n].copy(), ys[:n].copy()
+
 
 class OracleSlot:
     """A window slot of n_mgr oracle estimators with the batch interface the
@@ -336,6 +350,18 @@ class Reference(_EstimatorBase):
 
     def last_step_seconds(self):
         return float(self._l.lib.ref_last_step_seconds(self.h))
+
+    def cpdf_1d_grid(self, marg, low, high, res, max_points=100000):
+        """The reference's own marginal 1-D pdf grid; returns (x, y, bar_nu)."""
+        f = self._l.lib.ref_cpdf_1d_grid
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                      ctypes.c_int, _dp, _dp, _dp]
+        xs, ys, nu = np.zeros(max_points), np.zeros(max_points), np.zeros(self.d)
+        n = f(self.h, int(marg), float(low), float(high), float(res), max_points, _ptr(xs), _ptr(ys), _ptr(nu))
+        if n < 0:
+            raise RuntimeError("ref_cpdf_1d_grid returned %d" % n)
+        return xs[:n].copy(), ys[:n].copy(), nu
 
 
 def run(est, prob, record_terms_upto=0):

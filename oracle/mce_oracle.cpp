@@ -340,6 +340,11 @@ struct Term {
     GTable g;                                // table built at this step
 };
 
+// Per-term constants of the 1-D marginal pdf (Cached1DCPDFTerm, cpdf_ndim.hpp:216-222).
+struct Cpdf1DTerm {
+    double a, b, w, s;
+};
+
 struct Estimator {
     int d, cmcc, pncc, p, num_steps, shape_range;
     int master_step = 0;
@@ -356,6 +361,9 @@ struct Estimator {
     bool skip_post_mu = false;
     std::vector<std::vector<int>> combos;  // per shape
     long long post_mu_terms = 0;           // sum over steps of terms after MU
+    // 1-D marginal pdf cache, keyed like the reference's by (master step, index)
+    std::vector<Cpdf1DTerm> cpdf1d_cache;
+    int cpdf1d_step = -1, cpdf1d_marg = -1;
 };
 
 // ----------------------------------------------------------------------------
@@ -1294,6 +1302,72 @@ static void step_rest(Estimator& E, double msmt, const double* Phi, const double
 
 // ----------------------------------------------------------------------------
 // C ABI
+// ----------------------------------------------------------------------------
+// Marginal 1-D conditional pdf: PointWiseNDimCauchyCPDF::evaluate_1D_marginal_cpdf
+// (cpdf_ndim.hpp:1233-1352) over the current terms in shape/index order, and
+// the grid of CauchyCPDFGridDispatcher1D (cpdf_ndim.hpp:2055-2139), which
+// evaluates every point with caching on: the first evaluation at a master step
+// and marginal index takes the exact complex formula and fills the per-term
+// cache (a, b, w, s); every later one at that step and index sums
+// (a x + b) / (w^2 + (x - s)^2).
+
+// number of grid points: reset_grid (cpdf_ndim.hpp:2055-2072)
+static int cpdf_grid_points(double low, double high, double res)
+{
+    return (int)((high - low + res - 1e-15) / res) + 1;
+}
+
+static double cpdf1d_eval(Estimator& E, int marg, double x, const double* bar_nu)
+{
+    const int d = E.d;
+    const bool use_cache = E.cpdf1d_step == E.master_step && E.cpdf1d_marg == marg;
+    double fx = 0;
+    if (use_cache) {
+        for (const Cpdf1DTerm& c : E.cpdf1d_cache) {
+            const double w2 = c.w * c.w;
+            double xms = x - c.s;
+            xms *= xms;
+            fx += (c.a * x + c.b) / (w2 + xms);
+        }
+        return fx / __real__ E.fz;
+    }
+    E.cpdf1d_step = E.master_step;
+    E.cpdf1d_marg = marg;
+    E.cpdf1d_cache.clear();
+    for (const Term& T : E.terms) {
+        const int m = T.m;
+        const double b_c = T.b[marg] - x;
+        double p_cc = 0;
+        int lhs = 0, rhs = 0;
+        for (int j = 0; j < m; j++) {
+            const double a_cj = T.A[j * d + marg];
+            const double fa = fabs(a_cj);
+            p_cc += T.p[j] * fa;
+            bool left;
+            if (fa > 1e-15) {
+                left = a_cj > 0;
+            } else {
+                double ip = 0.0;  // dot_prod, cauchy_linalg.hpp:559-565
+                for (int l = 0; l < d; l++) ip += T.A[j * d + l] * bar_nu[l];
+                left = ip > 0;
+            }
+            if (left) lhs |= 1 << j;
+            else rhs |= 1 << j;
+        }
+        const cplx gl = lookup_num(T.gp.get(), lhs, m);
+        const cplx gr = lookup_num(T.gp.get(), rhs, m);
+        const cplx g = cdiv(gl, mkc(p_cc, b_c)) - cdiv(gr, mkc(-p_cc, b_c));
+        fx += __real__ g;
+        Cpdf1DTerm c;
+        c.s = T.b[marg];
+        c.w = p_cc;
+        c.a = __imag__ gr / M_PI;
+        c.b = (__real__ gr * c.w - __imag__ gr * c.s) / M_PI;
+        E.cpdf1d_cache.push_back(c);
+    }
+    return fx * kTwoPiInv / __real__ E.fz;
+}
+
 extern "C" {
 
 void* orc_create(const double* A0, const double* p0, const double* b0, int steps, int d, int cmcc, int pncc,
@@ -1414,6 +1488,27 @@ void orc_dump_terms(void* h, int* shape, double* A, double* p, double* b, int* c
             c++;
         }
     }
+}
+
+// Marginal 1-D pdf grid: CauchyCPDFGridDispatcher1D::reset_grid and
+// evaluate_point_grid (cpdf_ndim.hpp:2055-2139).  Returns the point count, -2
+// if it exceeds max_points, -1 before the first step, -5 at the last step
+// (its g-tables are skipped).
+int orc_cpdf_1d_grid(void* h, int marg, const double* bar_nu, double low, double high, double res, int max_points,
+                     double* xs, double* ys)
+{
+    Estimator& E = *(Estimator*)h;
+    const int n = cpdf_grid_points(low, high, res);
+    if (n > max_points) return -2;
+    if (E.master_step < 1) return -1;
+    if (E.master_step >= E.num_steps) return -5;  // num_steps counts updates (p * steps)
+    for (int i = 0; i < n; i++) {
+        double x = low + i * res;
+        if (x > high) x = high;
+        xs[i] = x;
+        ys[i] = cpdf1d_eval(E, marg, x, bar_nu);
+    }
+    return n;
 }
 
 }  // extern "C"

@@ -64,9 +64,11 @@ static int harness_covariance_checker(C_COMPLEX_TYPE* cov, const int d, const in
 #define covariance_checker harness_covariance_checker
 
 #include "cauchy_estimator.hpp"
+#include "cpdf_ndim.hpp"
 
 struct RefHandle {
     CauchyEstimator* est;
+    PointWiseNDimCauchyCPDF* cpdf;  // made on first use, as pycauchy does
     int d;
     double raw_fz[2];
     double* raw_mean;
@@ -209,6 +211,29 @@ void ref_dump_terms(void* vh, int* shape, double* A, double* p, double* b, int* 
             t++;
         }
     }
+}
+
+// Marginal 1-D pdf on a grid through the reference's own
+// PointWiseNDimCauchyCPDF and CauchyCPDFGridDispatcher1D
+// (include/cpdf_ndim.hpp), as pycauchy_get_marginal_1D_pointwise_cpdf does
+// (scripts/swig/cauchy/pycauchy.hpp:890-931): the pdf object is made on the
+// first call (it draws bar_nu from rand()) and kept; a dispatcher per call.
+// Returns the point count, -2 if it exceeds max_points, -5 if the reference
+// refuses (the last step).  bar_nu[d] receives the pdf object's draws.
+int ref_cpdf_1d_grid(void* vh, int marg, double low, double high, double res, int max_points, double* xs,
+                     double* ys, double* bar_nu)
+{
+    RefHandle* h = (RefHandle*)vh;
+    if (!h->cpdf) h->cpdf = new PointWiseNDimCauchyCPDF(h->est);
+    for (int i = 0; i < h->d; i++) bar_nu[i] = h->cpdf->bar_nu[i];
+    CauchyCPDFGridDispatcher1D grid(h->cpdf, low, high, res);
+    if (grid.num_grid_points > max_points) return -2;
+    if (grid.evaluate_point_grid(marg, 1)) return -5;
+    for (int i = 0; i < grid.num_grid_points; i++) {
+        xs[i] = grid.points[i].x;
+        ys[i] = grid.points[i].y;
+    }
+    return grid.num_grid_points;
 }
 
 }  // extern "C"

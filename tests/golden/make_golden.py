@@ -6,8 +6,12 @@ and records, after every measurement update: the error bitmask, the term count,
 terms per shape, the reported and raw moments, G_SCALE_FACTOR, and (for small
 steps) every term's shape, A, p, b and sorted g-table.
 
+It also records the reference's marginal 1-D pdf grids (cpdf1d_*.npz) after
+a few updates of some of the same problems.
+
 Needs the reference sources (only present where the fixtures are made):
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py          # everything
+    python tests/golden/make_golden.py --cpdf   # the pdf fixtures only
 """
 import os
 import sys
@@ -62,11 +66,67 @@ def pack(name, prob, seed):
     return len(recs)
 
 
+def cpdf_cases():
+    """(name, problem, srand seed, updates before the pdf, srand seed of the pdf object)."""
+    return [
+        ("cpdf1d_three_state_lti", W.three_state_lti(seed=0, steps=8), 1, 5, 77),
+        ("cpdf1d_two_state_lti", W.two_state_lti(seed=0, steps=8), 2, 6, 78),
+        ("cpdf1d_four_state_lti", W.four_state_lti(seed=0, steps=5), 3, 4, 79),
+        ("cpdf1d_five_state_two_msmt", W.five_state_two_msmt(seed=0, steps=3), 4, 3, 80),
+        ("cpdf1d_batched_three_state_0", W.batched_three_state(6, seed=3, steps_lo=4, steps_hi=7)[0], 10, 3, 81),
+    ]
+
+
+def pack_cpdf(name, prob, seed, updates, cpdf_seed):
+    """The reference's marginal 1-D pdf grids (CauchyCPDFGridDispatcher1D)
+    after `updates` measurement updates: for every state, two grid calls (the
+    first exact at its first point and caching, the second from the cache)."""
+    import ctypes
+    ref = oracle.Reference(prob, seed=seed)
+    rp, bp = ref.constants()
+    n = 0
+    for k in range(prob["steps"]):
+        for s in range(prob["p"]):
+            if n < updates:
+                ref.step(k, s)
+                n += 1
+    mo = ref.moments()
+    ctypes.CDLL(None).srand(cpdf_seed)
+    arr = {
+        "d": prob["d"], "pncc": prob["pncc"], "cmcc": prob["cmcc"], "p": prob["p"], "steps": prob["steps"],
+        "Phi": prob["Phi"], "Gamma": prob["Gamma"], "beta": prob["beta"], "H": prob["H"],
+        "gamma": prob["gamma"], "A0": prob["A0"], "p0": prob["p0"], "b0": prob["b0"],
+        "msmts": prob["msmts"], "srand_seed": seed, "root_point": rp, "b_pert": bp, "updates": updates,
+    }
+    for marg in range(prob["d"]):
+        mu = float(mo["raw_mean"].real[marg])
+        sd = float(np.sqrt(abs(mo["raw_cov"].real[marg, marg])))
+        if not np.isfinite(mu):
+            mu = 0.0
+        if not (np.isfinite(sd) and sd > 1e-6):
+            sd = 1.0
+        lo, hi, res = mu - 4 * sd, mu + 4 * sd, 8 * sd / 50
+        for call in range(2):
+            x, y, nu = ref.cpdf_1d_grid(marg, lo, hi, res)
+            pre = "m%d_c%d_" % (marg, call)
+            arr[pre + "grid"] = np.array([lo, hi, res])
+            arr[pre + "x"] = x
+            arr[pre + "y"] = y
+        arr["bar_nu"] = nu
+    ref.close()
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **arr)
+
+
 def main():
     oracle.build()
-    for name, prob, seed in cases():
-        n = pack(name, prob, seed)
-        print("wrote %s.npz (%d updates)" % (name, n))
+    only_cpdf = "--cpdf" in sys.argv
+    if not only_cpdf:
+        for name, prob, seed in cases():
+            n = pack(name, prob, seed)
+            print("wrote %s.npz (%d updates)" % (name, n))
+    for name, prob, seed, updates, cseed in cpdf_cases():
+        pack_cpdf(name, prob, seed, updates, cseed)
+        print("wrote %s.npz" % name)
 
 
 if __name__ == "__main__":

@@ -13,7 +13,28 @@ REL_TOL = 1e-9
 
 
 def names():
-    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    """The step-record fixtures (the marginal pdf ones are cpdf_names())."""
+    return sorted(n for n in (os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+                  if not n.startswith("cpdf1d_"))
+
+
+def cpdf_names():
+    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "cpdf1d_*.npz")))
+
+
+def load_cpdf(name):
+    """(problem, (root_point, b_pert), updates, bar_nu, [(marg, call, (lo, hi, res), x, y)])"""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    prob = {k: z[k] for k in ("Phi", "Gamma", "beta", "H", "gamma", "A0", "p0", "b0", "msmts")}
+    for k in ("d", "pncc", "cmcc", "p", "steps"):
+        prob[k] = int(z[k])
+    prob["B"] = None
+    grids = []
+    for marg in range(prob["d"]):
+        for call in range(2):
+            pre = "m%d_c%d_" % (marg, call)
+            grids.append((marg, call, tuple(float(v) for v in z[pre + "grid"]), z[pre + "x"], z[pre + "y"]))
+    return prob, (z["root_point"], z["b_pert"]), int(z["updates"]), z["bar_nu"], grids
 
 
 def load(name):
