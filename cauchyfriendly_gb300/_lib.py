@@ -26,6 +26,9 @@ SIGNATURES = {
     "mce_batch_create": (_vp, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _ip, _dp, _dp,
                                _dp, _dp, _dp, ctypes.c_int, _ip]),
     "mce_batch_step": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int, _ip]),
+    "mce_shift_cf_by_bias": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
+    "mce_deterministic_time_prop": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp]),
+    "mce_finalize_extended_moments": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
     "mce_cpdf_1d_grid": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_double, ctypes.c_int, _dp, _dp]),
     "mce_draw_bar_nu": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_int, _dp]),

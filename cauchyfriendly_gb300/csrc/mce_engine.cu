@@ -180,6 +180,10 @@ public:
                            int* keys, double* g) = 0;
     virtual long long total_cells(int est) = 0;
     virtual int reset() = 0;
+    // every current term of estimator e: b += v (sub = 0) or b -= v (sub = 1)
+    virtual int shift_terms_b(int e, const double* v, int sub) = 0;
+    // every current term of estimator e: time_prop with Phi and B u (Bu may be null)
+    virtual int time_prop_terms(int e, const double* Phi, const double* Bu) = 0;
     virtual int cpdf_1d_grid(int est, int marg, const double* bar_nu, double low, double high, double res,
                              int max_points, double* xs, double* ys) = 0;
     // waits for the work the engine queued (after a step that stopped early)
@@ -1111,6 +1115,35 @@ public:
     void k_gather_bounds(const long long* scan, int E_);
     void k_status_init(TermRecs R, long long nR);
 
+    // ---- extended-mode helpers (cauchy_estimator.hpp:1312-1394)
+    DevBuf<double> ext_buf;
+
+    int shift_terms_b(int e, const double* v, int sub) override
+    {
+        if (e < 0 || e >= E || !v) return MCE_ERR_ARG;
+        int s;
+        if ((s = ext_buf.ensure(D))) return s;
+        MCE_CUDA(cudaMemcpyAsync(ext_buf.ptr, v, sizeof(double) * D, cudaMemcpyHostToDevice, lc.stream));
+        const long long a = hpstart.empty() ? 0 : hpstart[e], n = hpstart.empty() ? 0 : hpstart[e + 1] - a;
+        Kernels<D>::shift_b(Pb[cur].view(), a, n, ext_buf.ptr, sub, lc);
+        MCE_CUDA(cudaStreamSynchronize(lc.stream));
+        return MCE_OK;
+    }
+
+    int time_prop_terms(int e, const double* Phi, const double* Bu) override
+    {
+        if (e < 0 || e >= E || !Phi) return MCE_ERR_ARG;
+        int s;
+        if ((s = ext_buf.ensure(D * D + D))) return s;
+        MCE_CUDA(cudaMemcpyAsync(ext_buf.ptr, Phi, sizeof(double) * D * D, cudaMemcpyHostToDevice, lc.stream));
+        if (Bu)
+            MCE_CUDA(cudaMemcpyAsync(ext_buf.ptr + D * D, Bu, sizeof(double) * D, cudaMemcpyHostToDevice, lc.stream));
+        const long long a = hpstart.empty() ? 0 : hpstart[e], n = hpstart.empty() ? 0 : hpstart[e + 1] - a;
+        Kernels<D>::det_tp(Pb[cur].view(), a, n, ext_buf.ptr, Bu ? ext_buf.ptr + D * D : nullptr, MC, lc);
+        MCE_CUDA(cudaStreamSynchronize(lc.stream));
+        return MCE_OK;
+    }
+
     // ---- marginal 1-D pdf: CauchyCPDFGridDispatcher1D (cpdf_ndim.hpp:2017-2139)
     // over PointWiseNDimCauchyCPDF::evaluate_1D_marginal_cpdf (:1233-1352),
     // with the reference's per-estimator cache of per-term constants, kept on
@@ -1626,6 +1659,54 @@ int mce_cpdf_1d_grid(mce_handle* h, int e, int marg_idx, const double* bar_nu, d
 {
     if (bad(h, e)) return MCE_ERR_ARG;
     return h->eng->cpdf_1d_grid(e, marg_idx, bar_nu, grid_low, grid_high, grid_res, max_points, x, y);
+}
+// shift_cf_by_bias (cauchy_estimator.hpp:1312-1327): no shift after the final MU
+int mce_shift_cf_by_bias(mce_handle* h, int e, const double* bias)
+{
+    if (bad(h, e) || !bias) return MCE_ERR_ARG;
+    EngineBase* g = h->eng;
+    if (g->master_step >= g->est[e].num_updates) return MCE_OK;
+    return g->shift_terms_b(e, bias, 0);
+}
+// deterministic_time_prop (cauchy_estimator.hpp:1329-1352): B u only when both are given
+int mce_deterministic_time_prop(mce_handle* h, int e, const double* Phi, const double* B, const double* u)
+{
+    if (bad(h, e) || !Phi) return MCE_ERR_ARG;
+    if ((B == nullptr) != (u == nullptr)) {
+        set_error("deterministic_time_prop: give both B and u or neither");
+        return MCE_ERR_ARG;
+    }
+    EngineBase* g = h->eng;
+    const int d = g->d, cm = g->cmcc;
+    std::vector<double> Bu;
+    if (B && cm > 0) {
+        // matvecmul(B, u) in the reference's order (cauchy_term.hpp:449-453)
+        Bu.assign(d, 0.0);
+        for (int i = 0; i < d; i++) {
+            double s = 0.0;
+            for (int j = 0; j < cm; j++) s += B[i * cm + j] * u[j];
+            Bu[i] = s;
+        }
+    }
+    return g->time_prop_terms(e, Phi, Bu.empty() ? nullptr : Bu.data());
+}
+// finalize_extended_moments (cauchy_estimator.hpp:1354-1388): b -= Re(mean) for
+// every term (not after the final MU), then mean += x_bar, x_bar = Re(mean)
+int mce_finalize_extended_moments(mce_handle* h, int e, double* x_bar)
+{
+    if (bad(h, e) || !x_bar) return MCE_ERR_ARG;
+    EngineBase* g = h->eng;
+    const int d = g->d;
+    EstHost& eh = g->est[e];
+    if (g->master_step < g->est[e].num_updates) {
+        std::vector<double> dx(d);
+        for (int i = 0; i < d; i++) dx[i] = eh.mean[2 * i];
+        const int s = g->shift_terms_b(e, dx.data(), 1);
+        if (s != MCE_OK) return s;
+    }
+    for (int i = 0; i < d; i++) eh.mean[2 * i] += x_bar[i];
+    for (int i = 0; i < d; i++) x_bar[i] = eh.mean[2 * i];
+    return MCE_OK;
 }
 int mce_draw_bar_nu(long long seed, int d, double* bar_nu)
 {

@@ -2202,6 +2202,64 @@ void Kernels<D>::cpdf1d_terms(ParentList P, long long a, long long n, int marg, 
     k_cpdf1d_terms<D><<<grid_for(n, 128, c.num_sms, 16), 128, 0, c.stream>>>(P, a, n, marg, bar_nu, T, MC, tt);
 }
 
+// Extended-mode helpers (cauchy_estimator.hpp:1312-1394) over the terms of
+// one estimator: b +/- v (shift_cf_by_bias, finalize_extended_moments) and
+// time_prop (cauchy_term.hpp:435-456: A <- A Phi^T, b <- Phi b, b += B u).
+template <int D>
+__global__ void k_shift_b(ParentList P, long long a, long long n, const double* v, int sub)
+{
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
+        double* b = P.b + (a + j) * D;
+        for (int k = 0; k < D; k++) b[k] = sub ? b[k] - v[k] : b[k] + v[k];
+    }
+}
+
+template <int D>
+__global__ void k_det_tp(ParentList P, long long a, long long n, const double* Phi, const double* Bu, int MC)
+{
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
+        const long long i = a + j;
+        const int m = P.m[i];
+        double* A = P.A + i * MC * D;
+        for (int r = 0; r < m; r++) {
+            double w[D];
+            for (int k = 0; k < D; k++) w[k] = A[r * D + k];
+            for (int c = 0; c < D; c++) {
+                double s = 0.0;
+                for (int k = 0; k < D; k++) s += w[k] * Phi[c * D + k];
+                A[r * D + c] = s;
+            }
+        }
+        double* b = P.b + i * D;
+        double wb[D];
+        for (int k = 0; k < D; k++) wb[k] = b[k];
+        for (int r = 0; r < D; r++) {
+            double s = 0.0;
+            for (int k = 0; k < D; k++) s += Phi[r * D + k] * wb[k];
+            b[r] = s;
+        }
+        if (Bu)
+            for (int r = 0; r < D; r++) b[r] += 1.0 * Bu[r];
+    }
+}
+
+template <int D>
+void Kernels<D>::shift_b(ParentList P, long long a, long long n, const double* v, int sub, const LaunchCfg& c)
+{
+    if (n == 0) return;
+    ++g_launches;
+    k_shift_b<D><<<grid_for(n, 128, c.num_sms, 16), 128, 0, c.stream>>>(P, a, n, v, sub);
+}
+
+template <int D>
+void Kernels<D>::det_tp(ParentList P, long long a, long long n, const double* Phi, const double* Bu, int MC,
+                        const LaunchCfg& c)
+{
+    if (n == 0) return;
+    ++g_launches;
+    k_det_tp<D><<<grid_for(n, 128, c.num_sms, 16), 128, 0, c.stream>>>(P, a, n, Phi, Bu, MC);
+}
+
 #if MCE_COMMON_UNIT
 // One thread per point, the terms summed in order.  Points below `exact`
 // take the complex formula (fx * 1/(2 pi) / fz), the others the cached one

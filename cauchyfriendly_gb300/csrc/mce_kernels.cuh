@@ -68,6 +68,9 @@ struct Kernels {
                             const long long* goff, const int* members, ParentList P, Tables Told, const int* Bkeys,
                             const long long* toff, Tables Tnew, const GFlat& f, int* gitems, int* gcells, int MC,
                             int* err, const LaunchCfg& c);
+    static void shift_b(ParentList P, long long a, long long n, const double* v, int sub, const LaunchCfg& c);
+    static void det_tp(ParentList P, long long a, long long n, const double* Phi, const double* Bu, int MC,
+                       const LaunchCfg& c);
     static void cpdf1d_terms(ParentList P, long long a, long long n, int marg, const double* bar_nu, Tables T,
                              int MC, double* tt, const LaunchCfg& c);
     static void gtable_combine(TermRecs R, const int* roots_list, long long nroots, const long long* coff,

@@ -169,6 +169,24 @@ class BatchedCauchyEstimator:
     def set_win_num(self, w):
         _lib.check(self._lib.mce_set_window_number(self._h, int(w)), "mce_set_window_number")
 
+    # -- extended (nonlinear) mode helpers, cauchy_estimator.hpp:1312-1394 ---
+    def shift_cf_by_bias(self, bias, e=0):
+        b = _f64(bias).reshape(self.d)
+        _lib.check(self._lib.mce_shift_cf_by_bias(self._h, int(e), _p(b)), "mce_shift_cf_by_bias")
+
+    def deterministic_time_prop(self, Phi, B=None, u=None, e=0):
+        Phi = _f64(Phi).reshape(self.d, self.d)
+        B = None if B is None else _f64(B)
+        u = None if u is None else _f64(u)
+        _lib.check(self._lib.mce_deterministic_time_prop(self._h, int(e), _p(Phi), _p(B), _p(u)),
+                   "mce_deterministic_time_prop")
+
+    def finalize_extended_moments(self, x_bar, e=0):
+        """Shifts the terms by -Re(mean), sets mean += x_bar; returns the new x_bar = Re(mean)."""
+        x = _f64(x_bar).reshape(self.d).copy()
+        _lib.check(self._lib.mce_finalize_extended_moments(self._h, int(e), _p(x)), "mce_finalize_extended_moments")
+        return x
+
     def cpdf_1d_grid(self, e, marg_idx, gridx_low, gridx_high, gridx_resolution, bar_nu):
         """Marginal 1-D conditional pdf of estimator e on the grid
         gridx_low..gridx_high step gridx_resolution

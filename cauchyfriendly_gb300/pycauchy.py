@@ -33,13 +33,15 @@ class C_CauchyDynamicsUpdateContainer(ct.Structure):
 
 
 _CALLBACK = ct.CFUNCTYPE(None, ct.POINTER(C_CauchyDynamicsUpdateContainer))
+_MSMT_CALLBACK = ct.CFUNCTYPE(None, ct.POINTER(C_CauchyDynamicsUpdateContainer), ct.POINTER(ct.c_double))
 
 
 class _Handle:
     """What pycauchy_initialize_* returns: the estimator plus the dynamics
     container (pycauchy.hpp:240-280 PyCauchyDataHandler)."""
 
-    def __init__(self, num_steps, A0, p0, b0, Phi, Gamma, B, beta, H, gamma, dt, init_step, debug_print):
+    def __init__(self, num_steps, A0, p0, b0, Phi, Gamma, B, beta, H, gamma, dt, init_step, debug_print,
+                 est_cmcc=None):
         n = int(np.asarray(b0).size)
         self.n = n
         self.pncc = int(np.asarray(beta).size)
@@ -67,7 +69,8 @@ class _Handle:
         self.duc.other_stuff = None
         self.callback = None
         self.est = CauchyEstimator(np.asarray(A0, dtype=np.float64).reshape(n, n), p0, b0, int(num_steps), n,
-                                   self.cmcc, self.pncc, self.p, bool(debug_print))
+                                   self.cmcc if est_cmcc is None else int(est_cmcc), self.pncc, self.p,
+                                   bool(debug_print))
 
 
 def pycauchy_initialize_lti(num_steps, A0, p0, b0, Phi, Gamma, B, beta, H, gamma, dt, init_step, debug_print):
@@ -81,6 +84,71 @@ def pycauchy_initialize_ltv(num_steps, A0, p0, b0, Phi, Gamma, B, beta, H, gamma
     h = _Handle(num_steps, A0, p0, b0, Phi, Gamma, B, beta, H, gamma, dt, init_step, debug_print)
     h.callback = _CALLBACK(int(f_dyn_update_callback))
     return h
+
+
+def pycauchy_initialize_nonlin(num_steps, x0, A0, p0, b0, beta, gamma, f_dyn_update_callback, f_nonlinear_msmt_model,
+                               f_extended_msmt_update_callback, cmcc, dt, init_step, debug_print):
+    """pycauchy.hpp:365-396: an estimator (no controls) whose linearised
+    dynamics and measurement models come from three callbacks, raw C function
+    pointers (ints) taking the dynamics container."""
+    n = int(np.asarray(b0).size)
+    pncc = int(np.asarray(beta).size)
+    p = int(np.asarray(gamma).size)
+    h = _Handle(num_steps, A0, p0, b0, None, np.zeros(n * pncc), np.zeros(n * int(cmcc)), beta, np.zeros(p * n),
+                gamma, dt, init_step, debug_print, est_cmcc=0)
+    h.x[:] = np.asarray(x0, dtype=np.float64).reshape(n)
+    h.f_dyn = _CALLBACK(int(f_dyn_update_callback))
+    h.f_msmt = _MSMT_CALLBACK(int(f_nonlinear_msmt_model))
+    h.f_ext = _CALLBACK(int(f_extended_msmt_update_callback))
+    return h
+
+
+def pycauchy_single_step_nonlin(h, msmts, controls, with_propagate):
+    """pycauchy.hpp:545-652: propagate x_bar through the dynamics callback
+    (unless with_propagate is false), then for each of the last len(msmts)
+    measurements: the nonlinear measurement model gives z_bar, the extended
+    update callback sets H, the estimator takes z - z_bar, and
+    finalize_extended_moments moves x_bar to the new estimate.  Returns
+    (Phi, Gamma, B, H, beta, gamma, fz, xhat, Phat, xbar, zbar, cerr_fz,
+    cerr_xhat, cerr_Phat, err_code)."""
+    msmts = np.atleast_1d(np.asarray(msmts, dtype=np.float64)).reshape(-1)
+    controls = np.atleast_1d(np.asarray(controls, dtype=np.float64)).reshape(-1)
+    n, p, pncc, cmcc, k = h.n, h.p, h.pncc, h.cmcc, msmts.size
+    assert p >= k
+    if cmcc > 0 and controls.size:
+        h.u[:cmcc] = controls[:cmcc]
+    out_Phi, out_Gamma, out_B = np.zeros(n * n), np.zeros(n * pncc), np.zeros(n * cmcc)
+    out_beta, out_H, out_gamma = np.zeros(pncc), np.zeros(k * n), np.zeros(k)
+    if with_propagate:
+        h.duc.is_xbar_set_for_ece = False
+        h.f_dyn(ct.pointer(h.duc))
+        assert h.duc.is_xbar_set_for_ece
+        out_Phi[:], out_B[:], out_Gamma[:], out_beta[:] = h.Phi, h.B, h.Gamma, h.beta
+    fz, xhat, Phat = np.zeros(k), np.zeros(k * n), np.zeros(k * n * n)
+    xbar, zbar_out = np.zeros(k * n), np.zeros(k)
+    cfz, cx, cP, err = np.zeros(k), np.zeros(k), np.zeros(k), np.zeros(k, dtype=np.int32)
+    start = p - k
+    zbar = np.zeros(p)
+    for i in range(k):
+        idx = start + i
+        h.f_msmt(ct.pointer(h.duc), zbar.ctypes.data_as(ct.POINTER(ct.c_double)))
+        h.f_ext(ct.pointer(h.duc))
+        xbar[i * n:(i + 1) * n] = h.x
+        zbar_out[i] = zbar[idx]
+        out_H[i * n:(i + 1) * n] = h.H[idx * n:(idx + 1) * n]
+        out_gamma[i] = h.gamma[idx]
+        err[i] = h.est.step(msmts[i] - zbar[idx], h.Phi.reshape(n, n), h.Gamma.reshape(n, pncc) if pncc else None,
+                            h.beta if pncc else None, h.H[idx * n:(idx + 1) * n], h.gamma[idx])
+        h.x[:] = h.est.finalize_extended_moments(h.x)
+        mo = h.est.moments()
+        fz[i], cfz[i] = mo["fz"].real, mo["fz"].imag
+        xhat[i * n:(i + 1) * n] = mo["mean"].real
+        Phat[i * n * n:(i + 1) * n * n] = mo["cov"].real.reshape(-1)
+        cx[i] = np.max(np.abs(mo["mean"].imag))
+        cP[i] = np.max(np.abs(mo["cov"].imag))
+        err[i] = h.est.errors()
+    h.duc.step += 1
+    return (out_Phi, out_Gamma, out_B, out_H, out_beta, out_gamma, fz, xhat, Phat, xbar, zbar_out, cfz, cx, cP, err)
 
 
 def pycauchy_single_step_ltiv(h, msmts, controls):
@@ -166,6 +234,12 @@ def pycauchy_single_step_reset(h, A0, p0, b0, xbar):
     if xbar.size:
         h.x[:] = xbar
     h.est.reset()
+
+
+def pycauchy_single_step_deterministic_transform(h, Trans, bias):
+    """pycauchy.hpp:654-663: deterministic_time_prop(Trans) then shift_cf_by_bias(bias)."""
+    h.est.deterministic_time_prop(np.asarray(Trans, dtype=np.float64).reshape(h.n, h.n))
+    h.est.shift_cf_by_bias(np.asarray(bias, dtype=np.float64).reshape(h.n))
 
 
 def pycauchy_get_marginal_1D_pointwise_cpdf(h, marg_idx1, gridx_low, gridx_high, gridx_resolution, log_dir=None):

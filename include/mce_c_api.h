@@ -116,6 +116,19 @@ int mce_get_errors(mce_handle* h, int est);
 long long mce_num_terms(mce_handle* h, int est);
 /* terms_per_shape (n entries, shape index = hyperplane count). */
 int mce_terms_per_shape(mce_handle* h, int est, int* out, int n);
+/* Extended (nonlinear) mode helpers of CauchyEstimator
+ * (include/cauchy_estimator.hpp:1312-1394), on one estimator's current terms:
+ *  - mce_shift_cf_by_bias: every term's b += bias[d] (nothing after the
+ *    final update, whose terms are not kept);
+ *  - mce_deterministic_time_prop: every term's time_prop with Phi[d*d], and
+ *    B[d*cmcc] u[cmcc] when both are given (A <- A Phi^T, b <- Phi b + B u);
+ *  - mce_finalize_extended_moments: every term's b -= Re(mean) (not after
+ *    the final update), then mean += x_bar and x_bar = Re(mean); x_bar[d] is
+ *    read and written. */
+int mce_shift_cf_by_bias(mce_handle* h, int est, const double* bias);
+int mce_deterministic_time_prop(mce_handle* h, int est, const double* Phi, const double* B, const double* u);
+int mce_finalize_extended_moments(mce_handle* h, int est, double* x_bar);
+
 /* Marginal 1-D conditional pdf of estimator `est` on the grid
  * grid_low, grid_low + grid_res, ..., grid_high (the last point clamped), as
  * CauchyCPDFGridDispatcher1D (include/cpdf_ndim.hpp:2017-2139) evaluates

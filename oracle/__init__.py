@@ -274,6 +274,25 @@ class Oracle(_EstimatorBase):
     def errors(self):
         return int(self._l.lib.orc_errors(self.h))
 
+    def shift_cf_by_bias(self, bias):
+        b = _arr(bias)
+        self._l.lib.orc_shift_cf_by_bias.argtypes = [ctypes.c_void_p, _dp]
+        self._l.lib.orc_shift_cf_by_bias(self.h, _ptr(b))
+
+    def deterministic_time_prop(self, Phi, B=None, u=None):
+        f = self._l.lib.orc_deterministic_time_prop
+        f.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+        Phi = _arr(Phi)
+        B = None if B is None else _arr(B)
+        u = None if u is None else _arr(u)
+        f(self.h, _ptr(Phi), _ptr(B), _ptr(u))
+
+    def finalize_extended_moments(self, x_bar):
+        x = _arr(x_bar).copy()
+        self._l.lib.orc_finalize_extended_moments.argtypes = [ctypes.c_void_p, _dp]
+        self._l.lib.orc_finalize_extended_moments(self.h, _ptr(x))
+        return x
+
     def cpdf_1d_grid(self, marg, bar_nu, low, high, res, max_points=100000):
         """Marginal 1-D pdf on the grid low..high step res (the reference's
         CauchyCPDFGridDispatcher1D); returns (x, y) or raises with the status."""
@@ -350,6 +369,25 @@ class Reference(_EstimatorBase):
 
     def last_step_seconds(self):
         return float(self._l.lib.ref_last_step_seconds(self.h))
+
+    def shift_cf_by_bias(self, bias):
+        b = _arr(bias)
+        self._l.lib.ref_shift_cf_by_bias.argtypes = [ctypes.c_void_p, _dp]
+        self._l.lib.ref_shift_cf_by_bias(self.h, _ptr(b))
+
+    def deterministic_time_prop(self, Phi, B=None, u=None):
+        f = self._l.lib.ref_deterministic_time_prop
+        f.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+        Phi = _arr(Phi)
+        B = None if B is None else _arr(B)
+        u = None if u is None else _arr(u)
+        f(self.h, _ptr(Phi), _ptr(B), _ptr(u))
+
+    def finalize_extended_moments(self, x_bar):
+        x = _arr(x_bar).copy()
+        self._l.lib.ref_finalize_extended_moments.argtypes = [ctypes.c_void_p, _dp]
+        self._l.lib.ref_finalize_extended_moments(self.h, _ptr(x))
+        return x
 
     def cpdf_1d_grid(self, marg, low, high, res, max_points=100000):
         """The reference's own marginal 1-D pdf grid; returns (x, y, bar_nu)."""

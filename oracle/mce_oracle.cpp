@@ -1490,6 +1490,41 @@ void orc_dump_terms(void* h, int* shape, double* A, double* p, double* b, int* c
     }
 }
 
+// Extended (nonlinear) mode helpers, cauchy_estimator.hpp:1312-1394.
+// shift_cf_by_bias: every term's b += bias, unless the last update was the
+// final MU (whose terms are not kept).
+void orc_shift_cf_by_bias(void* h, const double* bias)
+{
+    Estimator& E = *(Estimator*)h;
+    if (E.skip_post_mu) return;
+    for (Term& T : E.terms)
+        for (int j = 0; j < E.d; j++) T.b[j] += bias[j];
+}
+
+// deterministic_time_prop: time_prop of every term with (Phi) or (Phi, B, u).
+void orc_deterministic_time_prop(void* h, const double* Phi, const double* B, const double* u)
+{
+    Estimator& E = *(Estimator*)h;
+    const int cm = (B && u) ? E.cmcc : 0;
+    for (Term& T : E.terms) time_prop(T, E.d, Phi, B, u, cm);
+}
+
+// finalize_extended_moments: every term's b -= Re(mean) (not after the final
+// MU), then mean += x_bar and x_bar = Re(mean).
+void orc_finalize_extended_moments(void* h, double* x_bar)
+{
+    Estimator& E = *(Estimator*)h;
+    const int d = E.d;
+    if (!E.skip_post_mu) {
+        std::vector<double> dx(d);
+        for (int i = 0; i < d; i++) dx[i] = __real__ E.mean[i];
+        for (Term& T : E.terms)
+            for (int j = 0; j < d; j++) T.b[j] -= dx[j];
+    }
+    for (int i = 0; i < d; i++) __real__ E.mean[i] += x_bar[i];
+    for (int i = 0; i < d; i++) x_bar[i] = __real__ E.mean[i];
+}
+
 // Marginal 1-D pdf grid: CauchyCPDFGridDispatcher1D::reset_grid and
 // evaluate_point_grid (cpdf_ndim.hpp:2055-2139).  Returns the point count, -2
 // if it exceeds max_points, -1 before the first step, -5 at the last step

@@ -213,6 +213,14 @@ void ref_dump_terms(void* vh, int* shape, double* A, double* p, double* b, int* 
     }
 }
 
+// The reference's extended-mode helpers (include/cauchy_estimator.hpp:1312-1394).
+void ref_shift_cf_by_bias(void* vh, const double* bias) { ((RefHandle*)vh)->est->shift_cf_by_bias((double*)bias); }
+void ref_deterministic_time_prop(void* vh, const double* Phi, const double* B, const double* u)
+{
+    ((RefHandle*)vh)->est->deterministic_time_prop((double*)Phi, (double*)B, (double*)u);
+}
+void ref_finalize_extended_moments(void* vh, double* x_bar) { ((RefHandle*)vh)->est->finalize_extended_moments(x_bar); }
+
 // Marginal 1-D pdf on a grid through the reference's own
 // PointWiseNDimCauchyCPDF and CauchyCPDFGridDispatcher1D
 // (include/cpdf_ndim.hpp), as pycauchy_get_marginal_1D_pointwise_cpdf does

@@ -7,11 +7,13 @@ terms per shape, the reported and raw moments, G_SCALE_FACTOR, and (for small
 steps) every term's shape, A, p, b and sorted g-table.
 
 It also records the reference's marginal 1-D pdf grids (cpdf1d_*.npz) after
-a few updates of some of the same problems.
+a few updates of some of the same problems, and the moments through a fixed
+sequence of updates and extended-mode calls (ext_*.npz).
 
 Needs the reference sources (only present where the fixtures are made):
     python tests/golden/make_golden.py          # everything
     python tests/golden/make_golden.py --cpdf   # the pdf fixtures only
+    python tests/golden/make_golden.py --ext    # the extended-mode fixtures only
 """
 import os
 import sys
@@ -117,16 +119,50 @@ def pack_cpdf(name, prob, seed, updates, cpdf_seed):
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **arr)
 
 
+def ext_cases():
+    return [
+        ("ext_three_state_lti", W.three_state_lti(seed=0, steps=6), 1),
+        ("ext_two_state_lti", W.two_state_lti(seed=0, steps=6), 2),
+        ("ext_five_state_two_msmt", W.five_state_two_msmt(seed=0, steps=3), 4),
+    ]
+
+
+def pack_ext(name, prob, seed):
+    """The reference through a fixed sequence of updates and extended-mode
+    calls (finalize_extended_moments, deterministic_time_prop,
+    shift_cf_by_bias; the sequence is tests.golden_cases.extended_ops)."""
+    from tests import golden_cases as G
+    ref = oracle.Reference(prob, seed=seed)
+    rp, bp = ref.constants()
+    recs = G.run_extended(ref, prob, G.extended_ops(prob))
+    ref.close()
+    arr = {
+        "d": prob["d"], "pncc": prob["pncc"], "cmcc": prob["cmcc"], "p": prob["p"], "steps": prob["steps"],
+        "Phi": prob["Phi"], "Gamma": prob["Gamma"], "beta": prob["beta"], "H": prob["H"],
+        "gamma": prob["gamma"], "A0": prob["A0"], "p0": prob["p0"], "b0": prob["b0"],
+        "msmts": prob["msmts"], "srand_seed": seed, "root_point": rp, "b_pert": bp, "n_ops": len(recs),
+    }
+    for i, r in enumerate(recs):
+        for k, v in r.items():
+            arr["r%d_%s" % (i, k)] = np.asarray(v)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **arr)
+
+
 def main():
     oracle.build()
-    only_cpdf = "--cpdf" in sys.argv
-    if not only_cpdf:
+    only = [a[2:] for a in sys.argv[1:] if a.startswith("--")]
+    if not only:
         for name, prob, seed in cases():
             n = pack(name, prob, seed)
             print("wrote %s.npz (%d updates)" % (name, n))
-    for name, prob, seed, updates, cseed in cpdf_cases():
-        pack_cpdf(name, prob, seed, updates, cseed)
-        print("wrote %s.npz" % name)
+    if not only or "cpdf" in only:
+        for name, prob, seed, updates, cseed in cpdf_cases():
+            pack_cpdf(name, prob, seed, updates, cseed)
+            print("wrote %s.npz" % name)
+    if not only or "ext" in only:
+        for name, prob, seed in ext_cases():
+            pack_ext(name, prob, seed)
+            print("wrote %s.npz" % name)
 
 
 if __name__ == "__main__":

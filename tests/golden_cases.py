@@ -15,7 +15,7 @@ REL_TOL = 1e-9
 def names():
     """The step-record fixtures (the marginal pdf ones are cpdf_names())."""
     return sorted(n for n in (os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
-                  if not n.startswith("cpdf1d_"))
+                  if not n.startswith(("cpdf1d_", "ext_")))
 
 
 def cpdf_names():
@@ -87,3 +87,85 @@ def compare_records(got, want, rel_tol=REL_TOL, check_terms=True, first_raw_from
             for k in ("A", "p", "b"):
                 assert relerr(gt[k], wt[k]) <= 1e-12, (ctx, k, relerr(gt[k], wt[k]))
             assert relerr(gt["g"], wt["g"]) <= rel_tol, (ctx, "g values", relerr(gt["g"], wt["g"]))
+
+
+def extended_ops(prob):
+    """A fixed sequence of updates and extended-mode calls for a problem:
+    ("step", k, s), ("finalize", x_bar), ("dtp", Phi), ("bias", b)."""
+    d = prob["d"]
+    rng = np.random.Generator(np.random.PCG64(1234 + d))
+    ups = [(k, s) for k in range(prob["steps"]) for s in range(prob["p"])]
+    ops = []
+    for i, (k, s) in enumerate(ups):
+        ops.append(("step", k, s))
+        if i == len(ups) - 1:
+            ops.append(("finalize", 0.1 * rng.standard_normal(d)))  # after the final MU: mean only
+            break
+        if i % 3 == 0:
+            ops.append(("finalize", 0.1 * rng.standard_normal(d)))
+        elif i % 3 == 1:
+            M = np.eye(d) + 0.05 * rng.standard_normal((d, d))
+            ops.append(("dtp", M))
+            ops.append(("bias", 0.05 * rng.standard_normal(d)))
+    return ops
+
+
+def run_extended(est, prob, ops):
+    """Applies ops to an estimator with step(k, s), finalize_extended_moments,
+    deterministic_time_prop, shift_cf_by_bias and the read-outs; one record
+    per op (moments, Nt, error bits, and x_bar after a finalize)."""
+    recs = []
+    for op in ops:
+        r = {}
+        if op[0] == "step":
+            r["err"] = int(est.step(op[1], op[2]))
+        elif op[0] == "finalize":
+            r["xbar"] = np.asarray(est.finalize_extended_moments(op[1]))
+        elif op[0] == "dtp":
+            est.deterministic_time_prop(op[1])
+        elif op[0] == "bias":
+            est.shift_cf_by_bias(op[1])
+        r.update(est.moments())
+        r["Nt"] = est.num_terms()
+        recs.append(r)
+    return recs
+
+
+def compare_extended(got, want, rel_tol=REL_TOL):
+    """Records of run_extended: exact term counts and error bits, moments and
+    x_bar within rel_tol.  The raw (pre-check) moments exist from the second
+    update on: the first update never reaches the numeric check."""
+    assert len(got) == len(want)
+    steps = 0
+    for i, (g, w) in enumerate(zip(got, want)):
+        steps += "err" in w
+        assert g["Nt"] == w["Nt"], (i, g["Nt"], w["Nt"])
+        if "err" in w:
+            assert g["err"] == w["err"], (i, "err")
+        if "xbar" in w:
+            assert relerr(g["xbar"], w["xbar"]) <= rel_tol, (i, "xbar")
+        keys = ("fz", "mean", "cov") + (("raw_fz", "raw_mean", "raw_cov") if steps >= 2 else ())
+        for k in keys:
+            assert relerr(g[k], w[k]) <= rel_tol, (i, k, relerr(g[k], w[k]))
+
+
+def ext_names():
+    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "ext_*.npz")))
+
+
+def load_ext(name):
+    """(problem, (root_point, b_pert), records) of an extended-mode fixture."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    prob = {k: z[k] for k in ("Phi", "Gamma", "beta", "H", "gamma", "A0", "p0", "b0", "msmts")}
+    for k in ("d", "pncc", "cmcc", "p", "steps"):
+        prob[k] = int(z[k])
+    prob["B"] = None
+    recs = []
+    for i in range(int(z["n_ops"])):
+        pre = "r%d_" % i
+        r = {k[len(pre):]: z[k] for k in z.files if k.startswith(pre)}
+        r["Nt"] = int(r["Nt"])
+        if "err" in r:
+            r["err"] = int(r["err"])
+        recs.append(r)
+    return prob, (z["root_point"], z["b_pert"]), recs
