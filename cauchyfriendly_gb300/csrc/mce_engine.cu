@@ -343,8 +343,8 @@ public:
         }
     } Rb;
     DevBuf<cd> fam_mom, est_raw, scratch, g_vals;
-    DevBuf<int> g_nr, g_items, g_cells, g_rflag, g_minfo, g_mflag;
-    DevBuf<long long> g_ioff, g_coff;
+    DevBuf<int> g_nr, g_items, g_cells, g_rflag, g_minfo, g_mflag, nvert, vsv;
+    DevBuf<long long> g_ioff, g_coff, voff;
     DevBuf<double> g_rps2, g_mps2;
     DevBuf<double> gscale, mom_tot;
     DevBuf<long long> goff, toff, rscan, bucket_off, rbase, scan_tmp, kall_est;
@@ -838,33 +838,38 @@ public:
         Tables Told{Tb[cur].keys.ptr, Tb[cur].vals.ptr};
         int* err = counters.ptr;
         if ((s = Bcap.ensure(nP + 1))) return s;
+        if ((s = nvert.ensure(nP + 1))) return s;
+        if ((s = voff.ensure(nP + 2))) return s;
         if ((s = kall_scan.ensure(nP + 2))) return s;
 
         if ((s = ensure_scan_scratch(nP + 1))) return s;
         pbeg(KID_TP);
-        Kernels<D>::tp(PV, nP, dsteps.ptr, with_tp ? 1 : 0, MC, Bcap.ptr, err, lc);
+        Kernels<D>::tp(PV, nP, dsteps.ptr, with_tp ? 1 : 0, MC, Bcap.ptr, nvert.ptr, err, lc);
         pend();
         pbeg(KID_SCAN);
         scan_int_to_ll(PV.nkids, PV.kscan, nP, ss, lc);
         scan_int_to_ll(Bcap.ptr, PV.B_off, nP, ss, lc);
         scan_int_to_ll(PV.nkids_all, kall_scan.ptr, nP, ss, lc);
+        scan_int_to_ll(nvert.ptr, voff.ptr, nP, ss, lc);
         pend();
-        long long tot[3] = {0, 0, 0};
+        long long tot[4] = {0, 0, 0, 0};
         MCE_CUDA(cudaMemcpyAsync(&tot[0], PV.kscan + nP, sizeof(long long), cudaMemcpyDeviceToHost, lc.stream));
         MCE_CUDA(cudaMemcpyAsync(&tot[1], PV.B_off + nP, sizeof(long long), cudaMemcpyDeviceToHost, lc.stream));
         MCE_CUDA(cudaMemcpyAsync(&tot[2], kall_scan.ptr + nP, sizeof(long long), cudaMemcpyDeviceToHost, lc.stream));
+        MCE_CUDA(cudaMemcpyAsync(&tot[3], voff.ptr + nP, sizeof(long long), cudaMemcpyDeviceToHost, lc.stream));
         // per-estimator post-MU counts for the un-reduced final MU
         std::vector<long long> kall_at(E + 1, 0);
         MCE_CUDA(cudaStreamSynchronize(lc.stream));
-        const long long K = tot[0], Btot = tot[1], Kall = tot[2];
+        const long long K = tot[0], Btot = tot[1], Kall = tot[2], Nvert = tot[3];
         const long long nR = nP + K;
         post_mu_terms += nP + Kall;
         if ((s = fam_mom.ensure((size_t)(nP + Kall + 1) * (1 + D + D * D)))) return s;
         if ((s = Bkeys.ensure(Btot + 1))) return s;
+        if ((s = vsv.ensure(Nvert + 1))) return s;
         if ((s = Rb.ensure(nR, MC))) return s;
         pbeg(KID_BUILD_B);
         Kernels<D>::build_B(PV, nP, dsteps.ptr, with_tp ? 1 : 0, Told, Bkeys.ptr, Btot, dbpert.ptr, MC,
-                            dcombo_off.ptr, dcombos.ptr, err, lc);
+                            dcombo_off.ptr, dcombos.ptr, voff.ptr, Nvert, vsv.ptr, err, lc);
         pend();
         TermRecs R = Rb.view();
         pbeg(KID_MU);

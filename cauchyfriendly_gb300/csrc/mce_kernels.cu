@@ -335,7 +335,8 @@ __global__ void k_first_tables(ParentList P, long long nP, const double* cval, c
 // Time propagation + TP coalignment (cauchy_term.hpp:435-531) and the count
 // of hyperplanes the MU will integrate (cauchy_term.hpp:106-130).
 template <int D>
-__global__ void k_tp(ParentList P, long long nP, const EstStep<D>* st, int with_tp, int MC, int* Bcap, int* err)
+__global__ void k_tp(ParentList P, long long nP, const EstStep<D>* st, int with_tp, int MC, int* Bcap, int* nvert,
+                     int* err)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nP; i += (long long)gridDim.x * blockDim.x) {
         const int e = P.est[i];
@@ -404,6 +405,9 @@ __global__ void k_tp(ParentList P, long long nP, const EstStep<D>* st, int with_
         else if (with_tp && m != P.m_old[i]) cap = m < D ? (1 << (m - 1)) : half_cells_cap(m, D);
         else cap = P.tab_cnt[i];
         Bcap[i] = cap;
+        // d-subsets the TP enumeration solves (none for m <= d: the reference
+        // has no subsets for m == d)
+        nvert[i] = (!S.skip && with_tp && m != P.m_old[i] && m > D) ? (int)binom_ll(m, D) : 0;
     }
 }
 
@@ -416,19 +420,77 @@ __global__ void k_tp(ParentList P, long long nP, const EstStep<D>* st, int with_
 // sign vector is output (half storage) when its negation was found too.  The
 // sets are held as shared-memory bitmaps, so the output comes out sorted and
 // de-duplicated without hashing.  Other parents copy their table keys.
+// The FP64 half of the enumeration, a thread per (parent, d-subset) of every
+// enumerating parent (voff: exclusive subset offsets): cond(A_c) > 1e12 skips
+// the subset (cell_enumeration.hpp:751-757); otherwise the vertex
+// A_c v = b_pert_c and the signs of the other rows at it give the subset's
+// sign vector, written to vsv (-1: skipped).  Most parents have few subsets
+// (a 3-state term of 4-6 hyperplanes has 4-20), so one parent per warp would
+// leave most lanes idle; here every lane solves a subset.
+template <int D>
+__global__ void k_build_B_vertices(ParentList P, long long nP, const long long* voff, long long nv,
+                                   const double* bpert_all, int MC, const int* combo_off,
+                                   const unsigned char* combos, int* vsv)
+{
+    for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < nv; x += (long long)gridDim.x * blockDim.x) {
+        long long lo = 0, hi = nP;
+        while (hi - lo > 1) {
+            const long long mid = (lo + hi) >> 1;
+            if (voff[mid] <= x) lo = mid;
+            else hi = mid;
+        }
+        const long long i = lo;
+        const int m = P.m[i];
+        const double* As = P.A + i * MC * D;
+        const double* bp = bpert_all + (long long)P.est[i] * MC;
+        const unsigned char* c = combos + combo_off[m] + (x - voff[i]) * D;
+        double Ac[D * D], bc[D], v[D];
+        int Pv[D];
+        for (int j = 0; j < D; j++) {
+            for (int l = 0; l < D; l++) Ac[j * D + l] = As[c[j] * D + l];
+            bc[j] = bp[c[j]];
+        }
+        int out = -1;
+        // cond(A) > 1e12 skips the vertex.  A single-precision upper bound from
+        // the exact LU factors settles the well-conditioned subsets; the
+        // reference's explicit-inverse value is computed only when the bound is
+        // not at least ten times below 1e12.
+        double nrm = -1;
+        for (int cc = 0; cc < D; cc++) {
+            double sm = 0;
+            for (int r = 0; r < D; r++) sm += fabs(Ac[r * D + cc]);
+            if (dlt(nrm, sm)) nrm = sm;
+        }
+        if (plu<D>(Ac, Pv)) {
+            const double bound = nrm * (double)inv_norm1_bound<D>(Ac);
+            if ((bound <= 0.1 * kCondEps) || !(cond1_from_lu<D>(Ac, Pv, nrm) > kCondEps)) {
+                solve_lu<D>(Ac, Pv, bc, v);
+                unsigned inmask = 0;
+                for (int j = 0; j < D; j++) inmask |= 1u << c[j];
+                int niv = 0;
+                for (int a = 0; a < m; a++) {
+                    if (inmask & (1u << a)) continue;
+                    double s = 0.0;
+                    for (int j = 0; j < D; j++) s += As[a * D + j] * v[j];
+                    if (neg(s - bp[a])) niv |= 1 << a;
+                }
+                out = niv;
+            }
+        }
+        vsv[x] = out;
+    }
+}
+
 template <int D>
 __global__ void k_build_B(ParentList P, long long nP, const EstStep<D>* st, int with_tp, Tables Told, int* Bkeys,
                           const double* bpert_all, int MC, const int* combo_off, const unsigned char* combos,
-                          int* err)
+                          const long long* voff, const int* vsv, int* err)
 {
     extern __shared__ unsigned long long smem_u64[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
     const int words = (1 << MC) > 32 ? (1 << MC) / 32 : 1;
-    const int per_warp_u32 = 2 * words + 2 * MC * D + 2;  // two bitmaps + A rows (as doubles)
-    unsigned* base = reinterpret_cast<unsigned*>(smem_u64) + (size_t)wib * ((per_warp_u32 + 1) & ~1);
-    double* As = reinterpret_cast<double*>(base);
-    unsigned* PB = base + 2 * MC * D;
-    unsigned* IS = PB + words;
+    unsigned* PB = reinterpret_cast<unsigned*>(smem_u64) + (size_t)wib * 2 * words;  // parent cells
+    unsigned* IS = PB + words;                                                     // cells found
     for (long long i = (long long)blockIdx.x * nwb + wib; i < nP; i += (long long)gridDim.x * nwb) {
         const int e = P.est[i];
         const EstStep<D>& S = st[e];
@@ -454,8 +516,6 @@ __global__ void k_build_B(ParentList P, long long nP, const EstStep<D>* st, int 
             if (lane == 0) P.B_cnt[i] = n;
             continue;
         }
-        const double* A = P.A + i * MC * D;
-        for (int k = lane; k < m * D; k += 32) As[k] = A[k];
         const int mw = (1 << m) > 32 ? (1 << m) / 32 : 1;
         const int pw = (1 << phc) > 32 ? (1 << phc) / 32 : 1;
         for (int k = lane; k < mw; k += 32) IS[k] = 0;
@@ -466,41 +526,16 @@ __global__ void k_build_B(ParentList P, long long nP, const EstStep<D>* st, int 
             if (key >= 0 && key < (1 << phc)) atomicOr(&PB[key >> 5], 1u << (key & 31));
         }
         __syncwarp();
-        const double* bp = bpert_all + (long long)e * MC;
         const int gmask = (1 << phc) - 1, ptop = 1 << (phc - 1);
         const int ncomb = m > D ? (int)binom_ll(m, D) : 0;
         const unsigned char* cmb = combos + combo_off[m];
+        const int* vv = vsv + voff[i];
         for (int ci = lane; ci < ncomb; ci += 32) {
+            // the subset's sign vector from k_build_B_vertices, then the 2^d
+            // cells around its vertex whose parent part is a parent cell
+            const int niv = vv[ci];
+            if (niv < 0) continue;
             const unsigned char* c = cmb + (long long)ci * D;
-            double Ac[D * D], bc[D], v[D];
-            int Pv[D];
-            for (int j = 0; j < D; j++) {
-                for (int l = 0; l < D; l++) Ac[j * D + l] = As[c[j] * D + l];
-                bc[j] = bp[c[j]];
-            }
-            // cond(A) > 1e12 skips the vertex (cell_enumeration.hpp:751-757).  A
-            // single-precision upper bound from the exact LU factors settles the
-            // well-conditioned subsets; the reference's explicit-inverse value is
-            // computed only when the bound is not at least ten times below 1e12.
-            double nrm = -1;
-            for (int cc = 0; cc < D; cc++) {
-                double sm = 0;
-                for (int r = 0; r < D; r++) sm += fabs(Ac[r * D + cc]);
-                if (dlt(nrm, sm)) nrm = sm;
-            }
-            if (!plu<D>(Ac, Pv)) continue;
-            const double bound = nrm * (double)inv_norm1_bound<D>(Ac);
-            if (!(bound <= 0.1 * kCondEps) && cond1_from_lu<D>(Ac, Pv, nrm) > kCondEps) continue;
-            solve_lu<D>(Ac, Pv, bc, v);
-            unsigned inmask = 0;
-            for (int j = 0; j < D; j++) inmask |= 1u << c[j];
-            int niv = 0;
-            for (int a = 0; a < m; a++) {
-                if (inmask & (1u << a)) continue;
-                double s = 0.0;
-                for (int j = 0; j < D; j++) s += As[a * D + j] * v[j];
-                if (neg(s - bp[a])) niv |= 1 << a;
-            }
             for (int j = 0; j < (1 << D); j++) {
                 int sv = niv;
                 for (int k = 0; k < D; k++)
@@ -1940,36 +1975,43 @@ void Kernels<D>::first_tables(ParentList P, long long nP, const double* cval, co
 }
 
 template <int D>
-void Kernels<D>::tp(ParentList P, long long nP, const EstStep<D>* st, int with_tp, int MC, int* Bcap, int* err,
-                    const LaunchCfg& c)
+void Kernels<D>::tp(ParentList P, long long nP, const EstStep<D>* st, int with_tp, int MC, int* Bcap, int* nvert,
+                    int* err, const LaunchCfg& c)
 {
     if (nP == 0) return;
     ++g_launches;
-    k_tp<D><<<grid_for(nP, 128, c.num_sms), 128, 0, c.stream>>>(P, nP, st, with_tp, MC, Bcap, err);
+    k_tp<D><<<grid_for(nP, 128, c.num_sms), 128, 0, c.stream>>>(P, nP, st, with_tp, MC, Bcap, nvert, err);
 }
 
 static inline size_t build_B_smem_per_warp(int MC, int D)
 {
+    (void)D;
     const int words = (1 << MC) > 32 ? (1 << MC) / 32 : 1;
-    const int u32 = 2 * words + 2 * MC * D + 2;
-    return (size_t)((u32 + 1) & ~1) * 4;
+    return (size_t)2 * words * 4;
 }
 
 template <int D>
 void Kernels<D>::build_B(ParentList P, long long nP, const EstStep<D>* st, int with_tp, Tables Told, int* Bkeys,
                          long long Bcap_total, const double* bpert, int MC, const int* combo_off,
-                         const unsigned char* combos, int* err, const LaunchCfg& c)
+                         const unsigned char* combos, const long long* voff, long long nv, int* vsv, int* err,
+                         const LaunchCfg& c)
 {
     (void)Bcap_total;
     if (nP == 0) return;
+    if (nv > 0) {
+        ++g_launches;
+        k_build_B_vertices<D><<<grid_for(nv, 128, c.num_sms, 16), 128, 0, c.stream>>>(P, nP, voff, nv, bpert, MC,
+                                                                                      combo_off, combos, vsv);
+    }
     const size_t pw = build_B_smem_per_warp(MC, D);
     int warps = (int)(96 * 1024 / pw);
     if (warps > 8) warps = 8;
     if (warps < 1) warps = 1;
     const size_t sm = pw * warps;
     cudaFuncSetAttribute(k_build_B<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    ++g_launches;
     k_build_B<D><<<grid_for(nP, warps, c.num_sms, 8), warps * 32, sm, c.stream>>>(
-        P, nP, st, with_tp, Told, Bkeys, bpert, MC, combo_off, combos, err);
+        P, nP, st, with_tp, Told, Bkeys, bpert, MC, combo_off, combos, voff, vsv, err);
 }
 
 template <int D>

@@ -35,11 +35,12 @@ struct Kernels {
 
     // Time propagation, TP coalignment and child counting (cauchy_term.hpp:84-145, 435-531).
     static void tp(ParentList P, long long nP, const EstStep<D>* st, int with_tp, int MC, int* Bcap,
-                   int* err, const LaunchCfg& c);
+                   int* nvert, int* err, const LaunchCfg& c);
     // B tables: TP enumeration (cell_enumeration.hpp:676-855) or a copy of the parent keys.
     static void build_B(ParentList P, long long nP, const EstStep<D>* st, int with_tp, Tables Told,
                         int* Bkeys, long long Bcap_total, const double* bpert, int MC, const int* combo_off,
-                        const unsigned char* combos, int* err, const LaunchCfg& c);
+                        const unsigned char* combos, const long long* voff, long long nv, int* vsv, int* err,
+                        const LaunchCfg& c);
     // Measurement update, g/yei evaluation, moment partials, MU coalignment.
     static void mu(ParentList P, long long nP, const EstStep<D>* st, const long long* pstart,
                    const double* roots, Tables Told, int* Bkeys, TermRecs R, long long nR,
