@@ -346,7 +346,8 @@ public:
     DevBuf<int> g_nr, g_items, g_cells, g_rflag, g_minfo, g_mflag, nvert, vsv;
     DevBuf<long long> g_ioff, g_coff, voff;
     DevBuf<double> g_rps2, g_mps2;
-    DevBuf<double> gscale, mom_tot;
+    DevBuf<double> gscale, mom_tot, mu_rows;
+    DevBuf<int> mu_ints;
     DevBuf<long long> goff, toff, rscan, bucket_off, rbase, scan_tmp, kall_est;
     DevBuf<int> status, owner, gcnt, gfill, members, members_tmp, is_root, cap, roots_list, alive, src,
         tcnt, hist, new_slot, counters, first_cnt, bcount, bfill, slot_of;
@@ -872,9 +873,11 @@ public:
                             dcombo_off.ptr, dcombos.ptr, voff.ptr, Nvert, vsv.ptr, err, lc);
         pend();
         TermRecs R = Rb.view();
+        if ((s = mu_rows.ensure((size_t)(nP + 1) * ((MC + 1) * (D + 1) + 1)))) return s;
+        if ((s = mu_ints.ensure((size_t)(nP + 1) * 4))) return s;
         pbeg(KID_MU);
-        Kernels<D>::mu(PV, nP, dsteps.ptr, dpstart.ptr, droots.ptr, Told, Bkeys.ptr, R, nR, kall_scan.ptr,
-                       fam_mom.ptr, MC, err, lc);
+        Kernels<D>::mu(PV, nP, dsteps.ptr, dpstart.ptr, droots.ptr, Told, Bkeys.ptr, R, nR, kall_scan.ptr, nP + Kall,
+                       mu_rows.ptr, mu_ints.ptr, fam_mom.ptr, MC, err, lc);
         pend();
         pbeg(KID_MOMENTS);
         Kernels<D>::moments(fam_mom.ptr, dpstart.ptr, kall_scan.ptr, E, dsteps.ptr, mom_tot.ptr, est_raw.ptr,

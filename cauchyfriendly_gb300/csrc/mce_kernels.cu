@@ -677,277 +677,225 @@ __device__ inline int mu_coalign_smem(double* A, double* p, double* q, int m, un
     return ns;
 }
 
-// Shared memory of k_mu per warp, in doubles: per lane one MU row and its
-// scale, a staged term (A rows, p, q) and its moment contribution; then the
-// round's rank -> lane table, record slots and per-family scalars.
-__host__ __device__ inline int mu_warp_doubles(int MC, int D)
+// Measurement update (cauchy_term.hpp:84-310) in two passes.
+//
+// k_mu_rows, a thread per parent: the MU rows mu_l = A_l / (H . A_l) with
+// rho_l = p_l |H . A_l| (an H-orthogonal row keeps A_l and p_l and gets no
+// child), the measurement row (0, gamma), zeta = z - H . b, the masks of
+// integrable rows and of negative H . A_l, and the parent's B -> B_mu flip
+// (cauchy_term.hpp:245-250).  Per parent the row record holds (MC + 1) x D mu
+// values, MC + 1 rho values and zeta; the int record holds the integrable
+// mask, enc_lhp and the flip mask.
+template <int D>
+__global__ void k_mu_rows(ParentList P, long long nP, const EstStep<D>* st, int* Bkeys, double* frow, int* fint,
+                          int MC)
 {
-    const int NM = 1 + D + D * D;
-    return 32 * (D + 1) + 32 * (MC * D + 2 * MC) + 32 * 2 * NM + 16 + 32 + 32;
+    const int FR = (MC + 1) * (D + 1) + 1;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nP; i += (long long)gridDim.x * blockDim.x) {
+        const EstStep<D>& S = st[P.est[i]];
+        const int m = P.m[i], phc = P.m_old[i];
+        const double* A = P.A + i * MC * D;
+        const double* p = P.p + i * MC;
+        const double* b = P.b + i * D;
+        double* mu = frow + i * FR;
+        double* rho = mu + (MC + 1) * D;
+        unsigned integ = 0;
+        int esg = 0;
+        for (int l = 0; l < m; l++) {
+            double h = 0.0;
+            for (int j = 0; j < D; j++) h += S.H[j] * A[l * D + j];
+            const double ah = fabs(h);
+            if (abs_lt(h, kMuEps)) {
+                for (int j = 0; j < D; j++) mu[l * D + j] = A[l * D + j];
+                rho[l] = p[l];
+            } else {
+                const double r = 1.0 / h;
+                for (int j = 0; j < D; j++) mu[l * D + j] = A[l * D + j] * r;
+                rho[l] = p[l] * ah;
+                integ |= 1u << l;
+                if (!(h > 0)) esg |= 1 << l;
+            }
+        }
+        for (int j = 0; j < D; j++) mu[m * D + j] = 0.0;
+        rho[m] = S.gamma;
+        double hb = 0.0;
+        for (int j = 0; j < D; j++) hb += S.H[j] * b[j];
+        mu[(MC + 1) * (D + 1)] = S.msmt - hb;
+        int lhp = esg;
+        if (phc < m) lhp &= (1 << phc) - 1;
+        const int esg_c = (esg & (1 << (m - 1))) ? (esg ^ ((1 << m) - 1)) : esg;
+        fint[i * 4 + 0] = (int)integ;
+        fint[i * 4 + 1] = lhp;
+        fint[i * 4 + 2] = esg_c;
+        P.bflip[i] = esg_c;
+        if (!S.skip) {
+            int* B = Bkeys + P.B_off[i];
+            const int n = P.B_cnt[i];
+            for (int k = 0; k < n; k++) B[k] ^= esg_c;
+        }
+    }
 }
 
-// Measurement update of every parent (cauchy_term.hpp:84-310), fused with the
-// g/yei evaluation of the parent and its children (cauchy_term.hpp:312-401),
-// the moment contributions (cache_moments, cauchy_estimator.hpp:307), the
-// parent's re-normalisation and the children's MU coalignment.
-//
-// Lane packing: a family (parent of m hyperplanes and its children) needs
-// m + 1 lanes, lane t < m for hyperplane t / child t and lane m for the
-// measurement row / the parent itself.  Each warp walks a chunk of up to 32
-// consecutive parents in rounds; a round takes as many consecutive families
-// as fit in the 32 lanes (3-state terms have 4-12 lanes each), so the FP64
-// work, which the SM issues per warp instruction whatever the number of
-// active lanes, runs on nearly full warps.  The per-term arithmetic is the
-// same as with one family per warp.  Each round's contributions and records
-// leave with coalesced warp-wide stores (the families of consecutive parents
-// are contiguous in both).
+// k_mu_terms, a thread per post-MU term, in the moment-contribution order
+// (each parent, then its children by hyperplane): the child's rows
+// mu_l - mu_t (the parent's rows for the parent), the g/yei evaluation
+// (cauchy_term.hpp:312-401), the moment contribution (cache_moments,
+// cauchy_estimator.hpp:307), and the record with the parent's
+// re-normalisation or the child's MU coalignment (cauchy_term.hpp:533-745).
+// Every lane runs the same per-term code, so the FP64 work fills the warps
+// whatever the families' sizes.  Each thread stages its term's rows in shared
+// memory for the coalignment.
 template <int D>
-__global__ void __launch_bounds__(128) k_mu(ParentList P, long long nP, const EstStep<D>* st, const long long* pstart,
-                                            const double* roots, Tables Told, int* Bkeys, TermRecs R, long long nR,
-                                            const long long* kall_scan, cd* contrib, int MC, int chunk, int* err)
+__global__ void __launch_bounds__(128) k_mu_terms(ParentList P, long long nP, const EstStep<D>* st,
+                                                  const long long* pstart, const double* roots, Tables Told,
+                                                  TermRecs R, long long nR, const long long* kall_scan,
+                                                  long long nterms, const double* frow, const int* fint,
+                                                  cd* contrib, int MC, int* err)
 {
     extern __shared__ double smem_d[];
     constexpr int NM = 1 + D + D * D;
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
-    const int RS = MC * D + 2 * MC;  // staged doubles per lane
-    double* wbase = smem_d + (size_t)wib * mu_warp_doubles(MC, D);
-    double* mu = wbase;                // 32 x D: the row of lane L
-    double* rho = mu + 32 * D;         // 32
-    double* stage = rho + 32;          // 32 x RS
-    double* cstage = stage + 32 * RS;  // 32 x 2 NM
-    int* rank2lane = reinterpret_cast<int*>(cstage + 32 * 2 * NM);       // round rank -> staging lane
-    long long* slot_of = reinterpret_cast<long long*>(rank2lane + 32);  // round rank -> record slot (-1: none)
-    int* fam_esgc = reinterpret_cast<int*>(slot_of + 32);                // family -> B flip mask
-    int* fam_bok = fam_esgc + 32;                                        // family -> flips its B table
-    double* At = stage + lane * RS;
+    const int RS = MC * D + 2 * MC;
+    const int FR = (MC + 1) * (D + 1) + 1;
+    double* At = smem_d + (size_t)threadIdx.x * RS;
     double* pt = At + MC * D;
     double* qt = pt + MC;
-    const long long nchunks = (nP + chunk - 1) / chunk;
-    for (long long ch = (long long)blockIdx.x * nwb + wib; ch < nchunks; ch += (long long)gridDim.x * nwb) {
-        const long long cend = (ch + 1) * chunk < nP ? (ch + 1) * chunk : nP;
-        long long cur = ch * chunk;
-        while (cur < cend) {
-            // ---- the round: consecutive families whose lanes fit in the warp
-            const int my_need = (cur + lane < cend) ? P.m[cur + lane] + 1 : 64;
-            int pre = my_need;
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y = __shfl_up_sync(kFull, pre, o);
-                if (lane >= o) pre += y;
+    for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < nterms;
+         x += (long long)gridDim.x * blockDim.x) {
+        // the family: the last parent i with i + kall_scan[i] <= x
+        long long lo = 0, hi = nP;
+        while (hi - lo > 1) {
+            const long long mid = (lo + hi) >> 1;
+            if (mid + kall_scan[mid] <= x) lo = mid;
+            else hi = mid;
+        }
+        const long long i = lo;
+        const int ford = (int)(x - (i + kall_scan[i]));  // 0: the parent, c + 1: child c
+        const int e = P.est[i];
+        const EstStep<D>& S = st[e];
+        const int m = P.m[i], phc = P.m_old[i];
+        const double* mu = frow + i * FR;
+        const double* rho = mu + (MC + 1) * D;
+        const double zeta = mu[(MC + 1) * (D + 1)];
+        const unsigned integ_mask = (unsigned)fint[i * 4 + 0];
+        const int lhp = fint[i * 4 + 1];
+        const double* b = P.b + i * D;
+        const double* root = roots + (long long)e * D;
+        int t = m;
+        if (ford > 0) {
+            unsigned msk = integ_mask;
+            for (int c = 1; c < ford; c++) msk &= msk - 1;
+            t = __ffs(msk) - 1;
+        }
+        double bt[D], ty[D];
+        for (int j = 0; j < D; j++) {
+            bt[j] = b[j] + zeta * mu[t * D + j];
+            ty[j] = 0;
+        }
+        unsigned hof = 0;
+        int sneg = 0;
+        double ygi = 0;
+        int l = 0;
+        for (int ll = 0; ll <= m; ll++) {
+            if (ll == t) continue;
+            const bool fi = (ll < m) ? ((integ_mask >> ll) & 1u) : true;
+            double row[D];
+            if (fi)
+                for (int j = 0; j < D; j++) row[j] = mu[ll * D + j] - mu[t * D + j];
+            else {
+                for (int j = 0; j < D; j++) row[j] = mu[ll * D + j];
+                hof |= 1u << l;
             }
-            const int nfam = __popc(__ballot_sync(kFull, pre <= 32));  // >= 1: m + 1 <= 32
-            const unsigned starts = __reduce_or_sync(kFull, lane < nfam ? (1u << (pre - my_need)) : 0u);
-            const int used = __shfl_sync(kFull, pre, nfam - 1);
-            const unsigned le = starts & ((2u << lane) - 1u);  // family starts at or below this lane
-            const int f = __popc(le) - 1;
-            const int fb = 31 - __clz(le);  // first lane of this lane's family
-            const int t = lane - fb;
-            const bool active = lane < used;
-            const long long i = cur + f;
-            int e = 0, m = 0, phc = 0;
-            if (active) {
-                e = P.est[i];
-                m = P.m[i];
-                phc = P.m_old[i];
-            }
-            const EstStep<D>& S = st[e];
-            const double* A = P.A + i * MC * D;
-            const double* p = P.p + i * MC;
-            const double* b = P.b + i * D;
-            const double* root = roots + (long long)e * D;
-            // ---- MU rows: lane t < m hyperplane t, lane m the measurement row
-            bool integ = false, neg = false;
-            double zeta_l = 0;
-            if (active) {
-                if (t < m) {
-                    double h = 0.0;
-                    for (int j = 0; j < D; j++) h += S.H[j] * A[t * D + j];
-                    const double ah = fabs(h);
-                    if (abs_lt(h, kMuEps)) {
-                        for (int j = 0; j < D; j++) mu[lane * D + j] = A[t * D + j];
-                        rho[lane] = p[t];
-                    } else {
-                        const double r = 1.0 / h;
-                        for (int j = 0; j < D; j++) mu[lane * D + j] = A[t * D + j] * r;
-                        rho[lane] = p[t] * ah;
-                        integ = true;
-                        neg = !(h > 0);
-                    }
-                } else {
-                    for (int j = 0; j < D; j++) mu[lane * D + j] = 0.0;
-                    rho[lane] = S.gamma;
-                    double hb = 0.0;
-                    for (int j = 0; j < D; j++) hb += S.H[j] * b[j];
-                    zeta_l = S.msmt - hb;
+            const double pl = rho[ll];
+            double s = 0.0;
+            for (int j = 0; j < D; j++) s += row[j] * root[j];
+            const bool sgp = pos(s);
+            if (!sgp) sneg |= 1 << l;
+            const double sc = sgp ? pl : -pl;  // p_l * sign, exact
+            for (int j = 0; j < D; j++) ty[j] += sc * row[j];
+            if (!(hof & (1u << l))) ygi += sc;
+            for (int j = 0; j < D; j++) At[l * D + j] = row[j];
+            pt[l] = pl;
+            l++;
+        }
+        // lambda keys into the parent table (cauchy_term.hpp:357-381)
+        int lp = 0, lm = 0, k = 0;
+        for (int l2 = 0; l2 < m; l2++) {
+            if (k < phc) {
+                if (k == t) {
+                    lm |= 1 << k;
+                    k++;
+                    if (k == phc) continue;
                 }
-            }
-            const unsigned integ_all = __ballot_sync(kFull, integ);
-            const unsigned neg_all = __ballot_sync(kFull, neg);
-            const double zeta = __shfl_sync(kFull, zeta_l, (fb + m) & 31);
-            __syncwarp();
-            const unsigned fmask = m >= 32 ? kFull : ((1u << m) - 1u);
-            const unsigned integ_mask = (integ_all >> fb) & fmask;
-            const int esg = (int)((neg_all >> fb) & fmask);
-            int lhp = esg, esg_c = 0;
-            if (active) {
-                if (phc < m) lhp &= (1 << phc) - 1;
-                esg_c = (esg & (1 << (m - 1))) ? (esg ^ ((1 << m) - 1)) : esg;
-            }
-            const bool write = !S.skip;
-            const long long kbase = active ? P.kscan[pstart[e]] : 0;
-            const long long pslot = i + kbase;                              // parent's record
-            const long long cslot0 = active ? pstart[e + 1] + P.kscan[i] : 0;  // first child's record
-            const int nk = __popc(integ_mask);
-            const bool mine = active && (t < m ? ((integ_mask >> t) & 1u) != 0 : true);
-            // family order of this lane's term: parent 0, child c -> 1 + c
-            const int ford = (t == m) ? 0 : 1 + __popc(integ_mask & ((1u << t) - 1u));
-            const long long fbase0 = cur + kall_scan[cur];  // the round's first contribution row
-            if (mine) {
-                const int q = (int)(i + kall_scan[i] - fbase0) + ford;
-                const bool rec_ok = write && pslot < nR && cslot0 + nk <= nR;
-                rank2lane[q] = lane;
-                slot_of[q] = rec_ok ? ((t == m) ? pslot : cslot0 + (ford - 1)) : -1;
-            }
-            if (active && t == m) {
-                fam_esgc[f] = esg_c;
-                fam_bok[f] = write ? 1 : 0;
-                P.bflip[i] = esg_c;
-            }
-            if (mine) {
-                double bt[D], ty[D];
-                for (int j = 0; j < D; j++) {
-                    bt[j] = b[j] + zeta * mu[lane * D + j];
-                    ty[j] = 0;
+                if ((sneg >> l2) & 1) {
+                    lp |= 1 << k;
+                    lm |= 1 << k;
                 }
-                unsigned hof = 0;
-                int sneg = 0;
-                double ygi = 0;
-                int l = 0;
-                for (int ll = 0; ll <= m; ll++) {
-                    if (ll == t) continue;
-                    const bool fi = (ll < m) ? ((integ_mask >> ll) & 1u) : true;
-                    const double* mrow = mu + (fb + ll) * D;
-                    double row[D];
-                    if (fi)
-                        for (int j = 0; j < D; j++) row[j] = mrow[j] - mu[lane * D + j];
-                    else {
-                        for (int j = 0; j < D; j++) row[j] = mrow[j];
-                        hof |= 1u << l;
-                    }
-                    const double pl = rho[fb + ll];
-                    double s = 0.0;
-                    for (int j = 0; j < D; j++) s += row[j] * root[j];
-                    const bool sgp = pos(s);
-                    if (!sgp) sneg |= 1 << l;
-                    const double sc = sgp ? pl : -pl;  // p_l * sign, exact
-                    for (int j = 0; j < D; j++) ty[j] += sc * row[j];
-                    if (!(hof & (1u << l))) ygi += sc;
-                    for (int j = 0; j < D; j++) At[l * D + j] = row[j];
-                    pt[l] = pl;
-                    l++;
-                }
-                // lambda keys into the parent table (cauchy_term.hpp:357-381)
-                int lp = 0, lm = 0, k = 0;
-                for (int l2 = 0; l2 < m; l2++) {
-                    if (k < phc) {
-                        if (k == t) {
-                            lm |= 1 << k;
-                            k++;
-                            if (k == phc) continue;
-                        }
-                        if ((sneg >> l2) & 1) {
-                            lp |= 1 << k;
-                            lm |= 1 << k;
-                        }
-                        k++;
-                    }
-                }
-                const int* pk = Told.keys + P.tab_off[i];
-                const cd* pv = Told.vals + P.tab_off[i];
-                const int pcnt = P.tab_cnt[i];
-                const cd gp = lookup_num(pk, pv, pcnt, lp ^ lhp, phc);
-                const cd gm = lookup_num(pk, pv, pcnt, lm ^ lhp, phc);
-                const double dv = rho[lane];
-                cd g = csub(cdiv(gp, mkcd(ygi + dv, zeta)), cdiv(gm, mkcd(ygi - dv, zeta)));
-                g = cscale(g, kTwoPiInv);
-                cd* cs = reinterpret_cast<cd*>(cstage) + lane * NM;
-                cs[0] = g;
-                for (int j = 0; j < D; j++) {
-                    const cd y = mkcd(-ty[j], bt[j]);
-                    const cd gy = cmul(g, y);
-                    cs[1 + j] = gy;
-                    for (int kk = 0; kk < D; kk++) cs[1 + D + j * D + kk] = cmul(gy, mkcd(-ty[kk], bt[kk]));
-                }
-                if (write) {
-                    const long long slot = (t == m) ? pslot : cslot0 + (ford - 1);
-                    if (slot >= nR) {
-                        set_err(err, kErrTableOverflow);
-                    } else {
-                        int mfin = m;
-                        int flags = (t == m) ? 0 : kFlagNewChild;
-                        if (t == m) {
-                            // parent: normalize_hps(true), no coalignment
-                            for (int r = 0; r < m; r++) {
-                                qt[r] = pt[r];
-                                double n1 = 0;
-                                for (int j = 0; j < D; j++) n1 += fabs(At[r * D + j]);
-                                pt[r] *= n1;
-                                for (int j = 0; j < D; j++) At[r * D + j] /= n1;
-                            }
-                        } else {
-                            mfin = mu_coalign_smem<D>(At, pt, qt, m, hof, R.cmap + slot * MC, R.csmap + slot * MC,
-                                                      err);
-                            if (mfin != m) flags |= kFlagHasCmap;
-                        }
-                        for (int j = 0; j < D; j++) R.b[slot * D + j] = bt[j];
-                        R.est[slot] = e;
-                        R.m[slot] = mfin;
-                        R.pbc[slot] = m;
-                        R.phc[slot] = phc;
-                        R.z[slot] = t;
-                        R.lhp[slot] = lhp;
-                        R.fam[slot] = (int)i;
-                        R.horthog[slot] = hof;
-                        R.cval[slot] = zeta;
-                        R.dval[slot] = dv;
-                        R.flags[slot] = flags;
-                    }
-                } else if (t == m && pslot < nR) {
-                    // a final MU keeps no records; mark the parent's slot empty
-                    R.est[pslot] = -1;
-                }
+                k++;
             }
-            const int T = __popc(__ballot_sync(kFull, mine));  // terms of the round
-            __syncwarp();
-            // moment contributions of the round's families in the reference's
-            // summation order (each parent followed by its children)
-            {
-                double* out = reinterpret_cast<double*>(contrib + fbase0 * NM);
-                for (int x = lane; x < T * 2 * NM; x += 32) {
-                    const int q = x / (2 * NM), o = x % (2 * NM);
-                    out[x] = cstage[rank2lane[q] * 2 * NM + o];
-                }
+        }
+        const int* pk = Told.keys + P.tab_off[i];
+        const cd* pv = Told.vals + P.tab_off[i];
+        const int pcnt = P.tab_cnt[i];
+        const cd gp = lookup_num(pk, pv, pcnt, lp ^ lhp, phc);
+        const cd gm = lookup_num(pk, pv, pcnt, lm ^ lhp, phc);
+        const double dv = rho[t];
+        cd g = csub(cdiv(gp, mkcd(ygi + dv, zeta)), cdiv(gm, mkcd(ygi - dv, zeta)));
+        g = cscale(g, kTwoPiInv);
+        cd* cs = contrib + x * NM;
+        cs[0] = g;
+        for (int j = 0; j < D; j++) {
+            const cd y = mkcd(-ty[j], bt[j]);
+            const cd gy = cmul(g, y);
+            cs[1 + j] = gy;
+            for (int kk = 0; kk < D; kk++) cs[1 + D + j * D + kk] = cmul(gy, mkcd(-ty[kk], bt[kk]));
+        }
+        const long long pslot = i + P.kscan[pstart[e]];            // parent's record
+        const long long cslot0 = pstart[e + 1] + P.kscan[i];       // first child's record
+        if (S.skip) {
+            // a final MU keeps no records; mark the parent's slot empty
+            if (t == m && pslot < nR) R.est[pslot] = -1;
+            continue;
+        }
+        const long long slot = (t == m) ? pslot : cslot0 + (ford - 1);
+        if (slot >= nR) {
+            set_err(err, kErrTableOverflow);
+            continue;
+        }
+        int mfin = m;
+        int flags = (t == m) ? 0 : kFlagNewChild;
+        if (t == m) {
+            // parent: normalize_hps(true), no coalignment
+            for (int r = 0; r < m; r++) {
+                qt[r] = pt[r];
+                double n1 = 0;
+                for (int j = 0; j < D; j++) n1 += fabs(At[r * D + j]);
+                pt[r] *= n1;
+                for (int j = 0; j < D; j++) At[r * D + j] /= n1;
             }
-            // records: A, p, q rows (padded to MC) of the families that keep them
-            for (int x = lane; x < T * RS; x += 32) {
-                const int q = x / RS, o = x % RS;
-                const long long slot = slot_of[q];
-                if (slot < 0) continue;
-                const double v = stage[rank2lane[q] * RS + o];
-                if (o < MC * D) R.A[slot * MC * D + o] = v;
-                else if (o < MC * D + MC) R.p[slot * MC + (o - MC * D)] = v;
-                else R.q[slot * MC + (o - MC * D - MC)] = v;
+        } else {
+            mfin = mu_coalign_smem<D>(At, pt, qt, m, hof, R.cmap + slot * MC, R.csmap + slot * MC, err);
+            if (mfin != m) flags |= kFlagHasCmap;
+        }
+        for (int j = 0; j < D; j++) R.b[slot * D + j] = bt[j];
+        R.est[slot] = e;
+        R.m[slot] = mfin;
+        R.pbc[slot] = m;
+        R.phc[slot] = phc;
+        R.z[slot] = t;
+        R.lhp[slot] = lhp;
+        R.fam[slot] = (int)i;
+        R.horthog[slot] = hof;
+        R.cval[slot] = zeta;
+        R.dval[slot] = dv;
+        R.flags[slot] = flags;
+        // rows of a family whose records do not all fit are dropped, as before
+        if (pslot < nR && cslot0 + __popc(integ_mask) <= nR) {
+            double* Ao = R.A + slot * MC * D;
+            for (int q = 0; q < mfin * D; q++) Ao[q] = At[q];
+            for (int q = 0; q < mfin; q++) {
+                R.p[slot * MC + q] = pt[q];
+                R.q[slot * MC + q] = qt[q];
             }
-            // parent B -> B_mu (cauchy_term.hpp:245-250)
-            for (int ff = 0; ff < nfam; ff++) {
-                if (!fam_bok[ff]) continue;
-                const long long ip = cur + ff;
-                int* B = Bkeys + P.B_off[ip];
-                const int n = P.B_cnt[ip];
-                const int ec = fam_esgc[ff];
-                for (int k = lane; k < n; k += 32) B[k] ^= ec;
-            }
-            __syncwarp();
-            cur += nfam;
         }
     }
 }
@@ -2016,27 +1964,23 @@ void Kernels<D>::build_B(ParentList P, long long nP, const EstStep<D>* st, int w
 
 template <int D>
 void Kernels<D>::mu(ParentList P, long long nP, const EstStep<D>* st, const long long* pstart, const double* roots,
-                    Tables Told, int* Bkeys, TermRecs R, long long nR, const long long* kall_scan, cd* contrib,
-                    int MC, int* err, const LaunchCfg& c)
+                    Tables Told, int* Bkeys, TermRecs R, long long nR, const long long* kall_scan, long long nterms,
+                    double* frow, int* fint, cd* contrib, int MC, int* err, const LaunchCfg& c)
 {
     if (nP == 0) return;
-    const size_t pw = (size_t)mu_warp_doubles(MC, D) * sizeof(double);
-    int warps = (int)(200 * 1024 / pw);
-    if (warps > 4) warps = 4;
-    if (warps < 1) warps = 1;
-    const size_t sm = pw * warps;
-    cudaFuncSetAttribute(k_mu<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     ++g_launches;
-    // parents per warp: up to 32, fewer when that would leave the GPU with
-    // less than 16 warps per SM
-    const long long want = (long long)c.num_sms * 16;
-    long long chunk = (nP + want - 1) / want;
-    if (chunk > 32) chunk = 32;
-    if (chunk < 1) chunk = 1;
-    const long long nchunks = (nP + chunk - 1) / chunk;
-    k_mu<D><<<grid_for(nchunks, warps, c.num_sms, 16), warps * 32, sm, c.stream>>>(P, nP, st, pstart, roots, Told,
-                                                                                   Bkeys, R, nR, kall_scan, contrib,
-                                                                                   MC, (int)chunk, err);
+    k_mu_rows<D><<<grid_for(nP, 128, c.num_sms, 16), 128, 0, c.stream>>>(P, nP, st, Bkeys, frow, fint, MC);
+    if (nterms == 0) return;
+    // each thread stages one term's rows (MC x D, p, q) in shared memory
+    const size_t rs = (size_t)(MC * D + 2 * MC) * sizeof(double);
+    int threads = (int)(96 * 1024 / rs) / 32 * 32;
+    if (threads > 128) threads = 128;
+    if (threads < 32) threads = 32;
+    const size_t sm = rs * threads;
+    cudaFuncSetAttribute(k_mu_terms<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    ++g_launches;
+    k_mu_terms<D><<<grid_for(nterms, threads, c.num_sms, 16), threads, sm, c.stream>>>(
+        P, nP, st, pstart, roots, Told, R, nR, kall_scan, nterms, frow, fint, contrib, MC, err);
 }
 
 template <int D>

@@ -44,7 +44,8 @@ struct Kernels {
     // Measurement update, g/yei evaluation, moment partials, MU coalignment.
     static void mu(ParentList P, long long nP, const EstStep<D>* st, const long long* pstart,
                    const double* roots, Tables Told, int* Bkeys, TermRecs R, long long nR,
-                   const long long* kall_scan, cd* contrib, int MC, int* err, const LaunchCfg& c);
+                   const long long* kall_scan, long long nterms, double* frow, int* fint, cd* contrib, int MC,
+                   int* err, const LaunchCfg& c);
     // Per-estimator moment sums in the reference's order and finalisation
     // (cauchy_estimator.hpp:307-357).
     static void moments(const cd* contrib, const long long* pstart, const long long* kall_scan, int E,
