@@ -18,7 +18,7 @@
 namespace mce {
 
 #if MCE_COMMON_UNIT
-long long g_launches = 0;
+thread_local long long g_launches = 0;
 #endif
 
 static constexpr unsigned kFull = 0xffffffffu;

@@ -6,8 +6,9 @@
 
 namespace mce {
 
-// Kernels launched by this library since load (every launch site counts itself).
-extern long long g_launches;
+// Kernels launched by the calling host thread (every launch site counts
+// itself; per thread, so handles stepped from several threads count their own).
+extern thread_local long long g_launches;
 
 struct LaunchCfg {
     cudaStream_t stream;
