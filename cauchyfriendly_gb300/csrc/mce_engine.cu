@@ -184,6 +184,9 @@ public:
     virtual int shift_terms_b(int e, const double* v, int sub) = 0;
     // every current term of estimator e: time_prop with Phi and B u (Bu may be null)
     virtual int time_prop_terms(int e, const double* Phi, const double* Bu) = 0;
+    virtual int cpdf_2d_grid(int est, int i1, int i2, const double* bar_nu, double lx, double hx, double rx,
+                             double ly, double hy, double ry, int reset_cache, int max_points, double* xs,
+                             double* ys, double* zs) = 0;
     virtual int cpdf_1d_grid(int est, int marg, const double* bar_nu, double low, double high, double res,
                              int max_points, double* xs, double* ys) = 0;
     // waits for the work the engine queued (after a step that stopped early)
@@ -548,7 +551,8 @@ public:
         master_step = 0;
         nP = 0;
         post_mu_terms = 0;
-        cpdf_step.assign(cpdf_step.size(), -1);  // the pdf cache belongs to the old terms
+        cpdf_step.assign(cpdf_step.size(), -1);  // the pdf caches belong to the old terms
+        cpdf2_step.assign(cpdf2_step.size(), -1);
         device_errors = 0;
         MCE_CUDA(cudaMemset(counters.ptr, 0, 8 * sizeof(int)));
         return MCE_OK;
@@ -1152,6 +1156,98 @@ public:
         return MCE_OK;
     }
 
+    // ---- marginal 2-D pdf: CauchyCPDFGridDispatcher2D (cpdf_ndim.hpp:1774-1919)
+    // over PointWiseNDimCauchyCPDF::evaluate_2D_marginal_cpdf (:1356-1455), with
+    // the reference's per-term cache kept on the device, keyed by (master step,
+    // the two indices) and, as for the 1-D pdf, the term count
+    std::vector<int> cpdf2_step, cpdf2_i1, cpdf2_i2;
+    std::vector<long long> cpdf2_n;
+    std::vector<std::unique_ptr<DevBuf<double>>> cpdf2_tt;
+    DevBuf<double> cpdf2_x, cpdf2_y, cpdf2_z;
+
+    int cpdf_2d_grid(int e, int i1, int i2, const double* bar_nu, double lx, double hx, double rx, double ly,
+                     double hy, double ry, int reset_cache, int max_points, double* xs, double* ys,
+                     double* zs) override
+    {
+        if (e < 0 || e >= E || i1 < 0 || i1 >= i2 || i2 >= D || !bar_nu) return MCE_ERR_ARG;
+        if (!(hx > lx) || !(rx > 0) || !(hy > ly) || !(ry > 0)) return MCE_ERR_ARG;
+        const double sx = (hx - lx + rx - 1e-15) / rx, sy = (hy - ly + ry - 1e-15) / ry;
+        if (!(sx < 1e6) || !(sy < 1e6)) {
+            set_error("cpdf grid: too many points");
+            return MCE_ERR_ARG;
+        }
+        const int nx = (int)sx + 1, ny = (int)sy + 1;  // reset_grid, cpdf_ndim.hpp:1816-1845
+        if ((long long)nx * ny > 100000000LL) {
+            set_error("cpdf grid: too many points");
+            return MCE_ERR_ARG;
+        }
+        const int npts = nx * ny;
+        if (!xs || !ys || !zs) return npts;
+        if (npts > max_points) {
+            set_error("cpdf grid: " + std::to_string(npts) + " points do not fit in " + std::to_string(max_points));
+            return MCE_ERR_ARG;
+        }
+        if (master_step < 1) {
+            set_error("cpdf: the estimator has not been stepped");
+            return MCE_ERR_ARG;
+        }
+        if (master_step >= est[e].num_updates) {
+            set_error("cpdf: the last step keeps no g-tables");
+            return MCE_ERR_DONE;
+        }
+        for (int i = 0; i < ny; i++) {
+            double y = ly + i * ry;
+            if (y > hy) y = hy;
+            for (int j = 0; j < nx; j++) {
+                double x = lx + j * rx;
+                if (x > hx) x = hx;
+                xs[i * nx + j] = x;
+                ys[i * nx + j] = y;
+            }
+        }
+        if ((int)cpdf2_step.size() != E) {
+            cpdf2_step.assign(E, -1);
+            cpdf2_i1.assign(E, -1);
+            cpdf2_i2.assign(E, -1);
+            cpdf2_n.assign(E, -1);
+            cpdf2_tt.clear();
+            cpdf2_tt.resize(E);
+        }
+        const long long a = hpstart[e], n = hpstart[e + 1] - a;
+        int s;
+        if (cpdf2_step[e] != master_step || cpdf2_i1[e] != i1 || cpdf2_i2[e] != i2 || cpdf2_n[e] != n) {
+            if (!cpdf2_tt[e]) cpdf2_tt[e].reset(new DevBuf<double>());
+            if ((s = cpdf2_tt[e]->ensure((size_t)(n + 1) * cpdf2d_stride(MC)))) return s;
+            if ((s = cpdf_nu.ensure(D))) return s;
+            MCE_CUDA(cudaMemcpyAsync(cpdf_nu.ptr, bar_nu, sizeof(double) * D, cudaMemcpyHostToDevice, lc.stream));
+            Kernels<D>::cpdf2d_terms(Pb[cur].view(), a, n, i1, i2, cpdf_nu.ptr,
+                                     Tables{Tb[cur].keys.ptr, Tb[cur].vals.ptr}, MC, cpdf2_tt[e]->ptr, lc);
+            cpdf2_step[e] = master_step;
+            cpdf2_i1[e] = i1;
+            cpdf2_i2[e] = i2;
+            cpdf2_n[e] = n;
+        }
+        if ((s = cpdf2_x.ensure(npts))) return s;
+        if ((s = cpdf2_y.ensure(npts))) return s;
+        if ((s = cpdf2_z.ensure(npts))) return s;
+        MCE_CUDA(cudaMemcpyAsync(cpdf2_x.ptr, xs, sizeof(double) * npts, cudaMemcpyHostToDevice, lc.stream));
+        MCE_CUDA(cudaMemcpyAsync(cpdf2_y.ptr, ys, sizeof(double) * npts, cudaMemcpyHostToDevice, lc.stream));
+        MCE_CUDA(cudaMemsetAsync(counters.ptr + 7, 0, sizeof(int), lc.stream));
+        cpdf2d_points(cpdf2_tt[e]->ptr, n, MC, cpdf2_x.ptr, cpdf2_y.ptr, npts, est[e].fz[0], cpdf2_z.ptr,
+                      counters.ptr + 7, lc);
+        int bad = 0;
+        MCE_CUDA(cudaMemcpyAsync(zs, cpdf2_z.ptr, sizeof(double) * npts, cudaMemcpyDeviceToHost, lc.stream));
+        MCE_CUDA(cudaMemcpyAsync(&bad, counters.ptr + 7, sizeof(int), cudaMemcpyDeviceToHost, lc.stream));
+        MCE_CUDA(cudaStreamSynchronize(lc.stream));
+        // the cache survives unless the caller drops it (pycauchy.hpp:856-859)
+        if (reset_cache) cpdf2_step[e] = -1;
+        if (bad) {
+            set_error("cpdf: a cell with gamma1 = gamma2 = 0 (the reference exits here)");
+            return MCE_ERR_DEVICE;
+        }
+        return npts;
+    }
+
     // ---- marginal 1-D pdf: CauchyCPDFGridDispatcher1D (cpdf_ndim.hpp:2017-2139)
     // over PointWiseNDimCauchyCPDF::evaluate_1D_marginal_cpdf (:1233-1352),
     // with the reference's per-estimator cache of per-term constants, kept on
@@ -1715,6 +1811,14 @@ int mce_finalize_extended_moments(mce_handle* h, int e, double* x_bar)
     for (int i = 0; i < d; i++) eh.mean[2 * i] += x_bar[i];
     for (int i = 0; i < d; i++) x_bar[i] = eh.mean[2 * i];
     return MCE_OK;
+}
+int mce_cpdf_2d_grid(mce_handle* h, int e, int marg_idx1, int marg_idx2, const double* bar_nu, double gridx_low,
+                     double gridx_high, double gridx_res, double gridy_low, double gridy_high, double gridy_res,
+                     int reset_cache, int max_points, double* x, double* y, double* z)
+{
+    if (bad(h, e)) return MCE_ERR_ARG;
+    return h->eng->cpdf_2d_grid(e, marg_idx1, marg_idx2, bar_nu, gridx_low, gridx_high, gridx_res, gridy_low,
+                                gridy_high, gridy_res, reset_cache, max_points, x, y, z);
 }
 int mce_draw_bar_nu(long long seed, int d, double* bar_nu)
 {

@@ -2246,6 +2246,172 @@ void Kernels<D>::det_tp(ParentList P, long long a, long long n, const double* Ph
     k_det_tp<D><<<grid_for(n, 128, c.num_sms, 16), 128, 0, c.stream>>>(P, a, n, Phi, Bu, MC);
 }
 
+// ---------------------------------------------------------------------------
+// Marginal 2-D conditional pdf over the current terms
+// (PointWiseNDimCauchyCPDF::evaluate_2D_marginal_cpdf, cpdf_ndim.hpp:1356-1455).
+// k_cpdf2d_terms, a thread per term: the two marginal columns of A
+// normalised, zero rows marked and coaligned rows merged
+// (marg2d_remove_zeros_and_coalign, :42-140); the 2m cell-wall angles sorted
+// (:143-174); per half-plane cell its sign vector at the mid angle (:177-202),
+// its parent-table key (zero rows take the sign of A_j . bar_nu), g value and
+// the real parts of gamma1, gamma2 (:1551-1600).  This is the reference's
+// per-term cache (Cached2DCPDFTerm); its exact first evaluation uses the same
+// sines, cosines and gammas, so every grid point is summed from the cache.
+// Record per term (cpdf2d_stride doubles): m, b1, b2, sin[MC+1], cos[MC+1],
+// g1r[MC], g2r[MC], g[MC] (re, im).
+
+template <int D>
+__global__ void k_cpdf2d_terms(ParentList P, long long a, long long n, int i1, int i2, const double* bar_nu, Tables T,
+                               int MC, double* tt)
+{
+    const int RT = cpdf2d_stride(MC);
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const long long i = a + q;
+        const int m = P.m[i];
+        const double* At = P.A + i * MC * D;
+        double A[2 * kMaxRows], p[kMaxRows], A2[2 * kMaxRows], p2[kMaxRows];
+        int cmap[kMaxRows], csmap[kMaxRows], fidx[kMaxRows];
+        unsigned F = 0;
+        for (int r = 0; r < m; r++) {
+            A[2 * r] = At[r * D + i1];
+            A[2 * r + 1] = At[r * D + i2];
+            p[r] = P.p[i * MC + r];
+            F |= 1u << r;
+        }
+        for (int r = 0; r < m; r++) {
+            const double f0 = fabs(A[2 * r]), f1 = fabs(A[2 * r + 1]);
+            if (f0 < kMuEps && f1 < kMuEps) {
+                cmap[r] = csmap[r] = fidx[r] = 32;
+                F &= ~(1u << r);
+                continue;
+            }
+            const double s = f0 + f1;
+            A[2 * r] /= s;
+            A[2 * r + 1] /= s;
+            p[r] *= s;
+        }
+        int mn = 0;
+        for (int r = 0; r < m; r++) {
+            if (!((F >> r) & 1u)) continue;
+            cmap[r] = mn;
+            csmap[r] = 1;
+            fidx[r] = r;
+            p2[mn] = p[r];
+            for (int j = r + 1; j < m; j++) {
+                if (!((F >> j) & 1u)) continue;
+                if (fabs(A[2 * r] - A[2 * j]) < kCoalignEps && fabs(A[2 * r + 1] - A[2 * j + 1]) < kCoalignEps) {
+                    cmap[j] = mn;
+                    csmap[j] = 1;
+                    F &= ~(1u << j);
+                    fidx[j] = r;
+                    p2[mn] += p[j];
+                    continue;
+                }
+                if (fabs(A[2 * r] + A[2 * j]) < kCoalignEps && fabs(A[2 * r + 1] + A[2 * j + 1]) < kCoalignEps) {
+                    cmap[j] = mn;
+                    csmap[j] = -1;
+                    F &= ~(1u << j);
+                    fidx[j] = r;
+                    p2[mn] += p[j];
+                }
+            }
+            mn++;
+        }
+        {
+            int u = 0;
+            for (int r = 0; r < m; r++)
+                if (mn == m || fidx[r] == r) {
+                    A2[2 * u] = A[2 * r];
+                    A2[2 * u + 1] = A[2 * r + 1];
+                    u++;
+                }
+        }
+        double th[2 * kMaxRows];
+        for (int r = 0; r < mn; r++) {
+            const double a0 = A2[2 * r], a1 = A2[2 * r + 1];
+            double pt0, pt1;
+            if (fabs(a0) < fabs(a1)) {
+                pt0 = 1;
+                pt1 = -a0 / a1;
+            } else {
+                pt0 = -a1 / a0;
+                pt1 = 1;
+            }
+            double t1 = atan2(pt1, pt0);
+            if (t1 < 0) t1 += kPi;
+            th[2 * r] = t1;
+            th[2 * r + 1] = t1 + kPi;
+        }
+        for (int x = 1; x < 2 * mn; x++) {  // ascending (the reference's qsort of distinct angles)
+            const double v = th[x];
+            int y = x - 1;
+            while (y >= 0 && th[y] > v) {
+                th[y + 1] = th[y];
+                y--;
+            }
+            th[y + 1] = v;
+        }
+        double* o = tt + q * RT;
+        double* os = o + 3;
+        double* oc = os + (MC + 1);
+        double* o1 = oc + (MC + 1);
+        double* o2 = o1 + MC;
+        double* og = o2 + MC;
+        o[0] = mn;
+        o[1] = P.b[i * D + i1];
+        o[2] = P.b[i * D + i2];
+        const int* keys = T.keys + P.tab_off[i];
+        const cd* vals = T.vals + P.tab_off[i];
+        const int cnt = P.tab_cnt[i];
+        for (int c = 0; c < mn; c++) {
+            const double tm = (th[c + 1] + th[c]) / 2.0;
+            const double ct = cos(tm), st = sin(tm);
+            unsigned neg = 0;  // sv[j] = -1
+            for (int j = 0; j < mn; j++)
+                if (!(A2[2 * j] * ct + A2[2 * j + 1] * st > 0)) neg |= 1u << j;
+            int enc = 0;
+            if (mn == m) {
+                enc = (int)neg;
+            } else {
+                for (int j = 0; j < m; j++) {
+                    if (cmap[j] == 32) {
+                        double ip = 0.0;
+                        for (int l = 0; l < D; l++) ip += At[j * D + l] * bar_nu[l];
+                        if (ip < 0) enc |= 1 << j;
+                    } else {
+                        const bool sneg = (neg >> cmap[j]) & 1u;
+                        if (sneg != (csmap[j] < 0)) enc |= 1 << j;
+                    }
+                }
+            }
+            const cd g = lookup_num(keys, vals, cnt, enc, m);
+            double g1r = 0, g2r = 0;
+            for (int j = 0; j < mn; j++) {
+                const double sv = ((neg >> j) & 1u) ? -1.0 : 1.0;
+                g1r -= (A2[2 * j] * p2[j]) * sv;
+                g2r -= (A2[2 * j + 1] * p2[j]) * sv;
+            }
+            os[c] = sin(th[c]);
+            oc[c] = cos(th[c]);
+            o1[c] = g1r;
+            o2[c] = g2r;
+            og[2 * c] = g.re;
+            og[2 * c + 1] = g.im;
+        }
+        os[mn] = mn > 0 ? sin(th[mn]) : 0.0;
+        oc[mn] = mn > 0 ? cos(th[mn]) : 0.0;
+    }
+}
+
+template <int D>
+void Kernels<D>::cpdf2d_terms(ParentList P, long long a, long long n, int i1, int i2, const double* bar_nu, Tables T,
+                              int MC, double* tt, const LaunchCfg& c)
+{
+    if (n == 0) return;
+    ++g_launches;
+    k_cpdf2d_terms<D><<<grid_for(n, 128, c.num_sms, 16), 128, 0, c.stream>>>(P, a, n, i1, i2, bar_nu, T, MC, tt);
+}
+
 #if MCE_COMMON_UNIT
 // One thread per point, the terms summed in order.  Points below `exact`
 // take the complex formula (fx * 1/(2 pi) / fz), the others the cached one
@@ -2275,6 +2441,79 @@ __global__ void k_cpdf1d_points(const double* tt, long long n, const double* xs,
         }
         ys[q] = fx / fz;
     }
+}
+
+// One cell's integral (marg2d_eval_term_for_cpdf / marg2d_cached_eval_term_for_cpdf,
+// cpdf_ndim.hpp:1602-1640, 1710-1740): the fast form, or, with gamma1 ~ 0,
+// the form that also handles gamma2 ~ 0; both ~ 0 is the reference's exit,
+// reported here through *bad.
+__device__ inline double marg2d_cell(double s1, double c1, double s2, double c2, double g1r, double g1i, double g2r,
+                                     double g2i, bool check, cd g, int* bad)
+{
+    cd gamma1 = mkcd(g1r, g1i), gamma2 = mkcd(g2r, g2i);
+    bool fast = true;
+    if (check && fabs(g1r) < 1e-8) {
+        fast = false;
+        if (fabs(g2r) < 1e-8 && fabs(g2i) < 1e-8) {
+            *bad = 1;
+            return 0.0;
+        }
+    }
+    cd cell;
+    if (fast) {
+        gamma2 = cmul(gamma2, gamma1);
+        gamma1 = cmul(gamma1, gamma1);
+        const cd lo = cdiv(mkcd(s1, 0), cadd(cscale(gamma1, c1), cscale(gamma2, s1)));
+        const cd hi = cdiv(mkcd(s2, 0), cadd(cscale(gamma1, c2), cscale(gamma2, s2)));
+        cell = cmul(csub(hi, lo), g);
+    } else {
+        const cd lo = cdiv(csub(cscale(gamma1, s1), cscale(gamma2, c1)), cadd(cscale(gamma1, c1), cscale(gamma2, s1)));
+        const cd hi = cdiv(csub(cscale(gamma1, s2), cscale(gamma2, c2)), cadd(cscale(gamma1, c2), cscale(gamma2, s2)));
+        cell = csub(hi, lo);
+        gamma1 = cmul(gamma1, gamma1);
+        gamma2 = cmul(gamma2, gamma2);
+        cell = cmul(cell, cdiv(g, cadd(gamma1, gamma2)));
+    }
+    return cell.re;
+}
+
+// A thread per grid point; terms and their cells summed in order, then
+// 2 fx / (2 pi)^2 / fz (cpdf_ndim.hpp:1447).
+__global__ void k_cpdf2d_points(const double* tt, long long n, int MC, const double* xs, const double* ys, int npts,
+                                double fz, double* zs, int* bad)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= npts) return;
+    const int RT = cpdf2d_stride(MC);
+    const double x1 = xs[q], x2 = ys[q];
+    double fx = 0;
+    int b = 0;
+    for (long long j = 0; j < n; j++) {
+        const double* o = tt + j * RT;
+        const int mn = (int)o[0];
+        const double* os = o + 3;
+        const double* oc = os + (MC + 1);
+        const double* o1 = oc + (MC + 1);
+        const double* o2 = o1 + MC;
+        const double* og = o2 + MC;
+        const double g1i = o[1] - x1, g2i = o[2] - x2;
+        const bool check = fabs(g1i) < 1e-8;
+        double t = 0;
+        for (int c = 0; c < mn; c++)
+            t += marg2d_cell(os[c], oc[c], os[c + 1], oc[c + 1], o1[c], g1i, o2[c], g2i, check,
+                             mkcd(og[2 * c], og[2 * c + 1]), &b);
+        fx += t;
+    }
+    zs[q] = 2 * fx * kTwoPiInv * kTwoPiInv / fz;
+    if (b) atomicOr(bad, 1);
+}
+
+void cpdf2d_points(const double* tt, long long n, int MC, const double* xs, const double* ys, int npts, double fz,
+                   double* zs, int* bad, const LaunchCfg& c)
+{
+    if (npts <= 0) return;
+    ++g_launches;
+    k_cpdf2d_points<<<(npts + 63) / 64, 64, 0, c.stream>>>(tt, n, MC, xs, ys, npts, fz, zs, bad);
 }
 
 void cpdf1d_points(const double* tt, long long n, const double* xs, int npts, int exact, double fz, double* ys,

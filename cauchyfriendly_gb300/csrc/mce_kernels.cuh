@@ -74,6 +74,8 @@ struct Kernels {
     static void shift_b(ParentList P, long long a, long long n, const double* v, int sub, const LaunchCfg& c);
     static void det_tp(ParentList P, long long a, long long n, const double* Phi, const double* Bu, int MC,
                        const LaunchCfg& c);
+    static void cpdf2d_terms(ParentList P, long long a, long long n, int i1, int i2, const double* bar_nu, Tables T,
+                             int MC, double* tt, const LaunchCfg& c);
     static void cpdf1d_terms(ParentList P, long long a, long long n, int marg, const double* bar_nu, Tables T,
                              int MC, double* tt, const LaunchCfg& c);
     static void gtable_combine(TermRecs R, const int* roots_list, long long nroots, const long long* coff,
@@ -91,6 +93,11 @@ struct Kernels {
 
 // Shape-agnostic kernels.
 void group_count(const int* status, const int* owner, long long nR, int* gcnt, const LaunchCfg& c);
+// doubles per term record of the marginal 2-D pdf
+__host__ __device__ inline int cpdf2d_stride(int MC) { return 6 * MC + 6; }
+// marginal 2-D pdf at npts points (xs, ys) from the per-term records of k_cpdf2d_terms
+void cpdf2d_points(const double* tt, long long n, int MC, const double* xs, const double* ys, int npts, double fz,
+                   double* zs, int* bad, const LaunchCfg& c);
 // marginal 1-D pdf at npts points from the per-term records of k_cpdf1d_terms
 void cpdf1d_points(const double* tt, long long n, const double* xs, int npts, int exact, double fz, double* ys,
                    const LaunchCfg& c);

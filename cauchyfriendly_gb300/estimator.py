@@ -187,6 +187,21 @@ class BatchedCauchyEstimator:
         _lib.check(self._lib.mce_finalize_extended_moments(self._h, int(e), _p(x)), "mce_finalize_extended_moments")
         return x
 
+    def cpdf_2d_grid(self, e, marg_idx1, marg_idx2, gridx, gridy, bar_nu, reset_cache=True):
+        """Marginal 2-D conditional pdf of estimator e on gridx = (low, high,
+        resolution) by gridy (CauchyCPDFGridDispatcher2D,
+        include/cpdf_ndim.hpp:1774-1919); returns flat (X, Y, Z), x fastest."""
+        nu = _f64(bar_nu).reshape(self.d)
+        g = [float(v) for v in gridx] + [float(v) for v in gridy]
+        n = self._lib.mce_cpdf_2d_grid(self._h, int(e), int(marg_idx1), int(marg_idx2), _p(nu), *g,
+                                       int(bool(reset_cache)), 0, None, None, None)
+        _lib.check(n, "mce_cpdf_2d_grid")
+        X, Y, Z = np.zeros(n), np.zeros(n), np.zeros(n)
+        n = self._lib.mce_cpdf_2d_grid(self._h, int(e), int(marg_idx1), int(marg_idx2), _p(nu), *g,
+                                       int(bool(reset_cache)), n, _p(X), _p(Y), _p(Z))
+        _lib.check(n, "mce_cpdf_2d_grid")
+        return X, Y, Z
+
     def cpdf_1d_grid(self, e, marg_idx, gridx_low, gridx_high, gridx_resolution, bar_nu):
         """Marginal 1-D conditional pdf of estimator e on the grid
         gridx_low..gridx_high step gridx_resolution
@@ -271,6 +286,26 @@ class CauchyEstimator(BatchedCauchyEstimator):
         if getattr(self, "_bar_nu", None) is None:
             self._bar_nu = draw_bar_nu(self.d)
         return self.cpdf_1d_grid(0, marg_idx, gridx_low, gridx_high, gridx_resolution, self._bar_nu)
+
+    def get_marginal_2D_pointwise_cpdf(self, marg_idx1, marg_idx2, gridx_low, gridx_high, gridx_resolution,
+                                       gridy_low, gridy_high, gridy_resolution, log_dir=None, reset_cache=True):
+        """CauchyEstimator.get_marginal_2D_pointwise_cpdf
+        (scripts/swig/cauchy/cauchy_estimator.py:954-993): (X, Y, Z) as
+        (num_gridy, num_gridx) arrays."""
+        if getattr(self, "_bar_nu", None) is None:
+            self._bar_nu = draw_bar_nu(self.d)
+        X, Y, Z = self.cpdf_2d_grid(0, marg_idx1, marg_idx2, (gridx_low, gridx_high, gridx_resolution),
+                                    (gridy_low, gridy_high, gridy_resolution), self._bar_nu, reset_cache)
+        nx = int(np.sum(Y == Y[0]))
+        return X.reshape(-1, nx), Y.reshape(-1, nx), Z.reshape(-1, nx)
+
+    def get_2D_pointwise_cpdf(self, gridx_low, gridx_high, gridx_resolution, gridy_low, gridy_high, gridy_resolution,
+                              log_dir=None, reset_cache=True):
+        """The 2-state case of get_marginal_2D_pointwise_cpdf."""
+        if self.d != 2:
+            raise ValueError("get_2D_pointwise_cpdf needs a 2-state estimator")
+        return self.get_marginal_2D_pointwise_cpdf(0, 1, gridx_low, gridx_high, gridx_resolution, gridy_low,
+                                                   gridy_high, gridy_resolution, log_dir, reset_cache)
 
     def get_1D_pointwise_cpdf(self, gridx_low, gridx_high, gridx_resolution, log_dir=None):
         """The 1-state case of get_marginal_1D_pointwise_cpdf (cauchy_estimator.py:1033-1043)."""

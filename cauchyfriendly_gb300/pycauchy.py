@@ -242,6 +242,25 @@ def pycauchy_single_step_deterministic_transform(h, Trans, bias):
     h.est.shift_cf_by_bias(np.asarray(bias, dtype=np.float64).reshape(h.n))
 
 
+def pycauchy_get_marginal_2D_pointwise_cpdf(h, marg_idx1, marg_idx2, gridx_low, gridx_high, gridx_resolution,
+                                            gridy_low, gridy_high, gridy_resolution, log_dir=None, reset_cache=True):
+    """pycauchy.hpp:822-862: the grid as (x, y, z) triples, flattened, and its
+    x and y sizes."""
+    X, Y, Z = h.est.get_marginal_2D_pointwise_cpdf(int(marg_idx1), int(marg_idx2), gridx_low, gridx_high,
+                                                   gridx_resolution, gridy_low, gridy_high, gridy_resolution,
+                                                   reset_cache=reset_cache)
+    pts = np.empty(3 * X.size)
+    pts[0::3], pts[1::3], pts[2::3] = X.reshape(-1), Y.reshape(-1), Z.reshape(-1)
+    return pts, int(X.shape[1]), int(X.shape[0])
+
+
+def pycauchy_get_2D_pointwise_cpdf(h, gridx_low, gridx_high, gridx_resolution, gridy_low, gridy_high,
+                                   gridy_resolution, log_dir=None, reset_cache=True):
+    """pycauchy.hpp:864-887"""
+    return pycauchy_get_marginal_2D_pointwise_cpdf(h, 0, 1, gridx_low, gridx_high, gridx_resolution, gridy_low,
+                                                   gridy_high, gridy_resolution, log_dir, reset_cache)
+
+
 def pycauchy_get_marginal_1D_pointwise_cpdf(h, marg_idx1, gridx_low, gridx_high, gridx_resolution, log_dir=None):
     """pycauchy.hpp:890-931: the grid as (x, y) pairs, flattened, and its size.
     The pdf object (and its rand() draws) is made on the first call."""

@@ -145,6 +145,22 @@ int mce_finalize_extended_moments(mce_handle* h, int est, double* x_bar);
 int mce_cpdf_1d_grid(mce_handle* h, int est, int marg_idx, const double* bar_nu, double grid_low, double grid_high,
                      double grid_res, int max_points, double* x, double* y);
 
+/* Marginal 2-D conditional pdf of estimator `est` over states
+ * marg_idx1 < marg_idx2 on the grid x = gridx_low ... gridx_high (step
+ * gridx_res) by y = gridy_low ... gridy_high, x varying fastest, as
+ * CauchyCPDFGridDispatcher2D (include/cpdf_ndim.hpp:1774-1919) evaluates
+ * PointWiseNDimCauchyCPDF::evaluate_2D_marginal_cpdf (:1356-1455) and
+ * pycauchy_get_marginal_2D_pointwise_cpdf returns it
+ * (scripts/swig/cauchy/pycauchy.hpp:822-862).  The per-term cache (kept for
+ * the same step and indices) is dropped after the grid when reset_cache != 0.
+ * x, y, z receive the points; with any of them NULL only the point count is
+ * returned.  Returns the number of points or a negative status (MCE_ERR_DONE
+ * after the last step; MCE_ERR_DEVICE for a cell with gamma1 = gamma2 = 0,
+ * where the reference exits). */
+int mce_cpdf_2d_grid(mce_handle* h, int est, int marg_idx1, int marg_idx2, const double* bar_nu, double gridx_low,
+                     double gridx_high, double gridx_res, double gridy_low, double gridy_high, double gridy_res,
+                     int reset_cache, int max_points, double* x, double* y, double* z);
+
 /* The draws of PointWiseNDimCauchyCPDF's constructor
  * (include/cpdf_ndim.hpp:385-388): bar_nu[i] = 2 (rand() + 1)/(RAND_MAX + 2)
  * for i < d.  seed >= 0 calls srand(seed) first. */

@@ -293,6 +293,21 @@ class Oracle(_EstimatorBase):
         self._l.lib.orc_finalize_extended_moments(self.h, _ptr(x))
         return x
 
+    def cpdf_2d_grid(self, i1, i2, bar_nu, gx, gy, reset_cache=False, max_points=200000):
+        """Marginal 2-D pdf on the grid gx = (low, high, res) x gy (the
+        reference's CauchyCPDFGridDispatcher2D); returns (x, y, z)."""
+        f = self._l.lib.orc_cpdf_2d_grid
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp] + [ctypes.c_double] * 6 + \
+            [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
+        nu = _arr(bar_nu)
+        xs, ys, zs = np.zeros(max_points), np.zeros(max_points), np.zeros(max_points)
+        n = f(self.h, int(i1), int(i2), _ptr(nu), *[float(v) for v in gx], *[float(v) for v in gy],
+              int(bool(reset_cache)), max_points, _ptr(xs), _ptr(ys), _ptr(zs))
+        if n < 0:
+            raise RuntimeError("orc_cpdf_2d_grid returned %d" % n)
+        return xs[:n].copy(), ys[:n].copy(), zs[:n].copy()
+
     def cpdf_1d_grid(self, marg, bar_nu, low, high, res, max_points=100000):
         """Marginal 1-D pdf on the grid low..high step res (the reference's
         CauchyCPDFGridDispatcher1D); returns (x, y) or raises with the status."""
@@ -388,6 +403,19 @@ class Reference(_EstimatorBase):
         self._l.lib.ref_finalize_extended_moments.argtypes = [ctypes.c_void_p, _dp]
         self._l.lib.ref_finalize_extended_moments(self.h, _ptr(x))
         return x
+
+    def cpdf_2d_grid(self, i1, i2, gx, gy, reset_cache=False, max_points=200000):
+        """The reference's own marginal 2-D pdf grid; returns (x, y, z, bar_nu)."""
+        f = self._l.lib.ref_cpdf_2d_grid
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 6 + \
+            [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp]
+        xs, ys, zs, nu = np.zeros(max_points), np.zeros(max_points), np.zeros(max_points), np.zeros(self.d)
+        n = f(self.h, int(i1), int(i2), *[float(v) for v in gx], *[float(v) for v in gy], int(bool(reset_cache)),
+              max_points, _ptr(xs), _ptr(ys), _ptr(zs), _ptr(nu))
+        if n < 0:
+            raise RuntimeError("ref_cpdf_2d_grid returned %d" % n)
+        return xs[:n].copy(), ys[:n].copy(), zs[:n].copy(), nu
 
     def cpdf_1d_grid(self, marg, low, high, res, max_points=100000):
         """The reference's own marginal 1-D pdf grid; returns (x, y, bar_nu)."""

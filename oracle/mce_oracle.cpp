@@ -345,6 +345,14 @@ struct Cpdf1DTerm {
     double a, b, w, s;
 };
 
+// Per-term cache of the 2-D marginal pdf (Cached2DCPDFTerm, cpdf_ndim.hpp:205-214).
+struct Cpdf2DTerm {
+    std::vector<double> sin_t, cos_t, g1r, g2r;
+    std::vector<cplx> g;
+    double b[2];
+    int m;
+};
+
 struct Estimator {
     int d, cmcc, pncc, p, num_steps, shape_range;
     int master_step = 0;
@@ -364,6 +372,8 @@ struct Estimator {
     // 1-D marginal pdf cache, keyed like the reference's by (master step, index)
     std::vector<Cpdf1DTerm> cpdf1d_cache;
     int cpdf1d_step = -1, cpdf1d_marg = -1;
+    std::vector<Cpdf2DTerm> cpdf2d_cache;
+    int cpdf2d_step = -1, cpdf2d_m1 = -1, cpdf2d_m2 = -1;
 };
 
 // ----------------------------------------------------------------------------
@@ -1368,6 +1378,220 @@ static double cpdf1d_eval(Estimator& E, int marg, double x, const double* bar_nu
     return fx * kTwoPiInv / __real__ E.fz;
 }
 
+// ----------------------------------------------------------------------------
+// Marginal 2-D conditional pdf: PointWiseNDimCauchyCPDF::evaluate_2D_marginal_cpdf
+// (cpdf_ndim.hpp:1356-1455) with marg2d_eval_term_for_cpdf (:1474-1658), the
+// cached evaluation (:1660-1748) and the helpers marg2d_extract_2D_HPA,
+// marg2d_remove_zeros_and_coalign, marg2d_get_cell_wall_angles and
+// marg2d_get_SVs (:31-203); the grid of CauchyCPDFGridDispatcher2D
+// (:1816-1919).  Per term: the two marginal columns of A, normalised and
+// coaligned; the 2m cell-wall angles; each of the m half-plane cells'
+// sign vector (at its mid angle), g value and closed-form integral.
+
+static const double kIntegralGammaEps = 1e-8;  // INTEGRAL_GAMMA_EPS
+static const int kZeroHpMarker = 32;           // ZERO_HP_MARKER_VALUE
+
+// the integral of one cell; returns false on the reference's singularity exit
+static bool marg2d_cell(double sin_t1, double cos_t1, double sin_t2, double cos_t2, double g1r, double g1i,
+                        double g2r, double g2i, bool check_gamma1, cplx g, double* out)
+{
+    cplx gamma1 = mkc(g1r, g1i), gamma2 = mkc(g2r, g2i);
+    bool fast = true;
+    if (check_gamma1 && fabs(g1r) < kIntegralGammaEps) {
+        fast = false;
+        if (fabs(g2r) < kIntegralGammaEps && fabs(g2i) < kIntegralGammaEps) return false;
+    }
+    cplx lo, hi, cell;
+    if (fast) {
+        gamma2 *= gamma1;
+        gamma1 *= gamma1;
+        lo = cdiv(mkc(sin_t1, 0), gamma1 * cos_t1 + gamma2 * sin_t1);
+        hi = cdiv(mkc(sin_t2, 0), gamma1 * cos_t2 + gamma2 * sin_t2);
+        cell = hi - lo;
+        cell *= g;
+    } else {
+        lo = cdiv(gamma1 * sin_t1 - gamma2 * cos_t1, gamma1 * cos_t1 + gamma2 * sin_t1);
+        hi = cdiv(gamma1 * sin_t2 - gamma2 * cos_t2, gamma1 * cos_t2 + gamma2 * sin_t2);
+        cell = hi - lo;
+        gamma1 *= gamma1;
+        gamma2 *= gamma2;
+        cell *= cdiv(g, gamma1 + gamma2);
+    }
+    *out = __real__ cell;
+    return true;
+}
+
+static double cpdf2d_eval(Estimator& E, int i1, int i2, double x1, double x2, const double* bar_nu, int* err)
+{
+    const int d = E.d;
+    const bool use_cache = E.cpdf2d_step == E.master_step && E.cpdf2d_m1 == i1 && E.cpdf2d_m2 == i2;
+    double fx = 0;
+    if (use_cache) {
+        for (const Cpdf2DTerm& c : E.cpdf2d_cache) {
+            const double g1i = c.b[0] - x1, g2i = c.b[1] - x2;
+            const bool check = fabs(g1i) < kIntegralGammaEps;
+            double t = 0;
+            for (int i = 0; i < c.m; i++) {
+                double v;
+                if (!marg2d_cell(c.sin_t[i], c.cos_t[i], c.sin_t[i + 1], c.cos_t[i + 1], c.g1r[i], g1i, c.g2r[i], g2i,
+                                 check, c.g[i], &v)) {
+                    *err = 1;
+                    v = 0;
+                }
+                t += v;
+            }
+            fx += t;
+        }
+        return 2 * fx * kTwoPiInv * kTwoPiInv / __real__ E.fz;
+    }
+    E.cpdf2d_step = E.master_step;
+    E.cpdf2d_m1 = i1;
+    E.cpdf2d_m2 = i2;
+    E.cpdf2d_cache.clear();
+    for (const Term& T : E.terms) {
+        const int m = T.m;
+        // marg2d_extract_2D_HPA
+        double A[2 * 32], p[32], A2[2 * 32], p2[32], b[2];
+        int cmap[32], csmap[32], fidx[32];
+        bool F[32];
+        for (int i = 0; i < m; i++) {
+            A[2 * i] = T.A[i * d + i1];
+            A[2 * i + 1] = T.A[i * d + i2];
+            p[i] = T.p[i];
+            F[i] = true;
+        }
+        b[0] = T.b[i1];
+        b[1] = T.b[i2];
+        // marg2d_remove_zeros_and_coalign
+        for (int i = 0; i < m; i++) {
+            const double f0 = fabs(A[2 * i]), f1 = fabs(A[2 * i + 1]);
+            if (f0 < kMuEps && f1 < kMuEps) {
+                cmap[i] = csmap[i] = fidx[i] = kZeroHpMarker;
+                F[i] = false;
+                continue;
+            }
+            const double s = f0 + f1;
+            A[2 * i] /= s;
+            A[2 * i + 1] /= s;
+            p[i] *= s;
+        }
+        int mu = 0;
+        for (int i = 0; i < m; i++) {
+            if (!F[i]) continue;
+            cmap[i] = mu;
+            csmap[i] = 1;
+            fidx[i] = i;
+            p2[mu] = p[i];
+            for (int j = i + 1; j < m; j++) {
+                if (!F[j]) continue;
+                if (fabs(A[2 * i] - A[2 * j]) < kCoalignEps && fabs(A[2 * i + 1] - A[2 * j + 1]) < kCoalignEps) {
+                    cmap[j] = mu;
+                    csmap[j] = 1;
+                    F[j] = false;
+                    fidx[j] = i;
+                    p2[mu] += p[j];
+                    continue;
+                }
+                if (fabs(A[2 * i] + A[2 * j]) < kCoalignEps && fabs(A[2 * i + 1] + A[2 * j + 1]) < kCoalignEps) {
+                    cmap[j] = mu;
+                    csmap[j] = -1;
+                    F[j] = false;
+                    fidx[j] = i;
+                    p2[mu] += p[j];
+                }
+            }
+            mu++;
+        }
+        const int mn = mu;
+        if (mn < m) {
+            int u = 0;
+            for (int i = 0; i < m; i++)
+                if (fidx[i] == i) {
+                    A2[2 * u] = A[2 * i];
+                    A2[2 * u + 1] = A[2 * i + 1];
+                    u++;
+                }
+        } else {
+            memcpy(A2, A, sizeof(double) * 2 * m);
+        }
+        // marg2d_get_cell_wall_angles
+        double th[64];
+        for (int i = 0; i < mn; i++) {
+            const double* a = A2 + 2 * i;
+            double pt0, pt1;
+            if (fabs(a[0]) < fabs(a[1])) {
+                pt0 = 1;
+                pt1 = -a[0] / a[1];
+            } else {
+                pt0 = -a[1] / a[0];
+                pt1 = 1;
+            }
+            double t1 = atan2(pt1, pt0);
+            if (t1 < 0) t1 += M_PI;
+            th[2 * i] = t1;
+            th[2 * i + 1] = t1 + M_PI;
+        }
+        std::sort(th, th + 2 * mn);
+        // cells
+        Cpdf2DTerm c;
+        c.m = mn;
+        c.b[0] = b[0];
+        c.b[1] = b[1];
+        const double g1i = b[0] - x1, g2i = b[1] - x2;
+        const bool check = fabs(g1i) < kIntegralGammaEps;
+        double t = 0, s2 = 0, c2 = 0;
+        for (int i = 0; i < mn; i++) {
+            // marg2d_get_SVs: the signs at the cell's mid angle
+            const double tm = (th[i + 1] + th[i]) / 2.0;
+            const double ct = cos(tm), st = sin(tm);
+            double sv[32];
+            for (int j = 0; j < mn; j++) sv[j] = (A2[2 * j] * ct + A2[2 * j + 1] * st > 0) ? 1 : -1;
+            int enc = 0;
+            if (mn == m) {
+                for (int j = 0; j < m; j++)
+                    if (sv[j] < 0) enc |= 1 << j;
+            } else {
+                for (int j = 0; j < m; j++) {
+                    if (cmap[j] == kZeroHpMarker) {
+                        double ip = 0.0;
+                        for (int l = 0; l < d; l++) ip += T.A[j * d + l] * bar_nu[l];
+                        if (ip < 0) enc |= 1 << j;
+                    } else {
+                        const int s = (int)(sv[cmap[j]] * csmap[j]);
+                        if (s < 0) enc |= 1 << j;
+                    }
+                }
+            }
+            const cplx g = lookup_num(T.gp.get(), enc, m);
+            double g1r = 0, g2r = 0;
+            for (int j = 0; j < mn; j++) {
+                g1r -= (A2[2 * j] * p2[j]) * sv[j];
+                g2r -= (A2[2 * j + 1] * p2[j]) * sv[j];
+            }
+            const double t1 = th[i], t2 = th[i + 1];
+            const double s1 = sin(t1), c1 = cos(t1);
+            s2 = sin(t2);
+            c2 = cos(t2);
+            c.sin_t.push_back(s1);
+            c.cos_t.push_back(c1);
+            c.g1r.push_back(g1r);
+            c.g2r.push_back(g2r);
+            c.g.push_back(g);
+            double v;
+            if (!marg2d_cell(s1, c1, s2, c2, g1r, g1i, g2r, g2i, check, g, &v)) {
+                *err = 1;
+                v = 0;
+            }
+            t += v;
+        }
+        c.sin_t.push_back(s2);
+        c.cos_t.push_back(c2);
+        E.cpdf2d_cache.push_back(std::move(c));
+        fx += t;
+    }
+    return 2 * fx * kTwoPiInv * kTwoPiInv / __real__ E.fz;
+}
+
 extern "C" {
 
 void* orc_create(const double* A0, const double* p0, const double* b0, int steps, int d, int cmcc, int pncc,
@@ -1544,6 +1768,36 @@ int orc_cpdf_1d_grid(void* h, int marg, const double* bar_nu, double low, double
         ys[i] = cpdf1d_eval(E, marg, x, bar_nu);
     }
     return n;
+}
+
+// Marginal 2-D pdf grid: CauchyCPDFGridDispatcher2D::reset_grid and
+// evaluate_point_grid (cpdf_ndim.hpp:1816-1919), x varying fastest; with
+// reset_cache the cache is dropped afterwards (pycauchy.hpp:856-859).
+// Returns the point count, -2 if it exceeds max_points, -1 before the first
+// step, -5 at the last step, -6 on the reference's singular-cell exit.
+int orc_cpdf_2d_grid(void* h, int i1, int i2, const double* bar_nu, double lx, double hx, double rx, double ly,
+                     double hy, double ry, int reset_cache, int max_points, double* xs, double* ys, double* zs)
+{
+    Estimator& E = *(Estimator*)h;
+    const int nx = cpdf_grid_points(lx, hx, rx), ny = cpdf_grid_points(ly, hy, ry);
+    if ((long long)nx * ny > max_points) return -2;
+    if (E.master_step < 1) return -1;
+    if (E.master_step >= E.num_steps) return -5;
+    int err = 0;
+    for (int i = 0; i < ny; i++) {
+        double y = ly + i * ry;
+        if (y > hy) y = hy;
+        for (int j = 0; j < nx; j++) {
+            double x = lx + j * rx;
+            if (x > hx) x = hx;
+            const int q = i * nx + j;
+            xs[q] = x;
+            ys[q] = y;
+            zs[q] = cpdf2d_eval(E, i1, i2, x, y, bar_nu, &err);
+        }
+    }
+    if (reset_cache) E.cpdf2d_step = E.cpdf2d_m1 = E.cpdf2d_m2 = -1;
+    return err ? -6 : nx * ny;
 }
 
 }  // extern "C"

@@ -213,6 +213,27 @@ void ref_dump_terms(void* vh, int* shape, double* A, double* p, double* b, int* 
     }
 }
 
+// Marginal 2-D pdf on a grid through the reference's CauchyCPDFGridDispatcher2D,
+// as pycauchy_get_marginal_2D_pointwise_cpdf does (pycauchy.hpp:822-862),
+// including its optional cache reset after the grid.
+int ref_cpdf_2d_grid(void* vh, int i1, int i2, double lx, double hx, double rx, double ly, double hy, double ry,
+                     int reset_cache, int max_points, double* xs, double* ys, double* zs, double* bar_nu)
+{
+    RefHandle* h = (RefHandle*)vh;
+    if (!h->cpdf) h->cpdf = new PointWiseNDimCauchyCPDF(h->est);
+    for (int i = 0; i < h->d; i++) bar_nu[i] = h->cpdf->bar_nu[i];
+    CauchyCPDFGridDispatcher2D grid(h->cpdf, lx, hx, rx, ly, hy, ry);
+    if (grid.num_grid_points > max_points) return -2;
+    if (grid.evaluate_point_grid(i1, i2, 1)) return -5;
+    if (reset_cache) h->cpdf->reset_2D_marginal_cpdf();
+    for (int i = 0; i < grid.num_grid_points; i++) {
+        xs[i] = grid.points[i].x;
+        ys[i] = grid.points[i].y;
+        zs[i] = grid.points[i].z;
+    }
+    return grid.num_grid_points;
+}
+
 // The reference's extended-mode helpers (include/cauchy_estimator.hpp:1312-1394).
 void ref_shift_cf_by_bias(void* vh, const double* bias) { ((RefHandle*)vh)->est->shift_cf_by_bias((double*)bias); }
 void ref_deterministic_time_prop(void* vh, const double* Phi, const double* B, const double* u)

@@ -119,6 +119,56 @@ def pack_cpdf(name, prob, seed, updates, cpdf_seed):
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **arr)
 
 
+def pack_cpdf2d(name, prob, seed, updates, cpdf_seed):
+    """The reference's marginal 2-D pdf grids (CauchyCPDFGridDispatcher2D)
+    after `updates` updates, for the state pairs (0, 1) and (0, d-1): three
+    grid calls each (caching, cached with a reset after, exact again)."""
+    import ctypes
+    ref = oracle.Reference(prob, seed=seed)
+    rp, bp = ref.constants()
+    n = 0
+    for k in range(prob["steps"]):
+        for s in range(prob["p"]):
+            if n < updates:
+                ref.step(k, s)
+                n += 1
+    mo = ref.moments()
+    ctypes.CDLL(None).srand(cpdf_seed)
+    d = prob["d"]
+    arr = {
+        "d": d, "pncc": prob["pncc"], "cmcc": prob["cmcc"], "p": prob["p"], "steps": prob["steps"],
+        "Phi": prob["Phi"], "Gamma": prob["Gamma"], "beta": prob["beta"], "H": prob["H"],
+        "gamma": prob["gamma"], "A0": prob["A0"], "p0": prob["p0"], "b0": prob["b0"],
+        "msmts": prob["msmts"], "srand_seed": seed, "root_point": rp, "b_pert": bp, "updates": updates,
+    }
+    pairs = sorted({(0, 1), (0, d - 1)})
+    arr["pairs"] = np.array(pairs)
+    mu = mo["raw_mean"].real
+    sd = np.sqrt(np.abs(np.diag(mo["raw_cov"].real)))
+    sd = np.where(np.isfinite(sd) & (sd > 1e-6), sd, 1.0)
+    mu = np.where(np.isfinite(mu), mu, 0.0)
+    for pi, (i1, i2) in enumerate(pairs):
+        gx = (mu[i1] - 3 * sd[i1], mu[i1] + 3 * sd[i1], 6 * sd[i1] / 16)
+        gy = (mu[i2] - 3 * sd[i2], mu[i2] + 3 * sd[i2], 6 * sd[i2] / 16)
+        for call in range(3):
+            x, y, z, nu = ref.cpdf_2d_grid(i1, i2, gx, gy, reset_cache=(call == 1))
+            pre = "p%d_c%d_" % (pi, call)
+            arr[pre + "grid"] = np.array(list(gx) + list(gy))
+            arr[pre + "x"], arr[pre + "y"], arr[pre + "z"] = x, y, z
+        arr["bar_nu"] = nu
+    ref.close()
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **arr)
+
+
+def cpdf2d_cases():
+    return [
+        ("cpdf2d_three_state_lti", W.three_state_lti(seed=0, steps=8), 1, 5, 91),
+        ("cpdf2d_two_state_lti", W.two_state_lti(seed=0, steps=8), 2, 5, 92),
+        ("cpdf2d_four_state_lti", W.four_state_lti(seed=0, steps=5), 3, 4, 93),
+        ("cpdf2d_five_state_two_msmt", W.five_state_two_msmt(seed=0, steps=3), 4, 3, 94),
+    ]
+
+
 def ext_cases():
     return [
         ("ext_three_state_lti", W.three_state_lti(seed=0, steps=6), 1),
@@ -158,6 +208,10 @@ def main():
     if not only or "cpdf" in only:
         for name, prob, seed, updates, cseed in cpdf_cases():
             pack_cpdf(name, prob, seed, updates, cseed)
+            print("wrote %s.npz" % name)
+    if not only or "cpdf" in only:
+        for name, prob, seed, updates, cseed in cpdf2d_cases():
+            pack_cpdf2d(name, prob, seed, updates, cseed)
             print("wrote %s.npz" % name)
     if not only or "ext" in only:
         for name, prob, seed in ext_cases():

@@ -15,7 +15,7 @@ REL_TOL = 1e-9
 def names():
     """The step-record fixtures (the marginal pdf ones are cpdf_names())."""
     return sorted(n for n in (os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
-                  if not n.startswith(("cpdf1d_", "ext_")))
+                  if not n.startswith(("cpdf1d_", "cpdf2d_", "ext_")))
 
 
 def cpdf_names():
@@ -169,3 +169,25 @@ def load_ext(name):
             r["err"] = int(r["err"])
         recs.append(r)
     return prob, (z["root_point"], z["b_pert"]), recs
+
+
+def cpdf2d_names():
+    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "cpdf2d_*.npz")))
+
+
+def load_cpdf2d(name):
+    """(problem, (root_point, b_pert), updates, bar_nu,
+    [(i1, i2, call, gx, gy, x, y, z)]); call 1 resets the cache afterwards."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    prob = {k: z[k] for k in ("Phi", "Gamma", "beta", "H", "gamma", "A0", "p0", "b0", "msmts")}
+    for k in ("d", "pncc", "cmcc", "p", "steps"):
+        prob[k] = int(z[k])
+    prob["B"] = None
+    grids = []
+    for pi, (i1, i2) in enumerate(z["pairs"]):
+        for call in range(3):
+            pre = "p%d_c%d_" % (pi, call)
+            g = [float(v) for v in z[pre + "grid"]]
+            grids.append((int(i1), int(i2), call, tuple(g[:3]), tuple(g[3:]), z[pre + "x"], z[pre + "y"],
+                          z[pre + "z"]))
+    return prob, (z["root_point"], z["b_pert"]), int(z["updates"]), z["bar_nu"], grids

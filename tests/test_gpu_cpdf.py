@@ -82,3 +82,23 @@ def test_gpu_cpdf_batch_matches_oracle_and_refuses_last_step():
     for o in orcs:
         o.close()
     bat.close()
+
+
+@pytest.mark.parametrize("name", G.cpdf2d_names())
+def test_gpu_cpdf2d_matches_reference_grids(name):
+    """mce_cpdf_2d_grid against the reference's 2-D grids.  The GPU's sines,
+    cosines and arctangents are CUDA's, the reference's glibc's: the values
+    agree within REL_TOL, the grid points exactly."""
+    _, CE, _ = _need_gpu()
+    prob, (rp, bp), updates, bar_nu, grids = G.load_cpdf2d(name)
+    est = CE(prob["A0"], prob["p0"], prob["b0"], prob["steps"], prob["d"], prob["cmcc"], prob["pncc"], prob["p"],
+             root_point=rp, b_pert=bp)
+    for k, s in _updates(prob)[:updates]:
+        Phi = prob["Phi"] if prob["Phi"].ndim == 2 else prob["Phi"][k]
+        est.step(prob["msmts"][k, s], Phi, prob["Gamma"], prob["beta"], prob["H"][s], prob["gamma"][s])
+    for i1, i2, call, gx, gy, x, y, z in grids:
+        xg, yg, zg = est.cpdf_2d_grid(0, i1, i2, gx, gy, bar_nu, reset_cache=(call == 1))
+        assert np.array_equal(xg, x) and np.array_equal(yg, y), (i1, i2, call)
+        assert G.relerr(zg, z) <= G.REL_TOL, (i1, i2, call, G.relerr(zg, z))
+    assert est.device_errors() == 0
+    est.close()

@@ -39,3 +39,17 @@ def test_oracle_cpdf_refuses_the_last_step():
     with pytest.raises(RuntimeError):
         est.cpdf_1d_grid(0, np.ones(3), -1.0, 1.0, 0.1)
     est.close()
+
+
+@pytest.mark.parametrize("name", G.cpdf2d_names())
+def test_oracle_cpdf2d_matches_reference_grids(name):
+    """PointWiseNDimCauchyCPDF::evaluate_2D_marginal_cpdf through
+    CauchyCPDFGridDispatcher2D: every state pair's three grid calls (caching,
+    cached then reset, exact again)."""
+    prob, consts, updates, bar_nu, grids = G.load_cpdf2d(name)
+    est = _stepped_oracle(prob, consts, updates)
+    for i1, i2, call, gx, gy, x, y, z in grids:
+        xo, yo, zo = est.cpdf_2d_grid(i1, i2, bar_nu, gx, gy, reset_cache=(call == 1))
+        assert np.array_equal(xo, x) and np.array_equal(yo, y), (i1, i2, call)
+        assert G.relerr(zo, z) <= G.REL_TOL, (i1, i2, call, G.relerr(zo, z))
+    est.close()
