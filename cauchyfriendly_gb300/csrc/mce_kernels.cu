@@ -1652,6 +1652,17 @@ __global__ void k_gtable(GCtx c, const int* roots_list, long long nroots, const 
         if (rflag[ri]) continue;  // kept root: k_gtable_combine
         // the root is approximated out (or has no cells): the serial path
         const long long r = roots_list[ri];
+        // a group of at most kFlatMaxCells cells had its root evaluated by the
+        // flat pass, so its root is known to be approximated out; alone, the
+        // group simply dies
+        const bool root_out = gnr[ri] <= kFlatMaxCells;
+        if (root_out && gcnt[r] == 0) {
+            if (lane == 0) {
+                alive[r] = 0;
+                tcnt[r] = 0;
+            }
+            continue;
+        }
         const int m = R.m[r];
         const int e = R.est[r];
         const double gs = gscale_e[e];
@@ -1670,16 +1681,19 @@ __global__ void k_gtable(GCtx c, const int* roots_list, long long nroots, const 
             nR = cap < capMC ? cap : capMC;
         }
         long long root = r;
-        // ---- root values and the term-approximation test (flattening.hpp:242-247)
-        double ps2 = p_sum_sq(R.p + root * MC, m);
+        // ---- root values and the term-approximation test (flattening.hpp:242-247),
+        // unless the flat pass already found the root approximated out
         bool negl = true;
-        for (int k = lane; k < nR; k += 32) {
-            const cd v = g_cell<D>(c, root, RKL[k], gs);
-            okeys[k] = RKL[k];
-            ovals[k] = v;
-            if (above_approx_threshold(ps2, v.re, v.im)) negl = false;
+        if (!root_out) {
+            const double ps2 = p_sum_sq(R.p + root * MC, m);
+            for (int k = lane; k < nR; k += 32) {
+                const cd v = g_cell<D>(c, root, RKL[k], gs);
+                okeys[k] = RKL[k];
+                ovals[k] = v;
+                if (above_approx_threshold(ps2, v.re, v.im)) negl = false;
+            }
+            negl = __all_sync(kFull, negl);
         }
-        negl = __all_sync(kFull, negl);
         const int nmem = gcnt[r];
         const int* mem = members + goff[r];
         int kidx = 0;

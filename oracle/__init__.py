@@ -71,7 +71,16 @@ def build(force=False, with_reference=True, verbose=False):
 
 
 def reference_available():
-    return os.path.exists(os.path.join(REF_OUT, "libmce_ref_serial.so"))
+    """True when the reference harness is built for this host and loads (a
+    copy built on another architecture does not)."""
+    path = os.path.join(REF_OUT, "libmce_ref_serial.so")
+    if not os.path.exists(path):
+        return False
+    try:
+        ctypes.CDLL(path)
+    except OSError:
+        return False
+    return True
 
 
 _libc = ctypes.CDLL(None)
