@@ -233,6 +233,9 @@ class Engine : public EngineBase {
 public:
     LaunchCfg lc{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // the moment chains run on a side stream, overlapping the term reduction
+    cudaStream_t mstream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // per-estimator device inputs
     DevBuf<double> dA0, dp0, db0, droots, dbpert;
     DevBuf<EstStep<D>> dsteps;
@@ -373,7 +376,8 @@ public:
     long long p_l0 = 0;
     DevBuf<double> alg;  // [KID_COUNT][2] bytes, flops
 
-    void pbeg(int id)
+    // profiling brackets on the engine's stream (or on st when given)
+    void pbeg(int id, cudaStream_t st = nullptr)
     {
         p_l0 = g_launches;
         p_id = id;
@@ -386,15 +390,15 @@ public:
             }
         }
         p_a = ev_used++;
-        cudaEventRecord(evpool[p_a], lc.stream);
+        cudaEventRecord(evpool[p_a], st ? st : lc.stream);
     }
-    void pend()
+    void pend(cudaStream_t st = nullptr)
     {
         const long long nl = g_launches - p_l0;
         launches += nl;
         if (!prof_mode || p_a >= ev_used) return;
         const int b_ = ev_used++;
-        cudaEventRecord(evpool[b_], lc.stream);
+        cudaEventRecord(evpool[b_], st ? st : lc.stream);
         pevs.push_back(PEv{p_id, p_a, b_, nl});
     }
     void collect_prof()
@@ -471,6 +475,9 @@ public:
         MCE_CUDA(cudaStreamCreateWithFlags(&lc.stream, cudaStreamNonBlocking));
         MCE_CUDA(cudaEventCreate(&ev0));
         MCE_CUDA(cudaEventCreate(&ev1));
+        MCE_CUDA(cudaStreamCreateWithFlags(&mstream, cudaStreamNonBlocking));
+        MCE_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+        MCE_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
         int s = MCE_OK;
         s |= dA0.ensure((size_t)E * D * D);
         s |= dp0.ensure((size_t)E * D);
@@ -522,8 +529,12 @@ public:
     ~Engine() override
     {
         if (lc.stream) cudaStreamSynchronize(lc.stream);
+        if (mstream) cudaStreamSynchronize(mstream);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        if (mstream) cudaStreamDestroy(mstream);
         for (cudaEvent_t ev : evpool) cudaEventDestroy(ev);
         if (lc.stream) cudaStreamDestroy(lc.stream);
     }
@@ -531,6 +542,7 @@ public:
     void drain() override
     {
         if (lc.stream) cudaStreamSynchronize(lc.stream);
+        if (mstream) cudaStreamSynchronize(mstream);
     }
 
     int reset() override
@@ -783,6 +795,14 @@ public:
         }
     }
 
+    // the engine's stream waits for the side stream's moments; then the
+    // raw moments and G_SCALE_FACTOR are copied to the host
+    int join_moments()
+    {
+        MCE_CUDA(cudaStreamWaitEvent(lc.stream, ev_join, 0));
+        return read_moments();
+    }
+
     int read_moments()
     {
         const int NM = 1 + D + D * D;
@@ -842,6 +862,8 @@ public:
         ParentList PV = P.view();
         Tables Told{Tb[cur].keys.ptr, Tb[cur].vals.ptr};
         int* err = counters.ptr;
+        // a step that ended early on an error may have left moments running
+        MCE_CUDA(cudaStreamWaitEvent(lc.stream, ev_join, 0));
         if ((s = Bcap.ensure(nP + 1))) return s;
         if ((s = nvert.ensure(nP + 1))) return s;
         if ((s = voff.ensure(nP + 2))) return s;
@@ -883,11 +905,20 @@ public:
         Kernels<D>::mu(PV, nP, dsteps.ptr, dpstart.ptr, droots.ptr, Told, Bkeys.ptr, R, nR, kall_scan.ptr, nP + Kall,
                        mu_rows.ptr, mu_ints.ptr, fam_mom.ptr, MC, err, lc);
         pend();
-        pbeg(KID_MOMENTS);
-        Kernels<D>::moments(fam_mom.ptr, dpstart.ptr, kall_scan.ptr, E, dsteps.ptr, mom_tot.ptr, est_raw.ptr,
-                            gscale.ptr, lc);
-        pend();
-        read_moments();
+        // the moment chains (and G_SCALE_FACTOR) on the side stream: the term
+        // reduction below does not read them; the g-table evaluation does, so
+        // the engine's stream waits for them before it (join_moments)
+        MCE_CUDA(cudaEventRecord(ev_fork, lc.stream));
+        MCE_CUDA(cudaStreamWaitEvent(mstream, ev_fork, 0));
+        {
+            LaunchCfg lcm = lc;
+            lcm.stream = mstream;
+            pbeg(KID_MOMENTS, mstream);
+            Kernels<D>::moments(fam_mom.ptr, dpstart.ptr, kall_scan.ptr, E, dsteps.ptr, mom_tot.ptr, est_raw.ptr,
+                                gscale.ptr, lcm);
+            pend(mstream);
+        }
+        MCE_CUDA(cudaEventRecord(ev_join, mstream));
         // terms after the MU per estimator (un-reduced count, cauchy_estimator.hpp:749-751, 806-812)
         if ((s = kall_est.ensure(E + 2))) return s;
         pbeg(KID_SCAN);
@@ -925,6 +956,7 @@ public:
         if (prof_mode >= 2) alg_stats(with_tp, nR, false);
         if (!any_keep || nR == 0) {
             // every estimator that stepped has now finished
+            if ((s = join_moments())) return s;
             nP = 0;
             std::vector<long long> z(E + 1, 0);
             hpstart = z;
@@ -1057,6 +1089,7 @@ public:
         const long long nitems = gt[0], ncells = gt[1];
         if ((s = g_vals.ensure(nitems + 1))) return s;
         gf.gv = g_vals.ptr;
+        if ((s = join_moments())) return s;
         pbeg(KID_GTABLE);
         Kernels<D>::gtable_eval(R, roots_list.ptr, nroots, nitems, goff.ptr, members.ptr, PV, Told, Bkeys.ptr,
                                 gscale.ptr, toff.ptr, Tnv, gf, MC, lc);
