@@ -439,6 +439,77 @@ class Reference(_EstimatorBase):
         return xs[:n].copy(), ys[:n].copy(), nu
 
 
+
+def _unpack_rel_moments(mom):
+    return {"fz": complex(mom[0], mom[1]), "mean": mom[2:6:2] + 1j * mom[3:6:2],
+            "cov": (mom[6:14:2] + 1j * mom[7:14:2]).reshape(2, 2)}
+
+
+def oracle_rel2d(prim, sec, Trel, bar_nu_full, gx, gy, full_solve=False, with_term_approx=True,
+                 term_approx_eps=1e-8, center=True, max_points=200000):
+    """Relative-then-transformed system of two oracle estimators
+    (rel = sec - prim, projected by the 2 x d Trel): its moments, pair counts
+    and 2-D pdf on the grid gx = (low, high, step) x gy, offset by the
+    relative mean when center (as pycauchy_single_step_eval_2d_rsys_cpdf)."""
+    lib = prim._l.lib
+    f = lib.orc_rel2d_create
+    f.restype = ctypes.c_void_p
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                  ctypes.c_double, _dp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_int)]
+    T, nu = _arr(Trel), _arr(bar_nu_full)
+    mom = np.zeros(14)
+    counts = (ctypes.c_longlong * 2)()
+    st = ctypes.c_int(0)
+    r = f(prim.h, sec.h, _ptr(T), _ptr(nu), int(bool(full_solve)), 1, int(bool(with_term_approx)),
+          float(term_approx_eps), _ptr(mom), counts, ctypes.byref(st))
+    if not r:
+        raise RuntimeError("orc_rel2d_create status %d" % st.value)
+    try:
+        out = _unpack_rel_moments(mom)
+        out["pairs"], out["approxed_out"] = int(counts[0]), int(counts[1])
+        g = lib.orc_rel2d_grid
+        g.restype = ctypes.c_int
+        g.argtypes = [ctypes.c_void_p] + [ctypes.c_double] * 8 + [ctypes.c_int, _dp, _dp, _dp]
+        ox, oy = (mom[2], mom[4]) if center else (0.0, 0.0)
+        xs, ys, zs = np.zeros(max_points), np.zeros(max_points), np.zeros(max_points)
+        n = g(r, gx[0] + ox, gx[1] + ox, float(gx[2]), gy[0] + oy, gy[1] + oy, float(gy[2]),
+              float(prim.moments()["fz"].real), float(sec.moments()["fz"].real), max_points, _ptr(xs), _ptr(ys),
+              _ptr(zs))
+        if n < 0:
+            raise RuntimeError("orc_rel2d_grid returned %d" % n)
+        out["x"], out["y"], out["z"] = xs[:n].copy(), ys[:n].copy(), zs[:n].copy()
+    finally:
+        lib.orc_rel2d_destroy.argtypes = [ctypes.c_void_p]
+        lib.orc_rel2d_destroy(r)
+    return out
+
+
+def reference_rel2d(prim, sec, Trel, bar_seed, gx, gy, full_solve=False, with_term_approx=True,
+                    term_approx_eps=1e-8, center=True, max_points=200000):
+    """The reference's own relative-then-transformed system of two reference
+    estimators; the same dictionary as oracle_rel2d plus "bar_nu_full", the
+    point the reference drew after srand(bar_seed)."""
+    lib = prim._l.lib
+    f = lib.ref_rel2d
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _dp, ctypes.c_uint, ctypes.c_int, ctypes.c_int,
+                  ctypes.c_double] + [ctypes.c_double] * 6 + [ctypes.c_int, ctypes.c_int, _dp, _dp,
+                                                              ctypes.POINTER(ctypes.c_longlong), _dp, _dp, _dp]
+    T = _arr(Trel)
+    nu, mom = np.zeros(prim.d), np.zeros(14)
+    counts = (ctypes.c_longlong * 2)()
+    xs, ys, zs = np.zeros(max_points), np.zeros(max_points), np.zeros(max_points)
+    n = f(prim.h, sec.h, _ptr(T), int(bar_seed), int(bool(full_solve)), int(bool(with_term_approx)),
+          float(term_approx_eps), *[float(v) for v in gx[:2]], float(gx[2]), *[float(v) for v in gy[:2]],
+          float(gy[2]), int(bool(center)), max_points, _ptr(nu), _ptr(mom), counts, _ptr(xs), _ptr(ys), _ptr(zs))
+    if n < 0:
+        raise RuntimeError("ref_rel2d returned %d" % n)
+    out = _unpack_rel_moments(mom)
+    out["pairs"], out["approxed_out"] = int(counts[0]), int(counts[1])
+    out["x"], out["y"], out["z"] = xs[:n].copy(), ys[:n].copy(), zs[:n].copy()
+    out["bar_nu_full"] = nu
+    return out
+
 def run(est, prob, record_terms_upto=0):
     """Steps ``est`` through the whole problem; returns per-measurement records."""
     recs = []

@@ -1592,6 +1592,213 @@ static double cpdf2d_eval(Estimator& E, int i1, int i2, double x1, double x2, co
     return 2 * fx * kTwoPiInv * kTwoPiInv / __real__ E.fz;
 }
 
+// ----------------------------------------------------------------------------
+// Relative-then-transformed system of two estimators
+// (include/cauchy_prediction.hpp).  rel = secondary - primary, projected by
+// the 2 x d matrix Trel.  Every (primary term, secondary term) pair becomes
+// one 2-D term: A_rel = [-A_prim; A_sec], p_rel = [p_prim; p_sec],
+// b_rel = b_sec - b_prim (:573-584), A_2d = A_rel Trel^T, b_2d = Trel b_rel
+// (:587-588), then marg2d_remove_zeros_and_coalign (cpdf_ndim.hpp:42-138).
+// Pairs run over primary shapes, secondary shapes, primary terms, secondary
+// terms (:789-800, the single-thread order).
+
+struct RelSys {
+    int full = 0;
+    std::vector<Cpdf2DTerm> terms;
+    long long total = 0, approxed_out = 0;
+};
+
+static double rel_sgn(double x) { return (double)((x > 0) - (x < 0)); }
+
+// one pair; returns false on the reference's singular-cell exit (never here:
+// caching evaluates no integral) -- the moments go into acc[7] when given
+static void rel2d_pair(const Term& P, const Term& S, int d, const double* Trel, const double* bar_nu_full,
+                       const double* bar_nu, int full, cplx* acc, Cpdf2DTerm& c)
+{
+    const int mp = P.m, ms = S.m, mps = mp + ms;
+    double Arel[32 * 8], prel[32], brel[8], A2[2 * 32], b2[2], Ac[2 * 32], pc[32];
+    int cmap[32], csmap[32], fidx[32];
+    bool F[32];
+    for (int i = 0; i < d; i++) brel[i] = S.b[i] - P.b[i];
+    for (int i = 0; i < mp * d; i++) Arel[i] = P.A[i] * -1;
+    for (int i = 0; i < ms * d; i++) Arel[mp * d + i] = S.A[i];
+    for (int i = 0; i < mp; i++) prel[i] = P.p[i];
+    for (int i = 0; i < ms; i++) prel[mp + i] = S.p[i];
+    // matmatmul(A_rel, Trel, A_2d, mps, d, 2, d, false, true) (cauchy_linalg.hpp:352-367)
+    for (int i = 0; i < mps; i++)
+        for (int j = 0; j < 2; j++) {
+            double s = 0.0;
+            for (int k = 0; k < d; k++) s += Arel[i * d + k] * Trel[j * d + k];
+            A2[i * 2 + j] = s;
+        }
+    for (int i = 0; i < 2; i++) {
+        double s = 0.0;
+        for (int j = 0; j < d; j++) s += Trel[i * d + j] * brel[j];
+        b2[i] = s;
+    }
+    // marg2d_remove_zeros_and_coalign: A2 and prel are normalised in place
+    for (int i = 0; i < mps; i++) {
+        F[i] = true;
+        const double f0 = fabs(A2[2 * i]), f1 = fabs(A2[2 * i + 1]);
+        if (f0 < kMuEps && f1 < kMuEps) {
+            cmap[i] = csmap[i] = fidx[i] = kZeroHpMarker;
+            F[i] = false;
+            continue;
+        }
+        const double s = f0 + f1;
+        A2[2 * i] /= s;
+        A2[2 * i + 1] /= s;
+        prel[i] *= s;
+    }
+    int mn = 0;
+    for (int i = 0; i < mps; i++) {
+        if (!F[i]) continue;
+        cmap[i] = mn;
+        csmap[i] = 1;
+        fidx[i] = i;
+        pc[mn] = prel[i];
+        for (int j = i + 1; j < mps; j++) {
+            if (!F[j]) continue;
+            if (fabs(A2[2 * i] - A2[2 * j]) < kCoalignEps && fabs(A2[2 * i + 1] - A2[2 * j + 1]) < kCoalignEps) {
+                cmap[j] = mn;
+                csmap[j] = 1;
+                F[j] = false;
+                fidx[j] = i;
+                pc[mn] += prel[j];
+                continue;
+            }
+            if (fabs(A2[2 * i] + A2[2 * j]) < kCoalignEps && fabs(A2[2 * i + 1] + A2[2 * j + 1]) < kCoalignEps) {
+                cmap[j] = mn;
+                csmap[j] = -1;
+                F[j] = false;
+                fidx[j] = i;
+                pc[mn] += prel[j];
+            }
+        }
+        mn++;
+    }
+    {
+        int u = 0;
+        for (int i = 0; i < mps; i++)
+            if (mn == mps || fidx[i] == i) {
+                Ac[2 * u] = A2[2 * i];
+                Ac[2 * u + 1] = A2[2 * i + 1];
+                u++;
+            }
+    }
+    // eval_rel_sys_moments_for_term (cauchy_prediction.hpp:207-285), on the
+    // normalised, un-coalesced rows; zero rows take the sign of the full row
+    if (acc) {
+        double ty[2] = {0, 0};
+        int encp = 0, encs = 0;
+        for (int i = 0; i < mps; i++) {
+            double v;
+            if (cmap[i] != kZeroHpMarker) v = A2[2 * i] * bar_nu[0] + A2[2 * i + 1] * bar_nu[1];
+            else {
+                v = 0.0;
+                for (int l = 0; l < d; l++) v += Arel[i * d + l] * bar_nu_full[l];
+            }
+            const double s = rel_sgn(v);
+            const double sc = prel[i] * s;
+            ty[0] += sc * A2[2 * i];
+            ty[1] += sc * A2[2 * i + 1];
+            if (s < 0) {
+                if (i < mp) encp |= 1 << i;
+                else encs |= 1 << (i - mp);
+            }
+        }
+        const cplx g = lookup_num(P.gp.get(), encp, mp) * lookup_num(S.gp.get(), encs, ms);
+        const cplx y[2] = {mkc(-ty[0], b2[0]), mkc(-ty[1], b2[1])};
+        acc[0] += g;
+        for (int j = 0; j < 2; j++) {
+            acc[1 + j] += g * y[j];
+            for (int k = 0; k < 2; k++) acc[3 + j * 2 + k] -= g * y[j] * y[k];
+        }
+    }
+    // cache_rel_marg2d_term_for_cpdf (cauchy_prediction.hpp:306-443)
+    double th[2 * 32 + 1];
+    for (int i = 0; i < mn; i++) {
+        const double* a = Ac + 2 * i;
+        double pt0, pt1;
+        if (fabs(a[0]) < fabs(a[1])) {
+            pt0 = 1;
+            pt1 = -a[0] / a[1];
+        } else {
+            pt0 = -a[1] / a[0];
+            pt1 = 1;
+        }
+        double t1 = atan2(pt1, pt0);
+        if (t1 < 0) t1 += M_PI;
+        th[2 * i] = t1;
+        th[2 * i + 1] = t1 + M_PI;
+    }
+    std::sort(th, th + 2 * mn);
+    if (full && mn > 0) th[2 * mn] = th[0] + 2 * M_PI;
+    const int cells = mn * (1 + full);
+    c.m = mn;
+    c.b[0] = b2[0];
+    c.b[1] = b2[1];
+    c.sin_t.clear();
+    c.cos_t.clear();
+    c.g1r.clear();
+    c.g2r.clear();
+    c.g.clear();
+    const int maskp = (1 << mp) - 1;
+    for (int i = 0; i < cells; i++) {
+        // marg2d_get_SVs: the half at the mid angles, the other half flipped
+        const int h = i < mn ? i : i - mn;
+        const double tm = (th[h + 1] + th[h]) / 2.0;
+        const double ct = cos(tm), st = sin(tm);
+        double sv[32];
+        for (int j = 0; j < mn; j++) {
+            sv[j] = (Ac[2 * j] * ct + Ac[2 * j + 1] * st > 0) ? 1 : -1;
+            if (i >= mn) sv[j] = -1 * sv[j];
+        }
+        int enc = 0;
+        for (int j = 0; j < mps; j++) {
+            if (cmap[j] == kZeroHpMarker) {
+                double ip = 0.0;
+                for (int l = 0; l < d; l++) ip += Arel[j * d + l] * bar_nu_full[l];
+                if (ip < 0) enc |= 1 << j;
+            } else {
+                const int s = (int)(sv[cmap[j]] * csmap[j]);
+                if (s < 0) enc |= 1 << j;
+            }
+        }
+        const cplx g = lookup_num(P.gp.get(), enc & maskp, mp) * lookup_num(S.gp.get(), enc >> mp, ms);
+        double g1r = 0, g2r = 0;
+        for (int j = 0; j < mn; j++) {
+            g1r -= (Ac[2 * j] * pc[j]) * sv[j];
+            g2r -= (Ac[2 * j + 1] * pc[j]) * sv[j];
+        }
+        c.sin_t.push_back(sin(th[i]));
+        c.cos_t.push_back(cos(th[i]));
+        c.g1r.push_back(g1r);
+        c.g2r.push_back(g2r);
+        c.g.push_back(g);
+    }
+    c.sin_t.push_back(cells > 0 ? sin(th[cells]) : 0.0);
+    c.cos_t.push_back(cells > 0 ? cos(th[cells]) : 0.0);
+}
+
+// approx_out_rel_marg2d_term_for_cpdf (cauchy_prediction.hpp:445-470)
+static bool rel2d_negligible(const Cpdf2DTerm& c, double norm_fact, double eps)
+{
+    double total = 0;
+    for (int i = 0; i < c.m; i++) {
+        const double a1 = c.g1r[i], a2 = c.g2r[i];
+        const double c1 = c.cos_t[i], s1 = c.sin_t[i], c2 = c.cos_t[i + 1], s2 = c.sin_t[i + 1];
+        const double den1 = a1 * (a1 * c1 + a2 * s1);
+        const double den2 = a1 * (a1 * c2 + a2 * s2);
+        if (fabs(den1) < 1e-14) return false;
+        if (fabs(den2) < 1e-14) return false;
+        const double gr = hypot(__real__ c.g[i], __imag__ c.g[i]);
+        total += fabs((gr * s2) / den2) + fabs((gr * s1) / den1);
+    }
+    total *= (2 * norm_fact);
+    return fabs(total) < eps;
+}
+
 extern "C" {
 
 void* orc_create(const double* A0, const double* p0, const double* b0, int steps, int d, int cmcc, int pncc,
@@ -1797,6 +2004,136 @@ int orc_cpdf_2d_grid(void* h, int i1, int i2, const double* bar_nu, double lx, d
         }
     }
     if (reset_cache) E.cpdf2d_step = E.cpdf2d_m1 = E.cpdf2d_m2 = -1;
+    return err ? -6 : nx * ny;
+}
+
+
+// get_marg2d_relative_and_transformed_cpdf (cauchy_prediction.hpp:653-971),
+// single-thread order.  bar_nu_full[d] is the point the reference draws
+// (2 u - 1, u = random_uniform_open()).  mom[14] receives the relative
+// moments finalised (fz re/im, mean 2 x re/im, covariance 4 x re/im) when
+// get_moments; counts[2] the pairs and the pairs approximated out.  *status:
+// 0, -1 before the first step, -5 at the last step of either estimator,
+// -3 dimension mismatch or too many rows.
+void* orc_rel2d_create(void* hp, void* hs, const double* Trel, const double* bar_nu_full, int full_solve,
+                       int get_moments, int with_term_approx, double term_approx_eps, double* mom, long long* counts,
+                       int* status)
+{
+    Estimator& P = *(Estimator*)hp;
+    Estimator& S = *(Estimator*)hs;
+    *status = 0;
+    if (P.d != S.d) {
+        *status = -3;
+        return nullptr;
+    }
+    if (P.master_step < 1 || S.master_step < 1) {
+        *status = -1;
+        return nullptr;
+    }
+    if (P.master_step >= P.num_steps || S.master_step >= S.num_steps) {
+        *status = -5;
+        return nullptr;
+    }
+    const int d = P.d;
+    if ((P.shape_range - 1) + (S.shape_range - 1) >= 32) {
+        *status = -3;
+        return nullptr;
+    }
+    const double nf = kTwoPiInv * kTwoPiInv / __real__ P.fz / __real__ S.fz;
+    double bar_nu[2];
+    for (int i = 0; i < 2; i++) {
+        double s = 0.0;
+        for (int j = 0; j < d; j++) s += Trel[i * d + j] * bar_nu_full[j];
+        bar_nu[i] = s;
+    }
+    // terms by shape, in order
+    std::vector<std::vector<const Term*>> bp(P.shape_range), bs(S.shape_range);
+    for (const Term& t : P.terms) bp[t.m].push_back(&t);
+    for (const Term& t : S.terms) bs[t.m].push_back(&t);
+    RelSys* R = new RelSys();
+    R->full = full_solve ? 1 : 0;
+    cplx acc[7];
+    for (int i = 0; i < 7; i++) acc[i] = mkc(0, 0);
+    for (int mp = 1; mp < P.shape_range; mp++)
+        for (int ms = 1; ms < S.shape_range; ms++)
+            for (const Term* tp : bp[mp])
+                for (const Term* ts : bs[ms]) {
+                    Cpdf2DTerm c;
+                    rel2d_pair(*tp, *ts, d, Trel, bar_nu_full, bar_nu, R->full, get_moments ? acc : nullptr, c);
+                    R->total++;
+                    if (with_term_approx && rel2d_negligible(c, nf, term_approx_eps)) {
+                        R->approxed_out++;
+                        continue;
+                    }
+                    R->terms.push_back(std::move(c));
+                }
+    if (get_moments) {
+        // finalize_rel_sys_moments (cauchy_prediction.hpp:288-303)
+        const cplx fz = acc[0];
+        const cplx ifz = mkc(0, __real__ fz);
+        cplx mean[2], cov[4];
+        for (int i = 0; i < 2; i++) mean[i] = cdiv(acc[1 + i], ifz);
+        for (int i = 0; i < 2; i++)
+            for (int j = 0; j < 2; j++) cov[i * 2 + j] = cdiv(acc[3 + i * 2 + j], fz) - mean[i] * mean[j];
+        mom[0] = __real__ fz;
+        mom[1] = __imag__ fz;
+        for (int i = 0; i < 2; i++) {
+            mom[2 + 2 * i] = __real__ mean[i];
+            mom[3 + 2 * i] = __imag__ mean[i];
+        }
+        for (int i = 0; i < 4; i++) {
+            mom[6 + 2 * i] = __real__ cov[i];
+            mom[7 + 2 * i] = __imag__ cov[i];
+        }
+    }
+    counts[0] = R->total;
+    counts[1] = R->approxed_out;
+    return R;
+}
+
+void orc_rel2d_destroy(void* r) { delete (RelSys*)r; }
+
+// grid_eval_marg2d_relative_and_transformed_cpdf (cauchy_prediction.hpp:1091-1186)
+// with eval_marg2d_relative_and_transformed_cpdf (:1062-1073): x outermost,
+// point (i, j) at i * ny + j.  Returns the point count, -2 if it exceeds
+// max_points, -3 for a grid of fewer than two points per axis, -6 on the
+// reference's singular-cell exit.
+int orc_rel2d_grid(void* r, double xlow, double xhigh, double dx, double ylow, double yhigh, double dy,
+                   double nf_prim, double nf_sec, int max_points, double* xs, double* ys, double* zs)
+{
+    RelSys& R = *(RelSys*)r;
+    if (!(xhigh > xlow) || !(yhigh > ylow)) return -3;
+    const int nx = (int)ceil((xhigh - xlow) / dx + 1), ny = (int)ceil((yhigh - ylow) / dy + 1);
+    if (nx <= 1 || ny <= 1) return -3;
+    if ((long long)nx * ny > max_points) return -2;
+    int err = 0;
+    for (int i = 0; i < nx; i++) {
+        const double x = i == nx - 1 ? xhigh : xlow + dx * i;
+        for (int j = 0; j < ny; j++) {
+            const double y = j == ny - 1 ? yhigh : ylow + dy * j;
+            double fx = 0;
+            for (const Cpdf2DTerm& c : R.terms) {
+                const double g1i = c.b[0] - x, g2i = c.b[1] - y;
+                const bool check = fabs(g1i) < kIntegralGammaEps;
+                double t = 0;
+                const int cells = c.m * (1 + R.full);
+                for (int k = 0; k < cells; k++) {
+                    double v;
+                    if (!marg2d_cell(c.sin_t[k], c.cos_t[k], c.sin_t[k + 1], c.cos_t[k + 1], c.g1r[k], g1i, c.g2r[k],
+                                     g2i, check, c.g[k], &v)) {
+                        err = 1;
+                        v = 0;
+                    }
+                    t += v;
+                }
+                fx += t;
+            }
+            const int q = i * ny + j;
+            xs[q] = x;
+            ys[q] = y;
+            zs[q] = ((double)(2 - R.full)) * fx * kTwoPiInv * kTwoPiInv / (nf_prim * nf_sec);
+        }
+    }
     return err ? -6 : nx * ny;
 }
 

@@ -65,6 +65,7 @@ static int harness_covariance_checker(C_COMPLEX_TYPE* cov, const int d, const in
 
 #include "cauchy_estimator.hpp"
 #include "cpdf_ndim.hpp"
+#include "cauchy_prediction.hpp"
 
 struct RefHandle {
     CauchyEstimator* est;
@@ -263,6 +264,70 @@ int ref_cpdf_1d_grid(void* vh, int marg, double low, double high, double res, in
         ys[i] = grid.points[i].y;
     }
     return grid.num_grid_points;
+}
+
+
+// Relative-then-transformed system of two estimators through the reference's
+// own get_marg2d_relative_and_transformed_cpdf and
+// grid_eval_marg2d_relative_and_transformed_cpdf (include/cauchy_prediction.hpp),
+// single-thread creation (its term order).  With center, the grid is offset by
+// the relative mean as pycauchy_single_step_eval_2d_rsys_cpdf does
+// (scripts/swig/cauchy/pycauchy.hpp:672-747).  rand() is seeded with bar_seed
+// right before the call; bar_nu_full[d] receives the point it then draws.
+// mom[14]: fz, mean[2], cov[4] as re/im pairs; counts[2]: pairs, pairs
+// approximated out.  Returns the point count, -2 if it exceeds max_points,
+// -5 if the reference refuses.
+int ref_rel2d(void* vp, void* vs, const double* Trel, unsigned bar_seed, int full_solve, int with_term_approx,
+              double term_approx_eps, double xlow, double xhigh, double dx, double ylow, double yhigh, double dy,
+              int center, int max_points, double* bar_nu_full, double* mom, long long* counts, double* xs,
+              double* ys, double* zs)
+{
+    RefHandle* p = (RefHandle*)vp;
+    RefHandle* s = (RefHandle*)vs;
+    const int d = p->d;
+    srand(bar_seed);
+    for (int i = 0; i < d; i++) bar_nu_full[i] = 2 * random_uniform_open() - 1;
+    srand(bar_seed);
+    C_COMPLEX_TYPE fz[1], mean[2], cov[4];
+    Cached2DCPDFTermContainer* c = get_marg2d_relative_and_transformed_cpdf(
+        p->est, s->est, (double*)Trel, full_solve != 0, false, true, fz, mean, cov, with_term_approx != 0,
+        term_approx_eps, 1);
+    if (!c) return -5;
+    mom[0] = creal(fz[0]);
+    mom[1] = cimag(fz[0]);
+    for (int i = 0; i < 2; i++) {
+        mom[2 + 2 * i] = creal(mean[i]);
+        mom[3 + 2 * i] = cimag(mean[i]);
+    }
+    for (int i = 0; i < 4; i++) {
+        mom[6 + 2 * i] = creal(cov[i]);
+        mom[7 + 2 * i] = cimag(cov[i]);
+    }
+    const long long total = (long long)p->est->Nt * s->est->Nt;
+    counts[0] = total;
+    counts[1] = total - (long long)c->current_term_idx;
+    const double ox = center ? mom[2] : 0.0, oy = center ? mom[4] : 0.0;
+    const int nx = (int)ceil((xhigh - xlow) / dx + 1), ny = (int)ceil((yhigh - ylow) / dy + 1);
+    if ((long long)nx * ny > max_points) {
+        c->deinit();
+        free(c);
+        return -2;
+    }
+    int rx = 0, ry = 0;
+    // two threads: the single-thread grid path prints every point
+    CauchyPoint3D* pts = grid_eval_marg2d_relative_and_transformed_cpdf(
+        c, xlow + ox, xhigh + ox, dx, ylow + oy, yhigh + oy, dy, creal(p->est->fz), creal(s->est->fz), &rx, &ry, 2,
+        full_solve != 0, false);
+    const int n = rx * ry;
+    for (int i = 0; i < n; i++) {
+        xs[i] = pts[i].x;
+        ys[i] = pts[i].y;
+        zs[i] = pts[i].z;
+    }
+    free(pts);
+    c->deinit();
+    free(c);
+    return n;
 }
 
 }  // extern "C"
