@@ -7,13 +7,15 @@ terms per shape, the reported and raw moments, G_SCALE_FACTOR, and (for small
 steps) every term's shape, A, p, b and sorted g-table.
 
 It also records the reference's marginal 1-D pdf grids (cpdf1d_*.npz) after
-a few updates of some of the same problems, and the moments through a fixed
-sequence of updates and extended-mode calls (ext_*.npz).
+a few updates of some of the same problems, the moments through a fixed
+sequence of updates and extended-mode calls (ext_*.npz), and the
+relative-then-transformed 2-D system of two estimators (rel2d_*.npz).
 
 Needs the reference sources (only present where the fixtures are made):
     python tests/golden/make_golden.py          # everything
     python tests/golden/make_golden.py --cpdf   # the pdf fixtures only
     python tests/golden/make_golden.py --ext    # the extended-mode fixtures only
+    python tests/golden/make_golden.py --rel    # the relative-system fixtures only
 """
 import os
 import sys
@@ -198,6 +200,70 @@ def pack_ext(name, prob, seed):
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **arr)
 
 
+def rel2d_cases():
+    """(name, problem family, primary/secondary workload seeds, srand seeds,
+    updates, Trel rows, full solve, bar_nu seed)"""
+    return [
+        ("rel2d_three_state_lti", W.three_state_lti, (0, 1), (1, 5), 4, [[1, 0, 0], [0, 1, 0]], False, 71),
+        ("rel2d_two_state_lti_full", W.two_state_lti, (0, 1), (2, 6), 5, [[1, 0], [0, 1]], True, 72),
+        ("rel2d_four_state_lti", W.four_state_lti, (0, 1), (3, 7), 3, [[1, 0, 0.5, 0], [0, 1, 0, -0.25]], False,
+         73),
+        ("rel2d_five_state_two_msmt", W.five_state_two_msmt, (0, 1), (4, 8), 2,
+         [[1, 0, 0, 0, 0], [0, 0, 1, 0, 0]], False, 74),
+    ]
+
+
+def _prob_arrays(prefix, prob, seed, rp, bp):
+    out = {}
+    for k in ("d", "pncc", "cmcc", "p", "steps", "Phi", "Gamma", "beta", "H", "gamma", "A0", "p0", "b0", "msmts"):
+        out[prefix + k] = prob[k]
+    out[prefix + "srand_seed"] = seed
+    out[prefix + "root_point"] = rp
+    out[prefix + "b_pert"] = bp
+    return out
+
+
+def pack_rel2d(name, family, wseeds, seeds, updates, trel, full, bar_seed):
+    """The reference's relative-then-transformed system of two estimators of
+    the same family (get_marg2d_relative_and_transformed_cpdf, single-thread
+    term order) after `updates` updates of both: the relative moments, the
+    pair counts and the pdf grid centred on the relative mean, as
+    pycauchy_single_step_eval_2d_rsys_cpdf evaluates it (term approximation
+    on, eps 1e-8)."""
+    probs = [family(seed=ws, steps=6) for ws in wseeds]
+    refs, arr = [], {"updates": updates, "Trel": np.array(trel, dtype=float), "full": int(full),
+                     "bar_seed": bar_seed, "eps": 1e-8}
+    for pre, prob, seed in zip(("P_", "S_"), probs, seeds):
+        ref = oracle.Reference(prob, seed=seed)
+        rp, bp = ref.constants()
+        arr.update(_prob_arrays(pre, prob, seed, rp, bp))
+        n = 0
+        for k in range(prob["steps"]):
+            for s in range(prob["p"]):
+                if n < updates:
+                    ref.step(k, s)
+                    n += 1
+        refs.append(ref)
+    # a first call on a wide grid gives the relative covariance for the grid
+    wide = oracle.reference_rel2d(refs[0], refs[1], arr["Trel"], bar_seed, (-1.0, 1.0, 1.0), (-1.0, 1.0, 1.0),
+                                  full_solve=full)
+    sd = np.sqrt(np.abs(np.diag(wide["cov"].real)))
+    sd = np.where(np.isfinite(sd) & (sd > 1e-6), sd, 1.0)
+    gx, gy = (-3 * sd[0], 3 * sd[0], 6 * sd[0] / 16), (-3 * sd[1], 3 * sd[1], 6 * sd[1] / 16)
+    out = oracle.reference_rel2d(refs[0], refs[1], arr["Trel"], bar_seed, gx, gy, full_solve=full)
+    arr["grid"] = np.array(list(gx) + list(gy))
+    arr["bar_nu_full"] = out["bar_nu_full"]
+    arr["fz"] = np.array([out["fz"].real, out["fz"].imag])
+    arr["mean"] = out["mean"]
+    arr["cov"] = out["cov"]
+    arr["pairs"] = out["pairs"]
+    arr["approxed_out"] = out["approxed_out"]
+    arr["x"], arr["y"], arr["z"] = out["x"], out["y"], out["z"]
+    for r in refs:
+        r.close()
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **arr)
+
+
 def main():
     oracle.build()
     only = [a[2:] for a in sys.argv[1:] if a.startswith("--")]
@@ -217,6 +283,10 @@ def main():
         for name, prob, seed in ext_cases():
             pack_ext(name, prob, seed)
             print("wrote %s.npz" % name)
+    if not only or "rel" in only:
+        for c in rel2d_cases():
+            pack_rel2d(*c)
+            print("wrote %s.npz" % c[0])
 
 
 if __name__ == "__main__":

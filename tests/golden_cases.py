@@ -15,7 +15,7 @@ REL_TOL = 1e-9
 def names():
     """The step-record fixtures (the marginal pdf ones are cpdf_names())."""
     return sorted(n for n in (os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
-                  if not n.startswith(("cpdf1d_", "cpdf2d_", "ext_")))
+                  if not n.startswith(("cpdf1d_", "cpdf2d_", "ext_", "rel2d_")))
 
 
 def cpdf_names():
@@ -36,6 +36,29 @@ def load_cpdf(name):
             grids.append((marg, call, tuple(float(v) for v in z[pre + "grid"]), z[pre + "x"], z[pre + "y"]))
     return prob, (z["root_point"], z["b_pert"]), int(z["updates"]), z["bar_nu"], grids
 
+
+def rel2d_names():
+    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "rel2d_*.npz")))
+
+
+def load_rel2d(name):
+    """(primary problem, primary (root_point, b_pert), secondary problem, its
+    constants, updates, case dict: Trel, full, eps, grid, bar_nu_full and the
+    reference's fz, mean, cov, pairs, approxed_out, x, y, z)"""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    out = []
+    for pre in ("P_", "S_"):
+        prob = {k: z[pre + k] for k in ("Phi", "Gamma", "beta", "H", "gamma", "A0", "p0", "b0", "msmts")}
+        for k in ("d", "pncc", "cmcc", "p", "steps"):
+            prob[k] = int(z[pre + k])
+        prob["B"] = None
+        out += [prob, (z[pre + "root_point"], z[pre + "b_pert"])]
+    case = {k: z[k] for k in ("Trel", "grid", "bar_nu_full", "mean", "cov", "x", "y", "z")}
+    case["fz"] = complex(z["fz"][0], z["fz"][1])
+    for k in ("full", "pairs", "approxed_out"):
+        case[k] = int(z[k])
+    case["eps"] = float(z["eps"])
+    return out[0], out[1], out[2], out[3], int(z["updates"]), case
 
 def load(name):
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
