@@ -6,6 +6,6 @@ reached through the C ABI in include/mce_c_api.h.  This package holds the
 build recipe, the ctypes binding, the estimator mirrors and the seeded
 synthetic workloads.
 """
-from .estimator import BatchedCauchyEstimator, CauchyEstimator, max_shape  # noqa: F401
+from .estimator import BatchedCauchyEstimator, CauchyEstimator, RelativeSystem2D, max_shape  # noqa: F401
 
-__all__ = ["BatchedCauchyEstimator", "CauchyEstimator", "max_shape"]
+__all__ = ["BatchedCauchyEstimator", "CauchyEstimator", "RelativeSystem2D", "max_shape"]

@@ -34,6 +34,12 @@ SIGNATURES = {
     "mce_cpdf_2d_grid": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp] + [ctypes.c_double] * 6
                          + [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]),
     "mce_draw_bar_nu": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_int, _dp]),
+    "mce_rel2d_create": (_vp, [_vp, ctypes.c_int, _vp, ctypes.c_int, _dp, _dp, ctypes.c_int, ctypes.c_int,
+                               ctypes.c_double, _dp, _lp, _ip]),
+    "mce_rel2d_grid": (ctypes.c_int, [_vp] + [ctypes.c_double] * 8 + [ctypes.c_int, _dp, _dp, _dp]),
+    "mce_rel2d_num_pairs": (ctypes.c_longlong, [_vp]),
+    "mce_rel2d_num_terms": (ctypes.c_longlong, [_vp]),
+    "mce_rel2d_destroy": (None, [_vp]),
     "mce_batch_step_noalloc": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int, _ip]),
     "mce_batch_run": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int, _dp,
                                      _dp, _dp, _ip, _lp]),

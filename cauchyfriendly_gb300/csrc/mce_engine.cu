@@ -191,6 +191,20 @@ public:
                              int max_points, double* xs, double* ys) = 0;
     // waits for the work the engine queued (after a step that stopped early)
     virtual void drain() = 0;
+    // Estimator e's current terms for the relative system: the device lists,
+    // the term indices grouped by shape (ascending, positions in order) and
+    // the reported fz.  Refused before the first and after the last update.
+    struct TermsView {
+        ParentList P;
+        Tables T;
+        int MC = 0;
+        std::vector<long long> idx;
+        std::vector<int> shape_off, shape_cnt;  // per shape 0..MC
+        double fz = 0;
+    };
+    virtual int terms_view(int e, TermsView* v) = 0;
+    // launches the pair kernel of this engine's state dimension
+    virtual void rel2d_pairs(const Rel2DArgs& a, cudaStream_t st) = 0;
 
     int E = 0, d = 0, cmcc = 0, pncc = 0, p = 0, MC = 0;
     // When set (only by mce_batch_step_noalloc), the g-table kernel takes its
@@ -1281,6 +1295,51 @@ public:
         return npts;
     }
 
+    int terms_view(int e, TermsView* v) override
+    {
+        if (e < 0 || e >= E || !v) return MCE_ERR_ARG;
+        if (master_step < 1) {
+            set_error("relative system: the estimator has not been stepped");
+            return MCE_ERR_ARG;
+        }
+        if (master_step >= est[e].num_updates) {
+            set_error("relative system: the last step keeps no g-tables");
+            return MCE_ERR_DONE;
+        }
+        drain();
+        const long long a = hpstart[e], n = hpstart[e + 1] - a;
+        std::vector<int> hm((size_t)n + 1);
+        if (n > 0)
+            MCE_CUDA(cudaMemcpyAsync(hm.data(), Pb[cur].m.ptr + a, sizeof(int) * n, cudaMemcpyDeviceToHost,
+                                     lc.stream));
+        MCE_CUDA(cudaStreamSynchronize(lc.stream));
+        v->P = Pb[cur].view();
+        v->T = Tables{Tb[cur].keys.ptr, Tb[cur].vals.ptr};
+        v->MC = MC;
+        v->fz = est[e].fz[0];
+        v->shape_cnt.assign(MC + 1, 0);
+        v->shape_off.assign(MC + 2, 0);
+        for (long long i = 0; i < n; i++) {
+            if (hm[i] < 0 || hm[i] > MC) {
+                set_error("relative system: a term shape out of range");
+                return MCE_ERR_DEVICE;
+            }
+            v->shape_cnt[hm[i]]++;
+        }
+        for (int m = 0; m <= MC; m++) v->shape_off[m + 1] = v->shape_off[m] + v->shape_cnt[m];
+        v->idx.assign((size_t)n, 0);
+        std::vector<int> fill(MC + 1, 0);
+        for (long long i = 0; i < n; i++) v->idx[v->shape_off[hm[i]] + fill[hm[i]]++] = a + i;
+        return MCE_OK;
+    }
+
+    void rel2d_pairs(const Rel2DArgs& a, cudaStream_t st) override
+    {
+        LaunchCfg c = lc;
+        c.stream = st;
+        Kernels<D>::rel2d_pairs(a, c);
+    }
+
     // ---- marginal 1-D pdf: CauchyCPDFGridDispatcher1D (cpdf_ndim.hpp:2017-2139)
     // over PointWiseNDimCauchyCPDF::evaluate_1D_marginal_cpdf (:1233-1352),
     // with the reference's per-estimator cache of per-term constants, kept on
@@ -1606,6 +1665,198 @@ struct mce_handle {
     EngineBase* eng;
 };
 
+// Relative-then-transformed 2-D system of two estimators: the pair cache and
+// the buffers of its grid evaluations, on a stream of its own (either
+// estimator may be stepped or destroyed while it lives).
+struct mce_rel2d {
+    cudaStream_t stream = nullptr;
+    LaunchCfg lc{};
+    int full = 0, CC = 0;
+    long long npairs = 0, nkept = 0;
+    DevBuf<double> tt, mrows, mpart, mout, trel, nu, part, xs, ys, zs;
+    DevBuf<int> keep, bad;
+    DevBuf<long long> idxP, idxS;
+    DevBuf<Rel2DBlock> blk;
+    ~mce_rel2d()
+    {
+        if (stream) {
+            cudaStreamSynchronize(stream);
+            cudaStreamDestroy(stream);
+        }
+    }
+};
+
+namespace {
+
+// get_marg2d_relative_and_transformed_cpdf (cauchy_prediction.hpp:653-971)
+int rel2d_build(mce_rel2d* r, EngineBase& P, int ep, EngineBase& S, int es, const double* Trel,
+                const double* bar_nu_full, int full, int approx, double eps, double* moments, long long* counts)
+{
+    const int d = P.d;
+    if (S.d != d) {
+        set_error("relative system: the estimators' state dimensions differ");
+        return MCE_ERR_ARG;
+    }
+    if (P.est[ep].max_shape + S.est[es].max_shape > kMaxRows) {
+        set_error("relative system: the two estimators' hyperplanes exceed 31 (cauchy_prediction.hpp:695)");
+        return MCE_ERR_SHAPE;
+    }
+    EngineBase::TermsView vp, vs;
+    int s;
+    if ((s = P.terms_view(ep, &vp))) return s;
+    if ((s = S.terms_view(es, &vs))) return s;
+    int dev = 0;
+    MCE_CUDA(cudaGetDevice(&dev));
+    MCE_CUDA(cudaDeviceGetAttribute(&r->lc.num_sms, cudaDevAttrMultiProcessorCount, dev));
+    MCE_CUDA(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking));
+    r->lc.stream = r->stream;
+    r->full = full ? 1 : 0;
+    r->CC = (P.est[ep].max_shape + S.est[es].max_shape) * (1 + r->full);
+    // pair blocks: primary shape, secondary shape (cauchy_prediction.hpp:789-800)
+    std::vector<Rel2DBlock> blks;
+    long long off = 0;
+    for (int mp = 1; mp <= vp.MC; mp++)
+        for (int ms = 1; ms <= vs.MC; ms++) {
+            if (!vp.shape_cnt[mp] || !vs.shape_cnt[ms]) continue;
+            blks.push_back(Rel2DBlock{off, vp.shape_off[mp], vp.shape_cnt[mp], vs.shape_off[ms], vs.shape_cnt[ms]});
+            off += (long long)vp.shape_cnt[mp] * vs.shape_cnt[ms];
+        }
+    r->npairs = off;
+    const int RT = rel2d_stride(r->CC);
+    const bool mom = moments != nullptr;
+    if ((s = r->tt.ensure((size_t)(off + 1) * RT))) return s;
+    if ((s = r->keep.ensure(off + 1))) return s;
+    if (mom && (s = r->mrows.ensure((size_t)(off + 1) * 14))) return s;
+    if ((s = r->idxP.ensure(vp.idx.size() + 1))) return s;
+    if ((s = r->idxS.ensure(vs.idx.size() + 1))) return s;
+    if ((s = r->blk.ensure(blks.size() + 1))) return s;
+    if ((s = r->trel.ensure(2 * d))) return s;
+    if ((s = r->nu.ensure(d))) return s;
+    cudaStream_t st = r->stream;
+    if (!vp.idx.empty())
+        MCE_CUDA(cudaMemcpyAsync(r->idxP.ptr, vp.idx.data(), sizeof(long long) * vp.idx.size(), cudaMemcpyHostToDevice,
+                                 st));
+    if (!vs.idx.empty())
+        MCE_CUDA(cudaMemcpyAsync(r->idxS.ptr, vs.idx.data(), sizeof(long long) * vs.idx.size(), cudaMemcpyHostToDevice,
+                                 st));
+    if (!blks.empty())
+        MCE_CUDA(cudaMemcpyAsync(r->blk.ptr, blks.data(), sizeof(Rel2DBlock) * blks.size(), cudaMemcpyHostToDevice,
+                                 st));
+    MCE_CUDA(cudaMemcpyAsync(r->trel.ptr, Trel, sizeof(double) * 2 * d, cudaMemcpyHostToDevice, st));
+    MCE_CUDA(cudaMemcpyAsync(r->nu.ptr, bar_nu_full, sizeof(double) * d, cudaMemcpyHostToDevice, st));
+    Rel2DArgs a;
+    a.P = vp.P;
+    a.S = vs.P;
+    a.TP = vp.T;
+    a.TS = vs.T;
+    a.MCp = vp.MC;
+    a.MCs = vs.MC;
+    a.idxP = r->idxP.ptr;
+    a.idxS = r->idxS.ptr;
+    a.blk = r->blk.ptr;
+    a.nblk = (int)blks.size();
+    a.npairs = off;
+    a.Trel = r->trel.ptr;
+    a.nu_full = r->nu.ptr;
+    a.full = r->full;
+    a.approx = approx ? 1 : 0;
+    a.moments = mom ? 1 : 0;
+    a.eps = eps;
+    // approx_norm_factor (cauchy_prediction.hpp:679)
+    a.approx_nf = kTwoPiInv * kTwoPiInv / vp.fz / vs.fz;
+    a.CC = r->CC;
+    a.tt = r->tt.ptr;
+    a.keep = r->keep.ptr;
+    a.mrows = mom ? r->mrows.ptr : nullptr;
+    P.rel2d_pairs(a, st);
+    MCE_CUDA(cudaGetLastError());
+    if (mom) {
+        const long long chunk = 65536;
+        const long long nch = (off + chunk - 1) / chunk;
+        if ((s = r->mpart.ensure((size_t)(nch + 1) * 14))) return s;
+        if ((s = r->mout.ensure(14))) return s;
+        rel2d_moments(r->mrows.ptr, off, chunk, r->mpart.ptr, r->mout.ptr, r->lc);
+        MCE_CUDA(cudaGetLastError());
+        MCE_CUDA(cudaMemcpyAsync(moments, r->mout.ptr, sizeof(double) * 14, cudaMemcpyDeviceToHost, st));
+    }
+    std::vector<int> hk((size_t)off + 1);
+    if (off > 0) MCE_CUDA(cudaMemcpyAsync(hk.data(), r->keep.ptr, sizeof(int) * off, cudaMemcpyDeviceToHost, st));
+    MCE_CUDA(cudaStreamSynchronize(st));
+    long long kept = 0;
+    for (long long i = 0; i < off; i++) kept += hk[i] != 0;
+    r->nkept = kept;
+    if (counts) {
+        counts[0] = off;
+        counts[1] = off - kept;
+    }
+    return MCE_OK;
+}
+
+// grid_eval_marg2d_relative_and_transformed_cpdf (cauchy_prediction.hpp:1091-1186)
+int rel2d_grid(mce_rel2d* r, double xlow, double xhigh, double dx, double ylow, double yhigh, double dy,
+               double nf_prim, double nf_sec, int max_points, double* x, double* y, double* z)
+{
+    if (!(xhigh > xlow) || !(yhigh > ylow) || !(dx > 0) || !(dy > 0)) return MCE_ERR_ARG;
+    const double sx = ceil((xhigh - xlow) / dx + 1), sy = ceil((yhigh - ylow) / dy + 1);
+    if (!(sx < 1e8) || !(sy < 1e8) || sx * sy > 1e8) {
+        set_error("relative pdf grid: too many points");
+        return MCE_ERR_ARG;
+    }
+    const int nx = (int)sx, ny = (int)sy;
+    if (nx <= 1 || ny <= 1) {
+        set_error("relative pdf grid: fewer than two points on an axis");
+        return MCE_ERR_ARG;
+    }
+    const int npts = nx * ny;
+    if (!x || !y || !z) return npts;
+    if (npts > max_points) {
+        set_error("relative pdf grid: " + std::to_string(npts) + " points do not fit in " +
+                  std::to_string(max_points));
+        return MCE_ERR_ARG;
+    }
+    for (int i = 0; i < nx; i++) {
+        const double xv = i == nx - 1 ? xhigh : xlow + dx * i;
+        for (int j = 0; j < ny; j++) {
+            x[i * ny + j] = xv;
+            y[i * ny + j] = j == ny - 1 ? yhigh : ylow + dy * j;
+        }
+    }
+    // enough (point, chunk) threads to fill the GPU; one chunk keeps the
+    // reference's summation order exactly
+    long long nch = (80000 + npts - 1) / npts;
+    const long long maxch = (r->npairs + 255) / 256;
+    if (nch > maxch) nch = maxch;
+    if (nch < 1) nch = 1;
+    if (nch > 65535) nch = 65535;
+    long long chunk = r->npairs > 0 ? (r->npairs + nch - 1) / nch : 1;
+    nch = r->npairs > 0 ? (r->npairs + chunk - 1) / chunk : 1;
+    int s;
+    if ((s = r->xs.ensure(npts))) return s;
+    if ((s = r->ys.ensure(npts))) return s;
+    if ((s = r->zs.ensure(npts))) return s;
+    if ((s = r->part.ensure((size_t)nch * npts))) return s;
+    if ((s = r->bad.ensure(1))) return s;
+    cudaStream_t st = r->stream;
+    MCE_CUDA(cudaMemcpyAsync(r->xs.ptr, x, sizeof(double) * npts, cudaMemcpyHostToDevice, st));
+    MCE_CUDA(cudaMemcpyAsync(r->ys.ptr, y, sizeof(double) * npts, cudaMemcpyHostToDevice, st));
+    MCE_CUDA(cudaMemsetAsync(r->bad.ptr, 0, sizeof(int), st));
+    rel2d_points(r->tt.ptr, r->keep.ptr, r->npairs, r->CC, r->full, chunk, (int)nch, r->xs.ptr, r->ys.ptr, npts,
+                 r->part.ptr, r->bad.ptr, r->lc);
+    rel2d_finish(r->part.ptr, (int)nch, npts, r->full, nf_prim, nf_sec, r->zs.ptr, r->lc);
+    MCE_CUDA(cudaGetLastError());
+    int bad = 0;
+    MCE_CUDA(cudaMemcpyAsync(z, r->zs.ptr, sizeof(double) * npts, cudaMemcpyDeviceToHost, st));
+    MCE_CUDA(cudaMemcpyAsync(&bad, r->bad.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MCE_CUDA(cudaStreamSynchronize(st));
+    if (bad) {
+        set_error("relative pdf: a cell with gamma1 = gamma2 = 0 (the reference exits here)");
+        return MCE_ERR_DEVICE;
+    }
+    return npts;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char* mce_last_error(void) { return g_last_error.c_str(); }
@@ -1861,6 +2112,33 @@ int mce_draw_bar_nu(long long seed, int d, double* bar_nu)
     for (int i = 0; i < d; i++) bar_nu[i] = 2 * (((double)rand() + 1.0) / ((double)RAND_MAX + 2.0));
     return MCE_OK;
 }
+mce_rel2d* mce_rel2d_create(mce_handle* primary, int est_p, mce_handle* secondary, int est_s, const double* Trel,
+                            const double* bar_nu_full, int full_solve, int with_term_approx, double term_approx_eps,
+                            double* moments, long long* counts, int* status)
+{
+    int s = MCE_ERR_ARG;
+    mce_rel2d* r = nullptr;
+    if (!bad(primary, est_p) && !bad(secondary, est_s) && Trel && bar_nu_full) {
+        r = new mce_rel2d();
+        s = rel2d_build(r, *primary->eng, est_p, *secondary->eng, est_s, Trel, bar_nu_full, full_solve,
+                        with_term_approx, term_approx_eps, moments, counts);
+        if (s != MCE_OK) {
+            delete r;
+            r = nullptr;
+        }
+    }
+    if (status) *status = s;
+    return r;
+}
+int mce_rel2d_grid(mce_rel2d* r, double xlow, double xhigh, double dx, double ylow, double yhigh, double dy,
+                   double norm_factor_prim, double norm_factor_sec, int max_points, double* x, double* y, double* z)
+{
+    if (!r) return MCE_ERR_ARG;
+    return rel2d_grid(r, xlow, xhigh, dx, ylow, yhigh, dy, norm_factor_prim, norm_factor_sec, max_points, x, y, z);
+}
+long long mce_rel2d_num_pairs(mce_rel2d* r) { return r ? r->npairs : MCE_ERR_ARG; }
+long long mce_rel2d_num_terms(mce_rel2d* r) { return r ? r->nkept : MCE_ERR_ARG; }
+void mce_rel2d_destroy(mce_rel2d* r) { delete r; }
 long long mce_post_mu_terms(mce_handle* h) { return h ? h->eng->post_mu_terms : MCE_ERR_ARG; }
 int mce_master_step(mce_handle* h) { return h ? h->eng->master_step : MCE_ERR_ARG; }
 int mce_device_errors(mce_handle* h) { return h ? h->eng->device_errors : MCE_ERR_ARG; }

@@ -2426,6 +2426,269 @@ void Kernels<D>::cpdf2d_terms(ParentList P, long long a, long long n, int i1, in
     k_cpdf2d_terms<D><<<grid_for(n, 128, c.num_sms, 16), 128, 0, c.stream>>>(P, a, n, i1, i2, bar_nu, T, MC, tt);
 }
 
+// ---------------------------------------------------------------------------
+// Relative-then-transformed 2-D system (cauchy_prediction.hpp), a thread per
+// (primary term, secondary term) pair:
+//   A_rel = [-A_prim; A_sec], p_rel = [p_prim; p_sec], b_rel = b_sec - b_prim
+//   (:573-584); A_2d = A_rel Trel^T, b_2d = Trel b_rel (:587-588);
+//   marg2d_remove_zeros_and_coalign (cpdf_ndim.hpp:42-138);
+//   eval_rel_sys_moments_for_term (:207-285) on the normalised rows;
+//   cache_rel_marg2d_term_for_cpdf (:306-443): the 2m sorted cell-wall angles,
+//   per cell the sign vector at its mid angle (flipped for the second half of
+//   a full solve), the product of the two parent-table values and the real
+//   parts of gamma1, gamma2;
+//   approx_out_rel_marg2d_term_for_cpdf (:445-470).
+// Zero rows (both projected components below MU_EPS) take the sign of the
+// full-dimensional row against bar_nu_full.
+template <int D>
+__global__ void __launch_bounds__(128) k_rel2d_pairs(Rel2DArgs a)
+{
+    const int RT = rel2d_stride(a.CC);
+    for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < a.npairs;
+         x += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = a.nblk;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (a.blk[mid].off <= x) lo = mid;
+            else hi = mid;
+        }
+        const Rel2DBlock B = a.blk[lo];
+        const long long loc = x - B.off;
+        const long long tp = loc / B.sc;
+        const long long ts = loc - tp * B.sc;
+        const long long ip = a.idxP[B.po + tp], is = a.idxS[B.so + ts];
+        const int mp = a.P.m[ip], ms = a.S.m[is], mps = mp + ms;
+        if (mp < 1 || ms < 1 || mps > kMaxRows || mps * (1 + a.full) > a.CC) {
+            // cannot happen for terms within their estimators' max shapes
+            // (the host checks those); an empty, dropped term keeps it in bounds
+            a.tt[x * RT] = 0;
+            a.keep[x] = 0;
+            if (a.moments)
+                for (int k = 0; k < 14; k++) a.mrows[x * 14 + k] = 0;
+            continue;
+        }
+        const double* Ap = a.P.A + ip * a.MCp * D;
+        const double* As = a.S.A + is * a.MCs * D;
+        double b2[2];
+        {
+            double br[D];
+            for (int i = 0; i < D; i++) br[i] = a.S.b[is * D + i] - a.P.b[ip * D + i];
+            for (int r = 0; r < 2; r++) {
+                double s = 0.0;
+                for (int j = 0; j < D; j++) s += a.Trel[r * D + j] * br[j];
+                b2[r] = s;
+            }
+        }
+        double A2[2 * kMaxRows], pr[kMaxRows], Ac[2 * kMaxRows], pc[kMaxRows];
+        signed char cmap[kMaxRows], csmap[kMaxRows], fidx[kMaxRows];
+        for (int i = 0; i < mps; i++) {
+            const double* row = i < mp ? Ap + i * D : As + (i - mp) * D;
+            const double sg = i < mp ? -1.0 : 1.0;
+            for (int j = 0; j < 2; j++) {
+                double s = 0.0;
+                for (int k = 0; k < D; k++) s += (row[k] * sg) * a.Trel[j * D + k];
+                A2[2 * i + j] = s;
+            }
+            pr[i] = i < mp ? a.P.p[ip * a.MCp + i] : a.S.p[is * a.MCs + (i - mp)];
+        }
+        // zero rows: normalisation skipped, sign from the full row
+        unsigned zmask = 0, zneg = 0, zpos = 0, F = 0;
+        for (int i = 0; i < mps; i++) {
+            const double f0 = fabs(A2[2 * i]), f1 = fabs(A2[2 * i + 1]);
+            if (f0 < kMuEps && f1 < kMuEps) {
+                cmap[i] = csmap[i] = fidx[i] = 32;
+                zmask |= 1u << i;
+                const double* row = i < mp ? Ap + i * D : As + (i - mp) * D;
+                const double sg = i < mp ? -1.0 : 1.0;
+                double v = 0.0;
+                for (int l = 0; l < D; l++) v += (row[l] * sg) * a.nu_full[l];
+                if (v < 0) zneg |= 1u << i;
+                if (v > 0) zpos |= 1u << i;
+                continue;
+            }
+            F |= 1u << i;
+            const double s = f0 + f1;
+            A2[2 * i] /= s;
+            A2[2 * i + 1] /= s;
+            pr[i] *= s;
+        }
+        int mn = 0;
+        for (int i = 0; i < mps; i++) {
+            if (!((F >> i) & 1u)) continue;
+            cmap[i] = (signed char)mn;
+            csmap[i] = 1;
+            fidx[i] = (signed char)i;
+            pc[mn] = pr[i];
+            for (int j = i + 1; j < mps; j++) {
+                if (!((F >> j) & 1u)) continue;
+                if (fabs(A2[2 * i] - A2[2 * j]) < kCoalignEps && fabs(A2[2 * i + 1] - A2[2 * j + 1]) < kCoalignEps) {
+                    cmap[j] = (signed char)mn;
+                    csmap[j] = 1;
+                    F &= ~(1u << j);
+                    fidx[j] = (signed char)i;
+                    pc[mn] += pr[j];
+                    continue;
+                }
+                if (fabs(A2[2 * i] + A2[2 * j]) < kCoalignEps && fabs(A2[2 * i + 1] + A2[2 * j + 1]) < kCoalignEps) {
+                    cmap[j] = (signed char)mn;
+                    csmap[j] = -1;
+                    F &= ~(1u << j);
+                    fidx[j] = (signed char)i;
+                    pc[mn] += pr[j];
+                }
+            }
+            mn++;
+        }
+        {
+            int u = 0;
+            for (int i = 0; i < mps; i++)
+                if (mn == mps || fidx[i] == i) {
+                    Ac[2 * u] = A2[2 * i];
+                    Ac[2 * u + 1] = A2[2 * i + 1];
+                    u++;
+                }
+        }
+        const int* kp = a.TP.keys + a.P.tab_off[ip];
+        const cd* vp = a.TP.vals + a.P.tab_off[ip];
+        const int np_ = a.P.tab_cnt[ip];
+        const int* ks = a.TS.keys + a.S.tab_off[is];
+        const cd* vs = a.TS.vals + a.S.tab_off[is];
+        const int ns_ = a.S.tab_cnt[is];
+        const int maskp = (1 << mp) - 1;
+        if (a.moments) {
+            double nu[2];
+            for (int r = 0; r < 2; r++) {
+                double s = 0.0;
+                for (int j = 0; j < D; j++) s += a.Trel[r * D + j] * a.nu_full[j];
+                nu[r] = s;
+            }
+            double ty0 = 0, ty1 = 0;
+            int enc = 0;
+            for (int i = 0; i < mps; i++) {
+                double v;
+                if ((zmask >> i) & 1u) v = ((zneg >> i) & 1u) ? -1.0 : (((zpos >> i) & 1u) ? 1.0 : 0.0);  // its sign
+                else v = A2[2 * i] * nu[0] + A2[2 * i + 1] * nu[1];
+                const double sgn = (double)((v > 0) - (v < 0));
+                const double sc = pr[i] * sgn;
+                ty0 += sc * A2[2 * i];
+                ty1 += sc * A2[2 * i + 1];
+                if (v < 0) enc |= 1 << i;
+            }
+            const cd g = cmul(lookup_num(kp, vp, np_, enc & maskp, mp), lookup_num(ks, vs, ns_, enc >> mp, ms));
+            const cd y[2] = {mkcd(-ty0, b2[0]), mkcd(-ty1, b2[1])};
+            double* mr = a.mrows + x * 14;
+            mr[0] = g.re;
+            mr[1] = g.im;
+            for (int j = 0; j < 2; j++) {
+                const cd gy = cmul(g, y[j]);
+                mr[2 + 2 * j] = gy.re;
+                mr[3 + 2 * j] = gy.im;
+                for (int k = 0; k < 2; k++) {
+                    const cd t = cmul(gy, y[k]);
+                    mr[6 + 2 * (2 * j + k)] = -t.re;
+                    mr[7 + 2 * (2 * j + k)] = -t.im;
+                }
+            }
+        }
+        double th[2 * kMaxRows + 1];
+        for (int r = 0; r < mn; r++) {
+            const double a0 = Ac[2 * r], a1 = Ac[2 * r + 1];
+            double pt0, pt1;
+            if (fabs(a0) < fabs(a1)) {
+                pt0 = 1;
+                pt1 = -a0 / a1;
+            } else {
+                pt0 = -a1 / a0;
+                pt1 = 1;
+            }
+            double t1 = atan2(pt1, pt0);
+            if (t1 < 0) t1 += kPi;
+            th[2 * r] = t1;
+            th[2 * r + 1] = t1 + kPi;
+        }
+        for (int u = 1; u < 2 * mn; u++) {  // ascending (the reference's qsort of distinct angles)
+            const double v = th[u];
+            int w = u - 1;
+            while (w >= 0 && th[w] > v) {
+                th[w + 1] = th[w];
+                w--;
+            }
+            th[w + 1] = v;
+        }
+        if (a.full && mn > 0) th[2 * mn] = th[0] + 2 * kPi;
+        const int cells = mn * (1 + a.full);
+        double* o = a.tt + x * RT;
+        double* os = o + 3;
+        double* oc = os + (a.CC + 1);
+        double* o1 = oc + (a.CC + 1);
+        double* o2 = o1 + a.CC;
+        double* og = o2 + a.CC;
+        o[0] = mn;
+        o[1] = b2[0];
+        o[2] = b2[1];
+        const unsigned allm = mn >= 32 ? 0xffffffffu : ((1u << mn) - 1u);
+        for (int c = 0; c < cells; c++) {
+            const int h = c < mn ? c : c - mn;
+            const double tm = (th[h + 1] + th[h]) / 2.0;
+            const double ct = cos(tm), st = sin(tm);
+            unsigned neg = 0;  // sv[j] = -1
+            for (int j = 0; j < mn; j++)
+                if (!(Ac[2 * j] * ct + Ac[2 * j + 1] * st > 0)) neg |= 1u << j;
+            if (c >= mn) neg ^= allm;
+            int enc = (int)zneg;
+            for (int j = 0; j < mps; j++) {
+                if ((zmask >> j) & 1u) continue;
+                const bool sneg = (neg >> cmap[j]) & 1u;
+                if (sneg != (csmap[j] < 0)) enc |= 1 << j;
+            }
+            const cd g = cmul(lookup_num(kp, vp, np_, enc & maskp, mp), lookup_num(ks, vs, ns_, enc >> mp, ms));
+            double g1r = 0, g2r = 0;
+            for (int j = 0; j < mn; j++) {
+                const double sv = ((neg >> j) & 1u) ? -1.0 : 1.0;
+                g1r -= (Ac[2 * j] * pc[j]) * sv;
+                g2r -= (Ac[2 * j + 1] * pc[j]) * sv;
+            }
+            os[c] = sin(th[c]);
+            oc[c] = cos(th[c]);
+            o1[c] = g1r;
+            o2[c] = g2r;
+            og[2 * c] = g.re;
+            og[2 * c + 1] = g.im;
+        }
+        os[cells] = cells > 0 ? sin(th[cells]) : 0.0;
+        oc[cells] = cells > 0 ? cos(th[cells]) : 0.0;
+        int keep = 1;
+        if (a.approx) {
+            double total = 0;
+            bool den_small = false;
+            for (int i = 0; i < mn; i++) {
+                const double a1 = o1[i], a2 = o2[i], c1 = oc[i], s1 = os[i], c2 = oc[i + 1], s2 = os[i + 1];
+                const double den1 = a1 * (a1 * c1 + a2 * s1);
+                const double den2 = a1 * (a1 * c2 + a2 * s2);
+                if (fabs(den1) < 1e-14 || fabs(den2) < 1e-14) {
+                    den_small = true;
+                    break;
+                }
+                const double gr = hypot(og[2 * i], og[2 * i + 1]);
+                total += fabs((gr * s2) / den2) + fabs((gr * s1) / den1);
+            }
+            if (!den_small) {
+                total *= (2 * a.approx_nf);
+                if (fabs(total) < a.eps) keep = 0;
+            }
+        }
+        a.keep[x] = keep;
+    }
+}
+
+template <int D>
+void Kernels<D>::rel2d_pairs(const Rel2DArgs& a, const LaunchCfg& c)
+{
+    if (a.npairs == 0) return;
+    ++g_launches;
+    k_rel2d_pairs<D><<<grid_for(a.npairs, 128, c.num_sms, 16), 128, 0, c.stream>>>(a);
+}
+
 #if MCE_COMMON_UNIT
 // One thread per point, the terms summed in order.  Points below `exact`
 // take the complex formula (fx * 1/(2 pi) / fz), the others the cached one
@@ -2536,6 +2799,123 @@ void cpdf1d_points(const double* tt, long long n, const double* xs, int npts, in
     if (npts <= 0) return;
     ++g_launches;
     k_cpdf1d_points<<<(npts + 63) / 64, 64, 0, c.stream>>>(tt, n, xs, npts, exact, fz, ys);
+}
+
+// Relative 2-D pdf (eval_marg2d_relative_and_transformed_cpdf,
+// cauchy_prediction.hpp:973-1073): a thread per (grid point, chunk of pairs),
+// the chunk's kept terms and their cells summed in order; the integral of a
+// cell is the marginal 2-D one.
+__global__ void k_rel2d_points(const double* tt, const int* keep, long long n, int CC, int full, long long chunk,
+                               const double* xs, const double* ys, int npts, double* part, int* bad)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= npts) return;
+    const long long j0 = (long long)blockIdx.y * chunk;
+    const long long j1 = j0 + chunk < n ? j0 + chunk : n;
+    const int RT = rel2d_stride(CC);
+    const double x1 = xs[q], x2 = ys[q];
+    double fx = 0;
+    int b = 0;
+    for (long long j = j0; j < j1; j++) {
+        if (!keep[j]) continue;
+        const double* o = tt + j * RT;
+        const int cells = (int)o[0] * (1 + full);
+        const double* os = o + 3;
+        const double* oc = os + (CC + 1);
+        const double* o1 = oc + (CC + 1);
+        const double* o2 = o1 + CC;
+        const double* og = o2 + CC;
+        const double g1i = o[1] - x1, g2i = o[2] - x2;
+        const bool check = fabs(g1i) < 1e-8;
+        double t = 0;
+        for (int c = 0; c < cells; c++)
+            t += marg2d_cell(os[c], oc[c], os[c + 1], oc[c + 1], o1[c], g1i, o2[c], g2i, check,
+                             mkcd(og[2 * c], og[2 * c + 1]), &b);
+        fx += t;
+    }
+    part[(long long)blockIdx.y * npts + q] = fx;
+    if (b) atomicOr(bad, 1);
+}
+
+__global__ void k_rel2d_finish(const double* part, int nch, int npts, int full, double nf_prim, double nf_sec,
+                               double* zs)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= npts) return;
+    double fx = 0;
+    for (int ch = 0; ch < nch; ch++) fx += part[(long long)ch * npts + q];
+    zs[q] = ((double)(2 - full)) * fx * kTwoPiInv * kTwoPiInv / (nf_prim * nf_sec);
+}
+
+void rel2d_points(const double* tt, const int* keep, long long n, int CC, int full, long long chunk, int nch,
+                  const double* xs, const double* ys, int npts, double* part, int* bad, const LaunchCfg& c)
+{
+    if (npts <= 0) return;
+    ++g_launches;
+    k_rel2d_points<<<dim3((npts + 63) / 64, nch), 64, 0, c.stream>>>(tt, keep, n, CC, full, chunk, xs, ys, npts,
+                                                                      part, bad);
+}
+
+void rel2d_finish(const double* part, int nch, int npts, int full, double nf_prim, double nf_sec, double* zs,
+                  const LaunchCfg& c)
+{
+    if (npts <= 0) return;
+    ++g_launches;
+    k_rel2d_finish<<<(npts + 127) / 128, 128, 0, c.stream>>>(part, nch, npts, full, nf_prim, nf_sec, zs);
+}
+
+// Relative moments: a thread per (chunk, column) sums its chunk of pairs in
+// order, then one thread per column sums the chunks in order and thread 0
+// applies finalize_rel_sys_moments (cauchy_prediction.hpp:288-303).
+__global__ void k_rel2d_msum(const double* mrows, long long n, long long chunk, int nch, double* part)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nch * 14) return;
+    const long long ch = t / 14;
+    const int col = (int)(t - ch * 14);
+    const long long j0 = ch * chunk, j1 = j0 + chunk < n ? j0 + chunk : n;
+    double acc = 0;
+    for (long long j = j0; j < j1; j++) acc += mrows[j * 14 + col];
+    part[ch * 14 + col] = acc;
+}
+
+__global__ void k_rel2d_mfinal(const double* part, int nch, double* out)
+{
+    __shared__ double s[14];
+    const int col = threadIdx.x;
+    if (col < 14) {
+        double acc = 0;
+        for (int ch = 0; ch < nch; ch++) acc += part[(long long)ch * 14 + col];
+        s[col] = acc;
+    }
+    __syncthreads();
+    if (col != 0) return;
+    const cd fz = mkcd(s[0], s[1]);
+    const cd ifz = mkcd(0, fz.re);
+    cd mean[2];
+    for (int i = 0; i < 2; i++) mean[i] = cdiv(mkcd(s[2 + 2 * i], s[3 + 2 * i]), ifz);
+    out[0] = fz.re;
+    out[1] = fz.im;
+    for (int i = 0; i < 2; i++) {
+        out[2 + 2 * i] = mean[i].re;
+        out[3 + 2 * i] = mean[i].im;
+    }
+    for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 2; j++) {
+            const int k = 2 * i + j;
+            const cd v = csub(cdiv(mkcd(s[6 + 2 * k], s[7 + 2 * k]), fz), cmul(mean[i], mean[j]));
+            out[6 + 2 * k] = v.re;
+            out[7 + 2 * k] = v.im;
+        }
+}
+
+void rel2d_moments(const double* mrows, long long n, long long chunk, double* part, double* out, const LaunchCfg& c)
+{
+    const long long nch = n > 0 ? (n + chunk - 1) / chunk : 0;
+    g_launches += 2;
+    if (nch > 0)
+        k_rel2d_msum<<<(unsigned)((nch * 14 + 127) / 128), 128, 0, c.stream>>>(mrows, n, chunk, (int)nch, part);
+    k_rel2d_mfinal<<<1, 32, 0, c.stream>>>(part, (int)nch, out);
 }
 #endif  // MCE_COMMON_UNIT
 

@@ -24,6 +24,38 @@ struct ScanScratch {
 // out[i] = sum_{k<i} in[k] for i in [0, n]; out[n] holds the total.
 void scan_int_to_ll(const int* in, long long* out, long long n, ScanScratch& s, const LaunchCfg& c);
 
+// Relative-then-transformed 2-D system of two estimators
+// (cauchy_prediction.hpp:306-971).  Pairs are numbered in the reference's
+// single-thread order: primary shape, secondary shape, primary term,
+// secondary term; a block is one (primary shape, secondary shape) pair.
+struct Rel2DBlock {
+    long long off;  // first pair of the block
+    int po, pc;     // primary terms of the shape: first slot in idxP, count
+    int so, sc;     // secondary terms of the shape: first slot in idxS, count
+};
+struct Rel2DArgs {
+    ParentList P, S;  // the two estimators' term lists
+    Tables TP, TS;
+    int MCp, MCs;
+    const long long* idxP;  // term indices of the primary, by shape then position
+    const long long* idxS;
+    const Rel2DBlock* blk;
+    int nblk;
+    long long npairs;
+    const double* Trel;     // 2 x D, row-major
+    const double* nu_full;  // D
+    int full;               // FULL_SOLVE: all 2m cells instead of m
+    int approx;             // with_term_approx
+    int moments;            // get_relative_moments
+    double eps, approx_nf;  // term_approx_eps; (1/2pi)^2 / fz_prim / fz_sec
+    int CC;                 // cells per cache row
+    double* tt;             // npairs x rel2d_stride(CC)
+    int* keep;              // npairs: 0 where the term was approximated out
+    double* mrows;          // npairs x 14: g, g y_j, -(g y_j y_k) as (re, im)
+};
+// doubles per cache row: m, b[2], sin[CC+1], cos[CC+1], gamma1 re[CC], gamma2 re[CC], g[CC] (re, im)
+__host__ __device__ inline int rel2d_stride(int CC) { return 6 * CC + 5; }
+
 template <int D>
 struct Kernels {
     // First measurement update (cauchy_estimator.hpp:1179-1208).
@@ -86,6 +118,9 @@ struct Kernels {
                             const long long* goff, const int* members, ParentList P, Tables Told, const int* Bkeys,
                             const double* gscale, const long long* toff, Tables Tnew, const GFlat& f, int MC,
                             const LaunchCfg& c);
+    // One relative 2-D term per (primary term, secondary term) pair: its
+    // cache row, kept flag and moment contributions.
+    static void rel2d_pairs(const Rel2DArgs& a, const LaunchCfg& c);
     // Next parent list (shape-bucketed, stable) from the surviving roots.
     static void compact(TermRecs R, const int* alive, const int* src, long long nR, const int* new_slot,
                         const long long* toff, const int* tcnt, ParentList Pn, int MC, const LaunchCfg& c);
@@ -101,6 +136,16 @@ void cpdf2d_points(const double* tt, long long n, int MC, const double* xs, cons
 // marginal 1-D pdf at npts points from the per-term records of k_cpdf1d_terms
 void cpdf1d_points(const double* tt, long long n, const double* xs, int npts, int exact, double fz, double* ys,
                    const LaunchCfg& c);
+// relative 2-D pdf at npts points from the pair cache rows (kept ones, in
+// order), the pairs split into nch chunks: part[nch x npts], then the chunk
+// sums in order scaled by (2 - full) (1/2pi)^2 / (nf_prim nf_sec)
+void rel2d_points(const double* tt, const int* keep, long long n, int CC, int full, long long chunk, int nch,
+                  const double* xs, const double* ys, int npts, double* part, int* bad, const LaunchCfg& c);
+void rel2d_finish(const double* part, int nch, int npts, int full, double nf_prim, double nf_sec, double* zs,
+                  const LaunchCfg& c);
+// relative moments: the 14 columns of mrows summed over the pairs in order
+// (chunks of `chunk` pairs, then the chunk sums), finalised into out[14]
+void rel2d_moments(const double* mrows, long long n, long long chunk, double* part, double* out, const LaunchCfg& c);
 void group_fill(const int* status, const int* owner, long long nR, const long long* goff, int* gfill,
                 int* members, const LaunchCfg& c);
 void group_sort(const int* gcnt, const long long* goff, long long nR, const int* members_in, int* members_out,

@@ -226,6 +226,87 @@ def draw_bar_nu(d, seed=-1):
     return out
 
 
+
+def draw_rel_bar_nu(d, seed=-1):
+    """The d draws of get_marg2d_relative_and_transformed_cpdf
+    (include/cauchy_prediction.hpp:697-698): 2 u - 1 with u from libc rand()
+    as random_uniform_open; seed >= 0 seeds it first."""
+    return draw_bar_nu(d, seed) - 1.0
+
+
+class RelativeSystem2D:
+    """The relative-then-transformed 2-D system of two estimators: rel =
+    secondary - primary projected by the 2 x d matrix Trel, one cached 2-D
+    term per (primary term, secondary term) pair, on the GPU
+    (get_marg2d_relative_and_transformed_cpdf,
+    include/cauchy_prediction.hpp:653-971, single-thread term order).
+
+    primary / secondary: (BatchedCauchyEstimator, index) pairs or
+    CauchyEstimator objects.  bar_nu_full defaults to the reference's own
+    rand() draw.  After construction: moments (fz, mean, cov, complex, when
+    get_relative_moments), pairs, terms (kept) and approxed_out; grid()
+    evaluates the pdf."""
+
+    def __init__(self, primary, secondary, Trel, full_solve=False, get_relative_moments=True,
+                 with_term_approx=False, term_approx_eps=1e-8, bar_nu_full=None):
+        (pe, pi), (se, si) = (self._split(primary), self._split(secondary))
+        self._lib = _lib.load()
+        d = pe.d
+        self.full_solve = bool(full_solve)
+        T = _f64(Trel).reshape(2, d)
+        nu = draw_rel_bar_nu(d) if bar_nu_full is None else _f64(bar_nu_full).reshape(d)
+        self.bar_nu_full = nu.copy()
+        mom = np.zeros(14) if get_relative_moments else None
+        counts = np.zeros(2, dtype=np.int64)
+        st = ctypes.c_int(0)
+        self._h = self._lib.mce_rel2d_create(pe._h, int(pi), se._h, int(si), _p(T), _p(nu), int(self.full_solve),
+                                             int(bool(with_term_approx)), float(term_approx_eps), _p(mom),
+                                             counts.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
+                                             ctypes.byref(st))
+        if not self._h:
+            _lib.check(st.value if st.value < 0 else -1, "mce_rel2d_create")
+        self.pairs, self.approxed_out = int(counts[0]), int(counts[1])
+        self.terms = self.pairs - self.approxed_out
+        self.moments = None
+        if mom is not None:
+            c = mom[0::2] + 1j * mom[1::2]
+            self.moments = {"fz": c[0], "mean": c[1:3], "cov": c[3:7].reshape(2, 2)}
+        # norm factors the reference passes to the grid: the reported fz of each
+        self.norm_factor_prim = float(pe.moments(pi)["fz"].real)
+        self.norm_factor_sec = float(se.moments(si)["fz"].real)
+
+    @staticmethod
+    def _split(x):
+        if isinstance(x, tuple):
+            return x[0], int(x[1])
+        return x, 0
+
+    def grid(self, xlow, xhigh, delta_x, ylow, yhigh, delta_y, norm_factor_prim=None, norm_factor_sec=None):
+        """grid_eval_marg2d_relative_and_transformed_cpdf
+        (include/cauchy_prediction.hpp:1091-1186): flat (X, Y, Z), x outermost,
+        and the point counts nx, ny."""
+        nfp = self.norm_factor_prim if norm_factor_prim is None else float(norm_factor_prim)
+        nfs = self.norm_factor_sec if norm_factor_sec is None else float(norm_factor_sec)
+        g = [float(v) for v in (xlow, xhigh, delta_x, ylow, yhigh, delta_y)]
+        n = self._lib.mce_rel2d_grid(self._h, *g, nfp, nfs, 0, None, None, None)
+        _lib.check(n, "mce_rel2d_grid")
+        X, Y, Z = np.zeros(n), np.zeros(n), np.zeros(n)
+        n = self._lib.mce_rel2d_grid(self._h, *g, nfp, nfs, n, _p(X), _p(Y), _p(Z))
+        _lib.check(n, "mce_rel2d_grid")
+        ny = int(np.ceil((g[4] - g[3]) / g[5] + 1))
+        return X, Y, Z, n // ny, ny
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.mce_rel2d_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
 class CauchyEstimator(BatchedCauchyEstimator):
     """CauchyEstimator(A0, p0, b0, steps, d, cmcc, pncc, p, print_basic_info)
     (include/cauchy_estimator.hpp:87): a batch of one."""

@@ -261,6 +261,34 @@ def pycauchy_get_2D_pointwise_cpdf(h, gridx_low, gridx_high, gridx_resolution, g
                                                    gridy_high, gridy_resolution, log_dir, reset_cache)
 
 
+def pycauchy_single_step_eval_2d_rsys_cpdf(Trel, s_pcdh, p_pcdh, RSYS_APPROX_EPS, xlow, xhigh, delta_x, ylow, yhigh,
+                                           delta_y):
+    """pycauchy.hpp:672-747: the relative system secondary - primary projected
+    by Trel (2 x n, flattened), term approximation at RSYS_APPROX_EPS, its
+    moments and its pdf on the grid offset by the relative mean.  Returns
+    (fz[1], xhat[2], Phat[4], cerr_fz[1], cerr_xhat[2], cerr_Phat[4],
+    cpdf points as flattened (x, y, z) triples, num_gridx, num_gridy).  The
+    terms are taken in the reference's single-thread order."""
+    from .estimator import RelativeSystem2D
+    n = p_pcdh.n
+    rs = RelativeSystem2D(p_pcdh.est, s_pcdh.est, np.asarray(Trel, dtype=np.float64).reshape(2, n),
+                          full_solve=False, get_relative_moments=True, with_term_approx=True,
+                          term_approx_eps=float(RSYS_APPROX_EPS))
+    try:
+        m = rs.moments
+        fz = np.array([m["fz"].real])
+        cerr_fz = np.array([m["fz"].imag])
+        xhat, cerr_xhat = m["mean"].real.copy(), m["mean"].imag.copy()
+        Phat, cerr_Phat = m["cov"].real.reshape(-1).copy(), m["cov"].imag.reshape(-1).copy()
+        X, Y, Z, nx, ny = rs.grid(xlow + xhat[0], xhigh + xhat[0], delta_x, ylow + xhat[1], yhigh + xhat[1],
+                                  delta_y)
+    finally:
+        rs.close()
+    pts = np.empty(3 * X.size)
+    pts[0::3], pts[1::3], pts[2::3] = X, Y, Z
+    return fz, xhat, Phat, cerr_fz, cerr_xhat, cerr_Phat, pts, nx, ny
+
+
 def pycauchy_get_marginal_1D_pointwise_cpdf(h, marg_idx1, gridx_low, gridx_high, gridx_resolution, log_dir=None):
     """pycauchy.hpp:890-931: the grid as (x, y) pairs, flattened, and its size.
     The pdf object (and its rand() draws) is made on the first call."""

@@ -166,6 +166,46 @@ int mce_cpdf_2d_grid(mce_handle* h, int est, int marg_idx1, int marg_idx2, const
  * for i < d.  seed >= 0 calls srand(seed) first. */
 int mce_draw_bar_nu(long long seed, int d, double* bar_nu);
 
+/* Relative-then-transformed 2-D system of two estimators, rel = secondary -
+ * primary projected by the 2 x d matrix Trel (row-major): one cached 2-D term
+ * per (primary term, secondary term) pair.  Replaces
+ * get_marg2d_relative_and_transformed_cpdf
+ * (include/cauchy_prediction.hpp:653-971, single-thread term order; the
+ * container it returns is the mce_rel2d object) and, with the grid below,
+ * pycauchy_single_step_eval_2d_rsys_cpdf (scripts/swig/cauchy/pycauchy.hpp:672-747).
+ *   est_p / est_s      the estimators within their batches (may be one batch)
+ *   bar_nu_full[d]     the point the reference draws as 2 u - 1,
+ *                      u = (rand() + 1) / (RAND_MAX + 2), for rows that the
+ *                      projection zeroes
+ *   full_solve         FULL_SOLVE: all 2m cells of each term instead of m
+ *   with_term_approx   drop terms whose bound on the pdf contribution is
+ *                      below term_approx_eps (approx_out_rel_marg2d_term_for_cpdf)
+ *   moments[14]        or NULL: the relative moments fz, mean[2], cov[2x2],
+ *                      finalised, as (re, im) pairs
+ *   counts[2]          or NULL: pairs, pairs approximated out
+ * Returns NULL with *status < 0 on failure: MCE_ERR_ARG before the first
+ * update or for differing dimensions, MCE_ERR_DONE after the last update (no
+ * g-tables), MCE_ERR_SHAPE when the two estimators' hyperplanes exceed 31. */
+typedef struct mce_rel2d mce_rel2d;
+mce_rel2d* mce_rel2d_create(mce_handle* primary, int est_p, mce_handle* secondary, int est_s, const double* Trel,
+                            const double* bar_nu_full, int full_solve, int with_term_approx, double term_approx_eps,
+                            double* moments, long long* counts, int* status);
+
+/* The relative pdf on the grid xlow..xhigh (step dx, last point xhigh) by
+ * ylow..yhigh, x outermost: point (i, j) at i * ny + j, as
+ * grid_eval_marg2d_relative_and_transformed_cpdf
+ * (include/cauchy_prediction.hpp:1091-1186) lays it out; the value is the real
+ * part of (2 - full) sum / (2 pi)^2 / (norm_factor_prim norm_factor_sec).
+ * With x, y or z NULL only the point count is returned.  Returns the number
+ * of points or a negative status (MCE_ERR_DEVICE for a cell with
+ * gamma1 = gamma2 = 0, where the reference exits). */
+int mce_rel2d_grid(mce_rel2d* r, double xlow, double xhigh, double dx, double ylow, double yhigh, double dy,
+                   double norm_factor_prim, double norm_factor_sec, int max_points, double* x, double* y, double* z);
+/* Pairs formed, and pairs kept after the term approximation. */
+long long mce_rel2d_num_pairs(mce_rel2d* r);
+long long mce_rel2d_num_terms(mce_rel2d* r);
+void mce_rel2d_destroy(mce_rel2d* r);
+
 /* Sum over all updates and estimators of the terms present after each MU. */
 long long mce_post_mu_terms(mce_handle* h);
 int mce_master_step(mce_handle* h);
