@@ -51,10 +51,12 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="batched3", choices=["batched3", "windows5"],
+    ap.add_argument("--workload", default="batched3", choices=["batched3", "windows5", "rel2d"],
                     help="batched3: the batched 3-state configuration (default); windows5: the sliding-window "
-                         "5-state LTV configuration for --window-steps steps")
+                         "5-state LTV configuration for --window-steps steps; rel2d: the relative 2-D system of "
+                         "two 5-state estimators")
     ap.add_argument("--window-steps", type=int, default=12)
+    ap.add_argument("--rel-updates", type=int, default=6, help="rel2d: updates of both estimators (6: 12.2 M pairs)")
     return ap.parse_args()
 
 
@@ -322,6 +324,148 @@ def run_windows5(args):
     print(json.dumps(line), flush=True)
 
 
+
+def run_rel2d(args):
+    """Relative-then-transformed 2-D system (rel = secondary - primary through
+    Trel = rows e0, e2) of two 5-state estimators with two measurements per
+    step, after 6 updates each (3,076 x 3,962 = 12.2 M term pairs): one
+    evaluation = the pair cache with term approximation (eps 1e-8), the
+    relative moments and a 17 x 17 pdf grid around the relative mean.
+    value: pairs/s over the device time of the three phases (CUDA events on
+    the object's stream; the kept-pair compaction counts with the moments);
+    e2e: pairs/s over the wall clock of the public calls
+    (RelativeSystem2D(...) + grid())."""
+    import ctypes
+    import torch
+    from cauchyfriendly_gb300 import CauchyEstimator, RelativeSystem2D, _lib, workloads as W
+    torch.cuda.set_device(0)
+    lib = _lib.load()
+    probs = [W.five_state_two_msmt(seed=s, steps=4) for s in (0, 1)]
+    updates = args.rel_updates
+    ests, consts = [], []
+    for i, q in enumerate(probs):
+        ms = (q["steps"] - 1) * q["pncc"] + q["d"]
+        rp, bp = np.zeros(q["d"]), np.zeros(ms)
+        P = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        lib.mce_draw_reference_constants(40 + i, q["d"], ms, 1, P(rp), P(bp))
+        consts.append((rp, bp))
+        est = CauchyEstimator(q["A0"], q["p0"], q["b0"], q["steps"], q["d"], q["cmcc"], q["pncc"], q["p"],
+                              root_point=rp, b_pert=bp)
+        n = 0
+        for k in range(q["steps"]):
+            for sub in range(q["p"]):
+                if n < updates:
+                    est.step(q["msmts"][k, sub], q["Phi"][k] if q["Phi"].ndim == 3 else q["Phi"], q["Gamma"],
+                             q["beta"], q["H"][sub], q["gamma"][sub])
+                    n += 1
+        ests.append(est)
+    T = np.zeros((2, 5))
+    T[0, 0] = T[1, 2] = 1.0
+    nu = np.array([0.3, -0.2, 0.5, -0.7, 0.1])
+
+    def grid_of(mom):
+        mu = mom["mean"].real
+        sd = np.sqrt(np.abs(np.diag(mom["cov"].real)))
+        sd = np.where(np.isfinite(sd) & (sd > 1e-6), sd, 1.0)
+        return (mu[0] - 3 * sd[0], mu[0] + 3 * sd[0], 6 * sd[0] / 16), (mu[1] - 3 * sd[1], mu[1] + 3 * sd[1],
+                                                                        6 * sd[1] / 16)
+
+    def one():
+        t0 = time.perf_counter()
+        rs = RelativeSystem2D(ests[0], ests[1], T, with_term_approx=True, term_approx_eps=1e-8, bar_nu_full=nu)
+        gx, gy = grid_of(rs.moments)
+        X, Y, Z, nx, ny = rs.grid(*gx, *gy)
+        wall = time.perf_counter() - t0
+        out = (rs.pairs, rs.terms, rs.device_ms(), wall, nx * ny, rs.launch_count())
+        rs.close()
+        return out
+
+    for _ in range(args.warmup):
+        one()
+    torch.cuda.synchronize()
+    clk = ClockSampler()
+    clk.start()
+    tot = {"pairs": 0.0, "moments": 0.0, "grid": 0.0}
+    walls, pairs, kept, npts, launches = 0.0, 0, 0, 0, 0
+    for _ in range(args.steps):
+        pairs, kept, dm, wl, npts, nl = one()
+        launches += nl
+        walls += wl
+        for k in tot:
+            tot[k] += dm[k]
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    dev_s = sum(tot.values()) / 1e3 / args.steps
+    wall_s = walls / args.steps
+    # algorithmic work: per pair the two terms read (A, p, b), a cache row of
+    # (mp + ms) cells written (6 doubles a cell + 5) with its kept flag and
+    # moment row; per grid point and kept term, 56 FP64 flops a cell
+    tps = [e.terms_per_shape(0).astype(np.float64) for e in ests]
+    mp = np.arange(len(tps[0]))
+    msh = np.arange(len(tps[1]))
+    Np, Ns = tps[0].sum(), tps[1].sum()
+    rd = lambda m: 8.0 * (m * 5 + m + 5)
+    pair_bytes = Ns * float((tps[0] * rd(mp)).sum()) + Np * float((tps[1] * rd(msh)).sum())
+    cells_sum = Ns * float((tps[0] * mp).sum()) + Np * float((tps[1] * msh).sum())
+    pair_bytes += 8.0 * (6 * cells_sum + 5 * pairs) + (4 + 112) * pairs
+    mean_cells = cells_sum / max(1, pairs)
+    grid_flops = 56.0 * npts * kept * mean_cells
+    peak, peak_kind = measured_peaks()
+    ms_pairs, ms_grid = tot["pairs"] / args.steps, tot["grid"] / args.steps
+    top = "grid" if ms_grid >= ms_pairs else "pairs"
+    roofline = {"bound": "hbm", "kernel": "k_rel2d_points" if top == "grid" else "k_rel2d_pairs",
+                "achieved": (pair_bytes / (ms_pairs / 1e3) if top == "pairs" else
+                             8.0 * kept * (6 * mean_cells + 5) / (ms_grid / 1e3)) / 1e9,
+                "peak": peak, "unit": "GB/s", "peak_source": peak_kind, "traffic": None,
+                "note": "FP64-bound: the grid kernel reads the pair cache from L2 once per point block; the FP64 "
+                        "pipe is its limit (see fp64)",
+                "fp64": {"algorithmic_tflops": grid_flops / (ms_grid / 1e3) / 1e12 if ms_grid > 0 else 0.0,
+                         "nominal_peak_tflops": 1.25}}
+    roofline["frac"] = roofline["achieved"] / peak
+    line = {"metric": "relative-system 2-D term pairs/s (cache + moments + 17x17 pdf grid, FP64)",
+            "value": pairs / dev_s, "unit": "pairs/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dev_s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "relative 2-D system of two 5-state, 2-measurement estimators after %d updates "
+                                   "(Trel rows e0, e2)" % updates, "pairs": int(pairs), "kept_terms": int(kept),
+                       "grid_points": int(npts), "l2": "the pair cache (several GB) exceeds L2"},
+            "e2e": {"value": pairs / wall_s, "unit": "pairs/s", "h2d_bytes_per_step": int(8 * (10 + 5 + 2 * npts)),
+                    "d2h_bytes_per_step": int(8 * (14 + npts) + 4 * pairs), "wall_s_per_step": wall_s},
+            "gpu_launches": launches,
+            "device_ms_per_step": {k: round(v / args.steps, 3) for k, v in tot.items()},
+            "roofline": roofline, "clocks": clocks}
+    if not args.no_cpu_baseline:
+        import oracle
+        oracle.build(with_reference=False)
+        orcs = []
+        for q, c in zip(probs, consts):
+            o = oracle.Oracle(q, *c)
+            n = 0
+            for k in range(q["steps"]):
+                for sub in range(q["p"]):
+                    if n < updates:
+                        o.step(k, sub)
+                        n += 1
+            orcs.append(o)
+        stride = 512
+        t0 = time.perf_counter()
+        oracle.oracle_rel2d(orcs[0], orcs[1], T, nu, (-1.0, 1.0, 0.125), (-1.0, 1.0, 0.125), pair_stride=stride)
+        t1 = time.perf_counter() - t0
+        stride = int(max(1, stride * t1 / max(args.cpu_seconds, 1e-3)))
+        t0 = time.perf_counter()
+        r = oracle.oracle_rel2d(orcs[0], orcs[1], T, nu, (-1.0, 1.0, 0.125), (-1.0, 1.0, 0.125),
+                                pair_stride=stride)
+        t1 = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": r["pairs"] / t1, "unit": "pairs/s", "cores": 1, "kind": "port",
+                                "sample": "every %d-th pair of the same evaluation (cache, moments, 17x17 grid): "
+                                          "%d pairs, %.1f s" % (stride, r["pairs"], t1)}
+        for o in orcs:
+            o.close()
+    for e in ests:
+        e.close()
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -329,6 +473,9 @@ def main():
         return
     if args.workload == "windows5":
         run_windows5(args)
+        return
+    if args.workload == "rel2d":
+        run_rel2d(args)
         return
     import torch
     rank = int(os.environ.get("RANK", "0"))

@@ -39,6 +39,8 @@ SIGNATURES = {
     "mce_rel2d_grid": (ctypes.c_int, [_vp] + [ctypes.c_double] * 8 + [ctypes.c_int, _dp, _dp, _dp]),
     "mce_rel2d_num_pairs": (ctypes.c_longlong, [_vp]),
     "mce_rel2d_num_terms": (ctypes.c_longlong, [_vp]),
+    "mce_rel2d_device_ms": (ctypes.c_double, [_vp, ctypes.c_int]),
+    "mce_rel2d_launch_count": (ctypes.c_longlong, [_vp]),
     "mce_rel2d_destroy": (None, [_vp]),
     "mce_batch_step_noalloc": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int, _ip]),
     "mce_batch_run": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int, _dp,

@@ -380,6 +380,7 @@ struct TermRecs {
     double* dval;
     signed char* cmap;   // [n][MC]
     signed char* csmap;  // [n][MC]
+    double* ps2;         // (sum of p)^2, the term-approximation weight (flattening.hpp:103-108)
 };
 
 // Parent list at the start of a step (one slot per term, ordered by

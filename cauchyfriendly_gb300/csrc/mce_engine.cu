@@ -315,13 +315,14 @@ public:
     struct RBufs {
         DevBuf<int> est, m, pbc, phc, z, lhp, fam, flags;
         DevBuf<unsigned> horthog;
-        DevBuf<double> A, p, q, b, cval, dval;
+        DevBuf<double> A, p, q, b, cval, dval, ps2;
         DevBuf<signed char> cmap, csmap;
         int ensure(long long n, int MC)
         {
             int s = MCE_OK;
             s |= est.ensure(n + 1);
             s |= m.ensure(n + 1);
+            s |= ps2.ensure(n + 1);
             s |= pbc.ensure(n + 1);
             s |= phc.ensure(n + 1);
             s |= z.ensure(n + 1);
@@ -357,6 +358,7 @@ public:
             R.b = b.ptr;
             R.cval = cval.ptr;
             R.dval = dval.ptr;
+            R.ps2 = ps2.ptr;
             R.cmap = cmap.ptr;
             R.csmap = csmap.ptr;
             return R;
@@ -1675,14 +1677,29 @@ struct mce_rel2d {
     long long npairs = 0, nkept = 0;
     DevBuf<double> tt, mrows, mpart, mout, trel, nu, part, xs, ys, zs;
     DevBuf<int> keep, bad;
-    DevBuf<long long> idxP, idxS;
+    DevBuf<long long> idxP, idxS, kpos, kidx, scan_tmp;
     DevBuf<Rel2DBlock> blk;
+    // device time of the last pair pass, moment sum and grid (CUDA events on the stream)
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    double ms[3] = {0, 0, 0};
+    long long launches = 0;  // kernels launched by the construction and the grids
     ~mce_rel2d()
     {
         if (stream) {
             cudaStreamSynchronize(stream);
             cudaStreamDestroy(stream);
         }
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+    double elapsed(int k)
+    {
+        float t = 0;
+        if (cudaEventElapsedTime(&t, ev[2 * k], ev[2 * k + 1]) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        return t;
     }
 };
 
@@ -1693,6 +1710,7 @@ int rel2d_build(mce_rel2d* r, EngineBase& P, int ep, EngineBase& S, int es, cons
                 const double* bar_nu_full, int full, int approx, double eps, double* moments, long long* counts)
 {
     const int d = P.d;
+    const long long l0 = g_launches;
     if (S.d != d) {
         set_error("relative system: the estimators' state dimensions differ");
         return MCE_ERR_ARG;
@@ -1709,6 +1727,7 @@ int rel2d_build(mce_rel2d* r, EngineBase& P, int ep, EngineBase& S, int es, cons
     MCE_CUDA(cudaGetDevice(&dev));
     MCE_CUDA(cudaDeviceGetAttribute(&r->lc.num_sms, cudaDevAttrMultiProcessorCount, dev));
     MCE_CUDA(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : r->ev) MCE_CUDA(cudaEventCreate(&e));
     r->lc.stream = r->stream;
     r->full = full ? 1 : 0;
     r->CC = (P.est[ep].max_shape + S.est[es].max_shape) * (1 + r->full);
@@ -1768,8 +1787,25 @@ int rel2d_build(mce_rel2d* r, EngineBase& P, int ep, EngineBase& S, int es, cons
     a.tt = r->tt.ptr;
     a.keep = r->keep.ptr;
     a.mrows = mom ? r->mrows.ptr : nullptr;
+    MCE_CUDA(cudaEventRecord(r->ev[0], st));
     P.rel2d_pairs(a, st);
+    MCE_CUDA(cudaEventRecord(r->ev[1], st));
     MCE_CUDA(cudaGetLastError());
+    MCE_CUDA(cudaEventRecord(r->ev[2], st));
+    // the kept pairs in order, for the grid's even chunks
+    {
+        long long need = 4, t = off;
+        while (t > 1) {
+            t = (t + 2047) / 2048;
+            need += t + 2;
+        }
+        if ((s = r->scan_tmp.ensure(need + 64))) return s;
+        if ((s = r->kpos.ensure(off + 2))) return s;
+        if ((s = r->kidx.ensure(off + 1))) return s;
+        ScanScratch ss{r->scan_tmp.ptr, (long long)r->scan_tmp.cap};
+        scan_int_to_ll(r->keep.ptr, r->kpos.ptr, off, ss, r->lc);
+        rel2d_compact(r->keep.ptr, r->kpos.ptr, off, r->kidx.ptr, r->lc);
+    }
     if (mom) {
         const long long chunk = 65536;
         const long long nch = (off + chunk - 1) / chunk;
@@ -1777,14 +1813,16 @@ int rel2d_build(mce_rel2d* r, EngineBase& P, int ep, EngineBase& S, int es, cons
         if ((s = r->mout.ensure(14))) return s;
         rel2d_moments(r->mrows.ptr, off, chunk, r->mpart.ptr, r->mout.ptr, r->lc);
         MCE_CUDA(cudaGetLastError());
-        MCE_CUDA(cudaMemcpyAsync(moments, r->mout.ptr, sizeof(double) * 14, cudaMemcpyDeviceToHost, st));
     }
-    std::vector<int> hk((size_t)off + 1);
-    if (off > 0) MCE_CUDA(cudaMemcpyAsync(hk.data(), r->keep.ptr, sizeof(int) * off, cudaMemcpyDeviceToHost, st));
-    MCE_CUDA(cudaStreamSynchronize(st));
+    MCE_CUDA(cudaEventRecord(r->ev[3], st));
+    if (mom) MCE_CUDA(cudaMemcpyAsync(moments, r->mout.ptr, sizeof(double) * 14, cudaMemcpyDeviceToHost, st));
     long long kept = 0;
-    for (long long i = 0; i < off; i++) kept += hk[i] != 0;
+    MCE_CUDA(cudaMemcpyAsync(&kept, r->kpos.ptr + off, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    MCE_CUDA(cudaStreamSynchronize(st));
     r->nkept = kept;
+    r->launches += g_launches - l0;
+    r->ms[0] = r->elapsed(0);
+    r->ms[1] = r->elapsed(1);
     if (counts) {
         counts[0] = off;
         counts[1] = off - kept;
@@ -1821,15 +1859,16 @@ int rel2d_grid(mce_rel2d* r, double xlow, double xhigh, double dx, double ylow, 
             y[i * ny + j] = j == ny - 1 ? yhigh : ylow + dy * j;
         }
     }
-    // enough (point, chunk) threads to fill the GPU; one chunk keeps the
-    // reference's summation order exactly
-    long long nch = (80000 + npts - 1) / npts;
-    const long long maxch = (r->npairs + 255) / 256;
+    // enough (point, chunk) threads for two full waves, chunks of at least 32
+    // kept terms; one chunk keeps the reference's summation order exactly
+    const long long nk = r->nkept;
+    long long nch = ((long long)r->lc.num_sms * 2048 * 2 + npts - 1) / npts;
+    const long long maxch = (nk + 31) / 32;
     if (nch > maxch) nch = maxch;
     if (nch < 1) nch = 1;
     if (nch > 65535) nch = 65535;
-    long long chunk = r->npairs > 0 ? (r->npairs + nch - 1) / nch : 1;
-    nch = r->npairs > 0 ? (r->npairs + chunk - 1) / chunk : 1;
+    long long chunk = nk > 0 ? (nk + nch - 1) / nch : 1;
+    nch = nk > 0 ? (nk + chunk - 1) / chunk : 1;
     int s;
     if ((s = r->xs.ensure(npts))) return s;
     if ((s = r->ys.ensure(npts))) return s;
@@ -1840,14 +1879,18 @@ int rel2d_grid(mce_rel2d* r, double xlow, double xhigh, double dx, double ylow, 
     MCE_CUDA(cudaMemcpyAsync(r->xs.ptr, x, sizeof(double) * npts, cudaMemcpyHostToDevice, st));
     MCE_CUDA(cudaMemcpyAsync(r->ys.ptr, y, sizeof(double) * npts, cudaMemcpyHostToDevice, st));
     MCE_CUDA(cudaMemsetAsync(r->bad.ptr, 0, sizeof(int), st));
-    rel2d_points(r->tt.ptr, r->keep.ptr, r->npairs, r->CC, r->full, chunk, (int)nch, r->xs.ptr, r->ys.ptr, npts,
+    MCE_CUDA(cudaEventRecord(r->ev[4], st));
+    r->launches += 2;
+    rel2d_points(r->tt.ptr, r->kidx.ptr, nk, r->CC, r->full, chunk, (int)nch, r->xs.ptr, r->ys.ptr, npts,
                  r->part.ptr, r->bad.ptr, r->lc);
     rel2d_finish(r->part.ptr, (int)nch, npts, r->full, nf_prim, nf_sec, r->zs.ptr, r->lc);
+    MCE_CUDA(cudaEventRecord(r->ev[5], st));
     MCE_CUDA(cudaGetLastError());
     int bad = 0;
     MCE_CUDA(cudaMemcpyAsync(z, r->zs.ptr, sizeof(double) * npts, cudaMemcpyDeviceToHost, st));
     MCE_CUDA(cudaMemcpyAsync(&bad, r->bad.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
     MCE_CUDA(cudaStreamSynchronize(st));
+    r->ms[2] = r->elapsed(2);
     if (bad) {
         set_error("relative pdf: a cell with gamma1 = gamma2 = 0 (the reference exits here)");
         return MCE_ERR_DEVICE;
@@ -2138,6 +2181,8 @@ int mce_rel2d_grid(mce_rel2d* r, double xlow, double xhigh, double dx, double yl
 }
 long long mce_rel2d_num_pairs(mce_rel2d* r) { return r ? r->npairs : MCE_ERR_ARG; }
 long long mce_rel2d_num_terms(mce_rel2d* r) { return r ? r->nkept : MCE_ERR_ARG; }
+double mce_rel2d_device_ms(mce_rel2d* r, int which) { return r && which >= 0 && which < 3 ? r->ms[which] : -1.0; }
+long long mce_rel2d_launch_count(mce_rel2d* r) { return r ? r->launches : MCE_ERR_ARG; }
 void mce_rel2d_destroy(mce_rel2d* r) { delete r; }
 long long mce_post_mu_terms(mce_handle* h) { return h ? h->eng->post_mu_terms : MCE_ERR_ARG; }
 int mce_master_step(mce_handle* h) { return h ? h->eng->master_step : MCE_ERR_ARG; }

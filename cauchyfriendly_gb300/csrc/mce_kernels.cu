@@ -892,10 +892,13 @@ __global__ void __launch_bounds__(128) k_mu_terms(ParentList P, long long nP, co
         if (pslot < nR && cslot0 + __popc(integ_mask) <= nR) {
             double* Ao = R.A + slot * MC * D;
             for (int q = 0; q < mfin * D; q++) Ao[q] = At[q];
+            double ps = 0;
             for (int q = 0; q < mfin; q++) {
                 R.p[slot * MC + q] = pt[q];
                 R.q[slot * MC + q] = qt[q];
+                ps += pt[q];
             }
+            R.ps2[slot] = ps * ps;  // (sum of p)^2 in row order
         }
     }
 }
@@ -1342,12 +1345,6 @@ __device__ inline int bm_extract(const unsigned* bm, int m, int* out, int cap, i
     return count;
 }
 
-__device__ inline double p_sum_sq(const double* p, int m)
-{
-    double s = 0;
-    for (int k = 0; k < m; k++) s += p[k];
-    return s * s;
-}
 
 // Root cells of a new child: make_new_child_btable (cell_enumeration.hpp:206-371)
 // into the bitmap RK (2^m bits).  PB receives the parent's B_mu as a bitmap.
@@ -1490,7 +1487,7 @@ __global__ void k_gtable_prep(GCtx c, const int* roots_list, long long nroots, c
             gnr[ri] = nR;
             gitems[ri] = flat ? (1 + nmem) * nR : 0;
             gcells[ri] = flat ? nR : 0;
-            rps2[ri] = p_sum_sq(R.p + r * MC, m);
+            rps2[ri] = R.ps2[r];
             rflag[ri] = 0;
         }
         const long long mb = goff[r];
@@ -1499,7 +1496,7 @@ __global__ void k_gtable_prep(GCtx c, const int* roots_list, long long nroots, c
             const bool own = !(R.flags[cm] & kFlagNewChild) && c.P.B_cnt[R.fam[cm]] == nR;
             const int sig = orientation_mask<D>(R.A + r * MC * D, R.A + cm * MC * D, m);
             minfo[mb + j] = sig | (own ? kInfoOwn : 0);
-            mps2[mb + j] = p_sum_sq(R.p + cm * MC, m);
+            mps2[mb + j] = R.ps2[cm];
             mflag[mb + j] = 0;
         }
         __syncwarp();
@@ -1685,7 +1682,7 @@ __global__ void k_gtable(GCtx c, const int* roots_list, long long nroots, const 
         // unless the flat pass already found the root approximated out
         bool negl = true;
         if (!root_out) {
-            const double ps2 = p_sum_sq(R.p + root * MC, m);
+            const double ps2 = R.ps2[root];
             for (int k = lane; k < nR; k += 32) {
                 const cd v = g_cell<D>(c, root, RKL[k], gs);
                 okeys[k] = RKL[k];
@@ -1730,7 +1727,7 @@ __global__ void k_gtable(GCtx c, const int* roots_list, long long nroots, const 
                     if (lane == 0) set_err(err, kErrTableOverflow);
                     nR = cap;
                 }
-                const double ps2c = p_sum_sq(R.p + cm * MC, m);
+                const double ps2c = R.ps2[cm];
                 bool ng = true;
                 for (int k = lane; k < nR; k += 32) {
                     const cd v = g_cell<D>(c, cm, RKL[k], gs);
@@ -1765,7 +1762,7 @@ __global__ void k_gtable(GCtx c, const int* roots_list, long long nroots, const 
             if (lane == 0) sig = orientation_mask<D>(R.A + root * MC * D, R.A + cm * MC * D, m);
             sig = __shfl_sync(kFull, sig, 0);
             const int sigf = (sig & top) ? (sig ^ rev) : sig;
-            const double ps2c = p_sum_sq(R.p + cm * MC, m);
+            const double ps2c = R.ps2[cm];
             bool ng = true;
             if (!own) {
                 for (int k = lane; k < nR; k += 32) {
@@ -2630,7 +2627,8 @@ __global__ void __launch_bounds__(128) k_rel2d_pairs(Rel2DArgs a)
         for (int c = 0; c < cells; c++) {
             const int h = c < mn ? c : c - mn;
             const double tm = (th[h + 1] + th[h]) / 2.0;
-            const double ct = cos(tm), st = sin(tm);
+            double st, ct;
+            sincos(tm, &st, &ct);
             unsigned neg = 0;  // sv[j] = -1
             for (int j = 0; j < mn; j++)
                 if (!(Ac[2 * j] * ct + Ac[2 * j + 1] * st > 0)) neg |= 1u << j;
@@ -2648,15 +2646,14 @@ __global__ void __launch_bounds__(128) k_rel2d_pairs(Rel2DArgs a)
                 g1r -= (Ac[2 * j] * pc[j]) * sv;
                 g2r -= (Ac[2 * j + 1] * pc[j]) * sv;
             }
-            os[c] = sin(th[c]);
-            oc[c] = cos(th[c]);
+            sincos(th[c], os + c, oc + c);
             o1[c] = g1r;
             o2[c] = g2r;
             og[2 * c] = g.re;
             og[2 * c + 1] = g.im;
         }
-        os[cells] = cells > 0 ? sin(th[cells]) : 0.0;
-        oc[cells] = cells > 0 ? cos(th[cells]) : 0.0;
+        if (cells > 0) sincos(th[cells], os + cells, oc + cells);
+        else os[0] = oc[0] = 0.0;
         int keep = 1;
         if (a.approx) {
             double total = 0;
@@ -2805,20 +2802,19 @@ void cpdf1d_points(const double* tt, long long n, const double* xs, int npts, in
 // cauchy_prediction.hpp:973-1073): a thread per (grid point, chunk of pairs),
 // the chunk's kept terms and their cells summed in order; the integral of a
 // cell is the marginal 2-D one.
-__global__ void k_rel2d_points(const double* tt, const int* keep, long long n, int CC, int full, long long chunk,
-                               const double* xs, const double* ys, int npts, double* part, int* bad)
+__global__ void k_rel2d_points(const double* tt, const long long* kidx, long long nk, int CC, int full,
+                               long long chunk, const double* xs, const double* ys, int npts, double* part, int* bad)
 {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= npts) return;
     const long long j0 = (long long)blockIdx.y * chunk;
-    const long long j1 = j0 + chunk < n ? j0 + chunk : n;
+    const long long j1 = j0 + chunk < nk ? j0 + chunk : nk;
     const int RT = rel2d_stride(CC);
     const double x1 = xs[q], x2 = ys[q];
     double fx = 0;
     int b = 0;
     for (long long j = j0; j < j1; j++) {
-        if (!keep[j]) continue;
-        const double* o = tt + j * RT;
+        const double* o = tt + kidx[j] * RT;
         const int cells = (int)o[0] * (1 + full);
         const double* os = o + 3;
         const double* oc = os + (CC + 1);
@@ -2847,13 +2843,27 @@ __global__ void k_rel2d_finish(const double* part, int nch, int npts, int full, 
     zs[q] = ((double)(2 - full)) * fx * kTwoPiInv * kTwoPiInv / (nf_prim * nf_sec);
 }
 
-void rel2d_points(const double* tt, const int* keep, long long n, int CC, int full, long long chunk, int nch,
-                  const double* xs, const double* ys, int npts, double* part, int* bad, const LaunchCfg& c)
+void rel2d_points(const double* tt, const long long* kidx, long long nk, int CC, int full, long long chunk,
+                  int nch, const double* xs, const double* ys, int npts, double* part, int* bad, const LaunchCfg& c)
 {
     if (npts <= 0) return;
     ++g_launches;
-    k_rel2d_points<<<dim3((npts + 63) / 64, nch), 64, 0, c.stream>>>(tt, keep, n, CC, full, chunk, xs, ys, npts,
+    k_rel2d_points<<<dim3((npts + 63) / 64, nch), 64, 0, c.stream>>>(tt, kidx, nk, CC, full, chunk, xs, ys, npts,
                                                                       part, bad);
+}
+
+// kidx[kpos[j]] = j for every kept pair j (kpos: exclusive scan of keep)
+__global__ void k_rel2d_compact(const int* keep, const long long* kpos, long long n, long long* kidx)
+{
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x)
+        if (keep[j]) kidx[kpos[j]] = j;
+}
+
+void rel2d_compact(const int* keep, const long long* kpos, long long n, long long* kidx, const LaunchCfg& c)
+{
+    if (n <= 0) return;
+    ++g_launches;
+    k_rel2d_compact<<<grid_for(n, 256, c.num_sms, 8), 256, 0, c.stream>>>(keep, kpos, n, kidx);
 }
 
 void rel2d_finish(const double* part, int nch, int npts, int full, double nf_prim, double nf_sec, double* zs,

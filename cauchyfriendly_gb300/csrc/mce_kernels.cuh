@@ -136,11 +136,13 @@ void cpdf2d_points(const double* tt, long long n, int MC, const double* xs, cons
 // marginal 1-D pdf at npts points from the per-term records of k_cpdf1d_terms
 void cpdf1d_points(const double* tt, long long n, const double* xs, int npts, int exact, double fz, double* ys,
                    const LaunchCfg& c);
-// relative 2-D pdf at npts points from the pair cache rows (kept ones, in
-// order), the pairs split into nch chunks: part[nch x npts], then the chunk
+// relative 2-D pdf at npts points from the cache rows of the nk kept pairs
+// kidx (in order), split into nch chunks: part[nch x npts], then the chunk
 // sums in order scaled by (2 - full) (1/2pi)^2 / (nf_prim nf_sec)
-void rel2d_points(const double* tt, const int* keep, long long n, int CC, int full, long long chunk, int nch,
-                  const double* xs, const double* ys, int npts, double* part, int* bad, const LaunchCfg& c);
+void rel2d_points(const double* tt, const long long* kidx, long long nk, int CC, int full, long long chunk,
+                  int nch, const double* xs, const double* ys, int npts, double* part, int* bad, const LaunchCfg& c);
+// kept pair indices in order from the keep flags and their exclusive scan
+void rel2d_compact(const int* keep, const long long* kpos, long long n, long long* kidx, const LaunchCfg& c);
 void rel2d_finish(const double* part, int nch, int npts, int full, double nf_prim, double nf_sec, double* zs,
                   const LaunchCfg& c);
 // relative moments: the 14 columns of mrows summed over the pairs in order

@@ -296,6 +296,15 @@ class RelativeSystem2D:
         ny = int(np.ceil((g[4] - g[3]) / g[5] + 1))
         return X, Y, Z, n // ny, ny
 
+    def device_ms(self):
+        """Device time (ms) of the pair kernel and of the kept-pair compaction
+        with the moment sums of the construction, and of the last grid."""
+        return {k: float(self._lib.mce_rel2d_device_ms(self._h, i)) for i, k in enumerate(("pairs", "moments", "grid"))}
+
+    def launch_count(self):
+        """Kernels launched by the construction and the grids so far."""
+        return int(self._lib.mce_rel2d_launch_count(self._h))
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.mce_rel2d_destroy(self._h)

@@ -204,6 +204,12 @@ int mce_rel2d_grid(mce_rel2d* r, double xlow, double xhigh, double dx, double yl
 /* Pairs formed, and pairs kept after the term approximation. */
 long long mce_rel2d_num_pairs(mce_rel2d* r);
 long long mce_rel2d_num_terms(mce_rel2d* r);
+/* Device time in ms (CUDA events on the object's stream) of the pair kernel
+ * (which = 0), of the kept-pair compaction and moment sums (1) of
+ * mce_rel2d_create, and of the last mce_rel2d_grid (2). */
+double mce_rel2d_device_ms(mce_rel2d* r, int which);
+/* Kernels launched by mce_rel2d_create and every mce_rel2d_grid so far. */
+long long mce_rel2d_launch_count(mce_rel2d* r);
 void mce_rel2d_destroy(mce_rel2d* r);
 
 /* Sum over all updates and estimators of the terms present after each MU. */
