@@ -1049,11 +1049,14 @@ __device__ inline long long cell_slot(int e, int m, const long long* c, long lon
     return (long long)(h & (unsigned long long)hmask);
 }
 
+// A bucket entry: the term, its (estimator, shape) and the integer keys of
+// its b window (b - eps, b + eps], computed once per term instead of once
+// per candidate test.
 template <int D>
 struct CellEntry {
     int idx;
     int est_m;  // est << 5 | m
-    double b[D];
+    long long lo[D], hi[D];
 };
 
 template <int D>
@@ -1084,7 +1087,11 @@ __global__ void k_ftr_scatter(TermRecs R, long long nR, const int* slot_of, cons
         CellEntry<D> c;
         c.idx = (int)j;
         c.est_m = (R.est[j] << 5) | R.m[j];
-        for (int a = 0; a < D; a++) c.b[a] = R.b[j * D + a];
+        for (int a = 0; a < D; a++) {
+            const double b = R.b[j * D + a];
+            c.lo[a] = dkey(b - kReductionEps);
+            c.hi[a] = dkey(b + kReductionEps);
+        }
         ent[pos] = c;
     }
 }
@@ -1138,10 +1145,11 @@ __global__ void k_ftr_resolve_scan(TermRecs R, long long nR, const CellEntry<D>*
         const int m = R.m[j];
         const int em = (e << 5) | m;
         double bj[D];
-        long long lo[D], nc[D];
+        long long kj[D], lo[D], nc[D];
         int nprobe = 1;
         for (int a = 0; a < D; a++) {
             bj[a] = R.b[j * D + a];
+            kj[a] = dkey(bj[a]);
             lo[a] = cell_of(bj[a] - kProbeHalfWidth);
             const long long hi = cell_of(bj[a] + kProbeHalfWidth);
             nc[a] = hi - lo[a] + 1;
@@ -1169,10 +1177,8 @@ __global__ void k_ftr_resolve_scan(TermRecs R, long long nR, const CellEntry<D>*
                 if (ce.idx >= j) break;  // ascending: no predecessors beyond
                 if (ce.est_m != em) continue;
                 bool ok = true;
-                for (int a = 0; a < D && ok; a++) {
-                    const double lo_a = ce.b[a] - kReductionEps, hi_a = ce.b[a] + kReductionEps;
-                    if (!(dlt(lo_a, bj[a]) && dle(bj[a], hi_a))) ok = false;
-                }
+                for (int a = 0; a < D && ok; a++)
+                    if (!(ce.lo[a] < kj[a] && kj[a] <= ce.hi[a])) ok = false;
                 if (!ok || !ftr_near_pm<D>(R, ce.idx, j, m, MC)) continue;
                 const int st = ((volatile int*)status)[ce.idx];
                 if (st == 2) continue;  // a member: look further
