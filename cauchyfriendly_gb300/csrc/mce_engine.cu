@@ -365,6 +365,7 @@ public:
         }
     } Rb;
     DevBuf<cd> fam_mom, est_raw, scratch, g_vals;
+    DevBuf<int> ftr_wl[2], ftr_resume;
     DevBuf<int> g_nr, g_items, g_cells, g_rflag, g_minfo, g_mflag, nvert, vsv;
     DevBuf<long long> g_ioff, g_coff, voff;
     DevBuf<double> g_rps2, g_mps2;
@@ -1005,13 +1006,17 @@ public:
         Kernels<D>::ftr_sort(cell_ent.ptr, nent, slot_of.ptr, boff.ptr, cell_ent2.ptr, lc);
         k_status_init(R, nR);
         pend();
+        if ((s = ftr_wl[0].ensure(nR + 1))) return s;
+        if ((s = ftr_wl[1].ensure(nR + 1))) return s;
+        if ((s = ftr_resume.ensure((size_t)(nR + 1) * kFtrResume))) return s;
+        int unk = 0;
         for (int round = 0;; round++) {
             MCE_CUDA(cudaMemsetAsync(counters.ptr + 1, 0, sizeof(int), lc.stream));
             pbeg(KID_FTR);
-            Kernels<D>::ftr_resolve(R, nR, cell_ent2.ptr, boff.ptr, H - 1, MC, status.ptr, owner.ptr, counters.ptr + 1,
-                                    lc);
+            Kernels<D>::ftr_resolve(R, nR, cell_ent2.ptr, boff.ptr, H - 1, MC, status.ptr, owner.ptr,
+                                    round ? ftr_wl[(round - 1) & 1].ptr : nullptr, unk, ftr_wl[round & 1].ptr,
+                                    counters.ptr + 1, ftr_resume.ptr, lc);
             pend();
-            int unk = 0;
             MCE_CUDA(cudaMemcpyAsync(&unk, counters.ptr + 1, sizeof(int), cudaMemcpyDeviceToHost, lc.stream));
             MCE_CUDA(cudaStreamSynchronize(lc.stream));
             if (unk == 0) break;

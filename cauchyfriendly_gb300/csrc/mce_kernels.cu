@@ -1135,11 +1135,18 @@ __global__ void k_ftr_sort_buckets(const CellEntry<D>* in, long long n, const in
 // with no such predecessor is a root; otherwise it waits for the next round.
 // Near predecessors are found by scanning the sorted buckets of the cells
 // around b in ascending index, stopping at the first one that is not a member.
+// Members and non-near entries stay what they are, so a term that must wait
+// resumes each bucket at the entry that stopped it (resume[j][q] for its q-th
+// distinct bucket), and later rounds run over the worklist of waiting terms.
+
 template <int D>
 __global__ void k_ftr_resolve_scan(TermRecs R, long long nR, const CellEntry<D>* ent, const long long* boff,
-                                   long long hmask, int MC, int* status, int* owner, int* unknown)
+                                   long long hmask, int MC, int* status, int* owner, const int* wl_in, long long n_in,
+                                   int* wl_out, int* n_out, int* resume)
 {
-    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nR; j += (long long)gridDim.x * blockDim.x) {
+    const long long n = wl_in ? n_in : nR;
+    for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < n; w += (long long)gridDim.x * blockDim.x) {
+        const long long j = wl_in ? wl_in[w] : w;
         if (status[j] != 0) continue;
         const int e = R.est[j];
         const int m = R.m[j];
@@ -1171,8 +1178,11 @@ __global__ void k_ftr_resolve_scan(TermRecs R, long long nR, const CellEntry<D>*
             bool dup = false;
             for (int q = 0; q < nseen; q++) dup |= seen[q] == s;
             if (dup) continue;
+            const int q = nseen;
             if (nseen < (1 << (D < 5 ? D : 5))) seen[nseen++] = s;
-            for (long long k = boff[s]; k < boff[s + 1]; k++) {
+            const long long kb = boff[s], ke = boff[s + 1];
+            long long k = kb + ((wl_in && q < kFtrResume) ? resume[j * kFtrResume + q] : 0);
+            for (; k < ke; k++) {
                 const CellEntry<D>& ce = ent[k];
                 if (ce.idx >= j) break;  // ascending: no predecessors beyond
                 if (ce.est_m != em) continue;
@@ -1186,6 +1196,7 @@ __global__ void k_ftr_resolve_scan(TermRecs R, long long nR, const CellEntry<D>*
                 else minu = ce.idx < minu ? ce.idx : minu;
                 break;  // the first non-member near predecessor of this bucket decides it
             }
+            if (q < kFtrResume) resume[j * kFtrResume + q] = (int)(k - kb);
         }
         if (best < minu) {
             owner[j] = best;
@@ -1194,7 +1205,7 @@ __global__ void k_ftr_resolve_scan(TermRecs R, long long nR, const CellEntry<D>*
             owner[j] = (int)j;
             ((volatile int*)status)[j] = 1;
         } else
-            atomicAdd(unknown, 1);
+            wl_out[atomicAdd(n_out, 1)] = (int)j;
     }
 }
 
@@ -2046,12 +2057,15 @@ void Kernels<D>::ftr_sort(const void* in, long long n, const int* slot_of, const
 
 template <int D>
 void Kernels<D>::ftr_resolve(TermRecs R, long long nR, const void* ent, const long long* boff, long long hmask,
-                             int MC, int* status, int* owner, int* unknown, const LaunchCfg& c)
+                             int MC, int* status, int* owner, const int* wl_in, long long n_in, int* wl_out,
+                             int* n_out, int* resume, const LaunchCfg& c)
 {
-    if (nR == 0) return;
+    const long long n = wl_in ? n_in : nR;
+    if (n == 0) return;
     ++g_launches;
-    k_ftr_resolve_scan<D><<<grid_for(nR, 128, c.num_sms), 128, 0, c.stream>>>(
-        R, nR, static_cast<const CellEntry<D>*>(ent), boff, hmask, MC, status, owner, unknown);
+    k_ftr_resolve_scan<D><<<grid_for(n, 128, c.num_sms), 128, 0, c.stream>>>(
+        R, nR, static_cast<const CellEntry<D>*>(ent), boff, hmask, MC, status, owner, wl_in, n_in, wl_out, n_out,
+        resume);
 }
 
 static inline size_t gtable_smem_per_warp(int MC, int D)

@@ -56,6 +56,9 @@ struct Rel2DArgs {
 // doubles per cache row: m, b[2], sin[CC+1], cos[CC+1], gamma1 re[CC], gamma2 re[CC], g[CC] (re, im)
 __host__ __device__ inline int rel2d_stride(int CC) { return 6 * CC + 5; }
 
+// bucket positions kept per record between term-reduction rounds
+constexpr int kFtrResume = 8;
+
 template <int D>
 struct Kernels {
     // First measurement update (cauchy_estimator.hpp:1179-1208).
@@ -91,8 +94,13 @@ struct Kernels {
     static size_t cell_entry_bytes();
     static void ftr_sort(const void* in, long long n, const int* slot_of, const long long* boff, void* out,
                          const LaunchCfg& c);
+    // One resolution round: over every record (wl_in null) or over the
+    // worklist of records still waiting; the ones that must wait again are
+    // appended to wl_out (count n_out); resume holds kFtrResume bucket
+    // positions per record.
     static void ftr_resolve(TermRecs R, long long nR, const void* ent, const long long* boff, long long hmask, int MC,
-                            int* status, int* owner, int* unknown, const LaunchCfg& c);
+                            int* status, int* owner, const int* wl_in, long long n_in, int* wl_out, int* n_out,
+                            int* resume, const LaunchCfg& c);
     // g-tables of every reduction group (flattening.hpp:318-568).
     static void gtable(TermRecs R, const int* roots_list, long long nroots, const int* gcnt,
                        const long long* goff, const int* members, ParentList P, Tables Told, const int* Bkeys,
