@@ -419,6 +419,18 @@ struct GFlat {
     double* mps2;
     int* mflag;
     cd* gv;
+    // groups whose root the flat pass approximated out and whose promoted
+    // root the serial path found (per root list index): the members left
+    // after it go through the promoted-root flat pass
+    int* pr_root;          // the promoted root record
+    int* pr_mb;            // its first remaining member's slot in the members list
+    int* pr_mcnt;          // remaining members (0: nothing handed over)
+    int* pr_cells;         // the promoted root's cell count (0 when nothing is handed over)
+    int* pr_items;         // pr_mcnt * pr_cells
+    long long* pr_moff;    // exclusive scans of pr_mcnt, pr_items, pr_cells
+    long long* pr_ioff;
+    long long* pr_coff;
+    cd* pr_gv;             // the remaining members' values
 };
 
 // Per-estimator step inputs, packed by the host each step.

@@ -364,7 +364,9 @@ public:
             return R;
         }
     } Rb;
-    DevBuf<cd> fam_mom, est_raw, scratch, g_vals;
+    DevBuf<cd> fam_mom, est_raw, scratch, g_vals, pr_gv;
+    DevBuf<int> pr_root, pr_mb, pr_mcnt, pr_cells, pr_items;
+    DevBuf<long long> pr_moff, pr_ioff, pr_coff;
     DevBuf<int> ftr_wl[2], ftr_resume;
     DevBuf<int> g_nr, g_items, g_cells, g_rflag, g_minfo, g_mflag, nvert, vsv;
     DevBuf<long long> g_ioff, g_coff, voff;
@@ -1091,7 +1093,17 @@ public:
         if ((s = g_mps2.ensure(nmembers + 1))) return s;
         if ((s = g_mflag.ensure(nmembers + 1))) return s;
         if ((s = ensure_scan_scratch(nroots + 1))) return s;
-        GFlat gf{g_nr.ptr, g_ioff.ptr, g_rps2.ptr, g_rflag.ptr, g_minfo.ptr, g_mps2.ptr, g_mflag.ptr, nullptr};
+        if ((s = pr_root.ensure(nroots + 1))) return s;
+        if ((s = pr_mb.ensure(nroots + 1))) return s;
+        if ((s = pr_mcnt.ensure(nroots + 1))) return s;
+        if ((s = pr_cells.ensure(nroots + 1))) return s;
+        if ((s = pr_items.ensure(nroots + 1))) return s;
+        if ((s = pr_moff.ensure(nroots + 2))) return s;
+        if ((s = pr_ioff.ensure(nroots + 2))) return s;
+        if ((s = pr_coff.ensure(nroots + 2))) return s;
+        GFlat gf{g_nr.ptr,    g_ioff.ptr,    g_rps2.ptr,    g_rflag.ptr,  g_minfo.ptr,  g_mps2.ptr,
+                 g_mflag.ptr, nullptr,       pr_root.ptr,   pr_mb.ptr,    pr_mcnt.ptr,  pr_cells.ptr,
+                 pr_items.ptr, pr_moff.ptr,  pr_ioff.ptr,   pr_coff.ptr,  nullptr};
         const Tables Tnv{Tn.keys.ptr, Tn.vals.ptr};
         pbeg(KID_GTABLE);
         Kernels<D>::gtable_prep(R, roots_list.ptr, nroots, gcnt.ptr, goff.ptr, members.ptr, PV, Told, Bkeys.ptr,
@@ -1116,9 +1128,34 @@ public:
                                 gscale.ptr, toff.ptr, Tnv, gf, MC, lc);
         Kernels<D>::gtable_combine(R, roots_list.ptr, nroots, g_coff.ptr, ncells, gcnt.ptr, goff.ptr, members.ptr, PV,
                                    Told, Bkeys.ptr, toff.ptr, Tnv, tcnt.ptr, alive.ptr, src.ptr, gf, MC, lc);
+        MCE_CUDA(cudaMemsetAsync(pr_mcnt.ptr, 0, sizeof(int) * (nroots + 1), lc.stream));
+        MCE_CUDA(cudaMemsetAsync(pr_cells.ptr, 0, sizeof(int) * (nroots + 1), lc.stream));
+        MCE_CUDA(cudaMemsetAsync(pr_items.ptr, 0, sizeof(int) * (nroots + 1), lc.stream));
         Kernels<D>::gtable(R, roots_list.ptr, nroots, gcnt.ptr, goff.ptr, members.ptr, PV, Told, Bkeys.ptr, gscale.ptr,
                            toff.ptr, Tnv, tcnt.ptr, alive.ptr, src.ptr, gscr, capMC, gf, MC, err, lc, gscr_warps);
+        // members left after promotions: the promoted-root flat pass
+        scan_int_to_ll(pr_mcnt.ptr, pr_moff.ptr, nroots, ss, lc);
+        scan_int_to_ll(pr_items.ptr, pr_ioff.ptr, nroots, ss, lc);
+        scan_int_to_ll(pr_cells.ptr, pr_coff.ptr, nroots, ss, lc);
         pend();
+        long long pt[3] = {0, 0, 0};
+        if (nroots > 0) {
+            MCE_CUDA(cudaMemcpyAsync(&pt[0], pr_moff.ptr + nroots, sizeof(long long), cudaMemcpyDeviceToHost,
+                                     lc.stream));
+            MCE_CUDA(cudaMemcpyAsync(&pt[1], pr_ioff.ptr + nroots, sizeof(long long), cudaMemcpyDeviceToHost,
+                                     lc.stream));
+            MCE_CUDA(cudaMemcpyAsync(&pt[2], pr_coff.ptr + nroots, sizeof(long long), cudaMemcpyDeviceToHost,
+                                     lc.stream));
+            MCE_CUDA(cudaStreamSynchronize(lc.stream));
+        }
+        if (pt[1] > 0) {
+            if ((s = pr_gv.ensure(pt[1] + 1))) return s;
+            gf.pr_gv = pr_gv.ptr;
+            pbeg(KID_GTABLE);
+            Kernels<D>::gtable_promoted(R, roots_list.ptr, nroots, pt[0], pt[1], pt[2], members.ptr, PV, Told,
+                                        Bkeys.ptr, gscale.ptr, toff.ptr, Tnv, gf, MC, lc);
+            pend();
+        }
         if (prof_mode >= 2) alg_stats(with_tp, nR, true);
         // ---- next parent list
         if ((s = hist.ensure((size_t)E * MCp))) return s;

@@ -1646,7 +1646,7 @@ template <int D>
 __global__ void k_gtable(GCtx c, const int* roots_list, long long nroots, const int* gcnt, const long long* goff,
                          const int* members, const double* gscale_e, const long long* toff, Tables Tnew, int* tcnt,
                          int* alive, int* src, cd* scratch, long long scratch_per_warp, const int* rflag,
-                         const long long* ioff, const int* gnr, const int* minfo, const int* mflag, const cd* gv,
+                         const int* gnr, int* pr_root, int* pr_mb, int* pr_mcnt, int* pr_cells, int* pr_items,
                          int* err)
 {
     extern __shared__ unsigned smem_g[];
@@ -1768,7 +1768,24 @@ __global__ void k_gtable(GCtx c, const int* roots_list, long long nroots, const 
             __syncwarp();
             continue;
         }
-        // RK holds the root's cells as a bitmap, RKL as a sorted list
+        // RK holds the root's cells as a bitmap, RKL as a sorted list.
+        // A group of at most kFlatMaxCells cells hands the members left to the
+        // promoted-root flat pass (k_gtable_prom_*), which computes what the
+        // loop below would, relative to the same root and cells.
+        if (root != r && nR <= kFlatMaxCells && kidx < nmem) {
+            if (lane == 0) {
+                pr_root[ri] = (int)root;
+                pr_mb[ri] = (int)(goff[r] + kidx);
+                pr_mcnt[ri] = nmem - kidx;
+                pr_cells[ri] = nR;
+                pr_items[ri] = nR * (nmem - kidx);
+                alive[r] = 1;
+                tcnt[r] = nR;
+                src[r] = (int)root;
+            }
+            __syncwarp();
+            continue;
+        }
         // ---- members: make_gtable + add_gtables (flattening.hpp:493-552)
         for (; kidx < nmem; kidx++) {
             const long long cm = mem[kidx];
@@ -1831,6 +1848,117 @@ __global__ void k_gtable(GCtx c, const int* roots_list, long long nroots, const 
             src[r] = (int)root;
         }
         __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Promoted-root flat pass: the members left after a promotion, against the
+// promoted root and its cells (already in the output table), in three flat
+// steps like the first pass: member info (orientation relative to the
+// promoted root and the own-table mode), a thread per (member, cell) value
+// with the term-approximation flag, and a thread per root cell summing the
+// kept members in order (flattening.hpp:493-552).
+__device__ inline long long last_le(const long long* off, long long n, long long x)
+{
+    long long lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const long long mid = (lo + hi) >> 1;
+        if (off[mid] <= x) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <int D>
+__global__ void k_gtable_prom_prep(GCtx c, long long nroots, long long nmem_total, const int* members, GFlat f)
+{
+    const TermRecs& R = c.R;
+    for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < nmem_total;
+         x += (long long)gridDim.x * blockDim.x) {
+        const long long ri = last_le(f.pr_moff, nroots, x);
+        const long long root = f.pr_root[ri];
+        const int nR = f.pr_cells[ri];
+        const long long mi = f.pr_mb[ri] + (x - f.pr_moff[ri]);
+        const long long cm = members[mi];
+        const int m = R.m[root];
+        const bool own = !(R.flags[cm] & kFlagNewChild) && c.P.B_cnt[R.fam[cm]] == nR;
+        const int sig = orientation_mask<D>(R.A + root * c.MC * D, R.A + cm * c.MC * D, m);
+        f.minfo[mi] = sig | (own ? kInfoOwn : 0);
+        f.mflag[mi] = 0;
+    }
+}
+
+template <int D>
+__global__ void k_gtable_prom_eval(GCtx c, const int* roots_list, long long nroots, long long nitems,
+                                   const int* members, const double* gscale_e, const long long* toff, Tables Tnew,
+                                   GFlat f)
+{
+    const TermRecs& R = c.R;
+    for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < nitems;
+         x += (long long)gridDim.x * blockDim.x) {
+        const long long ri = last_le(f.pr_ioff, nroots, x);
+        const long long r = roots_list[ri];
+        const int nR = f.pr_cells[ri];
+        const long long loc = x - f.pr_ioff[ri];
+        const int jj = (int)(loc / nR), k = (int)(loc - (long long)jj * nR);
+        const long long mi = f.pr_mb[ri] + jj;
+        const long long s = members[mi];
+        const int info = f.minfo[mi];
+        int key;
+        if (info & kInfoOwn) {
+            key = c.Bkeys[c.P.B_off[R.fam[s]] + k];
+        } else {
+            const int m = R.m[r];
+            const int top = 1 << (m - 1), rev = (1 << m) - 1;
+            const int sig = info & 0xffff;
+            key = Tnew.keys[toff[r] + k] ^ ((sig & top) ? (sig ^ rev) : sig);
+        }
+        const cd v = g_cell<D>(c, s, key, gscale_e[R.est[r]]);
+        f.pr_gv[x] = v;
+        if (above_approx_threshold(R.ps2[s], v.re, v.im)) f.mflag[mi] = 1;
+    }
+}
+
+template <int D>
+__global__ void k_gtable_prom_combine(GCtx c, const int* roots_list, long long nroots, long long ncells,
+                                      const int* members, const long long* toff, Tables Tnew, GFlat f)
+{
+    const TermRecs& R = c.R;
+    for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < ncells;
+         x += (long long)gridDim.x * blockDim.x) {
+        const long long ri = last_le(f.pr_coff, nroots, x);
+        const long long r = roots_list[ri];
+        const int m = R.m[r];
+        const int top = 1 << (m - 1), rev = (1 << m) - 1;
+        const int nR = f.pr_cells[ri];
+        const int k = (int)(x - f.pr_coff[ri]);
+        const long long base = f.pr_ioff[ri];
+        const int* okeys = Tnew.keys + toff[r];
+        const int nm = f.pr_mcnt[ri];
+        const long long mb = f.pr_mb[ri];
+        const int bi = okeys[k];
+        cd acc = Tnew.vals[toff[r] + k];  // the promoted root's value
+        for (int jj = 0; jj < nm; jj++) {
+            if (!f.mflag[mb + jj]) continue;
+            const int info = f.minfo[mb + jj];
+            const int sig = info & 0xffff;
+            const int sigf = (sig & top) ? (sig ^ rev) : sig;
+            const int t = bi ^ sig;
+            const bool cj = t & top;
+            const int bj = cj ? (t ^ rev) : t;
+            int idx;
+            if (info & kInfoOwn) {
+                if (bj < 0 || bj >= (1 << m)) continue;
+                const int fam = R.fam[members[mb + jj]];
+                idx = bsearch_key_xor(c.Bkeys + c.P.B_off[fam], c.P.B_cnt[fam], bj, c.P.bflip[fam]);
+            } else {
+                idx = (bj == (bi ^ sigf)) ? k : bsearch_key(okeys, nR, bj ^ sigf);
+            }
+            if (idx < 0) continue;
+            const cd v = f.pr_gv[base + (long long)jj * nR + idx];
+            acc = cadd(acc, cj ? cconj(v) : v);
+        }
+        Tnew.vals[toff[r] + k] = acc;
     }
 }
 
@@ -2097,8 +2225,24 @@ void Kernels<D>::gtable(TermRecs R, const int* roots_list, long long nroots, con
     if (max_warps > 0 && (long long)grid * warps > max_warps) grid = (int)(max_warps / warps);
     ++g_launches;
     k_gtable<D><<<grid, warps * 32, sm, c.stream>>>(ctx, roots_list, nroots, gcnt, goff, members, gscale, toff, Tnew,
-                                                    tcnt, alive, src, scratch, scratch_per_warp, f.rflag, f.ioff,
-                                                    f.gnr, f.minfo, f.mflag, f.gv, err);
+                                                    tcnt, alive, src, scratch, scratch_per_warp, f.rflag, f.gnr,
+                                                    f.pr_root, f.pr_mb, f.pr_mcnt, f.pr_cells, f.pr_items, err);
+}
+
+template <int D>
+void Kernels<D>::gtable_promoted(TermRecs R, const int* roots_list, long long nroots, long long nmem, long long nitems,
+                                 long long ncells, const int* members, ParentList P, Tables Told, const int* Bkeys,
+                                 const double* gscale, const long long* toff, Tables Tnew, const GFlat& f, int MC,
+                                 const LaunchCfg& c)
+{
+    if (nitems == 0) return;
+    GCtx ctx{R, P, Told, Bkeys, MC};
+    g_launches += 3;
+    k_gtable_prom_prep<D><<<grid_for(nmem, 128, c.num_sms, 8), 128, 0, c.stream>>>(ctx, nroots, nmem, members, f);
+    k_gtable_prom_eval<D><<<grid_for(nitems, 128, c.num_sms, 16), 128, 0, c.stream>>>(
+        ctx, roots_list, nroots, nitems, members, gscale, toff, Tnew, f);
+    k_gtable_prom_combine<D><<<grid_for(ncells, 128, c.num_sms, 8), 128, 0, c.stream>>>(
+        ctx, roots_list, nroots, ncells, members, toff, Tnew, f);
 }
 
 template <int D>

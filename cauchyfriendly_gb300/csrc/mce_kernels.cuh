@@ -107,6 +107,11 @@ struct Kernels {
                        const double* gscale, const long long* toff, Tables Tnew, int* tcnt, int* alive,
                        int* src, cd* scratch, long long scratch_per_warp, const GFlat& f, int MC, int* err,
                        const LaunchCfg& c, long long max_warps = 0);
+    // the members left after promotions (GFlat::pr_*), a flat pass
+    static void gtable_promoted(TermRecs R, const int* roots_list, long long nroots, long long nmem,
+                                long long nitems, long long ncells, const int* members, ParentList P, Tables Told,
+                                const int* Bkeys, const double* gscale, const long long* toff, Tables Tnew,
+                                const GFlat& f, int MC, const LaunchCfg& c);
     static void gtable_prep(TermRecs R, const int* roots_list, long long nroots, const int* gcnt,
                             const long long* goff, const int* members, ParentList P, Tables Told, const int* Bkeys,
                             const long long* toff, Tables Tnew, const GFlat& f, int* gitems, int* gcells, int MC,

@@ -116,9 +116,9 @@ def test_batched_matches_golden_per_estimator():
         G.compare_records(got, want)
 
 
-def _oracle_records(prob, rp, bp):
+def _oracle_records(prob, rp, bp, terms_upto=0):
     est = oracle.Oracle(prob, rp, bp)
-    r = oracle.run(est, prob, 0)
+    r = oracle.run(est, prob, terms_upto)
     n = est.post_mu_terms()
     est.close()
     return r, n
@@ -135,6 +135,19 @@ def test_batched_random_three_state_against_oracle():
         want_total += n
         G.compare_records(got, want, check_terms=False)
     assert total == want_total
+
+
+def test_batched_tables_against_oracle_with_promoted_roots():
+    """Every term's g-table against the oracle for a batch in which many
+    reduction groups lose their root to the term approximation and promote a
+    member (the promoted-root flat pass takes the members left after it)."""
+    from cauchyfriendly_gb300 import workloads as W
+    probs = W.batched_three_state(32, seed=4, steps_lo=6, steps_hi=8)
+    consts = [oracle.draw_reference_constants(300 + i, 3, oracle.max_shape_of(p)) for i, p in enumerate(probs)]
+    recs, _ = _batch_run_compare(probs, consts, check_terms=True)
+    for prob, c, got in zip(probs, consts, recs):
+        want, _ = _oracle_records(prob, *c, terms_upto=10**9)
+        G.compare_records(got, want, check_terms=True)
 
 
 @pytest.mark.parametrize("steps", [10])
