@@ -541,6 +541,7 @@ def main():
         kstats[g] = (ms.value, nl.value)
     dev_ms = dev_ms_total / args.steps
     wall_s = sum(walls) / args.steps
+    host_ms = {k: lib.mce_host_time_ms(est._h, i) / args.steps for i, k in enumerate(("step", "pack", "checks"))}
     if world > 1:
         import torch.distributed as dist
         t = torch.tensor([dev_ms, wall_s], device="cuda", dtype=torch.float64)
@@ -582,6 +583,7 @@ def main():
                                                                        + B["H"].nbytes + B["gamma"].nbytes),
                 "d2h_bytes_per_step": int(B["steps"].sum() * (2 + 2 * 3 + 2 * 9) * 8), "wall_s_per_step": wall_s},
         "gpu_launches": launches,
+        "host_ms_per_step": {k: round(v, 3) for k, v in host_ms.items()},
         "kernel_time_share": share,
         "alg_per_pass": alg_per_pass,
         "roofline": roofline,

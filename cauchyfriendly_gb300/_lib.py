@@ -54,6 +54,7 @@ SIGNATURES = {
     "mce_num_terms": (ctypes.c_longlong, [_vp, ctypes.c_int]),
     "mce_terms_per_shape": (ctypes.c_int, [_vp, ctypes.c_int, _ip, ctypes.c_int]),
     "mce_post_mu_terms": (ctypes.c_longlong, [_vp]),
+    "mce_host_time_ms": (ctypes.c_double, [_vp, ctypes.c_int]),
     "mce_master_step": (ctypes.c_int, [_vp]),
     "mce_device_errors": (ctypes.c_int, [_vp]),
     "mce_total_cells": (ctypes.c_longlong, [_vp, ctypes.c_int]),

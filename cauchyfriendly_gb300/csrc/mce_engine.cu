@@ -14,12 +14,17 @@
 #include "../../include/mce_c_api.h"
 
 #include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #ifndef MCE_ONLY_DIM
@@ -145,6 +150,75 @@ static int cov_flags(const double* cre, const double* cim, int d)
     return f;
 }
 
+// Host threads for the per-estimator host work of a step (input packing and
+// the moment checks of finalize/moments_numerical_check), which is
+// independent per estimator: run(n, f) calls f(a, b) on contiguous ranges
+// covering [0, n), one on the calling thread, and returns when all are done.
+class HostPool {
+public:
+    explicit HostPool(int workers)
+    {
+        for (int i = 0; i < workers; i++) th_.emplace_back([this, i] { loop(i + 1); });
+    }
+    ~HostPool()
+    {
+        {
+            std::lock_guard<std::mutex> l(m_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (std::thread& t : th_) t.join();
+    }
+    void run(int n, const std::function<void(int, int)>& f)
+    {
+        const int parts = (int)th_.size() + 1;
+        {
+            std::lock_guard<std::mutex> l(m_);
+            job_ = &f;
+            n_ = n;
+            pending_ = (int)th_.size();
+            gen_++;
+        }
+        cv_.notify_all();
+        part(0, parts, n, f);
+        std::unique_lock<std::mutex> l(m_);
+        done_.wait(l, [this] { return pending_ == 0; });
+    }
+
+private:
+    static void part(int k, int parts, int n, const std::function<void(int, int)>& f)
+    {
+        const int a = (int)((long long)n * k / parts), b = (int)((long long)n * (k + 1) / parts);
+        if (a < b) f(a, b);
+    }
+    void loop(int k)
+    {
+        long long seen = 0;
+        for (;;) {
+            const std::function<void(int, int)>* f;
+            int n;
+            {
+                std::unique_lock<std::mutex> l(m_);
+                cv_.wait(l, [&] { return stop_ || gen_ != seen; });
+                if (stop_) return;
+                seen = gen_;
+                f = job_;
+                n = n_;
+            }
+            part(k, (int)th_.size() + 1, n, *f);
+            std::lock_guard<std::mutex> l(m_);
+            if (--pending_ == 0) done_.notify_one();
+        }
+    }
+    std::vector<std::thread> th_;
+    std::mutex m_;
+    std::condition_variable cv_, done_;
+    const std::function<void(int, int)>* job_ = nullptr;
+    int n_ = 0, pending_ = 0;
+    long long gen_ = 0;
+    bool stop_ = false;
+};
+
 enum KernelGroup {
     KID_FIRST = 0, KID_TP, KID_BUILD_B, KID_MU, KID_MOMENTS, KID_FTR, KID_GROUPS, KID_GTABLE, KID_PARTITION,
     KID_SCAN, KID_COUNT
@@ -216,6 +290,20 @@ public:
     size_t gtable_scratch_bytes_per_warp() const { return sizeof(cd) * (size_t)half_cells_cap(MC, d); }
     int master_step = 0;
     int device_errors = 0;
+    // host wall time of the steps (ms): whole step, input packing, moment checks
+    double host_ms[3] = {0, 0, 0};
+    // per-estimator host work, split over host threads for large batches
+    std::unique_ptr<HostPool> pool;
+    void for_estimators(const std::function<void(int, int)>& f)
+    {
+        if (E >= 256 && !pool) {
+            const unsigned hw = std::thread::hardware_concurrency();
+            const int workers = (int)std::min<unsigned>(hw > 1 ? hw - 1 : 0, 15);
+            if (workers > 0) pool.reset(new HostPool(workers));
+        }
+        if (pool && E >= 256) pool->run(E, f);
+        else f(0, E);
+    }
     long long post_mu_terms = 0;
     double last_ms = 0;
     // profiling: per-kernel-group device time (CUDA events on the engine's
@@ -230,6 +318,7 @@ public:
     void clear_prof()
     {
         device_ms_total = 0;
+        host_ms[0] = host_ms[1] = host_ms[2] = 0;
         launches = 0;
         for (int k = 0; k < KID_COUNT; k++) {
             kms[k] = 0;
@@ -680,6 +769,8 @@ public:
     int step(const double* msmt, const double* Phi, const double* Gamma, const double* beta, const double* H,
              const double* gamma, const double* B, const double* u, int shared, int* err_out) override
     {
+        using clk = std::chrono::steady_clock;
+        const auto t0 = clk::now();
         const int ms = master_step;
         const int sub = ms % p;
         const bool with_tp = sub == 0;
@@ -688,13 +779,20 @@ public:
             const EstHost& h = est[e];
             const bool done = ms >= h.num_updates;
             const bool blocked = (h.errors >> E_FZ_NEG) & 1;
-            const bool active = !done && !blocked;
-            const bool skip = active && ms == h.num_updates - 1;
-            const size_t oe = shared ? 0 : (size_t)e;
-            pack(e, msmt[e], Phi + oe * D * D, Gamma + oe * D * pncc, beta + oe * pncc, H + (size_t)e * D, gamma[e],
-                 B ? B + oe * D * cmcc : nullptr, u ? u + (size_t)e * cmcc : nullptr, active, skip);
-            any_active |= active;
+            any_active |= !done && !blocked;
         }
+        for_estimators([&](int a, int b) {
+            for (int e = a; e < b; e++) {
+                const EstHost& h = est[e];
+                const bool done = ms >= h.num_updates;
+                const bool blocked = (h.errors >> E_FZ_NEG) & 1;
+                const bool active = !done && !blocked;
+                const bool skip = active && ms == h.num_updates - 1;
+                const size_t oe = shared ? 0 : (size_t)e;
+                pack(e, msmt[e], Phi + oe * D * D, Gamma + oe * D * pncc, beta + oe * pncc, H + (size_t)e * D,
+                     gamma[e], B ? B + oe * D * cmcc : nullptr, u ? u + (size_t)e * cmcc : nullptr, active, skip);
+            }
+        });
         bool any_done_past = true;
         for (int e = 0; e < E; e++)
             if (ms < est[e].num_updates) any_done_past = false;
@@ -704,6 +802,7 @@ public:
         }
         MCE_CUDA(cudaMemcpyAsync(dsteps.ptr, hsteps.data(), sizeof(EstStep<D>) * E, cudaMemcpyHostToDevice,
                                  lc.stream));
+        const auto t1 = clk::now();
         MCE_CUDA(cudaEventRecord(ev0, lc.stream));
         int rc = any_active ? (ms == 0 ? step_first() : step_main(with_tp)) : MCE_OK;
         if (rc != MCE_OK) return rc;
@@ -716,7 +815,12 @@ public:
         device_ms_total += msf;
         collect_prof();
         // moments of every active estimator
+        const auto t2 = clk::now();
         finish_moments(ms);
+        const auto t3 = clk::now();
+        host_ms[0] += std::chrono::duration<double, std::milli>(t3 - t0).count();
+        host_ms[1] += std::chrono::duration<double, std::milli>(t1 - t0).count();
+        host_ms[2] += std::chrono::duration<double, std::milli>(t3 - t2).count();
         master_step++;
         if (err_out)
             for (int e = 0; e < E; e++) err_out[e] = est[e].errors;
@@ -725,8 +829,13 @@ public:
 
     void finish_moments(int ms)
     {
+        for_estimators([&](int a, int b) { finish_moments_range(ms, a, b); });
+    }
+
+    void finish_moments_range(int ms, int a, int b)
+    {
         const int NM = 1 + D + D * D;
-        for (int e = 0; e < E; e++) {
+        for (int e = a; e < b; e++) {
             const EstStep<D>& S = hsteps[e];
             if (!S.active) continue;
             EstHost& h = est[e];
@@ -2227,6 +2336,7 @@ double mce_rel2d_device_ms(mce_rel2d* r, int which) { return r && which >= 0 && 
 long long mce_rel2d_launch_count(mce_rel2d* r) { return r ? r->launches : MCE_ERR_ARG; }
 void mce_rel2d_destroy(mce_rel2d* r) { delete r; }
 long long mce_post_mu_terms(mce_handle* h) { return h ? h->eng->post_mu_terms : MCE_ERR_ARG; }
+double mce_host_time_ms(mce_handle* h, int which) { return h && which >= 0 && which < 3 ? h->eng->host_ms[which] : -1.0; }
 int mce_master_step(mce_handle* h) { return h ? h->eng->master_step : MCE_ERR_ARG; }
 int mce_device_errors(mce_handle* h) { return h ? h->eng->device_errors : MCE_ERR_ARG; }
 long long mce_total_cells(mce_handle* h, int e) { return bad(h, e) ? MCE_ERR_ARG : h->eng->total_cells(e); }

@@ -212,6 +212,10 @@ double mce_rel2d_device_ms(mce_rel2d* r, int which);
 long long mce_rel2d_launch_count(mce_rel2d* r);
 void mce_rel2d_destroy(mce_rel2d* r);
 
+/* Host wall time (ms) of the steps since the last mce_clear_profile: which = 0
+ * whole steps, 1 input packing, 2 the moment checks after the device work. */
+double mce_host_time_ms(mce_handle* h, int which);
+
 /* Sum over all updates and estimators of the terms present after each MU. */
 long long mce_post_mu_terms(mce_handle* h);
 int mce_master_step(mce_handle* h);
