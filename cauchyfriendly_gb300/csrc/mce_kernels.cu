@@ -595,17 +595,12 @@ __global__ void k_build_B(ParentList P, long long nP, const EstStep<D>* st, int 
 // MU coalignment of one staged child (cauchy_term.hpp:533-745), in place on
 // the lane's shared-memory rows.  Returns the new row count.
 template <int D>
+// The coalignment of mu_coalign after its normalize_hps(true) (the caller
+// normalises the rows: the parent's record takes the same normalisation, so
+// parents and children of one warp share those instructions).
 __device__ inline int mu_coalign_smem(double* A, double* p, double* q, int m, unsigned& hof, signed char* cmap,
                                       signed char* csmap, int* err)
 {
-    // normalize_hps(true): q keeps the un-normalised scales
-    for (int i = 0; i < m; i++) {
-        q[i] = p[i];
-        double n1 = 0;
-        for (int j = 0; j < D; j++) n1 += fabs(A[i * D + j]);
-        p[i] *= n1;
-        for (int j = 0; j < D; j++) A[i * D + j] /= n1;
-    }
     unsigned F = (m >= 32) ? kFull : ((1u << m) - 1);
     unsigned hf = hof;
     for (int j = 0; j < m; j++) {
@@ -863,16 +858,16 @@ __global__ void __launch_bounds__(128) k_mu_terms(ParentList P, long long nP, co
         }
         int mfin = m;
         int flags = (t == m) ? 0 : kFlagNewChild;
-        if (t == m) {
-            // parent: normalize_hps(true), no coalignment
-            for (int r = 0; r < m; r++) {
-                qt[r] = pt[r];
-                double n1 = 0;
-                for (int j = 0; j < D; j++) n1 += fabs(At[r * D + j]);
-                pt[r] *= n1;
-                for (int j = 0; j < D; j++) At[r * D + j] /= n1;
-            }
-        } else {
+        // normalize_hps(true) (cauchy_term.hpp:458-472): q keeps the
+        // un-normalised scales; the parent stops there, a child is coaligned
+        for (int r = 0; r < m; r++) {
+            qt[r] = pt[r];
+            double n1 = 0;
+            for (int j = 0; j < D; j++) n1 += fabs(At[r * D + j]);
+            pt[r] *= n1;
+            for (int j = 0; j < D; j++) At[r * D + j] /= n1;
+        }
+        if (t != m) {
             mfin = mu_coalign_smem<D>(At, pt, qt, m, hof, R.cmap + slot * MC, R.csmap + slot * MC, err);
             if (mfin != m) flags |= kFlagHasCmap;
         }
