@@ -14,6 +14,7 @@
 #include "../../include/mce_c_api.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <functional>
@@ -152,13 +153,16 @@ static int cov_flags(const double* cre, const double* cim, int d)
 
 // Host threads for the per-estimator host work of a step (input packing and
 // the moment checks of finalize/moments_numerical_check), which is
-// independent per estimator: run(n, f) calls f(a, b) on contiguous ranges
-// covering [0, n), one on the calling thread, and returns when all are done.
+// independent per estimator: run(n, f) calls f(a, b) on contiguous chunks
+// covering [0, n) and returns when all are done.  Chunks are claimed
+// dynamically (the calling thread takes part), so a worker that wakes late
+// only finds fewer chunks left; a claim names the job's generation, so a late
+// worker never takes a chunk of a later job.
 class HostPool {
 public:
     explicit HostPool(int workers)
     {
-        for (int i = 0; i < workers; i++) th_.emplace_back([this, i] { loop(i + 1); });
+        for (int i = 0; i < workers; i++) th_.emplace_back([this] { loop(); });
     }
     ~HostPool()
     {
@@ -172,50 +176,69 @@ public:
     void run(int n, const std::function<void(int, int)>& f)
     {
         const int parts = (int)th_.size() + 1;
+        int chunk = n / (4 * parts);
+        if (chunk < 32) chunk = 32;
+        const int nch = (n + chunk - 1) / chunk;
+        unsigned long long g;
         {
             std::lock_guard<std::mutex> l(m_);
+            g = ++gen_;
             job_ = &f;
             n_ = n;
-            pending_ = (int)th_.size();
-            gen_++;
+            chunk_ = chunk;
+            nch_ = nch;
+            done_.store(0);
+            claim_.store(g << 32);
         }
         cv_.notify_all();
-        part(0, parts, n, f);
-        std::unique_lock<std::mutex> l(m_);
-        done_.wait(l, [this] { return pending_ == 0; });
+        work(g, &f, n, chunk, nch);
+        while (done_.load() < nch) std::this_thread::yield();
     }
 
 private:
-    static void part(int k, int parts, int n, const std::function<void(int, int)>& f)
+    void work(unsigned long long g, const std::function<void(int, int)>* f, int n, int chunk, int nch)
     {
-        const int a = (int)((long long)n * k / parts), b = (int)((long long)n * (k + 1) / parts);
-        if (a < b) f(a, b);
-    }
-    void loop(int k)
-    {
-        long long seen = 0;
         for (;;) {
+            unsigned long long w = claim_.load();
+            int c;
+            do {
+                if ((w >> 32) != g) return;
+                c = (int)(w & 0xffffffffull);
+                if (c >= nch) return;
+            } while (!claim_.compare_exchange_weak(w, w + 1));
+            const int a = c * chunk, b = a + chunk < n ? a + chunk : n;
+            (*f)(a, b);
+            done_.fetch_add(1);
+        }
+    }
+    void loop()
+    {
+        unsigned long long seen = 0;
+        for (;;) {
+            unsigned long long g;
             const std::function<void(int, int)>* f;
-            int n;
+            int n, chunk, nch;
             {
                 std::unique_lock<std::mutex> l(m_);
                 cv_.wait(l, [&] { return stop_ || gen_ != seen; });
                 if (stop_) return;
-                seen = gen_;
+                seen = g = gen_;
                 f = job_;
                 n = n_;
+                chunk = chunk_;
+                nch = nch_;
             }
-            part(k, (int)th_.size() + 1, n, *f);
-            std::lock_guard<std::mutex> l(m_);
-            if (--pending_ == 0) done_.notify_one();
+            work(g, f, n, chunk, nch);
         }
     }
     std::vector<std::thread> th_;
     std::mutex m_;
-    std::condition_variable cv_, done_;
+    std::condition_variable cv_;
     const std::function<void(int, int)>* job_ = nullptr;
-    int n_ = 0, pending_ = 0;
-    long long gen_ = 0;
+    int n_ = 0, chunk_ = 1, nch_ = 0;
+    unsigned long long gen_ = 0;
+    std::atomic<unsigned long long> claim_{0};
+    std::atomic<int> done_{0};
     bool stop_ = false;
 };
 

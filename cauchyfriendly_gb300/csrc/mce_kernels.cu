@@ -756,15 +756,27 @@ __global__ void __launch_bounds__(128) k_mu_terms(ParentList P, long long nP, co
     double* qt = pt + MC;
     for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < nterms;
          x += (long long)gridDim.x * blockDim.x) {
-        // the family: the last parent i with i + kall_scan[i] <= x
-        long long lo = 0, hi = nP;
-        while (hi - lo > 1) {
-            const long long mid = (lo + hi) >> 1;
-            if (mid + kall_scan[mid] <= x) lo = mid;
-            else hi = mid;
+        // threads [0, nP) take the parents, the rest the children in order,
+        // so a warp runs either the parent path or the coalignment of children
+        long long i;
+        int ford;  // 0: the parent, c + 1: child c
+        if (x < nP) {
+            i = x;
+            ford = 0;
+        } else {
+            // the family of child cidx: the last parent i with kall_scan[i] <= cidx
+            const long long cidx = x - nP;
+            long long lo = 0, hi = nP;
+            while (hi - lo > 1) {
+                const long long mid = (lo + hi) >> 1;
+                if (kall_scan[mid] <= cidx) lo = mid;
+                else hi = mid;
+            }
+            i = lo;
+            ford = (int)(cidx - kall_scan[i]) + 1;
         }
-        const long long i = lo;
-        const int ford = (int)(x - (i + kall_scan[i]));  // 0: the parent, c + 1: child c
+        // the term's position in the reference's order (parent, then its children)
+        const long long xo = i + kall_scan[i] + ford;
         const int e = P.est[i];
         const EstStep<D>& S = st[e];
         const int m = P.m[i], phc = P.m_old[i];
@@ -836,7 +848,7 @@ __global__ void __launch_bounds__(128) k_mu_terms(ParentList P, long long nP, co
         const double dv = rho[t];
         cd g = csub(cdiv(gp, mkcd(ygi + dv, zeta)), cdiv(gm, mkcd(ygi - dv, zeta)));
         g = cscale(g, kTwoPiInv);
-        cd* cs = contrib + x * NM;
+        cd* cs = contrib + xo * NM;
         cs[0] = g;
         for (int j = 0; j < D; j++) {
             const cd y = mkcd(-ty[j], bt[j]);
