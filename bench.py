@@ -175,6 +175,21 @@ def profile_figures():
     return out
 
 
+def combine_ranks(dev_ms, wall_s, terms, device):
+    """Whole-job figures of a replicas run (one independent batch per rank, no
+    data-path collective): the slowest rank's device and wall times per pass
+    and the terms all ranks processed.  A single process returns its own."""
+    import torch
+    import torch.distributed as dist
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return dev_ms, wall_s, terms
+    t = torch.tensor([dev_ms, wall_s], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    n = torch.tensor([float(terms)], device=device, dtype=torch.float64)
+    dist.all_reduce(n, op=dist.ReduceOp.SUM)
+    return float(t[0]), float(t[1]), int(round(float(n[0])))
+
+
 def cpu_sample(probs, consts, target_seconds):
     """Bounded sample of the same workload for the CPU baseline: every k-th
     estimator, k chosen so the oracle port needs about target_seconds."""
@@ -542,12 +557,7 @@ def main():
     dev_ms = dev_ms_total / args.steps
     wall_s = sum(walls) / args.steps
     host_ms = {k: lib.mce_host_time_ms(est._h, i) / args.steps for i, k in enumerate(("step", "pack", "checks"))}
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([dev_ms, wall_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_ms, wall_s = float(t[0]), float(t[1])
-    total_terms = terms_per_pass * world
+    dev_ms, wall_s, total_terms = combine_ranks(dev_ms, wall_s, terms_per_pass, "cuda")
     value = total_terms / (dev_ms / 1e3)
     e2e = total_terms / wall_s
     # roofline of the dominant kernel group (largest device time)
