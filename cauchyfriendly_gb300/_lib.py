@@ -63,6 +63,7 @@ SIGNATURES = {
     "mce_reinitialize_start_statistics": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp]),
     "mce_set_master_step": (ctypes.c_int, [_vp, ctypes.c_int]),
     "mce_set_window_number": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "mce_set_print_basic_info": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
     "mce_last_step_ms": (ctypes.c_double, [_vp]),
     "mce_device_time_ms": (ctypes.c_double, [_vp]),
     "mce_launch_count": (ctypes.c_longlong, [_vp]),

@@ -265,6 +265,9 @@ struct EstHost {
     long long nt = 1;
     std::vector<int> tps;
     int win_num = 0;
+    // the constructor's print_basic_info: the moments reported after each
+    // table build are those of compute_moments(false)
+    bool print_basic_info = false;
 };
 
 class EngineBase {
@@ -477,6 +480,13 @@ public:
         }
     } Rb;
     DevBuf<cd> fam_mom, est_raw, scratch, g_vals, pr_gv;
+    // post-FTR moments (print_basic_info): rows, chain totals, results
+    DevBuf<cd> pf_rows, pf_raw;
+    DevBuf<double> pf_tot, pf_gscale;
+    DevBuf<long long> pf_zero;
+    std::vector<cd> h_pf_raw;
+    std::vector<double> h_pf_gscale;
+    bool have_post = false;
     DevBuf<int> pr_root, pr_mb, pr_mcnt, pr_cells, pr_items;
     DevBuf<long long> pr_moff, pr_ioff, pr_coff;
     DevBuf<int> ftr_wl[2], ftr_resume;
@@ -826,6 +836,7 @@ public:
         MCE_CUDA(cudaMemcpyAsync(dsteps.ptr, hsteps.data(), sizeof(EstStep<D>) * E, cudaMemcpyHostToDevice,
                                  lc.stream));
         const auto t1 = clk::now();
+        have_post = false;
         MCE_CUDA(cudaEventRecord(ev0, lc.stream));
         int rc = any_active ? (ms == 0 ? step_first() : step_main(with_tp)) : MCE_OK;
         if (rc != MCE_OK) return rc;
@@ -878,23 +889,49 @@ public:
             h.fz[1] = h.raw_fz[1];
             h.mean = h.raw_mean;
             h.cov = h.raw_cov;
+            const bool post = have_post && h.print_basic_info;
             if (ms == 0) {
                 // step_first reports through compute_moments without the checks
+                if (post) post_ftr_report(h, e);
+                else {
+                    h.fz[0] = 1;
+                    h.fz[1] = 0;
+                }
                 h.last_mean = h.mean;
                 h.last_cov = h.cov;
-                h.fz[0] = 1;
-                h.fz[1] = 0;
-                h.last_fz[0] = 1;
-                h.last_fz[1] = 0;
+                h.last_fz[0] = h.fz[0];
+                h.last_fz[1] = h.fz[1];
                 continue;
             }
             numeric_check(h, ms);
             if (!S.skip) {
-                // fz is set to 1 after the tables are rebuilt (cauchy_estimator.hpp:1172-1176)
-                h.fz[0] = 1;
-                h.fz[1] = 0;
+                // after the tables are rebuilt fz is set to 1, or, with
+                // print_basic_info, compute_moments(false) replaces fz, the
+                // moments and G_SCALE_FACTOR (cauchy_estimator.hpp:1166-1177)
+                if (post) post_ftr_report(h, e);
+                else {
+                    h.fz[0] = 1;
+                    h.fz[1] = 0;
+                }
             }
         }
+    }
+
+    void post_ftr_report(EstHost& h, int e)
+    {
+        const int NM = 1 + D + D * D;
+        const cd* r = &h_pf_raw[(size_t)e * NM];
+        h.fz[0] = r[0].re;
+        h.fz[1] = r[0].im;
+        for (int j = 0; j < D; j++) {
+            h.mean[2 * j] = r[1 + j].re;
+            h.mean[2 * j + 1] = r[1 + j].im;
+        }
+        for (int j = 0; j < D * D; j++) {
+            h.cov[2 * j] = r[1 + D + j].re;
+            h.cov[2 * j + 1] = r[1 + D + j].im;
+        }
+        h.gscale = h_pf_gscale[e];
     }
 
     void numeric_check(EstHost& h, int ms)
@@ -1000,7 +1037,7 @@ public:
             est[e].tps[D] = cnt[e];
             post_mu_terms += cnt[e];
         }
-        return MCE_OK;
+        return post_ftr_moments(true);
     }
 
     void k_gscale_from_raw(int E_);
@@ -1328,6 +1365,38 @@ public:
                                  lc.stream));
         nP = nPn;
         cur ^= 1;
+        return post_ftr_moments(false);
+    }
+
+    // compute_moments(false) for the estimators that set print_basic_info
+    // (cauchy_estimator.hpp:1166-1177, 1197-1203) over the current terms
+    int post_ftr_moments(bool first)
+    {
+        have_post = false;
+        bool any = false;
+        for (int e = 0; e < E; e++)
+            if (est[e].print_basic_info && hsteps[e].active && (first || !hsteps[e].skip)) any = true;
+        if (!any) return MCE_OK;
+        constexpr int NM = 1 + D + D * D;
+        int s;
+        if ((s = pf_rows.ensure((size_t)(nP + 1) * NM))) return s;
+        if ((s = pf_zero.ensure(nP + 2))) return s;
+        if ((s = pf_tot.ensure((size_t)E * 2 * NM))) return s;
+        if ((s = pf_raw.ensure((size_t)E * NM))) return s;
+        if ((s = pf_gscale.ensure(E))) return s;
+        MCE_CUDA(cudaMemsetAsync(pf_zero.ptr, 0, sizeof(long long) * (nP + 2), lc.stream));
+        Kernels<D>::post_ftr_terms(Pb[cur].view(), nP, droots.ptr, Tables{Tb[cur].keys.ptr, Tb[cur].vals.ptr}, MC,
+                                   pf_rows.ptr, lc);
+        Kernels<D>::moments(pf_rows.ptr, dpstart.ptr, pf_zero.ptr, E, dsteps.ptr, pf_tot.ptr, pf_raw.ptr,
+                            pf_gscale.ptr, lc);
+        h_pf_raw.resize((size_t)E * NM);
+        h_pf_gscale.resize(E);
+        MCE_CUDA(cudaMemcpyAsync(h_pf_raw.data(), pf_raw.ptr, sizeof(cd) * E * NM, cudaMemcpyDeviceToHost,
+                                 lc.stream));
+        MCE_CUDA(cudaMemcpyAsync(h_pf_gscale.data(), pf_gscale.ptr, sizeof(double) * E, cudaMemcpyDeviceToHost,
+                                 lc.stream));
+        MCE_CUDA(cudaStreamSynchronize(lc.stream));
+        have_post = true;
         return MCE_OK;
     }
 
@@ -2384,6 +2453,17 @@ int mce_set_master_step(mce_handle* h, int ms)
 {
     if (!h || ms < 0) return MCE_ERR_ARG;
     h->eng->master_step = ms;
+    return MCE_OK;
+}
+int mce_set_print_basic_info(mce_handle* h, int e, int on)
+{
+    if (!h) return MCE_ERR_ARG;
+    if (e < 0) {
+        for (auto& s : h->eng->est) s.print_basic_info = on != 0;
+        return MCE_OK;
+    }
+    if (bad(h, e)) return MCE_ERR_ARG;
+    h->eng->est[e].print_basic_info = on != 0;
     return MCE_OK;
 }
 int mce_set_window_number(mce_handle* h, int w)

@@ -2849,6 +2849,54 @@ __global__ void __launch_bounds__(128) k_rel2d_pairs(Rel2DArgs a)
     }
 }
 
+// compute_moments(false) (cauchy_estimator.hpp:524-602), the moments of the
+// reduced terms after the table build when print_basic_info is set: a thread
+// per term, eval_g_yei_after_ftr (cauchy_term.hpp:403-433) -- the rows' signs
+// at the root point (0 counts as negative), the term's table value there,
+// yei = -sum p_l s_l A_l + i b -- into a moment row laid out as k_mu_terms
+// writes them (g, g y_j, g y_j y_k), for the same chain and finalisation.
+template <int D>
+__global__ void k_post_ftr_terms(ParentList P, long long nP, const double* roots, Tables T, int MC, cd* contrib)
+{
+    constexpr int NM = 1 + D + D * D;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nP;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int e = P.est[i];
+        const int m = P.m[i];
+        const double* A = P.A + i * MC * D;
+        const double* p = P.p + i * MC;
+        const double* root = roots + (long long)e * D;
+        int enc = 0;
+        double ty[D];
+        for (int j = 0; j < D; j++) ty[j] = 0;
+        for (int l = 0; l < m; l++) {
+            double s = 0.0;
+            for (int j = 0; j < D; j++) s += A[l * D + j] * root[j];
+            const bool sp = s > 0;
+            const double sc = sp ? p[l] : -p[l];  // p_l * sign, exact
+            for (int j = 0; j < D; j++) ty[j] += sc * A[l * D + j];
+            if (!sp) enc |= 1 << l;
+        }
+        const cd g = lookup_num(T.keys + P.tab_off[i], T.vals + P.tab_off[i], P.tab_cnt[i], enc, m);
+        cd* cs = contrib + i * NM;
+        cs[0] = g;
+        for (int j = 0; j < D; j++) {
+            const cd gy = cmul(g, mkcd(-ty[j], P.b[i * D + j]));
+            cs[1 + j] = gy;
+            for (int k = 0; k < D; k++) cs[1 + D + j * D + k] = cmul(gy, mkcd(-ty[k], P.b[i * D + k]));
+        }
+    }
+}
+
+template <int D>
+void Kernels<D>::post_ftr_terms(ParentList P, long long nP, const double* roots, Tables T, int MC, cd* contrib,
+                                const LaunchCfg& c)
+{
+    if (nP == 0) return;
+    ++g_launches;
+    k_post_ftr_terms<D><<<grid_for(nP, 128, c.num_sms, 16), 128, 0, c.stream>>>(P, nP, roots, T, MC, contrib);
+}
+
 template <int D>
 void Kernels<D>::rel2d_pairs(const Rel2DArgs& a, const LaunchCfg& c)
 {

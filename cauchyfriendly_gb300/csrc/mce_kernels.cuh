@@ -131,6 +131,9 @@ struct Kernels {
                             const long long* goff, const int* members, ParentList P, Tables Told, const int* Bkeys,
                             const double* gscale, const long long* toff, Tables Tnew, const GFlat& f, int MC,
                             const LaunchCfg& c);
+    // Moment rows of the current (reduced) terms, compute_moments(false).
+    static void post_ftr_terms(ParentList P, long long nP, const double* roots, Tables T, int MC, cd* contrib,
+                               const LaunchCfg& c);
     // One relative 2-D term per (primary term, secondary term) pair: its
     // cache row, kept flag and moment contributions.
     static void rel2d_pairs(const Rel2DArgs& a, const LaunchCfg& c);

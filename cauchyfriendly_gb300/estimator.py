@@ -166,6 +166,13 @@ class BatchedCauchyEstimator:
     def set_master_step(self, ms):
         _lib.check(self._lib.mce_set_master_step(self._h, int(ms)), "mce_set_master_step")
 
+    def set_print_basic_info(self, on, e=-1):
+        """The constructor's print_basic_info for estimator e (every one for
+        e < 0): after each update that rebuilds the tables the reported fz,
+        moments and G_SCALE_FACTOR are the post-reduction ones of
+        compute_moments(false) (include/cauchy_estimator.hpp:524-602)."""
+        _lib.check(self._lib.mce_set_print_basic_info(self._h, int(e), int(bool(on))), "mce_set_print_basic_info")
+
     def set_win_num(self, w):
         _lib.check(self._lib.mce_set_window_number(self._h, int(w)), "mce_set_window_number")
 
@@ -330,6 +337,8 @@ class CauchyEstimator(BatchedCauchyEstimator):
         bp = None if b_pert is None else _f64(b_pert).reshape(1, -1)
         super().__init__(A0, p0, b0, [int(steps)], d, cmcc, pncc, p, rp, bp)
         self.print_basic_info = bool(print_basic_info)
+        if self.print_basic_info:
+            self.set_print_basic_info(True)
 
     def step(self, msmt, Phi, Gamma, beta, H, gamma, B=None, u=None):
         """CauchyEstimator::step (include/cauchy_estimator.hpp:1211): returns

@@ -233,6 +233,15 @@ int mce_dump_terms(mce_handle* h, int est, int max_shape, int* shape, double* A,
 int mce_reset(mce_handle* h);
 /* reinitialize_start_statistics (include/cauchy_estimator.hpp:1302). */
 int mce_reinitialize_start_statistics(mce_handle* h, int est, const double* A0, const double* p0, const double* b0);
+/* The constructor's print_basic_info (include/cauchy_estimator.hpp:87, 165)
+ * for estimator est (est < 0: every estimator of the handle).  When set, the
+ * moments reported after each update that rebuilds the tables (and after the
+ * first update) are the post-reduction ones of compute_moments(false)
+ * (include/cauchy_estimator.hpp:524-602, 1166-1177, 1197-1203), which also
+ * replace G_SCALE_FACTOR; otherwise fz is reported as 1 there.  Nothing is
+ * printed. */
+int mce_set_print_basic_info(mce_handle* h, int est, int on);
+
 /* master_step setter used by the window manager (pycauchy.hpp:776). */
 int mce_set_master_step(mce_handle* h, int master_step);
 int mce_set_window_number(mce_handle* h, int win_num);

@@ -283,6 +283,11 @@ class Oracle(_EstimatorBase):
     def errors(self):
         return int(self._l.lib.orc_errors(self.h))
 
+    def set_print_basic_info(self, on):
+        """The constructor's print_basic_info: post-FTR moments are reported."""
+        self._l.lib.orc_set_print_basic_info.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        self._l.lib.orc_set_print_basic_info(self.h, int(bool(on)))
+
     def shift_cf_by_bias(self, bias):
         b = _arr(bias)
         self._l.lib.orc_shift_cf_by_bias.argtypes = [ctypes.c_void_p, _dp]
@@ -393,6 +398,11 @@ class Reference(_EstimatorBase):
 
     def last_step_seconds(self):
         return float(self._l.lib.ref_last_step_seconds(self.h))
+
+    def set_print_basic_info(self, on):
+        """The constructor's print_basic_info (the reference also prints its progress)."""
+        self._l.lib.ref_set_print_basic_info.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        self._l.lib.ref_set_print_basic_info(self.h, int(bool(on)))
 
     def shift_cf_by_bias(self, bias):
         b = _arr(bias)

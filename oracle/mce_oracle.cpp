@@ -367,6 +367,7 @@ struct Estimator {
     double gscale = 0;
     int errors = 0;
     bool skip_post_mu = false;
+    bool print_basic_info = false;  // compute_moments(false) after each table build
     std::vector<std::vector<int>> combos;  // per shape
     long long post_mu_terms = 0;           // sum over steps of terms after MU
     // 1-D marginal pdf cache, keyed like the reference's by (master step, index)
@@ -1152,6 +1153,41 @@ static void finalize_moments(Estimator& E)
     numeric_check(E);
 }
 
+// compute_moments(false) (cauchy_estimator.hpp:524-602), run after the
+// tables are built when print_basic_info is set: every current term in shape
+// and index order through eval_g_yei_after_ftr (cauchy_term.hpp:403-433) --
+// the sign vector of the rows at the root point (0 counts as negative), the
+// parent-table value there, yei = -sum p_l s_l A_l + i b -- summed as in
+// cache_moments, then fz, G_SCALE_FACTOR, mean and covariance replaced.
+static void post_ftr_moments(Estimator& E)
+{
+    const int d = E.d;
+    E.fz = mkc(0, 0);
+    E.mean.assign(d, mkc(0, 0));
+    E.cov.assign(d * d, mkc(0, 0));
+    for (const Term& t : E.terms) {
+        int enc = 0;
+        double ty[16] = {0};
+        for (int l = 0; l < t.m; l++) {
+            double s = 0.0;
+            for (int j = 0; j < d; j++) s += t.A[l * d + j] * E.root[j];
+            const double sg = s > 0 ? 1 : -1;
+            const double sc = t.p[l] * sg;
+            for (int j = 0; j < d; j++) ty[j] += sc * t.A[l * d + j];
+            if (sg < 0) enc |= 1 << l;
+        }
+        const cplx g = lookup_num(t.gp.get(), enc, t.m);
+        cplx y[16];
+        for (int j = 0; j < d; j++) y[j] = mkc(-ty[j], t.b[j]);
+        accumulate(E, g, y);
+    }
+    E.gscale = kTwoPiInv / __real__ E.fz;
+    cplx ifz = mkc(0, __real__ E.fz);
+    for (int i = 0; i < d; i++) E.mean[i] = cdiv(E.mean[i], ifz);
+    for (int i = 0; i < d; i++)
+        for (int j = 0; j < d; j++) E.cov[i * d + j] = cdiv(E.cov[i * d + j], E.fz) - E.mean[i] * E.mean[j];
+}
+
 static void reset_terms(Estimator& E)
 {
     E.terms.clear();
@@ -1214,7 +1250,8 @@ static void step_first(Estimator& E, double msmt, const double* H, double gamma)
     E.terms_per_shape.assign(E.shape_range, 0);
     E.terms_per_shape[d] = E.Nt;
     E.post_mu_terms += E.Nt;
-    E.fz = mkc(1, 0);
+    if (E.print_basic_info) post_ftr_moments(E);
+    else E.fz = mkc(1, 0);
     E.last_mean = E.mean;
     E.last_cov = E.cov;
     E.last_fz = E.fz;
@@ -1307,7 +1344,8 @@ static void step_rest(Estimator& E, double msmt, const double* Phi, const double
     E.terms = std::move(next);
     E.Nt = (int)E.terms.size();
     E.terms_per_shape = tps;
-    E.fz = mkc(1, 0);
+    if (E.print_basic_info) post_ftr_moments(E);
+    else E.fz = mkc(1, 0);
 }
 
 // ----------------------------------------------------------------------------
@@ -1854,6 +1892,9 @@ void orc_reinit(void* h, const double* A0, const double* p0, const double* b0)
     E.b0.assign(b0, b0 + E.d);
 }
 void orc_set_master_step(void* h, int ms) { ((Estimator*)h)->master_step = ms; }
+// print_basic_info of the constructor (cauchy_estimator.hpp:87, 165): the
+// moments reported after each table build come from compute_moments(false)
+void orc_set_print_basic_info(void* h, int on) { ((Estimator*)h)->print_basic_info = on != 0; }
 int orc_errors(void* h) { return ((Estimator*)h)->errors; }
 
 int orc_num_terms(void* h) { return ((Estimator*)h)->Nt; }

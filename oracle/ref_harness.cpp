@@ -235,6 +235,11 @@ int ref_cpdf_2d_grid(void* vh, int i1, int i2, double lx, double hx, double rx, 
     return grid.num_grid_points;
 }
 
+// The constructor's print_basic_info (include/cauchy_estimator.hpp:87, 165),
+// set after construction: the reference then reports the post-FTR moments of
+// compute_moments(false) after every table build (and prints its progress).
+void ref_set_print_basic_info(void* vh, int on) { ((RefHandle*)vh)->est->print_basic_info = on != 0; }
+
 // The reference's extended-mode helpers (include/cauchy_estimator.hpp:1312-1394).
 void ref_shift_cf_by_bias(void* vh, const double* bias) { ((RefHandle*)vh)->est->shift_cf_by_bias((double*)bias); }
 void ref_deterministic_time_prop(void* vh, const double* Phi, const double* B, const double* u)

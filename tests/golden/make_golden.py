@@ -16,6 +16,7 @@ Needs the reference sources (only present where the fixtures are made):
     python tests/golden/make_golden.py --cpdf   # the pdf fixtures only
     python tests/golden/make_golden.py --ext    # the extended-mode fixtures only
     python tests/golden/make_golden.py --rel    # the relative-system fixtures only
+    python tests/golden/make_golden.py --postftr  # print_basic_info fixtures only
 """
 import os
 import sys
@@ -43,9 +44,15 @@ def cases():
     return out
 
 
-def pack(name, prob, seed):
+def pack(name, prob, seed, print_basic_info=False):
+    """Step records of the reference; with print_basic_info the constructor
+    flag is set, so the reported moments after every table build are the
+    post-FTR ones of compute_moments(false) (the reference also prints its
+    progress on stdout)."""
     ref = oracle.Reference(prob, seed=seed)
     rp, bp = ref.constants()
+    if print_basic_info:
+        ref.set_print_basic_info(True)
     recs = oracle.run(ref, prob, record_terms_upto=TERM_DUMP_CAP)
     ref.close()
     arr = {
@@ -53,7 +60,7 @@ def pack(name, prob, seed):
         "Phi": prob["Phi"], "Gamma": prob["Gamma"], "beta": prob["beta"], "H": prob["H"],
         "gamma": prob["gamma"], "A0": prob["A0"], "p0": prob["p0"], "b0": prob["b0"],
         "msmts": prob["msmts"], "srand_seed": seed, "root_point": rp, "b_pert": bp,
-        "n_updates": len(recs),
+        "n_updates": len(recs), "print_basic_info": int(bool(print_basic_info)),
     }
     for i, r in enumerate(recs):
         pre = "u%d_" % i
@@ -68,6 +75,15 @@ def pack(name, prob, seed):
                 arr[pre + "T_" + k] = v
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **arr)
     return len(recs)
+
+
+def post_ftr_cases():
+    """Problems run with print_basic_info (post-FTR moments reported)."""
+    return [
+        ("postftr_three_state_lti", W.three_state_lti(seed=0, steps=8), 1),
+        ("postftr_five_state_two_msmt", W.five_state_two_msmt(seed=0, steps=3), 4),
+        ("postftr_batched_three_state", W.batched_three_state(1, seed=7, steps_lo=7, steps_hi=8)[0], 17),
+    ]
 
 
 def cpdf_cases():
@@ -271,6 +287,10 @@ def main():
         for name, prob, seed in cases():
             n = pack(name, prob, seed)
             print("wrote %s.npz (%d updates)" % (name, n))
+    if not only or "postftr" in only:
+        for name, prob, seed in post_ftr_cases():
+            n = pack(name, prob, seed, print_basic_info=True)
+            print("wrote %s.npz (%d updates)" % (name, n), file=sys.stderr)
     if not only or "cpdf" in only:
         for name, prob, seed, updates, cseed in cpdf_cases():
             pack_cpdf(name, prob, seed, updates, cseed)

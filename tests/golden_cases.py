@@ -66,6 +66,7 @@ def load(name):
     for k in ("d", "pncc", "cmcc", "p", "steps"):
         prob[k] = int(z[k])
     prob["B"] = None
+    prob["print_basic_info"] = bool(int(z["print_basic_info"])) if "print_basic_info" in z else False
     recs = []
     for i in range(int(z["n_updates"])):
         pre = "u%d_" % i

@@ -30,7 +30,8 @@ class _GpuAdapter:
         CE, _ = _gpu()
         self.prob = prob
         self.est = CE(prob["A0"], prob["p0"], prob["b0"], prob["steps"], prob["d"], prob["cmcc"], prob["pncc"],
-                      prob["p"], root_point=root_point, b_pert=b_pert)
+                      prob["p"], print_basic_info=prob.get("print_basic_info", False), root_point=root_point,
+                      b_pert=b_pert)
 
     def step(self, k, sub=0):
         pr = self.prob
@@ -148,6 +149,52 @@ def test_batched_tables_against_oracle_with_promoted_roots():
     for prob, c, got in zip(probs, consts, recs):
         want, _ = _oracle_records(prob, *c, terms_upto=10**9)
         G.compare_records(got, want, check_terms=True)
+
+
+def test_batched_print_basic_info_on_some_estimators():
+    """print_basic_info set on every other estimator of a batch: those report
+    the post-reduction moments (compute_moments(false)), the others fz = 1."""
+    _, BCE = _gpu()
+    from cauchyfriendly_gb300 import workloads as W
+    probs = W.batched_three_state(8, seed=6, steps_lo=5, steps_hi=7)
+    consts = [oracle.draw_reference_constants(400 + i, 3, oracle.max_shape_of(p)) for i, p in enumerate(probs)]
+    n = len(probs)
+    steps = np.array([p["steps"] for p in probs], np.int32)
+    ms = oracle.max_shape_of({"steps": int(steps.max()), "d": 3, "pncc": 1})
+    bp = np.zeros((n, ms))
+    for i, c in enumerate(consts):
+        bp[i, :len(c[1])] = c[1]
+    bat = BCE(np.stack([p["A0"] for p in probs]), np.stack([p["p0"] for p in probs]),
+              np.stack([p["b0"] for p in probs]), steps, 3, 0, 1, 1, np.stack([c[0] for c in consts]), bp)
+    orcs = []
+    for i, (p, c) in enumerate(zip(probs, consts)):
+        o = oracle.Oracle(p, *c)
+        if i % 2 == 0:
+            bat.set_print_basic_info(True, i)
+            o.set_print_basic_info(True)
+        orcs.append(o)
+    Phi = np.stack([p["Phi"] for p in probs])
+    Gam = np.stack([p["Gamma"] for p in probs])
+    beta = np.stack([p["beta"] for p in probs])
+    H = np.stack([p["H"][0] for p in probs])
+    gam = np.stack([p["gamma"][0] for p in probs])
+    for k in range(int(steps.max())):
+        bat.step(np.array([p["msmts"][min(k, p["steps"] - 1), 0] for p in probs]), Phi, Gam, beta, H, gam,
+                 shared_model=False)
+        for i, (p, o) in enumerate(zip(probs, orcs)):
+            if k >= p["steps"]:
+                continue
+            o.step(k, 0)
+            got, want = bat.moments(i), o.moments()
+            for key in ("fz", "mean", "cov"):
+                assert G.relerr(np.atleast_1d(got[key]), np.atleast_1d(want[key])) <= G.REL_TOL, (i, k, key)
+            assert abs(got["gscale"] - want["gscale"]) <= G.REL_TOL * abs(want["gscale"]), (i, k)
+            if i % 2 and k < p["steps"] - 1:
+                assert got["fz"] == 1
+    assert bat.device_errors() == 0
+    bat.close()
+    for o in orcs:
+        o.close()
 
 
 @pytest.mark.parametrize("steps", [10])

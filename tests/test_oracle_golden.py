@@ -16,6 +16,8 @@ def _build():
 def test_oracle_matches_reference_golden(name):
     prob, (rp, bp), want = G.load(name)
     est = oracle.Oracle(prob, rp, bp)
+    if prob["print_basic_info"]:
+        est.set_print_basic_info(True)
     got = oracle.run(est, prob, record_terms_upto=10**9)
     est.close()
     G.compare_records(got, want)
