@@ -468,11 +468,15 @@ __global__ void k_build_B_vertices(ParentList P, long long nP, const long long* 
                 unsigned inmask = 0;
                 for (int j = 0; j < D; j++) inmask |= 1u << c[j];
                 int niv = 0;
-                for (int a = 0; a < m; a++) {
-                    if (inmask & (1u << a)) continue;
+                // the m - D rows outside the subset, every lane on one of its
+                // own rows per iteration (no idle lanes in the FP64 work)
+                int a = 0;
+                for (int q = 0; q < m - D; q++) {
+                    while ((inmask >> a) & 1u) a++;
                     double s = 0.0;
                     for (int j = 0; j < D; j++) s += As[a * D + j] * v[j];
                     if (neg(s - bp[a])) niv |= 1 << a;
+                    a++;
                 }
                 out = niv;
             }
@@ -801,9 +805,11 @@ __global__ void __launch_bounds__(128) k_mu_terms(ParentList P, long long nP, co
         unsigned hof = 0;
         int sneg = 0;
         double ygi = 0;
-        int l = 0;
-        for (int ll = 0; ll <= m; ll++) {
-            if (ll == t) continue;
+        // the m rows other than t (the parent: rows 0..m-1; child t: the
+        // other MU rows and the measurement row m), one per iteration on
+        // every lane
+        for (int l = 0; l < m; l++) {
+            const int ll = l < t ? l : l + 1;
             const bool fi = (ll < m) ? ((integ_mask >> ll) & 1u) : true;
             double row[D];
             if (fi)
@@ -822,7 +828,6 @@ __global__ void __launch_bounds__(128) k_mu_terms(ParentList P, long long nP, co
             if (!(hof & (1u << l))) ygi += sc;
             for (int j = 0; j < D; j++) At[l * D + j] = row[j];
             pt[l] = pl;
-            l++;
         }
         // lambda keys into the parent table (cauchy_term.hpp:357-381)
         int lp = 0, lm = 0, k = 0;
