@@ -578,7 +578,10 @@ def main():
                 "note": "FP64-bound: the FP64 pipe, not HBM, limits this kernel (see fp64)",
                 "fp64": {"algorithmic_tflops": af / secs / 1e12 if secs > 0 else 0.0, "nominal_peak_tflops": 1.25,
                          "pipe_active_pct_ncu": figs.get(("fp64_pipe_active_pct", top)),
-                         "peak_source": "nominal GB300 FP64; pipe activity from the committed ncu capture"}}
+                         "frac_pipe": (figs[("fp64_pipe_active_pct", top)] / 100.0
+                                       if ("fp64_pipe_active_pct", top) in figs else None),
+                         "peak_source": "nominal GB300 FP64; pipe activity (the fraction of SM cycles the FP64 "
+                                        "pipe is busy, the roof these kernels meet) from the committed ncu capture"}}
     alg_per_pass = {g: {"bytes": alg[g][0], "flops": alg[g][1]} for g in alg}
     share = {g: round(kstats[g][0] / max(1e-9, sum(v[0] for v in kstats.values())), 4) for g in kstats}
     line = {
