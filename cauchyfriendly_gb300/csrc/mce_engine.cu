@@ -244,10 +244,11 @@ private:
 
 enum KernelGroup {
     KID_FIRST = 0, KID_TP, KID_BUILD_B, KID_MU, KID_MOMENTS, KID_FTR, KID_GROUPS, KID_GTABLE, KID_PARTITION,
-    KID_SCAN, KID_COUNT
+    KID_SCAN, KID_WAIT, KID_COUNT
 };
+// "wait": the engine's stream waiting for the side stream's moment chains
 static const char* kKernelGroupNames[KID_COUNT] = {
-    "first_step", "tp", "build_B", "mu", "moments", "ftr", "groups", "gtable", "partition", "scan"};
+    "first_step", "tp", "build_B", "mu", "moments", "ftr", "groups", "gtable", "partition", "scan", "wait"};
 
 struct EstHost {
     int steps = 0;          // estimation steps
@@ -495,9 +496,9 @@ public:
     DevBuf<double> g_rps2, g_mps2;
     DevBuf<double> gscale, mom_tot, mu_rows;
     DevBuf<int> mu_ints;
-    DevBuf<long long> goff, toff, rscan, bucket_off, rbase, scan_tmp, kall_est;
+    DevBuf<long long> goff, toff, rscan, bucket_off, rbase, scan_tmp, kall_est, ptile_start;
     DevBuf<int> status, owner, gcnt, gfill, members, members_tmp, is_root, cap, roots_list, alive, src,
-        tcnt, hist, new_slot, counters, first_cnt, bcount, bfill, slot_of;
+        tcnt, hist, new_slot, counters, first_cnt, bcount, bfill, slot_of, ptile_n, ptile_c;
     DevBuf<long long> boff;
     DevBuf<unsigned char> cell_ent, cell_ent2;
     // number of bucket entries (valid records), known after the bucket scan
@@ -987,7 +988,9 @@ public:
     // raw moments and G_SCALE_FACTOR are copied to the host
     int join_moments()
     {
+        pbeg(KID_WAIT);
         MCE_CUDA(cudaStreamWaitEvent(lc.stream, ev_join, 0));
+        pend();
         return read_moments();
     }
 
@@ -1124,6 +1127,14 @@ public:
         const int MCp = MC + 1;
         if (any_skip) {
             if ((s = hist.ensure((size_t)E * MCp))) return s;
+            if (!any_keep) {
+                // every estimator ends its step here: the step waits for its
+                // moment chains in any case, so the wait is taken (and timed)
+                // before the shape histogram rather than behind it
+                pbeg(KID_WAIT);
+                MCE_CUDA(cudaStreamWaitEvent(lc.stream, ev_join, 0));
+                pend();
+            }
             MCE_CUDA(cudaMemsetAsync(hist.ptr, 0, sizeof(int) * E * MCp, lc.stream));
             pbeg(KID_PARTITION);
             k_skip_hist(PV, nP, MCp);
@@ -1331,13 +1342,17 @@ public:
         if ((s = bucket_off.ensure((size_t)E * MCp + 2))) return s;
         if ((s = new_slot.ensure(nR + 1))) return s;
         if ((s = rbase.ensure(E + 2))) return s;
-        MCE_CUDA(cudaMemsetAsync(hist.ptr, 0, sizeof(int) * E * MCp, lc.stream));
+        if ((s = ptile_n.ensure(E + 1))) return s;
+        if ((s = ptile_start.ensure(E + 2))) return s;
+        if ((s = ptile_c.ensure((size_t)partition_tiles_cap(nR, E) * MCp + 1))) return s;
         if ((s = ensure_scan_scratch((long long)E * MCp + 1))) return s;
         pbeg(KID_PARTITION);
-        partition_count(alive.ptr, Rb.est.ptr, Rb.m.ptr, nR, MCp, hist.ptr, lc);
-        scan_int_to_ll(hist.ptr, bucket_off.ptr, (long long)E * MCp, ss, lc);
         rbase_kernel(dpstart.ptr, PV.kscan, E, rbase.ptr, lc);
-        partition_rank(alive.ptr, Rb.m.ptr, rbase.ptr, E, MCp, bucket_off.ptr, new_slot.ptr, lc);
+        partition_tiles(alive.ptr, Rb.m.ptr, rbase.ptr, E, MCp, nR, ptile_n.ptr, ptile_start.ptr, ptile_c.ptr,
+                        hist.ptr, ss, lc);
+        scan_int_to_ll(hist.ptr, bucket_off.ptr, (long long)E * MCp, ss, lc);
+        partition_rank(alive.ptr, Rb.m.ptr, rbase.ptr, E, MCp, nR, ptile_start.ptr, ptile_c.ptr, bucket_off.ptr,
+                       new_slot.ptr, lc);
         pend();
         h_hist.resize((size_t)E * MCp);
         MCE_CUDA(cudaMemcpyAsync(h_hist.data(), hist.ptr, sizeof(int) * E * MCp, cudaMemcpyDeviceToHost, lc.stream));

@@ -1980,24 +1980,86 @@ __global__ void k_gtable_prom_combine(GCtx c, const int* roots_list, long long n
 // within each shape; shapes ascend).
 
 #if MCE_COMMON_UNIT
-__global__ void k_partition_count(const int* alive, const int* est, const int* m, long long nR, int MCp, int* hist)
+// Stable partition of the surviving records by (estimator, shape).  Each
+// estimator's record range is cut into tiles of kPartTile records; a block
+// counts a tile's records per shape, a thread per (estimator, shape) scans
+// the counts over the estimator's tiles (its totals are the shape histogram),
+// and a block per tile ranks its records in order.  One estimator of 10^7
+// records thus spreads over thousands of blocks instead of one.
+constexpr int kPartTile = 4096;
+
+__global__ void k_ptile_count(const long long* rbase, int E, int* ntile)
 {
-    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nR; j += (long long)gridDim.x * blockDim.x)
-        if (alive[j]) atomicAdd(&hist[(long long)est[j] * MCp + m[j]], 1);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < E; e += gridDim.x * blockDim.x)
+        ntile[e] = (int)((rbase[e + 1] - rbase[e] + kPartTile - 1) / kPartTile);
 }
 
-__global__ void k_partition_rank(const int* alive, const int* m, const long long* rbase, int E, int MCp,
-                                 const long long* bucket_off, int* new_slot)
+// the estimator of tile t: the last e with tstart[e] <= t
+__device__ inline int tile_est(const long long* tstart, int E, long long t)
+{
+    int lo = 0, hi = E;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (tstart[mid] <= t) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_ptile_hist(const int* alive, const int* m, const long long* rbase, int E, int MCp,
+                             const long long* tstart, int* C)
+{
+    __shared__ int cnt[33];
+    const long long NT = tstart[E];
+    for (long long t = blockIdx.x; t < NT; t += gridDim.x) {
+        if (threadIdx.x < MCp) cnt[threadIdx.x] = 0;
+        __syncthreads();
+        const int e = tile_est(tstart, E, t);
+        const long long a = rbase[e] + (t - tstart[e]) * kPartTile;
+        const long long b = a + kPartTile < rbase[e + 1] ? a + kPartTile : rbase[e + 1];
+        for (long long j = a + threadIdx.x; j < b; j += blockDim.x)
+            if (alive[j]) atomicAdd(&cnt[m[j]], 1);
+        __syncthreads();
+        if (threadIdx.x < MCp) C[t * MCp + threadIdx.x] = cnt[threadIdx.x];
+        __syncthreads();
+    }
+}
+
+// per (estimator, shape): tile counts -> exclusive prefix over the
+// estimator's tiles, the total into the shape histogram
+__global__ void k_ptile_scan(int E, int MCp, const long long* tstart, int* C, int* hist)
+{
+    for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < (long long)E * MCp;
+         x += (long long)gridDim.x * blockDim.x) {
+        const int e = (int)(x / MCp), sh = (int)(x - (long long)e * MCp);
+        int run = 0;
+        for (long long t = tstart[e]; t < tstart[e + 1]; t++) {
+            const int c = C[t * MCp + sh];
+            C[t * MCp + sh] = run;
+            run += c;
+        }
+        hist[x] = run;
+    }
+}
+
+// a block per tile: each surviving record's slot, bucket start + records of
+// its shape in earlier tiles + earlier ones in this tile
+__global__ void k_ptile_rank(const int* alive, const int* m, const long long* rbase, int E, int MCp,
+                             const long long* tstart, const int* P, const long long* bucket_off, int* new_slot)
 {
     __shared__ long long running[33];
     __shared__ int wcnt[8][33];
     __shared__ int total[33];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int e = blockIdx.x; e < E; e += gridDim.x) {
-        if (threadIdx.x < MCp) running[threadIdx.x] = bucket_off[(long long)e * MCp + threadIdx.x];
+    const long long NT = tstart[E];
+    for (long long t = blockIdx.x; t < NT; t += gridDim.x) {
+        const int e = tile_est(tstart, E, t);
+        if (threadIdx.x < MCp)
+            running[threadIdx.x] = bucket_off[(long long)e * MCp + threadIdx.x] + P[t * MCp + threadIdx.x];
         for (int k = threadIdx.x; k < 8 * 33; k += blockDim.x) wcnt[k / 33][k % 33] = 0;
         __syncthreads();
-        const long long a = rbase[e], bnd = rbase[e + 1];
+        const long long a = rbase[e] + (t - tstart[e]) * kPartTile;
+        const long long bnd = a + kPartTile < rbase[e + 1] ? a + kPartTile : rbase[e + 1];
         for (long long base = a; base < bnd; base += blockDim.x) {
             const long long j = base + threadIdx.x;
             const int key = (j < bnd && alive[j]) ? m[j] : -1;
@@ -2009,9 +2071,9 @@ __global__ void k_partition_rank(const int* alive, const int* m, const long long
             if (threadIdx.x < MCp) {
                 int acc = 0;
                 for (int ww = 0; ww < (int)(blockDim.x >> 5); ww++) {
-                    const int t = wcnt[ww][threadIdx.x];
+                    const int c = wcnt[ww][threadIdx.x];
                     wcnt[ww][threadIdx.x] = acc;
-                    acc += t;
+                    acc += c;
                 }
                 total[threadIdx.x] = acc;
             }
@@ -3186,20 +3248,30 @@ void roots_list(const int* is_root, const long long* rscan, long long nR, int* l
     ++g_launches;
     k_roots_list<<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(is_root, rscan, nR, list);
 }
-void partition_count(const int* alive, const int* est, const int* m, long long nR, int MCp, int* hist,
-                     const LaunchCfg& c)
+long long partition_tiles_cap(long long nR, int E) { return nR / kPartTile + E + 1; }
+
+void partition_tiles(const int* alive, const int* m, const long long* rbase, int E, int MCp, long long nR,
+                     int* ntile, long long* tstart, int* C, int* hist, ScanScratch& ss, const LaunchCfg& c)
 {
-    if (nR == 0) return;
-    ++g_launches;
-    k_partition_count<<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(alive, est, m, nR, MCp, hist);
+    if (E <= 0) return;
+    const long long cap = partition_tiles_cap(nR, E);
+    const int g = (int)(cap < (long long)c.num_sms * 16 ? cap : (long long)c.num_sms * 16);
+    g_launches += 3;
+    k_ptile_count<<<(E + 255) / 256, 256, 0, c.stream>>>(rbase, E, ntile);
+    scan_int_to_ll(ntile, tstart, E, ss, c);
+    k_ptile_hist<<<g, 256, 0, c.stream>>>(alive, m, rbase, E, MCp, tstart, C);
+    k_ptile_scan<<<grid_for((long long)E * MCp, 256, c.num_sms), 256, 0, c.stream>>>(E, MCp, tstart, C, hist);
 }
-void partition_rank(const int* alive, const int* m, const long long* rbase, int E, int MCp,
-                    const long long* bucket_off, int* new_slot, const LaunchCfg& c)
+
+void partition_rank(const int* alive, const int* m, const long long* rbase, int E, int MCp, long long nR,
+                    const long long* tstart, const int* P, const long long* bucket_off, int* new_slot,
+                    const LaunchCfg& c)
 {
-    int g = E < c.num_sms * 8 ? E : c.num_sms * 8;
-    if (g < 1) g = 1;
+    if (E <= 0) return;
+    const long long cap = partition_tiles_cap(nR, E);
+    const int g = (int)(cap < (long long)c.num_sms * 16 ? cap : (long long)c.num_sms * 16);
     ++g_launches;
-    k_partition_rank<<<g, 256, 0, c.stream>>>(alive, m, rbase, E, MCp, bucket_off, new_slot);
+    k_ptile_rank<<<g, 256, 0, c.stream>>>(alive, m, rbase, E, MCp, tstart, P, bucket_off, new_slot);
 }
 void rbase_kernel(const long long* pstart, const long long* kscan, int E, long long* rbase, const LaunchCfg& c)
 {

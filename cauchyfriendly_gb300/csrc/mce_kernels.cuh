@@ -171,11 +171,16 @@ void group_sort(const int* gcnt, const long long* goff, long long nR, const int*
 void roots_flags(const int* status, const int* m, long long nR, int D, int* is_root, int* cap,
                  const LaunchCfg& c);
 void roots_list(const int* is_root, const long long* rscan, long long nR, int* list, const LaunchCfg& c);
-// Stable partition of alive roots of each estimator by shape.
-void partition_count(const int* alive, const int* est, const int* m, long long nR, int MCp, int* hist,
-                     const LaunchCfg& c);
-void partition_rank(const int* alive, const int* m, const long long* rbase, int E, int MCp,
-                    const long long* bucket_off, int* new_slot, const LaunchCfg& c);
+// Stable partition of the surviving records of each estimator by shape:
+// tiles of records within each estimator (at most partition_tiles_cap(nR, E)
+// of them), per-tile shape counts turned into per-tile prefixes (C, in
+// place) and the (estimator, shape) histogram; then the slots.
+long long partition_tiles_cap(long long nR, int E);
+void partition_tiles(const int* alive, const int* m, const long long* rbase, int E, int MCp, long long nR,
+                     int* ntile, long long* tstart, int* C, int* hist, ScanScratch& ss, const LaunchCfg& c);
+void partition_rank(const int* alive, const int* m, const long long* rbase, int E, int MCp, long long nR,
+                    const long long* tstart, const int* P, const long long* bucket_off, int* new_slot,
+                    const LaunchCfg& c);
 void rbase_kernel(const long long* pstart, const long long* kscan, int E, long long* rbase,
                   const LaunchCfg& c);
 
