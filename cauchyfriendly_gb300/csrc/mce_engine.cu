@@ -372,6 +372,8 @@ public:
     std::vector<EstStep<D>> hsteps;
     DevBuf<long long> dpstart;
     std::vector<long long> hpstart;  // E+1
+    std::vector<int> h_order;       // moment-chain launch order
+    DevBuf<int> d_order;
     // combos per shape (lexicographic d-subsets)
     DevBuf<int> dcombo_off;
     DevBuf<unsigned char> dcombos;
@@ -1099,14 +1101,29 @@ public:
         // the moment chains (and G_SCALE_FACTOR) on the side stream: the term
         // reduction below does not read them; the g-table evaluation does, so
         // the engine's stream waits for them before it (join_moments)
+        // a chain's length follows its estimator's parent count: chains
+        // start longest first, so that the longest does not wait for a
+        // later wave of blocks
+        const int* order = nullptr;
+        if (E > 1) {
+            h_order.resize(E);
+            for (int e = 0; e < E; e++) h_order[e] = e;
+            std::stable_sort(h_order.begin(), h_order.end(), [&](int x, int y) {
+                return hpstart[x + 1] - hpstart[x] > hpstart[y + 1] - hpstart[y];
+            });
+            if ((s = d_order.ensure(E))) return s;
+            MCE_CUDA(cudaMemcpyAsync(d_order.ptr, h_order.data(), sizeof(int) * E, cudaMemcpyHostToDevice,
+                                     lc.stream));
+            order = d_order.ptr;
+        }
         MCE_CUDA(cudaEventRecord(ev_fork, lc.stream));
         MCE_CUDA(cudaStreamWaitEvent(mstream, ev_fork, 0));
         {
             LaunchCfg lcm = lc;
             lcm.stream = mstream;
             pbeg(KID_MOMENTS, mstream);
-            Kernels<D>::moments(fam_mom.ptr, dpstart.ptr, kall_scan.ptr, E, dsteps.ptr, mom_tot.ptr, est_raw.ptr,
-                                gscale.ptr, lcm);
+            Kernels<D>::moments(fam_mom.ptr, dpstart.ptr, kall_scan.ptr, E, order, dsteps.ptr, mom_tot.ptr,
+                                est_raw.ptr, gscale.ptr, lcm);
             pend(mstream);
         }
         MCE_CUDA(cudaEventRecord(ev_join, mstream));
@@ -1402,7 +1419,7 @@ public:
         MCE_CUDA(cudaMemsetAsync(pf_zero.ptr, 0, sizeof(long long) * (nP + 2), lc.stream));
         Kernels<D>::post_ftr_terms(Pb[cur].view(), nP, droots.ptr, Tables{Tb[cur].keys.ptr, Tb[cur].vals.ptr}, MC,
                                    pf_rows.ptr, lc);
-        Kernels<D>::moments(pf_rows.ptr, dpstart.ptr, pf_zero.ptr, E, dsteps.ptr, pf_tot.ptr, pf_raw.ptr,
+        Kernels<D>::moments(pf_rows.ptr, dpstart.ptr, pf_zero.ptr, E, nullptr, dsteps.ptr, pf_tot.ptr, pf_raw.ptr,
                             pf_gscale.ptr, lc);
         h_pf_raw.resize((size_t)E * NM);
         h_pf_gscale.resize(E);

@@ -941,16 +941,19 @@ __device__ inline void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n
 
 template <int D>
 __global__ void __launch_bounds__(32) k_moments_chain(const cd* contrib, const long long* pstart,
-                                                      const long long* kall_scan, int E, const EstStep<D>* st,
-                                                      double* tot)
+                                                      const long long* kall_scan, int E, const int* order,
+                                                      const EstStep<D>* st, double* tot)
 {
     constexpr int NM = 1 + D + D * D;
     constexpr int ND = 2 * NM;              // doubles per term
     constexpr int NS = (ND + 31) / 32;      // 32-component slices
     __shared__ double ring[kMomStages][kMomRows][32];
     const int lane = threadIdx.x;
-    const int e = blockIdx.x / NS, slice = blockIdx.x - e * NS;
-    if (e >= E || !st[e].active) return;
+    const int eb = blockIdx.x / NS, slice = blockIdx.x - eb * NS;
+    if (eb >= E) return;
+    // blocks start in launch order: the longest chains go first
+    const int e = order ? order[eb] : eb;
+    if (!st[e].active) return;
     const long long a = pstart[e] + kall_scan[pstart[e]];
     const long long n = pstart[e + 1] + kall_scan[pstart[e + 1]] - a;
     const int comp = slice * 32 + lane;
@@ -2215,11 +2218,12 @@ void Kernels<D>::mu(ParentList P, long long nP, const EstStep<D>* st, const long
 
 template <int D>
 void Kernels<D>::moments(const cd* contrib, const long long* pstart, const long long* kall_scan, int E,
-                         const EstStep<D>* st, double* tot, cd* est_raw, double* gscale, const LaunchCfg& c)
+                         const int* order, const EstStep<D>* st, double* tot, cd* est_raw, double* gscale,
+                         const LaunchCfg& c)
 {
     constexpr int NS = (2 * (1 + D + D * D) + 31) / 32;
     g_launches += 2;
-    k_moments_chain<D><<<(unsigned)E * NS, 32, 0, c.stream>>>(contrib, pstart, kall_scan, E, st, tot);
+    k_moments_chain<D><<<(unsigned)E * NS, 32, 0, c.stream>>>(contrib, pstart, kall_scan, E, order, st, tot);
     k_moments_final<D><<<(E + 127) / 128, 128, 0, c.stream>>>(tot, E, st, est_raw, gscale);
 }
 

@@ -83,9 +83,11 @@ struct Kernels {
                    const long long* kall_scan, long long nterms, double* frow, int* fint, cd* contrib, int MC,
                    int* err, const LaunchCfg& c);
     // Per-estimator moment sums in the reference's order and finalisation
-    // (cauchy_estimator.hpp:307-357).
+    // (cauchy_estimator.hpp:307-357); the chains start in the estimator order
+    // given by order (null: 0..E-1), longest first when the caller sorts.
     static void moments(const cd* contrib, const long long* pstart, const long long* kall_scan, int E,
-                        const EstStep<D>* st, double* tot, cd* est_raw, double* gscale, const LaunchCfg& c);
+                        const int* order, const EstStep<D>* st, double* tot, cd* est_raw, double* gscale,
+                        const LaunchCfg& c);
     // Fast term reduction (term_reduction.hpp:159-276) over the post-MU records:
     // grid cells of b, counting-sorted buckets, near predecessors.
     static void ftr_cells(TermRecs R, long long nR, long long hmask, int* slot_of, int* bcount, const LaunchCfg& c);
