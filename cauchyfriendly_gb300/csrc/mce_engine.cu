@@ -373,6 +373,8 @@ public:
     DevBuf<long long> dpstart;
     std::vector<long long> hpstart;  // E+1
     std::vector<int> h_order;       // moment-chain launch order
+    DevBuf<int> ftr_cnt;            // worklist lengths of the resolution rounds
+    static constexpr int kFtrFirstBatch = 4, kFtrBatch = 2, kFtrCntSlots = 8;
     DevBuf<int> d_order;
     // combos per shape (lexicographic d-subsets)
     DevBuf<int> dcombo_off;
@@ -1208,17 +1210,30 @@ public:
         if ((s = ftr_wl[0].ensure(nR + 1))) return s;
         if ((s = ftr_wl[1].ensure(nR + 1))) return s;
         if ((s = ftr_resume.ensure((size_t)(nR + 1) * kFtrResume))) return s;
+        // resolution rounds, queued kFtrBatch at a time (the first batch
+        // kFtrFirstBatch): a round reads the previous round's worklist length
+        // on the device, a round after the last is empty, and the host reads
+        // the count once per batch
+        if ((s = ftr_cnt.ensure(kFtrCntSlots))) return s;
         int unk = 0;
-        for (int round = 0;; round++) {
-            MCE_CUDA(cudaMemsetAsync(counters.ptr + 1, 0, sizeof(int), lc.stream));
+        long long bound = nR;
+        for (int round = 0;;) {
+            const int K = round == 0 ? kFtrFirstBatch : kFtrBatch;
             pbeg(KID_FTR);
-            Kernels<D>::ftr_resolve(R, nR, cell_ent2.ptr, boff.ptr, H - 1, MC, status.ptr, owner.ptr,
-                                    round ? ftr_wl[(round - 1) & 1].ptr : nullptr, unk, ftr_wl[round & 1].ptr,
-                                    counters.ptr + 1, ftr_resume.ptr, lc);
+            for (int q = 0; q < K; q++, round++) {
+                int* n_out = ftr_cnt.ptr + round % kFtrCntSlots;
+                MCE_CUDA(cudaMemsetAsync(n_out, 0, sizeof(int), lc.stream));
+                Kernels<D>::ftr_resolve(R, nR, cell_ent2.ptr, boff.ptr, H - 1, MC, status.ptr, owner.ptr,
+                                        round ? ftr_wl[(round - 1) & 1].ptr : nullptr,
+                                        round ? ftr_cnt.ptr + (round - 1) % kFtrCntSlots : nullptr, bound,
+                                        ftr_wl[round & 1].ptr, n_out, ftr_resume.ptr, lc);
+            }
             pend();
-            MCE_CUDA(cudaMemcpyAsync(&unk, counters.ptr + 1, sizeof(int), cudaMemcpyDeviceToHost, lc.stream));
+            MCE_CUDA(cudaMemcpyAsync(&unk, ftr_cnt.ptr + (round - 1) % kFtrCntSlots, sizeof(int),
+                                     cudaMemcpyDeviceToHost, lc.stream));
             MCE_CUDA(cudaStreamSynchronize(lc.stream));
             if (unk == 0) break;
+            bound = unk;
             if (round > 100000) {
                 set_error("term reduction did not converge");
                 device_errors |= kErrResolveStalled;
@@ -1235,7 +1250,9 @@ public:
         group_count(status.ptr, owner.ptr, nR, gcnt.ptr, lc);
         scan_int_to_ll(gcnt.ptr, goff.ptr, nR, ss, lc);
         pend();
-        const long long nmembers = read_ll(goff.ptr + nR);
+        // each record is a member of at most one group: nR bounds the
+        // members, so their buffers are sized without reading the count back
+        const long long nmembers = nR;
         if ((s = members.ensure(nmembers + 1))) return s;
         if ((s = members_tmp.ensure(nmembers + 1))) return s;
         pbeg(KID_GROUPS);

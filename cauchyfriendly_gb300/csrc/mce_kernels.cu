@@ -1156,10 +1156,10 @@ __global__ void k_ftr_sort_buckets(const CellEntry<D>* in, long long n, const in
 
 template <int D>
 __global__ void k_ftr_resolve_scan(TermRecs R, long long nR, const CellEntry<D>* ent, const long long* boff,
-                                   long long hmask, int MC, int* status, int* owner, const int* wl_in, long long n_in,
+                                   long long hmask, int MC, int* status, int* owner, const int* wl_in, const int* n_in,
                                    int* wl_out, int* n_out, int* resume)
 {
-    const long long n = wl_in ? n_in : nR;
+    const long long n = wl_in ? (long long)*n_in : nR;
     for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < n; w += (long long)gridDim.x * blockDim.x) {
         const long long j = wl_in ? wl_in[w] : w;
         if (status[j] != 0) continue;
@@ -2263,10 +2263,10 @@ void Kernels<D>::ftr_sort(const void* in, long long n, const int* slot_of, const
 
 template <int D>
 void Kernels<D>::ftr_resolve(TermRecs R, long long nR, const void* ent, const long long* boff, long long hmask,
-                             int MC, int* status, int* owner, const int* wl_in, long long n_in, int* wl_out,
-                             int* n_out, int* resume, const LaunchCfg& c)
+                             int MC, int* status, int* owner, const int* wl_in, const int* n_in, long long n_bound,
+                             int* wl_out, int* n_out, int* resume, const LaunchCfg& c)
 {
-    const long long n = wl_in ? n_in : nR;
+    const long long n = wl_in ? n_bound : nR;
     if (n == 0) return;
     ++g_launches;
     k_ftr_resolve_scan<D><<<grid_for(n, 128, c.num_sms), 128, 0, c.stream>>>(

@@ -97,12 +97,14 @@ struct Kernels {
     static void ftr_sort(const void* in, long long n, const int* slot_of, const long long* boff, void* out,
                          const LaunchCfg& c);
     // One resolution round: over every record (wl_in null) or over the
-    // worklist of records still waiting; the ones that must wait again are
-    // appended to wl_out (count n_out); resume holds kFtrResume bucket
-    // positions per record.
+    // worklist of records still waiting, whose length the kernel reads from
+    // n_in (device memory, written by the previous round; n_bound, known on
+    // the host, bounds it and sizes the grid); the ones that must wait again
+    // are appended to wl_out (count n_out); resume holds kFtrResume bucket
+    // positions per record.  Rounds thus queue back to back without the host.
     static void ftr_resolve(TermRecs R, long long nR, const void* ent, const long long* boff, long long hmask, int MC,
-                            int* status, int* owner, const int* wl_in, long long n_in, int* wl_out, int* n_out,
-                            int* resume, const LaunchCfg& c);
+                            int* status, int* owner, const int* wl_in, const int* n_in, long long n_bound,
+                            int* wl_out, int* n_out, int* resume, const LaunchCfg& c);
     // g-tables of every reduction group (flattening.hpp:318-568).
     static void gtable(TermRecs R, const int* roots_list, long long nroots, const int* gcnt,
                        const long long* goff, const int* members, ParentList P, Tables Told, const int* Bkeys,
