@@ -91,6 +91,35 @@ struct DevBuf {
     }
 };
 
+// Page-locked host buffer: device-to-host copies into it are asynchronous, so
+// the host goes on queueing work while they wait on the stream.
+template <typename T>
+struct PinnedBuf {
+    T* ptr = nullptr;
+    size_t cap = 0;
+    ~PinnedBuf()
+    {
+        if (ptr) cudaFreeHost(ptr);
+    }
+    int ensure(size_t n)
+    {
+        if (n <= cap && ptr) return MCE_OK;
+        if (ptr) cudaFreeHost(ptr);
+        ptr = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMallocHost(&ptr, std::max<size_t>(n, 1) * sizeof(T));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            set_error(std::string("cudaMallocHost failed: ") + cudaGetErrorString(e));
+            return MCE_ERR_NOMEM;
+        }
+        cap = std::max<size_t>(n, 1);
+        return MCE_OK;
+    }
+    T* data() { return ptr; }
+    T& operator[](size_t i) { return ptr[i]; }
+};
+
 // Numeric checks of one estimator's raw moments (cauchy_estimator.hpp:359-461,
 // covariance_checker cauchy_util.hpp:1882-2004).
 enum {
@@ -507,8 +536,10 @@ public:
     DevBuf<unsigned char> cell_ent, cell_ent2;
     // number of bucket entries (valid records), known after the bucket scan
     long long nvalid_entries(long long H) { return read_ll(boff.ptr + H); }
-    std::vector<cd> h_raw;
-    std::vector<double> h_gscale;
+    // raw moments and G_SCALE_FACTOR per estimator, read back asynchronously
+    // at the join and used after the step's final synchronisation
+    PinnedBuf<cd> h_raw;
+    PinnedBuf<double> h_gscale;
     std::vector<int> h_hist;
     ScanScratch ss{};
     // profiling events
@@ -638,6 +669,8 @@ public:
         s |= counters.ensure(8);
         s |= first_cnt.ensure(E + 1);
         s |= scan_tmp.ensure(1 << 16);
+        s |= h_raw.ensure((size_t)E * (1 + D + D * D));
+        s |= h_gscale.ensure(E);
         if (s) return MCE_ERR_NOMEM;
         ss.block_sums = scan_tmp.ptr;
         ss.cap = (long long)scan_tmp.cap;
@@ -1001,8 +1034,6 @@ public:
     int read_moments()
     {
         const int NM = 1 + D + D * D;
-        h_raw.resize((size_t)E * NM);
-        h_gscale.resize(E);
         MCE_CUDA(cudaMemcpyAsync(h_raw.data(), est_raw.ptr, sizeof(cd) * E * NM, cudaMemcpyDeviceToHost, lc.stream));
         MCE_CUDA(cudaMemcpyAsync(h_gscale.data(), gscale.ptr, sizeof(double) * E, cudaMemcpyDeviceToHost, lc.stream));
         return MCE_OK;
