@@ -966,7 +966,12 @@ __global__ void __launch_bounds__(32) k_moments_chain(const cd* contrib, const l
             const long long r0 = k * kMomRows;
             const int cnt = n - r0 < kMomRows ? (int)(n - r0) : kMomRows;
             double(*slot)[32] = ring[k % kMomStages];
-            for (int r = 0; r < cnt; r++) cp_async8(&slot[r][lane], col + (r0 + r) * ND);
+            const double* src = col + r0 * ND;
+            if (cnt == kMomRows) {
+#pragma unroll
+                for (int r = 0; r < kMomRows; r++) cp_async8(&slot[r][lane], src + r * ND);
+            } else
+                for (int r = 0; r < cnt; r++) cp_async8(&slot[r][lane], src + r * ND);
         }
         cp_async_commit();
     };
