@@ -138,6 +138,23 @@ def test_batched_random_three_state_against_oracle():
     assert total == want_total
 
 
+def test_full_size_bench_batch_sampled_against_oracle():
+    """The bench's batch at its full size (4096 3-state LTI estimators, steps
+    U{4..9}, 5% outliers at 100x, seed 0, the bench's reference constants):
+    the whole batch on the GPU, every 16th estimator against the oracle at
+    every step (moments, Nt, terms per shape, error bits)."""
+    import bench
+    from cauchyfriendly_gb300 import workloads as W
+    probs = W.batched_three_state(4096, seed=0)
+    rp, bp = bench.constants(probs, 0)
+    consts = [(rp[i], bp[i, :oracle.max_shape_of(p)]) for i, p in enumerate(probs)]
+    recs, total = _batch_run_compare(probs, consts)
+    assert total > 5e7  # the bench's 53.5 M post-MU terms per pass
+    for i in range(0, len(probs), 16):
+        want, _ = _oracle_records(probs[i], *consts[i])
+        G.compare_records(recs[i], want, check_terms=False)
+
+
 def test_batched_tables_against_oracle_with_promoted_roots():
     """Every term's g-table against the oracle for a batch in which many
     reduction groups lose their root to the term approximation and promote a
