@@ -928,7 +928,7 @@ __global__ void __launch_bounds__(128) k_mu_terms(ParentList P, long long nP, co
 // estimator of 10^6 terms the chain runs at the FP64 add rate instead of
 // waiting on DRAM once every few rows.  Each lane copies and reads only its
 // own column, so its own cp.async.wait_group is the only synchronisation.
-constexpr int kMomStages = 2, kMomRows = 64;
+constexpr int kMomStages = 3, kMomRows = 64;
 
 __device__ inline void cp_async8(double* smem_dst, const double* gmem_src)
 {
