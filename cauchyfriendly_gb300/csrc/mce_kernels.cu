@@ -347,14 +347,20 @@ __global__ void k_tp(ParentList P, long long nP, const EstStep<D>* st, int with_
         double* p = P.p + i * MC;
         double* b = P.b + i * D;
         if (with_tp) {
+            // A <- A Phi^T, then normalize_hps(false): per row in registers,
+            // one read and one write of the row
             for (int r = 0; r < m; r++) {
-                double w[D];
+                double w[D], v[D];
                 for (int k = 0; k < D; k++) w[k] = A[r * D + k];
                 for (int j = 0; j < D; j++) {
                     double s = 0.0;
                     for (int k = 0; k < D; k++) s += w[k] * S.Phi[j * D + k];
-                    A[r * D + j] = s;
+                    v[j] = s;
                 }
+                double n1 = 0;
+                for (int j = 0; j < D; j++) n1 += fabs(v[j]);
+                p[r] *= n1;
+                for (int j = 0; j < D; j++) A[r * D + j] = v[j] / n1;
             }
             double wb[D];
             for (int j = 0; j < D; j++) wb[j] = b[j];
@@ -365,13 +371,6 @@ __global__ void k_tp(ParentList P, long long nP, const EstStep<D>* st, int with_
             }
             if (S.has_control)
                 for (int r = 0; r < D; r++) b[r] += 1.0 * S.Bu[r];
-            // normalize_hps(false)
-            for (int r = 0; r < m; r++) {
-                double n1 = 0;
-                for (int j = 0; j < D; j++) n1 += fabs(A[r * D + j]);
-                p[r] *= n1;
-                for (int j = 0; j < D; j++) A[r * D + j] /= n1;
-            }
             bool F[kMaxGamma];
             for (int j = 0; j < S.gcnt; j++) F[j] = true;
             for (int j = 0; j < S.gcnt; j++)
