@@ -7,15 +7,16 @@ import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
-# fz, mean and covariance tolerance (relative to the largest magnitude of the
-# quantity at that update); integer structure is compared exactly.
+# fz, mean and covariance tolerance, element by element (relerr); integer
+# structure is compared exactly.
 REL_TOL = 1e-9
 
 
 def names():
     """The step-record fixtures (the marginal pdf ones are cpdf_names())."""
     return sorted(n for n in (os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
-                  if not n.startswith(("cpdf1d_", "cpdf2d_", "ext_", "rel2d_")))
+                  if not n.startswith(("cpdf1d_", "cpdf2d_", "ext_", "rel2d_", "win_", "speyer_", "tr_ordering_",
+                                       "adj_")))
 
 
 def cpdf_names():
@@ -79,10 +80,28 @@ def load(name):
     return prob, (z["root_point"], z["b_pert"]), recs
 
 
-def relerr(a, b):
+ABS_FLOOR = 1e-12
+
+
+def relerr(a, b, floor=ABS_FLOOR):
+    """Largest element-wise relative error of a against the reference b:
+    max_i |a_i - b_i| / max(|b_i|, floor * max_j |b_j|).  The floor only
+    covers entries that are structurally zero up to rounding (a covariance
+    entry of a decoupled state, a pdf value far in the tail); every other
+    entry is held to the tolerance on its own magnitude."""
     a = np.asarray(a); b = np.asarray(b)
-    scale = max(np.max(np.abs(a)), 1e-300)
-    return float(np.max(np.abs(a - b)) / scale)
+    if a.size == 0 and b.size == 0:
+        return 0.0
+    mag = np.abs(b)
+    den = np.maximum(mag, max(floor * float(np.max(mag)), 1e-300))
+    return float(np.max(np.abs(a - b) / den))
+
+
+def bitwise_equal(a, b):
+    """True when a and b hold the same doubles element by element (complex
+    parts included; +0 and -0 count as equal, so do two NaNs)."""
+    a = np.asarray(a); b = np.asarray(b)
+    return a.shape == b.shape and bool(np.array_equal(a, b, equal_nan=True))
 
 
 def compare_records(got, want, rel_tol=REL_TOL, check_terms=True, first_raw_from_reported=True):
@@ -111,6 +130,26 @@ def compare_records(got, want, rel_tol=REL_TOL, check_terms=True, first_raw_from
             for k in ("A", "p", "b"):
                 assert relerr(gt[k], wt[k]) <= 1e-12, (ctx, k, relerr(gt[k], wt[k]))
             assert relerr(gt["g"], wt["g"]) <= rel_tol, (ctx, "g values", relerr(gt["g"], wt["g"]))
+
+
+def bitwise_mismatches(got, want):
+    """Names of the floating-point quantities of a run's per-update records
+    that are not bit-identical to the golden ones (raw and reported moments,
+    G_SCALE_FACTOR, every dumped term's A, p, b and g values)."""
+    bad = []
+    for i, (g, w) in enumerate(zip(got, want)):
+        keys = ("fz", "mean", "cov") if i == 0 else ("raw_fz", "raw_mean", "raw_cov", "fz", "mean", "cov")
+        for k in keys:
+            if not bitwise_equal(np.asarray(g[k], np.complex128).ravel(), np.asarray(w[k], np.complex128).ravel()):
+                bad.append((i, k, relerr(g[k], w[k])))
+        if float(g["gscale"]) != float(w["gscale"]):
+            bad.append((i, "gscale", abs(g["gscale"] / float(w["gscale"]) - 1)))
+        if "terms" in w and "terms" in g:
+            for k in ("A", "p", "b", "g"):
+                a = np.asarray(g["terms"][k]).ravel(); b = np.asarray(w["terms"][k]).ravel()
+                if not bitwise_equal(a.astype(b.dtype), b):
+                    bad.append((i, "term " + k, relerr(a, b)))
+    return bad
 
 
 def extended_ops(prob):
