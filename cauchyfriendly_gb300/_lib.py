@@ -73,6 +73,16 @@ SIGNATURES = {
     "mce_kernel_group_name": (ctypes.c_char_p, [ctypes.c_int]),
     "mce_kernel_group_stats": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _lp, _dp, _dp]),
     "mce_destroy": (None, [_vp]),
+    "mce_sym_eig": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp]),
+    "mce_speyers_window_init": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double, _dp,
+                                               _dp, _dp, _dp]),
+    "mce_swm_create": (_vp, [ctypes.c_int] * 7 + [_dp] * 9 + [ctypes.c_double, ctypes.c_int, _vp, _dp, _dp, _dp,
+                                                              ctypes.c_int, _ip]),
+    "mce_swm_step": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip]),
+    "mce_swm_post_mu_terms": (ctypes.c_longlong, [_vp]),
+    "mce_swm_window": (_vp, [_vp, ctypes.c_int]),
+    "mce_swm_window_count": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "mce_swm_destroy": (None, [_vp]),
 }
 
 _LIB = None
@@ -101,6 +111,11 @@ def load(build_if_missing=True):
         f.argtypes = args
     _LIB = lib
     return lib
+
+
+def dp(a):
+    """A double* to a contiguous float64 array, or NULL for None."""
+    return None if a is None else a.ctypes.data_as(_dp)
 
 
 def last_error():

@@ -337,6 +337,8 @@ public:
     virtual void rel2d_pairs(const Rel2DArgs& a, cudaStream_t st) = 0;
 
     int E = 0, d = 0, cmcc = 0, pncc = 0, p = 0, MC = 0;
+    // the device the handle's streams and buffers live on
+    int device = 0;
     // When set (only by mce_batch_step_noalloc), the g-table kernel takes its
     // per-warp scratch from this caller-owned region instead of the handle's
     // own buffer, with as many warps as fit in it.
@@ -648,6 +650,7 @@ public:
         }
         int dev = 0;
         MCE_CUDA(cudaGetDevice(&dev));
+        device = dev;
         MCE_CUDA(cudaDeviceGetAttribute(&lc.num_sms, cudaDevAttrMultiProcessorCount, dev));
         MCE_CUDA(cudaStreamCreateWithFlags(&lc.stream, cudaStreamNonBlocking));
         MCE_CUDA(cudaEventCreate(&ev0));
@@ -656,6 +659,8 @@ public:
         MCE_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
         MCE_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
         int s = MCE_OK;
+        // profiling counters, sized here so no later step has to allocate them
+        s |= alg.ensure(2 * KID_COUNT);
         s |= dA0.ensure((size_t)E * D * D);
         s |= dp0.ensure((size_t)E * D);
         s |= db0.ensure((size_t)E * D);
@@ -2602,6 +2607,14 @@ int batch_step_in_fixed_scratch(mce_handle* h, void* scratch, size_t bytes, cons
 {
     if (!h || !scratch) return MCE_ERR_ARG;
     EngineBase* g = h->eng;
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess || cur != g->device) {
+        cudaGetLastError();
+        set_error("mce_batch_step_noalloc: the current device (" + std::to_string(cur) +
+                  ") is not the handle's device (" + std::to_string(g->device) +
+                  "); make the handle's device current first");
+        return MCE_ERR_DEVICE;
+    }
     // the launcher puts up to 4 warps in a block: one block's slots must fit
     const size_t need = 4 * g->gtable_scratch_bytes_per_warp();
     if (need > bytes) {

@@ -19,6 +19,12 @@ extern "C" {
 
 typedef struct mce_handle mce_handle;
 
+#ifdef __cplusplus
+#define MCE_BOOL bool
+#else
+#define MCE_BOOL _Bool
+#endif
+
 /* status codes */
 #define MCE_OK 0
 #define MCE_ERR_ARG (-1)       /* invalid argument */
@@ -78,9 +84,11 @@ int mce_batch_step(mce_handle* h, const double* msmt, const double* Phi, const d
  *    representative history, then mce_reset); a buffer that would have to
  *    grow stops the step with MCE_ERR_NOMEM, after which the handle must be
  *    reset.
- * The first call on a device looks the array up (cudaGetSymbolAddress); make
- * it before any stream capture.  Every call on a device shares the array:
- * calls that overlap on the GPU race, so serialise them. */
+ * The handle's device must be the current device (MCE_ERR_DEVICE otherwise:
+ * the array's address is looked up on the current device).  The first call
+ * on a device looks the array up (cudaGetSymbolAddress); make it before any
+ * stream capture.  Every call on a device shares the array: calls that
+ * overlap on the GPU race, so serialise them. */
 int mce_batch_step_noalloc(mce_handle* h, const double* msmt, const double* Phi, const double* Gamma,
                            const double* beta, const double* H, const double* gamma, const double* B, const double* u,
                            int shared_model, int* err_out);
@@ -211,6 +219,83 @@ double mce_rel2d_device_ms(mce_rel2d* r, int which);
 /* Kernels launched by mce_rel2d_create and every mce_rel2d_grid so far. */
 long long mce_rel2d_launch_count(mce_rel2d* r);
 void mce_rel2d_destroy(mce_rel2d* r);
+
+/* ---- window managers ---------------------------------------------------- */
+
+/* Eigen-decomposition of the symmetric n x n matrix A (row-major): evals[n],
+ * evecs[n*n] with eigenvector i in column i, by Householder tridiagonalisation
+ * and implicit-shift QL as the reference's sym_eig (include/eig_solve.hpp:404)
+ * computes it (same order and signs of the eigenvectors).  Host code. */
+int mce_sym_eig(int n, const double* A, double* evals, double* evecs);
+
+/* Speyer's restart statistics of a window about an estimate
+ * (speyers_window_init, include/cauchy_util.hpp:23-113, as
+ * pycauchy_speyers_window_init returns them, scripts/swig/cauchy/pycauchy.hpp:973):
+ * A0[n*n] (rows = eigenvectors of P + P H^T H P / s, s = gamma^2 + (z - H x)^2),
+ * p0[n], b0[n].  var_boost[n] (or NULL) is added to P's diagonal first; P is
+ * not modified.  Returns 1 when P had an eigenvalue below -1e-5 and its
+ * diagonal was raised (the reference prints a warning there), else MCE_OK.
+ * Host code. */
+int mce_speyers_window_init(int n, const double* xhat, const double* Phat, const double* H, double gamma, double z,
+                            const double* var_boost, double* A0, double* p0, double* b0);
+
+/* The reference's CauchyDynamicsUpdateContainer (include/dynamic_models.hpp:62-80),
+ * the struct LTV dynamics callbacks receive (same field order and types). */
+typedef struct mce_dynamics_container {
+    double* x;
+    double* u;
+    double dt;
+    int step;
+    int n;
+    int cmcc;
+    int pncc;
+    int p;
+    double* Phi;
+    double* Gamma;
+    double* B;
+    double* H;
+    double* beta;
+    double* gamma;
+    MCE_BOOL is_xbar_set_for_ece;
+    void* other_stuff;
+} mce_dynamics_container;
+typedef void (*mce_dynamics_callback)(mce_dynamics_container*);
+
+/* Sliding-window manager of the C++ front end: SlidingWindowManager(num_windows,
+ * num_sim_steps, A0, p0, b0, duc, ..., dyn_cb, ..., win_var_boost, ...)
+ * (include/cauchy_windows.hpp:814-1022), .step(msmts, controls) (:1025-1165)
+ * and .shutdown() (:1167), for n_mgr independent managers stepped together
+ * (one batched GPU handle per window slot).  Per-manager arrays are stacked:
+ * A0[n_mgr*d*d], p0, b0[n_mgr*d], Phi[n_mgr*d*d], Gamma[n_mgr*d*pncc],
+ * B[n_mgr*d*cmcc], beta[n_mgr*pncc], H[n_mgr*p*d], gamma[n_mgr*p].  dyn_cb
+ * (or NULL for LTI) is the LTV callback; each window and the manager call it
+ * on their own copy of the container, as the reference's window processes do.
+ * root_point[n_mgr*d] / b_pert[n_mgr*bpert_stride] (or both NULL: drawn with
+ * rand()) are shared by a manager's windows, as the reference's forked windows
+ * share the rand() state they inherit.  Logging options of the reference have
+ * no counterpart; the extended (nonlinear) manager is not provided. */
+typedef struct mce_swm mce_swm;
+mce_swm* mce_swm_create(int n_mgr, int num_windows, int num_sim_steps, int d, int cmcc, int pncc, int p,
+                        const double* A0, const double* p0, const double* b0, const double* Phi,
+                        const double* Gamma, const double* B, const double* beta, const double* H,
+                        const double* gamma, double dt, int init_step, mce_dynamics_callback dyn_cb,
+                        const double* win_var_boost, const double* root_point, const double* b_pert,
+                        int bpert_stride, int* status);
+/* SlidingWindowManager::step + the read-out pycauchy_step returns
+ * (scripts/swig/cauchy/pycauchy.hpp:187-221), per manager (each output may be
+ * NULL): fz[n_mgr], xhat[n_mgr*d], Phat[n_mgr*d*d], cerr_fz, cerr_xhat,
+ * cerr_Phat[n_mgr], win_idx[n_mgr], err_code[n_mgr].  msmts[n_mgr*p],
+ * controls[n_mgr*cmcc] (or NULL).  MCE_ERR_DONE after num_sim_steps steps;
+ * MCE_ERR_DEVICE when no window is usable (the reference exits). */
+int mce_swm_step(mce_swm* s, const double* msmts, const double* controls, double* fz, double* xhat, double* Phat,
+                 double* cerr_fz, double* cerr_xhat, double* cerr_Phat, int* win_idx, int* err_code);
+/* Terms present after every MU of every window since creation. */
+long long mce_swm_post_mu_terms(mce_swm* s);
+/* The batched handle of window slot j (for read-outs), and the steps window j
+ * has taken since its last restart. */
+mce_handle* mce_swm_window(mce_swm* s, int j);
+int mce_swm_window_count(mce_swm* s, int j);
+void mce_swm_destroy(mce_swm* s);
 
 /* Host wall time (ms) of the steps since the last mce_clear_profile: which = 0
  * whole steps, 1 input packing, 2 the moment checks after the device work. */
