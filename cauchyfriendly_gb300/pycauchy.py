@@ -7,11 +7,23 @@ scripts/swig/cauchy/pycauchy.hpp / pycauchy.i, so the reference's
 importable as ``pycauchy``.  Numpy arrays come in flattened (the numpy.i
 IN_ARRAY1 typemaps) and go out as float64 / int32 arrays (ARGOUTVIEWM_ARRAY1).
 
-Covered: pycauchy_initialize_lti / _ltv, pycauchy_single_step_ltiv,
-_get_number_of_terms, _set_master_step, _set_window_number, _get_duc, _reset,
-_shutdown, pycauchy_set_tr_search_idxs_ordering.  The window manager, the
-nonlinear (extended) mode, CPDF grids and relative-system functions of the
-SWIG module are not provided by this build.
+Covered:
+* single estimators: pycauchy_initialize_lti / _ltv / _nonlin,
+  pycauchy_single_step_ltiv / _nonlin / _deterministic_transform,
+  _get_number_of_terms, _set_master_step, _set_window_number, _get_duc,
+  _reset, _shutdown;
+* window restarts: pycauchy_get_reinitialization_statistics,
+  pycauchy_speyers_window_init (Speyer's statistics, computed by the
+  library's C++ with the reference's eigen-solver);
+* the C++ window manager: pycauchy_initialize_lti_window_manager / _ltv_,
+  pycauchy_step (8-tuple), pycauchy_shutdown -- one manager per process, as
+  the reference's globals allow;
+* pdf grids: pycauchy_get_marginal_1D/2D_pointwise_cpdf, _get_1D/2D_;
+  the relative system: pycauchy_single_step_eval_2d_rsys_cpdf;
+* pycauchy_set_tr_search_idxs_ordering (accepted, no effect: see its
+  docstring).
+Not provided: pycauchy_initialize_nonlin_window_manager (the extended-mode
+window manager).
 """
 from __future__ import annotations
 
@@ -309,10 +321,91 @@ def pycauchy_single_step_shutdown(h):
 
 
 def pycauchy_set_tr_search_idxs_ordering(ordering):
-    """pycauchy.hpp:994.  The axis order only changes how the reference walks
-    its sorted candidate lists; the reduction groups are the same for every
-    order, so the ordering is accepted and has no effect here."""
+    """pycauchy.hpp:994.  The ordering only says which axis of b the
+    reference searches first and in which order it prunes the others
+    (include/term_reduction.hpp:159-276): a candidate survives iff
+    b_i - eps < b_j <= b_i + eps on every axis, which no order changes, and
+    each survivor gets the same root whatever the order it is visited in.
+    The reduction groups, and so every result, are therefore the same for
+    every ordering (the reference's own runs under two orderings give the same
+    doubles: tests/golden/tr_ordering_three_state.npz); this build's term
+    reduction (grid buckets over all axes) has no ordering, and the call is
+    accepted with no effect.  Returns 1 for more than 12 axes, as the
+    reference does."""
     ordering = np.asarray(ordering).reshape(-1)
     if ordering.size > 12:
         return 1
     return 0
+
+
+def pycauchy_get_reinitialization_statistics(h, z, xhat, Phat, H, gamma):
+    """pycauchy.hpp:948-971: Speyer's restart statistics (A0 flattened, p0,
+    b0) about the estimate (xhat, Phat) and the measurement z with model row
+    H and scale gamma."""
+    return pycauchy_speyers_window_init(xhat, Phat, H, gamma, z)
+
+
+def pycauchy_speyers_window_init(x1_hat, Var, H, gamma, z):
+    """pycauchy.hpp:973-992 (speyers_window_init, cauchy_util.hpp:23-113):
+    (A0 flattened, p0, b0).  The caller's Var is not modified (the
+    reference raises its diagonal in place when it is indefinite)."""
+    from .windows import speyers_window_init
+    A0, p0, b0 = speyers_window_init(x1_hat, Var, H, gamma, z)
+    return A0.reshape(-1), p0, b0
+
+
+# The reference keeps its C++ window manager in a global (pycauchy.hpp:8):
+# one manager per process.
+_SWM = None
+
+
+def _init_window_manager(num_windows, num_sim_steps, A0, p0, b0, Phi, Gamma, B, beta, H, gamma, dt, init_step,
+                         win_var_boost, callback):
+    global _SWM
+    from .windows import CppSlidingWindowManager
+    n = int(np.asarray(b0).size)
+    if _SWM is not None:
+        _SWM.close()
+    f = lambda a: None if a is None or np.asarray(a).size == 0 else np.asarray(a, dtype=np.float64).reshape(1, -1)
+    wvb = None if win_var_boost is None or np.asarray(win_var_boost).size == 0 else win_var_boost
+    _SWM = CppSlidingWindowManager(num_windows, num_sim_steps, np.asarray(A0, dtype=np.float64).reshape(1, n, n),
+                                   f(p0), f(b0), f(Phi), f(Gamma), f(B), f(beta), f(H), f(gamma), dt=float(dt),
+                                   init_step=int(init_step), dyn_callback=callback, win_var_boost=wvb)
+
+
+def pycauchy_initialize_lti_window_manager(num_windows, num_sim_steps, A0, p0, b0, Phi, Gamma, B, beta, H, gamma,
+                                           debug_print, log_seq, log_full, log_dir, dt, init_step, win_var_boost):
+    """pycauchy.hpp:80-113: the C++ SlidingWindowManager over an LTI model
+    (the logging options have no counterpart and are ignored).  The windows'
+    root point and b_pert are drawn from the process's rand() state, once,
+    as the reference's forked windows each draw the same values."""
+    _init_window_manager(num_windows, num_sim_steps, A0, p0, b0, Phi, Gamma, B, beta, H, gamma, dt, init_step,
+                         win_var_boost, None)
+
+
+def pycauchy_initialize_ltv_window_manager(num_windows, num_sim_steps, A0, p0, b0, Phi, Gamma, B, beta, H, gamma,
+                                           f_dyn_update_callback, debug_print, log_seq, log_full, log_dir, dt,
+                                           init_step, win_var_boost):
+    """pycauchy.hpp:116-149: as the LTI manager, with the dynamics callback
+    (a raw C function pointer, int) that every window and the manager call on
+    their own copy of the dynamics container."""
+    _init_window_manager(num_windows, num_sim_steps, A0, p0, b0, Phi, Gamma, B, beta, H, gamma, dt, init_step,
+                         win_var_boost, int(f_dyn_update_callback))
+
+
+def pycauchy_step(msmts, controls):
+    """pycauchy.hpp:187-221: one step of the window manager; returns
+    (fz, xhat, Phat, cerr_fz, cerr_xhat, cerr_Phat, win_idx, err_code) of the
+    window chosen at this step."""
+    if _SWM is None:
+        raise RuntimeError("pycauchy_step: no window manager (call pycauchy_initialize_*_window_manager first)")
+    fz, x, P, cfz, cx, cP, wi, err = _SWM.step(msmts, controls)[0]
+    return float(fz), x.copy(), P.reshape(-1).copy(), float(cfz), float(cx), float(cP), wi, err
+
+
+def pycauchy_shutdown():
+    """pycauchy.hpp:223-228"""
+    global _SWM
+    if _SWM is not None:
+        _SWM.close()
+        _SWM = None

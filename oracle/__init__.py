@@ -26,7 +26,11 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE_INCLUDE = "/root/reference/include"
+# Where the reference checkout lies (read only at build time, by build()).
+REFERENCE_ROOT = os.environ.get("MCE_REFERENCE_ROOT", "/root/reference")
+# build() copies the reference's headers here (git-ignored) so that the
+# reference C++ can also be compiled on a host without the checkout.
+REF_SRC = os.path.join(REF_OUT, "src")
 ORACLE_SO = os.path.join(BUILD, "libmce_oracle.so")
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -39,28 +43,59 @@ def _ptr(a, kind=_dp):
     return a.ctypes.data_as(kind)
 
 
+def _refresh_reference_copy():
+    """Copies the reference's include/ and its SWIG glue header into
+    oracle/_ref/src (git-ignored), keeping their relative layout, when the
+    checkout is present.  Returns the include directory to compile against,
+    or None when neither the checkout nor a copy exists."""
+    import shutil
+    inc = os.path.join(REFERENCE_ROOT, "include")
+    if os.path.isdir(inc):
+        dst_inc = os.path.join(REF_SRC, "include")
+        glue = os.path.join(REFERENCE_ROOT, "scripts", "swig", "cauchy", "pycauchy.hpp")
+        dst_glue = os.path.join(REF_SRC, "scripts", "swig", "cauchy")
+        os.makedirs(dst_glue, exist_ok=True)
+        shutil.copytree(inc, dst_inc, dirs_exist_ok=True)
+        if os.path.exists(glue):
+            shutil.copy2(glue, dst_glue)
+    own = os.path.join(REF_SRC, "include")
+    return own if os.path.isdir(own) else None
+
+
+def host_cpus_pow2():
+    """The largest power of two <= the host's core count (the reference's
+    threaded term reduction and sort merges need a power of two)."""
+    n = 1
+    while n * 2 <= (os.cpu_count() or 1):
+        n *= 2
+    return n
+
+
 def build(force=False, with_reference=True, verbose=False):
-    """Compiles the oracle (always) and the reference harness (when the
-    reference headers are present).  -ffp-contract=off keeps a*b+c unfused on
-    every host so results match across x86 and aarch64."""
+    """Compiles the oracle (always) and the reference harnesses (when the
+    reference headers are present, as a checkout or as the copy in
+    oracle/_ref/src).  -ffp-contract=off keeps a*b+c unfused on every host so
+    results match across x86 and aarch64."""
     os.makedirs(BUILD, exist_ok=True)
     jobs = []
     src = os.path.join(HERE, "mce_oracle.cpp")
     if force or not os.path.exists(ORACLE_SO) or os.path.getmtime(ORACLE_SO) < os.path.getmtime(src):
         jobs.append(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-std=c++17", src,
                      "-o", ORACLE_SO, "-lpthread"])
-    if with_reference and os.path.isdir(REFERENCE_INCLUDE):
+    inc = _refresh_reference_copy() if with_reference else None
+    if inc:
         os.makedirs(REF_OUT, exist_ok=True)
-        hsrc = os.path.join(HERE, "ref_harness.cpp")
-        ncpu = 1
-        while ncpu * 2 <= (os.cpu_count() or 1):
-            ncpu *= 2
-        for name, n in (("libmce_ref_serial.so", 1), ("libmce_ref_threaded.so", ncpu)):
+        glue_dir = os.path.join(REF_SRC, "scripts", "swig", "cauchy")
+        ncpu = host_cpus_pow2()
+        targets = [("libmce_ref_serial.so", "ref_harness.cpp", 1), ("libmce_ref_threaded.so", "ref_harness.cpp", ncpu)]
+        if os.path.exists(os.path.join(glue_dir, "pycauchy.hpp")):
+            targets.append(("libmce_ref_pycauchy.so", "ref_pycauchy.cpp", 1))
+        for name, cpp, n in targets:
             out = os.path.join(REF_OUT, name)
+            hsrc = os.path.join(HERE, cpp)
             if force or not os.path.exists(out) or os.path.getmtime(out) < os.path.getmtime(hsrc):
-                jobs.append(["g++", "-O3", "-ffp-contract=off", "-fPIC", "-shared", "-w",
-                             "-I" + REFERENCE_INCLUDE, "-DHARNESS_NUM_CPUS=%d" % n, hsrc, "-o", out,
-                             "-lpthread"])
+                jobs.append(["g++", "-O3", "-ffp-contract=off", "-fPIC", "-shared", "-w", "-I" + inc,
+                             "-I" + glue_dir, "-DHARNESS_NUM_CPUS=%d" % n, hsrc, "-o", out, "-lpthread"])
     procs = [subprocess.Popen(j, stdout=subprocess.PIPE, stderr=subprocess.STDOUT) for j in jobs]
     for j, p in zip(jobs, procs):
         out, _ = p.communicate()
@@ -561,3 +596,59 @@ def run_oracle_batch(probs, constants, threads=None):
     with ThreadPoolExecutor(max_workers=threads) as ex:
         counts = list(ex.map(one, range(len(probs))))
     return int(sum(counts)), time.perf_counter() - t0
+
+
+# ---- the reference's own C++ over a process pool (CPU baseline) ------------
+# One estimator per task, the serial build in every worker: the reference's
+# estimator keeps process-wide state (function pointers, flags, the harness's
+# raw-moment hook), so independent estimators run in separate processes, as the
+# reference's own window manager runs its windows.
+
+_POOL_PROBS = None
+_POOL_SEEDS = None
+
+
+def _pool_init(probs, seeds):
+    global _POOL_PROBS, _POOL_SEEDS
+    _POOL_PROBS, _POOL_SEEDS = probs, seeds
+    # the reference prints warnings on stdout; keep the caller's stdout clean
+    devnull = os.open(os.devnull, os.O_WRONLY)
+    os.dup2(devnull, 1)
+
+
+def _pool_run(i):
+    prob = _POOL_PROBS[i]
+    est = Reference(prob, seed=_POOL_SEEDS[i])
+    for k in range(prob["steps"]):
+        for s in range(prob["p"]):
+            est.step(k, s)
+    est.close()
+    return 1
+
+
+class ReferencePool:
+    """The reference's C++ (oracle/_ref, serial build) stepping independent
+    estimators in `workers` processes (spawned).  run(indices) steps every
+    listed estimator through its whole history and returns the wall seconds
+    (the post-MU term count of the same work comes from the oracle port,
+    which the tests hold equal to the reference's)."""
+
+    def __init__(self, probs, seeds, workers=None):
+        import multiprocessing as mp
+        self.workers = workers or (os.cpu_count() or 1)
+        self.probs = probs
+        self.pool = mp.get_context("spawn").Pool(self.workers, initializer=_pool_init, initargs=(probs, seeds))
+
+    def run(self, indices=None):
+        import time
+        idx = list(range(len(self.probs))) if indices is None else list(indices)
+        # largest first (term counts grow about 3x per step), handed out one by one
+        idx.sort(key=lambda i: -self.probs[i]["steps"] * self.probs[i]["p"])
+        t0 = time.perf_counter()
+        done = sum(self.pool.imap_unordered(_pool_run, idx, chunksize=1))
+        assert done == len(idx)
+        return time.perf_counter() - t0
+
+    def close(self):
+        self.pool.terminate()
+        self.pool.join()

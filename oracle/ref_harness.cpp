@@ -97,9 +97,11 @@ void* ref_create(const double* A0, const double* p0, const double* b0, int steps
 
 void ref_destroy(void* vh)
 {
-    // The reference's teardown helpers are not exercised here: the harness
-    // lives in short test processes, so its arenas are simply released at exit.
+    // runs the reference's own destructor (its arenas are released), so a
+    // process can step many estimators one after another
     RefHandle* h = (RefHandle*)vh;
+    delete h->cpdf;
+    delete h->est;
     free(h->raw_mean);
     free(h->raw_cov);
     delete h;

@@ -1,10 +1,61 @@
 """Host logic of the sliding-window manager (cauchyfriendly_gb300.windows) on
 CPU: Speyer's restart statistics and the window bookkeeping, driven by
 oracle estimators (no GPU)."""
+import os
+
 import numpy as np
 
 import oracle
 from cauchyfriendly_gb300 import windows, workloads as W
+from tests import golden_cases as G
+
+
+def test_speyer_restart_matches_reference_kats():
+    """The library's C++ Speyer restart (mce_speyers_window_init, host code:
+    no GPU needed) against the reference's pycauchy_speyers_window_init on 24
+    random estimates of 2-7 states, 6 of them with an indefinite covariance
+    that the restart boosts first (tests/golden/speyer_kats.npz): the same
+    doubles -- eigenvector order and signs included."""
+    z = np.load(os.path.join(G.GOLDEN, "speyer_kats.npz"))
+    boosted = 0
+    for i in range(int(z["count"])):
+        pre = "k%d_" % i
+        A0, p0, b0 = windows.speyers_window_init(z[pre + "x"], z[pre + "P"], z[pre + "H"], float(z[pre + "gamma"]),
+                                                 float(z[pre + "z"]))
+        assert np.array_equal(A0, z[pre + "A0"]), (i, G.relerr(A0, z[pre + "A0"]))
+        assert np.array_equal(p0, z[pre + "p0"]), (i, G.relerr(p0, z[pre + "p0"]))
+        assert np.array_equal(b0, z[pre + "b0"]), (i, G.relerr(b0, z[pre + "b0"]))
+        boosted += np.linalg.eigvalsh(z[pre + "P"]).min() < -1e-5
+    assert boosted == 6
+    # the drop-in module returns them flattened, as the SWIG module does
+    from cauchyfriendly_gb300 import pycauchy
+    a, p, b = pycauchy.pycauchy_speyers_window_init(z["k0_x"], z["k0_P"].reshape(-1), z["k0_H"],
+                                                    float(z["k0_gamma"]), float(z["k0_z"]))
+    assert np.array_equal(a, z["k0_A0"].reshape(-1)) and np.array_equal(p, z["k0_p0"])
+
+
+def test_sym_eig_is_an_eigen_decomposition():
+    rng = np.random.default_rng(3)
+    for n in (1, 2, 5, 8):
+        M = rng.standard_normal((n, n))
+        S = M + M.T
+        w, V = windows.sym_eig(S)
+        assert np.allclose(S @ V, V * w, atol=1e-12)
+        assert np.allclose(V.T @ V, np.eye(n), atol=1e-12)
+        assert np.allclose(np.sort(w), np.linalg.eigvalsh(S), atol=1e-12)
+
+
+def test_reference_results_do_not_depend_on_search_axis_ordering():
+    """The reference itself under two term-reduction search-axis orderings
+    (pycauchy_set_tr_search_idxs_ordering) gives the same doubles at every
+    update (tests/golden/tr_ordering_three_state.npz), which is why the
+    drop-in accepts the ordering with no effect."""
+    z = np.load(os.path.join(G.GOLDEN, "tr_ordering_three_state.npz"))
+    assert len(z["orderings"]) == 2 and not np.array_equal(z["orderings"][0], z["orderings"][1])
+    for k in range(int(z["steps"])):
+        for q in ("x", "P", "fz", "err", "nt"):
+            assert np.array_equal(z["o0_s%d_%s" % (k, q)], z["o1_s%d_%s" % (k, q)]), (k, q)
+    assert int(z["o0_s%d_nt" % (int(z["steps"]) - 1)]) > 1000
 
 
 def test_speyer_restart_statistics():
