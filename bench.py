@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the one-estimator-per-handle comparison")
+    ap.add_argument("--plain-stride", type=int, default=16)
     ap.add_argument("--workload", default="batched3", choices=["batched3", "windows5", "rel2d"],
                     help="batched3: the batched 3-state configuration (default); windows5: the sliding-window "
                          "5-state LTV configuration for --window-steps steps; rel2d: the relative 2-D system of "
@@ -190,89 +192,117 @@ def combine_ranks(dev_ms, wall_s, terms, device):
     return float(t[0]), float(t[1]), int(round(float(n[0])))
 
 
-def cpu_sample(probs, consts, target_seconds):
-    """Bounded sample of the same workload for the CPU baseline: every k-th
-    estimator, k chosen so the oracle port needs about target_seconds."""
+def _cpu_pass_fn(probs, consts, seeds, threads):
+    """A function timing one pass of the CPU implementation over a list of
+    estimator indices: the reference's own C++ (oracle/_ref, built on this
+    host from the reference's headers) in a process pool when it is built,
+    else the oracle port on a thread pool.  Returns (fn, kind, closer)."""
+    import oracle
+    oracle.build(with_reference=True)
+    if oracle.reference_available():
+        pool = oracle.ReferencePool(probs, seeds, threads)
+        return pool.run, "reference", pool.close
+
+    def port(idx):
+        return oracle.run_oracle_batch([probs[i] for i in idx], [consts[i] for i in idx], threads)[1]
+    return port, "port", lambda: None
+
+
+def _post_mu_terms(probs, consts, idx, threads):
     import oracle
     oracle.build(with_reference=False)
+    return oracle.run_oracle_batch([probs[i] for i in idx], [consts[i] for i in idx], threads)[0]
+
+
+def cpu_sample(probs, consts, seeds, target_seconds):
+    """Bounded sample of the same workload for the CPU baseline: every k-th
+    estimator, k chosen so one pass needs about target_seconds, on all host
+    cores."""
     threads = os.cpu_count() or 1
-    # calibrate on a small stride sample
-    k = 64
-    sub = probs[::k]
-    sc = [consts[i] for i in range(0, len(probs), k)]
-    n, t = oracle.run_oracle_batch(sub, sc, threads)
-    if t < target_seconds * 0.3 and k > 1:
-        k = max(1, int(k * t / (target_seconds * 0.5)))
-        sub = probs[::k]
-        sc = [consts[i] for i in range(0, len(probs), k)]
-        n, t = oracle.run_oracle_batch(sub, sc, threads)
-    return {"value": n / t, "unit": UNIT, "cores": threads, "kind": "port",
+    fn, kind, close = _cpu_pass_fn(probs, consts, seeds, threads)
+    try:
+        k = 64
+        t = fn(list(range(0, len(probs), k)))
+        if t < target_seconds * 0.3:
+            k = max(1, int(k * t / (target_seconds * 0.5)))
+        idx = list(range(0, len(probs), k))
+        t = fn(idx)
+    finally:
+        close()
+    n = _post_mu_terms(probs, consts, idx, threads)
+    return {"value": n / t, "unit": UNIT, "cores": threads, "kind": kind,
             "sample": "every %d-th estimator of the batch (%d estimators, %d post-MU terms, %.1f s)"
-                      % (k, len(sub), n, t)}
+                      % (k, len(idx), n, t)}
 
 
 def run_reference(args):
-    """Reference arm: the CPU implementation of the path on this host's cores,
-    over a bounded sample of the same batch (every 32nd estimator) per step.
-    Uses the reference's own C++ (oracle/_ref, compiled from its headers) when
-    it is built on this host, otherwise the oracle port."""
+    """Reference arm: the reference's own C++ (oracle/_ref, compiled on this
+    host from the reference's headers; serial build, one process per host
+    core, one estimator per task) stepping the whole batch of the gb300 arm
+    -- the same 4096 estimators, measurement histories and rand()-drawn
+    constants -- once per step.  Falls back to the oracle port on all host
+    threads where the reference is not built."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     from cauchyfriendly_gb300 import workloads as W
     import oracle
-    oracle.build(with_reference=True)
     probs = W.batched_three_state(args.n_est, seed=args.seed)
-    stride = 32
-    idx = list(range(0, len(probs), stride))
-    sub = [probs[i] for i in idx]
-    seeds = [args.seed * 100003 + i for i in idx]
-    consts = [oracle.draw_reference_constants(s, p["d"], oracle.max_shape_of(p)) for s, p in zip(seeds, sub)]
+    seeds = [args.seed * 100003 + i for i in range(len(probs))]
+    consts = [oracle.draw_reference_constants(s, p["d"], oracle.max_shape_of(p)) for s, p in zip(seeds, probs)]
     threads = os.cpu_count() or 1
-    use_ref = oracle.reference_available()
-    # terms after each MU of the sample (identical for the reference and the port)
-    n_terms, _ = oracle.run_oracle_batch(sub, consts, threads)
-
-    def one_pass():
-        if use_ref:
-            return _ref_pass(sub, seeds, threads)
-        return oracle.run_oracle_batch(sub, consts, threads)[1]
-
-    for _ in range(args.warmup):
-        one_pass()
-    tot_t = 0.0
-    for _ in range(args.steps):
-        tot_t += one_pass()
+    fn, kind, close = _cpu_pass_fn(probs, consts, seeds, threads)
+    idx = list(range(len(probs)))
+    try:
+        for _ in range(args.warmup):
+            fn(idx)
+        tot_t = 0.0
+        for _ in range(args.steps):
+            tot_t += fn(idx)
+    finally:
+        close()
+    # terms present after each MU of the batch (the GPU path and the reference agree exactly)
+    n_terms = _post_mu_terms(probs, consts, idx, threads)
     v = n_terms * args.steps / tot_t
-    kind = "reference" if use_ref else "port"
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "sample_stride": stride},
+            "data": "synthetic", "config": {"workload": WORKLOAD, "n_estimators": args.n_est, "seed": args.seed,
+                                            "terms_per_step": n_terms},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
-                             "sample": "every %d-th estimator of the batch per step (%d estimators, %d terms)" %
-                                       (stride, len(sub), n_terms)},
+                             "sample": "the whole batch per step (%d estimators, %d post-MU terms); %s" %
+                                       (len(probs), n_terms,
+                                        "the reference's C++, serial build, %d processes" % threads
+                                        if kind == "reference" else "oracle port, %d threads" % threads)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def _ref_pass(probs, seeds, threads):
-    """The reference's own C++ (oracle/_ref) on a thread pool, one estimator per
-    task; each estimator is seeded so its rand()-drawn constants equal the GPU
-    run's.  Returns wall seconds."""
-    import oracle
-    from concurrent.futures import ThreadPoolExecutor
-
-    def one(i):
-        est = oracle.Reference(probs[i], seed=seeds[i])
-        for k in range(probs[i]["steps"]):
-            est.step(k, 0)
+def plain_sample(probs, consts, stride):
+    """The plain path the metric compares against: one estimator per handle
+    (mce_create / mce_step, one launch sequence per estimator and update), on
+    every stride-th estimator of the batch.  Returns post-MU terms, device
+    seconds and wall seconds of the steps (handle creation excluded)."""
+    from cauchyfriendly_gb300 import CauchyEstimator
+    import torch
+    terms = 0
+    dev = wall = 0.0
+    for i in range(0, len(probs), stride):
+        p = probs[i]
+        ms = (p["steps"] - 1) * p["pncc"] + p["d"]
+        est = CauchyEstimator(p["A0"], p["p0"], p["b0"], p["steps"], p["d"], 0, p["pncc"], p["p"],
+                              root_point=consts[0][i], b_pert=consts[1][i][:ms])
+        d0 = est._lib.mce_device_time_ms(est._h)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(p["steps"]):
+            est.step(p["msmts"][k, 0], p["Phi"], p["Gamma"], p["beta"], p["H"][0], p["gamma"][0])
+        torch.cuda.synchronize()
+        wall += time.perf_counter() - t0
+        dev += (est._lib.mce_device_time_ms(est._h) - d0) / 1e3
+        terms += int(est._lib.mce_post_mu_terms(est._h))
         est.close()
-
-    t0 = time.perf_counter()
-    with ThreadPoolExecutor(max_workers=threads) as ex:
-        list(ex.map(one, range(len(probs))))
-    return time.perf_counter() - t0
+    return terms, dev, wall
 
 
 def run_windows5(args):
@@ -603,8 +633,16 @@ def main():
         "roofline": roofline,
         "clocks": clocks,
     }
+    if rank == 0 and not args.no_plain:
+        # batched vs plain: the same estimators one handle at a time
+        pt, pdev, pwall = plain_sample(probs, consts, args.plain_stride)
+        line["plain"] = {"workload": "every %d-th estimator of the batch, one handle each (mce_create/mce_step)"
+                                     % args.plain_stride, "terms": pt, "value_device": pt / pdev,
+                         "value_wall": pt / pwall, "unit": UNIT}
+        line["batched_over_plain"] = {"device": value / (pt / pdev), "wall": e2e / (pt / pwall)}
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_sample(probs, list(zip(consts[0], consts[1])), args.cpu_seconds)
+        seeds = [args.seed * 100003 + i for i in range(len(probs))]
+        line["cpu_baseline"] = cpu_sample(probs, list(zip(consts[0], consts[1])), seeds, args.cpu_seconds)
     est.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
