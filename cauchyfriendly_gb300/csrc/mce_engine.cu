@@ -310,6 +310,9 @@ public:
                            int* keys, double* g) = 0;
     virtual long long total_cells(int est) = 0;
     virtual int reset() = 0;
+    // copies estimator e's start statistics to the device, where the next
+    // first update reads them
+    virtual int upload_start(int e) = 0;
     // every current term of estimator e: b += v (sub = 0) or b -= v (sub = 1)
     virtual int shift_terms_b(int e, const double* v, int sub) = 0;
     // every current term of estimator e: time_prop with Phi and B u (Bu may be null)
@@ -727,6 +730,15 @@ public:
     {
         if (lc.stream) cudaStreamSynchronize(lc.stream);
         if (mstream) cudaStreamSynchronize(mstream);
+    }
+
+    int upload_start(int e) override
+    {
+        MCE_CUDA(cudaMemcpy(dA0.ptr + (size_t)e * D * D, est[e].A0.data(), D * D * sizeof(double),
+                            cudaMemcpyHostToDevice));
+        MCE_CUDA(cudaMemcpy(dp0.ptr + (size_t)e * D, est[e].p0.data(), D * sizeof(double), cudaMemcpyHostToDevice));
+        MCE_CUDA(cudaMemcpy(db0.ptr + (size_t)e * D, est[e].b0.data(), D * sizeof(double), cudaMemcpyHostToDevice));
+        return MCE_OK;
     }
 
     int reset() override
@@ -2532,7 +2544,9 @@ int mce_reinitialize_start_statistics(mce_handle* h, int e, const double* A0, co
     s.A0.assign(A0, A0 + d * d);
     s.p0.assign(p0, p0 + d);
     s.b0.assign(b0, b0 + d);
-    return MCE_OK;
+    // the reference re-creates the first term at once (setup_first_term,
+    // cauchy_estimator.hpp:1302-1309): the next first update starts from these
+    return h->eng->upload_start(e);
 }
 int mce_set_master_step(mce_handle* h, int ms)
 {
