@@ -83,6 +83,12 @@ SIGNATURES = {
     "mce_swm_window": (_vp, [_vp, ctypes.c_int]),
     "mce_swm_window_count": (ctypes.c_int, [_vp, ctypes.c_int]),
     "mce_swm_destroy": (None, [_vp]),
+    "mce_adjoint_create": (_vp, [ctypes.c_int] * 4 + [_dp] * 5 + [_ip]),
+    "mce_adjoint_forward": (ctypes.c_int, [_vp] + [_dp] * 7),
+    "mce_adjoint_num_params": (ctypes.c_int, [_vp]),
+    "mce_adjoint_backward": (ctypes.c_int, [_vp, _dp, _dp]),
+    "mce_adjoint_check": (ctypes.c_int, [_vp, _dp, _dp]),
+    "mce_adjoint_destroy": (None, [_vp]),
 }
 
 _LIB = None

@@ -1,0 +1,152 @@
+"""Gradients of the accumulated log-likelihood of an MCE run.
+
+``AdjointRun`` records one estimator's run through the GPU step path
+(mce_adjoint_* in libmce_gb300.so) and returns the gradient of
+sum_k w_k Re(fz_k) with respect to (beta, gamma, p0, Phi, Gamma, H), holding
+the enumerated cell structure fixed; fz_k = 1/(2 pi G_SCALE_FACTOR_k)
+(include/cauchy_estimator.hpp:340-357) is the normaliser of update k.
+Because every g-table is rescaled by 1/(2 pi Re fz_k) after update k and the
+rest of the computation is linear in the tables, sum_k log Re fz_k over a run
+is log Re of the unscaled last fz, so its gradient is one seed,
+w_K = 1/Re fz_K, on the last update (``loglik_weights``).
+
+``MCELogLikelihood`` exposes it as a torch.autograd.Function over float64
+tensors: forward runs the estimator and returns sum_k log fz_k, backward the
+hand-written adjoint.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+PARAM_NAMES = ("beta", "gamma", "p0", "Phi", "Gamma", "H")
+
+
+def loglik_weights(fz):
+    """Seeds of sum_k log Re fz_k: 1/Re fz on the last update, 0 elsewhere."""
+    w = np.zeros(len(fz))
+    w[-1] = 1.0 / fz[-1]
+    return w
+
+
+class AdjointRun:
+    """One estimator (LTI model, no controls) of d states, pncc process-noise
+    columns and p measurements per step, run for `steps` steps from
+    (A0, p0, b0).  root_point / b_pert are the constants the reference draws
+    with rand() (see oracle.draw_reference_constants / mce_draw_reference_constants)."""
+
+    def __init__(self, d, pncc, p, steps, A0, p0, b0, root_point, b_pert):
+        self._L = _lib.load()
+        self.d, self.pncc, self.p, self.steps = int(d), int(pncc), int(p), int(steps)
+        f = lambda a: np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(-1))
+        self.A0, self.b0 = f(A0), f(b0)
+        self.root_point, self.b_pert = f(root_point), f(b_pert)
+        st = ctypes.c_int(0)
+        self._h = self._L.mce_adjoint_create(self.d, self.pncc, self.p, self.steps, _lib.dp(self.A0),
+                                             _lib.dp(f(p0)), _lib.dp(self.b0), _lib.dp(self.root_point),
+                                             _lib.dp(self.b_pert), ctypes.byref(st))
+        if not self._h:
+            raise _lib.MceError("mce_adjoint_create failed (%d): %s" % (st.value, _lib.last_error()))
+        self.fz = None
+
+    def forward(self, msmts, Phi, Gamma, beta, H, gamma, p0=None):
+        """Runs and records every update; returns Re fz of each.  p0 (or None:
+        the constructor's) is the initial scale vector of this run."""
+        f = lambda a: np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(-1))
+        if p0 is not None:
+            self._recreate(f(p0))
+        self._model = [f(x) for x in (msmts, Phi, Gamma, beta, H, gamma)]
+        fz = np.zeros(self.steps * self.p)
+        _lib.check(self._L.mce_adjoint_forward(self._h, *[_lib.dp(x) for x in self._model], _lib.dp(fz)),
+                   "mce_adjoint_forward")
+        self.fz = fz
+        return fz
+
+    def _recreate(self, p0):
+        self._L.mce_adjoint_destroy(self._h)
+        st = ctypes.c_int(0)
+        self._h = self._L.mce_adjoint_create(self.d, self.pncc, self.p, self.steps, _lib.dp(self.A0), _lib.dp(p0),
+                                             _lib.dp(self.b0), _lib.dp(self.root_point), _lib.dp(self.b_pert),
+                                             ctypes.byref(st))
+        if not self._h:
+            raise _lib.MceError("mce_adjoint_create failed (%d): %s" % (st.value, _lib.last_error()))
+
+    def backward(self, w):
+        """Gradient of sum_k w_k Re fz_k as a dict of arrays shaped like the
+        parameters (beta (pncc,), gamma (p,), p0 (d,), Phi (d, d),
+        Gamma (d, pncc), H (p, d))."""
+        w = np.ascontiguousarray(np.asarray(w, dtype=np.float64).reshape(-1))
+        n = self._L.mce_adjoint_num_params(self._h)
+        g = np.zeros(n)
+        _lib.check(self._L.mce_adjoint_backward(self._h, _lib.dp(w), _lib.dp(g)), "mce_adjoint_backward")
+        d, pncc, p = self.d, self.pncc, self.p
+        shapes = ((pncc,), (p,), (d,), (d, d), (d, pncc), (p, d))
+        out, k = {}, 0
+        for name, sh in zip(PARAM_NAMES, shapes):
+            sz = int(np.prod(sh))
+            out[name] = g[k:k + sz].reshape(sh)
+            k += sz
+        return out
+
+    def check(self):
+        """(largest relative difference of the recorded g-tables, of the
+        recorded Re fz) from the GPU run."""
+        a, b = ctypes.c_double(), ctypes.c_double()
+        _lib.check(self._L.mce_adjoint_check(self._h, ctypes.byref(a), ctypes.byref(b)), "mce_adjoint_check")
+        return a.value, b.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.mce_adjoint_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _make_function():
+    import torch
+
+    class MCELogLikelihood(torch.autograd.Function):
+        """sum_k log fz_k of one estimator's run as a differentiable function
+        of (beta, gamma, p0, Phi, Gamma, H), float64 tensors; `run` is an
+        AdjointRun and `msmts` the measurement history (steps, p).  The
+        backward pass is the library's adjoint (mce_adjoint_backward)."""
+
+        @staticmethod
+        def forward(ctx, beta, gamma, p0, Phi, Gamma, H, run, msmts):
+            np_ = lambda t: t.detach().cpu().numpy().astype(np.float64)
+            fz = run.forward(msmts, np_(Phi), np_(Gamma), np_(beta), np_(H), np_(gamma), p0=np_(p0))
+            ctx.run = run
+            ctx.w = loglik_weights(fz)
+            ctx.like = [beta, gamma, p0, Phi, Gamma, H]
+            return torch.tensor(float(np.sum(np.log(fz))), dtype=torch.float64)
+
+        @staticmethod
+        def backward(ctx, gout):
+            g = ctx.run.backward(ctx.w)
+            outs = []
+            for name, like in zip(PARAM_NAMES, ctx.like):
+                outs.append(gout * torch.as_tensor(g[name].reshape(like.shape), dtype=like.dtype,
+                                                   device=like.device))
+            return (*outs, None, None)
+
+    return MCELogLikelihood
+
+
+_FN = None
+
+
+def mce_log_likelihood(beta, gamma, p0, Phi, Gamma, H, run, msmts):
+    """sum_k log fz_k of `run` (an AdjointRun) over `msmts`, differentiable in
+    the six parameter tensors (torch.autograd.Function)."""
+    global _FN
+    if _FN is None:
+        _FN = _make_function()
+    return _FN.apply(beta, gamma, p0, Phi, Gamma, H, run, msmts)

@@ -297,6 +297,37 @@ mce_handle* mce_swm_window(mce_swm* s, int j);
 int mce_swm_window_count(mce_swm* s, int j);
 void mce_swm_destroy(mce_swm* s);
 
+/* ---- adjoint ------------------------------------------------------------ */
+
+/* Gradient of sum_k w_k Re(fz_k) over one estimator's run -- and with
+ * w_K = 1/Re(fz_K) on the last update alone, of the accumulated
+ * log-likelihood sum_k log fz_k, fz_k = 1/(2 pi G_SCALE_FACTOR_k)
+ * (include/cauchy_estimator.hpp:340-357) -- with respect to the model's
+ * scales and matrices, holding the enumerated cell structure fixed.  No
+ * counterpart in the reference (which has no derivatives); the forward run is
+ * the GPU step path of CauchyEstimator::step.  LTI model, no controls.
+ *   create: d states, pncc process-noise columns, p measurements per step,
+ *           `steps` steps; A0[d*d], p0[d], b0[d]; root_point[d] and
+ *           b_pert[(steps-1)*pncc+d] as for mce_create (required here).
+ *   forward: runs every update (msmts[steps*p]; Phi[d*d], Gamma[d*pncc],
+ *           beta[pncc], H[p*d], gamma[p]) and records it; fz_raw[steps*p]
+ *           (or NULL) receives Re fz of every update.
+ *   backward: w[steps*p] seeds; grad[mce_adjoint_num_params] receives the
+ *           gradient in the order beta, gamma, p0, Phi (row-major), Gamma
+ *           (row-major), H (row-major).
+ *   check: the largest relative difference between the recorded tape and the
+ *           GPU run (every kept g-table, every Re fz); both ~1e-15 when the
+ *           tape describes the run. */
+typedef struct mce_adjoint mce_adjoint;
+mce_adjoint* mce_adjoint_create(int d, int pncc, int p, int steps, const double* A0, const double* p0,
+                                const double* b0, const double* root_point, const double* b_pert, int* status);
+int mce_adjoint_forward(mce_adjoint* a, const double* msmts, const double* Phi, const double* Gamma,
+                        const double* beta, const double* H, const double* gamma, double* fz_raw);
+int mce_adjoint_num_params(mce_adjoint* a);
+int mce_adjoint_backward(mce_adjoint* a, const double* w, double* grad);
+int mce_adjoint_check(mce_adjoint* a, double* max_table_rel_err, double* max_fz_rel_err);
+void mce_adjoint_destroy(mce_adjoint* a);
+
 /* Host wall time (ms) of the steps since the last mce_clear_profile: which = 0
  * whole steps, 1 input packing, 2 the moment checks after the device work. */
 double mce_host_time_ms(mce_handle* h, int which);

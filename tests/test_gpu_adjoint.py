@@ -1,0 +1,129 @@
+"""The adjoint of the accumulated log-likelihood (cauchyfriendly_gb300.adjoint,
+mce_adjoint_* in the library) on the GPU:
+
+* the recorded tape describes the GPU run: every kept g-table and every Re fz
+  recomputed from it agree with the run's within 1e-12;
+* the gradient of sum_k log fz_k with respect to (beta, gamma, p0, Phi,
+  Gamma, H) agrees with central finite differences of the REFERENCE's own
+  log-likelihood (tests/golden/adj_*.npz, made by the unmodified reference)
+  and with central finite differences of the GPU forward run;
+* the torch.autograd.Function returns the same value and gradient.
+
+Finite differences carry their own error (the fixtures keep a second set at a
+quarter of the step to show it), so the gradients are compared within 1e-4
+relative per entry, with a floor of 1e-6 of the largest entry.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from tests import golden_cases as G
+
+pytestmark = pytest.mark.gpu
+
+NAMES = ("beta", "gamma", "p0", "Phi", "Gamma", "H")
+
+
+def _need_gpu():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def _load(name):
+    return np.load(os.path.join(G.GOLDEN, name + ".npz"))
+
+
+def _run(z):
+    from cauchyfriendly_gb300.adjoint import AdjointRun
+    return AdjointRun(int(z["d"]), int(z["pncc"]), int(z["p"]), int(z["steps"]), z["A0"], z["p0"], z["b0"],
+                      z["root_point"], z["b_pert"])
+
+
+def _flat(g):
+    return np.concatenate([np.asarray(g[n]).reshape(-1) for n in NAMES])
+
+
+def _params(z):
+    return {n: np.asarray(z[n], dtype=np.float64) for n in NAMES}
+
+
+def _loglik(run, z, P):
+    fz = run.forward(z["msmts"].reshape(-1), P["Phi"], P["Gamma"], P["beta"], P["H"], P["gamma"], p0=P["p0"])
+    return float(np.sum(np.log(fz))), fz
+
+
+def _close(a, b, rtol=1e-4, floor=1e-6):
+    a = np.asarray(a); b = np.asarray(b)
+    tol = rtol * np.abs(b) + floor * np.max(np.abs(b))
+    return np.all(np.abs(a - b) <= tol), np.max(np.abs(a - b) / (np.abs(b) + floor * np.max(np.abs(b))))
+
+
+@pytest.mark.parametrize("name", ["adj_four_state", "adj_five_state_two_msmt"])
+def test_adjoint_matches_reference_finite_differences(name):
+    _need_gpu()
+    from cauchyfriendly_gb300.adjoint import loglik_weights
+    z = _load(name)
+    run = _run(z)
+    P = _params(z)
+    L, fz = _loglik(run, z, P)
+    # the GPU run's log-likelihood is the reference's
+    assert abs(L - float(z["loglik"])) <= 1e-9 * abs(float(z["loglik"])), (L, float(z["loglik"]))
+    te, fe = run.check()
+    assert te <= 1e-12 and fe <= 1e-12, (te, fe)
+    g = _flat(run.backward(loglik_weights(fz)))
+    ok, err = _close(g, z["fd_grad"])
+    assert ok, (err, g, z["fd_grad"])
+    run.close()
+
+
+def test_adjoint_matches_gpu_finite_differences():
+    """Central differences of the GPU forward run itself, on a second seed
+    of the four-state problem and a seed other than the loglik one."""
+    _need_gpu()
+    import oracle
+    from cauchyfriendly_gb300 import workloads as W
+    from cauchyfriendly_gb300.adjoint import loglik_weights
+    prob = W.four_state_lti(seed=9, steps=5)
+    rp, bp = oracle.draw_reference_constants(77, 4, oracle.max_shape_of(prob))
+    z = dict(prob)
+    z["root_point"], z["b_pert"] = rp, bp
+    run = _run(z)
+    P = _params(z)
+    L, fz = _loglik(run, z, P)
+    g = run.backward(loglik_weights(fz))
+    fd = {}
+    for n in NAMES:
+        a = P[n]
+        fd[n] = np.zeros_like(a)
+        for idx in np.ndindex(a.shape):
+            h = 1e-6 * max(abs(a[idx]), 1e-3)
+            Pp = {k: v.copy() for k, v in P.items()}
+            Pm = {k: v.copy() for k, v in P.items()}
+            Pp[n][idx] += h
+            Pm[n][idx] -= h
+            fd[n][idx] = (_loglik(run, z, Pp)[0] - _loglik(run, z, Pm)[0]) / (2 * h)
+    ok, err = _close(_flat(g), _flat(fd))
+    assert ok, err
+    run.close()
+
+
+def test_torch_function_gives_the_adjoint_gradient():
+    _need_gpu()
+    import torch
+    from cauchyfriendly_gb300.adjoint import loglik_weights, mce_log_likelihood
+    z = _load("adj_four_state")
+    run = _run(z)
+    ts = [torch.tensor(np.asarray(z[n], dtype=np.float64), requires_grad=True) for n in NAMES]
+    L = mce_log_likelihood(*ts, run, z["msmts"].reshape(-1))
+    assert abs(float(L) - float(z["loglik"])) <= 1e-9 * abs(float(z["loglik"]))
+    grads = torch.autograd.grad(L, ts)
+    run2 = _run(z)
+    P = _params(z)
+    _, fz = _loglik(run2, z, P)
+    want = run2.backward(loglik_weights(fz))
+    for n, gt in zip(NAMES, grads):
+        assert np.allclose(gt.numpy(), want[n], rtol=1e-12, atol=1e-14), n
+    run.close()
+    run2.close()
