@@ -53,7 +53,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the one-estimator-per-handle comparison")
     ap.add_argument("--plain-stride", type=int, default=16)
-    ap.add_argument("--workload", default="batched3", choices=["batched3", "windows5", "rel2d"],
+    ap.add_argument("--adjoint-steps", type=int, default=100)
+    ap.add_argument("--workload", default="batched3", choices=["batched3", "windows5", "rel2d", "adjoint"],
                     help="batched3: the batched 3-state configuration (default); windows5: the sliding-window "
                          "5-state LTV configuration for --window-steps steps; rel2d: the relative 2-D system of "
                          "two 5-state estimators")
@@ -370,6 +371,67 @@ def run_windows5(args):
 
 
 
+def run_adjoint(args):
+    """Adjoint workload (the 4-state LTI sliding-window configuration: Phi
+    random with spectral radius 0.95, Gamma 4x1 and H 1x4 N(0,1), beta 0.1,
+    gamma 0.2, window 7, 100 steps): one gradient = the sliding-window
+    log-likelihood sum_k log fz_k and its gradient with respect to (beta,
+    gamma, p0, Phi, Gamma, H) with the window checkpoints held fixed
+    (cauchyfriendly_gb300.adjoint.windowed_log_likelihood: the manager run,
+    every window life recomputed from its checkpoint, the reverse pass).
+    value: gradients/s (wall clock of the public call); forward_s: the same
+    manager run alone; the ratio is the gradient's cost in forward runs."""
+    import torch
+    from cauchyfriendly_gb300 import windows, workloads as W
+    from cauchyfriendly_gb300.adjoint import windowed_log_likelihood
+    import oracle
+    torch.cuda.set_device(0)
+    steps = args.adjoint_steps
+    prob = W.four_state_lti(seed=args.seed, steps=steps)
+    Wn = 7
+    ms = (Wn - 1) * 1 + 4
+    cs = [oracle.draw_reference_constants(1000 + w, 4, ms) for w in range(Wn)]
+    rp = np.stack([c[0] for c in cs])
+    bp = np.stack([c[1] for c in cs])
+
+    def forward():
+        t0 = time.perf_counter()
+        mgr = windows.SlidingWindowManager(Wn, prob["A0"][None], prob["p0"][None], prob["b0"][None], 4, 1, 1,
+                                           root_point=rp[:, None, :], b_pert=bp[:, None, :])
+        for k in range(steps):
+            mgr.step(prob["msmts"][k][None], prob["Phi"][None], prob["Gamma"][None], prob["beta"][None],
+                     prob["H"][None], prob["gamma"][None])
+        terms = mgr.total_post_mu_terms()
+        mgr.close()
+        return time.perf_counter() - t0, terms
+
+    def gradient():
+        t0 = time.perf_counter()
+        r = windowed_log_likelihood(prob, Wn, rp, bp)
+        return time.perf_counter() - t0, r
+
+    for _ in range(max(1, args.warmup - 2)):
+        forward()
+        gradient()
+    fw, gw, terms, r = 0.0, 0.0, 0, None
+    for _ in range(args.steps):
+        t, terms = forward()
+        fw += t
+        t, r = gradient()
+        gw += t
+    fw /= args.steps
+    gw /= args.steps
+    line = {"metric": "MCE log-likelihood gradients/s (1 GB300, FP64; sliding window, checkpointed adjoint)",
+            "value": 1.0 / gw, "unit": "gradients/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * gw, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "4-state LTI sliding-window MCE, window 7, %d steps, 1 msmt/step" % steps,
+                       "params": 30, "window_lives": len(r["starts"]), "terms_per_forward": terms},
+            "forward_s": fw, "gradient_s": gw, "gradient_over_forward": gw / fw,
+            "loglik": r["loglik"], "grad_norm": float(np.sqrt(sum(float(np.sum(v ** 2)) for v in r["grad"].values())))}
+    print(json.dumps(line), flush=True)
+
+
 def run_rel2d(args):
     """Relative-then-transformed 2-D system (rel = secondary - primary through
     Trel = rows e0, e2) of two 5-state estimators with two measurements per
@@ -521,6 +583,9 @@ def main():
         return
     if args.workload == "rel2d":
         run_rel2d(args)
+        return
+    if args.workload == "adjoint":
+        run_adjoint(args)
         return
     import torch
     rank = int(os.environ.get("RANK", "0"))

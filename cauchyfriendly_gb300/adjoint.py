@@ -140,6 +140,71 @@ def _make_function():
     return MCELogLikelihood
 
 
+def windowed_log_likelihood(prob, W, root_point, b_pert, p0=None, beta=None, gamma=None, Phi=None, Gamma=None,
+                            H=None, starts=None, best=None, with_grad=True):
+    """Sliding-window log-likelihood sum_k log fz_k of a one-measurement LTI
+    problem, fz_k the normaliser of the window chosen at step k
+    (PySlidingWindowManager's best window, cauchy_estimator.py:1181-1216),
+    and its gradient with respect to (beta, gamma, p0, Phi, Gamma, H) with the
+    window-boundary checkpoints held fixed: every window life is recomputed
+    from its start statistics (the initial ones for the first life of window
+    0, Speyer's restart about the best window for the others) by an
+    AdjointRun, and gets the seeds +1/Re fz on each update at which it is the
+    chosen window and -1/Re fz on the update before it (log fz_u =
+    log Re U_u - log Re U_(u-1), U the unscaled normaliser).  p0 enters only
+    the first life.
+
+    prob: a problem dict (workloads); root_point (W, d) / b_pert (W, stride)
+    the windows' constants.  The parameters default to prob's.  starts/best
+    (from a first call, returned in the result) hold the checkpoints fixed for
+    finite differences.  Returns a dict: loglik, grad (dict), starts, best."""
+    from .windows import SlidingWindowManager
+    d, pncc, p = prob["d"], prob["pncc"], prob["p"]
+    if p != 1:
+        raise ValueError("windowed_log_likelihood supports one measurement per step")
+    P = {"beta": prob["beta"] if beta is None else beta, "gamma": prob["gamma"] if gamma is None else gamma,
+         "p0": prob["p0"] if p0 is None else p0, "Phi": prob["Phi"] if Phi is None else Phi,
+         "Gamma": prob["Gamma"] if Gamma is None else Gamma, "H": prob["H"] if H is None else H}
+    P = {k: np.asarray(v, dtype=np.float64) for k, v in P.items()}
+    steps = prob["msmts"].shape[0]
+    rp = np.asarray(root_point, dtype=np.float64)
+    bp = np.asarray(b_pert, dtype=np.float64)
+    if starts is None:
+        mgr = SlidingWindowManager(W, prob["A0"][None], P["p0"][None], prob["b0"][None], d, pncc, p,
+                                   root_point=rp[:, None, :], b_pert=bp[:, None, :])
+        best = []
+        for k in range(steps):
+            out = mgr.step(prob["msmts"][k][None], P["Phi"][None], P["Gamma"].reshape(1, d, pncc),
+                           P["beta"][None], P["H"].reshape(1, p, d), P["gamma"][None])
+            best.append(out[0][2])
+        starts = [{"slot": s["slot"], "step": s["step"], "A0": np.asarray(s["A0"])[0], "p0": np.asarray(s["p0"])[0],
+                   "b0": np.asarray(s["b0"])[0]} for s in mgr.starts]
+        mgr.close()
+    L = 0.0
+    grad = {k: np.zeros_like(v) for k, v in P.items()}
+    for li, st in enumerate(starts):
+        s0 = st["step"]
+        n = min(W, steps - s0)
+        p0_life = P["p0"] if li == 0 else st["p0"]
+        run = AdjointRun(d, pncc, p, n, st["A0"], p0_life, st["b0"], rp[st["slot"]], bp[st["slot"]])
+        fz = run.forward(prob["msmts"][s0:s0 + n].reshape(-1), P["Phi"], P["Gamma"], P["beta"], P["H"], P["gamma"])
+        w = np.zeros(n)
+        for u in range(n):
+            if best[s0 + u] == st["slot"]:
+                L += float(np.log(fz[u]))
+                w[u] += 1.0 / fz[u]
+                if u >= 1:
+                    w[u - 1] -= 1.0 / fz[u - 1]
+        if with_grad and np.any(w != 0):
+            g = run.backward(w)
+            for k in grad:
+                if k == "p0" and li > 0:
+                    continue
+                grad[k] += g[k].reshape(grad[k].shape)
+        run.close()
+    return {"loglik": L, "grad": grad, "starts": starts, "best": best}
+
+
 _FN = None
 
 

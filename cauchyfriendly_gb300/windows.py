@@ -145,6 +145,9 @@ class SlidingWindowManager:
         self.post_mu_terms = 0
         self.history = []
         self.last = None
+        # window-boundary checkpoints: every window life's start (slot, step,
+        # and each manager's A0, p0, b0), the restarts being Speyer's statistics
+        self.starts = [{"slot": 0, "step": 0, "A0": A0.copy(), "p0": p0.copy(), "b0": b0.copy()}]
 
     def _step_slot(self, w, msmts, Phi, Gamma, beta, H, gamma):
         errs = None
@@ -218,10 +221,14 @@ class SlidingWindowManager:
             # last measurement of this step (reset_about_estimator, msmt_idx = p-1)
             j = self.p - 1
             slot = self.slots[min_idx]
+            st = {"slot": min_idx, "step": self.step_idx, "A0": np.zeros((self.n_mgr, self.d, self.d)),
+                  "p0": np.zeros((self.n_mgr, self.d)), "b0": np.zeros((self.n_mgr, self.d))}
             for m in range(self.n_mgr):
                 xh, Ph = out[m][0], out[m][1]
                 A0, p0, b0 = speyers_window_init(xh, Ph, H[m, j], gamma[m, j], msmts[m, j])
                 slot.reinit(m, A0, p0, b0)
+                st["A0"][m], st["p0"][m], st["b0"][m] = A0, p0, b0
+            self.starts.append(st)
             self.post_mu_terms += slot.post_mu_terms()  # a reset clears the slot's count
             slot.reset()  # pycauchy_single_step_reset: new start statistics, then reset
             slot.step(msmts[:, j], Phi, Gamma, beta, H[:, j, :], gamma[:, j])

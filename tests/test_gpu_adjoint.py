@@ -127,3 +127,37 @@ def test_torch_function_gives_the_adjoint_gradient():
         assert np.allclose(gt.numpy(), want[n], rtol=1e-12, atol=1e-14), n
     run.close()
     run2.close()
+
+
+def test_windowed_gradient_with_fixed_checkpoints():
+    """The sliding-window log-likelihood (4-state LTI, window 4, 10 steps;
+    each step's fz from the chosen window) and its gradient with the
+    window-boundary checkpoints held fixed: against central differences of the
+    same objective recomputed from the same checkpoints, on a subset of the
+    parameters (beta, gamma, a p0 entry, Phi, Gamma and H entries)."""
+    _need_gpu()
+    import oracle
+    from cauchyfriendly_gb300 import workloads as W
+    from cauchyfriendly_gb300.adjoint import windowed_log_likelihood
+    prob = W.four_state_lti(seed=4, steps=10)
+    Wn = 4
+    ms = oracle.max_shape_of({"steps": Wn, "d": 4, "pncc": 1})
+    cs = [oracle.draw_reference_constants(60 + w, 4, ms) for w in range(Wn)]
+    rp = np.stack([c[0] for c in cs])
+    bp = np.stack([c[1] for c in cs])
+    res = windowed_log_likelihood(prob, Wn, rp, bp)
+    assert len(res["starts"]) == 10 and np.isfinite(res["loglik"])
+    picks = [("beta", (0,)), ("gamma", (0,)), ("p0", (1,)), ("Phi", (2, 1)), ("Gamma", (3, 0)), ("H", (0, 2))]
+    for name, idx in picks:
+        base = np.asarray(prob[name], dtype=np.float64)
+        h = 1e-6 * max(abs(base[idx]), 1e-3)
+        vals = []
+        for sgn in (1, -1):
+            a = base.copy()
+            a[idx] += sgn * h
+            r = windowed_log_likelihood(prob, Wn, rp, bp, starts=res["starts"], best=res["best"], with_grad=False,
+                                        **{name: a})
+            vals.append(r["loglik"])
+        fd = (vals[0] - vals[1]) / (2 * h)
+        g = res["grad"][name][idx]
+        assert abs(g - fd) <= 1e-4 * abs(fd) + 1e-7, (name, idx, g, fd)
