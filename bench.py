@@ -428,6 +428,9 @@ def run_adjoint(args):
             "config": {"workload": "4-state LTI sliding-window MCE, window 7, %d steps, 1 msmt/step" % steps,
                        "params": 30, "window_lives": len(r["starts"]), "terms_per_forward": terms},
             "forward_s": fw, "gradient_s": gw, "gradient_over_forward": gw / fw,
+            "gradient_ms_split": {k: round(float(v) / 1.0, 1) for k, v in
+                                  zip(("step_path", "forward_tape", "table_reverse", "record_chain"),
+                                      r["timing_ms"])},
             "loglik": r["loglik"], "grad_norm": float(np.sqrt(sum(float(np.sum(v ** 2)) for v in r["grad"].values())))}
     print(json.dumps(line), flush=True)
 

@@ -88,6 +88,7 @@ SIGNATURES = {
     "mce_adjoint_num_params": (ctypes.c_int, [_vp]),
     "mce_adjoint_backward": (ctypes.c_int, [_vp, _dp, _dp]),
     "mce_adjoint_check": (ctypes.c_int, [_vp, _dp, _dp]),
+    "mce_adjoint_timing": (ctypes.c_int, [_vp, _dp]),
     "mce_adjoint_destroy": (None, [_vp]),
 }
 

@@ -98,6 +98,12 @@ class AdjointRun:
         _lib.check(self._L.mce_adjoint_check(self._h, ctypes.byref(a), ctypes.byref(b)), "mce_adjoint_check")
         return a.value, b.value
 
+    def timing(self):
+        """Wall ms so far: step path, forward tape, table reverse, record chain."""
+        t = np.zeros(4)
+        _lib.check(self._L.mce_adjoint_timing(self._h, _lib.dp(t)), "mce_adjoint_timing")
+        return t
+
     def close(self):
         if getattr(self, "_h", None):
             self._L.mce_adjoint_destroy(self._h)
@@ -182,6 +188,7 @@ def windowed_log_likelihood(prob, W, root_point, b_pert, p0=None, beta=None, gam
         mgr.close()
     L = 0.0
     grad = {k: np.zeros_like(v) for k, v in P.items()}
+    timing = np.zeros(4)
     for li, st in enumerate(starts):
         s0 = st["step"]
         n = min(W, steps - s0)
@@ -201,8 +208,9 @@ def windowed_log_likelihood(prob, W, root_point, b_pert, p0=None, beta=None, gam
                 if k == "p0" and li > 0:
                     continue
                 grad[k] += g[k].reshape(grad[k].shape)
+        timing += run.timing()
         run.close()
-    return {"loglik": L, "grad": grad, "starts": starts, "best": best}
+    return {"loglik": L, "grad": grad, "starts": starts, "best": best, "timing_ms": timing}
 
 
 _FN = None

@@ -38,10 +38,12 @@
 #include "../../include/mce_c_api.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace mce {
@@ -497,6 +499,10 @@ struct mce_adjoint {
     std::vector<Update> ups;
     double max_table_err = 0;
     double fz_check_err = 0;
+    int threads = 0;  // host threads of the record chain (0: all cores)
+    // wall ms: forward step path, forward tape (host records + GPU checks),
+    // reverse over the tables (GPU), record chain (host)
+    double ms[4] = {0, 0, 0, 0};
 
     ~mce_adjoint()
     {
@@ -1072,8 +1078,16 @@ int mce_adjoint_forward(mce_adjoint* o, const double* msmts, const double* Phi, 
         U.sub = u % o->p;
         U.with_tp = !U.first && (u % o->p) == 0;
         // the GPU step
+        auto t0 = std::chrono::steady_clock::now();
         st = mce_step(o->h, msmts[u], Phi, Gamma, beta, H + (size_t)U.sub * d, gamma[U.sub], nullptr, nullptr);
         if (st < 0) return st;
+        auto t1 = std::chrono::steady_clock::now();
+        o->ms[0] += std::chrono::duration<double, std::milli>(t1 - t0).count();
+        struct Lap {
+            double* acc;
+            std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+            ~Lap() { *acc += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count(); }
+        } lap{&o->ms[1]};
         double rfz[2], rm[16], rc[128], gs;
         st = mce_get_raw_moments(o->h, 0, rfz, rm, rc, &gs);
         if (st < 0) return st;
@@ -1244,6 +1258,13 @@ int mce_adjoint_check(mce_adjoint* o, double* max_table_rel_err, double* max_fz_
     return MCE_OK;
 }
 
+int mce_adjoint_timing(mce_adjoint* o, double* ms4)
+{
+    if (!o || !ms4) return MCE_ERR_ARG;
+    for (int i = 0; i < 4; i++) ms4[i] = o->ms[i];
+    return MCE_OK;
+}
+
 int mce_adjoint_num_params(mce_adjoint* o)
 {
     if (!o) return MCE_ERR_ARG;
@@ -1255,6 +1276,7 @@ int mce_adjoint_backward(mce_adjoint* o, const double* w, double* grad)
     if (!o || !w || !grad || o->ups.empty()) return MCE_ERR_ARG;
     const int nup = (int)o->ups.size();
     int st;
+    auto tb0 = std::chrono::steady_clock::now();
     // ---- reverse over the tables and the fz seeds (GPU)
     Buf<int> pk, kk, dcontrib;
     Buf<cd> pv, kbar, pbar;
@@ -1337,8 +1359,11 @@ int mce_adjoint_backward(mce_adjoint* o, const double* w, double* grad)
     if (cudaGetLastError() != cudaSuccess) return MCE_ERR_CUDA;
     // ---- the record chain: tangents of the scalars that enter the g values,
     // one parameter direction at a time, dotted with their adjoints
+    auto tb1 = std::chrono::steady_clock::now();
+    o->ms[2] += std::chrono::duration<double, std::milli>(tb1 - tb0).count();
     const int N = mce_adjoint_num_params(o);
-    for (int dir = 0; dir < N; dir++) {
+    // directions are independent: spread them over the host's cores
+    auto one_direction = [o, nup](int dir) {
         Params<D1> P = make_params<D1>(*o, dir);
         seed(P, dir);
         std::vector<Rec<D1>> parents(1), pre, post;
@@ -1372,8 +1397,17 @@ int mce_adjoint_backward(mce_adjoint* o, const double* w, double* grad)
             for (size_t k = 0; k < U.kept_term.size(); k++) next[k] = post[U.kept_term[k]];
             parents.swap(next);
         }
-        grad[dir] = g;
-    }
+        return g;
+    };
+    const int hw = std::max(1u, std::thread::hardware_concurrency());
+    const int T = std::max(1, std::min(N, o->threads > 0 ? o->threads : hw));
+    std::vector<std::thread> pool;
+    for (int tid = 0; tid < T; tid++)
+        pool.emplace_back([&, tid]() {
+            for (int dir = tid; dir < N; dir += T) grad[dir] = one_direction(dir);
+        });
+    for (auto& th : pool) th.join();
+    o->ms[3] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb1).count();
     return MCE_OK;
 }
 

@@ -1783,6 +1783,19 @@ public:
         MCE_CUDA(cudaMemcpy(hA.data(), P.A.ptr + a * MC * D, sizeof(double) * n * MC * D, cudaMemcpyDeviceToHost));
         MCE_CUDA(cudaMemcpy(hp.data(), P.p.ptr + a * MC, sizeof(double) * n * MC, cudaMemcpyDeviceToHost));
         MCE_CUDA(cudaMemcpy(hb.data(), P.b.ptr + a * D, sizeof(double) * n * D, cudaMemcpyDeviceToHost));
+        // the estimator's tables in one copy: the span its slices cover
+        long long lo = -1, hi = -1;
+        for (long long t = 0; t < n; t++)
+            if (tc[t] > 0) {
+                lo = lo < 0 ? to[t] : std::min(lo, to[t]);
+                hi = std::max(hi, to[t] + tc[t]);
+            }
+        std::vector<int> span_k(lo < 0 ? 0 : hi - lo);
+        std::vector<cd> span_v(lo < 0 ? 0 : hi - lo);
+        if (lo >= 0) {
+            MCE_CUDA(cudaMemcpy(span_k.data(), Tb[cur].keys.ptr + lo, sizeof(int) * (hi - lo), cudaMemcpyDeviceToHost));
+            MCE_CUDA(cudaMemcpy(span_v.data(), Tb[cur].vals.ptr + lo, sizeof(cd) * (hi - lo), cudaMemcpyDeviceToHost));
+        }
         long long c = 0;
         for (long long t = 0; t < n; t++) {
             shape[t] = m[t];
@@ -1792,16 +1805,10 @@ public:
             for (int k = 0; k < m[t] && k < max_shape; k++) p_[t * max_shape + k] = hp[t * MC + k];
             for (int k = 0; k < D; k++) b[t * D + k] = hb[t * D + k];
             cells[t] = tc[t];
-            std::vector<int> kk(tc[t]);
-            std::vector<cd> vv(tc[t]);
-            if (tc[t] > 0) {
-                MCE_CUDA(cudaMemcpy(kk.data(), Tb[cur].keys.ptr + to[t], sizeof(int) * tc[t], cudaMemcpyDeviceToHost));
-                MCE_CUDA(cudaMemcpy(vv.data(), Tb[cur].vals.ptr + to[t], sizeof(cd) * tc[t], cudaMemcpyDeviceToHost));
-            }
             for (int k = 0; k < tc[t]; k++) {
-                keys[c] = kk[k];
-                g[2 * c] = vv[k].re;
-                g[2 * c + 1] = vv[k].im;
+                keys[c] = span_k[to[t] - lo + k];
+                g[2 * c] = span_v[to[t] - lo + k].re;
+                g[2 * c + 1] = span_v[to[t] - lo + k].im;
                 c++;
             }
         }

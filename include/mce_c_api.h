@@ -326,6 +326,10 @@ int mce_adjoint_forward(mce_adjoint* a, const double* msmts, const double* Phi, 
 int mce_adjoint_num_params(mce_adjoint* a);
 int mce_adjoint_backward(mce_adjoint* a, const double* w, double* grad);
 int mce_adjoint_check(mce_adjoint* a, double* max_table_rel_err, double* max_fz_rel_err);
+/* Wall ms spent since creation: [0] the forward step path, [1] the forward
+ * tape (host records, GPU member values and checks), [2] the reverse over the
+ * tables (GPU), [3] the record chain (host). */
+int mce_adjoint_timing(mce_adjoint* a, double* ms4);
 void mce_adjoint_destroy(mce_adjoint* a);
 
 /* Host wall time (ms) of the steps since the last mce_clear_profile: which = 0
