@@ -31,9 +31,9 @@
 //    of the parent-table cells (atomic adds), and of every term's scalars
 //    that enter the g values: the row scales (q, or p before coalignment
 //    for the fz terms), d_val and c_val;
-//  * the record chain: the host runs the record derivation again in
-//    forward-mode dual numbers, one parameter direction at a time, and dots
-//    the tangents of those scalars with their adjoints.
+//  * the record chain, on the GPU: one thread per (parent, parameter
+//    direction) repeats the parent's derivation in forward-mode dual numbers
+//    and dots the tangents of those scalars with their adjoints.
 #include "mce_device.cuh"
 #include "../../include/mce_c_api.h"
 
@@ -43,7 +43,6 @@
 #include <cstring>
 #include <memory>
 #include <string>
-#include <thread>
 #include <vector>
 
 namespace mce {
@@ -55,32 +54,10 @@ using mce::cd;
 namespace {
 
 // ---------------------------------------------------------------------------
-// Scalars: plain doubles, or a value with one tangent (forward mode).  Every
-// branch of the record derivation reads only values, so both kinds take the
-// same branches and the values are the same doubles.
-struct D1 {
-    double v = 0, t = 0;
-    D1() {}
-    D1(double x) : v(x), t(0) {}
-    D1(double x, double dx) : v(x), t(dx) {}
-};
-inline D1 operator+(D1 a, D1 b) { return D1(a.v + b.v, a.t + b.t); }
-inline D1 operator-(D1 a, D1 b) { return D1(a.v - b.v, a.t - b.t); }
-inline D1 operator-(D1 a) { return D1(-a.v, -a.t); }
-inline D1 operator*(D1 a, D1 b) { return D1(a.v * b.v, a.t * b.v + a.v * b.t); }
-inline D1 operator/(D1 a, D1 b)
-{
-    const double q = a.v / b.v;
-    return D1(q, (a.t - q * b.t) / b.v);
-}
-inline D1& operator+=(D1& a, D1 b) { return a = a + b; }
-inline D1& operator-=(D1& a, D1 b) { return a = a - b; }
-inline D1& operator*=(D1& a, D1 b) { return a = a * b; }
-inline D1& operator/=(D1& a, D1 b) { return a = a / b; }
+// Host scalars of the record derivation (doubles; the GPU record chain below
+// repeats the derivation on dual numbers).
 inline double val(double x) { return x; }
-inline double val(const D1& x) { return x.v; }
 inline double absd(double x) { return std::fabs(x); }
-inline D1 absd(const D1& x) { return x.v < 0 ? -x : (x.v > 0 ? x : D1(0.0, std::fabs(x.t) * 0)); }
 
 constexpr double kCoalignEps = 1e-8;
 constexpr double kMuEps = 1e-10;
@@ -423,6 +400,305 @@ __global__ void k_adj_eval_fz(const EvalDev* ev, int nt, const int* pkeys, const
 }
 
 // ---------------------------------------------------------------------------
+// The record chain on the GPU: one thread per (parent, parameter direction)
+// re-derives the parent's post-MU terms in forward-mode dual numbers (the
+// host derivation's arithmetic, so the same values and branches), dots the
+// tangents of the scalars that enter the g values with their adjoints, and
+// passes the tangents of the kept terms' records to the next update.
+
+struct DD {
+    double v, t;
+};
+__device__ inline DD dd(double v) { return DD{v, 0.0}; }
+__device__ inline DD dadd(DD a, DD b) { return DD{a.v + b.v, a.t + b.t}; }
+__device__ inline DD dsub(DD a, DD b) { return DD{a.v - b.v, a.t - b.t}; }
+__device__ inline DD dneg(DD a) { return DD{-a.v, -a.t}; }
+__device__ inline DD dmul(DD a, DD b) { return DD{a.v * b.v, a.t * b.v + a.v * b.t}; }
+__device__ inline DD ddiv(DD a, DD b)
+{
+    const double q = a.v / b.v;
+    return DD{q, (a.t - q * b.t) / b.v};
+}
+__device__ inline DD dabs(DD x) { return x.v < 0 ? dneg(x) : (x.v > 0 ? x : DD{0.0, 0.0}); }
+
+constexpr int kRows = 16, kDim = 8;  // the step path's limits (16 hyperplanes, 8 states)
+
+struct ChainArgs {
+    int d, pncc, p, MS, N, first, last, with_tp, sub, nP;
+    double z;
+    const double *beta, *gamma, *p0, *Phi, *Gamma, *H, *A0, *b0;
+    // parents: kept records of the previous update (values), padded to MS rows
+    const double *PA, *Pp, *Pb;
+    const int* Pm;
+    // tangents: [dir][slot][MS*d + MS + d]
+    const double* Tin;
+    double* Tout;
+    int rec;  // MS*d + MS + d
+    int n_next;
+    const int* kid_off;  // per parent: term index of its first child
+    const unsigned *sneg, *hpre;
+    const double *ybar_e, *dbar_e, *cbar_e;
+    const double *qbar_t, *dbar_t, *cbar_t;  // member adjoints per term
+    const int* kept_of;
+    double* grad;
+};
+
+__device__ inline int dgate(const DD* r, const DD* c, int d)
+{
+    bool pos = true, ng = true;
+    for (int l = 0; l < d; l++) {
+        if (pos) pos &= fabs(r[l].v - c[l].v) < kCoalignEps;
+        if (ng) ng &= fabs(r[l].v + c[l].v) < kCoalignEps;
+        if (!(pos || ng)) break;
+    }
+    return pos ? 1 : (ng ? -1 : 0);
+}
+
+__global__ void __launch_bounds__(128) k_adj_chain(ChainArgs a)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)a.nP * a.N) return;
+    const int pi = (int)(idx % a.nP), dir = (int)(idx / a.nP);
+    const int d = a.d;
+    const int offb = 0, offg = offb + a.pncc, offp = offg + a.p, offPhi = offp + d, offG = offPhi + d * d,
+              offH = offG + d * a.pncc;
+    auto par = [&](const double* v, int i, int off) { return DD{v[i], dir == off + i ? 1.0 : 0.0}; };
+    // the parent's record
+    DD A[kRows * kDim], P[kRows], B[kDim];
+    int m;
+    if (a.first) {
+        m = d;
+        for (int i = 0; i < d * d; i++) A[i] = dd(a.A0[i]);
+        for (int i = 0; i < d; i++) P[i] = par(a.p0, i, offp);
+        for (int i = 0; i < d; i++) B[i] = dd(a.b0[i]);
+    } else {
+        m = a.Pm[pi];
+        const double* tin = a.Tin + ((size_t)dir * a.nP + pi) * a.rec;
+        for (int i = 0; i < m * d; i++) A[i] = DD{a.PA[(size_t)pi * a.MS * d + i], tin[i]};
+        for (int i = 0; i < m; i++) P[i] = DD{a.Pp[(size_t)pi * a.MS + i], tin[a.MS * d + i]};
+        for (int i = 0; i < d; i++) B[i] = DD{a.Pb[(size_t)pi * d + i], tin[a.MS * d + a.MS + i]};
+    }
+    if (a.with_tp) {
+        // Gamma pre-coalignment
+        DD Gt[kDim * kDim], bt[kDim];
+        const int pncc = a.pncc;
+        for (int i = 0; i < pncc; i++) {
+            for (int j = 0; j < d; j++) Gt[i * d + j] = par(a.Gamma, j * pncc + i, offG);
+            bt[i] = par(a.beta, i, offb);
+        }
+        for (int i = 0; i < pncc; i++) {
+            DD nf = dd(0.0);
+            for (int j = 0; j < d; j++) nf = dadd(nf, dabs(Gt[i * d + j]));
+            for (int j = 0; j < d; j++) Gt[i * d + j] = ddiv(Gt[i * d + j], nf);
+            bt[i] = dmul(bt[i], nf);
+        }
+        bool F[kDim];
+        for (int i = 0; i < pncc; i++) F[i] = true;
+        for (int i = 0; i < pncc - 1; i++)
+            if (F[i])
+                for (int j = i + 1; j < pncc; j++)
+                    if (F[j] && dgate(&Gt[i * d], &Gt[j * d], d) != 0) {
+                        F[j] = false;
+                        bt[i] = dadd(bt[i], bt[j]);
+                    }
+        int cnt = 0;
+        for (int i = 0; i < pncc; i++) cnt += F[i];
+        if (cnt != pncc) {
+            int u = 1;
+            for (int j = 1; j < pncc; j++)
+                if (F[j]) {
+                    if (u < j) {
+                        for (int l = 0; l < d; l++) Gt[u * d + l] = Gt[j * d + l];
+                        bt[u] = bt[j];
+                    }
+                    u++;
+                }
+        }
+        // time_prop
+        DD w[kRows * kDim];
+        for (int i = 0; i < m * d; i++) w[i] = A[i];
+        for (int i = 0; i < m; i++)
+            for (int j = 0; j < d; j++) {
+                DD sum = dd(0.0);
+                for (int k = 0; k < d; k++) sum = dadd(sum, dmul(w[i * d + k], par(a.Phi, k + j * d, offPhi)));
+                A[i * d + j] = sum;
+            }
+        DD wb[kDim];
+        for (int i = 0; i < d; i++) wb[i] = B[i];
+        for (int i = 0; i < d; i++) {
+            DD sum = dd(0.0);
+            for (int j = 0; j < d; j++) sum = dadd(sum, dmul(par(a.Phi, i * d + j, offPhi), wb[j]));
+            B[i] = sum;
+        }
+        // tp_coalign
+        for (int i = 0; i < m; i++) {
+            DD n1 = dd(0.0);
+            for (int j = 0; j < d; j++) n1 = dadd(n1, dabs(A[i * d + j]));
+            P[i] = dmul(P[i], n1);
+            for (int j = 0; j < d; j++) A[i * d + j] = ddiv(A[i * d + j], n1);
+        }
+        bool Fg[kDim];
+        for (int j = 0; j < cnt; j++) Fg[j] = true;
+        for (int j = 0; j < cnt; j++)
+            for (int k = 0; k < m; k++)
+                if (Fg[j] && dgate(&Gt[j * d], &A[k * d], d) != 0) {
+                    Fg[j] = false;
+                    P[k] = dadd(P[k], bt[j]);
+                }
+        for (int j = 0; j < cnt; j++)
+            if (Fg[j]) {
+                for (int l = 0; l < d; l++) A[m * d + l] = Gt[j * d + l];
+                P[m] = bt[j];
+                m++;
+            }
+    }
+    // measurement update
+    const DD* H = nullptr;
+    (void)H;
+    DD Hr[kDim];
+    for (int j = 0; j < d; j++) Hr[j] = par(a.H, a.sub * d + j, offH);
+    const DD gam = par(a.gamma, a.sub, offg);
+    DD mu[(kRows + 1) * kDim], rho[kRows + 1];
+    bool Fi[kRows + 1];
+    for (int i = 0; i < m * d; i++) mu[i] = A[i];
+    for (int i = 0; i < m; i++) rho[i] = P[i];
+    rho[m] = gam;
+    for (int j = 0; j < d; j++) mu[m * d + j] = dd(0.0);
+    Fi[m] = true;
+    for (int l = 0; l < m; l++) {
+        DD h = dd(0.0);
+        for (int j = 0; j < d; j++) h = dadd(h, dmul(Hr[j], mu[l * d + j]));
+        if (fabs(h.v) < kMuEps) {
+            rho[l] = P[l];
+            Fi[l] = false;
+        } else {
+            const DD r = ddiv(dd(1.0), h);
+            for (int j = 0; j < d; j++) mu[l * d + j] = dmul(mu[l * d + j], r);
+            rho[l] = dmul(P[l], dabs(h));
+            Fi[l] = true;
+        }
+    }
+    DD hb = dd(0.0);
+    for (int j = 0; j < d; j++) hb = dadd(hb, dmul(Hr[j], B[j]));
+    const DD zeta = dsub(dd(a.z), hb);
+    double g = 0.0;
+    int kid = 0;
+    for (int tt = 0; tt <= m; tt++) {
+        if (!Fi[tt]) continue;
+        const int term = tt == m ? pi : a.kid_off[pi] + kid++;
+        DD cA[kRows * kDim], cp[kRows], cq[kRows], cb[kDim];
+        const DD cc = zeta, cd_ = rho[tt];
+        for (int j = 0; j < d; j++) cb[j] = dadd(B[j], dmul(zeta, mu[tt * d + j]));
+        int l = 0;
+        unsigned hof = 0;
+        for (int ll = 0; ll <= m; ll++) {
+            if (ll == tt) continue;
+            cp[l] = rho[ll];
+            if (Fi[ll])
+                for (int j = 0; j < d; j++) cA[l * d + j] = dsub(mu[ll * d + j], mu[tt * d + j]);
+            else {
+                for (int j = 0; j < d; j++) cA[l * d + j] = mu[ll * d + j];
+                hof |= 1u << l;
+            }
+            l++;
+        }
+        // the fz seed's scalars (before coalignment)
+        {
+            const unsigned sn = a.sneg[term], hp = a.hpre[term];
+            double yt = 0;
+            for (int r = 0; r < m; r++)
+                if (!((hp >> r) & 1)) yt += cp[r].t * (((sn >> r) & 1) ? -1.0 : 1.0);
+            g += a.ybar_e[term] * yt + a.dbar_e[term] * cd_.t + a.cbar_e[term] * cc.t;
+        }
+        // coalignment (the parent only normalises; nothing at the first and last update)
+        int mm = m;
+        unsigned horth = hof;
+        for (int r = 0; r < m; r++) cq[r] = cp[r];
+        if (!a.first && !a.last) {
+            for (int i = 0; i < m; i++) {
+                DD n1 = dd(0.0);
+                for (int j = 0; j < d; j++) n1 = dadd(n1, dabs(cA[i * d + j]));
+                cp[i] = dmul(cp[i], n1);
+                for (int j = 0; j < d; j++) cA[i * d + j] = ddiv(cA[i * d + j], n1);
+            }
+            if (tt != m) {
+                bool F[kRows], hflag[kRows];
+                for (int j = 0; j < m; j++) {
+                    F[j] = true;
+                    hflag[j] = horth ? ((horth >> j) & 1) : false;
+                }
+                for (int j = 0; j < m - 1; j++) {
+                    if (!F[j]) continue;
+                    for (int k = j + 1; k < m; k++) {
+                        if (!F[k]) continue;
+                        const int gt = dgate(&cA[j * d], &cA[k * d], d);
+                        if (gt == 1) {
+                            if (horth) {
+                                const bool hj = hflag[j], hk = hflag[k];
+                                if (!hj && !hk) cq[j] = dadd(cq[j], cq[k]);
+                                else if (hj && !hk) {
+                                    cq[j] = cq[k];
+                                    hflag[j] = false;
+                                } else if (!hj && hk) hflag[k] = false;
+                                else {
+                                    hflag[k] = false;
+                                    cq[j] = dadd(cq[j], cq[k]);
+                                }
+                            } else
+                                cq[j] = dadd(cq[j], cq[k]);
+                            F[k] = false;
+                            cp[j] = dadd(cp[j], cp[k]);
+                        } else if (gt == -1) {
+                            if (horth) {
+                                const bool hj = hflag[j], hk = hflag[k];
+                                if (!hj && !hk) cq[j] = dsub(cq[j], cq[k]);
+                                else if (hj && !hk) {
+                                    cq[j] = dneg(cq[k]);
+                                    hflag[j] = false;
+                                } else if (!hj && hk) hflag[k] = false;
+                            } else
+                                cq[j] = dsub(cq[j], cq[k]);
+                            F[k] = false;
+                            cp[j] = dadd(cp[j], cp[k]);
+                        }
+                    }
+                }
+                int ns = 0;
+                for (int i = 0; i < m; i++) ns += F[i];
+                if (ns != m) {
+                    int u = 1;
+                    for (int j = 1; j < m; j++)
+                        if (F[j]) {
+                            if (u < j) {
+                                for (int l2 = 0; l2 < d; l2++) cA[u * d + l2] = cA[j * d + l2];
+                                cp[u] = cp[j];
+                                cq[u] = cq[j];
+                            }
+                            u++;
+                        }
+                    mm = ns;
+                }
+            }
+        }
+        // the g-table's scalars (after coalignment)
+        {
+            const double* qb = a.qbar_t + (size_t)term * 32;
+            for (int k = 0; k < mm; k++) g += qb[k] * cq[k].t;
+            g += a.dbar_t[term] * cd_.t + a.cbar_t[term] * cc.t;
+        }
+        // a kept term hands its record's tangents to the next update
+        const int slot = a.kept_of ? a.kept_of[term] : -1;
+        if (slot >= 0) {
+            double* tout = a.Tout + ((size_t)dir * a.n_next + slot) * a.rec;
+            for (int i = 0; i < mm * d; i++) tout[i] = cA[i].t;
+            for (int i = 0; i < mm; i++) tout[a.MS * d + i] = cp[i].t;
+            for (int i = 0; i < d; i++) tout[a.MS * d + a.MS + i] = cb[i].t;
+        }
+    }
+    atomicAdd(&a.grad[dir], g);
+}
+
+// ---------------------------------------------------------------------------
 // Device buffers (grow-only, owned by the object)
 
 template <class T>
@@ -499,7 +775,6 @@ struct mce_adjoint {
     std::vector<Update> ups;
     double max_table_err = 0;
     double fz_check_err = 0;
-    int threads = 0;  // host threads of the record chain (0: all cores)
     // wall ms: forward step path, forward tape (host records + GPU checks),
     // reverse over the tables (GPU), record chain (host)
     double ms[4] = {0, 0, 0, 0};
@@ -599,18 +874,6 @@ Params<S> make_params(const mce_adjoint& o, int dir)
     take(P.Gamma, o.Gamma);
     take(P.H, o.H);
     return P;
-}
-
-inline void seed(Params<D1>& P, int dir)
-{
-    std::vector<D1>* vs[6] = {&P.beta, &P.gamma, &P.p0, &P.Phi, &P.Gamma, &P.H};
-    for (auto* v : vs) {
-        if (dir < (int)v->size()) {
-            (*v)[dir].t = 1.0;
-            return;
-        }
-        dir -= (int)v->size();
-    }
 }
 
 // One update's record derivation (the host half of step_first / step_rest,
@@ -1361,52 +1624,114 @@ int mce_adjoint_backward(mce_adjoint* o, const double* w, double* grad)
     // one parameter direction at a time, dotted with their adjoints
     auto tb1 = std::chrono::steady_clock::now();
     o->ms[2] += std::chrono::duration<double, std::milli>(tb1 - tb0).count();
+    // ---- the record chain on the GPU: a thread per (parent, direction)
     const int N = mce_adjoint_num_params(o);
-    // directions are independent: spread them over the host's cores
-    auto one_direction = [o, nup](int dir) {
-        Params<D1> P = make_params<D1>(*o, dir);
-        seed(P, dir);
-        std::vector<Rec<D1>> parents(1), pre, post;
-        parents[0].m = o->d;
-        parents[0].A.assign(o->A0.begin(), o->A0.end());
-        parents[0].p.assign(P.p0.begin(), P.p0.end());
-        parents[0].b.assign(o->b0.begin(), o->b0.end());
-        double g = 0;
-        for (int u = 0; u < nup; u++) {
-            const Update& U = o->ups[u];
-            derive_update(*o, U, P, parents, pre, post, nullptr);
-            for (size_t t = 0; t < U.terms.size(); t++) {
-                const TermInfo& ti = U.terms[t];
-                if (U.ybar_e[t] != 0.0) {
-                    double yt = 0;
-                    for (int l = 0; l < ti.m_pre; l++)
-                        if (!((ti.horthog_pre >> l) & 1)) yt += pre[t].p[l].t * (((ti.sneg >> l) & 1) ? -1.0 : 1.0);
-                    g += U.ybar_e[t] * yt;
-                }
-                g += U.dbar_e[t] * pre[t].dv.t + U.cbar_e[t] * pre[t].c.t;
-            }
-            for (size_t j = 0; j < U.members.size(); j++) {
-                const Member& mb = U.members[j];
-                if (!mb.contrib) continue;
-                const Rec<D1>& r = post[mb.term];
-                for (int k = 0; k < r.m; k++) g += U.qbar[j * 32 + k] * r.q[k].t;
-                g += U.dbar_m[j] * r.dv.t + U.cbar_m[j] * r.c.t;
-            }
-            if (U.last) break;
-            std::vector<Rec<D1>> next(U.kept_term.size());
-            for (size_t k = 0; k < U.kept_term.size(); k++) next[k] = post[U.kept_term[k]];
-            parents.swap(next);
+    const int d = o->d, MS = o->MS, rec = MS * d + MS + d;
+    long long maxP = 1;
+    for (int u = 0; u + 1 < nup; u++) maxP = std::max<long long>(maxP, o->ups[u].kept.nt);
+    Buf<double> tin, tout, dgrad, dPA, dPp, dPb, dyb, ddb, dcb, dqt, ddt, dct;
+    Buf<double> dpar[8];
+    Buf<int> dPm, dkid, dkept;
+    Buf<unsigned> dsn, dhp;
+    if ((st = tin.ensure((size_t)N * maxP * rec))) return st;
+    if ((st = tout.ensure((size_t)N * maxP * rec))) return st;
+    if ((st = dgrad.ensure(N))) return st;
+    cudaMemset(dgrad.ptr, 0, sizeof(double) * N);
+    const std::vector<double>* pv_[8] = {&o->beta, &o->gamma, &o->p0, &o->Phi, &o->Gamma, &o->H, &o->A0, &o->b0};
+    for (int i = 0; i < 8; i++)
+        if ((st = dpar[i].upload(pv_[i]->data(), pv_[i]->size()))) return st;
+    for (int u = 0; u < nup; u++) {
+        const Update& U = o->ups[u];
+        const int nt = (int)U.terms.size();
+        const int nP = u == 0 ? 1 : o->ups[u - 1].kept.nt;
+        if (u > 0) {
+            const Tables& K = o->ups[u - 1].kept;
+            if ((st = dPm.upload(K.shape.data(), K.shape.size()))) return st;
+            if ((st = dPA.upload(K.A.data(), K.A.size()))) return st;
+            if ((st = dPp.upload(K.p.data(), K.p.size()))) return st;
+            if ((st = dPb.upload(K.b.data(), K.b.size()))) return st;
         }
-        return g;
-    };
-    const int hw = std::max(1u, std::thread::hardware_concurrency());
-    const int T = std::max(1, std::min(N, o->threads > 0 ? o->threads : hw));
-    std::vector<std::thread> pool;
-    for (int tid = 0; tid < T; tid++)
-        pool.emplace_back([&, tid]() {
-            for (int dir = tid; dir < N; dir += T) grad[dir] = one_direction(dir);
-        });
-    for (auto& th : pool) th.join();
+        std::vector<int> kid_off(nP, 0), nk(nP, 0);
+        for (int t = nP; t < nt; t++) nk[U.terms[t].parent < 0 ? 0 : U.terms[t].parent]++;
+        for (int i = 0, acc = nP; i < nP; i++) {
+            kid_off[i] = acc;
+            acc += nk[i];
+        }
+        std::vector<unsigned> sn(nt), hp(nt);
+        for (int t = 0; t < nt; t++) {
+            sn[t] = U.terms[t].sneg;
+            hp[t] = U.terms[t].horthog_pre;
+        }
+        std::vector<double> qt((size_t)nt * 32, 0.0), dt(nt, 0.0), ct(nt, 0.0);
+        for (size_t j = 0; j < U.members.size(); j++) {
+            const Member& mb = U.members[j];
+            if (!mb.contrib || U.qbar.empty()) continue;
+            for (int k = 0; k < 32; k++) qt[(size_t)mb.term * 32 + k] = U.qbar[j * 32 + k];
+            dt[mb.term] = U.dbar_m[j];
+            ct[mb.term] = U.cbar_m[j];
+        }
+        std::vector<int> kept_of(nt, -1);
+        const int n_next = U.last ? 0 : (int)U.kept_term.size();
+        for (int k = 0; k < n_next; k++) kept_of[U.kept_term[k]] = k;
+        if ((st = dkid.upload(kid_off.data(), nP))) return st;
+        if ((st = dsn.upload(sn.data(), nt))) return st;
+        if ((st = dhp.upload(hp.data(), nt))) return st;
+        if ((st = dyb.upload(U.ybar_e.data(), nt))) return st;
+        if ((st = ddb.upload(U.dbar_e.data(), nt))) return st;
+        if ((st = dcb.upload(U.cbar_e.data(), nt))) return st;
+        if ((st = dqt.upload(qt.data(), qt.size()))) return st;
+        if ((st = ddt.upload(dt.data(), nt))) return st;
+        if ((st = dct.upload(ct.data(), nt))) return st;
+        if ((st = dkept.upload(kept_of.data(), nt))) return st;
+        ChainArgs ca;
+        ca.d = d;
+        ca.pncc = o->pncc;
+        ca.p = o->p;
+        ca.MS = MS;
+        ca.N = N;
+        ca.first = U.first;
+        ca.last = U.last;
+        ca.with_tp = U.with_tp;
+        ca.sub = U.sub;
+        ca.nP = nP;
+        ca.z = o->msmts[u];
+        ca.beta = dpar[0].ptr;
+        ca.gamma = dpar[1].ptr;
+        ca.p0 = dpar[2].ptr;
+        ca.Phi = dpar[3].ptr;
+        ca.Gamma = dpar[4].ptr;
+        ca.H = dpar[5].ptr;
+        ca.A0 = dpar[6].ptr;
+        ca.b0 = dpar[7].ptr;
+        ca.PA = dPA.ptr;
+        ca.Pp = dPp.ptr;
+        ca.Pb = dPb.ptr;
+        ca.Pm = dPm.ptr;
+        ca.Tin = tin.ptr;
+        ca.Tout = tout.ptr;
+        ca.rec = rec;
+        ca.n_next = n_next;
+        ca.kid_off = dkid.ptr;
+        ca.sneg = dsn.ptr;
+        ca.hpre = dhp.ptr;
+        ca.ybar_e = dyb.ptr;
+        ca.dbar_e = ddb.ptr;
+        ca.cbar_e = dcb.ptr;
+        ca.qbar_t = dqt.ptr;
+        ca.dbar_t = ddt.ptr;
+        ca.cbar_t = dct.ptr;
+        ca.kept_of = dkept.ptr;
+        ca.grad = dgrad.ptr;
+        const long long nthr = (long long)nP * N;
+        k_adj_chain<<<(int)((nthr + 127) / 128), 128>>>(ca);
+        std::swap(tin.ptr, tout.ptr);
+        std::swap(tin.cap, tout.cap);
+    }
+    if (cudaMemcpy(grad, dgrad.ptr, sizeof(double) * N, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        mce::report_error("adjoint: the record chain failed on the GPU");
+        return MCE_ERR_CUDA;
+    }
     o->ms[3] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb1).count();
     return MCE_OK;
 }
