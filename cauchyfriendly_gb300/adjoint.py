@@ -186,30 +186,46 @@ def windowed_log_likelihood(prob, W, root_point, b_pert, p0=None, beta=None, gam
         starts = [{"slot": s["slot"], "step": s["step"], "A0": np.asarray(s["A0"])[0], "p0": np.asarray(s["p0"])[0],
                    "b0": np.asarray(s["b0"])[0]} for s in mgr.starts]
         mgr.close()
-    L = 0.0
-    grad = {k: np.zeros_like(v) for k, v in P.items()}
-    timing = np.zeros(4)
-    for li, st in enumerate(starts):
+    def life(li):
+        st = starts[li]
         s0 = st["step"]
         n = min(W, steps - s0)
         p0_life = P["p0"] if li == 0 else st["p0"]
         run = AdjointRun(d, pncc, p, n, st["A0"], p0_life, st["b0"], rp[st["slot"]], bp[st["slot"]])
-        fz = run.forward(prob["msmts"][s0:s0 + n].reshape(-1), P["Phi"], P["Gamma"], P["beta"], P["H"], P["gamma"])
-        w = np.zeros(n)
-        for u in range(n):
-            if best[s0 + u] == st["slot"]:
-                L += float(np.log(fz[u]))
-                w[u] += 1.0 / fz[u]
-                if u >= 1:
-                    w[u - 1] -= 1.0 / fz[u - 1]
-        if with_grad and np.any(w != 0):
-            g = run.backward(w)
+        try:
+            fz = run.forward(prob["msmts"][s0:s0 + n].reshape(-1), P["Phi"], P["Gamma"], P["beta"], P["H"],
+                             P["gamma"])
+            w = np.zeros(n)
+            Ll = 0.0
+            for u in range(n):
+                if best[s0 + u] == st["slot"]:
+                    Ll += float(np.log(fz[u]))
+                    w[u] += 1.0 / fz[u]
+                    if u >= 1:
+                        w[u - 1] -= 1.0 / fz[u - 1]
+            g = run.backward(w) if with_grad and np.any(w != 0) else None
+            return Ll, g, run.timing()
+        finally:
+            run.close()
+
+    # window lives are independent: their host work overlaps on the host's
+    # cores (the library's calls release the interpreter lock)
+    from concurrent.futures import ThreadPoolExecutor
+    import os
+    workers = max(1, min(len(starts), os.cpu_count() or 1, 16))
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        results = list(ex.map(life, range(len(starts))))
+    L = 0.0
+    grad = {k: np.zeros_like(v) for k, v in P.items()}
+    timing = np.zeros(4)
+    for li, (Ll, g, t) in enumerate(results):
+        L += Ll
+        timing += t
+        if g is not None:
             for k in grad:
                 if k == "p0" and li > 0:
                     continue
                 grad[k] += g[k].reshape(grad[k].shape)
-        timing += run.timing()
-        run.close()
     return {"loglik": L, "grad": grad, "starts": starts, "best": best, "timing_ms": timing}
 
 
