@@ -557,6 +557,7 @@ public:
     int ev_used = 0, p_id = 0, p_a = 0;
     long long p_l0 = 0;
     DevBuf<double> alg;  // [KID_COUNT][2] bytes, flops
+    DevBuf<unsigned> gbits;  // cell bitmaps of terms above kSmemBitmapRows hyperplanes
 
     // profiling brackets on the engine's stream (or on st when given)
     void pbeg(int id, cudaStream_t st = nullptr)
@@ -633,9 +634,11 @@ public:
             set_error("max shape exceeds 31 hyperplanes (cauchy_estimator.hpp:231-235)");
             return MCE_ERR_SHAPE;
         }
-        // the shared-memory bitmaps of the cell enumeration hold 2^MC bits per warp
-        if (MC > 16) {
-            set_error("this build supports up to 16 hyperplanes per term");
+        // cell bitmaps hold 2^MC bits per warp: in shared memory up to 16
+        // hyperplanes, in a global buffer above (its size, warps x 3 x 2^MC bits,
+        // bounds the build at 24)
+        if (MC > kMaxBitmapRows) {
+            set_error("this build supports up to " + std::to_string(kMaxBitmapRows) + " hyperplanes per term");
             return MCE_ERR_SHAPE;
         }
         if (bp && bp_stride < MC) {
@@ -664,6 +667,13 @@ public:
         int s = MCE_OK;
         // profiling counters, sized here so no later step has to allocate them
         s |= alg.ensure(2 * KID_COUNT);
+        if (MC > kSmemBitmapRows) {
+            // a region per warp for the bitmap kernels (8 warps per SM)
+            const long long warps = (long long)lc.num_sms * 8;
+            s |= gbits.ensure((size_t)(warps * gtable_bitmap_words(MC, D)));
+            lc.gbits = gbits.ptr;
+            lc.gbits_warps = warps;
+        }
         s |= dA0.ensure((size_t)E * D * D);
         s |= dp0.ensure((size_t)E * D);
         s |= db0.ensure((size_t)E * D);

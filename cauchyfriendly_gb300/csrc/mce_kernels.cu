@@ -487,12 +487,13 @@ __global__ void k_build_B_vertices(ParentList P, long long nP, const long long* 
 template <int D>
 __global__ void k_build_B(ParentList P, long long nP, const EstStep<D>* st, int with_tp, Tables Told, int* Bkeys,
                           const double* bpert_all, int MC, const int* combo_off, const unsigned char* combos,
-                          const long long* voff, const int* vsv, int* err)
+                          const long long* voff, const int* vsv, int* err, unsigned* gbits)
 {
     extern __shared__ unsigned long long smem_u64[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
     const int words = (1 << MC) > 32 ? (1 << MC) / 32 : 1;
-    unsigned* PB = reinterpret_cast<unsigned*>(smem_u64) + (size_t)wib * 2 * words;  // parent cells
+    unsigned* PB = gbits ? gbits + (size_t)((long long)blockIdx.x * nwb + wib) * 2 * words
+                         : reinterpret_cast<unsigned*>(smem_u64) + (size_t)wib * 2 * words;  // parent cells
     unsigned* IS = PB + words;                                                     // cells found
     for (long long i = (long long)blockIdx.x * nwb + wib; i < nP; i += (long long)gridDim.x * nwb) {
         const int e = P.est[i];
@@ -1293,6 +1294,7 @@ struct GCtx {
     Tables Told;
     const int* Bkeys;
     int MC;
+    unsigned* gbits;  // global bitmap regions (see LaunchCfg), or null: shared memory
 };
 
 // One cell of make_gtable (flattening.hpp:105-224) for record s at `key`.
@@ -1496,7 +1498,8 @@ __global__ void k_gtable_prep(GCtx c, const int* roots_list, long long nroots, c
     const int MC = c.MC;
     const int words = (1 << MC) > 32 ? (1 << MC) / 32 : 1;
     const int capMC = half_cells_cap(MC, D);
-    unsigned* PB = smem_g + (size_t)wib * (2 * words + 32 + capMC);
+    const size_t pw = (size_t)(2 * words + 32 + capMC);
+    unsigned* PB = c.gbits ? c.gbits + (size_t)((long long)blockIdx.x * nwb + wib) * pw : smem_g + (size_t)wib * pw;
     unsigned* RK = PB + words;
     int* bmk = reinterpret_cast<int*>(RK + words);
     int* RKL = bmk + 32;
@@ -1673,7 +1676,8 @@ __global__ void k_gtable(GCtx c, const int* roots_list, long long nroots, const 
     const int MC = c.MC;
     const int words = (1 << MC) > 32 ? (1 << MC) / 32 : 1;
     const int capMC = half_cells_cap(MC, D);
-    unsigned* PB = smem_g + (size_t)wib * (3 * words + 32 + capMC);
+    const size_t pw = (size_t)(3 * words + 32 + capMC);
+    unsigned* PB = c.gbits ? c.gbits + (size_t)((long long)blockIdx.x * nwb + wib) * pw : smem_g + (size_t)wib * pw;
     unsigned* RK = PB + words;
     unsigned* OK = RK + words;
     int* bmk = reinterpret_cast<int*>(OK + words);
@@ -2188,15 +2192,18 @@ void Kernels<D>::build_B(ParentList P, long long nP, const EstStep<D>* st, int w
         k_build_B_vertices<D><<<grid_for(nv, 128, c.num_sms, 16), 128, 0, c.stream>>>(P, nP, voff, nv, bpert, MC,
                                                                                       combo_off, combos, vsv);
     }
+    const bool global_bits = MC > kSmemBitmapRows && c.gbits;
     const size_t pw = build_B_smem_per_warp(MC, D);
-    int warps = (int)(96 * 1024 / pw);
+    int warps = global_bits ? 4 : (int)(96 * 1024 / pw);
     if (warps > 8) warps = 8;
     if (warps < 1) warps = 1;
-    const size_t sm = pw * warps;
-    cudaFuncSetAttribute(k_build_B<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    const size_t sm = global_bits ? 0 : pw * warps;
+    int grid = grid_for(nP, warps, c.num_sms, 8);
+    if (global_bits && (long long)grid * warps > c.gbits_warps) grid = (int)(c.gbits_warps / warps);
+    if (!global_bits) cudaFuncSetAttribute(k_build_B<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     ++g_launches;
-    k_build_B<D><<<grid_for(nP, warps, c.num_sms, 8), warps * 32, sm, c.stream>>>(
-        P, nP, st, with_tp, Told, Bkeys, bpert, MC, combo_off, combos, voff, vsv, err);
+    k_build_B<D><<<grid, warps * 32, sm, c.stream>>>(P, nP, st, with_tp, Told, Bkeys, bpert, MC, combo_off, combos,
+                                                     voff, vsv, err, global_bits ? c.gbits : nullptr);
 }
 
 template <int D>
@@ -2293,14 +2300,16 @@ void Kernels<D>::gtable(TermRecs R, const int* roots_list, long long nroots, con
                         long long max_warps)
 {
     if (nroots == 0) return;
-    GCtx ctx{R, P, Told, Bkeys, MC};
+    const bool global_bits = MC > kSmemBitmapRows && c.gbits;
+    GCtx ctx{R, P, Told, Bkeys, MC, global_bits ? c.gbits : nullptr};
     const size_t pw = gtable_smem_per_warp(MC, D);
-    int warps = (int)(96 * 1024 / pw);
+    int warps = global_bits ? 4 : (int)(96 * 1024 / pw);
     if (warps > 4) warps = 4;
     if (warps < 1) warps = 1;
-    const size_t sm = pw * warps;
-    cudaFuncSetAttribute(k_gtable<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    const size_t sm = global_bits ? 0 : pw * warps;
+    if (!global_bits) cudaFuncSetAttribute(k_gtable<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     int grid = grid_for(nroots, warps, c.num_sms, 16);
+    if (global_bits && (long long)grid * warps > c.gbits_warps) grid = (int)(c.gbits_warps / warps);
     // a scratch region sized for max_warps warps (the caller guarantees
     // max_warps >= 4 >= warps): the warps stride over the roots, so fewer of
     // them give the same tables
@@ -2318,7 +2327,7 @@ void Kernels<D>::gtable_promoted(TermRecs R, const int* roots_list, long long nr
                                  const LaunchCfg& c)
 {
     if (nitems == 0) return;
-    GCtx ctx{R, P, Told, Bkeys, MC};
+    GCtx ctx{R, P, Told, Bkeys, MC, nullptr};
     g_launches += 3;
     k_gtable_prom_prep<D><<<grid_for(nmem, 128, c.num_sms, 8), 128, 0, c.stream>>>(ctx, nroots, nmem, members, f);
     k_gtable_prom_eval<D><<<grid_for(nitems, 128, c.num_sms, 16), 128, 0, c.stream>>>(
@@ -2334,16 +2343,19 @@ void Kernels<D>::gtable_prep(TermRecs R, const int* roots_list, long long nroots
                              int* err, const LaunchCfg& c)
 {
     if (nroots == 0) return;
-    GCtx ctx{R, P, Told, Bkeys, MC};
+    const bool global_bits = MC > kSmemBitmapRows && c.gbits;
+    GCtx ctx{R, P, Told, Bkeys, MC, global_bits ? c.gbits : nullptr};
     const int words = (1 << MC) > 32 ? (1 << MC) / 32 : 1;
     const size_t pw = (size_t)(2 * words + 32 + half_cells_cap(MC, D)) * 4;
-    int warps = (int)(96 * 1024 / pw);
+    int warps = global_bits ? 4 : (int)(96 * 1024 / pw);
     if (warps > 4) warps = 4;
     if (warps < 1) warps = 1;
-    const size_t sm = pw * warps;
-    cudaFuncSetAttribute(k_gtable_prep<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    const size_t sm = global_bits ? 0 : pw * warps;
+    if (!global_bits) cudaFuncSetAttribute(k_gtable_prep<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    int grid = grid_for(nroots, warps, c.num_sms, 16);
+    if (global_bits && (long long)grid * warps > c.gbits_warps) grid = (int)(c.gbits_warps / warps);
     ++g_launches;
-    k_gtable_prep<D><<<grid_for(nroots, warps, c.num_sms, 16), warps * 32, sm, c.stream>>>(
+    k_gtable_prep<D><<<grid, warps * 32, sm, c.stream>>>(
         ctx, roots_list, nroots, gcnt, goff, members, toff, Tnew, f.gnr, gitems, gcells, f.minfo, f.rps2, f.mps2,
         f.rflag, f.mflag, err);
 }
@@ -2355,7 +2367,7 @@ void Kernels<D>::gtable_combine(TermRecs R, const int* roots_list, long long nro
                                 int* tcnt, int* alive, int* src, const GFlat& f, int MC, const LaunchCfg& c)
 {
     if (ncells == 0) return;
-    GCtx ctx{R, P, Told, Bkeys, MC};
+    GCtx ctx{R, P, Told, Bkeys, MC, nullptr};
     ++g_launches;
     k_gtable_combine<D><<<grid_for(ncells, 128, c.num_sms, 16), 128, 0, c.stream>>>(
         ctx, roots_list, nroots, coff, ncells, gcnt, goff, members, toff, Tnew, tcnt, alive, src, f.rflag, f.ioff,
@@ -2369,7 +2381,7 @@ void Kernels<D>::gtable_eval(TermRecs R, const int* roots_list, long long nroots
                              const LaunchCfg& c)
 {
     if (nitems == 0) return;
-    GCtx ctx{R, P, Told, Bkeys, MC};
+    GCtx ctx{R, P, Told, Bkeys, MC, nullptr};
     ++g_launches;
     k_gtable_eval<D><<<grid_for(nitems, 128, c.num_sms, 16), 128, 0, c.stream>>>(
         ctx, roots_list, nroots, f.ioff, nitems, f.gnr, goff, members, f.minfo, f.rps2, f.mps2, gscale, toff, Tnew,

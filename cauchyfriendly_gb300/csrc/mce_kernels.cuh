@@ -13,7 +13,21 @@ extern thread_local long long g_launches;
 struct LaunchCfg {
     cudaStream_t stream;
     int num_sms;
+    // Cell bitmaps (2^m bits per term) live in shared memory up to
+    // kSmemBitmapRows hyperplanes; above that each warp of the bitmap kernels
+    // takes a region of this global buffer (gbits_warps regions of the largest
+    // per-warp size), and the kernels launch at most that many warps.
+    unsigned* gbits = nullptr;
+    long long gbits_warps = 0;
 };
+constexpr int kSmemBitmapRows = 16;
+constexpr int kMaxBitmapRows = 24;
+// words of one warp's bitmap region in the g-table kernels (the largest user)
+inline long long gtable_bitmap_words(int MC, int D)
+{
+    const long long words = (1LL << MC) > 32 ? (1LL << MC) / 32 : 1;
+    return 3 * words + 32 + half_cells_cap(MC, D);
+}
 
 // Scratch for the device-wide scans.
 struct ScanScratch {

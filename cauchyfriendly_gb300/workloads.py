@@ -187,3 +187,18 @@ def five_state_ltv_windows(seed=0, steps=200, dt=0.1, outlier_frac=0.02, outlier
         zs[k] = H @ x + v
     prob["msmts"] = zs
     return prob
+
+
+def many_gamma(d, pncc, steps, seed=0):
+    """LTI problem whose terms grow pncc hyperplanes per step (pncc process-noise
+    columns, Gamma 0.3 N(0,1)): up to (steps-1)*pncc + d hyperplanes, the
+    shapes above the shared-memory bitmap limit.  Phi random stable
+    (eigenvalue moduli in [0.8, 0.95]), H N(0,1), beta 0.05, gamma 0.2,
+    p0 0.1."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    Phi = random_stable(rng, d, 0.8, 0.95)
+    Gamma = 0.3 * rng.standard_normal((d, pncc))
+    H = rng.standard_normal((1, d))
+    prob = _base(d, pncc, 1, Phi, Gamma, [0.05] * pncc, H, [0.2], [0.1] * d, steps)
+    prob["msmts"] = simulate(prob, rng)
+    return prob

@@ -77,8 +77,8 @@ int mce_batch_step(mce_handle* h, const double* msmt, const double* Phi, const d
  *    library, and the kernel runs as many warps as it has slots for; a
  *    handle whose full-shape terms would need more than 4 warps' worth
  *    (above 524,288 half-cells per term) is refused with MCE_ERR_SHAPE
- *    before any work.  Under this build's limit of 16 hyperplanes per term
- *    the largest need is 1 MiB (8 states), so every handle fits;
+ *    before any work.  Under this build's limit of 24 hyperplanes per term
+ *    the largest need is 390,656 half-cells (8 states), so every handle fits;
  *  - the handle's own device buffers must already be large enough (they grow
  *    only in the other calls: step the handle with mce_batch_step over a
  *    representative history, then mce_reset); a buffer that would have to

@@ -17,6 +17,7 @@ Needs the reference sources (only present where the fixtures are made):
     python tests/golden/make_golden.py --ext    # the extended-mode fixtures only
     python tests/golden/make_golden.py --rel    # the relative-system fixtures only
     python tests/golden/make_golden.py --postftr  # print_basic_info fixtures only
+    python tests/golden/make_golden.py --wide   # terms above 16 hyperplanes only
 """
 import os
 import sys
@@ -280,9 +281,24 @@ def pack_rel2d(name, family, wseeds, seeds, updates, trel, full, bar_seed):
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **arr)
 
 
+def wide_cases():
+    """Terms above 16 hyperplanes (the cell bitmaps leave shared memory):
+    three Gamma columns (3 states, up to 21 rows; 4 states, up to 19) and
+    four (2 states, up to 22)."""
+    return [
+        ("wide_three_state_21", W.many_gamma(3, 3, 7, seed=5), 41),
+        ("wide_two_state_22", W.many_gamma(2, 4, 6, seed=6), 42),
+        ("wide_four_state_19", W.many_gamma(4, 3, 6, seed=7), 43),
+    ]
+
+
 def main():
     oracle.build()
     only = [a[2:] for a in sys.argv[1:] if a.startswith("--")]
+    if not only or "wide" in only:
+        for name, prob, seed in wide_cases():
+            n = pack(name, prob, seed)
+            print("wrote %s.npz (%d updates)" % (name, n))
     if not only:
         for name, prob, seed in cases():
             n = pack(name, prob, seed)
