@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--no-autotune", action="store_true", help="fixed block sizes (no block-size autotuner)")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n-est", type=int, default=4096)
     ap.add_argument("--seed", type=int, default=0)
@@ -576,6 +577,16 @@ def run_rel2d(args):
     print(json.dumps(line), flush=True)
 
 
+def autotune_summary(table, passes, off):
+    """The autotuner's settled block sizes per kernel as {log2 items: block}."""
+    if off:
+        return {"enabled": False}
+    blocks = {}
+    for r in table:
+        blocks.setdefault(r["kernel"], {})[str(r["log2_items"])] = r["block"]
+    return {"enabled": True, "settled_keys": len(table), "tuning_passes": passes, "blocks": blocks}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -626,6 +637,19 @@ def main():
         lib.mce_kernel_group_stats(est._h, k, ctypes.byref(ms), ctypes.byref(nl), ctypes.byref(ab), ctypes.byref(af))
         alg[g] = (ab.value, af.value)
     lib.mce_set_profiling(est._h, 1)
+    from cauchyfriendly_gb300 import autotune_configure, autotune_table
+    tuning_passes = 0
+    if args.no_autotune:
+        autotune_configure(False)
+    else:
+        # untimed passes until the block-size autotuner settles every key it has seen
+        prev, stable = -1, 0
+        while tuning_passes < 16 and stable < 2:
+            one_pass()
+            tuning_passes += 1
+            n = len(autotune_table())
+            stable = stable + 1 if n == prev else 0
+            prev = n
     for _ in range(max(0, args.warmup - 1)):
         one_pass()
     terms_per_pass = est.post_mu_terms()
@@ -700,6 +724,7 @@ def main():
         "alg_per_pass": alg_per_pass,
         "roofline": roofline,
         "clocks": clocks,
+        "autotune": autotune_summary(autotune_table(), tuning_passes, args.no_autotune),
     }
     if rank == 0 and not args.no_plain:
         # batched vs plain: the same estimators one handle at a time

@@ -6,6 +6,7 @@ reached through the C ABI in include/mce_c_api.h.  This package holds the
 build recipe, the ctypes binding, the estimator mirrors and the seeded
 synthetic workloads.
 """
-from .estimator import BatchedCauchyEstimator, CauchyEstimator, RelativeSystem2D, max_shape  # noqa: F401
+from .estimator import (  # noqa: F401
+    BatchedCauchyEstimator, CauchyEstimator, RelativeSystem2D, autotune_configure, autotune_table, max_shape)
 
 __all__ = ["BatchedCauchyEstimator", "CauchyEstimator", "RelativeSystem2D", "max_shape"]

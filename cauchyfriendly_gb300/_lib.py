@@ -72,6 +72,9 @@ SIGNATURES = {
     "mce_num_kernel_groups": (ctypes.c_int, []),
     "mce_kernel_group_name": (ctypes.c_char_p, [ctypes.c_int]),
     "mce_kernel_group_stats": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _lp, _dp, _dp]),
+    "mce_autotune_configure": (ctypes.c_int, [ctypes.c_int]),
+    "mce_autotune_table": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
+    "mce_autotune_kernel_name": (ctypes.c_char_p, [ctypes.c_int]),
     "mce_destroy": (None, [_vp]),
     "mce_sym_eig": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp]),
     "mce_speyers_window_init": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double, _dp,

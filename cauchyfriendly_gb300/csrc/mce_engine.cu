@@ -2616,6 +2616,23 @@ int mce_kernel_group_stats(mce_handle* h, int k, double* ms, long long* launches
     if (alg_flops) *alg_flops = g->kflops[k];
     return MCE_OK;
 }
+int mce_autotune_configure(int enabled)
+{
+    if (enabled != 0 && enabled != 1) return MCE_ERR_ARG;
+    tune_configure(enabled);
+    return MCE_OK;
+}
+int mce_autotune_table(int* rows, float* best_ms, int max_rows)
+{
+    if (max_rows < 0 || (max_rows > 0 && !rows)) return MCE_ERR_ARG;
+    return tune_table(rows, best_ms, max_rows);
+}
+const char* mce_autotune_kernel_name(int k)
+{
+    static const char* names[TK_COUNT] = {"tp", "build_B_vertices", "mu_rows", "gtable_eval",
+                                          "gtable_combine", "gtable_prom_eval", "compact", "ftr_resolve"};
+    return (k >= 0 && k < TK_COUNT) ? names[k] : "";
+}
 void mce_destroy(mce_handle* h)
 {
     if (!h) return;

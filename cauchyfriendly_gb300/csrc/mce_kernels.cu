@@ -8,7 +8,11 @@
 // reduction group, member order, next parent order) is a rule on positions.
 #include "mce_kernels.cuh"
 
+#include <algorithm>
 #include <climits>
+#include <cstdlib>
+#include <mutex>
+#include <vector>
 
 #ifndef MCE_ONLY_DIM
 #define MCE_ONLY_DIM -1  // every dimension and the shape-agnostic kernels in one unit
@@ -19,6 +23,153 @@ namespace mce {
 
 #if MCE_COMMON_UNIT
 thread_local long long g_launches = 0;
+
+namespace {
+constexpr int kTuneCands[4] = {64, 128, 256, 512};
+constexpr int kTuneSamples = 2;
+struct TuneEntry {
+    int device, kernel, D, MC, bucket;
+    int next = 0;  // next measurement: candidate index * kTuneSamples + sample
+    float ms[4] = {1e30f, 1e30f, 1e30f, 1e30f};  // fastest sample per candidate
+    int best = -1;  // index into kTuneCands once tuned
+    int pending = -1;  // candidate whose events are in flight
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+};
+std::mutex g_tune_mu;
+std::vector<TuneEntry*> g_tune;
+int g_tune_enabled = -1;  // -1: read MCE_AUTOTUNE on first use
+
+TuneEntry* tune_find(int device, int kernel, int D, int MC, int bucket)
+{
+    for (TuneEntry* e : g_tune)
+        if (e->device == device && e->kernel == kernel && e->D == D && e->MC == MC && e->bucket == bucket) return e;
+    TuneEntry* e = new TuneEntry();
+    e->device = device;
+    e->kernel = kernel;
+    e->D = D;
+    e->MC = MC;
+    e->bucket = bucket;
+    if (cudaEventCreate(&e->e0) != cudaSuccess || cudaEventCreate(&e->e1) != cudaSuccess) {
+        cudaGetLastError();
+        e->best = 1;  // no events: keep the default block size
+    }
+    g_tune.push_back(e);
+    return e;
+}
+
+// Folds a finished measurement in; picks the winner after the last one.
+void tune_collect(TuneEntry* e)
+{
+    if (e->pending < 0) return;
+    const cudaError_t q = cudaEventQuery(e->e1);
+    if (q == cudaErrorNotReady) return;
+    float ms = 0;
+    if (q == cudaSuccess && cudaEventElapsedTime(&ms, e->e0, e->e1) == cudaSuccess) {
+        e->ms[e->pending] = std::min(e->ms[e->pending], ms);
+    } else {
+        cudaGetLastError();
+    }
+    e->pending = -1;
+    if (e->next >= 4 * kTuneSamples) {
+        int b = 1;
+        for (int c = 0; c < 4; c++)
+            if (e->ms[c] < e->ms[b]) b = c;
+        e->best = b;
+    }
+}
+}  // namespace
+
+TuneLaunch tune_begin(int kernel, int D, int MC, long long items, int def_block, int max_block, cudaStream_t st)
+{
+    TuneLaunch t;
+    t.block = def_block;
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    if (g_tune_enabled < 0) {
+        const char* v = getenv("MCE_AUTOTUNE");
+        g_tune_enabled = (v && v[0] == '0') ? 0 : 1;
+    }
+    if (!g_tune_enabled || items <= 0) return t;
+    int bucket = 0;
+    while (bucket < 62 && (1LL << (bucket + 1)) <= items) bucket++;
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess) {
+        cudaGetLastError();
+        return t;
+    }
+    TuneEntry* e = tune_find(device, kernel, D, MC, bucket);
+    tune_collect(e);
+    if (e->best >= 0) {
+        t.block = std::min(kTuneCands[e->best], max_block);
+        return t;
+    }
+    // one measurement in flight per key; launches meanwhile take the default
+    if (e->pending >= 0 || e->next >= 4 * kTuneSamples) return t;
+    int c = e->next / kTuneSamples;
+    while (c < 4 && kTuneCands[c] > max_block) {
+        e->ms[c] = 1e30f;
+        e->next = (c + 1) * kTuneSamples;
+        c++;
+    }
+    if (c >= 4) {
+        e->best = 1;
+        return t;
+    }
+    if (cudaEventRecord(e->e0, st) != cudaSuccess) {
+        cudaGetLastError();
+        return t;
+    }
+    e->next++;
+    e->pending = c;
+    t.block = kTuneCands[c];
+    t.entry = e;
+    return t;
+}
+
+void tune_end(const TuneLaunch& t, cudaStream_t st)
+{
+    if (!t.entry) return;
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    TuneEntry* e = static_cast<TuneEntry*>(t.entry);
+    if (cudaEventRecord(e->e1, st) != cudaSuccess) {
+        cudaGetLastError();
+        e->pending = -1;  // the sample is lost; the candidate is measured again
+        e->next--;
+    }
+}
+
+int tune_table(int* out, float* best_ms, int n)
+{
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    int k = 0;
+    for (TuneEntry* e : g_tune) {
+        tune_collect(e);
+        if (e->best < 0) continue;
+        if (k < n) {
+            out[5 * k] = e->kernel;
+            out[5 * k + 1] = e->D;
+            out[5 * k + 2] = e->MC;
+            out[5 * k + 3] = e->bucket;
+            out[5 * k + 4] = kTuneCands[e->best];
+            if (best_ms) best_ms[k] = e->ms[e->best] < 1e29f ? e->ms[e->best] : 0.0f;
+        }
+        k++;
+    }
+    return k;
+}
+
+void tune_configure(int enabled)
+{
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    for (TuneEntry* e : g_tune) {
+        if (e->pending >= 0) cudaEventSynchronize(e->e1);
+        if (e->e0) cudaEventDestroy(e->e0);
+        if (e->e1) cudaEventDestroy(e->e1);
+        delete e;
+    }
+    g_tune.clear();
+    cudaGetLastError();
+    g_tune_enabled = enabled ? 1 : 0;
+}
 #endif
 
 static constexpr unsigned kFull = 0xffffffffu;
@@ -35,6 +186,27 @@ static inline int grid_for(long long items, int per_block, int num_sms, int bloc
     if (g > cap) g = cap;
     if (g < 1) g = 1;
     return (int)g;
+}
+
+// Grid of a tuned launch: the same resident threads per SM as blocks_per_sm
+// blocks of 128 threads, whatever block size the tuner chose.
+static inline int tuned_grid(long long items, int block, int num_sms, int blocks_per_sm_at_128)
+{
+    int bps = blocks_per_sm_at_128 * 128 / block;
+    if (bps > 64) bps = 64;
+    if (bps < 1) bps = 1;
+    return grid_for(items, block, num_sms, bps);
+}
+
+// The largest block a kernel may launch with (registers bound it).
+static inline int max_block_of(const void* kern)
+{
+    cudaFuncAttributes a;
+    if (cudaFuncGetAttributes(&a, kern) != cudaSuccess) {
+        cudaGetLastError();
+        return 128;
+    }
+    return a.maxThreadsPerBlock;
 }
 
 // ---------------------------------------------------------------------------
@@ -2169,7 +2341,11 @@ void Kernels<D>::tp(ParentList P, long long nP, const EstStep<D>* st, int with_t
 {
     if (nP == 0) return;
     ++g_launches;
-    k_tp<D><<<grid_for(nP, 128, c.num_sms), 128, 0, c.stream>>>(P, nP, st, with_tp, MC, Bcap, nvert, err);
+    static const int mb = max_block_of((const void*)k_tp<D>);
+    const TuneLaunch t = tune_begin(TK_TP, D, MC, nP, 128, mb, c.stream);
+    k_tp<D><<<tuned_grid(nP, t.block, c.num_sms, 16), t.block, 0, c.stream>>>(P, nP, st, with_tp, MC, Bcap, nvert,
+                                                                             err);
+    tune_end(t, c.stream);
 }
 
 static inline size_t build_B_smem_per_warp(int MC, int D)
@@ -2189,8 +2365,11 @@ void Kernels<D>::build_B(ParentList P, long long nP, const EstStep<D>* st, int w
     if (nP == 0) return;
     if (nv > 0) {
         ++g_launches;
-        k_build_B_vertices<D><<<grid_for(nv, 128, c.num_sms, 16), 128, 0, c.stream>>>(P, nP, voff, nv, bpert, MC,
-                                                                                      combo_off, combos, vsv);
+        static const int mb = max_block_of((const void*)k_build_B_vertices<D>);
+        const TuneLaunch t = tune_begin(TK_BUILD_B_VERTICES, D, MC, nv, 128, mb, c.stream);
+        k_build_B_vertices<D><<<tuned_grid(nv, t.block, c.num_sms, 16), t.block, 0, c.stream>>>(
+            P, nP, voff, nv, bpert, MC, combo_off, combos, vsv);
+        tune_end(t, c.stream);
     }
     const bool global_bits = MC > kSmemBitmapRows && c.gbits;
     const size_t pw = build_B_smem_per_warp(MC, D);
@@ -2213,7 +2392,13 @@ void Kernels<D>::mu(ParentList P, long long nP, const EstStep<D>* st, const long
 {
     if (nP == 0) return;
     ++g_launches;
-    k_mu_rows<D><<<grid_for(nP, 128, c.num_sms, 16), 128, 0, c.stream>>>(P, nP, st, Bkeys, frow, fint, MC);
+    {
+        static const int mb = max_block_of((const void*)k_mu_rows<D>);
+        const TuneLaunch t = tune_begin(TK_MU_ROWS, D, MC, nP, 128, mb, c.stream);
+        k_mu_rows<D><<<tuned_grid(nP, t.block, c.num_sms, 16), t.block, 0, c.stream>>>(P, nP, st, Bkeys, frow, fint,
+                                                                                      MC);
+        tune_end(t, c.stream);
+    }
     if (nterms == 0) return;
     // each thread stages one term's rows (MC x D, p, q) in shared memory
     const size_t rs = (size_t)(MC * D + 2 * MC) * sizeof(double);
@@ -2280,9 +2465,12 @@ void Kernels<D>::ftr_resolve(TermRecs R, long long nR, const void* ent, const lo
     const long long n = wl_in ? n_bound : nR;
     if (n == 0) return;
     ++g_launches;
-    k_ftr_resolve_scan<D><<<grid_for(n, 128, c.num_sms), 128, 0, c.stream>>>(
+    static const int mb = max_block_of((const void*)k_ftr_resolve_scan<D>);
+    const TuneLaunch t = tune_begin(TK_FTR_RESOLVE, D, MC, n, 128, mb, c.stream);
+    k_ftr_resolve_scan<D><<<tuned_grid(n, t.block, c.num_sms, 16), t.block, 0, c.stream>>>(
         R, nR, static_cast<const CellEntry<D>*>(ent), boff, hmask, MC, status, owner, wl_in, n_in, wl_out, n_out,
         resume);
+    tune_end(t, c.stream);
 }
 
 static inline size_t gtable_smem_per_warp(int MC, int D)
@@ -2330,8 +2518,11 @@ void Kernels<D>::gtable_promoted(TermRecs R, const int* roots_list, long long nr
     GCtx ctx{R, P, Told, Bkeys, MC, nullptr};
     g_launches += 3;
     k_gtable_prom_prep<D><<<grid_for(nmem, 128, c.num_sms, 8), 128, 0, c.stream>>>(ctx, nroots, nmem, members, f);
-    k_gtable_prom_eval<D><<<grid_for(nitems, 128, c.num_sms, 16), 128, 0, c.stream>>>(
+    static const int mb = max_block_of((const void*)k_gtable_prom_eval<D>);
+    const TuneLaunch t = tune_begin(TK_GTABLE_PROM_EVAL, D, MC, nitems, 128, mb, c.stream);
+    k_gtable_prom_eval<D><<<tuned_grid(nitems, t.block, c.num_sms, 16), t.block, 0, c.stream>>>(
         ctx, roots_list, nroots, nitems, members, gscale, toff, Tnew, f);
+    tune_end(t, c.stream);
     k_gtable_prom_combine<D><<<grid_for(ncells, 128, c.num_sms, 8), 128, 0, c.stream>>>(
         ctx, roots_list, nroots, ncells, members, toff, Tnew, f);
 }
@@ -2369,9 +2560,12 @@ void Kernels<D>::gtable_combine(TermRecs R, const int* roots_list, long long nro
     if (ncells == 0) return;
     GCtx ctx{R, P, Told, Bkeys, MC, nullptr};
     ++g_launches;
-    k_gtable_combine<D><<<grid_for(ncells, 128, c.num_sms, 16), 128, 0, c.stream>>>(
+    static const int mb = max_block_of((const void*)k_gtable_combine<D>);
+    const TuneLaunch t = tune_begin(TK_GTABLE_COMBINE, D, MC, ncells, 128, mb, c.stream);
+    k_gtable_combine<D><<<tuned_grid(ncells, t.block, c.num_sms, 16), t.block, 0, c.stream>>>(
         ctx, roots_list, nroots, coff, ncells, gcnt, goff, members, toff, Tnew, tcnt, alive, src, f.rflag, f.ioff,
         f.gnr, f.minfo, f.mflag, f.gv);
+    tune_end(t, c.stream);
 }
 
 template <int D>
@@ -2383,9 +2577,12 @@ void Kernels<D>::gtable_eval(TermRecs R, const int* roots_list, long long nroots
     if (nitems == 0) return;
     GCtx ctx{R, P, Told, Bkeys, MC, nullptr};
     ++g_launches;
-    k_gtable_eval<D><<<grid_for(nitems, 128, c.num_sms, 16), 128, 0, c.stream>>>(
+    static const int mb = max_block_of((const void*)k_gtable_eval<D>);
+    const TuneLaunch t = tune_begin(TK_GTABLE_EVAL, D, MC, nitems, 128, mb, c.stream);
+    k_gtable_eval<D><<<tuned_grid(nitems, t.block, c.num_sms, 16), t.block, 0, c.stream>>>(
         ctx, roots_list, nroots, f.ioff, nitems, f.gnr, goff, members, f.minfo, f.rps2, f.mps2, gscale, toff, Tnew,
         f.gv, f.rflag, f.mflag);
+    tune_end(t, c.stream);
 }
 
 template <int D>
@@ -2394,7 +2591,11 @@ void Kernels<D>::compact(TermRecs R, const int* alive, const int* src, long long
 {
     if (nR == 0) return;
     ++g_launches;
-    k_compact<D><<<grid_for(nR, 256, c.num_sms), 256, 0, c.stream>>>(R, alive, src, nR, new_slot, toff, tcnt, Pn, MC);
+    static const int mb = max_block_of((const void*)k_compact<D>);
+    const TuneLaunch t = tune_begin(TK_COMPACT, D, MC, nR, 256, mb, c.stream);
+    k_compact<D><<<tuned_grid(nR, t.block, c.num_sms, 32), t.block, 0, c.stream>>>(R, alive, src, nR, new_slot, toff,
+                                                                                 tcnt, Pn, MC);
+    tune_end(t, c.stream);
 }
 
 // ---------------------------------------------------------------------------

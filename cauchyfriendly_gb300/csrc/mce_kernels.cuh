@@ -20,6 +20,35 @@ struct LaunchCfg {
     unsigned* gbits = nullptr;
     long long gbits_warps = 0;
 };
+// Block-size autotuner of the thread-per-item kernels (grid-stride loops with
+// no shared memory, no block-wide step and no reductions, so every block size
+// gives bit-identical results).  A launch site asks for its block size by
+// (kernel, state dimension, hyperplane capacity, log2 of the item count); the
+// first launches of a key try 64, 128, 256 and 512 threads, each twice, timed
+// with CUDA events on the launch's stream, and later launches take the
+// fastest.  MCE_AUTOTUNE=0 in the environment keeps the fixed sizes.
+enum TuneKernel {
+    TK_TP = 0,
+    TK_BUILD_B_VERTICES,
+    TK_MU_ROWS,
+    TK_GTABLE_EVAL,
+    TK_GTABLE_COMBINE,
+    TK_GTABLE_PROM_EVAL,
+    TK_COMPACT,
+    TK_FTR_RESOLVE,
+    TK_COUNT
+};
+struct TuneLaunch {
+    int block = 128;
+    void* entry = nullptr;  // set when this launch is a timed measurement
+};
+TuneLaunch tune_begin(int kernel, int D, int MC, long long items, int def_block, int max_block, cudaStream_t st);
+void tune_end(const TuneLaunch& t, cudaStream_t st);
+// The settled keys as rows (kernel, D, MC, log2 items, block) and the best
+// sample's ms; returns how many there are (fills at most n).
+int tune_table(int* out, float* best_ms, int n);
+// Drops every tuned key and turns the tuner on or off.
+void tune_configure(int enabled);
 constexpr int kSmemBitmapRows = 16;
 constexpr int kMaxBitmapRows = 24;
 // words of one warp's bitmap region in the g-table kernels (the largest user)

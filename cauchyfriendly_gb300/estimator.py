@@ -225,6 +225,28 @@ class BatchedCauchyEstimator:
         return X, Y
 
 
+def autotune_configure(enabled=True):
+    """Drops every tuned block size and turns the process-wide block-size
+    autotuner of the thread-per-item kernels on or off (off: fixed sizes)."""
+    _lib.check(_lib.load().mce_autotune_configure(1 if enabled else 0), "mce_autotune_configure")
+
+
+def autotune_table():
+    """The settled autotuner keys: dicts of kernel, d, hyperplane capacity
+    (mc), log2 of the launch's item count, the chosen block size and the
+    fastest sample's device ms."""
+    lib = _lib.load()
+    n = lib.mce_autotune_table(None, None, 0)
+    _lib.check(n, "mce_autotune_table")
+    if n == 0:
+        return []
+    rows = (ctypes.c_int * (5 * n))()
+    ms = (ctypes.c_float * n)()
+    got = min(n, lib.mce_autotune_table(rows, ms, n))
+    return [dict(kernel=lib.mce_autotune_kernel_name(rows[5 * i]).decode(), d=rows[5 * i + 1], mc=rows[5 * i + 2],
+                 log2_items=rows[5 * i + 3], block=rows[5 * i + 4], ms=float(ms[i])) for i in range(got)]
+
+
 def draw_bar_nu(d, seed=-1):
     """The d draws of PointWiseNDimCauchyCPDF's constructor
     (include/cpdf_ndim.hpp:385-389) from libc rand(); seed >= 0 seeds it first."""

@@ -382,6 +382,22 @@ const char* mce_kernel_group_name(int group);
 int mce_kernel_group_stats(mce_handle* h, int group, double* ms, long long* launches, double* alg_bytes,
                            double* alg_flops);
 
+/* Block-size autotuner of the thread-per-item kernels (kernel ids: 0 TP,
+ * 1 vertex build of the new hyperplane arrangements, 2 MU rows, 3 g-table
+ * evaluation, 4 g-table combination, 5 promoted-root g-table evaluation,
+ * 6 compaction, 7 FTR resolution).  Process-wide: each (kernel, state
+ * dimension, hyperplane capacity, log2 of the launch's item count) key tries
+ * 64/128/256/512 threads on its first launches, timed with CUDA events on the
+ * launching stream, and keeps the fastest.  Block size does not change any
+ * result.  mce_autotune_configure drops every tuned key and turns the tuner
+ * on (1, the default unless MCE_AUTOTUNE=0) or off (0, fixed block sizes).
+ * mce_autotune_table writes up to max_rows settled keys as 5 ints each
+ * (kernel, d, hyperplane capacity, log2 items, block) and the best sample's
+ * ms, and returns how many keys are settled. */
+int mce_autotune_configure(int enabled);
+int mce_autotune_table(int* rows, float* best_ms, int max_rows);
+const char* mce_autotune_kernel_name(int kernel);
+
 void mce_destroy(mce_handle* h);
 
 #ifdef __cplusplus

@@ -66,3 +66,12 @@ def test_invalid_arguments_return_status_without_device():
     assert "24" in _lib.last_error()
     # NULL handle
     assert lib.mce_step(None, 0.0, None, None, None, None, 0.0, None, None) == -1
+
+
+def test_autotune_entry_points_without_device():
+    lib = _lib.load()
+    assert lib.mce_autotune_table(None, None, 0) == 0
+    assert lib.mce_autotune_table(None, None, 4) < 0
+    assert lib.mce_autotune_configure(2) < 0
+    assert lib.mce_autotune_kernel_name(3) == b"gtable_eval"
+    assert lib.mce_autotune_kernel_name(99) == b""

@@ -257,3 +257,33 @@ def test_stepping_past_the_last_step_returns_status():
     assert est.num_terms() >= 1
     assert est.device_errors() == 0
     est.close()
+
+
+def test_autotuned_block_sizes_keep_results_bit_identical():
+    """The block-size autotuner only changes launch shapes: a batch run with
+    the tuner off, the run that tunes and a run on the tuned sizes give the
+    same doubles, and every settled key holds one of the candidate sizes."""
+    from cauchyfriendly_gb300 import autotune_configure, autotune_table
+    from cauchyfriendly_gb300 import workloads as W
+    probs = W.batched_three_state(512, seed=5, steps_lo=5, steps_hi=8)
+    consts = [oracle.draw_reference_constants(500 + i, 3, oracle.max_shape_of(p)) for i, p in enumerate(probs)]
+    try:
+        autotune_configure(False)
+        fixed, t0 = _batch_run_compare(probs, consts)
+        assert autotune_table() == []
+        autotune_configure(True)
+        tuning, t1 = _batch_run_compare(probs, consts)
+        tuned, t2 = _batch_run_compare(probs, consts)
+        table = autotune_table()
+    finally:
+        autotune_configure(True)
+    assert t0 == t1 == t2
+    assert table and all(r["block"] in (64, 128, 256, 512) for r in table), table
+    assert {r["kernel"] for r in table} >= {"tp", "build_B_vertices", "gtable_eval", "compact"}, table
+    for run in (tuning, tuned):
+        for a, b in zip(run, fixed):
+            assert len(a) == len(b)
+            for ra, rb in zip(a, b):
+                assert ra["Nt"] == rb["Nt"] and ra["err"] == rb["err"]
+                for k in ("fz", "mean", "cov"):
+                    assert G.bitwise_equal(np.asarray(ra[k]), np.asarray(rb[k])), k
