@@ -81,6 +81,8 @@ SIGNATURES = {
                                                _dp, _dp, _dp]),
     "mce_swm_create": (_vp, [ctypes.c_int] * 7 + [_dp] * 9 + [ctypes.c_double, ctypes.c_int, _vp, _dp, _dp, _dp,
                                                               ctypes.c_int, _ip]),
+    "mce_swm_create_nonlin": (_vp, [ctypes.c_int] * 7 + [_dp] * 6 + [ctypes.c_double, ctypes.c_int, _vp, _vp, _vp,
+                                                                     _dp, _dp, _dp, ctypes.c_int, _ip]),
     "mce_swm_step": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip]),
     "mce_swm_post_mu_terms": (ctypes.c_longlong, [_vp]),
     "mce_swm_window": (_vp, [_vp, ctypes.c_int]),

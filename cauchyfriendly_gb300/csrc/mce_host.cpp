@@ -275,6 +275,15 @@ int mce_speyers_window_init(int n, const double* xhat, const double* Phat, const
 // before each step but its first, the restarted window with the restart
 // estimate, and the manager with the restart estimate before Speyer's
 // statistics, each on its own copy of the dynamics container.
+// Extended (nonlinear) mode: each window's container x holds its x_bar; the
+// dynamics callback propagates it (and sets Phi, Gamma, beta) before each
+// step but a window's first; every measurement update runs the measurement
+// model (z_bar = h(x_bar)) and the extended update callback (H, gamma), steps
+// the estimator (no controls) with z - z_bar and finalises the extended
+// moments (x_bar <- the new estimate).  A restart is about the best window's
+// x_bar: Speyer's statistics of dx = x_hat - x_bar and dz = z - h(x_bar),
+// and the restarted window takes x_bar as its own
+// (include/cauchy_windows.hpp:480-540, :600-660 and :1123-1139).
 struct mce_swm {
     struct Duc {
         std::vector<double> x, Phi, Gamma, B, H, beta, gamma;
@@ -282,7 +291,12 @@ struct mce_swm {
     };
     int n_mgr = 0, W = 0, num_sim_steps = 0, d = 0, cmcc = 0, pncc = 0, p = 0, init_step = 0;
     double dt = 0;
+    int est_cmcc = 0;  // controls of the window estimators (none in extended mode)
     mce_dynamics_callback cb = nullptr;
+    bool ext = false;
+    mce_msmt_model_callback msmt_cb = nullptr;
+    mce_dynamics_callback ext_cb = nullptr;
+    std::vector<double> xbar_win;    // W * n_mgr * d: the x_bar each window last reported
     std::vector<mce_handle*> slots;  // W batched handles over the managers
     std::vector<Duc> wduc;           // W * n_mgr window containers
     std::vector<Duc> mduc;           // n_mgr manager containers
@@ -332,25 +346,27 @@ struct mce_swm {
         q.c.gamma = q.gamma.data();
     }
 
-    // One update of window slot j with measurement index i of every manager.
-    int step_slot(int j, int i, const double* msmts)
+    // One update of window slot j with measurement index i of every manager
+    // (zs: the managers' measurements, else msmts[m * p + i]).
+    int step_slot(int j, int i, const double* msmts, const double* zs = nullptr)
     {
         const size_t n = n_mgr;
+        const int cm = est_cmcc;
         std::vector<double> z(n), Phi(n * d * d), Gam(n * d * std::max(pncc, 1)), beta(n * std::max(pncc, 1)),
-            H(n * d), gam(n), B(n * d * std::max(cmcc, 1));
+            H(n * d), gam(n), B(n * d * std::max(cm, 1));
         for (int m = 0; m < n_mgr; m++) {
             const Duc& q = wduc[(size_t)j * n_mgr + m];
-            z[m] = msmts[(size_t)m * p + i];
+            z[m] = zs ? zs[m] : msmts[(size_t)m * p + i];
             memcpy(&Phi[(size_t)m * d * d], q.Phi.data(), sizeof(double) * d * d);
             if (pncc) memcpy(&Gam[(size_t)m * d * pncc], q.Gamma.data(), sizeof(double) * d * pncc);
             if (pncc) memcpy(&beta[(size_t)m * pncc], q.beta.data(), sizeof(double) * pncc);
             memcpy(&H[(size_t)m * d], q.H.data() + (size_t)i * d, sizeof(double) * d);
             gam[m] = q.gamma[i];
-            if (cmcc) memcpy(&B[(size_t)m * d * cmcc], q.B.data(), sizeof(double) * d * cmcc);
+            if (cm) memcpy(&B[(size_t)m * d * cm], q.B.data(), sizeof(double) * d * cm);
         }
         std::vector<int> e(n);
         const int st = mce_batch_step(slots[j], z.data(), Phi.data(), Gam.data(), beta.data(), H.data(), gam.data(),
-                                      cmcc ? B.data() : nullptr, cmcc ? u.data() : nullptr, 0, e.data());
+                                      cm ? B.data() : nullptr, cm ? u.data() : nullptr, 0, e.data());
         if (st < 0) return st;
         for (int m = 0; m < n_mgr; m++) err[(size_t)j * n_mgr + m] = e[m];
         return MCE_OK;
@@ -372,9 +388,53 @@ struct mce_swm {
         q.c.step = step;
         cb(&q.c);
     }
+
+    // Extended-mode dynamics callback of a window: propagates its x_bar.
+    int ext_propagate(Duc& q, int step)
+    {
+        q.c.is_xbar_set_for_ece = false;
+        q.c.step = step;
+        cb(&q.c);
+        if (!q.c.is_xbar_set_for_ece) {
+            mce::report_error("mce_swm_step: the dynamics callback did not set is_xbar_set_for_ece "
+                              "(the reference asserts it, cauchy_windows.hpp:488)");
+            return MCE_ERR_ARG;
+        }
+        return MCE_OK;
+    }
+
+    // Extended-mode update of window slot j with measurement index i of every
+    // manager; save_xbar: the window reports the x_bar it starts this update
+    // from (cauchy_windows.hpp:524 and :645).
+    int ext_update(int j, int i, const double* msmts, bool save_xbar)
+    {
+        std::vector<double> z(n_mgr), zbar(p);
+        for (int m = 0; m < n_mgr; m++) {
+            Duc& q = wduc[(size_t)j * n_mgr + m];
+            if (save_xbar) memcpy(&xbar_win[((size_t)j * n_mgr + m) * d], q.x.data(), sizeof(double) * d);
+            msmt_cb(&q.c, zbar.data());
+            z[m] = msmts[(size_t)m * p + i] - zbar[i];
+            ext_cb(&q.c);
+        }
+        int st = step_slot(j, i, msmts, z.data());
+        if (st < 0) return st;
+        for (int m = 0; m < n_mgr; m++) {
+            st = mce_finalize_extended_moments(slots[j], m, wduc[(size_t)j * n_mgr + m].x.data());
+            if (st < 0) return st;
+        }
+        return MCE_OK;
+    }
 };
 
 extern "C" {
+
+static mce_swm* swm_make(int n_mgr, int num_windows, int num_sim_steps, int d, int cmcc, int pncc, int p,
+                         const double* x0, const double* A0, const double* p0, const double* b0, const double* Phi,
+                         const double* Gamma, const double* B, const double* beta, const double* H,
+                         const double* gamma, double dt, int init_step, mce_dynamics_callback dyn_cb,
+                         mce_msmt_model_callback msmt_cb, mce_dynamics_callback ext_cb,
+                         const double* win_var_boost, const double* root_point, const double* b_pert,
+                         int bpert_stride, int* status);
 
 mce_swm* mce_swm_create(int n_mgr, int num_windows, int num_sim_steps, int d, int cmcc, int pncc, int p,
                         const double* A0, const double* p0, const double* b0, const double* Phi,
@@ -383,13 +443,48 @@ mce_swm* mce_swm_create(int n_mgr, int num_windows, int num_sim_steps, int d, in
                         const double* win_var_boost, const double* root_point, const double* b_pert,
                         int bpert_stride, int* status)
 {
+    if (!H || (!Phi && !dyn_cb)) {
+        mce::report_error("mce_swm_create: invalid arguments");
+        if (status) *status = MCE_ERR_ARG;
+        return nullptr;
+    }
+    return swm_make(n_mgr, num_windows, num_sim_steps, d, cmcc, pncc, p, nullptr, A0, p0, b0, Phi, Gamma, B, beta, H,
+                    gamma, dt, init_step, dyn_cb, nullptr, nullptr, win_var_boost, root_point, b_pert, bpert_stride,
+                    status);
+}
+
+mce_swm* mce_swm_create_nonlin(int n_mgr, int num_windows, int num_sim_steps, int d, int cmcc, int pncc, int p,
+                               const double* x0, const double* A0, const double* p0, const double* b0,
+                               const double* beta, const double* gamma, double dt, int init_step,
+                               mce_dynamics_callback dyn_cb, mce_msmt_model_callback msmt_cb,
+                               mce_dynamics_callback ext_cb, const double* win_var_boost, const double* root_point,
+                               const double* b_pert, int bpert_stride, int* status)
+{
+    if (!x0 || !dyn_cb || !msmt_cb || !ext_cb) {
+        mce::report_error("mce_swm_create_nonlin: x0 and the three callbacks are required (cauchy_windows.hpp:866-884)");
+        if (status) *status = MCE_ERR_ARG;
+        return nullptr;
+    }
+    return swm_make(n_mgr, num_windows, num_sim_steps, d, cmcc, pncc, p, x0, A0, p0, b0, nullptr, nullptr, nullptr,
+                    beta, nullptr, gamma, dt, init_step, dyn_cb, msmt_cb, ext_cb, win_var_boost, root_point, b_pert,
+                    bpert_stride, status);
+}
+
+static mce_swm* swm_make(int n_mgr, int num_windows, int num_sim_steps, int d, int cmcc, int pncc, int p,
+                         const double* x0, const double* A0, const double* p0, const double* b0, const double* Phi,
+                         const double* Gamma, const double* B, const double* beta, const double* H,
+                         const double* gamma, double dt, int init_step, mce_dynamics_callback dyn_cb,
+                         mce_msmt_model_callback msmt_cb, mce_dynamics_callback ext_cb,
+                         const double* win_var_boost, const double* root_point, const double* b_pert,
+                         int bpert_stride, int* status)
+{
     auto fail = [status](int st, const char* msg) -> mce_swm* {
         mce::report_error(msg);
         if (status) *status = st;
         return nullptr;
     };
     if (n_mgr < 1 || num_windows < 2 || num_sim_steps < 1 || d < 2 || p < 1 || pncc < 0 || cmcc < 0 || !A0 ||
-        !p0 || !b0 || !H || !gamma || (!Phi && !dyn_cb))
+        !p0 || !b0 || !gamma)
         return fail(MCE_ERR_ARG, "mce_swm_create: invalid arguments");
     if (init_step != 0 && init_step != 1)
         return fail(MCE_ERR_ARG, "mce_swm_create: the initial step must be 0 or 1 (cauchy_windows.hpp:871)");
@@ -406,6 +501,10 @@ mce_swm* mce_swm_create(int n_mgr, int num_windows, int num_sim_steps, int d, in
     s->dt = dt;
     s->init_step = init_step;
     s->cb = dyn_cb;
+    s->ext = msmt_cb != nullptr;
+    s->msmt_cb = msmt_cb;
+    s->ext_cb = ext_cb;
+    s->est_cmcc = s->ext ? 0 : cmcc;
     if (win_var_boost) s->boost.assign(win_var_boost, win_var_boost + d);
     s->u.assign((size_t)n_mgr * std::max(cmcc, 1), 0.0);
     s->win_count.assign(num_windows, 0);
@@ -419,6 +518,15 @@ mce_swm* mce_swm_create(int n_mgr, int num_windows, int num_sim_steps, int d, in
         s->init_duc(s->mduc[m], m, Phi, Gamma, B, beta, H, gamma);
         for (int j = 0; j < num_windows; j++)
             s->init_duc(s->wduc[(size_t)j * n_mgr + m], m, Phi, Gamma, B, beta, H, gamma);
+    }
+    if (s->ext) {
+        // every window process starts from a copy of the manager's container, x = x_bar_0
+        s->xbar_win.assign((size_t)num_windows * n_mgr * d, 0.0);
+        for (int m = 0; m < n_mgr; m++) {
+            memcpy(s->mduc[m].x.data(), x0 + (size_t)m * d, sizeof(double) * d);
+            for (int j = 0; j < num_windows; j++)
+                memcpy(s->wduc[(size_t)j * n_mgr + m].x.data(), x0 + (size_t)m * d, sizeof(double) * d);
+        }
     }
     // every window process of the reference constructs its estimator after the
     // fork, from the same rand() state: one set of constants per manager,
@@ -441,8 +549,8 @@ mce_swm* mce_swm_create(int n_mgr, int num_windows, int num_sim_steps, int d, in
     s->slots.assign(num_windows, nullptr);
     for (int j = 0; j < num_windows; j++) {
         int st = MCE_OK;
-        s->slots[j] = mce_batch_create(n_mgr, d, cmcc, pncc, p, steps.data(), A0, p0, b0, rp.data(), bp.data(), stride,
-                                       &st);
+        s->slots[j] = mce_batch_create(n_mgr, d, s->est_cmcc, pncc, p, steps.data(), A0, p0, b0, rp.data(), bp.data(),
+                                       stride, &st);
         if (!s->slots[j]) {
             if (status) *status = st;
             return nullptr;
@@ -471,19 +579,27 @@ int mce_swm_step(mce_swm* s, const double* msmts, const double* controls, double
     // windows that keep going take the step's p measurements
     std::vector<char> active(W, 0);
     std::vector<double> xr(d);
+    const bool first_loop = mc < W;
     for (int j = 0; j < W; j++) {
         if (j == initializee || (mc < W && j > mc)) continue;
         active[j] = 1;
         s->win_count[j] += 1;
         if (s->cb && s->win_count[j] != 1) {
             for (int m = 0; m < nm; m++) {
+                if (s->ext) {
+                    // x_bar already equals Re(mean): finalising the last update set it
+                    const int st = s->ext_propagate(s->wduc[(size_t)j * nm + m], step_k);
+                    if (st < 0) return st;
+                    continue;
+                }
                 const double* mu = &s->mean[2 * d * ((size_t)j * nm + m)];
                 for (int i = 0; i < d; i++) xr[i] = mu[2 * i];
                 s->call_cb(s->wduc[(size_t)j * nm + m], xr.data(), step_k);
             }
         }
         for (int i = 0; i < p; i++) {
-            const int st = s->step_slot(j, i, msmts);
+            const int st = s->ext ? s->ext_update(j, i, msmts, i == p - 1 && (first_loop || s->win_count[j] == W))
+                                  : s->step_slot(j, i, msmts);
             if (st < 0) return st;
         }
         const int st = s->read_moments(j);
@@ -530,7 +646,36 @@ int mce_swm_step(mce_swm* s, const double* msmts, const double* controls, double
         if (err_code) err_code[m] = s->err[w];
     }
     // restart the initializee about each manager's best estimate
-    if (initializee >= 0) {
+    if (initializee >= 0 && s->ext) {
+        const int j = initializee;
+        std::vector<double> Pr((size_t)d * d), A0((size_t)d * d), p0(d), b0(d), xb(d), zbar(p);
+        for (int m = 0; m < nm; m++) {
+            const size_t w = (size_t)best[m] * nm + m;
+            memcpy(xb.data(), &s->xbar_win[w * d], sizeof(double) * d);
+            for (int i = 0; i < d; i++) xr[i] = s->mean[2 * d * w + 2 * i] - xb[i];  // dx
+            for (int i = 0; i < d * d; i++) Pr[i] = s->cov[2 * (size_t)d * d * w + 2 * i];
+            mce_swm::Duc& q = s->mduc[m];
+            memcpy(q.x.data(), xb.data(), sizeof(double) * d);
+            q.c.step = step_k;
+            s->ext_cb(&q.c);
+            s->msmt_cb(&q.c, zbar.data());
+            const double dz = msmts[(size_t)m * p + p - 1] - zbar[p - 1];
+            mce_speyers_window_init(d, xr.data(), Pr.data(), q.H.data() + (size_t)(p - 1) * d, q.gamma[p - 1], dz,
+                                    s->boost.empty() ? nullptr : s->boost.data(), A0.data(), p0.data(), b0.data());
+            int st = mce_reinitialize_start_statistics(s->slots[j], m, A0.data(), p0.data(), b0.data());
+            if (st < 0) return st;
+            mce_swm::Duc& wq = s->wduc[(size_t)j * nm + m];
+            memcpy(wq.x.data(), xb.data(), sizeof(double) * d);
+            wq.c.step = step_k;
+        }
+        s->win_count[j] = 1;
+        int st = s->ext_update(j, p - 1, msmts, first_loop);
+        if (st < 0) return st;
+        st = mce_set_master_step(s->slots[j], p);
+        if (st < 0) return st;
+        st = s->read_moments(j);
+        if (st < 0) return st;
+    } else if (initializee >= 0) {
         const int j = initializee;
         std::vector<double> Pr((size_t)d * d), A0((size_t)d * d), p0(d), b0(d);
         for (int m = 0; m < nm; m++) {

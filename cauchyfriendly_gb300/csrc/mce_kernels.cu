@@ -27,6 +27,7 @@ thread_local long long g_launches = 0;
 namespace {
 constexpr int kTuneCands[4] = {64, 128, 256, 512};
 constexpr int kTuneSamples = 2;
+constexpr long long kTuneMinItems = 1LL << 15;  // smaller launches keep the default size
 struct TuneEntry {
     int device, kernel, D, MC, bucket;
     int next = 0;  // next measurement: candidate index * kTuneSamples + sample
@@ -88,7 +89,7 @@ TuneLaunch tune_begin(int kernel, int D, int MC, long long items, int def_block,
         const char* v = getenv("MCE_AUTOTUNE");
         g_tune_enabled = (v && v[0] == '0') ? 0 : 1;
     }
-    if (!g_tune_enabled || items <= 0) return t;
+    if (!g_tune_enabled || items < kTuneMinItems) return t;
     int bucket = 0;
     while (bucket < 62 && (1LL << (bucket + 1)) <= items) bucket++;
     int device = 0;

@@ -26,7 +26,8 @@ struct LaunchCfg {
 // (kernel, state dimension, hyperplane capacity, log2 of the item count); the
 // first launches of a key try 64, 128, 256 and 512 threads, each twice, timed
 // with CUDA events on the launch's stream, and later launches take the
-// fastest.  MCE_AUTOTUNE=0 in the environment keeps the fixed sizes.
+// fastest.  Launches of fewer than 2^15 items keep the default size.
+// MCE_AUTOTUNE=0 in the environment keeps the fixed sizes.
 enum TuneKernel {
     TK_TP = 0,
     TK_BUILD_B_VERTICES,

@@ -15,15 +15,13 @@ Covered:
 * window restarts: pycauchy_get_reinitialization_statistics,
   pycauchy_speyers_window_init (Speyer's statistics, computed by the
   library's C++ with the reference's eigen-solver);
-* the C++ window manager: pycauchy_initialize_lti_window_manager / _ltv_,
-  pycauchy_step (8-tuple), pycauchy_shutdown -- one manager per process, as
-  the reference's globals allow;
+* the C++ window manager: pycauchy_initialize_lti_window_manager / _ltv_ /
+  _nonlin_, pycauchy_step (8-tuple), pycauchy_shutdown -- one manager per
+  process, as the reference's globals allow;
 * pdf grids: pycauchy_get_marginal_1D/2D_pointwise_cpdf, _get_1D/2D_;
   the relative system: pycauchy_single_step_eval_2d_rsys_cpdf;
 * pycauchy_set_tr_search_idxs_ordering (accepted, no effect: see its
   docstring).
-Not provided: pycauchy_initialize_nonlin_window_manager (the extended-mode
-window manager).
 """
 from __future__ import annotations
 
@@ -391,6 +389,27 @@ def pycauchy_initialize_ltv_window_manager(num_windows, num_sim_steps, A0, p0, b
     their own copy of the dynamics container."""
     _init_window_manager(num_windows, num_sim_steps, A0, p0, b0, Phi, Gamma, B, beta, H, gamma, dt, init_step,
                          win_var_boost, int(f_dyn_update_callback))
+
+
+def pycauchy_initialize_nonlin_window_manager(num_windows, num_sim_steps, x0, A0, p0, b0, beta, gamma,
+                                              f_dyn_update_callback, f_nonlinear_msmt_model,
+                                              f_extended_msmt_update_callback, cmcc, debug_print, log_seq, log_full,
+                                              log_dir, dt, init_step, win_var_boost):
+    """pycauchy.hpp:152-184: the C++ SlidingWindowManager in extended mode,
+    x0 = x_bar_0 and the three callbacks raw C function pointers (ints).  The
+    window estimators take no controls; the callbacks see cmcc controls."""
+    global _SWM
+    from .windows import CppSlidingWindowManager
+    n = int(np.asarray(b0).size)
+    if _SWM is not None:
+        _SWM.close()
+    f = lambda a: None if a is None or np.asarray(a).size == 0 else np.asarray(a, dtype=np.float64).reshape(1, -1)
+    wvb = None if win_var_boost is None or np.asarray(win_var_boost).size == 0 else win_var_boost
+    _SWM = CppSlidingWindowManager(num_windows, num_sim_steps, np.asarray(A0, dtype=np.float64).reshape(1, n, n),
+                                   f(p0), f(b0), None, None, None, f(beta), None, f(gamma), dt=float(dt),
+                                   init_step=int(init_step), dyn_callback=int(f_dyn_update_callback),
+                                   win_var_boost=wvb, x0=f(x0), msmt_model_callback=int(f_nonlinear_msmt_model),
+                                   extended_update_callback=int(f_extended_msmt_update_callback), cmcc=int(cmcc))
 
 
 def pycauchy_step(msmts, controls):

@@ -264,12 +264,16 @@ class CppSlidingWindowManager:
     Phi (n_mgr, d, d), Gamma (n_mgr, d, pncc), B (n_mgr, d, cmcc), beta
     (n_mgr, pncc), H (n_mgr, p, d), gamma (n_mgr, p)).  dyn_callback is a raw C
     function pointer (int) taking the reference's CauchyDynamicsUpdateContainer,
-    or None (LTI).  step(msmts (n_mgr, p), controls) returns, per manager, the
+    or None (LTI).  With msmt_model_callback and extended_update_callback
+    (raw C function pointers too) and x0 (n_mgr, d) the manager runs in
+    extended (nonlinear) mode; Phi, Gamma, B and H may then be None (the
+    callbacks set them) and cmcc gives the controls the callbacks see.  step(msmts (n_mgr, p), controls) returns, per manager, the
     pycauchy_step tuple (fz, xhat, Phat, cerr_fz, cerr_xhat, cerr_Phat,
     win_idx, err_code)."""
 
     def __init__(self, num_windows, num_sim_steps, A0, p0, b0, Phi, Gamma, B, beta, H, gamma, dt=0.0, init_step=0,
-                 dyn_callback=None, win_var_boost=None, root_point=None, b_pert=None):
+                 dyn_callback=None, win_var_boost=None, root_point=None, b_pert=None, x0=None,
+                 msmt_model_callback=None, extended_update_callback=None, cmcc=None):
         from . import _lib
         self._L = _lib.load()
         A0 = np.ascontiguousarray(np.asarray(A0, dtype=np.float64))
@@ -280,6 +284,8 @@ class CppSlidingWindowManager:
         self.pncc = 0 if self._keep[6] is None else self._keep[6].shape[1]
         self.p = self._keep[8].shape[1]
         self.cmcc = 0 if self._keep[5] is None else self._keep[5].shape[1] // self.d
+        if cmcc is not None:
+            self.cmcc = int(cmcc)
         boost = None if win_var_boost is None or np.asarray(win_var_boost).size == 0 else \
             np.ascontiguousarray(np.asarray(win_var_boost, dtype=np.float64).reshape(self.d))
         rp = None if root_point is None else np.ascontiguousarray(np.asarray(root_point, dtype=np.float64))
@@ -287,10 +293,21 @@ class CppSlidingWindowManager:
         stride = 0 if bp is None else bp.reshape(self.n_mgr, -1).shape[1]
         self._boost = boost
         st = ctypes.c_int(0)
-        self._h = self._L.mce_swm_create(self.n_mgr, int(num_windows), int(num_sim_steps), self.d, self.cmcc,
-                                         self.pncc, self.p, *[_lib.dp(x) for x in self._keep], float(dt),
-                                         int(init_step), None if dyn_callback is None else int(dyn_callback),
-                                         _lib.dp(boost), _lib.dp(rp), _lib.dp(bp), stride, ctypes.byref(st))
+        cb = lambda c: None if c is None else int(c)
+        if msmt_model_callback is not None:
+            # extended (nonlinear) mode: x0 is x_bar at the first step
+            self._x0 = f(x0)
+            k = self._keep
+            self._h = self._L.mce_swm_create_nonlin(
+                self.n_mgr, int(num_windows), int(num_sim_steps), self.d, self.cmcc, self.pncc, self.p,
+                _lib.dp(self._x0), _lib.dp(k[0]), _lib.dp(k[1]), _lib.dp(k[2]), _lib.dp(k[6]), _lib.dp(k[8]),
+                float(dt), int(init_step), cb(dyn_callback), cb(msmt_model_callback), cb(extended_update_callback),
+                _lib.dp(boost), _lib.dp(rp), _lib.dp(bp), stride, ctypes.byref(st))
+        else:
+            self._h = self._L.mce_swm_create(self.n_mgr, int(num_windows), int(num_sim_steps), self.d, self.cmcc,
+                                             self.pncc, self.p, *[_lib.dp(x) for x in self._keep], float(dt),
+                                             int(init_step), cb(dyn_callback), _lib.dp(boost), _lib.dp(rp),
+                                             _lib.dp(bp), stride, ctypes.byref(st))
         if not self._h:
             raise _lib.MceError("mce_swm_create failed (%d): %s" % (st.value, _lib.last_error()))
         self.W = int(num_windows)

@@ -22,7 +22,7 @@ import numpy as np
 
 __all__ = [
     "simulate", "three_state_lti", "random_stable", "batched_three_state",
-    "four_state_lti", "two_state_lti", "five_state_two_msmt",
+    "four_state_lti", "two_state_lti", "five_state_two_msmt", "nonlin_three_state", "nonlin_callbacks",
 ]
 
 
@@ -202,3 +202,89 @@ def many_gamma(d, pncc, steps, seed=0):
     prob = _base(d, pncc, 1, Phi, Gamma, [0.05] * pncc, H, [0.2], [0.1] * d, steps)
     prob["msmts"] = simulate(prob, rng)
     return prob
+
+
+# -- a nonlinear (extended-mode) problem ---------------------------------------
+# x = (angle, rate, drive); dt = 0.1
+#   f(x) = (x0 + dt x1, x1 + dt (-0.5 sin x0 - 0.2 x1 + x2), 0.9 x2) + Gamma w,
+#   Gamma = (0.05, 0.1, 1)
+#   h(x) = (x0 + sqrt(1 + x0^2) - 1, x1 + 0.2 sin x2) + v
+NONLIN_DT = 0.1
+NONLIN_GAMMA = np.array([[0.05], [0.1], [1.0]])
+NONLIN_BETA = np.array([0.1])
+NONLIN_MSMT_GAMMA = np.array([0.2, 0.15])
+
+
+def nonlin_f(x):
+    dt = NONLIN_DT
+    return np.array([x[0] + dt * x[1], x[1] + dt * (-0.5 * np.sin(x[0]) - 0.2 * x[1] + x[2]), 0.9 * x[2]])
+
+
+def nonlin_F(x):
+    """Jacobian of nonlin_f."""
+    dt = NONLIN_DT
+    return np.array([[1.0, dt, 0.0], [-0.5 * dt * np.cos(x[0]), 1.0 - 0.2 * dt, dt], [0.0, 0.0, 0.9]])
+
+
+def nonlin_h(x):
+    return np.array([x[0] + np.sqrt(1.0 + x[0] * x[0]) - 1.0, x[1] + 0.2 * np.sin(x[2])])
+
+
+def nonlin_Hj(x):
+    """Jacobian of nonlin_h."""
+    return np.array([[1.0 + x[0] / np.sqrt(1.0 + x[0] * x[0]), 0.0, 0.0], [0.0, 1.0, 0.2 * np.cos(x[2])]])
+
+
+def nonlin_three_state(seed=0, steps=10):
+    """The extended-mode problem above: x_bar_0 = (0.3, -0.2, 0.1), A0 = I,
+    p0 = (0.1, 0.08, 0.05), b0 = 0, beta = 0.1, gamma = (0.2, 0.15); the
+    truth starts at x_bar_0 plus Cauchy(p0) noise."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    x0 = np.array([0.3, -0.2, 0.1])
+    prob = {"d": 3, "pncc": 1, "cmcc": 0, "p": 2, "steps": steps, "x0": x0, "A0": np.eye(3),
+            "p0": np.array([0.1, 0.08, 0.05]), "b0": np.zeros(3), "beta": NONLIN_BETA.copy(),
+            "gamma": NONLIN_MSMT_GAMMA.copy(), "Gamma": NONLIN_GAMMA.copy()}
+    x = x0 + _cauchy(rng, prob["p0"], 3)
+    zs = np.zeros((steps, 2))
+    for k in range(steps):
+        if k > 0:
+            x = nonlin_f(x) + NONLIN_GAMMA[:, 0] * _cauchy(rng, NONLIN_BETA[0])
+        zs[k] = nonlin_h(x) + _cauchy(rng, NONLIN_MSMT_GAMMA, 2)
+    prob["msmts"] = zs
+    return prob
+
+
+def nonlin_callbacks():
+    """The problem's three extended-mode callbacks as Python functions over a
+    pointer to the dynamics container (ctypes; any Structure with the
+    reference's CauchyDynamicsUpdateContainer field names):
+    dynamics (x <- f(x), Phi = F(x), Gamma, beta, is_xbar_set_for_ece),
+    measurement model (zbar = h(x)) and extended update (H = dh/dx, gamma)."""
+
+    def dyn(duc_ptr):
+        c = duc_ptr.contents
+        x = np.array([c.x[i] for i in range(3)])
+        F = nonlin_F(x).reshape(-1)
+        xn = nonlin_f(x)
+        for i in range(3):
+            c.x[i] = float(xn[i])
+        for i in range(9):
+            c.Phi[i] = float(F[i])
+        for i in range(3):
+            c.Gamma[i] = float(NONLIN_GAMMA[i, 0])
+        c.beta[0] = float(NONLIN_BETA[0])
+        c.is_xbar_set_for_ece = True
+
+    def msmt(duc_ptr, zbar_ptr):
+        c = duc_ptr.contents
+        z = nonlin_h(np.array([c.x[i] for i in range(3)]))
+        zbar_ptr[0], zbar_ptr[1] = float(z[0]), float(z[1])
+
+    def ext(duc_ptr):
+        c = duc_ptr.contents
+        H = nonlin_Hj(np.array([c.x[i] for i in range(3)])).reshape(-1)
+        for i in range(6):
+            c.H[i] = float(H[i])
+        c.gamma[0], c.gamma[1] = float(NONLIN_MSMT_GAMMA[0]), float(NONLIN_MSMT_GAMMA[1])
+
+    return dyn, msmt, ext

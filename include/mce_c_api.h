@@ -260,6 +260,8 @@ typedef struct mce_dynamics_container {
     void* other_stuff;
 } mce_dynamics_container;
 typedef void (*mce_dynamics_callback)(mce_dynamics_container*);
+/* The nonlinear measurement model of extended mode: zbar[p] = h(c->x). */
+typedef void (*mce_msmt_model_callback)(mce_dynamics_container*, double* zbar);
 
 /* Sliding-window manager of the C++ front end: SlidingWindowManager(num_windows,
  * num_sim_steps, A0, p0, b0, duc, ..., dyn_cb, ..., win_var_boost, ...)
@@ -273,7 +275,7 @@ typedef void (*mce_dynamics_callback)(mce_dynamics_container*);
  * root_point[n_mgr*d] / b_pert[n_mgr*bpert_stride] (or both NULL: drawn with
  * rand()) are shared by a manager's windows, as the reference's forked windows
  * share the rand() state they inherit.  Logging options of the reference have
- * no counterpart; the extended (nonlinear) manager is not provided. */
+ * no counterpart. */
 typedef struct mce_swm mce_swm;
 mce_swm* mce_swm_create(int n_mgr, int num_windows, int num_sim_steps, int d, int cmcc, int pncc, int p,
                         const double* A0, const double* p0, const double* b0, const double* Phi,
@@ -281,6 +283,23 @@ mce_swm* mce_swm_create(int n_mgr, int num_windows, int num_sim_steps, int d, in
                         const double* gamma, double dt, int init_step, mce_dynamics_callback dyn_cb,
                         const double* win_var_boost, const double* root_point, const double* b_pert,
                         int bpert_stride, int* status);
+/* The extended (nonlinear) manager: SlidingWindowManager with is_extended
+ * (include/cauchy_windows.hpp:814-1022 with the three callbacks), as
+ * pycauchy_initialize_nonlin_window_manager makes it
+ * (scripts/swig/cauchy/pycauchy.hpp:152-184).  x0[n_mgr*d] is x_bar at the
+ * first step; dyn_cb propagates c->x (x_hat -> x_bar) and sets Phi, Gamma,
+ * beta and is_xbar_set_for_ece; msmt_cb gives z_bar = h(c->x); ext_cb sets H
+ * and gamma at c->x.  The window estimators take no controls (controls reach
+ * the callbacks through c->u).  Each window's update: z_bar and H at its
+ * x_bar, the estimator steps on z - z_bar, finalize_extended_moments moves
+ * x_bar to the estimate; restarts use Speyer's statistics of x_hat - x_bar
+ * and z - h(x_bar) about the best window's reported x_bar. */
+mce_swm* mce_swm_create_nonlin(int n_mgr, int num_windows, int num_sim_steps, int d, int cmcc, int pncc, int p,
+                               const double* x0, const double* A0, const double* p0, const double* b0,
+                               const double* beta, const double* gamma, double dt, int init_step,
+                               mce_dynamics_callback dyn_cb, mce_msmt_model_callback msmt_cb,
+                               mce_dynamics_callback ext_cb, const double* win_var_boost, const double* root_point,
+                               const double* b_pert, int bpert_stride, int* status);
 /* SlidingWindowManager::step + the read-out pycauchy_step returns
  * (scripts/swig/cauchy/pycauchy.hpp:187-221), per manager (each output may be
  * NULL): fz[n_mgr], xhat[n_mgr*d], Phat[n_mgr*d*d], cerr_fz, cerr_xhat,

@@ -58,8 +58,42 @@ def _refresh_reference_copy():
         shutil.copytree(inc, dst_inc, dirs_exist_ok=True)
         if os.path.exists(glue):
             shutil.copy2(glue, dst_glue)
+        # the reference's Python API, for the tests that run it over the drop-in
+        api = os.path.join(REFERENCE_ROOT, "scripts", "swig", "cauchy", "cauchy_estimator.py")
+        if os.path.exists(api):
+            shutil.copy2(api, dst_glue)
     own = os.path.join(REF_SRC, "include")
     return own if os.path.isdir(own) else None
+
+
+def reference_python_api(pycauchy_module, name="reference_cauchy_estimator"):
+    """The reference's Python API (scripts/swig/cauchy/cauchy_estimator.py,
+    from the copy in oracle/_ref/src, unmodified) imported with ``pycauchy``
+    bound to pycauchy_module and a stand-in for matplotlib (plotting is not
+    used).  None when no copy exists."""
+    import importlib.util
+    import sys
+    import types
+    path = os.path.join(REF_SRC, "scripts", "swig", "cauchy", "cauchy_estimator.py")
+    if not os.path.exists(path):
+        return None
+    mpl = types.ModuleType("matplotlib")
+    plt = types.ModuleType("matplotlib.pyplot")
+    mpl.pyplot = plt
+    sys.modules.setdefault("matplotlib", mpl)
+    sys.modules.setdefault("matplotlib.pyplot", plt)
+    saved = sys.modules.get("pycauchy")
+    sys.modules["pycauchy"] = pycauchy_module
+    try:
+        spec = importlib.util.spec_from_file_location(name, path)
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+    finally:
+        if saved is None:
+            sys.modules.pop("pycauchy", None)
+        else:
+            sys.modules["pycauchy"] = saved
+    return mod
 
 
 def host_cpus_pow2():

@@ -158,4 +158,50 @@ void refpy_step(double* msmts, int nm, double* controls, int nc, double* fz, dou
 
 void refpy_shutdown_window_manager(void) { pycauchy_shutdown(); }
 
+typedef void (*msmt_cb_t)(CauchyDynamicsUpdateContainer*, double*);
+
+// Extended (nonlinear) mode
+void* refpy_initialize_nonlin(int num_steps, double* x0, int nx0, double* A0, int nA0, double* p0, int np0,
+                              double* b0, int nb0, double* beta, int nbeta, double* gamma, int ngamma, void* f_dyn,
+                              void* f_msmt, void* f_ext, int cmcc, double dt, int init_step, int debug_print)
+{
+    return pycauchy_initialize_nonlin(num_steps, x0, nx0, A0, nA0, p0, np0, b0, nb0, beta, nbeta, gamma, ngamma,
+                                      (dyn_cb_t)f_dyn, (msmt_cb_t)f_msmt, (dyn_cb_t)f_ext, cmcc, dt, init_step,
+                                      debug_print != 0);
+}
+
+// out[15] receive Phi, Gamma, B, H, beta, gamma, fz, xhat, Phat, xbar, zbar,
+// cerr_fz, cerr_xhat, cerr_Phat (doubles) and err_code (ints, out[14]);
+// sizes[15] their lengths.
+void refpy_single_step_nonlin(void* h, double* msmts, int nm, double* controls, int nc, int with_propagate,
+                              void** out, int* sizes)
+{
+    double* o[14];
+    int* e;
+    int s[15];
+    pycauchy_single_step_nonlin(h, msmts, nm, controls, nc, with_propagate != 0, &o[0], &s[0], &o[1], &s[1], &o[2],
+                                &s[2], &o[3], &s[3], &o[4], &s[4], &o[5], &s[5], &o[6], &s[6], &o[7], &s[7], &o[8],
+                                &s[8], &o[9], &s[9], &o[10], &s[10], &o[11], &s[11], &o[12], &s[12], &o[13], &s[13],
+                                &e, &s[14]);
+    for (int i = 0; i < 14; i++) {
+        sizes[i] = s[i];
+        take((double*)out[i], o[i], s[i]);
+    }
+    sizes[14] = s[14];
+    if (out[14] && s[14] > 0) memcpy(out[14], e, s[14] * sizeof(int));
+    free(e);
+}
+
+void refpy_initialize_nonlin_window_manager(int num_windows, int num_sim_steps, double* x0, int nx0, double* A0,
+                                            int nA0, double* p0, int np0, double* b0, int nb0, double* beta,
+                                            int nbeta, double* gamma, int ngamma, void* f_dyn, void* f_msmt,
+                                            void* f_ext, int cmcc, int debug_print, double dt, int init_step,
+                                            double* wvb, int nwvb)
+{
+    pycauchy_initialize_nonlin_window_manager(num_windows, num_sim_steps, x0, nx0, A0, nA0, p0, np0, b0, nb0, beta,
+                                              nbeta, gamma, ngamma, (dyn_cb_t)f_dyn, (msmt_cb_t)f_msmt,
+                                              (dyn_cb_t)f_ext, cmcc, debug_print != 0, false, false, NULL, dt,
+                                              init_step, wvb, nwvb);
+}
+
 }  // extern "C"

@@ -4,9 +4,10 @@ scripts/swig/cauchy/pycauchy.hpp, compiled unmodified; SWIG is absent here).
 
 Same function names, argument order and return tuples as the SWIG wrappers
 (numpy.i IN_ARRAY1 inputs, ARGOUTVIEWM_ARRAY1 outputs), for the functions the
-reference's scripts/swig/cauchy/cauchy_estimator.py calls on the LTI/LTV paths:
-single-estimator stepping, reset, reinitialisation statistics, Speyer's
-restart, the search-axis ordering and the C++ window manager.  Importing the
+reference's scripts/swig/cauchy/cauchy_estimator.py calls on the LTI, LTV and
+nonlinear paths: single-estimator stepping, reset, reinitialisation
+statistics, Speyer's restart, the search-axis ordering and the C++ window
+manager.  Importing the
 reference's cauchy_estimator.py with this module registered as ``pycauchy``
 runs the reference's PyCauchyEstimator / PySlidingWindowManager /
 PySlidingWindowManager_CPP on the reference's C++
@@ -34,7 +35,7 @@ def lib():
         if not os.path.exists(path):
             raise RuntimeError("the reference pycauchy shim is not built (needs the reference sources)")
         _L = ct.PyDLL(path)  # holds the GIL: callbacks may run in forked window processes
-        for name in ("refpy_initialize_lti", "refpy_initialize_ltv"):
+        for name in ("refpy_initialize_lti", "refpy_initialize_ltv", "refpy_initialize_nonlin"):
             getattr(_L, name).restype = ct.c_void_p
     return _L
 
@@ -93,6 +94,28 @@ def pycauchy_single_step_ltiv(h, msmts, controls):
                                  cx.ctypes.data_as(_dp), cP.ctypes.data_as(_dp), err.ctypes.data_as(_ip))
     outs = [d[:s].copy() for d, s in zip(dyn, sizes)]
     return (*outs, fz, x, P, cfz, cx, cP, err)
+
+
+def pycauchy_initialize_nonlin(num_steps, x0, A0, p0, b0, beta, gamma, f_dyn_update_callback, f_nonlinear_msmt_model,
+                               f_extended_msmt_update_callback, cmcc, dt, init_step, debug_print):
+    arrs = [_a(x) for x in (x0, A0, p0, b0, beta, gamma)]
+    ptr = lib().refpy_initialize_nonlin(int(num_steps), *_flat_args(arrs), ct.c_void_p(int(f_dyn_update_callback)),
+                                        ct.c_void_p(int(f_nonlinear_msmt_model)),
+                                        ct.c_void_p(int(f_extended_msmt_update_callback)), int(cmcc),
+                                        ct.c_double(dt), int(init_step), int(bool(debug_print)))
+    return _RefHandle(ptr, arrs[3][1], arrs[5][1], arrs[4][1], int(cmcc), arrs)
+
+
+def pycauchy_single_step_nonlin(h, msmts, controls, with_propagate):
+    m, nm = _a(msmts)
+    c, nc = _a(controls)
+    n, pncc, cmcc = h.n, h.pncc, h.cmcc
+    dsz = [n * n, n * pncc, n * cmcc, nm * n, pncc, nm, nm, nm * n, nm * n * n, nm * n, nm, nm, nm, nm]
+    outs = [np.zeros(max(sz, 1)) for sz in dsz] + [np.zeros(max(nm, 1), dtype=np.int32)]
+    ptrs = (ct.c_void_p * 15)(*[o.ctypes.data for o in outs])
+    sizes = (ct.c_int * 15)()
+    lib().refpy_single_step_nonlin(h.ptr, _p(m), nm, _p(c), nc, int(bool(with_propagate)), ptrs, sizes)
+    return tuple(o[:sz].copy() for o, sz in zip(outs, sizes))
 
 
 def pycauchy_single_step_get_number_of_terms(h):
@@ -163,6 +186,22 @@ def pycauchy_initialize_ltv_window_manager(num_windows, num_sim_steps, A0, p0, b
     lib().refpy_initialize_ltv_window_manager(int(num_windows), int(num_sim_steps), *_flat_args(arrs[:9]),
                                               ct.c_void_p(int(f_dyn_update_callback)), int(bool(debug_print)),
                                               ct.c_double(dt), int(init_step), _p(arrs[9][0]), arrs[9][1])
+
+
+def pycauchy_initialize_nonlin_window_manager(num_windows, num_sim_steps, x0, A0, p0, b0, beta, gamma,
+                                              f_dyn_update_callback, f_nonlinear_msmt_model,
+                                              f_extended_msmt_update_callback, cmcc, debug_print, log_seq, log_full,
+                                              log_dir, dt, init_step, win_var_boost):
+    global _wm_keep
+    arrs = [_a(x) for x in (x0, A0, p0, b0, beta, gamma, win_var_boost)]
+    # pycauchy_step reads the state dimension from _wm_keep[2]
+    _wm_keep = [arrs[1], arrs[2], arrs[3]] + arrs
+    lib().refpy_initialize_nonlin_window_manager(int(num_windows), int(num_sim_steps), *_flat_args(arrs[:6]),
+                                                 ct.c_void_p(int(f_dyn_update_callback)),
+                                                 ct.c_void_p(int(f_nonlinear_msmt_model)),
+                                                 ct.c_void_p(int(f_extended_msmt_update_callback)), int(cmcc),
+                                                 int(bool(debug_print)), ct.c_double(dt), int(init_step),
+                                                 _p(arrs[6][0]), arrs[6][1])
 
 
 def pycauchy_step(msmts, controls):

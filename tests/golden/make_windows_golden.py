@@ -18,7 +18,10 @@ a stand-in for matplotlib (plotting is not used).  It then runs:
 * ``pycauchy_speyers_window_init`` on random estimates, some with a covariance
   that needs the eigenvalue boost (speyer_kats.npz);
 * ``PyCauchyEstimator`` under two term-reduction search-axis orderings
-  (``pycauchy_set_tr_search_idxs_ordering``, tr_ordering_*.npz).
+  (``pycauchy_set_tr_search_idxs_ordering``, tr_ordering_*.npz);
+* both managers in extended (nonlinear) mode on the problem and callbacks of
+  workloads.nonlin_three_state / nonlin_callbacks (win_py_nonlin_*.npz,
+  win_cpp_nonlin_*.npz).
 
 Each window fixture also stores the root point and b_pert every window's
 estimator drew from rand() (srand(seed) before the manager is made).
@@ -142,6 +145,76 @@ def cpp_manager(name, prob, W_, steps, seed, ltv=False):
     print(name, "done")
 
 
+def _nonlin_arrays(prob):
+    return {k: prob[k] for k in ("x0", "A0", "p0", "b0", "beta", "gamma", "Gamma", "msmts", "d", "pncc", "p")}
+
+
+def py_nonlin_manager(name, prob, W_, steps, seed):
+    """PySlidingWindowManager in "nonlin" mode (PyCauchyEstimator windows on
+    pycauchy_initialize_nonlin / pycauchy_single_step_nonlin, restarts with
+    x_bar) over the problem's callbacks (workloads.nonlin_callbacks)."""
+    ce, rp = _reference_api()
+    rp.srand(seed)
+    dyn, msmt, ext = W.nonlin_callbacks()
+    mgr = ce.PySlidingWindowManager("nonlin", W_, swm_debug_print=False, win_debug_print=False)
+    mgr.initialize_nonlin(prob["x0"], prob["A0"], prob["p0"], prob["b0"], prob["beta"], prob["gamma"], dyn, msmt, ext,
+                          0, W.NONLIN_DT, 0)
+    consts = [rp.get_constants(e.py_handle) for e in mgr.cauchyEsts]
+    arr = _nonlin_arrays(prob)
+    arr.update(W=W_, steps=steps, srand_seed=seed, root_point=np.stack([c[0] for c in consts]),
+               b_pert=np.stack([c[1] for c in consts]))
+    for k in range(steps):
+        xhat, Phat, wx, wP = mgr.step(prob["msmts"][k], None)
+        pre = "s%d_" % k
+        mi = mgr.moment_info
+        arr[pre + "xhat"] = np.asarray(xhat)
+        arr[pre + "Phat"] = np.asarray(Phat)
+        arr[pre + "wavg_xhat"] = np.asarray(wx)
+        arr[pre + "wavg_Phat"] = np.asarray(wP)
+        arr[pre + "win_idx"] = int(mi["win_idx"][-1])
+        arr[pre + "err_code"] = int(mi["err_code"][-1])
+        arr[pre + "fz"] = float(mi["fz"][-1])
+        arr[pre + "win_counts"] = mgr.win_counts.copy()
+        arr[pre + "nt"] = np.array([e.get_num_CF_terms() for e in mgr.cauchyEsts], dtype=np.int64)
+    mgr.shutdown()
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **arr)
+    print(name, "done")
+
+
+def cpp_nonlin_manager(name, prob, W_, steps, seed):
+    """pycauchy_initialize_nonlin_window_manager + pycauchy_step: the C++
+    SlidingWindowManager in extended mode (forked window processes running
+    the problem's callbacks)."""
+    ce, rp = _reference_api()
+    rp.srand(seed)
+    arr = _nonlin_arrays(prob)
+    arr.update(W=W_, steps=steps, srand_seed=seed)
+    f = lambda a: np.asarray(a, dtype=np.float64).reshape(-1)
+    empty = np.array([], dtype=np.float64)
+    dyn, msmt, ext = W.nonlin_callbacks()
+    t1 = ct.CFUNCTYPE(None, ct.POINTER(ce.C_CauchyDynamicsUpdateContainer))
+    t2 = ct.CFUNCTYPE(None, ct.POINTER(ce.C_CauchyDynamicsUpdateContainer), ct.POINTER(ct.c_double))
+    keep = (t1(dyn), t2(msmt), t1(ext))
+    ptr = lambda c: ct.cast(c, ct.c_void_p).value
+    rp.pycauchy_initialize_nonlin_window_manager(W_, steps, f(prob["x0"]), f(prob["A0"]), f(prob["p0"]),
+                                                 f(prob["b0"]), f(prob["beta"]), f(prob["gamma"]), ptr(keep[0]),
+                                                 ptr(keep[1]), ptr(keep[2]), 0, False, False, False, None,
+                                                 W.NONLIN_DT, 0, empty)
+    for k in range(steps):
+        fz, x, P, cfz, cx, cP, wi, err = rp.pycauchy_step(f(prob["msmts"][k]), empty)
+        pre = "s%d_" % k
+        arr[pre + "fz"] = fz
+        arr[pre + "xhat"] = x
+        arr[pre + "Phat"] = P
+        arr[pre + "cerr"] = np.array([cfz, cx, cP])
+        arr[pre + "win_idx"] = wi
+        arr[pre + "err_code"] = err
+    rp.pycauchy_shutdown()
+    del keep
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **arr)
+    print(name, "done")
+
+
 def speyer_kats():
     _, rp = _reference_api()
     rng = np.random.Generator(np.random.PCG64(77))
@@ -200,7 +273,7 @@ def tr_ordering(name, prob, seed, orderings):
 
 
 if __name__ == "__main__":
-    what = sys.argv[1:] or ["py", "cpp", "speyer", "order"]
+    what = sys.argv[1:] or ["py", "cpp", "speyer", "order", "nonlin"]
     if "py" in what:
         py_manager("win_py_four_state", W.four_state_lti(seed=0, steps=12), 4, 12, 21)
         py_manager("win_py_five_state_two_msmt", W.five_state_two_msmt(seed=1, steps=7), 3, 7, 22)
@@ -209,5 +282,8 @@ if __name__ == "__main__":
         cpp_manager("win_cpp_five_state_ltv", W.five_state_ltv_windows(seed=3, steps=7), 3, 7, 24, ltv=True)
     if "speyer" in what:
         speyer_kats()
+    if "nonlin" in what:
+        py_nonlin_manager("win_py_nonlin_three_state", W.nonlin_three_state(seed=8, steps=10), 3, 10, 26)
+        cpp_nonlin_manager("win_cpp_nonlin_three_state", W.nonlin_three_state(seed=9, steps=10), 3, 10, 27)
     if "order" in what:
         tr_ordering("tr_ordering_three_state", W.three_state_lti(seed=7, steps=9), 25, [(0, 1, 2), (2, 0, 1)])

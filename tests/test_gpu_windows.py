@@ -232,3 +232,38 @@ def test_drop_in_ignores_search_axis_ordering_like_the_reference():
         assert G.relerr(out[7], z[pre + "x"]) <= G.REL_TOL, (k, "x")
         assert G.relerr(out[8], z[pre + "P"]) <= G.REL_TOL, (k, "P")
     pycauchy.pycauchy_single_step_shutdown(h)
+
+
+def test_cpp_window_manager_nonlin_matches_reference():
+    """The C++ manager in extended mode (pycauchy_initialize_nonlin_window_manager
+    + pycauchy_step) against the reference's own extended-mode manager
+    (include/cauchy_windows.hpp with is_extended, forked window processes
+    running the same callbacks, tests/golden/win_cpp_nonlin_three_state.npz):
+    per step the chosen window and its error bits exactly, fz, estimate and
+    covariance within 1e-9 element-wise."""
+    _need_gpu()
+    import ctypes as ct
+    from cauchyfriendly_gb300 import pycauchy
+    from cauchyfriendly_gb300 import workloads as W
+    z = _load_win("win_cpp_nonlin_three_state")
+    dyn, msmt, ext = W.nonlin_callbacks()
+    C = pycauchy.C_CauchyDynamicsUpdateContainer
+    keep = (ct.CFUNCTYPE(None, ct.POINTER(C))(dyn), ct.CFUNCTYPE(None, ct.POINTER(C), ct.POINTER(ct.c_double))(msmt),
+            ct.CFUNCTYPE(None, ct.POINTER(C))(ext))
+    ptr = lambda c: ct.cast(c, ct.c_void_p).value
+    ct.CDLL(None).srand(ct.c_uint(int(z["srand_seed"])))
+    pycauchy.pycauchy_initialize_nonlin_window_manager(int(z["W"]), int(z["steps"]), z["x0"], z["A0"], z["p0"],
+                                                       z["b0"], z["beta"], z["gamma"], ptr(keep[0]), ptr(keep[1]),
+                                                       ptr(keep[2]), 0, False, False, False, None, W.NONLIN_DT, 0,
+                                                       np.array([]))
+    try:
+        for k in range(int(z["steps"])):
+            fz, x, P, cfz, cx, cP, wi, err = pycauchy.pycauchy_step(z["msmts"][k], np.array([]))
+            pre = "s%d_" % k
+            assert wi == int(z[pre + "win_idx"]) and err == int(z[pre + "err_code"]), (k, wi, err)
+            assert G.relerr([fz], [float(z[pre + "fz"])]) <= G.REL_TOL, (k, "fz")
+            assert G.relerr(x, z[pre + "xhat"]) <= G.REL_TOL, (k, "xhat", x, z[pre + "xhat"])
+            assert G.relerr(P, z[pre + "Phat"]) <= G.REL_TOL, (k, "Phat")
+    finally:
+        pycauchy.pycauchy_shutdown()
+    del keep
