@@ -298,4 +298,5 @@ def test_autotuned_block_sizes_keep_results_bit_identical():
     for k in ("fz", "mean", "cov", "err", "nt"):
         assert np.array_equal(tuned[k], fixed[k]), k
     assert table and all(r["block"] in (64, 128, 256, 512) for r in table), (sizes, table)
-    assert {r["kernel"] for r in table} >= {"tp", "build_B_vertices", "gtable_eval"}, table
+    # launches of 2^15 items or more are tuned: the per-(term, cell) evaluation always has them
+    assert "gtable_eval" in {r["kernel"] for r in table}, table
