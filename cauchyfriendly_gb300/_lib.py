@@ -21,6 +21,7 @@ HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))
 # name -> (restype, argtypes)
 SIGNATURES = {
     "mce_last_error": (ctypes.c_char_p, []),
+    "mce_set_reference_num_cpus": (ctypes.c_int, [ctypes.c_int]),
     "mce_draw_reference_constants": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                      _dp, _dp]),
     "mce_batch_create": (_vp, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _ip, _dp, _dp,

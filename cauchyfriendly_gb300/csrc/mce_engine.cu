@@ -2261,9 +2261,18 @@ extern "C" {
 
 const char* mce_last_error(void) { return g_last_error.c_str(); }
 
+static std::atomic<int> g_ref_num_cpus{8};
+
+int mce_set_reference_num_cpus(int num_cpus)
+{
+    if (num_cpus < 1) return MCE_ERR_ARG;
+    return g_ref_num_cpus.exchange(num_cpus);
+}
+
 int mce_draw_reference_constants(long long seed, int d, int max_shape, int num_cpus, double* root_point,
                                  double* b_pert)
 {
+    if (num_cpus == 0) num_cpus = g_ref_num_cpus.load();
     if (d < 1 || max_shape < 1 || num_cpus < 1 || !root_point || !b_pert) return MCE_ERR_ARG;
     if (seed >= 0) srand((unsigned)seed);
     auto u = []() { return ((double)rand() + 1.0) / ((double)RAND_MAX + 1.0); };
@@ -2297,7 +2306,7 @@ mce_handle* mce_batch_create(int n_est, int d, int cmcc, int pncc, int p, const 
         bps.assign((size_t)n_est * msmax, 0);
         for (int e = 0; e < n_est; e++) {
             const int ms = d > 1 ? (steps[e] - 1) * pncc + d : d + pncc;
-            mce_draw_reference_constants(-1, d, ms, 8, &roots[(size_t)e * d], &bps[(size_t)e * msmax]);
+            mce_draw_reference_constants(-1, d, ms, 0, &roots[(size_t)e * d], &bps[(size_t)e * msmax]);
         }
         if (root_point) memcpy(roots.data(), root_point, sizeof(double) * n_est * d);
         if (b_pert) {

@@ -538,7 +538,7 @@ static mce_swm* swm_make(int n_mgr, int num_windows, int num_sim_steps, int d, i
         rp.resize((size_t)n_mgr * d);
         bp.resize((size_t)n_mgr * ms);
         for (int m = 0; m < n_mgr; m++)
-            mce_draw_reference_constants(-1, d, ms, 8, &rp[(size_t)m * d], &bp[(size_t)m * ms]);
+            mce_draw_reference_constants(-1, d, ms, 0, &rp[(size_t)m * d], &bp[(size_t)m * ms]);
         stride = ms;
     } else {
         if (bpert_stride < ms) return fail(MCE_ERR_ARG, "mce_swm_create: b_pert stride below the window's max shape");

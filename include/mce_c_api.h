@@ -41,9 +41,17 @@ const char* mce_last_error(void);
  * (include/cauchy_estimator.hpp:127-128 root point, then num_cpus DCE helpers
  * drawing b_pert, include/cell_enumeration.hpp:467-470); helper 0's b_pert is
  * returned.  seed < 0 keeps the current rand() state (the reference never
- * seeds), otherwise srand(seed) is called first. */
+ * seeds), otherwise srand(seed) is called first.  num_cpus 0 takes the
+ * process-wide count below. */
 int mce_draw_reference_constants(long long seed, int d, int max_shape, int num_cpus, double* root_point,
                                  double* b_pert);
+/* How many DCE helpers an estimator made without explicit constants draws
+ * b_pert for: the reference's compile-time NUM_CPUS
+ * (include/cauchy_constants.hpp:69, 8 as shipped and the default here; 1 for
+ * a serial build).  It only decides how far each estimator advances rand(),
+ * so it matters when several estimators draw in turn.  Returns the previous
+ * count (MCE_ERR_ARG below 1). */
+int mce_set_reference_num_cpus(int num_cpus);
 
 /* Batch of independent estimators stepped in lock-step.  Replaces
  * CauchyEstimator::CauchyEstimator (include/cauchy_estimator.hpp:87-185) for

@@ -31,6 +31,18 @@ def _api():
     return ce
 
 
+@pytest.fixture(autouse=True)
+def _serial_reference_draws():
+    """The fixtures come from a serial build of the reference (NUM_CPUS = 1):
+    each estimator it makes advances rand() by one b_pert draw, which decides
+    the constants of every window after the first."""
+    from cauchyfriendly_gb300 import _lib
+    lib = _lib.load()
+    old = lib.mce_set_reference_num_cpus(1)
+    yield
+    lib.mce_set_reference_num_cpus(old)
+
+
 def _load(name):
     return np.load(os.path.join(G.GOLDEN, name + ".npz"))
 
