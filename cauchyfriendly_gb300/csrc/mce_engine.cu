@@ -83,7 +83,7 @@ struct DevBuf {
         cudaError_t e = cudaMalloc(&ptr, want * sizeof(T));
         if (e != cudaSuccess) {
             cudaGetLastError();
-            set_error(std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+            set_error("cudaMalloc of " + std::to_string(want * sizeof(T)) + " bytes failed: " + cudaGetErrorString(e));
             return MCE_ERR_NOMEM;
         }
         cap = want;
@@ -310,6 +310,9 @@ public:
                            int* keys, double* g) = 0;
     virtual long long total_cells(int est) = 0;
     virtual int reset() = 0;
+    // Frees the buffers that grow with the term count (only between a reset
+    // or creation and the next step); returns the bytes released.
+    virtual long long trim() = 0;
     // copies estimator e's start statistics to the device, where the next
     // first update reads them
     virtual int upload_start(int e) = 0;
@@ -774,6 +777,33 @@ public:
         device_errors = 0;
         MCE_CUDA(cudaMemset(counters.ptr, 0, 8 * sizeof(int)));
         return MCE_OK;
+    }
+
+    long long trim() override
+    {
+        if (master_step != 0) return MCE_ERR_ARG;
+        long long freed = 0;
+        auto rel = [&freed](auto& buf) {
+            freed += (long long)(buf.cap * sizeof(*buf.ptr));
+            buf.release();
+        };
+        for (auto& P : Pb) {
+            rel(P.est), rel(P.m), rel(P.m_old), rel(P.tab_cnt), rel(P.B_cnt), rel(P.nkids), rel(P.nkids_all);
+            rel(P.bflip), rel(P.A), rel(P.p), rel(P.b), rel(P.tab_off), rel(P.B_off), rel(P.kscan);
+        }
+        for (auto& T : Tb) rel(T.keys), rel(T.vals);
+        rel(Rb.est), rel(Rb.m), rel(Rb.pbc), rel(Rb.phc), rel(Rb.z), rel(Rb.lhp), rel(Rb.fam), rel(Rb.flags);
+        rel(Rb.horthog), rel(Rb.A), rel(Rb.p), rel(Rb.q), rel(Rb.b), rel(Rb.cval), rel(Rb.dval), rel(Rb.ps2);
+        rel(Rb.cmap), rel(Rb.csmap);
+        rel(Bcap), rel(Bkeys), rel(kall_scan), rel(nvert), rel(voff), rel(vsv), rel(fam_mom), rel(mu_rows);
+        rel(mu_ints), rel(bcount), rel(bfill), rel(boff), rel(slot_of), rel(cell_ent), rel(cell_ent2), rel(status);
+        rel(owner), rel(ftr_wl[0]), rel(ftr_wl[1]), rel(ftr_resume), rel(gcnt), rel(gfill), rel(goff), rel(members);
+        rel(members_tmp), rel(is_root), rel(cap), rel(rscan), rel(toff), rel(roots_list), rel(alive), rel(src);
+        rel(tcnt), rel(g_nr), rel(g_items), rel(g_cells), rel(g_ioff), rel(g_coff), rel(g_rps2), rel(g_rflag);
+        rel(g_minfo), rel(g_mps2), rel(g_mflag), rel(pr_root), rel(pr_mb), rel(pr_mcnt), rel(pr_cells);
+        rel(pr_items), rel(pr_moff), rel(pr_ioff), rel(pr_coff), rel(pr_gv), rel(g_vals), rel(new_slot);
+        rel(ptile_c), rel(pf_rows), rel(pf_zero);
+        return freed;
     }
 
     // Packs one estimator's step parameters; Gamma pre-coalignment follows
@@ -2562,6 +2592,13 @@ int mce_dump_terms(mce_handle* h, int e, int max_shape, int* shape, double* A, d
     return h->eng->dump_terms(e, max_shape, shape, A, p, b, cells, keys, g);
 }
 int mce_reset(mce_handle* h) { return h ? h->eng->reset() : MCE_ERR_ARG; }
+long long mce_trim_memory(mce_handle* h)
+{
+    if (!h) return MCE_ERR_ARG;
+    const long long r = h->eng->trim();
+    if (r < 0) set_error("mce_trim_memory: only between mce_reset (or creation) and the next step");
+    return r;
+}
 int mce_reinitialize_start_statistics(mce_handle* h, int e, const double* A0, const double* p0, const double* b0)
 {
     if (bad(h, e) || !A0 || !p0 || !b0) return MCE_ERR_ARG;

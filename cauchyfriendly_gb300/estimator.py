@@ -158,6 +158,11 @@ class BatchedCauchyEstimator:
     def reset(self):
         _lib.check(self._lib.mce_reset(self._h), "mce_reset")
 
+    def trim_memory(self):
+        """Frees the device buffers that grow with the term count (between a
+        reset and the next step); returns the bytes released."""
+        return _lib.check(self._lib.mce_trim_memory(self._h), "mce_trim_memory")
+
     def reinitialize_start_statistics(self, A0, p0, b0, e=0):
         A0, p0, b0 = _f64(A0), _f64(p0), _f64(b0)
         _lib.check(self._lib.mce_reinitialize_start_statistics(self._h, e, _p(A0), _p(p0), _p(b0)),

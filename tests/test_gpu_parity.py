@@ -300,3 +300,25 @@ def test_autotuned_block_sizes_keep_results_bit_identical():
     assert table and all(r["block"] in (64, 128, 256, 512) for r in table), (sizes, table)
     # launches of 2^15 items or more are tuned: the per-(term, cell) evaluation always has them
     assert "gtable_eval" in {r["kernel"] for r in table}, table
+
+
+def test_trim_memory_between_reset_and_step():
+    """mce_trim_memory frees the term-sized buffers after a reset (not after a
+    step), and the next run allocates them again with the same results."""
+    _, BCE = _gpu()
+    from cauchyfriendly_gb300 import workloads as W
+    import bench
+    probs = W.batched_three_state(64, seed=6, steps_lo=5, steps_hi=7)
+    rp, bp = bench.constants(probs, 6)
+    B = bench.batch_arrays(probs)
+    est = BCE(B["A0"], B["p0"], B["b0"], B["steps"], 3, 0, 1, 1, rp, bp)
+    run = lambda: est.run(B["msmts"], B["Phi"], B["Gamma"], B["beta"], B["H"], B["gamma"], shared_model=False)
+    first = run()
+    assert est._lib.mce_trim_memory(est._h) == -1  # MCE_ERR_ARG: after a step
+    est.reset()
+    assert est.trim_memory() > 0
+    assert est.trim_memory() == 0
+    second = run()
+    est.close()
+    for k in ("fz", "mean", "cov", "err", "nt"):
+        assert np.array_equal(first[k], second[k]), k
