@@ -29,10 +29,13 @@ constexpr int kFlagHasCmap = 2;
 
 // device error bits (reported through the engine's status word)
 constexpr int kErrAntiCoalignedHorthog = 1;  // cauchy_term.hpp:673-687 exits the process
-constexpr int kErrTableOverflow = 2;
+constexpr int kErrTableOverflow = 2;  // a parent's B table above its capacity
 constexpr int kErrShapeTooLarge = 4;
 constexpr int kErrResolveStalled = 8;
 constexpr int kErrDceOverflow = 16;
+constexpr int kErrRecordOverflow = 32;       // an MU record past the step's record count
+constexpr int kErrRootCellsOverflow = 64;    // a reduction root's cells above its table slot
+constexpr int kErrMemberCellsOverflow = 128;  // a promoted member's cells above its table slot
 
 struct cd {
     double re, im;

@@ -561,6 +561,7 @@ public:
     long long p_l0 = 0;
     DevBuf<double> alg;  // [KID_COUNT][2] bytes, flops
     DevBuf<unsigned> gbits;  // cell bitmaps of terms above kSmemBitmapRows hyperplanes
+    DevBuf<int> g_over;      // g-table preparation: a root above its slot, the largest count
 
     // profiling brackets on the engine's stream (or on st when given)
     void pbeg(int id, cudaStream_t st = nullptr)
@@ -670,6 +671,7 @@ public:
         int s = MCE_OK;
         // profiling counters, sized here so no later step has to allocate them
         s |= alg.ensure(2 * KID_COUNT);
+        s |= g_over.ensure(2);
         if (MC > kSmemBitmapRows) {
             // a region per warp for the bitmap kernels (8 warps per SM)
             const long long warps = (long long)lc.num_sms * 8;
@@ -1372,17 +1374,11 @@ public:
         if ((s = src.ensure(nR + 1))) return s;
         if ((s = tcnt.ensure(nR + 1))) return s;
         MCE_CUDA(cudaMemsetAsync(alive.ptr, 0, sizeof(int) * (nR + 1), lc.stream));
-        const int capMC = half_cells_cap(MC, D);
-        cd* gscr = nullptr;
-        long long gscr_warps = 0;  // 0: the handle's buffer holds a warp slot for every launched warp
-        if (fixed_gtable_scratch) {
-            gscr = static_cast<cd*>(fixed_gtable_scratch);
-            gscr_warps = (long long)(fixed_gtable_scratch_bytes / (sizeof(cd) * capMC));
-        } else {
-            const long long max_warps = (long long)lc.num_sms * 16 * 4;
-            if ((s = scratch.ensure((size_t)max_warps * capMC))) return s;
-            gscr = scratch.ptr;
-        }
+        // cells a group may hold: a central arrangement in general position
+        // has at most half_cells_cap(m, d) half-cells; nearly degenerate
+        // arrangements can yield more, found by the preparation below
+        int capR = half_cells_cap(MC, D);
+        lc.cells_cap = capR;
         // flat evaluation: cells and orientations, item offsets, the items
         if ((s = g_nr.ensure(nroots + 1))) return s;
         if ((s = g_items.ensure(nroots + 1))) return s;
@@ -1406,20 +1402,60 @@ public:
         GFlat gf{g_nr.ptr,    g_ioff.ptr,    g_rps2.ptr,    g_rflag.ptr,  g_minfo.ptr,  g_mps2.ptr,
                  g_mflag.ptr, nullptr,       pr_root.ptr,   pr_mb.ptr,    pr_mcnt.ptr,  pr_cells.ptr,
                  pr_items.ptr, pr_moff.ptr,  pr_ioff.ptr,   pr_coff.ptr,  nullptr};
-        const Tables Tnv{Tn.keys.ptr, Tn.vals.ptr};
-        pbeg(KID_GTABLE);
-        Kernels<D>::gtable_prep(R, roots_list.ptr, nroots, gcnt.ptr, goff.ptr, members.ptr, PV, Told, Bkeys.ptr,
-                                toff.ptr, Tnv, gf, g_items.ptr, g_cells.ptr, MC, err, lc);
-        scan_int_to_ll(g_items.ptr, g_ioff.ptr, nroots, ss, lc);
-        scan_int_to_ll(g_cells.ptr, g_coff.ptr, nroots, ss, lc);
-        pend();
+        Tables Tnv{Tn.keys.ptr, Tn.vals.ptr};
         long long gt[2] = {0, 0};
-        if (nroots > 0) {
-            MCE_CUDA(cudaMemcpyAsync(&gt[0], g_ioff.ptr + nroots, sizeof(long long), cudaMemcpyDeviceToHost,
-                                     lc.stream));
-            MCE_CUDA(cudaMemcpyAsync(&gt[1], g_coff.ptr + nroots, sizeof(long long), cudaMemcpyDeviceToHost,
-                                     lc.stream));
+        for (int attempt = 0;; attempt++) {
+            MCE_CUDA(cudaMemsetAsync(g_over.ptr, 0, 2 * sizeof(int), lc.stream));
+            pbeg(KID_GTABLE);
+            Kernels<D>::gtable_prep(R, roots_list.ptr, nroots, gcnt.ptr, goff.ptr, members.ptr, PV, Told, Bkeys.ptr,
+                                    toff.ptr, Tnv, gf, g_items.ptr, g_cells.ptr, MC, cap.ptr, g_over.ptr, lc);
+            scan_int_to_ll(g_items.ptr, g_ioff.ptr, nroots, ss, lc);
+            scan_int_to_ll(g_cells.ptr, g_coff.ptr, nroots, ss, lc);
+            pend();
+            int ov[2] = {0, 0};
+            if (nroots > 0) {
+                MCE_CUDA(cudaMemcpyAsync(&gt[0], g_ioff.ptr + nroots, sizeof(long long), cudaMemcpyDeviceToHost,
+                                         lc.stream));
+                MCE_CUDA(cudaMemcpyAsync(&gt[1], g_coff.ptr + nroots, sizeof(long long), cudaMemcpyDeviceToHost,
+                                         lc.stream));
+                MCE_CUDA(cudaMemcpyAsync(ov, g_over.ptr, 2 * sizeof(int), cudaMemcpyDeviceToHost, lc.stream));
+                MCE_CUDA(cudaStreamSynchronize(lc.stream));
+            }
+            if (!ov[0]) break;
+            if (attempt > 0) {
+                device_errors |= kErrRootCellsOverflow;
+                set_error("g-table preparation: a root's cells still exceed its re-sized slot");
+                return MCE_ERR_DEVICE;
+            }
+            // roots with more cells than the general-position count: their
+            // slots (cap[r] now holds their counts) and the cells capacity grow
+            if (ov[1] > capR) capR = ov[1];
+            lc.cells_cap = capR;
+            scan_int_to_ll(cap.ptr, toff.ptr, nR, ss, lc);
+            long long tt = 0;
+            MCE_CUDA(cudaMemcpyAsync(&tt, toff.ptr + nR, sizeof(long long), cudaMemcpyDeviceToHost, lc.stream));
             MCE_CUDA(cudaStreamSynchronize(lc.stream));
+            if ((s = Tn.keys.ensure(tt + 1))) return s;
+            if ((s = Tn.vals.ensure(tt + 1))) return s;
+            Tnv = Tables{Tn.keys.ptr, Tn.vals.ptr};
+            if (MC > kSmemBitmapRows && lc.gbits) {
+                if ((s = gbits.ensure((size_t)(lc.gbits_warps * gtable_bitmap_words(MC, D, capR))))) return s;
+                lc.gbits = gbits.ptr;
+            }
+        }
+        cd* gscr = nullptr;
+        long long gscr_warps = 0;  // 0: the handle's buffer holds a warp slot for every launched warp
+        if (fixed_gtable_scratch) {
+            gscr = static_cast<cd*>(fixed_gtable_scratch);
+            gscr_warps = (long long)(fixed_gtable_scratch_bytes / (sizeof(cd) * capR));
+            if (gscr_warps < 4) {
+                set_error("the fixed g-table scratch holds fewer than 4 warps' cells for this step");
+                return MCE_ERR_NOMEM;
+            }
+        } else {
+            const long long max_warps = (long long)lc.num_sms * 16 * 4;
+            if ((s = scratch.ensure((size_t)max_warps * capR))) return s;
+            gscr = scratch.ptr;
         }
         const long long nitems = gt[0], ncells = gt[1];
         if ((s = g_vals.ensure(nitems + 1))) return s;
@@ -1434,7 +1470,7 @@ public:
         MCE_CUDA(cudaMemsetAsync(pr_cells.ptr, 0, sizeof(int) * (nroots + 1), lc.stream));
         MCE_CUDA(cudaMemsetAsync(pr_items.ptr, 0, sizeof(int) * (nroots + 1), lc.stream));
         Kernels<D>::gtable(R, roots_list.ptr, nroots, gcnt.ptr, goff.ptr, members.ptr, PV, Told, Bkeys.ptr, gscale.ptr,
-                           toff.ptr, Tnv, tcnt.ptr, alive.ptr, src.ptr, gscr, capMC, gf, MC, err, lc, gscr_warps);
+                           toff.ptr, Tnv, tcnt.ptr, alive.ptr, src.ptr, gscr, capR, gf, MC, err, lc, gscr_warps);
         // members left after promotions: the promoted-root flat pass
         scan_int_to_ll(pr_mcnt.ptr, pr_moff.ptr, nroots, ss, lc);
         scan_int_to_ll(pr_items.ptr, pr_ioff.ptr, nroots, ss, lc);

@@ -1043,7 +1043,7 @@ __global__ void __launch_bounds__(128) k_mu_terms(ParentList P, long long nP, co
         }
         const long long slot = (t == m) ? pslot : cslot0 + (ford - 1);
         if (slot >= nR) {
-            set_err(err, kErrTableOverflow);
+            set_err(err, kErrRecordOverflow);
             continue;
         }
         int mfin = m;
@@ -1468,6 +1468,7 @@ struct GCtx {
     const int* Bkeys;
     int MC;
     unsigned* gbits;  // global bitmap regions (see LaunchCfg), or null: shared memory
+    int capR;         // cells of a group's list and scratch (LaunchCfg::cells_cap)
 };
 
 // One cell of make_gtable (flattening.hpp:105-224) for record s at `key`.
@@ -1664,13 +1665,13 @@ template <int D>
 __global__ void k_gtable_prep(GCtx c, const int* roots_list, long long nroots, const int* gcnt, const long long* goff,
                               const int* members, const long long* toff, Tables Tnew, int* gnr, int* gitems,
                               int* gcells, int* minfo, double* rps2, double* mps2, int* rflag, int* mflag,
-                              int* err)
+                              int* need, int* over)
 {
     extern __shared__ unsigned smem_g[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
     const int MC = c.MC;
     const int words = (1 << MC) > 32 ? (1 << MC) / 32 : 1;
-    const int capMC = half_cells_cap(MC, D);
+    const int capMC = c.capR;
     const size_t pw = (size_t)(2 * words + 32 + capMC);
     unsigned* PB = c.gbits ? c.gbits + (size_t)((long long)blockIdx.x * nwb + wib) * pw : smem_g + (size_t)wib * pw;
     unsigned* RK = PB + words;
@@ -1687,7 +1688,13 @@ __global__ void k_gtable_prep(GCtx c, const int* roots_list, long long nroots, c
         int nR = bm_extract(RK, m, RKL, capMC, lane);
         __syncwarp();
         if (nR > cap || nR > capMC) {
-            if (lane == 0) set_err(err, kErrTableOverflow);
+            // more cells than a central arrangement in general position can
+            // have: the caller re-sizes this root's slot and runs again
+            if (lane == 0) {
+                need[r] = nR;
+                atomicOr(over, 1);
+                atomicMax(over + 1, nR);
+            }
             nR = cap < capMC ? cap : capMC;
         }
         for (int k = lane; k < nR; k += 32) okeys[k] = RKL[k];
@@ -1848,7 +1855,7 @@ __global__ void k_gtable(GCtx c, const int* roots_list, long long nroots, const 
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
     const int MC = c.MC;
     const int words = (1 << MC) > 32 ? (1 << MC) / 32 : 1;
-    const int capMC = half_cells_cap(MC, D);
+    const int capMC = c.capR;
     const size_t pw = (size_t)(3 * words + 32 + capMC);
     unsigned* PB = c.gbits ? c.gbits + (size_t)((long long)blockIdx.x * nwb + wib) * pw : smem_g + (size_t)wib * pw;
     unsigned* RK = PB + words;
@@ -1887,7 +1894,7 @@ __global__ void k_gtable(GCtx c, const int* roots_list, long long nroots, const 
         int nR = bm_extract(RK, m, RKL, capMC, lane);
         __syncwarp();
         if (nR > cap || nR > capMC) {
-            if (lane == 0) set_err(err, kErrTableOverflow);
+            if (lane == 0) set_err(err, kErrRootCellsOverflow);
             nR = cap < capMC ? cap : capMC;
         }
         long long root = r;
@@ -1937,7 +1944,7 @@ __global__ void k_gtable(GCtx c, const int* roots_list, long long nroots, const 
                 }
                 __syncwarp();
                 if (nR > cap) {
-                    if (lane == 0) set_err(err, kErrTableOverflow);
+                    if (lane == 0) set_err(err, kErrMemberCellsOverflow);
                     nR = cap;
                 }
                 const double ps2c = R.ps2[cm];
@@ -2474,11 +2481,10 @@ void Kernels<D>::ftr_resolve(TermRecs R, long long nR, const void* ent, const lo
     tune_end(t, c.stream);
 }
 
-static inline size_t gtable_smem_per_warp(int MC, int D)
+static inline size_t gtable_smem_per_warp(int MC, int capR)
 {
     const int words = (1 << MC) > 32 ? (1 << MC) / 32 : 1;
-    const int capMC = half_cells_cap(MC, D);
-    return (size_t)(3 * words + 32 + capMC) * 4;
+    return (size_t)(3 * words + 32 + capR) * 4;
 }
 
 template <int D>
@@ -2490,8 +2496,8 @@ void Kernels<D>::gtable(TermRecs R, const int* roots_list, long long nroots, con
 {
     if (nroots == 0) return;
     const bool global_bits = MC > kSmemBitmapRows && c.gbits;
-    GCtx ctx{R, P, Told, Bkeys, MC, global_bits ? c.gbits : nullptr};
-    const size_t pw = gtable_smem_per_warp(MC, D);
+    GCtx ctx{R, P, Told, Bkeys, MC, global_bits ? c.gbits : nullptr, cells_cap_of(c, MC, D)};
+    const size_t pw = gtable_smem_per_warp(MC, ctx.capR);
     int warps = global_bits ? 4 : (int)(96 * 1024 / pw);
     if (warps > 4) warps = 4;
     if (warps < 1) warps = 1;
@@ -2516,7 +2522,7 @@ void Kernels<D>::gtable_promoted(TermRecs R, const int* roots_list, long long nr
                                  const LaunchCfg& c)
 {
     if (nitems == 0) return;
-    GCtx ctx{R, P, Told, Bkeys, MC, nullptr};
+    GCtx ctx{R, P, Told, Bkeys, MC, nullptr, cells_cap_of(c, MC, D)};
     g_launches += 3;
     k_gtable_prom_prep<D><<<grid_for(nmem, 128, c.num_sms, 8), 128, 0, c.stream>>>(ctx, nroots, nmem, members, f);
     static const int mb = max_block_of((const void*)k_gtable_prom_eval<D>);
@@ -2532,13 +2538,13 @@ template <int D>
 void Kernels<D>::gtable_prep(TermRecs R, const int* roots_list, long long nroots, const int* gcnt,
                              const long long* goff, const int* members, ParentList P, Tables Told, const int* Bkeys,
                              const long long* toff, Tables Tnew, const GFlat& f, int* gitems, int* gcells, int MC,
-                             int* err, const LaunchCfg& c)
+                             int* need, int* over, const LaunchCfg& c)
 {
     if (nroots == 0) return;
     const bool global_bits = MC > kSmemBitmapRows && c.gbits;
-    GCtx ctx{R, P, Told, Bkeys, MC, global_bits ? c.gbits : nullptr};
+    GCtx ctx{R, P, Told, Bkeys, MC, global_bits ? c.gbits : nullptr, cells_cap_of(c, MC, D)};
     const int words = (1 << MC) > 32 ? (1 << MC) / 32 : 1;
-    const size_t pw = (size_t)(2 * words + 32 + half_cells_cap(MC, D)) * 4;
+    const size_t pw = (size_t)(2 * words + 32 + ctx.capR) * 4;
     int warps = global_bits ? 4 : (int)(96 * 1024 / pw);
     if (warps > 4) warps = 4;
     if (warps < 1) warps = 1;
@@ -2549,7 +2555,7 @@ void Kernels<D>::gtable_prep(TermRecs R, const int* roots_list, long long nroots
     ++g_launches;
     k_gtable_prep<D><<<grid, warps * 32, sm, c.stream>>>(
         ctx, roots_list, nroots, gcnt, goff, members, toff, Tnew, f.gnr, gitems, gcells, f.minfo, f.rps2, f.mps2,
-        f.rflag, f.mflag, err);
+        f.rflag, f.mflag, need, over);
 }
 
 template <int D>
@@ -2559,7 +2565,7 @@ void Kernels<D>::gtable_combine(TermRecs R, const int* roots_list, long long nro
                                 int* tcnt, int* alive, int* src, const GFlat& f, int MC, const LaunchCfg& c)
 {
     if (ncells == 0) return;
-    GCtx ctx{R, P, Told, Bkeys, MC, nullptr};
+    GCtx ctx{R, P, Told, Bkeys, MC, nullptr, cells_cap_of(c, MC, D)};
     ++g_launches;
     static const int mb = max_block_of((const void*)k_gtable_combine<D>);
     const TuneLaunch t = tune_begin(TK_GTABLE_COMBINE, D, MC, ncells, 128, mb, c.stream);
@@ -2576,7 +2582,7 @@ void Kernels<D>::gtable_eval(TermRecs R, const int* roots_list, long long nroots
                              const LaunchCfg& c)
 {
     if (nitems == 0) return;
-    GCtx ctx{R, P, Told, Bkeys, MC, nullptr};
+    GCtx ctx{R, P, Told, Bkeys, MC, nullptr, cells_cap_of(c, MC, D)};
     ++g_launches;
     static const int mb = max_block_of((const void*)k_gtable_eval<D>);
     const TuneLaunch t = tune_begin(TK_GTABLE_EVAL, D, MC, nitems, 128, mb, c.stream);

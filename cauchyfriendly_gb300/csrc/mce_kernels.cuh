@@ -19,6 +19,11 @@ struct LaunchCfg {
     // per-warp size), and the kernels launch at most that many warps.
     unsigned* gbits = nullptr;
     long long gbits_warps = 0;
+    // Cells one reduction group may hold in the g-table kernels' per-warp
+    // lists and scratch; 0: half_cells_cap(MC, d), the count of a central
+    // arrangement in general position.  A step whose groups hold more (nearly
+    // degenerate arrangements) raises it and re-runs the table preparation.
+    int cells_cap = 0;
 };
 // Block-size autotuner of the thread-per-item kernels (grid-stride loops with
 // no shared memory, no block-wide step and no reductions, so every block size
@@ -52,11 +57,15 @@ int tune_table(int* out, float* best_ms, int n);
 void tune_configure(int enabled);
 constexpr int kSmemBitmapRows = 16;
 constexpr int kMaxBitmapRows = 24;
+inline int cells_cap_of(const LaunchCfg& c, int MC, int D)
+{
+    return c.cells_cap > 0 ? c.cells_cap : half_cells_cap(MC, D);
+}
 // words of one warp's bitmap region in the g-table kernels (the largest user)
-inline long long gtable_bitmap_words(int MC, int D)
+inline long long gtable_bitmap_words(int MC, int D, int cells_cap = 0)
 {
     const long long words = (1LL << MC) > 32 ? (1LL << MC) / 32 : 1;
-    return 3 * words + 32 + half_cells_cap(MC, D);
+    return 3 * words + 32 + (cells_cap > 0 ? cells_cap : half_cells_cap(MC, D));
 }
 
 // Scratch for the device-wide scans.
@@ -160,10 +169,14 @@ struct Kernels {
                                 long long nitems, long long ncells, const int* members, ParentList P, Tables Told,
                                 const int* Bkeys, const double* gscale, const long long* toff, Tables Tnew,
                                 const GFlat& f, int MC, const LaunchCfg& c);
+    // Root cells into the output keys and each group's flat-pass layout.  A
+    // root with more cells than its table slot (toff) or than the cells
+    // capacity writes its count to need[r] and sets over[0] = 1, over[1] =
+    // max count: the caller re-sizes and runs the preparation again.
     static void gtable_prep(TermRecs R, const int* roots_list, long long nroots, const int* gcnt,
                             const long long* goff, const int* members, ParentList P, Tables Told, const int* Bkeys,
                             const long long* toff, Tables Tnew, const GFlat& f, int* gitems, int* gcells, int MC,
-                            int* err, const LaunchCfg& c);
+                            int* need, int* over, const LaunchCfg& c);
     static void shift_b(ParentList P, long long a, long long n, const double* v, int sub, const LaunchCfg& c);
     static void det_tp(ParentList P, long long a, long long n, const double* Phi, const double* Bu, int MC,
                        const LaunchCfg& c);

@@ -366,7 +366,13 @@ double mce_host_time_ms(mce_handle* h, int which);
 /* Sum over all updates and estimators of the terms present after each MU. */
 long long mce_post_mu_terms(mce_handle* h);
 int mce_master_step(mce_handle* h);
-/* Device error bits accumulated by the kernels (0 when healthy). */
+/* Device error bits accumulated by the kernels (0 when healthy): 1 an
+ * anti-coaligned orthogonal hyperplane (the reference exits,
+ * cauchy_term.hpp:673-687), 2 a B table above its capacity, 4 more
+ * hyperplanes than the handle's capacity, 8 the reduction's resolution
+ * stalled, 16 a vertex enumeration above its capacity, 32 an MU record past
+ * the step's record count, 64 a reduction root's cells above its table slot,
+ * 128 a promoted member's cells above its table slot. */
 int mce_device_errors(mce_handle* h);
 
 /* Parity hooks: terms of one estimator in (shape, index) order.  Sizes:
