@@ -548,33 +548,51 @@ def run_rel2d(args):
     if not args.no_cpu_baseline:
         import oracle
         oracle.build(with_reference=False)
-        orcs = []
-        for q, c in zip(probs, consts):
-            o = oracle.Oracle(q, *c)
-            n = 0
-            for k in range(q["steps"]):
-                for sub in range(q["p"]):
-                    if n < updates:
-                        o.step(k, sub)
-                        n += 1
-            orcs.append(o)
-        stride = 512
-        t0 = time.perf_counter()
-        oracle.oracle_rel2d(orcs[0], orcs[1], T, nu, (-1.0, 1.0, 0.125), (-1.0, 1.0, 0.125), pair_stride=stride)
-        t1 = time.perf_counter() - t0
-        stride = int(max(1, stride * t1 / max(args.cpu_seconds, 1e-3)))
-        t0 = time.perf_counter()
-        r = oracle.oracle_rel2d(orcs[0], orcs[1], T, nu, (-1.0, 1.0, 0.125), (-1.0, 1.0, 0.125),
-                                pair_stride=stride)
-        t1 = time.perf_counter() - t0
-        line["cpu_baseline"] = {"value": r["pairs"] / t1, "unit": "pairs/s", "cores": 1, "kind": "port",
-                                "sample": "every %d-th pair of the same evaluation (cache, moments, 17x17 grid): "
-                                          "%d pairs, %.1f s" % (stride, r["pairs"], t1)}
-        for o in orcs:
-            o.close()
+        # calibrate a per-process sample on one core, then run one process per
+        # host core, each on its own share of the pairs (offset i modulo the
+        # stride), as the reference spreads the pairs over NUM_CPUS threads
+        t1 = _rel2d_cpu_share((probs, consts, updates, T, nu, 512, 0))[1]
+        cores = os.cpu_count() or 1
+        stride = int(max(cores, 512 * t1 / max(args.cpu_seconds, 1e-3)))
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(cores) as pool:
+            t0 = time.perf_counter()
+            res = pool.map(_rel2d_cpu_share, [(probs, consts, updates, T, nu, stride, i) for i in range(cores)])
+            wall = time.perf_counter() - t0
+        done = sum(r[0] for r in res)
+        slowest = max(r[1] for r in res)
+        line["cpu_baseline"] = {"value": done / slowest, "unit": "pairs/s", "cores": cores, "kind": "port",
+                                "sample": "%d processes, each every %d-th pair of the same evaluation (cache, "
+                                          "moments, 17x17 grid) at its own offset: %d pairs, slowest share %.1f s "
+                                          "(%.1f s with process start)" % (cores, stride, done, slowest, wall)}
     for e in ests:
         e.close()
     print(json.dumps(line), flush=True)
+
+
+def _rel2d_cpu_share(job):
+    """One process's share of the relative-system CPU baseline: the oracle's
+    two estimators stepped as the GPU ones, then every stride-th pair from
+    offset; returns (pairs, seconds of the evaluation)."""
+    import oracle
+    probs, consts, updates, T, nu, stride, offset = job
+    orcs = []
+    for q, c in zip(probs, consts):
+        o = oracle.Oracle(q, *c)
+        n = 0
+        for k in range(q["steps"]):
+            for sub in range(q["p"]):
+                if n < updates:
+                    o.step(k, sub)
+                    n += 1
+        orcs.append(o)
+    t0 = time.perf_counter()
+    r = oracle.oracle_rel2d(orcs[0], orcs[1], T, nu, (-1.0, 1.0, 0.125), (-1.0, 1.0, 0.125), pair_stride=stride,
+                            pair_offset=offset)
+    t1 = time.perf_counter() - t0
+    for o in orcs:
+        o.close()
+    return r["pairs"], t1
 
 
 def autotune_summary(table, passes, off):

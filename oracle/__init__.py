@@ -525,24 +525,25 @@ def _unpack_rel_moments(mom):
 
 
 def oracle_rel2d(prim, sec, Trel, bar_nu_full, gx, gy, full_solve=False, with_term_approx=True,
-                 term_approx_eps=1e-8, center=True, max_points=200000, pair_stride=1):
+                 term_approx_eps=1e-8, center=True, max_points=200000, pair_stride=1, pair_offset=0):
     """Relative-then-transformed system of two oracle estimators
     (rel = sec - prim, projected by the 2 x d Trel): its moments, pair counts
     and 2-D pdf on the grid gx = (low, high, step) x gy, offset by the
     relative mean when center (as pycauchy_single_step_eval_2d_rsys_cpdf).
-    pair_stride > 1 takes every pair_stride-th pair only (a timing sample)."""
+    pair_stride > 1 takes only the pairs whose index is pair_offset modulo
+    pair_stride (a timing sample)."""
     lib = prim._l.lib
     f = lib.orc_rel2d_create
     f.restype = ctypes.c_void_p
     f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                   ctypes.c_double, _dp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_int),
-                  ctypes.c_longlong]
+                  ctypes.c_longlong, ctypes.c_longlong]
     T, nu = _arr(Trel), _arr(bar_nu_full)
     mom = np.zeros(14)
     counts = (ctypes.c_longlong * 2)()
     st = ctypes.c_int(0)
     r = f(prim.h, sec.h, _ptr(T), _ptr(nu), int(bool(full_solve)), 1, int(bool(with_term_approx)),
-          float(term_approx_eps), _ptr(mom), counts, ctypes.byref(st), int(pair_stride))
+          float(term_approx_eps), _ptr(mom), counts, ctypes.byref(st), int(pair_stride), int(pair_offset))
     if not r:
         raise RuntimeError("orc_rel2d_create status %d" % st.value)
     try:

@@ -2055,11 +2055,12 @@ int orc_cpdf_2d_grid(void* h, int i1, int i2, const double* bar_nu, double lx, d
 // moments finalised (fz re/im, mean 2 x re/im, covariance 4 x re/im) when
 // get_moments; counts[2] the pairs and the pairs approximated out.  *status:
 // 0, -1 before the first step, -5 at the last step of either estimator,
-// -3 dimension mismatch or too many rows.  pair_stride > 1 takes only every
-// pair_stride-th pair (a bounded sample for timing).
+// -3 dimension mismatch or too many rows.  pair_stride > 1 takes only the
+// pairs whose index is pair_offset modulo pair_stride (a bounded sample for
+// timing, which several processes can share).
 void* orc_rel2d_create(void* hp, void* hs, const double* Trel, const double* bar_nu_full, int full_solve,
                        int get_moments, int with_term_approx, double term_approx_eps, double* mom, long long* counts,
-                       int* status, long long pair_stride)
+                       int* status, long long pair_stride, long long pair_offset)
 {
     Estimator& P = *(Estimator*)hp;
     Estimator& S = *(Estimator*)hs;
@@ -2101,7 +2102,7 @@ void* orc_rel2d_create(void* hp, void* hs, const double* Trel, const double* bar
         for (int ms = 1; ms < S.shape_range; ms++)
             for (const Term* tp : bp[mp])
                 for (const Term* ts : bs[ms]) {
-                    if (pair_stride > 1 && (pair_index++ % pair_stride) != 0) continue;
+                    if (pair_stride > 1 && (pair_index++ % pair_stride) != pair_offset) continue;
                     Cpdf2DTerm c;
                     rel2d_pair(*tp, *ts, d, Trel, bar_nu_full, bar_nu, R->full, get_moments ? acc : nullptr, c);
                     R->total++;
