@@ -38,7 +38,7 @@ def _flags():
 
 def _sources():
     srcs = [os.path.join(CSRC, f) for f in ("mce_kernels.cu", "mce_engine.cu", "mce_no_alloc.cu", "mce_host.cpp",
-                                            "mce_adjoint.cu")]
+                                            "mce_adjoint.cu", "mce_ndpdf.cu")]
     hdrs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     hdrs.append(os.path.join(os.path.dirname(HERE), "include", "mce_c_api.h"))
     return srcs, hdrs
@@ -79,6 +79,9 @@ def build(force=False, verbose=False):
     obj = os.path.join(OUT, "mce_no_alloc.o")
     objs.append(obj)
     jobs.append([nvcc, "-c", os.path.join(CSRC, "mce_no_alloc.cu"), "-o", obj] + _flags())
+    obj = os.path.join(OUT, "mce_ndpdf.o")
+    objs.append(obj)
+    jobs.append([nvcc, "-c", os.path.join(CSRC, "mce_ndpdf.cu"), "-o", obj] + _flags())
     obj = os.path.join(OUT, "mce_adjoint.o")
     objs.append(obj)
     jobs.append([nvcc, "-c", os.path.join(CSRC, "mce_adjoint.cu"), "-o", obj] + _flags())

@@ -325,6 +325,8 @@ public:
                              double* ys, double* zs) = 0;
     virtual int cpdf_1d_grid(int est, int marg, const double* bar_nu, double low, double high, double res,
                              int max_points, double* xs, double* ys) = 0;
+    // PointWiseNDimCauchyCPDF::evaluate_cpdf at npts points (csrc/mce_ndpdf.cu)
+    virtual int cpdf_nd(int est, const double* x, int npts, double* out) = 0;
     // waits for the work the engine queued (after a step that stopped early)
     virtual void drain() = 0;
     // Estimator e's current terms for the relative system: the device lists,
@@ -731,6 +733,7 @@ public:
     ~Engine() override
     {
         if (lc.stream) cudaStreamSynchronize(lc.stream);
+        if (ndw) nd_work_destroy(ndw);
         if (mstream) cudaStreamSynchronize(mstream);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
@@ -1751,6 +1754,45 @@ public:
         return MCE_OK;
     }
 
+    // ---- N-D conditional pdf at points (PointWiseNDimCauchyCPDF::evaluate_cpdf,
+    // cpdf_ndim.hpp:677-904): the estimator's terms and tables as they are
+    NdWork* ndw = nullptr;
+    int cpdf_nd(int e, const double* x, int npts, double* out) override
+    {
+        if (e < 0 || e >= E || !x || !out || npts < 1) return MCE_ERR_ARG;
+        if (master_step < 1) {
+            set_error("N-D pdf: the estimator has not been stepped");
+            return MCE_ERR_ARG;
+        }
+        if (master_step >= est[e].num_updates) {
+            set_error("N-D pdf: the last step keeps no g-tables");
+            return MCE_ERR_DONE;
+        }
+        if (est[e].errors) {
+            set_error("N-D pdf: the last step reported moment errors (the reference asserts "
+                      "numeric_moment_errors == 0, cpdf_ndim.hpp:680)");
+            return MCE_ERR_ARG;
+        }
+        drain();
+        if (!ndw) ndw = nd_work_create();
+        const long long a = hpstart[e];
+        PBufs& P = Pb[cur];
+        NdInput in;
+        in.D = D;
+        in.MC = MC;
+        in.n = hpstart[e + 1] - a;
+        in.m = P.m.ptr + a;
+        in.A = P.A.ptr + a * MC * D;
+        in.p = P.p.ptr + a * MC;
+        in.b = P.b.ptr + a * D;
+        in.toff = P.tab_off.ptr + a;
+        in.tcnt = P.tab_cnt.ptr + a;
+        in.keys = Tb[cur].keys.ptr;
+        in.vals = Tb[cur].vals.ptr;
+        in.fz = est[e].fz[0];
+        return nd_pdf_eval(in, x, npts, out, ndw, lc, &launches);
+    }
+
     void rel2d_pairs(const Rel2DArgs& a, cudaStream_t st) override
     {
         LaunchCfg c = lc;
@@ -2570,6 +2612,11 @@ int mce_finalize_extended_moments(mce_handle* h, int e, double* x_bar)
     for (int i = 0; i < d; i++) eh.mean[2 * i] += x_bar[i];
     for (int i = 0; i < d; i++) x_bar[i] = eh.mean[2 * i];
     return MCE_OK;
+}
+int mce_cpdf_nd(mce_handle* h, int e, const double* x, int npts, double* out)
+{
+    if (bad(h, e)) return MCE_ERR_ARG;
+    return h->eng->cpdf_nd(e, x, npts, out);
 }
 int mce_cpdf_2d_grid(mce_handle* h, int e, int marg_idx1, int marg_idx2, const double* bar_nu, double gridx_low,
                      double gridx_high, double gridx_res, double gridy_low, double gridy_high, double gridy_res,

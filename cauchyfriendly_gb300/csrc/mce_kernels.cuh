@@ -68,6 +68,29 @@ inline long long gtable_bitmap_words(int MC, int D, int cells_cap = 0)
     return 3 * words + 32 + (cells_cap > 0 ? cells_cap : half_cells_cap(MC, D));
 }
 
+// N-D conditional pdf (csrc/mce_ndpdf.cu): one estimator's terms (a
+// contiguous range of a parent list) and tables.
+struct NdInput {
+    int D = 0, MC = 0;
+    long long n = 0;
+    const int* m = nullptr;
+    const double* A = nullptr;  // [n][MC][D]
+    const double* p = nullptr;  // [n][MC]
+    const double* b = nullptr;  // [n][D]
+    const long long* toff = nullptr;
+    const int* tcnt = nullptr;
+    const int* keys = nullptr;
+    const cd* vals = nullptr;
+    double fz = 0;  // Re fz, the normaliser
+};
+struct NdWork;
+NdWork* nd_work_create();
+void nd_work_destroy(NdWork* w);
+// The pdf at npts points x_host[npts][D] into out_host[2 * npts] (re, im);
+// kernels launched are added to *launches.
+int nd_pdf_eval(const NdInput& in, const double* x_host, int npts, double* out_host, NdWork* w, const LaunchCfg& lc,
+                long long* launches);
+
 // Scratch for the device-wide scans.
 struct ScanScratch {
     long long* block_sums;  // capacity >= ceil(n / 2048) + 1 at every level

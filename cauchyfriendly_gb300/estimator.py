@@ -214,6 +214,16 @@ class BatchedCauchyEstimator:
         _lib.check(n, "mce_cpdf_2d_grid")
         return X, Y, Z
 
+    def cpdf_nd(self, x, e=0):
+        """The conditional pdf of estimator e at the points x ([n][d] or [d]):
+        PointWiseNDimCauchyCPDF::evaluate_cpdf (include/cpdf_ndim.hpp:677-904)
+        for every point at once; complex values (the imaginary parts are
+        rounding)."""
+        X = np.ascontiguousarray(np.asarray(x, dtype=np.float64).reshape(-1, self.d))
+        out = np.zeros(2 * X.shape[0])
+        _lib.check(self._lib.mce_cpdf_nd(self._h, int(e), _p(X), X.shape[0], _p(out)), "mce_cpdf_nd")
+        return out[0::2] + 1j * out[1::2]
+
     def cpdf_1d_grid(self, e, marg_idx, gridx_low, gridx_high, gridx_resolution, bar_nu):
         """Marginal 1-D conditional pdf of estimator e on the grid
         gridx_low..gridx_high step gridx_resolution

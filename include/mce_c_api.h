@@ -161,6 +161,19 @@ int mce_finalize_extended_moments(mce_handle* h, int est, double* x_bar);
 int mce_cpdf_1d_grid(mce_handle* h, int est, int marg_idx, const double* bar_nu, double grid_low, double grid_high,
                      double grid_res, int max_points, double* x, double* y);
 
+/* The conditional pdf of estimator `est` at npts points x[npts*d]:
+ * PointWiseNDimCauchyCPDF::evaluate_cpdf (include/cpdf_ndim.hpp:677-904), the
+ * characteristic function integrated one spectral dimension at a time.
+ * out[2*npts] receives each value (re, im; the imaginary part is rounding).
+ * Each (point, term) pair is lowered on its own (the reference merges terms
+ * whose arrangements agree within 1e-8 between the lowerings): the same sum
+ * up to rounding.  MCE_ERR_ARG before the first step or when the last step
+ * reported moment errors (the reference asserts), MCE_ERR_DONE after the
+ * last step, MCE_ERR_SHAPE above 16 hyperplanes per term, MCE_ERR_DEVICE
+ * where the reference exits (an anti-coaligned pair of rows that do not
+ * enter the integration). */
+int mce_cpdf_nd(mce_handle* h, int est, const double* x, int npts, double* out);
+
 /* Marginal 2-D conditional pdf of estimator `est` over states
  * marg_idx1 < marg_idx2 on the grid x = gridx_low ... gridx_high (step
  * gridx_res) by y = gridy_low ... gridy_high, x varying fastest, as

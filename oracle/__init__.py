@@ -405,6 +405,11 @@ class Oracle(_EstimatorBase):
             raise RuntimeError("orc_cpdf_1d_grid returned %d" % n)
         return xs[:n].copy(), ys[:n].copy()
 
+    def cpdf_nd(self, x):
+        """The N-D conditional pdf at the point x (complex; the reference's
+        PointWiseNDimCauchyCPDF::evaluate_cpdf)."""
+        return _cpdf_nd_call(self._l.lib.orc_cpdf_nd, self.h, x, "orc_cpdf_nd")
+
 
 class OracleSlot:
     """A window slot of n_mgr oracle estimators with the batch interface the
@@ -505,6 +510,10 @@ class Reference(_EstimatorBase):
             raise RuntimeError("ref_cpdf_2d_grid returned %d" % n)
         return xs[:n].copy(), ys[:n].copy(), zs[:n].copy(), nu
 
+    def cpdf_nd(self, x):
+        """The reference's own PointWiseNDimCauchyCPDF::evaluate_cpdf at x."""
+        return _cpdf_nd_call(self._l.lib.ref_cpdf_nd, self.h, x, "ref_cpdf_nd")
+
     def cpdf_1d_grid(self, marg, low, high, res, max_points=100000):
         """The reference's own marginal 1-D pdf grid; returns (x, y, bar_nu)."""
         f = self._l.lib.ref_cpdf_1d_grid
@@ -517,6 +526,17 @@ class Reference(_EstimatorBase):
             raise RuntimeError("ref_cpdf_1d_grid returned %d" % n)
         return xs[:n].copy(), ys[:n].copy(), nu
 
+
+
+def _cpdf_nd_call(f, h, x, name):
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_void_p, _dp, _dp]
+    xx = _arr(x)
+    out = np.zeros(2)
+    st = f(h, _ptr(xx), _ptr(out))
+    if st < 0:
+        raise RuntimeError("%s returned %d" % (name, st))
+    return complex(out[0], out[1])
 
 
 def _unpack_rel_moments(mom):

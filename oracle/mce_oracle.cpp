@@ -851,6 +851,76 @@ static void new_child_btable(Term& t, int d)
     t.own_B = out;
 }
 
+// make_lowered_child_btable: cell_enumeration.hpp:1121-1279 (the N-D pdf's
+// lowering).  The child keeps the parent cells b (in the frame of enc_lhp)
+// whose neighbour across hyperplane z is a parent cell too, with bit z
+// removed; the last child keeps the smaller of the two opposite keys.
+static void lowered_child_btable(Term& t, int d)
+{
+    const int m = t.m;
+    std::vector<int> out;
+    if (m == d) {
+        for (int i = 0; i < (1 << d) / 2; i++) out.push_back(i);
+        t.own_B = out;
+        return;
+    }
+    const std::vector<int>& Bmu = *t.encB;
+    const int phc = t.phc, z = t.z;
+    const int top = 1 << (phc - 1), rev = (1 << phc) - 1, mz = 1 << z;
+    int lhp = t.enc_lhp;
+    if (lhp & top) lhp ^= rev;
+    std::vector<int> pos((size_t)1 << phc, -1);
+    for (size_t j = 0; j < Bmu.size(); j++)
+        if (pos[Bmu[j] ^ lhp] < 0) pos[Bmu[j] ^ lhp] = (int)j;
+    std::vector<char> F(Bmu.size(), 1);
+    const bool last = z == phc - 1;
+    auto remove_bit = [](int b, int bit) { return ((b >> (bit + 1)) << bit) | (b & ((1 << bit) - 1)); };
+    std::vector<int> buc;
+    for (size_t j = 0; j < Bmu.size(); j++) {
+        if (!F[j]) continue;
+        const int b = Bmu[j] ^ lhp;
+        int bq = b ^ mz;
+        if (last) bq ^= rev;
+        const int k = pos[bq];
+        if (k < 0) continue;
+        F[j] = 0;
+        F[k] = 0;
+        const int c1 = remove_bit(b, z);
+        if (last) {
+            const int c2 = remove_bit(bq, z);
+            buc.push_back(c1 < c2 ? c1 : c2);
+        } else
+            buc.push_back(c1);
+    }
+    if (t.has_cmap) {
+        // projection through the coalignment map, first occurrence kept.  The
+        // reference runs j up to phc, one past the child's phc - 1 mapped rows;
+        // that extra entry can only add a mask bit no key has, so the rows stop
+        // at phc - 1 here
+        std::vector<int> bitmask;
+        std::vector<char> Fc(phc, 1);
+        for (int j = 0; j < (int)t.cmap.size(); j++) {
+            const int ci = t.cmap[j];
+            if (Fc[ci]) {
+                Fc[ci] = 0;
+                bitmask.push_back(1 << j);
+            }
+        }
+        std::vector<char> seen((size_t)1 << bitmask.size(), 0);
+        for (int bb : buc) {
+            int bc = 0;
+            for (size_t l = 0; l < bitmask.size(); l++)
+                if (bb & bitmask[l]) bc |= 1 << l;
+            if (!seen[bc]) {
+                seen[bc] = 1;
+                out.push_back(bc);
+            }
+        }
+    } else
+        out = buc;
+    t.own_B = out;
+}
+
 // Orientation mask between two equal arrangements (first component that is
 // significant in both rows decides): cell_enumeration.hpp:630-640 and
 // flattening.hpp:279-288.
@@ -1017,7 +1087,7 @@ static void ftr(const std::vector<Term*>& T, int d, std::vector<int>& F)
 
 // make_gtables for one shape: flattening.hpp:318-568.
 static void make_gtables_shape(std::vector<Term*>& T, const std::vector<int>& F, int d, double gscale,
-                               std::vector<Term*>& out)
+                               std::vector<Term*>& out, bool lowered = false)
 {
     const int n = (int)T.size();
     std::vector<std::vector<int>> members(n);
@@ -1029,7 +1099,8 @@ static void make_gtables_shape(std::vector<Term*>& T, const std::vector<int>& F,
         bool have_root = true;
         std::vector<int> rootB;
         if (root->is_new_child) {
-            new_child_btable(*root, d);
+            if (lowered) lowered_child_btable(*root, d);
+            else new_child_btable(*root, d);
             rootB = root->own_B;
         } else
             rootB = *root->encB;
@@ -1360,6 +1431,143 @@ static void step_rest(Estimator& E, double msmt, const double* Phi, const double
 // (a x + b) / (w^2 + (x - s)^2).
 
 // number of grid points: reset_grid (cpdf_ndim.hpp:2055-2072)
+// ----------------------------------------------------------------------------
+// Point-wise N-D conditional pdf: PointWiseNDimCauchyCPDF::evaluate_cpdf
+// (cpdf_ndim.hpp:677-904).  The terms are lowered one spectral dimension at
+// a time (construct_lowered_parent_elements :392-443, construct_lowered_children
+// :520-641), each lowered child coaligned as after an MU, the children of each
+// shape reduced (FTR) and given g-tables (make_gtables with
+// make_lowered_child_btable, G_SCALE_FACTOR 1), and the 1-D terms left are
+// integrated in closed form (evaluate_1d_cf :643-666).
+
+// The lowered children of parent P (dimension ld) into out; xk (the point)
+// on the first lowering only.
+static void lower_children(const Term& P, int ld, const double* xk, std::vector<Term>& out)
+{
+    const int m = P.m, l1 = ld - 1;
+    std::vector<double> Alp((size_t)m * l1), Ald(m), plp(m), blp(l1);
+    std::vector<char> nz(m);
+    int lam = 0;
+    for (int i = 0; i < m; i++) {
+        Ald[i] = -P.A[i * ld + ld - 1];
+        nz[i] = fabs(Ald[i]) > kMuEps;
+    }
+    for (int i = 0; i < m; i++) {
+        if (nz[i]) {
+            for (int j = 0; j < l1; j++) Alp[i * l1 + j] = P.A[i * ld + j] / Ald[i];
+            if (Ald[i] < 0) lam |= 1 << i;
+            plp[i] = P.p[i] * fabs(Ald[i]);
+        } else {
+            for (int j = 0; j < l1; j++) Alp[i * l1 + j] = P.A[i * ld + j];
+            plp[i] = P.p[i];
+        }
+    }
+    double tb;
+    if (xk) {
+        for (int i = 0; i < l1; i++) blp[i] = P.b[i] - xk[i];
+        tb = P.b[l1] - xk[l1];
+    } else {
+        for (int i = 0; i < l1; i++) blp[i] = P.b[i];
+        tb = P.b[l1];
+    }
+    auto keys = std::make_shared<std::vector<int>>(P.gp->keys);
+    for (int t = 0; t < m; t++) {
+        if (!nz[t]) continue;
+        Term c;
+        c.m = m - 1;
+        c.A.assign((size_t)(m - 1) * l1, 0.0);
+        c.p.assign(m - 1, 0.0);
+        c.b.assign(l1, 0.0);
+        const double* mu_t = Alp.data() + t * l1;
+        int l_ = 0;
+        unsigned unint = 0;
+        for (int l = 0; l < m; l++) {
+            if (l == t) continue;
+            const double* mu_l = Alp.data() + l * l1;
+            double* row = c.A.data() + l_ * l1;
+            if (nz[l]) {
+                for (int j = 0; j < l1; j++) row[j] = mu_l[j] - mu_t[j];
+            } else {
+                for (int j = 0; j < l1; j++) row[j] = mu_l[j];
+                unint |= 1u << l_;
+            }
+            c.p[l_] = plp[l];
+            l_++;
+        }
+        for (int j = 0; j < l1; j++) c.b[j] = blp[j] + tb * mu_t[j];
+        c.c_val = tb;
+        c.d_val = plp[t];
+        c.z = t;
+        c.horthog = unint;
+        c.is_new_child = true;
+        c.enc_lhp = lam;
+        c.gp = P.gp;
+        c.encB = keys;
+        c.phc = m;
+        c.pbc = m;
+        out.push_back(std::move(c));
+    }
+}
+
+// Returns 0 and the complex value, or -1 before the first step / with
+// moment errors (the reference asserts), -3 when a lowered child
+// anti-coaligns two unintegrable rows (the reference exits).
+static int cpdf_nd_eval(Estimator& E, const double* xk, cplx* out)
+{
+    if (E.master_step < 1 || E.errors) return -1;
+    const int dim = E.d;
+    int top = 0;
+    for (int i = 0; i < E.shape_range; i++)
+        if (E.terms_per_shape[i] > 0) top = i;
+    int shape_range = top + 1;
+    // parents by shape, in term order
+    std::vector<std::vector<Term>> par(shape_range);
+    for (const Term& t : E.terms)
+        if (t.m < shape_range) par[t.m].push_back(t);
+    for (int d = dim; d > 1; d--) {
+        const int dl = d - 1;
+        std::vector<Term> kids;
+        for (int m = d; m < shape_range; m++)
+            for (const Term& P : par[m]) {
+                const size_t k0 = kids.size();
+                lower_children(P, d, d == dim ? xk : nullptr, kids);
+                for (size_t k = k0; k < kids.size(); k++) {
+                    const int pre = kids[k].m;
+                    const int ns = mu_coalign(kids[k], dl);
+                    if (ns < 0) return -3;
+                    kids[k].has_cmap = ns < pre;
+                }
+            }
+        std::vector<std::vector<Term*>> byshape(shape_range);
+        for (Term& c : kids) byshape[c.m].push_back(&c);
+        std::vector<std::vector<Term>> next(shape_range);
+        for (int m = 0; m < shape_range; m++) {
+            if (byshape[m].empty() || m < dl) continue;
+            std::vector<int> F;
+            ftr(byshape[m], dl, F);
+            std::vector<Term*> roots;
+            make_gtables_shape(byshape[m], F, dl, 1.0, roots, true);
+            for (Term* r : roots) next[m].push_back(std::move(*r));
+        }
+        par.swap(next);
+        shape_range -= 1;
+    }
+    cplx f = mkc(0, 0);
+    if (shape_range > 1)
+        for (const Term& t : par[1]) {
+            const int lp = t.A[0] > 0 ? 1 : 0, lm = t.A[0] > 0 ? 0 : 1;
+            const cplx gp = lookup_num(t.gp.get(), lp, 1);
+            const cplx gm = lookup_num(t.gp.get(), lm, 1);
+            f += cdiv(gp, mkc(t.p[0], t.b[0])) - cdiv(gm, mkc(-t.p[0], t.b[0]));
+        }
+    // unnormalized_f_x / norm_factor * pow(RECIPRICAL_TWO_PI, dim)
+    const double nf = __real__ E.fz;
+    f = mkc(__real__ f / nf, __imag__ f / nf);
+    const double s = pow(kTwoPiInv, dim);
+    *out = mkc(__real__ f * s, __imag__ f * s);
+    return 0;
+}
+
 static int cpdf_grid_points(double low, double high, double res)
 {
     return (int)((high - low + res - 1e-15) / res) + 1;
@@ -2001,6 +2209,18 @@ void orc_finalize_extended_moments(void* h, double* x_bar)
 // evaluate_point_grid (cpdf_ndim.hpp:2055-2139).  Returns the point count, -2
 // if it exceeds max_points, -1 before the first step, -5 at the last step
 // (its g-tables are skipped).
+// the N-D conditional pdf at x[d]; out[2] = (re, im)
+int orc_cpdf_nd(void* h, const double* x, double* out)
+{
+    cplx v;
+    const int st = cpdf_nd_eval(*(Estimator*)h, x, &v);
+    if (st == 0) {
+        out[0] = __real__ v;
+        out[1] = __imag__ v;
+    }
+    return st;
+}
+
 int orc_cpdf_1d_grid(void* h, int marg, const double* bar_nu, double low, double high, double res, int max_points,
                      double* xs, double* ys)
 {

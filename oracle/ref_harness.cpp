@@ -64,6 +64,7 @@ static int harness_covariance_checker(C_COMPLEX_TYPE* cov, const int d, const in
 #define covariance_checker harness_covariance_checker
 
 #include "cauchy_estimator.hpp"
+#include <vector>
 #include "cpdf_ndim.hpp"
 #include "cauchy_prediction.hpp"
 
@@ -257,6 +258,21 @@ void ref_finalize_extended_moments(void* vh, double* x_bar) { ((RefHandle*)vh)->
 // first call (it draws bar_nu from rand()) and kept; a dispatcher per call.
 // Returns the point count, -2 if it exceeds max_points, -5 if the reference
 // refuses (the last step).  bar_nu[d] receives the pdf object's draws.
+// PointWiseNDimCauchyCPDF::evaluate_cpdf (include/cpdf_ndim.hpp:677-904) at
+// x[d] with the handle's pdf object; out[2] = (re, im).  -5 where the
+// reference would assert (no step yet, or moment errors).
+int ref_cpdf_nd(void* vh, const double* x, double* out)
+{
+    RefHandle* h = (RefHandle*)vh;
+    if (h->est->master_step < 1 || h->est->numeric_moment_errors) return -5;
+    if (!h->cpdf) h->cpdf = new PointWiseNDimCauchyCPDF(h->est);
+    std::vector<double> xk(x, x + h->d);
+    const C_COMPLEX_TYPE v = h->cpdf->evaluate_cpdf(xk.data());
+    out[0] = __real__ v;
+    out[1] = __imag__ v;
+    return 0;
+}
+
 int ref_cpdf_1d_grid(void* vh, int marg, double low, double high, double res, int max_points, double* xs,
                      double* ys, double* bar_nu)
 {

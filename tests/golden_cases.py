@@ -15,8 +15,8 @@ REL_TOL = 1e-9
 def names():
     """The step-record fixtures (the marginal pdf ones are cpdf_names())."""
     return sorted(n for n in (os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
-                  if not n.startswith(("cpdf1d_", "cpdf2d_", "ext_", "rel2d_", "win_", "speyer_", "tr_ordering_",
-                                       "adj_")))
+                  if not n.startswith(("cpdf1d_", "cpdf2d_", "cpdfnd_", "ext_", "rel2d_", "win_", "speyer_",
+                                       "tr_ordering_", "adj_")))
 
 
 def cpdf_names():
@@ -36,6 +36,20 @@ def load_cpdf(name):
             pre = "m%d_c%d_" % (marg, call)
             grids.append((marg, call, tuple(float(v) for v in z[pre + "grid"]), z[pre + "x"], z[pre + "y"]))
     return prob, (z["root_point"], z["b_pert"]), int(z["updates"]), z["bar_nu"], grids
+
+
+def cpdfnd_names():
+    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "cpdfnd_*.npz")))
+
+
+def load_cpdfnd(name):
+    """(problem, (root_point, b_pert), updates, points [n][d], complex values)"""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    prob = {k: z[k] for k in ("Phi", "Gamma", "beta", "H", "gamma", "A0", "p0", "b0", "msmts")}
+    for k in ("d", "pncc", "cmcc", "p", "steps"):
+        prob[k] = int(z[k])
+    prob["B"] = None
+    return prob, (z["root_point"], z["b_pert"]), int(z["updates"]), z["x"], z["f"]
 
 
 def rel2d_names():

@@ -102,3 +102,73 @@ def test_gpu_cpdf2d_matches_reference_grids(name):
         assert G.relerr(zg, z) <= G.REL_TOL, (i1, i2, call, G.relerr(zg, z))
     assert est.device_errors() == 0
     est.close()
+
+
+def _stepped_gpu(CE, prob, rp, bp, updates):
+    est = CE(prob["A0"], prob["p0"], prob["b0"], prob["steps"], prob["d"], prob["cmcc"], prob["pncc"], prob["p"],
+             root_point=rp, b_pert=bp)
+    for k, s in _updates(prob)[:updates]:
+        Phi = prob["Phi"] if prob["Phi"].ndim == 2 else prob["Phi"][k]
+        est.step(prob["msmts"][k, s], Phi, prob["Gamma"], prob["beta"], prob["H"][s], prob["gamma"][s])
+    return est
+
+
+@pytest.mark.parametrize("name", G.cpdfnd_names())
+def test_gpu_nd_pdf_matches_reference(name):
+    """mce_cpdf_nd at all of a fixture's points in one call against the
+    reference's PointWiseNDimCauchyCPDF::evaluate_cpdf (tests/golden/
+    cpdfnd_*.npz, values from 1e-16 to 35): within 1e-9 element-wise, the
+    floor 1e-12 of the largest value (the reference merges nearly equal terms
+    before lowering them; the GPU lowers every (point, term) pair)."""
+    _, CE, _ = _need_gpu()
+    prob, (rp, bp), updates, X, F = G.load_cpdfnd(name)
+    est = _stepped_gpu(CE, prob, rp, bp, updates)
+    got = est.cpdf_nd(X)
+    assert G.relerr(got, F) <= G.REL_TOL, (name, G.relerr(got, F))
+    # one point at a time gives the same values
+    one = np.array([est.cpdf_nd(x)[0] for x in X[:3]])
+    assert G.bitwise_equal(one, got[:3])
+    assert est.device_errors() == 0
+    est.close()
+
+
+def test_gpu_nd_pdf_against_oracle_on_larger_estimators():
+    """Larger term sets than the fixtures (a 4-state estimator after 6 updates,
+    a 5-state two-measurement one after 5, a 3-state one after 8): the GPU
+    against the oracle's restatement (bit-exact with the reference) at 64
+    points each, and the status of the calls the reference refuses."""
+    _, CE, _lib = _need_gpu()
+    from cauchyfriendly_gb300 import workloads as W
+    cases = [(W.four_state_lti(seed=11, steps=7), 6), (W.five_state_two_msmt(seed=12, steps=4), 5),
+             (W.many_gamma(3, 1, 9, seed=13), 8)]
+    for prob, updates in cases:
+        rp, bp = oracle.draw_reference_constants(21, prob["d"], oracle.max_shape_of(prob))
+        est = _stepped_gpu(CE, prob, rp, bp, updates)
+        orc = oracle.Oracle(prob, rp, bp)
+        for k, s in _updates(prob)[:updates]:
+            orc.step(k, s)
+        if orc.errors():
+            est.close()
+            orc.close()
+            continue
+        mo = orc.moments()
+        mu = mo["mean"].real
+        sd = np.sqrt(np.abs(np.diag(mo["cov"].real)))
+        rng = np.random.Generator(np.random.PCG64(3))
+        X = mu + sd * rng.standard_normal((64, prob["d"])) * np.repeat([0.5, 1.5, 4.0, 10.0], 16)[:, None]
+        got = est.cpdf_nd(X)
+        want = np.array([orc.cpdf_nd(x) for x in X])
+        assert G.relerr(got, want) <= G.REL_TOL, (prob["d"], updates, est.num_terms(), G.relerr(got, want))
+        est.close()
+        orc.close()
+    # before the first step and after the last one
+    prob = W.four_state_lti(seed=1, steps=2)
+    rp, bp = oracle.draw_reference_constants(22, 4, oracle.max_shape_of(prob))
+    est = CE(prob["A0"], prob["p0"], prob["b0"], 2, 4, 0, 1, 1, root_point=rp, b_pert=bp)
+    with pytest.raises(_lib.MceError):
+        est.cpdf_nd(np.zeros(4))
+    for k in range(2):
+        est.step(prob["msmts"][k, 0], prob["Phi"], prob["Gamma"], prob["beta"], prob["H"][0], prob["gamma"][0])
+    with pytest.raises(_lib.MceError):
+        est.cpdf_nd(np.zeros(4))
+    est.close()

@@ -53,3 +53,24 @@ def test_oracle_cpdf2d_matches_reference_grids(name):
         assert np.array_equal(xo, x) and np.array_equal(yo, y), (i1, i2, call)
         assert G.relerr(zo, z) <= G.REL_TOL, (i1, i2, call, G.relerr(zo, z))
     est.close()
+
+
+@pytest.mark.parametrize("name", G.cpdfnd_names())
+def test_oracle_nd_pdf_matches_reference_bitwise(name):
+    """The oracle's N-D pdf (PointWiseNDimCauchyCPDF::evaluate_cpdf, with the
+    reference's lowering, term reduction and g-tables) gives the reference's
+    values bit for bit (tests/golden/cpdfnd_*.npz)."""
+    prob, consts, updates, X, F = G.load_cpdfnd(name)
+    est = _stepped_oracle(prob, consts, updates)
+    got = np.array([est.cpdf_nd(x) for x in X])
+    est.close()
+    assert G.bitwise_equal(got, F), (name, G.relerr(got, F))
+
+
+def test_oracle_nd_pdf_refuses_before_the_first_step():
+    from cauchyfriendly_gb300 import workloads as W
+    prob = W.four_state_lti(seed=0, steps=3)
+    est = oracle.Oracle(prob, *oracle.draw_reference_constants(5, 4, oracle.max_shape_of(prob)))
+    with pytest.raises(RuntimeError):
+        est.cpdf_nd(np.zeros(4))
+    est.close()
