@@ -761,6 +761,9 @@ int nd_level_dispatch(int LD, NdWork& w, NdTerms P, const int* pkeys, const cd* 
 
 }  // namespace
 
+int nd_pdf_chunk(const NdInput& in, const double* x_host, int npts, double* out_host, NdWork& w,
+                 const LaunchCfg& lc);
+
 int nd_pdf_eval(const NdInput& in, const double* x_host, int npts, double* out_host, NdWork* w, const LaunchCfg& lc,
                 long long* launches)
 {
@@ -770,6 +773,28 @@ int nd_pdf_eval(const NdInput& in, const double* x_host, int npts, double* out_h
         return MCE_ERR_SHAPE;
     }
     const int D = in.D, MC = in.MC;
+    if (D == 1) {
+        report_error("N-D pdf: one-dimensional estimators use the marginal 1-D pdf");
+        return MCE_ERR_ARG;
+    }
+    // points in chunks of about 2^20 (point, term) pairs: every lowering
+    // multiplies the pairs by the rows of their terms
+    const long long per = std::max<long long>(1, (1LL << 20) / std::max<long long>(1, in.n));
+    w->launches = 0;
+    for (long long p0 = 0; p0 < npts; p0 += per) {
+        const int np = (int)std::min<long long>(per, npts - p0);
+        const int s = nd_pdf_chunk(in, x_host + p0 * D, np, out_host + 2 * p0, *w, lc);
+        if (s) return s;
+    }
+    if (launches) *launches += w->launches;
+    return MCE_OK;
+}
+
+int nd_pdf_chunk(const NdInput& in, const double* x_host, int npts, double* out_host, NdWork& wr,
+                 const LaunchCfg& lc)
+{
+    NdWork* w = &wr;
+    const int D = in.D, MC = in.MC;
     int s;
     if ((s = w->x.ensure((size_t)npts * D))) return s;
     if ((s = w->out.ensure((size_t)2 * npts))) return s;
@@ -777,7 +802,6 @@ int nd_pdf_eval(const NdInput& in, const double* x_host, int npts, double* out_h
     ND_CUDA(cudaMemcpyAsync(w->x.ptr, x_host, sizeof(double) * npts * D, cudaMemcpyHostToDevice, lc.stream));
     ND_CUDA(cudaMemsetAsync(w->err.ptr, 0, sizeof(int), lc.stream));
     ND_CUDA(cudaMemsetAsync(w->out.ptr, 0, sizeof(double) * 2 * npts, lc.stream));
-    w->launches = 0;
     // level 0: the estimator's own terms and tables, shared by every point
     NdTerms P{nullptr, const_cast<int*>(in.m), const_cast<double*>(in.A), const_cast<double*>(in.p),
               const_cast<double*>(in.b), const_cast<long long*>(in.toff), const_cast<int*>(in.tcnt)};
@@ -809,12 +833,6 @@ int nd_pdf_eval(const NdInput& in, const double* x_host, int npts, double* out_h
         if (n == 0) empty = true;
     }
     if (!empty) {
-        if (D == 1) {
-            // a one-dimensional estimator integrates its own terms; they are shared by every point,
-            // each term's b shifted by the point
-            report_error("N-D pdf: one-dimensional estimators use the marginal 1-D pdf");
-            return MCE_ERR_ARG;
-        }
         // pow(RECIPRICAL_TWO_PI, dim) (cpdf_ndim.hpp:893)
         const double sc = pow(1.0 / (2.0 * M_PI), (double)D);
         const int thr = 128;
@@ -824,7 +842,6 @@ int nd_pdf_eval(const NdInput& in, const double* x_host, int npts, double* out_h
     }
     ND_CUDA(cudaMemcpyAsync(out_host, w->out.ptr, sizeof(double) * 2 * npts, cudaMemcpyDeviceToHost, lc.stream));
     ND_CUDA(cudaStreamSynchronize(lc.stream));
-    if (launches) *launches += w->launches;
     return MCE_OK;
 }
 
