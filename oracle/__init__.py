@@ -405,10 +405,11 @@ class Oracle(_EstimatorBase):
             raise RuntimeError("orc_cpdf_1d_grid returned %d" % n)
         return xs[:n].copy(), ys[:n].copy()
 
-    def cpdf_nd(self, x):
+    def cpdf_nd(self, x, reduce=True):
         """The N-D conditional pdf at the point x (complex; the reference's
-        PointWiseNDimCauchyCPDF::evaluate_cpdf)."""
-        return _cpdf_nd_call(self._l.lib.orc_cpdf_nd, self.h, x, "orc_cpdf_nd")
+        PointWiseNDimCauchyCPDF::evaluate_cpdf).  reduce=False keeps every
+        lowered child apart (no term reduction between the lowerings)."""
+        return _cpdf_nd_call(self._l.lib.orc_cpdf_nd, self.h, x, "orc_cpdf_nd", 1 if reduce else 0)
 
 
 class OracleSlot:
@@ -512,7 +513,7 @@ class Reference(_EstimatorBase):
 
     def cpdf_nd(self, x):
         """The reference's own PointWiseNDimCauchyCPDF::evaluate_cpdf at x."""
-        return _cpdf_nd_call(self._l.lib.ref_cpdf_nd, self.h, x, "ref_cpdf_nd")
+        return _cpdf_nd_call(self._l.lib.ref_cpdf_nd, self.h, x, "ref_cpdf_nd", None)
 
     def cpdf_1d_grid(self, marg, low, high, res, max_points=100000):
         """The reference's own marginal 1-D pdf grid; returns (x, y, bar_nu)."""
@@ -528,12 +529,12 @@ class Reference(_EstimatorBase):
 
 
 
-def _cpdf_nd_call(f, h, x, name):
+def _cpdf_nd_call(f, h, x, name, reduce):
     f.restype = ctypes.c_int
-    f.argtypes = [ctypes.c_void_p, _dp, _dp]
+    f.argtypes = [ctypes.c_void_p, _dp, _dp] + ([] if reduce is None else [ctypes.c_int])
     xx = _arr(x)
     out = np.zeros(2)
-    st = f(h, _ptr(xx), _ptr(out))
+    st = f(h, _ptr(xx), _ptr(out)) if reduce is None else f(h, _ptr(xx), _ptr(out), reduce)
     if st < 0:
         raise RuntimeError("%s returned %d" % (name, st))
     return complex(out[0], out[1])

@@ -1512,7 +1512,7 @@ static void lower_children(const Term& P, int ld, const double* xk, std::vector<
 // Returns 0 and the complex value, or -1 before the first step / with
 // moment errors (the reference asserts), -3 when a lowered child
 // anti-coaligns two unintegrable rows (the reference exits).
-static int cpdf_nd_eval(Estimator& E, const double* xk, cplx* out)
+static int cpdf_nd_eval(Estimator& E, const double* xk, cplx* out, bool reduce = true)
 {
     if (E.master_step < 1 || E.errors) return -1;
     const int dim = E.d;
@@ -1544,7 +1544,9 @@ static int cpdf_nd_eval(Estimator& E, const double* xk, cplx* out)
         for (int m = 0; m < shape_range; m++) {
             if (byshape[m].empty() || m < dl) continue;
             std::vector<int> F;
-            ftr(byshape[m], dl, F);
+            if (reduce) ftr(byshape[m], dl, F);
+            else
+                for (size_t i = 0; i < byshape[m].size(); i++) F.push_back((int)i);
             std::vector<Term*> roots;
             make_gtables_shape(byshape[m], F, dl, 1.0, roots, true);
             for (Term* r : roots) next[m].push_back(std::move(*r));
@@ -2209,11 +2211,13 @@ void orc_finalize_extended_moments(void* h, double* x_bar)
 // evaluate_point_grid (cpdf_ndim.hpp:2055-2139).  Returns the point count, -2
 // if it exceeds max_points, -1 before the first step, -5 at the last step
 // (its g-tables are skipped).
-// the N-D conditional pdf at x[d]; out[2] = (re, im)
-int orc_cpdf_nd(void* h, const double* x, double* out)
+// the N-D conditional pdf at x[d]; out[2] = (re, im).  reduce 0 skips the
+// term reduction between the lowerings (every lowered child kept apart: the
+// same sum up to rounding), for comparisons with the GPU's formulation.
+int orc_cpdf_nd(void* h, const double* x, double* out, int reduce)
 {
     cplx v;
-    const int st = cpdf_nd_eval(*(Estimator*)h, x, &v);
+    const int st = cpdf_nd_eval(*(Estimator*)h, x, &v, reduce != 0);
     if (st == 0) {
         out[0] = __real__ v;
         out[1] = __imag__ v;

@@ -117,14 +117,18 @@ def _stepped_gpu(CE, prob, rp, bp, updates):
 def test_gpu_nd_pdf_matches_reference(name):
     """mce_cpdf_nd at all of a fixture's points in one call against the
     reference's PointWiseNDimCauchyCPDF::evaluate_cpdf (tests/golden/
-    cpdfnd_*.npz, values from 1e-16 to 35): within 1e-9 element-wise, the
-    floor 1e-12 of the largest value (the reference merges nearly equal terms
-    before lowering them; the GPU lowers every (point, term) pair)."""
+    cpdfnd_*.npz, values from 1e-16 to 35): within 1e-9 relative wherever the
+    pdf is above 1e-3 of its largest value, within 1e-12 of that largest
+    value below.  The reference adds the g-tables of lowered terms whose
+    arrangements agree within REDUCTION_EPS (1e-8) and lowers the sum once;
+    the GPU lowers every (point, term) pair, and the oracle doing the same
+    differs from the reference by up to 3e-12 relative above 1e-3 of the peak
+    and 2.2e-14 of the peak below (the gap the floor covers)."""
     _, CE, _ = _need_gpu()
     prob, (rp, bp), updates, X, F = G.load_cpdfnd(name)
     est = _stepped_gpu(CE, prob, rp, bp, updates)
     got = est.cpdf_nd(X)
-    assert G.relerr(got, F) <= G.REL_TOL, (name, G.relerr(got, F))
+    assert G.relerr(got, F, floor=1e-3) <= G.REL_TOL, (name, G.relerr(got, F, floor=1e-3))
     # one point at a time gives the same values
     one = np.array([est.cpdf_nd(x)[0] for x in X[:3]])
     assert G.bitwise_equal(one, got[:3])
@@ -135,8 +139,11 @@ def test_gpu_nd_pdf_matches_reference(name):
 def test_gpu_nd_pdf_against_oracle_on_larger_estimators():
     """Larger term sets than the fixtures (a 4-state estimator after 6 updates,
     a 5-state two-measurement one after 5, a 3-state one after 8): the GPU
-    against the oracle's restatement (bit-exact with the reference) at 64
-    points each, and the status of the calls the reference refuses."""
+    against the oracle lowering every child apart as the GPU does (within
+    1e-9 element-wise, floor 1e-12 of the largest value: only the order of
+    the final sum differs) and against the oracle with the reference's term
+    reduction (the fixture tolerance), at 64 points each; and the status of
+    the calls the reference refuses."""
     _, CE, _lib = _need_gpu()
     from cauchyfriendly_gb300 import workloads as W
     cases = [(W.four_state_lti(seed=11, steps=7), 6), (W.five_state_two_msmt(seed=12, steps=4), 5),
@@ -157,8 +164,10 @@ def test_gpu_nd_pdf_against_oracle_on_larger_estimators():
         rng = np.random.Generator(np.random.PCG64(3))
         X = mu + sd * rng.standard_normal((64, prob["d"])) * np.repeat([0.5, 1.5, 4.0, 10.0], 16)[:, None]
         got = est.cpdf_nd(X)
+        apart = np.array([orc.cpdf_nd(x, reduce=False) for x in X])
+        assert G.relerr(got, apart) <= G.REL_TOL, (prob["d"], updates, est.num_terms(), G.relerr(got, apart))
         want = np.array([orc.cpdf_nd(x) for x in X])
-        assert G.relerr(got, want) <= G.REL_TOL, (prob["d"], updates, est.num_terms(), G.relerr(got, want))
+        assert G.relerr(got, want, floor=1e-3) <= G.REL_TOL, (prob["d"], G.relerr(got, want, floor=1e-3))
         est.close()
         orc.close()
     # before the first step and after the last one
