@@ -139,13 +139,13 @@ def test_gpu_nd_pdf_matches_reference(name):
 def test_gpu_nd_pdf_against_oracle_on_larger_estimators():
     """Larger term sets than the fixtures (a 4-state estimator after 6 updates,
     a 5-state two-measurement one after 5, a 3-state one after 8): the GPU
-    against the oracle lowering every child apart as the GPU does and
-    against the oracle with the reference's term reduction, at 64 points
-    each out to 10 standard deviations, both within 1e-9 relative above 1e-3
-    of the largest value and 1e-12 of it below (the values are sums of
-    10^4-10^6 terms as large as the peak: an order of summation moves a
-    far-tail value of 1e-15 by a few 1e-14); and the status of the calls the
-    reference refuses."""
+    at 64 points each out to 10 standard deviations in one call, against the
+    oracle with the reference's term reduction at 8 of them (two per scale)
+    and the oracle lowering every child apart as the GPU does at 2 (it is
+    slow), both within 1e-9 relative above 1e-3 of the largest value and
+    1e-12 of it below (the values are sums of 10^4-10^6 terms as large as the
+    peak: an order of summation moves a far-tail value of 1e-15 by a few
+    1e-14); and the status of the calls the reference refuses."""
     _, CE, _lib = _need_gpu()
     from cauchyfriendly_gb300 import workloads as W
     cases = [(W.four_state_lti(seed=11, steps=7), 6), (W.five_state_two_msmt(seed=12, steps=4), 5),
@@ -166,11 +166,13 @@ def test_gpu_nd_pdf_against_oracle_on_larger_estimators():
         rng = np.random.Generator(np.random.PCG64(3))
         X = mu + sd * rng.standard_normal((64, prob["d"])) * np.repeat([0.5, 1.5, 4.0, 10.0], 16)[:, None]
         got = est.cpdf_nd(X)
-        apart = np.array([orc.cpdf_nd(x, reduce=False) for x in X])
-        assert G.relerr(got, apart, floor=1e-3) <= G.REL_TOL, (prob["d"], updates, est.num_terms(),
-                                                              G.relerr(got, apart, floor=1e-3))
-        want = np.array([orc.cpdf_nd(x) for x in X])
-        assert G.relerr(got, want, floor=1e-3) <= G.REL_TOL, (prob["d"], G.relerr(got, want, floor=1e-3))
+        peak = float(np.max(np.abs(got)))
+        pick = [0, 1, 16, 17, 32, 33, 48, 49]
+        want = np.array([orc.cpdf_nd(X[i]) for i in pick])
+        apart = np.array([orc.cpdf_nd(X[i], reduce=False) for i in pick[:2]])
+        close = lambda a, b: np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-3 * peak))
+        assert close(got[pick], want) <= G.REL_TOL, (prob["d"], updates, est.num_terms(), close(got[pick], want))
+        assert close(got[pick[:2]], apart) <= G.REL_TOL, (prob["d"], close(got[pick[:2]], apart))
         est.close()
         orc.close()
     # before the first step and after the last one
