@@ -55,10 +55,12 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the one-estimator-per-handle comparison")
     ap.add_argument("--plain-stride", type=int, default=16)
     ap.add_argument("--adjoint-steps", type=int, default=100)
-    ap.add_argument("--workload", default="batched3", choices=["batched3", "windows5", "rel2d", "adjoint"],
+    ap.add_argument("--workload", default="batched3", choices=["batched3", "windows5", "rel2d", "adjoint", "cpdfnd"],
                     help="batched3: the batched 3-state configuration (default); windows5: the sliding-window "
                          "5-state LTV configuration for --window-steps steps; rel2d: the relative 2-D system of "
-                         "two 5-state estimators")
+                         "two 5-state estimators; cpdfnd: the N-D conditional pdf of a 4-state estimator at "
+                         "--nd-points points")
+    ap.add_argument("--nd-points", type=int, default=256)
     ap.add_argument("--window-steps", type=int, default=12)
     ap.add_argument("--rel-updates", type=int, default=6, help="rel2d: updates of both estimators (6: 12.2 M pairs)")
     return ap.parse_args()
@@ -570,6 +572,109 @@ def run_rel2d(args):
     print(json.dumps(line), flush=True)
 
 
+def _nd_problem():
+    from cauchyfriendly_gb300 import workloads as W
+    return W.four_state_lti(seed=11, steps=7), 6
+
+
+def _nd_points(mo, d, n):
+    mu = mo["mean"].real
+    sd = np.sqrt(np.abs(np.diag(mo["cov"].real)))
+    rng = np.random.Generator(np.random.PCG64(3))
+    return mu + sd * rng.standard_normal((n, d)) * np.resize([0.5, 1.5, 4.0], n)[:, None]
+
+
+def _nd_cpu_share(job):
+    """One process's share of the N-D pdf baseline: the reference's own
+    estimator (oracle/_ref, serial build) stepped like the GPU's, then
+    PointWiseNDimCauchyCPDF::evaluate_cpdf at its points; (points, seconds)."""
+    import oracle
+    seed, X = job
+    prob, updates = _nd_problem()
+    ref = oracle.Reference(prob, seed=seed)
+    n = 0
+    for k in range(prob["steps"]):
+        for s in range(prob["p"]):
+            if n < updates:
+                ref.step(k, s)
+                n += 1
+    t0 = time.perf_counter()
+    for x in X:
+        ref.cpdf_nd(x)
+    t1 = time.perf_counter() - t0
+    ref.close()
+    return len(X), t1
+
+
+def run_cpdfnd(args):
+    """The N-D conditional pdf (PointWiseNDimCauchyCPDF::evaluate_cpdf) of a
+    4-state LTI estimator after 6 updates (3,428 terms) at --nd-points points
+    around its mean (0.5, 1.5 and 4 standard deviations) per step, through
+    mce_cpdf_nd (one call, host points in, host values out): points/s over
+    the wall clock of the call (value and e2e; the call synchronises between
+    its lowering levels).  CPU baseline: the reference's own evaluate_cpdf,
+    one process per host core, each on its share of a point sample."""
+    import torch
+    import oracle
+    from cauchyfriendly_gb300 import CauchyEstimator
+    torch.cuda.set_device(0)
+    prob, updates = _nd_problem()
+    ref = oracle.Reference(prob, seed=77) if os.path.exists(os.path.join(oracle.REF_OUT, "libmce_ref_serial.so")) \
+        else None
+    if ref is not None:
+        rp, bp = ref.constants()
+        ref.close()
+    else:
+        rp, bp = oracle.draw_reference_constants(77, prob["d"], oracle.max_shape_of(prob))
+    est = CauchyEstimator(prob["A0"], prob["p0"], prob["b0"], prob["steps"], prob["d"], 0, prob["pncc"], prob["p"],
+                          root_point=rp, b_pert=bp)
+    n = 0
+    for k in range(prob["steps"]):
+        for s in range(prob["p"]):
+            if n < updates:
+                est.step(prob["msmts"][k, s], prob["Phi"], prob["Gamma"], prob["beta"], prob["H"][s],
+                         prob["gamma"][s])
+                n += 1
+    X = _nd_points(est.moments(), prob["d"], args.nd_points)
+    for _ in range(args.warmup):
+        est.cpdf_nd(X)
+    torch.cuda.synchronize()
+    clk = ClockSampler()
+    clk.start()
+    l0 = int(est._lib.mce_launch_count(est._h))
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        est.cpdf_nd(X)
+    wall = (time.perf_counter() - t0) / args.steps
+    launches = int(est._lib.mce_launch_count(est._h)) - l0
+    clocks = clk.stop()
+    line = {"metric": "N-D conditional pdf points/s (FP64, PointWiseNDimCauchyCPDF::evaluate_cpdf)",
+            "value": len(X) / wall, "unit": "points/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": wall * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "4-state LTI estimator after 6 updates (%d terms), %d points at 0.5/1.5/4 "
+                                   "standard deviations" % (est.num_terms(), len(X))},
+            "e2e": {"value": len(X) / wall, "unit": "points/s", "h2d_bytes_per_step": int(X.nbytes),
+                    "d2h_bytes_per_step": int(16 * len(X)), "wall_s_per_step": wall},
+            "gpu_launches": launches, "clocks": clocks,
+            "note": "value and e2e are both the wall clock of mce_cpdf_nd (it reads sizes back between levels)"}
+    if not args.no_cpu_baseline and ref is not None:
+        import multiprocessing as mp
+        cores = os.cpu_count() or 1
+        # about cpu_seconds of work: 0.5 s a point on one core
+        per = max(1, int(args.cpu_seconds / 0.5))
+        Xs = _nd_points(est.moments(), prob["d"], per * cores)
+        with mp.get_context("spawn").Pool(cores) as pool:
+            res = pool.map(_nd_cpu_share, [(77, Xs[i * per:(i + 1) * per]) for i in range(cores)])
+        done = sum(r[0] for r in res)
+        slowest = max(r[1] for r in res)
+        line["cpu_baseline"] = {"value": done / slowest, "unit": "points/s", "cores": cores, "kind": "reference",
+                                "sample": "%d processes, %d points each (the same estimator and point "
+                                          "distribution), slowest %.1f s" % (cores, per, slowest)}
+    est.close()
+    print(json.dumps(line), flush=True)
+
+
 def _rel2d_cpu_share(job):
     """One process's share of the relative-system CPU baseline: the oracle's
     two estimators stepped as the GPU ones, then every stride-th pair from
@@ -618,6 +723,9 @@ def main():
         return
     if args.workload == "adjoint":
         run_adjoint(args)
+        return
+    if args.workload == "cpdfnd":
+        run_cpdfnd(args)
         return
     import torch
     rank = int(os.environ.get("RANK", "0"))

@@ -777,9 +777,13 @@ int nd_pdf_eval(const NdInput& in, const double* x_host, int npts, double* out_h
         report_error("N-D pdf: one-dimensional estimators use the marginal 1-D pdf");
         return MCE_ERR_ARG;
     }
-    // points in chunks of about 2^20 (point, term) pairs: every lowering
-    // multiplies the pairs by the rows of their terms
-    const long long per = std::max<long long>(1, (1LL << 20) / std::max<long long>(1, in.n));
+    // points in chunks: every lowering multiplies the terms by their rows
+    // (at most MC, MC - 1, ...), so the first level's (point, term) pairs are
+    // bounded such that the last level stays under about 2^26 children
+    double growth = 1.0;
+    for (int l = 0; l < D - 1; l++) growth *= std::max(1, MC - l);
+    const double budget = (double)(1LL << 26) / growth;
+    const long long per = std::max<long long>(1, (long long)(budget / (double)std::max<long long>(1, in.n)));
     w->launches = 0;
     for (long long p0 = 0; p0 < npts; p0 += per) {
         const int np = (int)std::min<long long>(per, npts - p0);
