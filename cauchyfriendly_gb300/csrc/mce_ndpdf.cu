@@ -590,31 +590,44 @@ __global__ void k_nd_keep_int(const NdKids K, long long nk, int* keep_i)
         keep_i[c] = K.keep[c] && K.ccnt[c] > 0 ? 1 : 0;
 }
 
-// evaluate_1d_cf summed over each point's one-dimensional terms (a warp per
-// point; the terms of a point are contiguous), then / Re fz * (2 pi)^-d.
-__global__ void k_nd_final(NdTerms T, long long n, int MC, const int* keys, const cd* vals, int npts, double fz,
-                           double scale, double* out)
+// The first term of every point (terms are point-major): pstart[p] =
+// lower_bound(pt, p), p = 0..npts.
+__global__ void k_nd_point_starts(const int* pt, long long n, int npts, long long* pstart)
 {
-    const int lane = threadIdx.x & 31;
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (w >= npts) return;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p > npts) return;
     long long lo = 0, hi = n;
     while (lo < hi) {
         const long long mid = (lo + hi) >> 1;
-        if (T.pt[mid] < w) lo = mid + 1;
+        if (pt[mid] < p) lo = mid + 1;
         else hi = mid;
     }
-    long long a = lo;
-    lo = a;
-    hi = n;
-    while (lo < hi) {
-        const long long mid = (lo + hi) >> 1;
-        if (T.pt[mid] < w + 1) lo = mid + 1;
+    pstart[p] = lo;
+}
+
+constexpr int kNdFinalThreads = 256;
+constexpr long long kNdFinalChunk = 1LL << 14;  // terms per block of the final sum
+
+// evaluate_1d_cf (cpdf_ndim.hpp:643-666) summed over a chunk of one point's
+// one-dimensional terms; block b takes chunk b - coff[p] of point p (coff:
+// exclusive scan of the points' chunk counts).  Fixed-order tree sums: the
+// result does not depend on the launch.
+__global__ void k_nd_final_partial(NdTerms T, int MC, const int* keys, const cd* vals, const long long* pstart,
+                                   const long long* coff, int npts, cd* partial)
+{
+    __shared__ double sre[kNdFinalThreads], sim[kNdFinalThreads];
+    const long long b = blockIdx.x;
+    int lo = 0, hi = npts;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (coff[mid] <= b) lo = mid;
         else hi = mid;
     }
-    const long long e = lo;
+    const int p = lo;
+    const long long a = pstart[p] + (b - coff[p]) * kNdFinalChunk;
+    const long long e = min(pstart[p + 1], a + kNdFinalChunk);
     cd s = mkcd(0, 0);
-    for (long long i = a + lane; i < e; i += 32) {
+    for (long long i = a + threadIdx.x; i < e; i += kNdFinalThreads) {
         const bool pos_a = T.A[i * MC] > 0;  // A is [MC][1]: row 0 of term i
         const int lp = pos_a ? 1 : 0, lm = pos_a ? 0 : 1;
         const int* k = keys + T.toff[i];
@@ -625,14 +638,30 @@ __global__ void k_nd_final(NdTerms T, long long n, int MC, const int* keys, cons
         const double p0 = T.p[i * MC], b0 = T.b[i];
         s = cadd(s, csub(cdiv(gp, mkcd(p0, b0)), cdiv(gm, mkcd(-p0, b0))));
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        s.re += __shfl_down_sync(0xffffffffu, s.re, o);
-        s.im += __shfl_down_sync(0xffffffffu, s.im, o);
+    sre[threadIdx.x] = s.re;
+    sim[threadIdx.x] = s.im;
+    __syncthreads();
+    for (int o = kNdFinalThreads / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            sre[threadIdx.x] += sre[threadIdx.x + o];
+            sim[threadIdx.x] += sim[threadIdx.x + o];
+        }
+        __syncthreads();
     }
-    if (lane == 0) {
-        out[2 * w] = s.re / fz * scale;
-        out[2 * w + 1] = s.im / fz * scale;
-    }
+    if (threadIdx.x == 0) partial[b] = mkcd(sre[0], sim[0]);
+}
+
+// Each point's chunk sums in order, then / Re fz * (2 pi)^-d
+// (cpdf_ndim.hpp:892-893).
+__global__ void k_nd_final_combine(const cd* partial, const long long* coff, int npts, double fz, double scale,
+                                   double* out)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npts) return;
+    cd s = mkcd(0, 0);
+    for (long long c = coff[p]; c < coff[p + 1]; c++) s = cadd(s, partial[c]);
+    out[2 * p] = s.re / fz * scale;
+    out[2 * p + 1] = s.im / fz * scale;
 }
 
 }  // namespace
@@ -645,6 +674,9 @@ struct NdWork {
     NdBuf<long long> coff, cellof, kscan, scan_tmp;
     NdBuf<double> x, out;
     NdBuf<int> err;
+    NdBuf<long long> pstart, pcoff;
+    NdBuf<cd> partial;
+    std::vector<long long> h_pstart, h_pcoff;
     ScanScratch ss{};
     long long launches = 0;
     int ensure_scan(long long n)
@@ -839,10 +871,29 @@ int nd_pdf_chunk(const NdInput& in, const double* x_host, int npts, double* out_
     if (!empty) {
         // pow(RECIPRICAL_TWO_PI, dim) (cpdf_ndim.hpp:893)
         const double sc = pow(1.0 / (2.0 * M_PI), (double)D);
-        const int thr = 128;
-        const int blocks = (int)(((long long)npts * 32 + thr - 1) / thr);
-        k_nd_final<<<blocks, thr, 0, lc.stream>>>(P, n, MC, pkeys, pvals, npts, in.fz, sc, w->out.ptr);
-        w->launches += 1;
+        if ((s = w->pstart.ensure(npts + 1))) return s;
+        if ((s = w->pcoff.ensure(npts + 1))) return s;
+        k_nd_point_starts<<<(npts + 1 + 127) / 128, 128, 0, lc.stream>>>(P.pt, n, npts, w->pstart.ptr);
+        w->h_pstart.resize(npts + 1);
+        ND_CUDA(cudaMemcpyAsync(w->h_pstart.data(), w->pstart.ptr, sizeof(long long) * (npts + 1),
+                                cudaMemcpyDeviceToHost, lc.stream));
+        ND_CUDA(cudaStreamSynchronize(lc.stream));
+        w->h_pcoff.assign(npts + 1, 0);
+        for (int p = 0; p < npts; p++) {
+            const long long cnt = w->h_pstart[p + 1] - w->h_pstart[p];
+            w->h_pcoff[p + 1] = w->h_pcoff[p] + (cnt + kNdFinalChunk - 1) / kNdFinalChunk;
+        }
+        const long long nb = w->h_pcoff[npts];
+        ND_CUDA(cudaMemcpyAsync(w->pcoff.ptr, w->h_pcoff.data(), sizeof(long long) * (npts + 1),
+                                cudaMemcpyHostToDevice, lc.stream));
+        if (nb > 0) {
+            if ((s = w->partial.ensure(nb + 1))) return s;
+            k_nd_final_partial<<<(unsigned)nb, kNdFinalThreads, 0, lc.stream>>>(P, MC, pkeys, pvals, w->pstart.ptr,
+                                                                                 w->pcoff.ptr, npts, w->partial.ptr);
+        }
+        k_nd_final_combine<<<(npts + 127) / 128, 128, 0, lc.stream>>>(w->partial.ptr, w->pcoff.ptr, npts, in.fz, sc,
+                                                                     w->out.ptr);
+        w->launches += nb > 0 ? 3 : 2;
     }
     ND_CUDA(cudaMemcpyAsync(out_host, w->out.ptr, sizeof(double) * 2 * npts, cudaMemcpyDeviceToHost, lc.stream));
     ND_CUDA(cudaStreamSynchronize(lc.stream));
