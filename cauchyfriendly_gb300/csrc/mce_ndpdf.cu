@@ -280,105 +280,130 @@ __device__ int nd_coalign(double* A, double* p, double* q, unsigned& hor, int m,
     return ns;
 }
 
-// The lowered children of each (point, parent) pair, coaligned, written from
-// coff[i] on.  x: the points [npts][D] on the first level, else null.
+// The lowered children, coaligned, a thread per child: child c belongs to
+// the pair i whose children start at coff[i] <= c, and integrates the
+// (c - coff[i])-th of its parent's rows with a nonzero last component.
+// x: the points [npts][D] on the first level, else null.
 template <int LD>
 __global__ void k_nd_lower(NdTerms P, long long n, long long npairs, const double* x, int D, const long long* coff,
-                           int MC, NdKids K, int* err)
+                           long long nk, int MC, NdKids K, int* err)
 {
     constexpr int LC = LD - 1;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npairs;
-         i += (long long)gridDim.x * blockDim.x) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < nk;
+         c += (long long)gridDim.x * blockDim.x) {
+        long long lo = 0, hi = npairs;
+        while (hi - lo > 1) {
+            const long long mid = (lo + hi) >> 1;
+            if (coff[mid] <= c) lo = mid;
+            else hi = mid;
+        }
+        const long long i = lo;
+        const int ord = (int)(c - coff[i]);
         const long long t = i % n;
         const int m = P.m[t];
-        if (m < LD) continue;
         const int pt = x ? (int)(i / n) : P.pt[t];
         const double* A = P.A + t * MC * LD;
         const double* pp = P.p + t * MC;
         const double* bb = P.b + t * LD;
-        double Alp[kNdMaxRows * (LC > 0 ? LC : 1)], Ald[kNdMaxRows], plp[kNdMaxRows];
+        // construct_lowered_parent_elements (cpdf_ndim.hpp:392-443)
+        double Ald[kNdMaxRows];
         bool nz[kNdMaxRows];
-        int lam = 0;
+        int lam = 0, tz = 0, k = 0;
         for (int r = 0; r < m; r++) {
             Ald[r] = -A[r * LD + LD - 1];
             nz[r] = fabs(Ald[r]) > kMuEps;
-        }
-        for (int r = 0; r < m; r++) {
             if (nz[r]) {
-                for (int j = 0; j < LC; j++) Alp[r * LC + j] = A[r * LD + j] / Ald[r];
                 if (Ald[r] < 0) lam |= 1 << r;
-                plp[r] = pp[r] * fabs(Ald[r]);
-            } else {
-                for (int j = 0; j < LC; j++) Alp[r * LC + j] = A[r * LD + j];
-                plp[r] = pp[r];
+                if (k++ == ord) tz = r;
             }
         }
-        double blp[LC > 0 ? LC : 1], tb;
+        double mu_t[LC > 0 ? LC : 1];
+        for (int j = 0; j < LC; j++) mu_t[j] = A[tz * LD + j] / Ald[tz];
+        double tb;
+        double* bo = K.b + c * LC;
         if (x) {
             const double* xp = x + (long long)pt * D;
-            for (int j = 0; j < LC; j++) blp[j] = bb[j] - xp[j];
             tb = bb[LC] - xp[LC];
+            for (int j = 0; j < LC; j++) bo[j] = (bb[j] - xp[j]) + tb * mu_t[j];
         } else {
-            for (int j = 0; j < LC; j++) blp[j] = bb[j];
             tb = bb[LC];
+            for (int j = 0; j < LC; j++) bo[j] = bb[j] + tb * mu_t[j];
         }
-        long long c = coff[i];
-        for (int tz = 0; tz < m; tz++) {
-            if (!nz[tz]) continue;
-            double Ac[kNdMaxRows * (LC > 0 ? LC : 1)], pc[kNdMaxRows], qc[kNdMaxRows];
-            const double* mu_t = Alp + tz * LC;
-            int l_ = 0;
-            unsigned unint = 0;
-            for (int l = 0; l < m; l++) {
-                if (l == tz) continue;
-                const double* mu_l = Alp + l * LC;
-                if (nz[l]) {
-                    for (int j = 0; j < LC; j++) Ac[l_ * LC + j] = mu_l[j] - mu_t[j];
-                } else {
-                    for (int j = 0; j < LC; j++) Ac[l_ * LC + j] = mu_l[j];
-                    unint |= 1u << l_;
-                }
-                pc[l_] = plp[l];
-                l_++;
+        // construct_lowered_children (cpdf_ndim.hpp:579-636): rows mu_l - mu_t
+        double Ac[kNdMaxRows * (LC > 0 ? LC : 1)], pc[kNdMaxRows], qc[kNdMaxRows];
+        int l_ = 0;
+        unsigned unint = 0;
+        for (int l = 0; l < m; l++) {
+            if (l == tz) continue;
+            if (nz[l]) {
+                for (int j = 0; j < LC; j++) Ac[l_ * LC + j] = A[l * LD + j] / Ald[l] - mu_t[j];
+                pc[l_] = pp[l] * fabs(Ald[l]);
+            } else {
+                for (int j = 0; j < LC; j++) Ac[l_ * LC + j] = A[l * LD + j];
+                pc[l_] = pp[l];
+                unint |= 1u << l_;
             }
-            double* bo = K.b + c * LC;
-            for (int j = 0; j < LC; j++) bo[j] = blp[j] + tb * mu_t[j];
-            const int mpre = m - 1;
-            unsigned char* cm = K.cmap + c * MC;
-            signed char* cs = K.csmap + c * MC;
-            const int ns = nd_coalign<LC>(Ac, pc, qc, unint, mpre, cm, cs);
-            if (ns < 0) {
-                atomicOr(err, kErrAntiCoalignedHorthog);
-                K.m[c] = 0;
-                K.keep[c] = 0;
-                K.ccnt[c] = 0;
-                c++;
-                continue;
-            }
-            double* Ao = K.A + c * MC * LC;
-            for (int q = 0; q < ns * LC; q++) Ao[q] = Ac[q];
-            for (int q = 0; q < ns; q++) {
-                K.p[c * MC + q] = pc[q];
-                K.q[c * MC + q] = qc[q];
-            }
-            K.pt[c] = pt;
-            K.par[c] = t;
-            K.m[c] = ns;
-            K.mpre[c] = mpre;
-            K.phc[c] = m;
-            K.z[c] = tz;
-            K.lhp[c] = lam;
-            K.horthog[c] = unint;
-            K.hcm[c] = ns < mpre ? 1 : 0;
-            K.cval[c] = tb;
-            K.dval[c] = plp[tz];
+            l_++;
+        }
+        const int mpre = m - 1;
+        unsigned char* cm = K.cmap + c * MC;
+        signed char* cs = K.csmap + c * MC;
+        const int ns = nd_coalign<LC>(Ac, pc, qc, unint, mpre, cm, cs);
+        if (ns < 0) {
+            atomicOr(err, kErrAntiCoalignedHorthog);
+            K.m[c] = 0;
             K.keep[c] = 0;
-            c++;
+            K.ccnt[c] = 0;
+            continue;
         }
+        double* Ao = K.A + c * MC * LC;
+        for (int q = 0; q < ns * LC; q++) Ao[q] = Ac[q];
+        for (int q = 0; q < ns; q++) {
+            K.p[c * MC + q] = pc[q];
+            K.q[c * MC + q] = qc[q];
+        }
+        K.pt[c] = pt;
+        K.par[c] = t;
+        K.m[c] = ns;
+        K.mpre[c] = mpre;
+        K.phc[c] = m;
+        K.z[c] = tz;
+        K.lhp[c] = lam;
+        K.horthog[c] = unint;
+        K.hcm[c] = ns < mpre ? 1 : 0;
+        K.cval[c] = tb;
+        K.dval[c] = pp[tz] * fabs(Ald[tz]);
+        K.keep[c] = 0;
     }
 }
 
 __device__ inline int nd_remove_bit(int b, int bit) { return ((b >> (bit + 1)) << bit) | (b & ((1 << bit) - 1)); }
+
+// Children of at most lc rows, a thread each: no cells below lc rows (they
+// evaluate to zero and are not carried, cpdf_ndim.hpp:773-776), the
+// 2^lc / 2 trivial cells at lc rows (cell_enumeration.hpp:1129-1136).  The
+// others are flagged for the warp-per-child enumeration.
+template <int LC>
+__global__ void k_nd_cells_small(NdKids K, long long nk, const long long* coff, int* keys_out, int* big)
+{
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < nk;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int m = K.m[c];
+        if (!keys_out) {
+            big[c] = m > LC ? 1 : 0;
+            if (m <= LC) K.ccnt[c] = m < LC ? 0 : (1 << LC) / 2;
+        } else if (m == LC) {
+            for (int k = 0; k < (1 << LC) / 2; k++) keys_out[coff[c] + k] = k;
+        }
+    }
+}
+
+__global__ void k_nd_list(const int* big, const long long* bscan, long long nk, long long* list)
+{
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < nk;
+         c += (long long)gridDim.x * blockDim.x)
+        if (big[c]) list[bscan[c]] = c;
+}
 
 // Cells of each lowered child (make_lowered_child_btable): the parent cells
 // b (keys in the enc_lambda_bar frame) whose neighbour across the
@@ -388,8 +413,9 @@ __device__ inline int nd_remove_bit(int b, int bit) { return ((b >> (bit + 1)) <
 // cells as bitmaps in shared memory.  keys_out null: counts into ccnt;
 // else the ascending keys from coff[c] on.
 template <int LC>
-__global__ void k_nd_cells(const long long* ptoff, const int* ptcnt, const int* pkeys, NdKids K, long long nk,
-                           int MC, const long long* coff, int* keys_out)
+__global__ void k_nd_cells(const long long* ptoff, const int* ptcnt, const int* pkeys, NdKids K,
+                           const long long* list, const long long* nlist, int MC, const long long* coff,
+                           int* keys_out)
 {
     extern __shared__ unsigned nd_smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
@@ -397,7 +423,9 @@ __global__ void k_nd_cells(const long long* ptoff, const int* ptcnt, const int* 
     unsigned* PB = nd_smem + (size_t)wib * (2 * words + 32);
     unsigned* RK = PB + words;
     int* bmk = reinterpret_cast<int*>(RK + words);
-    for (long long c = (long long)blockIdx.x * nwb + wib; c < nk; c += (long long)gridDim.x * nwb) {
+    const long long nl = *nlist;
+    for (long long li = (long long)blockIdx.x * nwb + wib; li < nl; li += (long long)gridDim.x * nwb) {
+        const long long c = list[li];
         const int m = K.m[c];
         if (m < LC) {
             if (!keys_out && lane == 0) K.ccnt[c] = 0;
@@ -669,7 +697,8 @@ __global__ void k_nd_final_combine(const cd* partial, const long long* coff, int
 struct NdWork {
     NdTermBufs lev[2];
     NdKidBufs kids;
-    NdBuf<int> cnt, keep_i, keys[2];
+    NdBuf<int> cnt, keep_i, big, keys[2];
+    NdBuf<long long> blist;
     NdBuf<cd> vals[2];
     NdBuf<long long> coff, cellof, kscan, scan_tmp;
     NdBuf<double> x, out;
@@ -730,8 +759,8 @@ int nd_level(NdWork& w, NdTerms P, const int* pkeys, const cd* pvals, long long 
     }
     if ((s = w.kids.ensure(nk, MC, LC))) return s;
     NdKids K = w.kids.view();
-    k_nd_lower<LD><<<nd_grid(npairs, thr, lc.num_sms), thr, 0, lc.stream>>>(P, n, npairs, x, D, w.coff.ptr, MC, K,
-                                                                          w.err.ptr);
+    k_nd_lower<LD><<<nd_grid(nk, thr, lc.num_sms), thr, 0, lc.stream>>>(P, n, npairs, x, D, w.coff.ptr, nk, MC, K,
+                                                                      w.err.ptr);
     // cells: counts, offsets, keys
     const int words = (1 << MC) > 32 ? (1 << MC) / 32 : 1;
     const size_t pw = (size_t)(2 * words + 32) * 4;
@@ -743,8 +772,18 @@ int nd_level(NdWork& w, NdTerms P, const int* pkeys, const cd* pvals, long long 
     const int cgrid = nd_grid(nk, warps, lc.num_sms);
     if ((s = w.kscan.ensure(nk + 2))) return s;
     if ((s = w.cellof.ensure(nk + 2))) return s;
+    if ((s = w.big.ensure(nk + 1))) return s;
+    if ((s = w.blist.ensure(nk + 1))) return s;
     if ((s = w.ensure_scan(nk + 1))) return s;
-    k_nd_cells<LC><<<cgrid, warps * 32, sm, lc.stream>>>(P.toff, P.tcnt, pkeys, K, nk, MC, nullptr, nullptr);
+    // the children of at most lc rows a thread each; the others listed for
+    // the warp-per-child enumeration (in 1-D nearly every child coaligns to
+    // one row)
+    k_nd_cells_small<LC><<<nd_grid(nk, thr, lc.num_sms), thr, 0, lc.stream>>>(K, nk, nullptr, nullptr, w.big.ptr);
+    scan_int_to_ll(w.big.ptr, w.kscan.ptr, nk, w.ss, lc);
+    k_nd_list<<<nd_grid(nk, thr, lc.num_sms), thr, 0, lc.stream>>>(w.big.ptr, w.kscan.ptr, nk, w.blist.ptr);
+    const long long* nlist = w.kscan.ptr + nk;
+    k_nd_cells<LC><<<cgrid, warps * 32, sm, lc.stream>>>(P.toff, P.tcnt, pkeys, K, w.blist.ptr, nlist, MC, nullptr,
+                                                         nullptr);
     scan_int_to_ll(K.ccnt, w.cellof.ptr, nk, w.ss, lc);
     long long ncell = 0;
     ND_CUDA(cudaMemcpyAsync(&ncell, w.cellof.ptr + nk, sizeof(long long), cudaMemcpyDeviceToHost, lc.stream));
@@ -752,8 +791,10 @@ int nd_level(NdWork& w, NdTerms P, const int* pkeys, const cd* pvals, long long 
     w.launches += 3;
     if ((s = w.keys[kb].ensure(ncell + 1))) return s;
     if ((s = w.vals[kb].ensure(ncell + 1))) return s;
-    k_nd_cells<LC><<<cgrid, warps * 32, sm, lc.stream>>>(P.toff, P.tcnt, pkeys, K, nk, MC, w.cellof.ptr,
-                                                         w.keys[kb].ptr);
+    k_nd_cells_small<LC><<<nd_grid(nk, thr, lc.num_sms), thr, 0, lc.stream>>>(K, nk, w.cellof.ptr, w.keys[kb].ptr,
+                                                                            nullptr);
+    k_nd_cells<LC><<<cgrid, warps * 32, sm, lc.stream>>>(P.toff, P.tcnt, pkeys, K, w.blist.ptr, nlist, MC,
+                                                         w.cellof.ptr, w.keys[kb].ptr);
     if (ncell > 0)
         k_nd_gvals<LC><<<nd_grid(ncell, thr, lc.num_sms), thr, 0, lc.stream>>>(
             P.toff, P.tcnt, pkeys, pvals, K, nk, MC, w.cellof.ptr, ncell, w.keys[kb].ptr, w.vals[kb].ptr);
