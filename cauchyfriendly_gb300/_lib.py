@@ -61,7 +61,7 @@ SIGNATURES = {
     "mce_device_errors": (ctypes.c_int, [_vp]),
     "mce_total_cells": (ctypes.c_longlong, [_vp, ctypes.c_int]),
     "mce_dump_terms": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _ip, _dp, _dp, _dp, _ip, _ip, _dp]),
-    "mce_trim_memory": (ctypes.c_longlong, [_vp]),
+    "mce_trim_memory": (ctypes.c_longlong, [_vp, ctypes.c_longlong]),
     "mce_reset": (ctypes.c_int, [_vp]),
     "mce_reinitialize_start_statistics": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp]),
     "mce_set_master_step": (ctypes.c_int, [_vp, ctypes.c_int]),

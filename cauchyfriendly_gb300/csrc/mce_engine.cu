@@ -311,8 +311,9 @@ public:
     virtual long long total_cells(int est) = 0;
     virtual int reset() = 0;
     // Frees the buffers that grow with the term count (only between a reset
-    // or creation and the next step); returns the bytes released.
-    virtual long long trim() = 0;
+    // or creation and the next step) when they hold at least min_bytes;
+    // returns the bytes released.
+    virtual long long trim(long long min_bytes) = 0;
     // copies estimator e's start statistics to the device, where the next
     // first update reads them
     virtual int upload_start(int e) = 0;
@@ -784,13 +785,19 @@ public:
         return MCE_OK;
     }
 
-    long long trim() override
+    long long trim(long long min_bytes) override
     {
         if (master_step != 0) return MCE_ERR_ARG;
+        if (min_bytes > 0 && trim_pass(false) < min_bytes) return 0;
+        return trim_pass(true);
+    }
+    // the bytes the term-sized buffers hold; released when `release`
+    long long trim_pass(bool release)
+    {
         long long freed = 0;
-        auto rel = [&freed](auto& buf) {
+        auto rel = [&freed, release](auto& buf) {
             freed += (long long)(buf.cap * sizeof(*buf.ptr));
-            buf.release();
+            if (release) buf.release();
         };
         for (auto& P : Pb) {
             rel(P.est), rel(P.m), rel(P.m_old), rel(P.tab_cnt), rel(P.B_cnt), rel(P.nkids), rel(P.nkids_all);
@@ -2675,10 +2682,10 @@ int mce_dump_terms(mce_handle* h, int e, int max_shape, int* shape, double* A, d
     return h->eng->dump_terms(e, max_shape, shape, A, p, b, cells, keys, g);
 }
 int mce_reset(mce_handle* h) { return h ? h->eng->reset() : MCE_ERR_ARG; }
-long long mce_trim_memory(mce_handle* h)
+long long mce_trim_memory(mce_handle* h, long long min_bytes)
 {
-    if (!h) return MCE_ERR_ARG;
-    const long long r = h->eng->trim();
+    if (!h || min_bytes < 0) return MCE_ERR_ARG;
+    const long long r = h->eng->trim(min_bytes);
     if (r < 0) set_error("mce_trim_memory: only between mce_reset (or creation) and the next step");
     return r;
 }

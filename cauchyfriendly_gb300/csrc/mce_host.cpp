@@ -705,8 +705,8 @@ int mce_swm_step(mce_swm* s, const double* msmts, const double* controls, double
             s->post_mu_done += mce_post_mu_terms(s->slots[j]);
             const int st = mce_reset(s->slots[j]);
             if (st < 0) return st;
-            // the window restarts from one term: its large buffers go back to the device
-            const long long tr = mce_trim_memory(s->slots[j]);
+            // the window restarts from one term: buffers of a gigabyte or more go back to the device
+            const long long tr = mce_trim_memory(s->slots[j], 1LL << 30);
             if (tr < 0) return (int)tr;
             s->win_count[j] = 0;
         }

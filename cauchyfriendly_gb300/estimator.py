@@ -158,10 +158,11 @@ class BatchedCauchyEstimator:
     def reset(self):
         _lib.check(self._lib.mce_reset(self._h), "mce_reset")
 
-    def trim_memory(self):
+    def trim_memory(self, min_bytes=0):
         """Frees the device buffers that grow with the term count (between a
-        reset and the next step); returns the bytes released."""
-        return _lib.check(self._lib.mce_trim_memory(self._h), "mce_trim_memory")
+        reset and the next step) when they hold at least min_bytes; returns
+        the bytes released."""
+        return _lib.check(self._lib.mce_trim_memory(self._h, int(min_bytes)), "mce_trim_memory")
 
     def reinitialize_start_statistics(self, A0, p0, b0, e=0):
         A0, p0, b0 = _f64(A0), _f64(p0), _f64(b0)

@@ -90,9 +90,9 @@ class _GpuSlot:
         return self.est.num_terms(i)
 
     def reset(self):
-        # a window restarts from one term: its large buffers go back to the device
+        # a window restarts from one term: buffers of a gigabyte or more go back to the device
         self.est.reset()
-        self.est.trim_memory()
+        self.est.trim_memory(1 << 30)
 
     def reinit(self, i, A0, p0, b0):
         self.est.reinitialize_start_statistics(A0, p0, b0, i)

@@ -398,13 +398,15 @@ int mce_dump_terms(mce_handle* h, int est, int max_shape, int* shape, double* A,
 /* CauchyEstimator::reset (include/cauchy_estimator.hpp:1247) for every estimator. */
 int mce_reset(mce_handle* h);
 /* Frees the device buffers that grow with the term count (term records,
- * g-tables, reduction and evaluation scratch), returning the bytes released;
- * the next step allocates what it needs again.  Only between mce_reset (or
- * creation) and the next step, else MCE_ERR_ARG.  The window managers call
- * it on every window they reset, so that only the windows that are large
- * at the same time hold large buffers (the reference's terms are reallocated
- * each step, include/cauchy_estimator.hpp). */
-long long mce_trim_memory(mce_handle* h);
+ * g-tables, reduction and evaluation scratch) when together they hold at
+ * least min_bytes (0: whatever they hold), returning the bytes released (0
+ * below the threshold); the next step allocates what it needs again.  Only
+ * between mce_reset (or creation) and the next step, else MCE_ERR_ARG.  The
+ * window managers call it with 1 GiB on every window they reset, so that
+ * only the windows that are large at the same time hold large buffers (the
+ * reference's terms are reallocated each step, include/cauchy_estimator.hpp)
+ * while small windows keep theirs. */
+long long mce_trim_memory(mce_handle* h, long long min_bytes);
 /* reinitialize_start_statistics (include/cauchy_estimator.hpp:1302). */
 int mce_reinitialize_start_statistics(mce_handle* h, int est, const double* A0, const double* p0, const double* b0);
 /* The constructor's print_basic_info (include/cauchy_estimator.hpp:87, 165)

@@ -314,8 +314,9 @@ def test_trim_memory_between_reset_and_step():
     est = BCE(B["A0"], B["p0"], B["b0"], B["steps"], 3, 0, 1, 1, rp, bp)
     run = lambda: est.run(B["msmts"], B["Phi"], B["Gamma"], B["beta"], B["H"], B["gamma"], shared_model=False)
     first = run()
-    assert est._lib.mce_trim_memory(est._h) == -1  # MCE_ERR_ARG: after a step
+    assert est._lib.mce_trim_memory(est._h, 0) == -1  # MCE_ERR_ARG: after a step
     est.reset()
+    assert est.trim_memory(1 << 40) == 0  # below the threshold: kept
     assert est.trim_memory() > 0
     assert est.trim_memory() == 0
     second = run()
