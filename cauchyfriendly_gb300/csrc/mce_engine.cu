@@ -1767,6 +1767,10 @@ public:
     int cpdf_nd(int e, const double* x, int npts, double* out) override
     {
         if (e < 0 || e >= E || !x || !out || npts < 1) return MCE_ERR_ARG;
+        if (MC > 16) {
+            set_error("N-D pdf: terms of more than 16 hyperplanes are not supported");
+            return MCE_ERR_SHAPE;
+        }
         if (master_step < 1) {
             set_error("N-D pdf: the estimator has not been stepped");
             return MCE_ERR_ARG;

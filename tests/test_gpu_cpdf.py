@@ -175,6 +175,14 @@ def test_gpu_nd_pdf_against_oracle_on_larger_estimators():
         assert close(got[pick[:2]], apart) <= G.REL_TOL, (prob["d"], close(got[pick[:2]], apart))
         est.close()
         orc.close()
+    # terms of more than 16 hyperplanes (here up to 3 + 7 * 2 = 17) are refused
+    prob = W.many_gamma(3, 2, 8, seed=14)
+    rp, bp = oracle.draw_reference_constants(23, 3, oracle.max_shape_of(prob))
+    est = CE(prob["A0"], prob["p0"], prob["b0"], 8, 3, 0, 2, 1, root_point=rp, b_pert=bp)
+    est.step(prob["msmts"][0, 0], prob["Phi"], prob["Gamma"], prob["beta"], prob["H"][0], prob["gamma"][0])
+    with pytest.raises(_lib.MceError, match="16 hyperplanes"):
+        est.cpdf_nd(np.zeros(3))
+    est.close()
     # before the first step and after the last one
     prob = W.four_state_lti(seed=1, steps=2)
     rp, bp = oracle.draw_reference_constants(22, 4, oracle.max_shape_of(prob))
