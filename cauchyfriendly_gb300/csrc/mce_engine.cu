@@ -414,7 +414,7 @@ public:
     std::vector<long long> hpstart;  // E+1
     std::vector<int> h_order;       // moment-chain launch order
     DevBuf<int> ftr_cnt;            // worklist lengths of the resolution rounds
-    static constexpr int kFtrFirstBatch = 4, kFtrBatch = 2, kFtrCntSlots = 8;
+    static constexpr int kFtrFirstBatch = 4, kFtrBatch = 2, kFtrCntSlots = 8, kFtrMaxRounds = 100000;
     DevBuf<int> d_order;
     // combos per shape (lexicographic d-subsets)
     DevBuf<int> dcombo_off;
@@ -1315,9 +1315,19 @@ public:
         // on the device, a round after the last is empty, and the host reads
         // the count once per batch
         if ((s = ftr_cnt.ensure(kFtrCntSlots))) return s;
+        // every round in one persistent launch over the device worklists: no
+        // host round trip until the g-table stage reads its sizes
+        MCE_CUDA(cudaMemsetAsync(ftr_cnt.ptr, 0, sizeof(int) * kFtrCntSlots, lc.stream));
+        pbeg(KID_FTR);
+        const int pst = Kernels<D>::ftr_resolve_all(R, nR, cell_ent2.ptr, boff.ptr, H - 1, MC, status.ptr, owner.ptr,
+                                                    ftr_wl[0].ptr, ftr_wl[1].ptr, ftr_cnt.ptr, ftr_resume.ptr,
+                                                    reinterpret_cast<unsigned*>(ftr_cnt.ptr + 4), kFtrMaxRounds, err,
+                                                    lc);
+        pend();
         int unk = 0;
         long long bound = nR;
-        for (int round = 0;;) {
+        for (int round = 0; pst != MCE_OK;) {
+            // the cooperative launch is not available: rounds queued in batches
             const int K = round == 0 ? kFtrFirstBatch : kFtrBatch;
             pbeg(KID_FTR);
             for (int q = 0; q < K; q++, round++) {

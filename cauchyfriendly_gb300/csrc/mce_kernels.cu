@@ -7,6 +7,7 @@
 // out one after another, so every per-estimator rule (root = lowest index in a
 // reduction group, member order, next parent order) is a rule on positions.
 #include "mce_kernels.cuh"
+#include "mce_c_api.h"
 
 #include <algorithm>
 #include <climits>
@@ -1332,15 +1333,24 @@ __global__ void k_ftr_sort_buckets(const CellEntry<D>* in, long long n, const in
 // resumes each bucket at the entry that stopped it (resume[j][q] for its q-th
 // distinct bucket), and later rounds run over the worklist of waiting terms.
 
+// One resolution round over the records (wl_in null, the first round) or
+// the worklist wl_in[0..*n_in): each record still undecided looks for its
+// nearest near predecessor in its cell buckets; it becomes a member of a
+// root, a root, or waits for the next round (wl_out).  A decision is only
+// taken on predecessors that are decided, so the result does not depend on
+// the order the threads run in.
 template <int D>
-__global__ void k_ftr_resolve_scan(TermRecs R, long long nR, const CellEntry<D>* ent, const long long* boff,
-                                   long long hmask, int MC, int* status, int* owner, const int* wl_in, const int* n_in,
-                                   int* wl_out, int* n_out, int* resume)
+__device__ __forceinline__ void ftr_round(const TermRecs& R, long long nR, const CellEntry<D>* ent,
+                                          const long long* boff, long long hmask, int MC, int* status, int* owner,
+                                          const int* wl_in, const int* n_in, int* wl_out, int* n_out, int* resume,
+                                          long long tid, long long nth)
 {
-    const long long n = wl_in ? (long long)*n_in : nR;
-    for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < n; w += (long long)gridDim.x * blockDim.x) {
-        const long long j = wl_in ? wl_in[w] : w;
-        if (status[j] != 0) continue;
+    const long long n = wl_in ? (long long)*(volatile const int*)n_in : nR;
+    for (long long w = tid; w < n; w += nth) {
+        // records, states and resume points written in earlier rounds are read
+        // through L2 (a persistent launch does not refresh an SM's L1)
+        const long long j = wl_in ? (long long)__ldcg(wl_in + w) : w;
+        if (__ldcg(status + j) != 0) continue;
         const int e = R.est[j];
         const int m = R.m[j];
         const int em = (e << 5) | m;
@@ -1374,7 +1384,7 @@ __global__ void k_ftr_resolve_scan(TermRecs R, long long nR, const CellEntry<D>*
             const int q = nseen;
             if (nseen < (1 << (D < 5 ? D : 5))) seen[nseen++] = s;
             const long long kb = boff[s], ke = boff[s + 1];
-            long long k = kb + ((wl_in && q < kFtrResume) ? resume[j * kFtrResume + q] : 0);
+            long long k = kb + ((wl_in && q < kFtrResume) ? __ldcg(resume + j * kFtrResume + q) : 0);
             for (; k < ke; k++) {
                 const CellEntry<D>& ce = ent[k];
                 if (ce.idx >= j) break;  // ascending: no predecessors beyond
@@ -1399,6 +1409,83 @@ __global__ void k_ftr_resolve_scan(TermRecs R, long long nR, const CellEntry<D>*
             ((volatile int*)status)[j] = 1;
         } else
             wl_out[atomicAdd(n_out, 1)] = (int)j;
+    }
+}
+
+template <int D>
+__global__ void k_ftr_resolve_scan(TermRecs R, long long nR, const CellEntry<D>* ent, const long long* boff,
+                                   long long hmask, int MC, int* status, int* owner, const int* wl_in, const int* n_in,
+                                   int* wl_out, int* n_out, int* resume)
+{
+    ftr_round<D>(R, nR, ent, boff, hmask, MC, status, owner, wl_in, n_in, wl_out, n_out, resume,
+                 blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+}
+
+// Grid-wide barrier of a cooperative launch with a bounded wait: bar[0]
+// counts the blocks arrived, bar[1] is the generation.  Returns false (for
+// every thread of the block) when the wait ran past spin_limit polls; the
+// caller then stops.
+__device__ inline bool grid_barrier(unsigned* bar, long long spin_limit)
+{
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned gen = *(volatile unsigned*)(bar + 1);
+        __threadfence();
+        const unsigned arrived = atomicAdd(bar, 1u) + 1;
+        if (arrived == gridDim.x) {
+            *(volatile unsigned*)bar = 0;
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            long long it = 0;
+            while (*(volatile unsigned*)(bar + 1) == gen) {
+                if (++it > spin_limit) {
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Every resolution round in one persistent cooperative launch over a device
+// worklist: round r reads the worklist and count of round r - 1, writes its
+// own, and the grid synchronises between rounds; the loop ends when a round
+// leaves nothing undecided.  After max_rounds rounds, or a barrier wait past
+// its limit, it stops with kErrResolveStalled.  Round r's count is
+// cnt[r % 3]; cnt[(r + 1) % 3], which no thread touches in round r, is
+// cleared then for round r + 1.
+template <int D>
+__global__ void __launch_bounds__(128) k_ftr_resolve_all(TermRecs R, long long nR, const CellEntry<D>* ent,
+                                                         const long long* boff, long long hmask, int MC, int* status,
+                                                         int* owner, int* wl0, int* wl1, int* cnt, int* resume,
+                                                         unsigned* bar, int max_rounds, int* err)
+{
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long nth = (long long)gridDim.x * blockDim.x;
+    for (int r = 0;; r++) {
+        if (r >= max_rounds) {
+            if (tid == 0) atomicOr(err, kErrResolveStalled);
+            break;
+        }
+        int* wl_out = (r & 1) ? wl1 : wl0;
+        const int* wl_in = r ? ((r & 1) ? wl0 : wl1) : nullptr;
+        int* n_out = cnt + r % 3;
+        const int* n_in = r ? cnt + (r + 2) % 3 : nullptr;
+        if (tid == 0) cnt[(r + 1) % 3] = 0;
+        ftr_round<D>(R, nR, ent, boff, hmask, MC, status, owner, wl_in, n_in, wl_out, n_out, resume, tid, nth);
+        if (!grid_barrier(bar, 1LL << 26)) {
+            if (threadIdx.x == 0) atomicOr(err, kErrResolveStalled);
+            break;
+        }
+        if (*(volatile int*)n_out == 0) break;
     }
 }
 
@@ -2479,6 +2566,41 @@ void Kernels<D>::ftr_resolve(TermRecs R, long long nR, const void* ent, const lo
         R, nR, static_cast<const CellEntry<D>*>(ent), boff, hmask, MC, status, owner, wl_in, n_in, wl_out, n_out,
         resume);
     tune_end(t, c.stream);
+}
+
+template <int D>
+int Kernels<D>::ftr_resolve_all(TermRecs R, long long nR, const void* ent, const long long* boff, long long hmask,
+                                int MC, int* status, int* owner, int* wl0, int* wl1, int* cnt, int* resume,
+                                unsigned* bar, int max_rounds, int* err, const LaunchCfg& c)
+{
+    if (nR == 0) return MCE_OK;
+    // blocks that fit on the GPU at once (half of them: other streams' kernels
+    // may hold part of the SMs while this one waits at its barriers)
+    static int bps = -1;
+    if (bps < 0) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ftr_resolve_all<D>, 128, 0) != cudaSuccess) {
+            cudaGetLastError();
+            b = 0;
+        }
+        bps = b;
+    }
+    if (bps <= 0) return MCE_ERR_CUDA;
+    long long grid = (long long)std::max(1, bps / 2) * c.num_sms;
+    const long long need = (nR + 127) / 128;
+    if (grid > need) grid = need;
+    if (grid < 1) grid = 1;
+    const CellEntry<D>* e = static_cast<const CellEntry<D>*>(ent);
+    void* args[] = {&R, &nR, &e, &boff, &hmask, &MC, &status, &owner, &wl0, &wl1, &cnt, &resume, &bar, &max_rounds,
+                    &err};
+    const cudaError_t st = cudaLaunchCooperativeKernel((const void*)k_ftr_resolve_all<D>, dim3((unsigned)grid),
+                                                       dim3(128), args, 0, c.stream);
+    if (st != cudaSuccess) {
+        cudaGetLastError();
+        return MCE_ERR_CUDA;
+    }
+    ++g_launches;
+    return MCE_OK;
 }
 
 static inline size_t gtable_smem_per_warp(int MC, int capR)
