@@ -1315,20 +1315,24 @@ public:
         // on the device, a round after the last is empty, and the host reads
         // the count once per batch
         if ((s = ftr_cnt.ensure(kFtrCntSlots))) return s;
-        // every round in one persistent launch over the device worklists: no
-        // host round trip until the g-table stage reads its sizes
+        // the first round over every record as an ordinary (full-occupancy)
+        // launch, the rounds after it in one persistent launch over the device
+        // worklists: no host round trip until the g-table stage reads its sizes
         MCE_CUDA(cudaMemsetAsync(ftr_cnt.ptr, 0, sizeof(int) * kFtrCntSlots, lc.stream));
         pbeg(KID_FTR);
+        Kernels<D>::ftr_resolve(R, nR, cell_ent2.ptr, boff.ptr, H - 1, MC, status.ptr, owner.ptr, nullptr, nullptr,
+                                nR, ftr_wl[0].ptr, ftr_cnt.ptr, ftr_resume.ptr, lc);
         const int pst = Kernels<D>::ftr_resolve_all(R, nR, cell_ent2.ptr, boff.ptr, H - 1, MC, status.ptr, owner.ptr,
                                                     ftr_wl[0].ptr, ftr_wl[1].ptr, ftr_cnt.ptr, ftr_resume.ptr,
-                                                    reinterpret_cast<unsigned*>(ftr_cnt.ptr + 4), kFtrMaxRounds, err,
-                                                    lc);
+                                                    reinterpret_cast<unsigned*>(ftr_cnt.ptr + 4), 1, kFtrMaxRounds,
+                                                    err, lc);
         pend();
         int unk = 0;
         long long bound = nR;
-        for (int round = 0; pst != MCE_OK;) {
-            // the cooperative launch is not available: rounds queued in batches
-            const int K = round == 0 ? kFtrFirstBatch : kFtrBatch;
+        for (int round = 1; pst != MCE_OK;) {
+            // the cooperative launch is not available: the rounds after the
+            // first queued in batches (round r counts into ftr_cnt[r % 8])
+            const int K = round == 1 ? kFtrFirstBatch - 1 : kFtrBatch;
             pbeg(KID_FTR);
             for (int q = 0; q < K; q++, round++) {
                 int* n_out = ftr_cnt.ptr + round % kFtrCntSlots;

@@ -1455,10 +1455,10 @@ __device__ inline bool grid_barrier(unsigned* bar, long long spin_limit)
     return s_ok != 0;
 }
 
-// Every resolution round in one persistent cooperative launch over a device
-// worklist: round r reads the worklist and count of round r - 1, writes its
-// own, and the grid synchronises between rounds; the loop ends when a round
-// leaves nothing undecided.  After max_rounds rounds, or a barrier wait past
+// The resolution rounds from first_round on in one persistent cooperative
+// launch over a device worklist: round r reads the worklist and count of
+// round r - 1, writes its own, and the grid synchronises between rounds; the
+// loop ends when a round leaves nothing undecided.  After max_rounds rounds, or a barrier wait past
 // its limit, it stops with kErrResolveStalled.  Round r's count is
 // cnt[r % 3]; cnt[(r + 1) % 3], which no thread touches in round r, is
 // cleared then for round r + 1.
@@ -1466,11 +1466,11 @@ template <int D>
 __global__ void __launch_bounds__(128) k_ftr_resolve_all(TermRecs R, long long nR, const CellEntry<D>* ent,
                                                          const long long* boff, long long hmask, int MC, int* status,
                                                          int* owner, int* wl0, int* wl1, int* cnt, int* resume,
-                                                         unsigned* bar, int max_rounds, int* err)
+                                                         unsigned* bar, int first_round, int max_rounds, int* err)
 {
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long nth = (long long)gridDim.x * blockDim.x;
-    for (int r = 0;; r++) {
+    for (int r = first_round;; r++) {
         if (r >= max_rounds) {
             if (tid == 0) atomicOr(err, kErrResolveStalled);
             break;
@@ -2571,7 +2571,7 @@ void Kernels<D>::ftr_resolve(TermRecs R, long long nR, const void* ent, const lo
 template <int D>
 int Kernels<D>::ftr_resolve_all(TermRecs R, long long nR, const void* ent, const long long* boff, long long hmask,
                                 int MC, int* status, int* owner, int* wl0, int* wl1, int* cnt, int* resume,
-                                unsigned* bar, int max_rounds, int* err, const LaunchCfg& c)
+                                unsigned* bar, int first_round, int max_rounds, int* err, const LaunchCfg& c)
 {
     if (nR == 0) return MCE_OK;
     // blocks that fit on the GPU at once (half of them: other streams' kernels
@@ -2591,8 +2591,8 @@ int Kernels<D>::ftr_resolve_all(TermRecs R, long long nR, const void* ent, const
     if (grid > need) grid = need;
     if (grid < 1) grid = 1;
     const CellEntry<D>* e = static_cast<const CellEntry<D>*>(ent);
-    void* args[] = {&R, &nR, &e, &boff, &hmask, &MC, &status, &owner, &wl0, &wl1, &cnt, &resume, &bar, &max_rounds,
-                    &err};
+    void* args[] = {&R,    &nR,     &e,   &boff,   &hmask, &MC,          &status,     &owner,
+                    &wl0,  &wl1,    &cnt, &resume, &bar,   &first_round, &max_rounds, &err};
     const cudaError_t st = cudaLaunchCooperativeKernel((const void*)k_ftr_resolve_all<D>, dim3((unsigned)grid),
                                                        dim3(128), args, 0, c.stream);
     if (st != cudaSuccess) {

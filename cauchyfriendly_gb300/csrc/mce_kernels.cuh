@@ -181,12 +181,13 @@ struct Kernels {
     static void ftr_resolve(TermRecs R, long long nR, const void* ent, const long long* boff, long long hmask, int MC,
                             int* status, int* owner, const int* wl_in, const int* n_in, long long n_bound,
                             int* wl_out, int* n_out, int* resume, const LaunchCfg& c);
-    // every resolution round in one persistent cooperative launch (the
-    // worklists wl0/wl1, counts cnt[3] zeroed, barrier state bar[2] zeroed);
-    // MCE_ERR_CUDA when the cooperative launch is not available
+    // the resolution rounds from first_round on in one persistent cooperative
+    // launch (round r: worklist wl[r & 1], count cnt[r % 3]; the counts
+    // zeroed, barrier state bar[2] zeroed); MCE_ERR_CUDA when the cooperative
+    // launch is not available
     static int ftr_resolve_all(TermRecs R, long long nR, const void* ent, const long long* boff, long long hmask,
                                int MC, int* status, int* owner, int* wl0, int* wl1, int* cnt, int* resume,
-                               unsigned* bar, int max_rounds, int* err, const LaunchCfg& c);
+                               unsigned* bar, int first_round, int max_rounds, int* err, const LaunchCfg& c);
     // g-tables of every reduction group (flattening.hpp:318-568).
     static void gtable(TermRecs R, const int* roots_list, long long nroots, const int* gcnt,
                        const long long* goff, const int* members, ParentList P, Tables Told, const int* Bkeys,
