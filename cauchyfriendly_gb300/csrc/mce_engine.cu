@@ -415,6 +415,14 @@ public:
     std::vector<int> h_order;       // moment-chain launch order
     DevBuf<int> ftr_cnt;            // worklist lengths of the resolution rounds
     static constexpr int kFtrFirstBatch = 4, kFtrBatch = 2, kFtrCntSlots = 8, kFtrMaxRounds = 100000;
+    static bool ftr_persistent()
+    {
+        static const bool on = [] {
+            const char* v = getenv("MCE_FTR_PERSISTENT");
+            return v && v[0] == '1';
+        }();
+        return on;
+    }
     DevBuf<int> d_order;
     // combos per shape (lexicographic d-subsets)
     DevBuf<int> dcombo_off;
@@ -1316,22 +1324,26 @@ public:
         // the count once per batch
         if ((s = ftr_cnt.ensure(kFtrCntSlots))) return s;
         // the first round over every record as an ordinary (full-occupancy)
-        // launch, the rounds after it in one persistent launch over the device
-        // worklists: no host round trip until the g-table stage reads its sizes
+        // launch; the rounds after it either queued in batches, the host
+        // reading the worklist length once per batch (the default, the faster
+        // here), or, with MCE_FTR_PERSISTENT=1, in one persistent cooperative
+        // launch over the device worklists with no host round trip
         MCE_CUDA(cudaMemsetAsync(ftr_cnt.ptr, 0, sizeof(int) * kFtrCntSlots, lc.stream));
         pbeg(KID_FTR);
         Kernels<D>::ftr_resolve(R, nR, cell_ent2.ptr, boff.ptr, H - 1, MC, status.ptr, owner.ptr, nullptr, nullptr,
                                 nR, ftr_wl[0].ptr, ftr_cnt.ptr, ftr_resume.ptr, lc);
-        const int pst = Kernels<D>::ftr_resolve_all(R, nR, cell_ent2.ptr, boff.ptr, H - 1, MC, status.ptr, owner.ptr,
-                                                    ftr_wl[0].ptr, ftr_wl[1].ptr, ftr_cnt.ptr, ftr_resume.ptr,
-                                                    reinterpret_cast<unsigned*>(ftr_cnt.ptr + 4), 1, kFtrMaxRounds,
-                                                    err, lc);
+        const int pst = ftr_persistent()
+                            ? Kernels<D>::ftr_resolve_all(R, nR, cell_ent2.ptr, boff.ptr, H - 1, MC, status.ptr,
+                                                          owner.ptr, ftr_wl[0].ptr, ftr_wl[1].ptr, ftr_cnt.ptr,
+                                                          ftr_resume.ptr, reinterpret_cast<unsigned*>(ftr_cnt.ptr + 4),
+                                                          1, kFtrMaxRounds, err, lc)
+                            : MCE_ERR_ARG;
         pend();
         int unk = 0;
         long long bound = nR;
         for (int round = 1; pst != MCE_OK;) {
-            // the cooperative launch is not available: the rounds after the
-            // first queued in batches (round r counts into ftr_cnt[r % 8])
+            // the rounds after the first queued in batches (round r counts
+            // into ftr_cnt[r % 8])
             const int K = round == 1 ? kFtrFirstBatch - 1 : kFtrBatch;
             pbeg(KID_FTR);
             for (int q = 0; q < K; q++, round++) {

@@ -2575,7 +2575,8 @@ int Kernels<D>::ftr_resolve_all(TermRecs R, long long nR, const void* ent, const
 {
     if (nR == 0) return MCE_OK;
     // blocks that fit on the GPU at once (half of them: other streams' kernels
-    // may hold part of the SMs while this one waits at its barriers)
+    // may hold part of the SMs while this one waits at its barriers; one block
+    // per SM measured slower, 28.7 against 20.8 ms of term reduction per pass)
     static int bps = -1;
     if (bps < 0) {
         int b = 0;

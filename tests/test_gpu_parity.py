@@ -323,3 +323,21 @@ def test_trim_memory_between_reset_and_step():
     est.close()
     for k in ("fz", "mean", "cov", "err", "nt"):
         assert np.array_equal(first[k], second[k]), k
+
+
+def test_persistent_term_reduction_keeps_results_bit_identical():
+    """MCE_FTR_PERSISTENT=1 runs the term reduction's rounds after the first
+    in one persistent cooperative launch over the device worklists: the
+    golden fixtures stay bit-identical and a random batch matches the oracle
+    (a subprocess: the switch is read once per process)."""
+    _gpu()
+    import os
+    import subprocess
+    import sys
+    env = dict(os.environ, MCE_FTR_PERSISTENT="1")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-m", "pytest", os.path.join(root, "tests", "test_gpu_parity.py"), "-q",
+                        "-p", "no:cacheprovider", "-k", "(bit_identical or random_three_state) and not persistent"],
+                       cwd=root, env=env, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]
+    assert " passed" in r.stdout
