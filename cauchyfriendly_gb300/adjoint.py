@@ -116,6 +116,94 @@ class AdjointRun:
             pass
 
 
+class AdjointBatch:
+    """Adjoint runs of one LTI model (d states, pncc process-noise columns, p
+    measurements per step) stepped together: run r has steps[r] steps from
+    (A0[r], p0[r], b0[r]) with its own rand() constants (root_point[r],
+    b_pert[r]).  One batched handle steps every run (mce_adjoint_batch_*), and
+    the runs' records and reverses spread over the host's cores; each run's
+    gradient is the one an AdjointRun of its own gives."""
+
+    def __init__(self, d, pncc, p, steps, A0, p0, b0, root_point, b_pert):
+        self._L = _lib.load()
+        self.d, self.pncc, self.p = int(d), int(pncc), int(p)
+        self.steps = np.ascontiguousarray(np.asarray(steps, dtype=np.int32).reshape(-1))
+        self.n = len(self.steps)
+        f = lambda a, *sh: np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(self.n, *sh))
+        A0, p0, b0, rp = f(A0, d, d), f(p0, d), f(b0, d), f(root_point, d)
+        bp = np.ascontiguousarray(np.asarray(b_pert, dtype=np.float64).reshape(self.n, -1))
+        st = ctypes.c_int(0)
+        self._h = self._L.mce_adjoint_batch_create(
+            self.n, self.d, self.pncc, self.p, self.steps.ctypes.data_as(_lib._ip), _lib.dp(A0), _lib.dp(p0),
+            _lib.dp(b0), _lib.dp(rp), _lib.dp(bp), bp.shape[1], ctypes.byref(st))
+        if not self._h:
+            raise _lib.MceError("mce_adjoint_batch_create failed (%d): %s" % (st.value, _lib.last_error()))
+        self.max_steps = int(self.steps.max())
+
+    def forward(self, msmts, Phi, Gamma, beta, H, gamma):
+        """msmts: run r's measurements (steps[r]*p values) for every r.
+        Returns Re fz of every update of every run (a list of arrays)."""
+        stride = self.max_steps * self.p
+        M = np.zeros((self.n, stride))
+        for r, m in enumerate(msmts):
+            m = np.asarray(m, dtype=np.float64).reshape(-1)
+            M[r, :len(m)] = m
+        f = lambda a: np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(-1))
+        fz = np.zeros((self.n, stride))
+        _lib.check(self._L.mce_adjoint_batch_forward(self._h, _lib.dp(M), self.max_steps,
+                                                     *[_lib.dp(f(x)) for x in (Phi, Gamma, beta, H, gamma)],
+                                                     _lib.dp(fz)), "mce_adjoint_batch_forward")
+        return [fz[r, :self.steps[r] * self.p].copy() for r in range(self.n)]
+
+    def backward(self, ws):
+        """ws: run r's seeds (steps[r]*p values) for every r.  Returns a list
+        of gradient dicts shaped as AdjointRun.backward's."""
+        stride = self.max_steps * self.p
+        Wt = np.zeros((self.n, stride))
+        for r, w in enumerate(ws):
+            w = np.asarray(w, dtype=np.float64).reshape(-1)
+            Wt[r, :len(w)] = w
+        N = self._L.mce_adjoint_batch_num_params(self._h)
+        g = np.zeros((self.n, N))
+        _lib.check(self._L.mce_adjoint_batch_backward(self._h, _lib.dp(Wt), self.max_steps, _lib.dp(g)),
+                   "mce_adjoint_batch_backward")
+        d, pncc, p = self.d, self.pncc, self.p
+        shapes = ((pncc,), (p,), (d,), (d, d), (d, pncc), (p, d))
+        outs = []
+        for r in range(self.n):
+            out, k = {}, 0
+            for name, sh in zip(PARAM_NAMES, shapes):
+                sz = int(np.prod(sh))
+                out[name] = g[r, k:k + sz].reshape(sh)
+                k += sz
+            outs.append(out)
+        return outs
+
+    def check(self):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        _lib.check(self._L.mce_adjoint_batch_check(self._h, ctypes.byref(a), ctypes.byref(b)),
+                   "mce_adjoint_batch_check")
+        return a.value, b.value
+
+    def timing(self):
+        """Wall ms: batched step path, forward records, reverse; and the
+        runs' summed record-chain ms."""
+        t = np.zeros(4)
+        _lib.check(self._L.mce_adjoint_batch_timing(self._h, _lib.dp(t)), "mce_adjoint_batch_timing")
+        return t
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.mce_adjoint_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def _make_function():
     import torch
 
@@ -154,8 +242,8 @@ def windowed_log_likelihood(prob, W, root_point, b_pert, p0=None, beta=None, gam
     and its gradient with respect to (beta, gamma, p0, Phi, Gamma, H) with the
     window-boundary checkpoints held fixed: every window life is recomputed
     from its start statistics (the initial ones for the first life of window
-    0, Speyer's restart about the best window for the others) by an
-    AdjointRun, and gets the seeds +1/Re fz on each update at which it is the
+    0, Speyer's restart about the best window for the others) as one run of
+    an AdjointBatch, and gets the seeds +1/Re fz on each update at which it is the
     chosen window and -1/Re fz on the update before it (log fz_u =
     log Re U_u - log Re U_(u-1), U the unscaled normaliser).  p0 enters only
     the first life.
@@ -186,15 +274,19 @@ def windowed_log_likelihood(prob, W, root_point, b_pert, p0=None, beta=None, gam
         starts = [{"slot": s["slot"], "step": s["step"], "A0": np.asarray(s["A0"])[0], "p0": np.asarray(s["p0"])[0],
                    "b0": np.asarray(s["b0"])[0]} for s in mgr.starts]
         mgr.close()
-    def life(li):
-        st = starts[li]
-        s0 = st["step"]
-        n = min(W, steps - s0)
-        p0_life = P["p0"] if li == 0 else st["p0"]
-        run = AdjointRun(d, pncc, p, n, st["A0"], p0_life, st["b0"], rp[st["slot"]], bp[st["slot"]])
-        try:
-            fz = run.forward(prob["msmts"][s0:s0 + n].reshape(-1), P["Phi"], P["Gamma"], P["beta"], P["H"],
-                             P["gamma"])
+    # every window life is one run of a batch: one batched step per update,
+    # the records and reverses spread over the host's cores
+    lens = [min(W, steps - st["step"]) for st in starts]
+    batch = AdjointBatch(d, pncc, p, lens, [st["A0"] for st in starts],
+                         [P["p0"] if li == 0 else st["p0"] for li, st in enumerate(starts)],
+                         [st["b0"] for st in starts], [rp[st["slot"]] for st in starts],
+                         [bp[st["slot"]] for st in starts])
+    try:
+        fzs = batch.forward([prob["msmts"][st["step"]:st["step"] + n].reshape(-1) for st, n in zip(starts, lens)],
+                            P["Phi"], P["Gamma"], P["beta"], P["H"], P["gamma"])
+        Ls, ws = [], []
+        for st, n, fz in zip(starts, lens, fzs):
+            s0 = st["step"]
             w = np.zeros(n)
             Ll = 0.0
             for u in range(n):
@@ -203,24 +295,17 @@ def windowed_log_likelihood(prob, W, root_point, b_pert, p0=None, beta=None, gam
                     w[u] += 1.0 / fz[u]
                     if u >= 1:
                         w[u - 1] -= 1.0 / fz[u - 1]
-            g = run.backward(w) if with_grad and np.any(w != 0) else None
-            return Ll, g, run.timing()
-        finally:
-            run.close()
-
-    # window lives are independent: their host work overlaps on the host's
-    # cores (the library's calls release the interpreter lock)
-    from concurrent.futures import ThreadPoolExecutor
-    import os
-    workers = max(1, min(len(starts), os.cpu_count() or 1, 16))
-    with ThreadPoolExecutor(max_workers=workers) as ex:
-        results = list(ex.map(life, range(len(starts))))
+            Ls.append(Ll)
+            ws.append(w)
+        gs = batch.backward(ws) if with_grad else [None] * len(starts)
+        timing = batch.timing()
+    finally:
+        batch.close()
+    results = [(Ll, g if np.any(w != 0) else None, None) for Ll, g, w in zip(Ls, gs, ws)]
     L = 0.0
     grad = {k: np.zeros_like(v) for k, v in P.items()}
-    timing = np.zeros(4)
-    for li, (Ll, g, t) in enumerate(results):
+    for li, (Ll, g, _) in enumerate(results):
         L += Ll
-        timing += t
         if g is not None:
             for k in grad:
                 if k == "p0" and li > 0:

@@ -38,11 +38,14 @@
 #include "../../include/mce_c_api.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace mce {
@@ -54,49 +57,106 @@ using mce::cd;
 namespace {
 
 // ---------------------------------------------------------------------------
-// Host scalars of the record derivation (doubles; the GPU record chain below
-// repeats the derivation on dual numbers).
-inline double val(double x) { return x; }
-inline double absd(double x) { return std::fabs(x); }
-
+// Constants of the record derivation (the GPU record chain below repeats the
+// derivation on dual numbers).
 constexpr double kCoalignEps = 1e-8;
 constexpr double kMuEps = 1e-10;
 constexpr double kReductionEps = 1e-8;
 
-// A term's record at some point of an update.
-template <class S>
-struct Rec {
-    int m = 0;
-    std::vector<S> A, p, b;  // A m x d row-major
-    std::vector<S> q;        // row scales before normalisation (the g-table's)
-    S c = 0.0, dv = 0.0;     // c_val, d_val
-    unsigned horthog = 0;
+// Term records of one update: a slot per term with room for MS rows (A slot
+// major, its rows row-major, d wide), held in flat arrays that keep their
+// capacity from update to update, so deriving a term allocates nothing.
+struct RecSet {
+    int MS = 0, d = 0, n = 0, cap = 0;
+    std::vector<int> m;
+    std::vector<unsigned> horthog;
+    std::vector<double> c, dv;  // c_val, d_val
+    std::vector<double> A, p, b;
+    std::vector<double> q;      // row scales before normalisation (the g-table's)
+    void init(int MS_, int d_)
+    {
+        MS = MS_;
+        d = d_;
+        n = 0;
+    }
+    void ensure(int want)
+    {
+        if (want <= cap) return;
+        cap = std::max(want, 2 * cap);
+        m.resize(cap);
+        horthog.resize(cap);
+        c.resize(cap);
+        dv.resize(cap);
+        A.resize((size_t)cap * MS * d);
+        p.resize((size_t)cap * MS);
+        q.resize((size_t)cap * MS);
+        b.resize((size_t)cap * d);
+    }
+    int add()
+    {
+        ensure(n + 1);
+        return n++;
+    }
+    double* Ar(int t) { return &A[(size_t)t * MS * d]; }
+    const double* Ar(int t) const { return &A[(size_t)t * MS * d]; }
+    double* pr(int t) { return &p[(size_t)t * MS]; }
+    const double* pr(int t) const { return &p[(size_t)t * MS]; }
+    double* qr(int t) { return &q[(size_t)t * MS]; }
+    const double* qr(int t) const { return &q[(size_t)t * MS]; }
+    double* br(int t) { return &b[(size_t)t * d]; }
+    const double* br(int t) const { return &b[(size_t)t * d]; }
+    void copy_from(int t, const RecSet& o, int u)
+    {
+        m[t] = o.m[u];
+        horthog[t] = o.horthog[u];
+        c[t] = o.c[u];
+        dv[t] = o.dv[u];
+        memcpy(Ar(t), o.Ar(u), sizeof(double) * o.m[u] * d);
+        memcpy(pr(t), o.pr(u), sizeof(double) * o.m[u]);
+        memcpy(qr(t), o.qr(u), sizeof(double) * o.m[u]);
+        memcpy(br(t), o.br(u), sizeof(double) * d);
+    }
+    void swap(RecSet& o)
+    {
+        std::swap(MS, o.MS);
+        std::swap(d, o.d);
+        std::swap(n, o.n);
+        std::swap(cap, o.cap);
+        m.swap(o.m);
+        horthog.swap(o.horthog);
+        c.swap(o.c);
+        dv.swap(o.dv);
+        A.swap(o.A);
+        p.swap(o.p);
+        q.swap(o.q);
+        b.swap(o.b);
+    }
 };
 
+constexpr int kRowsMax = 32, kDMax = 8;
+
 // coalignment gate on values: +1 same, -1 opposite, 0 (cauchy_term.hpp:494-504)
-template <class S>
-int gate(const S* r, const S* c, int d)
+int gate(const double* r, const double* c, int d)
 {
     bool pos = true, neg = true;
     for (int l = 0; l < d; l++) {
-        if (pos) pos &= std::fabs(val(r[l]) - val(c[l])) < kCoalignEps;
-        if (neg) neg &= std::fabs(val(r[l]) + val(c[l])) < kCoalignEps;
+        if (pos) pos &= std::fabs(r[l] - c[l]) < kCoalignEps;
+        if (neg) neg &= std::fabs(r[l] + c[l]) < kCoalignEps;
         if (!(pos || neg)) break;
     }
     return pos ? 1 : (neg ? -1 : 0);
 }
 
-// normalize_hps (cauchy_term.hpp:458-472): p *= |A_i|_1, A_i /= |A_i|_1;
-// with set_q the scales before normalisation are kept in q.
-template <class S>
-void normalize(Rec<S>& t, int d, bool set_q)
+// normalize_hps (cauchy_term.hpp:458-472) on m rows: p *= |A_i|_1,
+// A_i /= |A_i|_1; q (if not null) receives the scales before normalisation.
+void normalize_rows(double* A, double* p, double* q, int m, int d)
 {
-    if (set_q) t.q.assign(t.p.begin(), t.p.begin() + t.m);
-    for (int i = 0; i < t.m; i++) {
-        S n1 = 0.0;
-        for (int j = 0; j < d; j++) n1 += absd(t.A[i * d + j]);
-        t.p[i] *= n1;
-        for (int j = 0; j < d; j++) t.A[i * d + j] /= n1;
+    if (q) memcpy(q, p, sizeof(double) * m);
+    for (int i = 0; i < m; i++) {
+        double n1 = 0.0;
+        for (int j = 0; j < d; j++) n1 += std::fabs(A[i * d + j]);
+        p[i] *= n1;
+        for (int j = 0; j < d; j++) A[i * d + j] /= n1;
     }
 }
 
@@ -699,39 +759,124 @@ __global__ void __launch_bounds__(128) k_adj_chain(ChainArgs a)
 }
 
 // ---------------------------------------------------------------------------
-// Device buffers (grow-only, owned by the object)
+// Device buffers (grow-only, half again as large as asked when they grow)
+// and the per-thread workspace that holds them.
 
 template <class T>
 struct Buf {
     T* ptr = nullptr;
     size_t cap = 0;
+    Buf() = default;
+    Buf(const Buf&) = delete;
+    Buf& operator=(const Buf&) = delete;
     ~Buf()
     {
         if (ptr) cudaFree(ptr);
     }
-    int ensure(size_t n)
+    // s: the stream that may still read the old buffer (finished first)
+    int ensure(size_t n, cudaStream_t s)
     {
         if (n <= cap) return MCE_OK;
-        if (ptr) cudaFree(ptr);
+        if (ptr) {
+            cudaStreamSynchronize(s);
+            cudaFree(ptr);
+        }
         ptr = nullptr;
+        const size_t want = std::max<size_t>(std::max<size_t>(n, 1), cap + cap / 2);
         cap = 0;
-        if (cudaMalloc(&ptr, sizeof(T) * std::max<size_t>(n, 1)) != cudaSuccess) {
+        if (cudaMalloc(&ptr, sizeof(T) * want) != cudaSuccess) {
             cudaGetLastError();
+            ptr = nullptr;
             mce::report_error("adjoint: device allocation failed");
             return MCE_ERR_NOMEM;
         }
-        cap = std::max<size_t>(n, 1);
+        cap = want;
         return MCE_OK;
     }
-    int upload(const T* src, size_t n)
+    // host -> device on stream s (the host buffer may be reused on return:
+    // pageable sources are staged before the call returns)
+    int upload(const T* src, size_t n, cudaStream_t s)
     {
-        int s = ensure(n);
-        if (s) return s;
-        if (n && cudaMemcpy(ptr, src, sizeof(T) * n, cudaMemcpyHostToDevice) != cudaSuccess) {
+        int st = ensure(n, s);
+        if (st) return st;
+        if (n && cudaMemcpyAsync(ptr, src, sizeof(T) * n, cudaMemcpyHostToDevice, s) != cudaSuccess) {
             mce::report_error("adjoint: host-to-device copy failed");
             return MCE_ERR_CUDA;
         }
         return MCE_OK;
+    }
+    int zero(size_t n, cudaStream_t s)
+    {
+        int st = ensure(std::max<size_t>(n, 1), s);
+        if (st) return st;
+        return cudaMemsetAsync(ptr, 0, sizeof(T) * std::max<size_t>(n, 1), s) == cudaSuccess ? MCE_OK : MCE_ERR_CUDA;
+    }
+    void swap(Buf& o)
+    {
+        std::swap(ptr, o.ptr);
+        std::swap(cap, o.cap);
+    }
+};
+
+// device -> host on stream s, waited for
+template <class T>
+int download(T* dst, const T* src, size_t n, cudaStream_t s)
+{
+    if (n == 0) return MCE_OK;
+    if (cudaMemcpyAsync(dst, src, sizeof(T) * n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+        cudaGetLastError();
+        mce::report_error("adjoint: device-to-host copy failed");
+        return MCE_ERR_CUDA;
+    }
+    return MCE_OK;
+}
+
+// Everything one host thread needs on the device to record or reverse runs,
+// on its own stream, kept from run to run so that nothing is allocated once
+// the sizes have settled.
+struct Workspace {
+    cudaStream_t s = nullptr;
+    // the parent tables (keys, values, offsets, cell counts) and whose they
+    // are: run `owner`'s kept tables after its update owner_u
+    Buf<int> pk, pcnt;
+    Buf<cd> pv;
+    Buf<long long> poff;
+    const void* owner = nullptr;
+    int owner_u = -1;
+    // the kept tables of the update being recorded or reversed
+    Buf<int> dk, dcnt;
+    Buf<cd> dv;
+    Buf<long long> doff;
+    Buf<MInfoDev> dmi;
+    Buf<long long> ditem, dkfirst;
+    Buf<cd> dvals, kbar, pbar;
+    Buf<int> dalive, dcontrib, dknm;
+    Buf<unsigned long long> derr;
+    Buf<EvalDev> dev;
+    Buf<double> dfz, qbar, dbar, cbar, ybar_e, dbar_e, cbar_e;
+    // the record chain
+    Buf<double> tin, tout, dgrad, dPA, dPp, dPb, dyb, ddb, dcb, dqt, ddt, dct;
+    Buf<double> dpar[8];
+    Buf<int> dPm, dkid, dkept;
+    Buf<unsigned> dsn, dhp;
+    int init()
+    {
+        if (s) return MCE_OK;
+        if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            s = nullptr;
+            mce::report_error("adjoint: stream creation failed");
+            return MCE_ERR_CUDA;
+        }
+        return MCE_OK;
+    }
+    ~Workspace()
+    {
+        if (s) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
     }
 };
 
@@ -770,24 +915,31 @@ struct mce_adjoint {
     int d = 0, pncc = 0, p = 0, steps = 0, MS = 0;
     std::vector<double> A0, p0, b0, root, bpert;
     mce_handle* h = nullptr;
+    int est = 0;          // this run's estimator in h
+    bool owns_h = true;   // false for the runs of an mce_adjoint_batch
     // model (LTI) and measurements of the recorded run
     std::vector<double> Phi, Gamma, beta, H, gamma, msmts;
     std::vector<Update> ups;
     double max_table_err = 0;
     double fz_check_err = 0;
     // wall ms: forward step path, forward tape (host records + GPU checks),
-    // reverse over the tables (GPU), record chain (host)
+    // reverse over the tables (GPU), record chain (GPU)
     double ms[4] = {0, 0, 0, 0};
+    // the records of the update being recorded: its parents (the previous
+    // update's kept terms), every post-MU term, the next parents
+    RecSet parents, post, next;
+    std::unique_ptr<Workspace> ws;  // the single-run calls' workspace
 
     ~mce_adjoint()
     {
-        if (h) mce_destroy(h);
+        ws.reset();
+        if (h && owns_h) mce_destroy(h);
     }
 
     int dump(Tables& T)
     {
-        T.nt = (int)mce_num_terms(h, 0);
-        const long long tot = mce_total_cells(h, 0);
+        T.nt = (int)mce_num_terms(h, est);
+        const long long tot = mce_total_cells(h, est);
         if (T.nt < 0 || tot < 0) return MCE_ERR_ARG;
         T.shape.assign(T.nt, 0);
         T.cells.assign(T.nt, 0);
@@ -796,7 +948,7 @@ struct mce_adjoint {
         T.b.assign((size_t)T.nt * d, 0);
         T.keys.assign(std::max<long long>(tot, 1), 0);
         std::vector<double> g(2 * std::max<long long>(tot, 1));
-        const int st = mce_dump_terms(h, 0, MS, T.shape.data(), T.A.data(), T.p.data(), T.b.data(), T.cells.data(),
+        const int st = mce_dump_terms(h, est, MS, T.shape.data(), T.A.data(), T.p.data(), T.b.data(), T.cells.data(),
                                       T.keys.data(), g.data());
         if (st < 0) return st;
         T.vals.resize(std::max<long long>(tot, 1));
@@ -810,9 +962,8 @@ struct mce_adjoint {
 namespace {
 
 // Gamma pre-coalignment (cauchy_util.hpp:128-210): normalised columns as rows
-template <class S>
-int precoalign(const mce_adjoint& o, const std::vector<S>& G, const std::vector<S>& beta, std::vector<S>& Gt,
-               std::vector<S>& bt)
+int precoalign(const mce_adjoint& o, const std::vector<double>& G, const std::vector<double>& beta,
+               std::vector<double>& Gt, std::vector<double>& bt)
 {
     const int d = o.d, pncc = o.pncc;
     Gt.assign((size_t)pncc * d, 0.0);
@@ -822,8 +973,8 @@ int precoalign(const mce_adjoint& o, const std::vector<S>& G, const std::vector<
         bt[i] = beta[i];
     }
     for (int i = 0; i < pncc; i++) {
-        S nf = 0.0;
-        for (int j = 0; j < d; j++) nf += absd(Gt[i * d + j]);
+        double nf = 0.0;
+        for (int j = 0; j < d; j++) nf += std::fabs(Gt[i * d + j]);
         for (int j = 0; j < d; j++) Gt[i * d + j] /= nf;
         bt[i] *= nf;
     }
@@ -851,117 +1002,177 @@ int precoalign(const mce_adjoint& o, const std::vector<S>& G, const std::vector<
     return cnt;
 }
 
-// The parameters of one run, as scalars of kind S (a tangent seeded on one).
-template <class S>
-struct Params {
-    std::vector<S> beta, gamma, p0, Phi, Gamma, H;
-};
-
-template <class S>
-Params<S> make_params(const mce_adjoint& o, int dir)
+// mu_coalign (cauchy_term.hpp:533-745) in place on a normalised record of m
+// rows (A, p, q, its orthogonal-row mask *horthog); returns the rows left and
+// fills cmap / csmap (row -> kept row, sign).
+int mu_coalign_rows(double* A, double* p, double* q, unsigned* horthog, int m, int d, int* cmap, int* csmap)
 {
-    Params<S> P;
-    int k = 0;
-    auto take = [&](std::vector<S>& v, const std::vector<double>& src) {
-        v.resize(src.size());
-        for (size_t i = 0; i < src.size(); i++, k++) v[i] = S(src[i]);
-        (void)dir;
-    };
-    take(P.beta, o.beta);
-    take(P.gamma, o.gamma);
-    take(P.p0, o.p0);
-    take(P.Phi, o.Phi);
-    take(P.Gamma, o.Gamma);
-    take(P.H, o.H);
-    return P;
+    char F[kRowsMax], hflag[kRowsMax];
+    for (int j = 0; j < m; j++) {
+        F[j] = 1;
+        hflag[j] = *horthog ? (char)((*horthog >> j) & 1) : 0;
+        cmap[j] = 255;
+        csmap[j] = 1;
+    }
+    const bool ho = *horthog != 0;
+    int uc = 0;
+    for (int j = 0; j < m - 1; j++) {
+        if (!F[j]) continue;
+        cmap[j] = uc;
+        for (int k = j + 1; k < m; k++) {
+            if (!F[k]) continue;
+            const int g = gate(&A[j * d], &A[k * d], d);
+            if (g == 1) {
+                if (ho) {
+                    const bool hj = hflag[j], hk = hflag[k];
+                    if (!hj && !hk) q[j] += q[k];
+                    else if (hj && !hk) {
+                        q[j] = q[k];
+                        hflag[j] = 0;
+                    } else if (!hj && hk) hflag[k] = 0;
+                    else {
+                        hflag[k] = 0;
+                        q[j] += q[k];
+                    }
+                } else
+                    q[j] += q[k];
+                F[k] = 0;
+                p[j] += p[k];
+                cmap[k] = uc;
+                csmap[k] = 1;
+            } else if (g == -1) {
+                if (ho) {
+                    const bool hj = hflag[j], hk = hflag[k];
+                    if (!hj && !hk) q[j] -= q[k];
+                    else if (hj && !hk) {
+                        q[j] = -q[k];
+                        hflag[j] = 0;
+                    } else if (!hj && hk) hflag[k] = 0;
+                } else
+                    q[j] -= q[k];
+                F[k] = 0;
+                p[j] += p[k];
+                cmap[k] = uc;
+                csmap[k] = -1;
+            }
+        }
+        uc++;
+    }
+    if (F[m - 1]) cmap[m - 1] = uc;
+    int ns = 0;
+    for (int i = 0; i < m; i++) ns += F[i];
+    if (ns != m) {
+        int u = 1;
+        for (int j = 1; j < m; j++)
+            if (F[j]) {
+                if (u < j) {
+                    for (int l2 = 0; l2 < d; l2++) A[u * d + l2] = A[j * d + l2];
+                    p[u] = p[j];
+                    q[u] = q[j];
+                }
+                u++;
+            }
+        if (ho) {
+            unsigned nh = 0;
+            int cc = 0;
+            for (int j = 0; j < m; j++)
+                if (F[j]) nh |= (unsigned)hflag[j] << cc++;
+            *horthog = nh;
+        }
+    }
+    return ns;
 }
 
 // One update's record derivation (the host half of step_first / step_rest,
 // include/cauchy_estimator.hpp:604-832, 1179-1208): from the kept records of
-// the previous update to every post-MU term's record before and after MU
-// coalignment.  pre[t] holds the MU output, post[t] the coalignment output.
-template <class S>
-void derive_update(const mce_adjoint& o, const Update& U, const Params<S>& P, const std::vector<Rec<S>>& parents,
-                   std::vector<Rec<S>>& pre, std::vector<Rec<S>>& post, std::vector<TermInfo>* info)
+// the previous update to every post-MU term's record after MU coalignment,
+// in creation order (the parents' own terms, then the children: step_first
+// keeps [parent, children] and step_rest lists the parents, then the
+// children).  info[t] keeps what the tape needs of the record before
+// coalignment (its g-value scalars, root-point signs and lookup keys).
+void derive_update(const mce_adjoint& o, const Update& U, const RecSet& parents, RecSet& post,
+                   std::vector<TermInfo>& info)
 {
     const int d = o.d;
-    std::vector<S> Gt, bt;
+    std::vector<double> Gt, bt;
     int gcnt = 0;
-    if (U.with_tp) gcnt = precoalign(o, P.Gamma, P.beta, Gt, bt);
-    const S* H = P.H.data() + (size_t)U.sub * d;
-    const S gam = P.gamma[U.sub];
+    if (U.with_tp) gcnt = precoalign(o, o.Gamma, o.beta, Gt, bt);
+    const double* H = o.H.data() + (size_t)U.sub * d;
+    const double gam = o.gamma[U.sub];
     const double z = o.msmts[(size_t)(&U - &o.ups[0])];
-    pre.clear();
-    post.clear();
-    if (info) info->clear();
-    std::vector<Rec<S>> kids_pre, kids_post;
-    std::vector<TermInfo> kids_info;
-    std::vector<Rec<S>> par_pre, par_post;
-    std::vector<TermInfo> par_info;
-    for (size_t pi = 0; pi < parents.size(); pi++) {
-        Rec<S> t = parents[pi];
-        const int phc = U.first ? 0 : t.m;  // the parent's table is over its rows before time propagation
+    const int nPar = parents.n;
+    post.init(o.MS, d);
+    post.ensure(nPar);
+    post.n = nPar;  // the parents' own terms come first, one per parent
+    info.clear();
+    info.resize(nPar);
+    double tA[kRowsMax * kDMax], tp_[kRowsMax], tb[kDMax], w[kRowsMax * kDMax], wb[kDMax];
+    double mu[(kRowsMax + 1) * kDMax], rho[kRowsMax + 1];
+    int sgn[kRowsMax];
+    char Fi[kRowsMax + 1];
+    for (int pi = 0; pi < nPar; pi++) {
+        int tm = parents.m[pi];
+        memcpy(tA, parents.Ar(pi), sizeof(double) * tm * d);
+        memcpy(tp_, parents.pr(pi), sizeof(double) * tm);
+        memcpy(tb, parents.br(pi), sizeof(double) * d);
+        const int phc = U.first ? 0 : tm;  // the parent's table is over its rows before time propagation
         if (U.with_tp) {
             // time_prop: A <- A Phi^T, b <- Phi b (cauchy_term.hpp:435-456)
-            std::vector<S> w(t.A.begin(), t.A.begin() + t.m * d);
-            for (int i = 0; i < t.m; i++)
+            memcpy(w, tA, sizeof(double) * tm * d);
+            for (int i = 0; i < tm; i++)
                 for (int j = 0; j < d; j++) {
-                    S s = 0.0;
-                    for (int k = 0; k < d; k++) s += w[i * d + k] * P.Phi[k + j * d];
-                    t.A[i * d + j] = s;
+                    double s = 0.0;
+                    for (int k = 0; k < d; k++) s += w[i * d + k] * o.Phi[k + j * d];
+                    tA[i * d + j] = s;
                 }
-            std::vector<S> wb(t.b);
+            memcpy(wb, tb, sizeof(double) * d);
             for (int i = 0; i < d; i++) {
-                S s = 0.0;
-                for (int j = 0; j < d; j++) s += P.Phi[i * d + j] * wb[j];
-                t.b[i] = s;
+                double s = 0.0;
+                for (int j = 0; j < d; j++) s += o.Phi[i * d + j] * wb[j];
+                tb[i] = s;
             }
             // tp_coalign (cauchy_term.hpp:475-531)
-            normalize(t, d, false);
-            std::vector<char> F(gcnt, 1);
+            normalize_rows(tA, tp_, nullptr, tm, d);
+            char F[kRowsMax];
+            for (int j = 0; j < gcnt; j++) F[j] = 1;
             for (int j = 0; j < gcnt; j++)
-                for (int k = 0; k < t.m; k++)
-                    if (F[j] && gate(&Gt[j * d], &t.A[k * d], d) != 0) {
+                for (int k = 0; k < tm; k++)
+                    if (F[j] && gate(&Gt[j * d], &tA[k * d], d) != 0) {
                         F[j] = 0;
-                        t.p[k] += bt[j];
+                        tp_[k] += bt[j];
                     }
             for (int j = 0; j < gcnt; j++)
                 if (F[j]) {
-                    t.A.resize((t.m + 1) * d);
-                    t.p.resize(t.m + 1);
-                    for (int l = 0; l < d; l++) t.A[t.m * d + l] = Gt[j * d + l];
-                    t.p[t.m] = bt[j];
-                    t.m++;
+                    for (int l = 0; l < d; l++) tA[tm * d + l] = Gt[j * d + l];
+                    tp_[tm] = bt[j];
+                    tm++;
                 }
         }
         // msmt_update (cauchy_term.hpp:84-310)
-        const int m = t.m;
-        std::vector<S> mu((m + 1) * d), rho(m + 1);
-        std::vector<int> sgn(m);
-        std::vector<char> Fi(m + 1);
-        for (int i = 0; i < m * d; i++) mu[i] = t.A[i];
-        for (int i = 0; i < m; i++) rho[i] = t.p[i];
+        const int m = tm;
+        for (int i = 0; i < m * d; i++) mu[i] = tA[i];
+        for (int i = 0; i < m; i++) rho[i] = tp_[i];
         rho[m] = gam;
         for (int j = 0; j < d; j++) mu[m * d + j] = 0.0;
         Fi[m] = 1;
         for (int l = 0; l < m; l++) {
-            S h = 0.0;
+            double h = 0.0;
             for (int j = 0; j < d; j++) h += H[j] * mu[l * d + j];
-            if (std::fabs(val(h)) < kMuEps) {
-                rho[l] = t.p[l];
+            if (std::fabs(h) < kMuEps) {
+                rho[l] = tp_[l];
                 sgn[l] = 1;
                 Fi[l] = 0;
             } else {
-                const S r = S(1.0) / h;
+                const double r = 1.0 / h;
                 for (int j = 0; j < d; j++) mu[l * d + j] *= r;
-                rho[l] = t.p[l] * absd(h);
-                sgn[l] = val(h) > 0 ? 1 : -1;
+                rho[l] = tp_[l] * std::fabs(h);
+                sgn[l] = h > 0 ? 1 : -1;
                 Fi[l] = 1;
             }
         }
-        S hb = 0.0;
-        for (int j = 0; j < d; j++) hb += H[j] * t.b[j];
-        const S zeta = S(z) - hb;
+        double hb = 0.0;
+        for (int j = 0; j < d; j++) hb += H[j] * tb[j];
+        const double zeta = z - hb;
         int esg = 0;
         for (int l = 0; l < m; l++)
             if (sgn[l] == -1) esg |= 1 << l;
@@ -969,30 +1180,32 @@ void derive_update(const mce_adjoint& o, const Update& U, const Params<S>& P, co
         if (phc < m) lhp &= (1 << phc) - 1;
         for (int tt = 0; tt <= m; tt++) {
             if (!Fi[tt]) continue;
-            Rec<S> c;
-            c.m = m;
-            c.c = zeta;
-            c.dv = rho[tt];
-            c.b.resize(d);
-            for (int j = 0; j < d; j++) c.b[j] = t.b[j] + zeta * mu[tt * d + j];
-            c.A.resize(m * d);
-            c.p.resize(m);
+            // the MU output, written into the term's slot
+            const int slot = tt == m ? pi : post.add();
+            double* cA = post.Ar(slot);
+            double* cp = post.pr(slot);
+            double* cq = post.qr(slot);
+            double* cb = post.br(slot);
+            post.m[slot] = m;
+            post.c[slot] = zeta;
+            post.dv[slot] = rho[tt];
+            for (int j = 0; j < d; j++) cb[j] = tb[j] + zeta * mu[tt * d + j];
             int l = 0;
             unsigned hof = 0;
             for (int ll = 0; ll <= m; ll++) {
                 if (ll == tt) continue;
-                c.p[l] = rho[ll];
+                cp[l] = rho[ll];
                 if (Fi[ll])
-                    for (int j = 0; j < d; j++) c.A[l * d + j] = mu[ll * d + j] - mu[tt * d + j];
+                    for (int j = 0; j < d; j++) cA[l * d + j] = mu[ll * d + j] - mu[tt * d + j];
                 else {
-                    for (int j = 0; j < d; j++) c.A[l * d + j] = mu[ll * d + j];
+                    for (int j = 0; j < d; j++) cA[l * d + j] = mu[ll * d + j];
                     hof |= 1u << l;
                 }
                 l++;
             }
-            c.horthog = hof;
+            post.horthog[slot] = hof;
             TermInfo ti;
-            ti.parent = U.first ? -1 : (int)pi;
+            ti.parent = U.first ? -1 : pi;
             ti.m_pre = m;
             ti.phc = phc;
             ti.z = tt;
@@ -1004,21 +1217,21 @@ void derive_update(const mce_adjoint& o, const Update& U, const Params<S>& P, co
             unsigned sneg = 0;
             for (int ll = 0; ll < m; ll++) {
                 double s = 0.0;
-                for (int j = 0; j < d; j++) s += val(c.A[ll * d + j]) * o.root[j];
+                for (int j = 0; j < d; j++) s += cA[ll * d + j] * o.root[j];
                 if (!(s > 0)) sneg |= 1u << ll;
             }
             if (hof) {
                 for (int ll = 0; ll < m; ll++)
-                    if (!(hof & (1u << ll))) y += val(c.p[ll]) * (((sneg >> ll) & 1) ? -1.0 : 1.0);
+                    if (!(hof & (1u << ll))) y += cp[ll] * (((sneg >> ll) & 1) ? -1.0 : 1.0);
             } else {
                 double zz = 0.0;
-                for (int ll = 0; ll < m; ll++) zz += val(c.p[ll]) * (((sneg >> ll) & 1) ? -1.0 : 1.0);
+                for (int ll = 0; ll < m; ll++) zz += cp[ll] * (((sneg >> ll) & 1) ? -1.0 : 1.0);
                 y = zz;
             }
             ti.y_eval = y;
             ti.sneg = sneg;
-            ti.d_eval = val(c.dv);
-            ti.c_eval = val(c.c);
+            ti.d_eval = rho[tt];
+            ti.c_eval = zeta;
             if (!U.first) {
                 int lp = 0, lm = 0, k = 0;
                 for (int ll = 0; ll < m; ll++) {
@@ -1040,131 +1253,36 @@ void derive_update(const mce_adjoint& o, const Update& U, const Params<S>& P, co
             } else {
                 ti.lp = ti.lm = -1;
             }
-            // MU coalignment (the parent only normalises)
-            Rec<S> cp = c;
+            // MU coalignment in place (the parent's own term only normalises)
             if (U.first || U.last) {
-                cp.q = cp.p;
+                memcpy(cq, cp, sizeof(double) * m);
                 ti.m = m;
                 ti.horthog = hof;
                 ti.has_cmap = false;
             } else if (tt == m) {
-                normalize(cp, d, true);
+                normalize_rows(cA, cp, cq, m, d);
                 ti.m = m;
                 ti.horthog = hof;
                 ti.has_cmap = false;
             } else {
-                // mu_coalign (cauchy_term.hpp:533-745)
-                normalize(cp, d, true);
-                std::vector<char> F(m, 1), hflag(m, 0);
-                int cmap[32], csmap[32];
-                for (int j = 0; j < m; j++) {
-                    cmap[j] = 255;
-                    csmap[j] = 1;
-                }
-                if (cp.horthog)
-                    for (int j = 0; j < m; j++) hflag[j] = (cp.horthog >> j) & 1;
-                int uc = 0;
-                for (int j = 0; j < m - 1; j++) {
-                    if (!F[j]) continue;
-                    cmap[j] = uc;
-                    for (int k = j + 1; k < m; k++) {
-                        if (!F[k]) continue;
-                        const int g = gate(&cp.A[j * d], &cp.A[k * d], d);
-                        if (g == 1) {
-                            if (cp.horthog) {
-                                const bool hj = hflag[j], hk = hflag[k];
-                                if (!hj && !hk) cp.q[j] += cp.q[k];
-                                else if (hj && !hk) {
-                                    cp.q[j] = cp.q[k];
-                                    hflag[j] = 0;
-                                } else if (!hj && hk) hflag[k] = 0;
-                                else {
-                                    hflag[k] = 0;
-                                    cp.q[j] += cp.q[k];
-                                }
-                            } else
-                                cp.q[j] += cp.q[k];
-                            F[k] = 0;
-                            cp.p[j] += cp.p[k];
-                            cmap[k] = uc;
-                            csmap[k] = 1;
-                        } else if (g == -1) {
-                            if (cp.horthog) {
-                                const bool hj = hflag[j], hk = hflag[k];
-                                if (!hj && !hk) cp.q[j] -= cp.q[k];
-                                else if (hj && !hk) {
-                                    cp.q[j] = -cp.q[k];
-                                    hflag[j] = 0;
-                                } else if (!hj && hk) hflag[k] = 0;
-                            } else
-                                cp.q[j] -= cp.q[k];
-                            F[k] = 0;
-                            cp.p[j] += cp.p[k];
-                            cmap[k] = uc;
-                            csmap[k] = -1;
-                        }
-                    }
-                    uc++;
-                }
-                if (F[m - 1]) cmap[m - 1] = uc;
-                int ns = 0;
-                for (int i = 0; i < m; i++) ns += F[i];
-                if (ns != m) {
-                    int u = 1;
-                    for (int j = 1; j < m; j++)
-                        if (F[j]) {
-                            if (u < j) {
-                                for (int l2 = 0; l2 < d; l2++) cp.A[u * d + l2] = cp.A[j * d + l2];
-                                cp.p[u] = cp.p[j];
-                                cp.q[u] = cp.q[j];
-                            }
-                            u++;
-                        }
-                    if (cp.horthog) {
-                        unsigned nh = 0;
-                        int cc = 0;
-                        for (int j = 0; j < m; j++)
-                            if (F[j]) nh |= (unsigned)hflag[j] << cc++;
-                        cp.horthog = nh;
-                    }
-                    cp.m = ns;
-                    cp.A.resize(ns * d);
-                    cp.p.resize(ns);
-                    cp.q.resize(ns);
-                }
-                ti.m = cp.m;
-                ti.horthog = cp.horthog;
+                normalize_rows(cA, cp, cq, m, d);
+                int cmap[kRowsMax], csmap[kRowsMax];
+                const int ns = mu_coalign_rows(cA, cp, cq, &post.horthog[slot], m, d, cmap, csmap);
+                post.m[slot] = ns;
+                ti.m = ns;
+                ti.horthog = post.horthog[slot];
                 ti.has_cmap = ns < m;
                 for (int j = 0; j < 32; j++) {
                     ti.cmap[j] = j < m ? cmap[j] : 0;
                     ti.csmap[j] = j < m ? csmap[j] : 1;
                 }
             }
-            if (tt == m) {
-                par_pre.push_back(c);
-                par_post.push_back(cp);
-                par_info.push_back(ti);
-            } else {
-                kids_pre.push_back(c);
-                kids_post.push_back(cp);
-                kids_info.push_back(ti);
-            }
+            if (tt == m)
+                info[pi] = ti;
+            else
+                info.push_back(ti);
         }
     }
-    // creation order: step_first keeps [parent, children]; step_rest lists
-    // the parents, then the children
-    if (U.first) {
-        pre = par_pre;
-        post = par_post;
-        if (info) *info = par_info;
-    } else {
-        pre = par_pre;
-        post = par_post;
-        if (info) *info = par_info;
-    }
-    pre.insert(pre.end(), kids_pre.begin(), kids_pre.end());
-    post.insert(post.end(), kids_post.begin(), kids_post.end());
-    if (info) info->insert(info->end(), kids_info.begin(), kids_info.end());
 }
 
 // orientation_mask (cell_enumeration.hpp:584-625)
@@ -1179,48 +1297,57 @@ int orientation_mask(const double* Ai, const double* Aj, int m, int d)
     return s;
 }
 
-bool same_record(const Rec<double>& t, const Tables& T, int k, int MS, int d)
+bool same_record(const RecSet& R, int t, const Tables& T, int k, int MS, int d)
 {
-    if (T.shape[k] != t.m) return false;
-    for (int i = 0; i < t.m * d; i++)
-        if (T.A[(size_t)k * MS * d + i] != t.A[i]) return false;
-    for (int i = 0; i < t.m; i++)
-        if (T.p[(size_t)k * MS + i] != t.p[i]) return false;
+    const int m = R.m[t];
+    if (T.shape[k] != m) return false;
+    const double* A = R.Ar(t);
+    const double* p = R.pr(t);
+    const double* b = R.br(t);
+    for (int i = 0; i < m * d; i++)
+        if (T.A[(size_t)k * MS * d + i] != A[i]) return false;
+    for (int i = 0; i < m; i++)
+        if (T.p[(size_t)k * MS + i] != p[i]) return false;
     for (int i = 0; i < d; i++)
-        if (T.b[(size_t)k * d + i] != t.b[i]) return false;
+        if (T.b[(size_t)k * d + i] != b[i]) return false;
     return true;
 }
 
 // fast_term_reduction (term_reduction.hpp:159-276) on one shape's terms
-void ftr(const std::vector<const Rec<double>*>& T, int d, std::vector<int>& F)
+// (indices T into R, all of m rows): F[j] = the group root of T[j]'s position
+void ftr(const RecSet& R, const std::vector<int>& T, int d, std::vector<int>& F)
 {
     const int n = (int)T.size();
     F.resize(n);
     for (int i = 0; i < n; i++) F[i] = i;
     if (n == 0) return;
-    const int m = T[0]->m;
+    const int m = R.m[T[0]];
     const double ep = kReductionEps;
     std::vector<int> ord(n);
     for (int i = 0; i < n; i++) ord[i] = i;
-    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return T[a]->b[0] < T[b]->b[0]; });
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return R.br(T[a])[0] < R.br(T[b])[0]; });
     std::vector<double> v0(n);
-    for (int i = 0; i < n; i++) v0[i] = T[ord[i]]->b[0];
+    for (int i = 0; i < n; i++) v0[i] = R.br(T[ord[i]])[0];
     for (int i = 0; i < n; i++) {
         if (F[i] != i) continue;
-        const double* bi = T[i]->b.data();
+        const double* bi = R.br(T[i]);
+        const double* pi_ = R.pr(T[i]);
+        const double* Ai = R.Ar(T[i]);
         const int s = (int)(std::upper_bound(v0.begin(), v0.end(), bi[0] - ep) - v0.begin());
         const int e = (int)(std::upper_bound(v0.begin(), v0.end(), bi[0] + ep) - v0.begin());
         for (int w = s; w < e; w++) {
             const int j = ord[w];
             if (j <= i || F[j] != j) continue;
-            const double* bj = T[j]->b.data();
+            const double* bj = R.br(T[j]);
+            const double* pj = R.pr(T[j]);
+            const double* Aj = R.Ar(T[j]);
             bool ok = true;
             for (int a = 1; a < d && ok; a++)
                 if (!(bj[a] > bi[a] - ep && bj[a] <= bi[a] + ep)) ok = false;
             for (int k = 0; k < m && ok; k++)
-                if (std::fabs(T[j]->p[k] - T[i]->p[k]) > ep) ok = false;
+                if (std::fabs(pj[k] - pi_[k]) > ep) ok = false;
             for (int k = 0; k < m && ok; k++) {
-                const double r = T[i]->A[k], c = T[j]->A[k];
+                const double r = Ai[k], c = Aj[k];
                 if (!(std::fabs(r - c) < ep || std::fabs(r + c) < ep)) ok = false;
             }
             if (ok) F[j] = i;
@@ -1228,17 +1355,17 @@ void ftr(const std::vector<const Rec<double>*>& T, int d, std::vector<int>& F)
     }
 }
 
-MInfoDev minfo_of(const TermInfo& ti, const Rec<double>& post, const Member& mb, const Tables& kept, bool first,
-                  int d)
+MInfoDev minfo_of(const TermInfo& ti, const RecSet& R, int t, const Member& mb, const Tables& kept, bool first)
 {
     MInfoDev M;
     memset(&M, 0, sizeof(M));
-    M.m = post.m;
+    const int m = R.m[t];
+    M.m = m;
     M.phc = ti.phc;
     M.z = ti.z;
     M.enc_lhp = ti.enc_lhp;
     M.flags = (ti.new_child ? kMiNewChild : 0) | (ti.has_cmap ? kMiHasCmap : 0) | (first ? kMiFirst : 0);
-    M.horthog = (int)post.horthog;
+    M.horthog = (int)R.horthog[t];
     M.s_fixed = mb.s_fixed;
     M.conj = mb.conj;
     M.kept = mb.kept;
@@ -1246,23 +1373,487 @@ MInfoDev minfo_of(const TermInfo& ti, const Rec<double>& post, const Member& mb,
     M.term = mb.term;
     M.cell_off = kept.off[mb.kept];
     M.cell_cnt = kept.cells[mb.kept];
-    M.d = post.dv;
-    M.c = post.c;
+    M.d = R.dv[t];
+    M.c = R.c[t];
+    const double* p = R.pr(t);
+    const double* q = R.qr(t);
     double ps = 0;
-    for (int i = 0; i < post.m; i++) ps += post.p[i];
+    for (int i = 0; i < m; i++) ps += p[i];
     M.ps2 = ps * ps;
-    for (int k = 0; k < post.m; k++) M.q[k] = post.q[k];
+    for (int k = 0; k < m; k++) M.q[k] = q[k];
     for (int k = 0; k < 32; k++) {
         M.cmap[k] = (signed char)ti.cmap[k];
         M.csmap[k] = (signed char)ti.csmap[k];
     }
-    (void)d;
     return M;
 }
 
 int grid_of(long long n) { return (int)std::min<long long>((n + 255) / 256, 152 * 32); }
 
+// ---------------------------------------------------------------------------
+// One run's forward record and reverse, on a workspace (its stream and
+// buffers).  The GPU step of each update is the caller's: one mce_step of the
+// run's own handle, or one mce_batch_step for every run of a batch.
+
+// Copies the model and measurements of a run and resets its records.
+int fwd_begin(mce_adjoint* o, const double* msmts, const double* Phi, const double* Gamma, const double* beta,
+              const double* H, const double* gamma)
+{
+    const int d = o->d, nup = o->steps * o->p;
+    o->msmts.assign(msmts, msmts + nup);
+    o->Phi.assign(Phi, Phi + d * d);
+    o->Gamma.assign(Gamma, Gamma + d * o->pncc);
+    o->beta.assign(beta, beta + o->pncc);
+    o->H.assign(H, H + o->p * d);
+    o->gamma.assign(gamma, gamma + o->p);
+    o->ups.assign(nup, Update());
+    o->max_table_err = 0;
+    o->fz_check_err = 0;
+    o->parents.init(o->MS, d);
+    o->next.init(o->MS, d);
+    o->parents.add();
+    o->parents.m[0] = d;
+    o->parents.horthog[0] = 0;
+    o->parents.c[0] = o->parents.dv[0] = 0.0;
+    memcpy(o->parents.Ar(0), o->A0.data(), sizeof(double) * d * d);
+    memcpy(o->parents.pr(0), o->p0.data(), sizeof(double) * d);
+    memcpy(o->parents.qr(0), o->p0.data(), sizeof(double) * d);
+    memcpy(o->parents.br(0), o->b0.data(), sizeof(double) * d);
+    return MCE_OK;
+}
+
+// Makes W's parent tables run o's kept tables after update u (no copy when
+// W recorded that update itself).
+int parent_tables(mce_adjoint* o, int u, Workspace& W)
+{
+    if (W.owner == o && W.owner_u == u) return MCE_OK;
+    const Tables& P = o->ups[u].kept;
+    int st;
+    if ((st = W.pk.upload(P.keys.data(), P.keys.size(), W.s))) return st;
+    if ((st = W.pv.upload(P.vals.data(), P.vals.size(), W.s))) return st;
+    if ((st = W.poff.upload(P.off.data(), P.off.size(), W.s))) return st;
+    if ((st = W.pcnt.upload(P.cells.data(), P.cells.size(), W.s))) return st;
+    W.owner = o;
+    W.owner_u = u;
+    return MCE_OK;
+}
+
+// Records update u of run o after the GPU step has run it: the update's fz,
+// every post-MU term's record, the reduction groups and the kept tables.
+int fwd_record(mce_adjoint* o, int u, Workspace& W, double* fz_raw)
+{
+    const int d = o->d, nup = (int)o->ups.size();
+    const cudaStream_t s = W.s;
+    Update& U = o->ups[u];
+    U.first = u == 0;
+    U.last = u == nup - 1;
+    U.sub = u % o->p;
+    U.with_tp = !U.first && (u % o->p) == 0;
+    struct Lap {
+        double* acc;
+        std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+        ~Lap() { *acc += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count(); }
+    } lap{&o->ms[1]};
+    int st;
+    double rfz[2], rm[16], rc[128], gs;
+    st = mce_get_raw_moments(o->h, o->est, rfz, rm, rc, &gs);
+    if (st < 0) return st;
+    // Re fz of the update: 1/(2 pi G_SCALE_FACTOR) (the raw copy of the
+    // first update is not kept by the step path)
+    U.gscale = gs;
+    U.fz_raw = 1.0 / (2.0 * mce::kPi * gs);
+    if (fz_raw) fz_raw[u] = U.fz_raw;
+    // host records
+    derive_update(*o, U, o->parents, o->post, U.terms);
+    const RecSet& post = o->post;
+    if (!U.first && (st = parent_tables(o, u - 1, W))) return st;
+    // the fz tape: recompute Re fz from the recorded lookups on the GPU
+    {
+        std::vector<EvalDev> ev(U.terms.size());
+        for (size_t t = 0; t < U.terms.size(); t++) {
+            const TermInfo& ti = U.terms[t];
+            ev[t] = EvalDev{ti.parent < 0 ? 0 : ti.parent, ti.lp, ti.lm, ti.enc_lhp, ti.phc, U.first ? 1 : 0,
+                            ti.y_eval, ti.d_eval, ti.c_eval};
+        }
+        if ((st = W.dev.upload(ev.data(), ev.size(), s))) return st;
+        if ((st = W.dfz.ensure(ev.size(), s))) return st;
+        if (!ev.empty())
+            k_adj_eval_fz<<<grid_of((long long)ev.size()), 256, 0, s>>>(W.dev.ptr, (int)ev.size(), W.pk.ptr, W.pv.ptr,
+                                                                    W.poff.ptr, W.pcnt.ptr, W.dfz.ptr);
+        std::vector<double> f(ev.size());
+        if ((st = download(f.data(), W.dfz.ptr, f.size(), s))) return st;
+        double sum = 0;
+        for (double x : f) sum += x;
+        o->fz_check_err =
+            std::max(o->fz_check_err, std::fabs(sum - U.fz_raw) / std::max(std::fabs(U.fz_raw), 1e-300));
+    }
+    if (U.last) return MCE_OK;
+    if ((st = o->dump(U.kept))) return st;
+    const Tables& K = U.kept;
+    // reduction groups and which post-MU term each kept slot holds
+    std::vector<std::vector<int>> byshape(o->MS + 1);
+    for (int t = 0; t < post.n; t++) byshape[post.m[t]].push_back(t);
+    U.kept_first.assign(K.nt, 0);
+    U.kept_n.assign(K.nt, 0);
+    U.kept_term.assign(K.nt, -1);
+    U.members.clear();
+    int slot = 0;
+    // candidates per kept slot (in member order): (term, s_fixed, conj)
+    for (int m = 0; m <= o->MS; m++) {
+        if (byshape[m].empty()) continue;
+        const std::vector<int>& T = byshape[m];
+        std::vector<int> F;
+        if (U.first) {
+            F.resize(T.size());
+            for (size_t i = 0; i < T.size(); i++) F[i] = (int)i;
+        } else
+            ftr(post, T, d, F);
+        std::vector<std::vector<int>> mem(T.size());
+        for (size_t j = 0; j < T.size(); j++)
+            if (F[j] != (int)j) mem[F[j]].push_back((int)j);
+        for (size_t j = 0; j < T.size(); j++) {
+            if (F[j] != (int)j) continue;
+            // which candidate (root, or the first surviving member) holds this group's kept slot
+            std::vector<int> cand;
+            cand.push_back((int)j);
+            for (int x : mem[j]) cand.push_back(x);
+            int holder = -1;
+            if (slot < K.nt)
+                for (size_t c = 0; c < cand.size(); c++)
+                    if (same_record(post, T[cand[c]], K, slot, o->MS, d)) {
+                        holder = (int)c;
+                        break;
+                    }
+            if (holder < 0) continue;  // the whole group was approximated out
+            const int root_term = T[cand[holder]];
+            U.kept_term[slot] = root_term;
+            U.kept_first[slot] = (int)U.members.size();
+            for (size_t c = holder; c < cand.size(); c++) {
+                const int term = T[cand[c]];
+                Member mb;
+                mb.term = term;
+                mb.kept = slot;
+                int sm = orientation_mask(post.Ar(root_term), post.Ar(term), m, d);
+                const int top = 1 << (m - 1), rev = (1 << m) - 1;
+                mb.conj = (sm & top) ? 1 : 0;
+                if (sm & top) sm ^= rev;
+                mb.s_fixed = c == (size_t)holder ? 0 : sm;
+                if (c == (size_t)holder) mb.conj = 0;
+                mb.contrib = 1;
+                U.members.push_back(mb);
+            }
+            U.kept_n[slot] = (int)U.members.size() - U.kept_first[slot];
+            slot++;
+        }
+    }
+    if (slot != K.nt) {
+        mce::report_error("adjoint: the reduction groups do not match the GPU's kept terms (update " +
+                          std::to_string(u) + ")");
+        return MCE_ERR_DEVICE;
+    }
+    // member values on the GPU: approximation flags and the table check
+    const int nmem = (int)U.members.size();
+    std::vector<MInfoDev> mi(nmem);
+    std::vector<long long> item_off(nmem + 1, 0);
+    for (int j = 0; j < nmem; j++) {
+        const Member& mb = U.members[j];
+        mi[j] = minfo_of(U.terms[mb.term], post, mb.term, mb, K, U.first);
+        item_off[j + 1] = item_off[j] + K.cells[mb.kept];
+    }
+    const long long nitems = item_off[nmem];
+    if ((st = W.dmi.upload(mi.data(), nmem, s))) return st;
+    if ((st = W.ditem.upload(item_off.data(), nmem + 1, s))) return st;
+    U.mi.swap(mi);
+    U.item_off.swap(item_off);
+    if ((st = W.dk.upload(K.keys.data(), K.keys.size(), s))) return st;
+    if ((st = W.dv.upload(K.vals.data(), K.vals.size(), s))) return st;
+    if ((st = W.doff.upload(K.off.data(), K.off.size(), s))) return st;
+    if ((st = W.dcnt.upload(K.cells.data(), K.cells.size(), s))) return st;
+    if ((st = W.dvals.ensure(nitems + 1, s))) return st;
+    if ((st = W.dalive.zero(nmem + 1, s))) return st;
+    if (nitems > 0)
+        k_adj_member_values<<<grid_of(nitems), 256, 0, s>>>(W.dmi.ptr, W.ditem.ptr, nmem, nitems, W.dk.ptr, W.pk.ptr,
+                                                          W.pv.ptr, W.poff.ptr, W.pcnt.ptr, U.gscale, W.dvals.ptr,
+                                                          W.dalive.ptr);
+    std::vector<int> alive(nmem);
+    if ((st = download(alive.data(), W.dalive.ptr, nmem, s))) return st;
+    for (int j = 0; j < nmem; j++) U.members[j].contrib = (U.first || alive[j]) ? 1 : 0;
+    for (int k = 0; k < K.nt; k++) U.members[U.kept_first[k]].contrib = 1;  // the holder itself
+    std::vector<int> contrib(nmem);
+    for (int j = 0; j < nmem; j++) contrib[j] = U.members[j].contrib;
+    std::vector<long long> kf(K.nt);
+    for (int k = 0; k < K.nt; k++) kf[k] = U.kept_first[k];
+    if ((st = W.dcontrib.upload(contrib.data(), nmem, s))) return st;
+    if ((st = W.dkfirst.upload(kf.data(), K.nt, s))) return st;
+    if ((st = W.dknm.upload(U.kept_n.data(), K.nt, s))) return st;
+    if ((st = W.derr.zero(1, s))) return st;
+    const long long ncells = K.off[K.nt];
+    if (ncells > 0)
+        k_adj_check_tables<<<grid_of(ncells), 256, 0, s>>>(W.dkfirst.ptr, W.dknm.ptr, W.dmi.ptr, W.ditem.ptr,
+                                                         W.dcontrib.ptr, W.dvals.ptr, W.doff.ptr, W.dcnt.ptr, W.dv.ptr,
+                                                         K.nt, W.derr.ptr);
+    unsigned long long eb = 0;
+    if ((st = download(&eb, W.derr.ptr, 1, s))) return st;
+    double e;
+    memcpy(&e, &eb, sizeof(e));
+    o->max_table_err = std::max(o->max_table_err, e);
+    // the next parents: the kept terms' records
+    o->next.init(o->MS, d);
+    o->next.ensure(K.nt);
+    o->next.n = K.nt;
+    for (int k = 0; k < K.nt; k++) o->next.copy_from(k, post, U.kept_term[k]);
+    o->parents.swap(o->next);
+    // the kept tables are the next update's parent tables
+    W.pk.swap(W.dk);
+    W.pv.swap(W.dv);
+    W.poff.swap(W.doff);
+    W.pcnt.swap(W.dcnt);
+    W.owner = o;
+    W.owner_u = u;
+    if (cudaGetLastError() != cudaSuccess) return MCE_ERR_CUDA;
+    return MCE_OK;
+}
+
+int num_params(const mce_adjoint* o)
+{
+    return o->pncc + o->p + o->d + o->d * o->d + o->d * o->pncc + o->p * o->d;
+}
+
+// The reverse of run o's recorded updates with seeds w[steps*p]: grad[num_params].
+int bwd_run(mce_adjoint* o, const double* w, double* grad, Workspace& W)
+{
+    const int nup = (int)o->ups.size();
+    const cudaStream_t s = W.s;
+    int st;
+    auto tb0 = std::chrono::steady_clock::now();
+    // ---- reverse over the tables and the fz seeds (GPU)
+    std::vector<cd> tbar;  // adjoint of the kept tables of update u (from update u+1)
+    for (int u = nup - 1; u >= 0; u--) {
+        Update& U = o->ups[u];
+        const Tables* P = u > 0 ? &o->ups[u - 1].kept : nullptr;
+        const long long npc = P ? P->off[P->nt] : 0;
+        if ((st = W.pbar.zero(npc + 1, s))) return st;
+        if (P && (st = parent_tables(o, u - 1, W))) return st;
+        // the tables built at this update
+        const int nmem = (int)U.mi.size();
+        U.qbar.assign((size_t)nmem * 32, 0.0);
+        U.dbar_m.assign(nmem, 0.0);
+        U.cbar_m.assign(nmem, 0.0);
+        if (!U.last && nmem > 0) {
+            const Tables& K = U.kept;
+            const long long nitems = U.item_off[nmem];
+            std::vector<int> contrib(nmem);
+            for (int j = 0; j < nmem; j++) contrib[j] = U.members[j].contrib;
+            if ((st = W.dmi.upload(U.mi.data(), nmem, s))) return st;
+            if ((st = W.ditem.upload(U.item_off.data(), nmem + 1, s))) return st;
+            if ((st = W.dcontrib.upload(contrib.data(), nmem, s))) return st;
+            if ((st = W.dk.upload(K.keys.data(), K.keys.size(), s))) return st;
+            if (tbar.size() != K.vals.size()) tbar.assign(K.vals.size(), mce::mkcd(0, 0));
+            if ((st = W.kbar.upload(tbar.data(), tbar.size(), s))) return st;
+            if ((st = W.qbar.zero((size_t)nmem * 32, s))) return st;
+            if ((st = W.dbar.zero(nmem, s))) return st;
+            if ((st = W.cbar.zero(nmem, s))) return st;
+            if (nitems > 0)
+                k_adj_member_reverse<<<grid_of(nitems), 256, 0, s>>>(
+                    W.dmi.ptr, W.ditem.ptr, nmem, nitems, W.dcontrib.ptr, W.dk.ptr, W.kbar.ptr, W.pk.ptr, W.pv.ptr,
+                    W.poff.ptr, W.pcnt.ptr, U.gscale, W.pbar.ptr, W.qbar.ptr, W.dbar.ptr, W.cbar.ptr);
+            if ((st = download(U.qbar.data(), W.qbar.ptr, (size_t)nmem * 32, s))) return st;
+            if ((st = download(U.dbar_m.data(), W.dbar.ptr, nmem, s))) return st;
+            if ((st = download(U.cbar_m.data(), W.cbar.ptr, nmem, s))) return st;
+        }
+        // the fz seed of this update
+        const int nt = (int)U.terms.size();
+        U.ybar_e.assign(nt, 0.0);
+        U.dbar_e.assign(nt, 0.0);
+        U.cbar_e.assign(nt, 0.0);
+        if (w[u] != 0.0 && nt > 0) {
+            std::vector<EvalDev> ev(nt);
+            for (int t = 0; t < nt; t++) {
+                const TermInfo& ti = U.terms[t];
+                ev[t] = EvalDev{ti.parent < 0 ? 0 : ti.parent, ti.lp, ti.lm, ti.enc_lhp, ti.phc, U.first ? 1 : 0,
+                                ti.y_eval, ti.d_eval, ti.c_eval};
+            }
+            if ((st = W.dev.upload(ev.data(), nt, s))) return st;
+            if ((st = W.ybar_e.ensure(nt, s))) return st;
+            if ((st = W.dbar_e.ensure(nt, s))) return st;
+            if ((st = W.cbar_e.ensure(nt, s))) return st;
+            k_adj_eval_reverse<<<grid_of(nt), 256, 0, s>>>(W.dev.ptr, nt, w[u], W.pk.ptr, W.pv.ptr, W.poff.ptr,
+                                                            W.pcnt.ptr, W.pbar.ptr, W.ybar_e.ptr, W.dbar_e.ptr,
+                                                            W.cbar_e.ptr);
+            if ((st = download(U.ybar_e.data(), W.ybar_e.ptr, nt, s))) return st;
+            if ((st = download(U.dbar_e.data(), W.dbar_e.ptr, nt, s))) return st;
+            if ((st = download(U.cbar_e.data(), W.cbar_e.ptr, nt, s))) return st;
+        }
+        tbar.assign(npc, mce::mkcd(0, 0));
+        if ((st = download(tbar.data(), W.pbar.ptr, npc, s))) return st;
+    }
+    if (cudaGetLastError() != cudaSuccess) return MCE_ERR_CUDA;
+    // ---- the record chain on the GPU: a thread per (parent, direction)
+    // repeats the parent's derivation on dual numbers and dots the tangents
+    // of the scalars that enter the g values with their adjoints
+    auto tb1 = std::chrono::steady_clock::now();
+    o->ms[2] += std::chrono::duration<double, std::milli>(tb1 - tb0).count();
+    const int N = num_params(o);
+    const int d = o->d, MS = o->MS, rec = MS * d + MS + d;
+    long long maxP = 1;
+    for (int u = 0; u + 1 < nup; u++) maxP = std::max<long long>(maxP, o->ups[u].kept.nt);
+    if ((st = W.tin.ensure((size_t)N * maxP * rec, s))) return st;
+    if ((st = W.tout.ensure((size_t)N * maxP * rec, s))) return st;
+    if ((st = W.dgrad.zero(N, s))) return st;
+    const std::vector<double>* pv_[8] = {&o->beta, &o->gamma, &o->p0, &o->Phi, &o->Gamma, &o->H, &o->A0, &o->b0};
+    for (int i = 0; i < 8; i++)
+        if ((st = W.dpar[i].upload(pv_[i]->data(), pv_[i]->size(), s))) return st;
+    for (int u = 0; u < nup; u++) {
+        const Update& U = o->ups[u];
+        const int nt = (int)U.terms.size();
+        const int nP = u == 0 ? 1 : o->ups[u - 1].kept.nt;
+        if (u > 0) {
+            const Tables& K = o->ups[u - 1].kept;
+            if ((st = W.dPm.upload(K.shape.data(), K.shape.size(), s))) return st;
+            if ((st = W.dPA.upload(K.A.data(), K.A.size(), s))) return st;
+            if ((st = W.dPp.upload(K.p.data(), K.p.size(), s))) return st;
+            if ((st = W.dPb.upload(K.b.data(), K.b.size(), s))) return st;
+        }
+        std::vector<int> kid_off(nP, 0), nk(nP, 0);
+        for (int t = nP; t < nt; t++) nk[U.terms[t].parent < 0 ? 0 : U.terms[t].parent]++;
+        for (int i = 0, acc = nP; i < nP; i++) {
+            kid_off[i] = acc;
+            acc += nk[i];
+        }
+        std::vector<unsigned> sn(nt), hp(nt);
+        for (int t = 0; t < nt; t++) {
+            sn[t] = U.terms[t].sneg;
+            hp[t] = U.terms[t].horthog_pre;
+        }
+        std::vector<double> qt((size_t)nt * 32, 0.0), dt(nt, 0.0), ct(nt, 0.0);
+        for (size_t j = 0; j < U.members.size(); j++) {
+            const Member& mb = U.members[j];
+            if (!mb.contrib || U.qbar.empty()) continue;
+            for (int k = 0; k < 32; k++) qt[(size_t)mb.term * 32 + k] = U.qbar[j * 32 + k];
+            dt[mb.term] = U.dbar_m[j];
+            ct[mb.term] = U.cbar_m[j];
+        }
+        std::vector<int> kept_of(nt, -1);
+        const int n_next = U.last ? 0 : (int)U.kept_term.size();
+        for (int k = 0; k < n_next; k++) kept_of[U.kept_term[k]] = k;
+        if ((st = W.dkid.upload(kid_off.data(), nP, s))) return st;
+        if ((st = W.dsn.upload(sn.data(), nt, s))) return st;
+        if ((st = W.dhp.upload(hp.data(), nt, s))) return st;
+        if ((st = W.dyb.upload(U.ybar_e.data(), nt, s))) return st;
+        if ((st = W.ddb.upload(U.dbar_e.data(), nt, s))) return st;
+        if ((st = W.dcb.upload(U.cbar_e.data(), nt, s))) return st;
+        if ((st = W.dqt.upload(qt.data(), qt.size(), s))) return st;
+        if ((st = W.ddt.upload(dt.data(), nt, s))) return st;
+        if ((st = W.dct.upload(ct.data(), nt, s))) return st;
+        if ((st = W.dkept.upload(kept_of.data(), nt, s))) return st;
+        ChainArgs ca;
+        ca.d = d;
+        ca.pncc = o->pncc;
+        ca.p = o->p;
+        ca.MS = MS;
+        ca.N = N;
+        ca.first = U.first;
+        ca.last = U.last;
+        ca.with_tp = U.with_tp;
+        ca.sub = U.sub;
+        ca.nP = nP;
+        ca.z = o->msmts[u];
+        ca.beta = W.dpar[0].ptr;
+        ca.gamma = W.dpar[1].ptr;
+        ca.p0 = W.dpar[2].ptr;
+        ca.Phi = W.dpar[3].ptr;
+        ca.Gamma = W.dpar[4].ptr;
+        ca.H = W.dpar[5].ptr;
+        ca.A0 = W.dpar[6].ptr;
+        ca.b0 = W.dpar[7].ptr;
+        ca.PA = W.dPA.ptr;
+        ca.Pp = W.dPp.ptr;
+        ca.Pb = W.dPb.ptr;
+        ca.Pm = W.dPm.ptr;
+        ca.Tin = W.tin.ptr;
+        ca.Tout = W.tout.ptr;
+        ca.rec = rec;
+        ca.n_next = n_next;
+        ca.kid_off = W.dkid.ptr;
+        ca.sneg = W.dsn.ptr;
+        ca.hpre = W.dhp.ptr;
+        ca.ybar_e = W.dyb.ptr;
+        ca.dbar_e = W.ddb.ptr;
+        ca.cbar_e = W.dcb.ptr;
+        ca.qbar_t = W.dqt.ptr;
+        ca.dbar_t = W.ddt.ptr;
+        ca.cbar_t = W.dct.ptr;
+        ca.kept_of = W.dkept.ptr;
+        ca.grad = W.dgrad.ptr;
+        const long long nthr = (long long)nP * N;
+        k_adj_chain<<<(int)((nthr + 127) / 128), 128, 0, s>>>(ca);
+        W.tin.swap(W.tout);
+    }
+    if ((st = download(grad, W.dgrad.ptr, N, s))) {
+        mce::report_error("adjoint: the record chain failed on the GPU");
+        return st;
+    }
+    o->ms[3] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb1).count();
+    return MCE_OK;
+}
+
+// Runs f(i, worker) for i in [0, n) on up to T host threads (worker 0 is the
+// caller), each on device `dev`; returns the first failure's status and
+// passes its message on to the calling thread.
+template <class F>
+int parallel_runs(int n, int T, int dev, F&& f)
+{
+    std::atomic<int> next{0};
+    std::atomic<int> err{0};
+    std::string msg;
+    std::mutex mm;
+    auto body = [&](int w) {
+        if (w > 0) cudaSetDevice(dev);
+        for (;;) {
+            const int i = next++;
+            if (i >= n || err.load() != 0) break;
+            const int st = f(i, w);
+            if (st < 0) {
+                int z = 0;
+                if (err.compare_exchange_strong(z, st)) {
+                    std::lock_guard<std::mutex> l(mm);
+                    msg = mce_last_error();
+                }
+            }
+        }
+    };
+    T = std::max(1, std::min(T, n));
+    std::vector<std::thread> th;
+    for (int w = 1; w < T; w++) th.emplace_back(body, w);
+    body(0);
+    for (auto& t : th) t.join();
+    if (err.load() != 0) mce::report_error(msg);
+    return err.load();
+}
+
+int host_threads(int n)
+{
+    int T = (int)std::thread::hardware_concurrency();
+    if (T <= 0) T = 1;
+    return std::max(1, std::min(std::min(T, 16), n));
+}
+
 }  // namespace
+
+// A batch of runs of one LTI model, stepped together by one batched handle.
+struct mce_adjoint_batch {
+    int n = 0, d = 0, pncc = 0, p = 0, dev = 0, threads = 1;
+    mce_handle* h = nullptr;
+    std::vector<std::unique_ptr<mce_adjoint>> runs;
+    std::vector<std::unique_ptr<Workspace>> ws;
+    double ms[4] = {0, 0, 0, 0};
+    ~mce_adjoint_batch()
+    {
+        runs.clear();
+        ws.clear();
+        if (h) mce_destroy(h);
+    }
+};
 
 extern "C" {
 
@@ -1302,214 +1893,21 @@ int mce_adjoint_forward(mce_adjoint* o, const double* msmts, const double* Phi, 
                         const double* beta, const double* H, const double* gamma, double* fz_raw)
 {
     if (!o || !msmts || !Phi || !Gamma || !beta || !H || !gamma) return MCE_ERR_ARG;
-    const int d = o->d, nup = o->steps * o->p;
-    o->msmts.assign(msmts, msmts + nup);
-    o->Phi.assign(Phi, Phi + d * d);
-    o->Gamma.assign(Gamma, Gamma + d * o->pncc);
-    o->beta.assign(beta, beta + o->pncc);
-    o->H.assign(H, H + o->p * d);
-    o->gamma.assign(gamma, gamma + o->p);
-    int st = mce_reset(o->h);
-    if (st < 0) return st;
-    o->ups.assign(nup, Update());
-    o->max_table_err = 0;
-    o->fz_check_err = 0;
-    Params<double> P = make_params<double>(*o, -1);
-    std::vector<Rec<double>> parents(1), pre, post;
-    parents[0].m = d;
-    parents[0].A = o->A0;
-    parents[0].p = o->p0;
-    parents[0].b = o->b0;
-    const Tables* prev = nullptr;
-    Buf<int> dk, pk;
-    Buf<cd> dv, pv;
-    Buf<long long> doff, poffb;
-    Buf<int> dcnt, pcntb;
-    Buf<MInfoDev> dmi;
-    Buf<long long> ditem;
-    Buf<cd> dvals;
-    Buf<int> dalive, dcontrib;
-    Buf<long long> dkfirst;
-    Buf<int> dknm;
-    Buf<unsigned long long> derr;
-    Buf<EvalDev> dev;
-    Buf<double> dfz;
+    int st;
+    if (!o->ws) o->ws.reset(new Workspace());
+    if ((st = o->ws->init())) return st;
+    o->ws->owner = nullptr;
+    if ((st = fwd_begin(o, msmts, Phi, Gamma, beta, H, gamma))) return st;
+    if ((st = mce_reset(o->h)) < 0) return st;
+    const int d = o->d, nup = (int)o->ups.size();
     for (int u = 0; u < nup; u++) {
-        Update& U = o->ups[u];
-        U.first = u == 0;
-        U.last = u == nup - 1;
-        U.sub = u % o->p;
-        U.with_tp = !U.first && (u % o->p) == 0;
-        // the GPU step
+        const int sub = u % o->p;
         auto t0 = std::chrono::steady_clock::now();
-        st = mce_step(o->h, msmts[u], Phi, Gamma, beta, H + (size_t)U.sub * d, gamma[U.sub], nullptr, nullptr);
+        st = mce_step(o->h, msmts[u], Phi, Gamma, beta, H + (size_t)sub * d, gamma[sub], nullptr, nullptr);
         if (st < 0) return st;
-        auto t1 = std::chrono::steady_clock::now();
-        o->ms[0] += std::chrono::duration<double, std::milli>(t1 - t0).count();
-        struct Lap {
-            double* acc;
-            std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
-            ~Lap() { *acc += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count(); }
-        } lap{&o->ms[1]};
-        double rfz[2], rm[16], rc[128], gs;
-        st = mce_get_raw_moments(o->h, 0, rfz, rm, rc, &gs);
-        if (st < 0) return st;
-        // Re fz of the update: 1/(2 pi G_SCALE_FACTOR) (the raw copy of the
-        // first update is not kept by the step path)
-        U.gscale = gs;
-        U.fz_raw = 1.0 / (2.0 * mce::kPi * gs);
-        if (fz_raw) fz_raw[u] = U.fz_raw;
-        // host records
-        derive_update(*o, U, P, parents, pre, post, &U.terms);
-        // the fz tape: recompute Re fz from the recorded lookups on the GPU
-        {
-            std::vector<EvalDev> ev(U.terms.size());
-            for (size_t t = 0; t < U.terms.size(); t++) {
-                const TermInfo& ti = U.terms[t];
-                ev[t] = EvalDev{ti.parent < 0 ? 0 : ti.parent, ti.lp, ti.lm, ti.enc_lhp, ti.phc, U.first ? 1 : 0,
-                                ti.y_eval, val(pre[t].dv), val(pre[t].c)};
-            }
-            if ((st = dev.upload(ev.data(), ev.size()))) return st;
-            if ((st = dfz.ensure(ev.size()))) return st;
-            if (!U.first) {
-                if ((st = pk.upload(prev->keys.data(), prev->keys.size()))) return st;
-                if ((st = pv.upload(prev->vals.data(), prev->vals.size()))) return st;
-                if ((st = poffb.upload(prev->off.data(), prev->off.size()))) return st;
-                if ((st = pcntb.upload(prev->cells.data(), prev->cells.size()))) return st;
-            }
-            if (!ev.empty())
-                k_adj_eval_fz<<<grid_of((long long)ev.size()), 256>>>(dev.ptr, (int)ev.size(), pk.ptr, pv.ptr,
-                                                                  poffb.ptr, pcntb.ptr, dfz.ptr);
-            std::vector<double> f(ev.size());
-            if (cudaMemcpy(f.data(), dfz.ptr, sizeof(double) * f.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
-                return MCE_ERR_CUDA;
-            double s = 0;
-            for (double x : f) s += x;
-            o->fz_check_err = std::max(o->fz_check_err, std::fabs(s - U.fz_raw) / std::max(std::fabs(U.fz_raw), 1e-300));
-        }
-        if (U.last) break;
-        if ((st = o->dump(U.kept))) return st;
-        const Tables& K = U.kept;
-        // reduction groups and which post-MU term each kept slot holds
-        std::vector<std::vector<int>> byshape(o->MS + 1);
-        for (size_t t = 0; t < post.size(); t++) byshape[post[t].m].push_back((int)t);
-        U.kept_first.assign(K.nt, 0);
-        U.kept_n.assign(K.nt, 0);
-        U.kept_term.assign(K.nt, -1);
-        int slot = 0;
-        // candidates per kept slot (in member order): (term, s_fixed, conj)
-        for (int m = 0; m <= o->MS; m++) {
-            if (byshape[m].empty()) continue;
-            std::vector<const Rec<double>*> T;
-            for (int t : byshape[m]) T.push_back(&post[t]);
-            std::vector<int> F;
-            if (U.first) {
-                F.resize(T.size());
-                for (size_t i = 0; i < T.size(); i++) F[i] = (int)i;
-            } else
-                ftr(T, d, F);
-            std::vector<std::vector<int>> mem(T.size());
-            for (size_t j = 0; j < T.size(); j++)
-                if (F[j] != (int)j) mem[F[j]].push_back((int)j);
-            for (size_t j = 0; j < T.size(); j++) {
-                if (F[j] != (int)j) continue;
-                // which candidate (root, or the first surviving member) holds this group's kept slot
-                std::vector<int> cand;
-                cand.push_back((int)j);
-                for (int x : mem[j]) cand.push_back(x);
-                int holder = -1;
-                if (slot < K.nt)
-                    for (size_t c = 0; c < cand.size(); c++)
-                        if (same_record(*T[cand[c]], K, slot, o->MS, d)) {
-                            holder = (int)c;
-                            break;
-                        }
-                if (holder < 0) continue;  // the whole group was approximated out
-                const int root_term = byshape[m][cand[holder]];
-                U.kept_term[slot] = root_term;
-                U.kept_first[slot] = (int)U.members.size();
-                for (size_t c = holder; c < cand.size(); c++) {
-                    const int term = byshape[m][cand[c]];
-                    Member mb;
-                    mb.term = term;
-                    mb.kept = slot;
-                    int s = orientation_mask(post[root_term].A.data(), post[term].A.data(), m, d);
-                    const int top = 1 << (m - 1), rev = (1 << m) - 1;
-                    mb.conj = (s & top) ? 1 : 0;
-                    if (s & top) s ^= rev;
-                    mb.s_fixed = c == (size_t)holder ? 0 : s;
-                    if (c == (size_t)holder) mb.conj = 0;
-                    mb.contrib = 1;
-                    U.members.push_back(mb);
-                }
-                U.kept_n[slot] = (int)U.members.size() - U.kept_first[slot];
-                slot++;
-            }
-        }
-        if (slot != K.nt) {
-            mce::report_error("adjoint: the reduction groups do not match the GPU's kept terms (update " +
-                              std::to_string(u) + ")");
-            return MCE_ERR_DEVICE;
-        }
-        // member values on the GPU: approximation flags and the table check
-        const int nmem = (int)U.members.size();
-        std::vector<MInfoDev> mi(nmem);
-        std::vector<long long> item_off(nmem + 1, 0);
-        for (int j = 0; j < nmem; j++) {
-            const Member& mb = U.members[j];
-            mi[j] = minfo_of(U.terms[mb.term], post[mb.term], mb, K, U.first, d);
-            item_off[j + 1] = item_off[j] + K.cells[mb.kept];
-        }
-        const long long nitems = item_off[nmem];
-        if ((st = dmi.upload(mi.data(), nmem))) return st;
-        if ((st = ditem.upload(item_off.data(), nmem + 1))) return st;
-        U.mi = mi;
-        U.item_off = item_off;
-        if ((st = dk.upload(K.keys.data(), K.keys.size()))) return st;
-        if ((st = dv.upload(K.vals.data(), K.vals.size()))) return st;
-        if ((st = doff.upload(K.off.data(), K.off.size()))) return st;
-        if ((st = dcnt.upload(K.cells.data(), K.cells.size()))) return st;
-        if ((st = dvals.ensure(nitems + 1))) return st;
-        if ((st = dalive.ensure(nmem + 1))) return st;
-        cudaMemset(dalive.ptr, 0, sizeof(int) * (nmem + 1));
-        if (nitems > 0)
-            k_adj_member_values<<<grid_of(nitems), 256>>>(dmi.ptr, ditem.ptr, nmem, nitems, dk.ptr, pk.ptr, pv.ptr,
-                                                       poffb.ptr, pcntb.ptr, U.gscale, dvals.ptr, dalive.ptr);
-        std::vector<int> alive(nmem);
-        if (cudaMemcpy(alive.data(), dalive.ptr, sizeof(int) * nmem, cudaMemcpyDeviceToHost) != cudaSuccess)
-            return MCE_ERR_CUDA;
-        for (int j = 0; j < nmem; j++) U.members[j].contrib = (U.first || alive[j]) ? 1 : 0;
-        for (int k = 0; k < K.nt; k++) U.members[U.kept_first[k]].contrib = 1;  // the holder itself
-        std::vector<int> contrib(nmem);
-        for (int j = 0; j < nmem; j++) contrib[j] = U.members[j].contrib;
-        std::vector<long long> kf(K.nt);
-        for (int k = 0; k < K.nt; k++) kf[k] = U.kept_first[k];
-        if ((st = dcontrib.upload(contrib.data(), nmem))) return st;
-        if ((st = dkfirst.upload(kf.data(), K.nt))) return st;
-        if ((st = dknm.upload(U.kept_n.data(), K.nt))) return st;
-        if ((st = derr.ensure(1))) return st;
-        cudaMemset(derr.ptr, 0, sizeof(unsigned long long));
-        const long long ncells = K.off[K.nt];
-        if (ncells > 0)
-            k_adj_check_tables<<<grid_of(ncells), 256>>>(dkfirst.ptr, dknm.ptr, dmi.ptr, ditem.ptr, dcontrib.ptr,
-                                                      dvals.ptr, doff.ptr, dcnt.ptr, dv.ptr, K.nt, derr.ptr);
-        unsigned long long eb = 0;
-        if (cudaMemcpy(&eb, derr.ptr, sizeof(eb), cudaMemcpyDeviceToHost) != cudaSuccess) return MCE_ERR_CUDA;
-        double e;
-        memcpy(&e, &eb, sizeof(e));
-        o->max_table_err = std::max(o->max_table_err, e);
-        // the next parents: the kept terms' records
-        std::vector<Rec<double>> next(K.nt);
-        for (int k = 0; k < K.nt; k++) next[k] = post[U.kept_term[k]];
-        parents.swap(next);
-        // the kept tables become the next update's parent tables
-        if ((st = pk.upload(K.keys.data(), K.keys.size()))) return st;
-        if ((st = pv.upload(K.vals.data(), K.vals.size()))) return st;
-        if ((st = poffb.upload(K.off.data(), K.off.size()))) return st;
-        if ((st = pcntb.upload(K.cells.data(), K.cells.size()))) return st;
-        prev = &U.kept;
+        o->ms[0] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if ((st = fwd_record(o, u, *o->ws, fz_raw))) return st;
     }
-    if (cudaGetLastError() != cudaSuccess) return MCE_ERR_CUDA;
     return MCE_OK;
 }
 
@@ -1531,211 +1929,171 @@ int mce_adjoint_timing(mce_adjoint* o, double* ms4)
 int mce_adjoint_num_params(mce_adjoint* o)
 {
     if (!o) return MCE_ERR_ARG;
-    return o->pncc + o->p + o->d + o->d * o->d + o->d * o->pncc + o->p * o->d;
+    return num_params(o);
 }
 
 int mce_adjoint_backward(mce_adjoint* o, const double* w, double* grad)
 {
     if (!o || !w || !grad || o->ups.empty()) return MCE_ERR_ARG;
-    const int nup = (int)o->ups.size();
     int st;
-    auto tb0 = std::chrono::steady_clock::now();
-    // ---- reverse over the tables and the fz seeds (GPU)
-    Buf<int> pk, kk, dcontrib;
-    Buf<cd> pv, kbar, pbar;
-    Buf<long long> poff, item;
-    Buf<int> pcnt;
-    Buf<MInfoDev> dmi;
-    Buf<double> qbar, dbar, cbar, ybar_e, dbar_e, cbar_e;
-    Buf<EvalDev> dev;
-    std::vector<cd> tbar;  // adjoint of the kept tables of update u (from update u+1)
-    for (int u = nup - 1; u >= 0; u--) {
-        Update& U = o->ups[u];
-        const Tables* P = u > 0 ? &o->ups[u - 1].kept : nullptr;
-        const long long npc = P ? P->off[P->nt] : 0;
-        if ((st = pbar.ensure(npc + 1))) return st;
-        if (cudaMemset(pbar.ptr, 0, sizeof(cd) * (npc + 1)) != cudaSuccess) return MCE_ERR_CUDA;
-        if (P) {
-            if ((st = pk.upload(P->keys.data(), P->keys.size()))) return st;
-            if ((st = pv.upload(P->vals.data(), P->vals.size()))) return st;
-            if ((st = poff.upload(P->off.data(), P->off.size()))) return st;
-            if ((st = pcnt.upload(P->cells.data(), P->cells.size()))) return st;
-        }
-        // the tables built at this update
-        const int nmem = (int)U.mi.size();
-        U.qbar.assign((size_t)nmem * 32, 0.0);
-        U.dbar_m.assign(nmem, 0.0);
-        U.cbar_m.assign(nmem, 0.0);
-        if (!U.last && nmem > 0) {
-            const Tables& K = U.kept;
-            const long long nitems = U.item_off[nmem];
-            std::vector<int> contrib(nmem);
-            for (int j = 0; j < nmem; j++) contrib[j] = U.members[j].contrib;
-            if ((st = dmi.upload(U.mi.data(), nmem))) return st;
-            if ((st = item.upload(U.item_off.data(), nmem + 1))) return st;
-            if ((st = dcontrib.upload(contrib.data(), nmem))) return st;
-            if ((st = kk.upload(K.keys.data(), K.keys.size()))) return st;
-            if (tbar.size() != K.vals.size()) tbar.assign(K.vals.size(), mce::mkcd(0, 0));
-            if ((st = kbar.upload(tbar.data(), tbar.size()))) return st;
-            if ((st = qbar.ensure((size_t)nmem * 32))) return st;
-            if ((st = dbar.ensure(nmem))) return st;
-            if ((st = cbar.ensure(nmem))) return st;
-            cudaMemset(qbar.ptr, 0, sizeof(double) * nmem * 32);
-            cudaMemset(dbar.ptr, 0, sizeof(double) * nmem);
-            cudaMemset(cbar.ptr, 0, sizeof(double) * nmem);
-            if (nitems > 0)
-                k_adj_member_reverse<<<grid_of(nitems), 256>>>(dmi.ptr, item.ptr, nmem, nitems, dcontrib.ptr, kk.ptr,
-                                                            kbar.ptr, pk.ptr, pv.ptr, poff.ptr, pcnt.ptr, U.gscale,
-                                                            pbar.ptr, qbar.ptr, dbar.ptr, cbar.ptr);
-            if (cudaMemcpy(U.qbar.data(), qbar.ptr, sizeof(double) * nmem * 32, cudaMemcpyDeviceToHost) ||
-                cudaMemcpy(U.dbar_m.data(), dbar.ptr, sizeof(double) * nmem, cudaMemcpyDeviceToHost) ||
-                cudaMemcpy(U.cbar_m.data(), cbar.ptr, sizeof(double) * nmem, cudaMemcpyDeviceToHost))
-                return MCE_ERR_CUDA;
-        }
-        // the fz seed of this update
-        const int nt = (int)U.terms.size();
-        U.ybar_e.assign(nt, 0.0);
-        U.dbar_e.assign(nt, 0.0);
-        U.cbar_e.assign(nt, 0.0);
-        if (w[u] != 0.0 && nt > 0) {
-            std::vector<EvalDev> ev(nt);
-            for (int t = 0; t < nt; t++) {
-                const TermInfo& ti = U.terms[t];
-                ev[t] = EvalDev{ti.parent < 0 ? 0 : ti.parent, ti.lp, ti.lm, ti.enc_lhp, ti.phc, U.first ? 1 : 0,
-                                ti.y_eval, ti.d_eval, ti.c_eval};
-            }
-            if ((st = dev.upload(ev.data(), nt))) return st;
-            if ((st = ybar_e.ensure(nt))) return st;
-            if ((st = dbar_e.ensure(nt))) return st;
-            if ((st = cbar_e.ensure(nt))) return st;
-            k_adj_eval_reverse<<<grid_of(nt), 256>>>(dev.ptr, nt, w[u], pk.ptr, pv.ptr, poff.ptr, pcnt.ptr, pbar.ptr,
-                                                      ybar_e.ptr, dbar_e.ptr, cbar_e.ptr);
-            if (cudaMemcpy(U.ybar_e.data(), ybar_e.ptr, sizeof(double) * nt, cudaMemcpyDeviceToHost) ||
-                cudaMemcpy(U.dbar_e.data(), dbar_e.ptr, sizeof(double) * nt, cudaMemcpyDeviceToHost) ||
-                cudaMemcpy(U.cbar_e.data(), cbar_e.ptr, sizeof(double) * nt, cudaMemcpyDeviceToHost))
-                return MCE_ERR_CUDA;
-        }
-        tbar.assign(npc, mce::mkcd(0, 0));
-        if (npc && cudaMemcpy(tbar.data(), pbar.ptr, sizeof(cd) * npc, cudaMemcpyDeviceToHost) != cudaSuccess)
-            return MCE_ERR_CUDA;
-    }
-    if (cudaGetLastError() != cudaSuccess) return MCE_ERR_CUDA;
-    // ---- the record chain: tangents of the scalars that enter the g values,
-    // one parameter direction at a time, dotted with their adjoints
-    auto tb1 = std::chrono::steady_clock::now();
-    o->ms[2] += std::chrono::duration<double, std::milli>(tb1 - tb0).count();
-    // ---- the record chain on the GPU: a thread per (parent, direction)
-    const int N = mce_adjoint_num_params(o);
-    const int d = o->d, MS = o->MS, rec = MS * d + MS + d;
-    long long maxP = 1;
-    for (int u = 0; u + 1 < nup; u++) maxP = std::max<long long>(maxP, o->ups[u].kept.nt);
-    Buf<double> tin, tout, dgrad, dPA, dPp, dPb, dyb, ddb, dcb, dqt, ddt, dct;
-    Buf<double> dpar[8];
-    Buf<int> dPm, dkid, dkept;
-    Buf<unsigned> dsn, dhp;
-    if ((st = tin.ensure((size_t)N * maxP * rec))) return st;
-    if ((st = tout.ensure((size_t)N * maxP * rec))) return st;
-    if ((st = dgrad.ensure(N))) return st;
-    cudaMemset(dgrad.ptr, 0, sizeof(double) * N);
-    const std::vector<double>* pv_[8] = {&o->beta, &o->gamma, &o->p0, &o->Phi, &o->Gamma, &o->H, &o->A0, &o->b0};
-    for (int i = 0; i < 8; i++)
-        if ((st = dpar[i].upload(pv_[i]->data(), pv_[i]->size()))) return st;
-    for (int u = 0; u < nup; u++) {
-        const Update& U = o->ups[u];
-        const int nt = (int)U.terms.size();
-        const int nP = u == 0 ? 1 : o->ups[u - 1].kept.nt;
-        if (u > 0) {
-            const Tables& K = o->ups[u - 1].kept;
-            if ((st = dPm.upload(K.shape.data(), K.shape.size()))) return st;
-            if ((st = dPA.upload(K.A.data(), K.A.size()))) return st;
-            if ((st = dPp.upload(K.p.data(), K.p.size()))) return st;
-            if ((st = dPb.upload(K.b.data(), K.b.size()))) return st;
-        }
-        std::vector<int> kid_off(nP, 0), nk(nP, 0);
-        for (int t = nP; t < nt; t++) nk[U.terms[t].parent < 0 ? 0 : U.terms[t].parent]++;
-        for (int i = 0, acc = nP; i < nP; i++) {
-            kid_off[i] = acc;
-            acc += nk[i];
-        }
-        std::vector<unsigned> sn(nt), hp(nt);
-        for (int t = 0; t < nt; t++) {
-            sn[t] = U.terms[t].sneg;
-            hp[t] = U.terms[t].horthog_pre;
-        }
-        std::vector<double> qt((size_t)nt * 32, 0.0), dt(nt, 0.0), ct(nt, 0.0);
-        for (size_t j = 0; j < U.members.size(); j++) {
-            const Member& mb = U.members[j];
-            if (!mb.contrib || U.qbar.empty()) continue;
-            for (int k = 0; k < 32; k++) qt[(size_t)mb.term * 32 + k] = U.qbar[j * 32 + k];
-            dt[mb.term] = U.dbar_m[j];
-            ct[mb.term] = U.cbar_m[j];
-        }
-        std::vector<int> kept_of(nt, -1);
-        const int n_next = U.last ? 0 : (int)U.kept_term.size();
-        for (int k = 0; k < n_next; k++) kept_of[U.kept_term[k]] = k;
-        if ((st = dkid.upload(kid_off.data(), nP))) return st;
-        if ((st = dsn.upload(sn.data(), nt))) return st;
-        if ((st = dhp.upload(hp.data(), nt))) return st;
-        if ((st = dyb.upload(U.ybar_e.data(), nt))) return st;
-        if ((st = ddb.upload(U.dbar_e.data(), nt))) return st;
-        if ((st = dcb.upload(U.cbar_e.data(), nt))) return st;
-        if ((st = dqt.upload(qt.data(), qt.size()))) return st;
-        if ((st = ddt.upload(dt.data(), nt))) return st;
-        if ((st = dct.upload(ct.data(), nt))) return st;
-        if ((st = dkept.upload(kept_of.data(), nt))) return st;
-        ChainArgs ca;
-        ca.d = d;
-        ca.pncc = o->pncc;
-        ca.p = o->p;
-        ca.MS = MS;
-        ca.N = N;
-        ca.first = U.first;
-        ca.last = U.last;
-        ca.with_tp = U.with_tp;
-        ca.sub = U.sub;
-        ca.nP = nP;
-        ca.z = o->msmts[u];
-        ca.beta = dpar[0].ptr;
-        ca.gamma = dpar[1].ptr;
-        ca.p0 = dpar[2].ptr;
-        ca.Phi = dpar[3].ptr;
-        ca.Gamma = dpar[4].ptr;
-        ca.H = dpar[5].ptr;
-        ca.A0 = dpar[6].ptr;
-        ca.b0 = dpar[7].ptr;
-        ca.PA = dPA.ptr;
-        ca.Pp = dPp.ptr;
-        ca.Pb = dPb.ptr;
-        ca.Pm = dPm.ptr;
-        ca.Tin = tin.ptr;
-        ca.Tout = tout.ptr;
-        ca.rec = rec;
-        ca.n_next = n_next;
-        ca.kid_off = dkid.ptr;
-        ca.sneg = dsn.ptr;
-        ca.hpre = dhp.ptr;
-        ca.ybar_e = dyb.ptr;
-        ca.dbar_e = ddb.ptr;
-        ca.cbar_e = dcb.ptr;
-        ca.qbar_t = dqt.ptr;
-        ca.dbar_t = ddt.ptr;
-        ca.cbar_t = dct.ptr;
-        ca.kept_of = dkept.ptr;
-        ca.grad = dgrad.ptr;
-        const long long nthr = (long long)nP * N;
-        k_adj_chain<<<(int)((nthr + 127) / 128), 128>>>(ca);
-        std::swap(tin.ptr, tout.ptr);
-        std::swap(tin.cap, tout.cap);
-    }
-    if (cudaMemcpy(grad, dgrad.ptr, sizeof(double) * N, cudaMemcpyDeviceToHost) != cudaSuccess) {
-        cudaGetLastError();
-        mce::report_error("adjoint: the record chain failed on the GPU");
-        return MCE_ERR_CUDA;
-    }
-    o->ms[3] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb1).count();
-    return MCE_OK;
+    if (!o->ws) o->ws.reset(new Workspace());
+    if ((st = o->ws->init())) return st;
+    return bwd_run(o, w, grad, *o->ws);
 }
 
 void mce_adjoint_destroy(mce_adjoint* o) { delete o; }
+
+mce_adjoint_batch* mce_adjoint_batch_create(int n_runs, int d, int pncc, int p, const int* steps, const double* A0,
+                                            const double* p0, const double* b0, const double* root_point,
+                                            const double* b_pert, int bpert_stride, int* status)
+{
+    auto fail = [status](int st, const std::string& msg) -> mce_adjoint_batch* {
+        mce::report_error(msg);
+        if (status) *status = st;
+        return nullptr;
+    };
+    if (n_runs < 1 || d < 2 || d > 8 || pncc < 1 || p < 1 || !steps || !A0 || !p0 || !b0 || !root_point ||
+        !b_pert || bpert_stride < 1)
+        return fail(MCE_ERR_ARG, "mce_adjoint_batch_create: invalid arguments");
+    std::unique_ptr<mce_adjoint_batch> b(new mce_adjoint_batch());
+    b->n = n_runs;
+    b->d = d;
+    b->pncc = pncc;
+    b->p = p;
+    for (int r = 0; r < n_runs; r++) {
+        if (steps[r] < 1) return fail(MCE_ERR_ARG, "mce_adjoint_batch_create: a run of no steps");
+        const int MS = (steps[r] - 1) * pncc + d;
+        if (MS > 31) return fail(MCE_ERR_SHAPE, "mce_adjoint_batch_create: more than 31 hyperplanes per term");
+        if (MS > bpert_stride) return fail(MCE_ERR_ARG, "mce_adjoint_batch_create: bpert_stride below a run's shape");
+    }
+    int st = MCE_OK;
+    b->h = mce_batch_create(n_runs, d, 0, pncc, p, steps, A0, p0, b0, root_point, b_pert, bpert_stride, &st);
+    if (!b->h) {
+        if (status) *status = st;
+        return nullptr;
+    }
+    cudaGetDevice(&b->dev);
+    for (int r = 0; r < n_runs; r++) {
+        std::unique_ptr<mce_adjoint> o(new mce_adjoint());
+        o->d = d;
+        o->pncc = pncc;
+        o->p = p;
+        o->steps = steps[r];
+        o->MS = (steps[r] - 1) * pncc + d;
+        o->A0.assign(A0 + (size_t)r * d * d, A0 + (size_t)(r + 1) * d * d);
+        o->p0.assign(p0 + (size_t)r * d, p0 + (size_t)(r + 1) * d);
+        o->b0.assign(b0 + (size_t)r * d, b0 + (size_t)(r + 1) * d);
+        o->root.assign(root_point + (size_t)r * d, root_point + (size_t)(r + 1) * d);
+        o->bpert.assign(b_pert + (size_t)r * bpert_stride, b_pert + (size_t)r * bpert_stride + o->MS);
+        o->h = b->h;
+        o->est = r;
+        o->owns_h = false;
+        b->runs.push_back(std::move(o));
+    }
+    b->threads = host_threads(n_runs);
+    for (int w = 0; w < b->threads; w++) {
+        b->ws.emplace_back(new Workspace());
+        if ((st = b->ws.back()->init())) {
+            if (status) *status = st;
+            return nullptr;
+        }
+    }
+    if (status) *status = MCE_OK;
+    return b.release();
+}
+
+int mce_adjoint_batch_forward(mce_adjoint_batch* b, const double* msmts, int max_steps, const double* Phi,
+                              const double* Gamma, const double* beta, const double* H, const double* gamma,
+                              double* fz_raw)
+{
+    if (!b || !msmts || !Phi || !Gamma || !beta || !H || !gamma || max_steps < 1) return MCE_ERR_ARG;
+    const int n = b->n, d = b->d, p = b->p, stride = max_steps * p;
+    int st, max_up = 0;
+    for (int r = 0; r < n; r++) {
+        mce_adjoint* o = b->runs[r].get();
+        if (o->steps > max_steps) return MCE_ERR_ARG;
+        if ((st = fwd_begin(o, msmts + (size_t)r * stride, Phi, Gamma, beta, H, gamma))) return st;
+        max_up = std::max(max_up, (int)o->ups.size());
+    }
+    for (auto& w : b->ws) w->owner = nullptr;
+    if (fz_raw) std::fill(fz_raw, fz_raw + (size_t)n * stride, 0.0);
+    if ((st = mce_reset(b->h)) < 0) return st;
+    std::vector<double> z(n), Hr((size_t)n * d), gam(n);
+    std::vector<int> act;
+    for (int u = 0; u < max_up; u++) {
+        const int sub = u % p;
+        act.clear();
+        for (int r = 0; r < n; r++) {
+            const bool on = u < (int)b->runs[r]->ups.size();
+            z[r] = on ? msmts[(size_t)r * stride + u] : 0.0;
+            for (int j = 0; j < d; j++) Hr[(size_t)r * d + j] = H[(size_t)sub * d + j];
+            gam[r] = gamma[sub];
+            if (on) act.push_back(r);
+        }
+        auto t0 = std::chrono::steady_clock::now();
+        st = mce_batch_step(b->h, z.data(), Phi, Gamma, beta, Hr.data(), gam.data(), nullptr, nullptr, 1, nullptr);
+        if (st < 0) return st;
+        auto t1 = std::chrono::steady_clock::now();
+        st = parallel_runs((int)act.size(), b->threads, b->dev, [&](int i, int w) {
+            const int r = act[i];
+            return fwd_record(b->runs[r].get(), u, *b->ws[w], fz_raw ? fz_raw + (size_t)r * stride : nullptr);
+        });
+        if (st < 0) return st;
+        auto t2 = std::chrono::steady_clock::now();
+        b->ms[0] += std::chrono::duration<double, std::milli>(t1 - t0).count();
+        b->ms[1] += std::chrono::duration<double, std::milli>(t2 - t1).count();
+    }
+    return MCE_OK;
+}
+
+int mce_adjoint_batch_backward(mce_adjoint_batch* b, const double* w, int max_steps, double* grad)
+{
+    if (!b || !w || !grad || max_steps < 1) return MCE_ERR_ARG;
+    const int n = b->n, stride = max_steps * b->p;
+    const int N = num_params(b->runs[0].get());
+    for (int r = 0; r < n; r++)
+        if (b->runs[r]->ups.empty() || b->runs[r]->steps > max_steps) return MCE_ERR_ARG;
+    std::fill(grad, grad + (size_t)n * N, 0.0);
+    auto t0 = std::chrono::steady_clock::now();
+    const int st = parallel_runs(n, b->threads, b->dev, [&](int r, int wk) {
+        mce_adjoint* o = b->runs[r].get();
+        const double* wr = w + (size_t)r * stride;
+        bool any = false;
+        for (size_t u = 0; u < o->ups.size(); u++) any |= wr[u] != 0.0;
+        return any ? bwd_run(o, wr, grad + (size_t)r * N, *b->ws[wk]) : MCE_OK;
+    });
+    b->ms[2] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return st;
+}
+
+int mce_adjoint_batch_num_params(mce_adjoint_batch* b)
+{
+    if (!b) return MCE_ERR_ARG;
+    return num_params(b->runs[0].get());
+}
+
+int mce_adjoint_batch_check(mce_adjoint_batch* b, double* max_table_rel_err, double* max_fz_rel_err)
+{
+    if (!b) return MCE_ERR_ARG;
+    double a = 0, c = 0;
+    for (auto& o : b->runs) {
+        a = std::max(a, o->max_table_err);
+        c = std::max(c, o->fz_check_err);
+    }
+    if (max_table_rel_err) *max_table_rel_err = a;
+    if (max_fz_rel_err) *max_fz_rel_err = c;
+    return MCE_OK;
+}
+
+int mce_adjoint_batch_timing(mce_adjoint_batch* b, double* ms4)
+{
+    if (!b || !ms4) return MCE_ERR_ARG;
+    for (int i = 0; i < 3; i++) ms4[i] = b->ms[i];
+    ms4[3] = 0;
+    for (auto& o : b->runs) ms4[3] += o->ms[3];
+    return MCE_OK;
+}
+
+void mce_adjoint_batch_destroy(mce_adjoint_batch* b) { delete b; }
 
 }  // extern "C"

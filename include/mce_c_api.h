@@ -368,9 +368,36 @@ int mce_adjoint_backward(mce_adjoint* a, const double* w, double* grad);
 int mce_adjoint_check(mce_adjoint* a, double* max_table_rel_err, double* max_fz_rel_err);
 /* Wall ms spent since creation: [0] the forward step path, [1] the forward
  * tape (host records, GPU member values and checks), [2] the reverse over the
- * tables (GPU), [3] the record chain (host). */
+ * tables (GPU), [3] the record chain (GPU). */
 int mce_adjoint_timing(mce_adjoint* a, double* ms4);
 void mce_adjoint_destroy(mce_adjoint* a);
+
+/* A batch of adjoint runs of one LTI model (the window lives of a sliding-
+ * window log-likelihood, say), stepped together by one batched handle
+ * (mce_batch_step per update) with their records and reverses spread over
+ * the host's cores, each core's GPU work on its own stream.  Run r has
+ * steps[r] steps from (A0[r], p0[r], b0[r]) with its own rand() constants
+ * root_point[r*d...] and b_pert[r*bpert_stride...]; every run gives the same
+ * gradient as an mce_adjoint of its own (the step path is the same doubles).
+ *   forward: msmts[n_runs*max_steps*p] (run r's updates from
+ *           r*max_steps*p); the model arrays as for mce_adjoint_forward;
+ *           fz_raw[n_runs*max_steps*p] (or NULL), 0 past a run's last update.
+ *   backward: w[n_runs*max_steps*p] seeds (a run whose seeds are all 0 is
+ *           skipped and gets a zero gradient); grad[n_runs*num_params].
+ *   timing: wall ms of the batched step path, of the forward records, of the
+ *           reverse, and the runs' summed record-chain ms. */
+typedef struct mce_adjoint_batch mce_adjoint_batch;
+mce_adjoint_batch* mce_adjoint_batch_create(int n_runs, int d, int pncc, int p, const int* steps, const double* A0,
+                                            const double* p0, const double* b0, const double* root_point,
+                                            const double* b_pert, int bpert_stride, int* status);
+int mce_adjoint_batch_forward(mce_adjoint_batch* b, const double* msmts, int max_steps, const double* Phi,
+                              const double* Gamma, const double* beta, const double* H, const double* gamma,
+                              double* fz_raw);
+int mce_adjoint_batch_backward(mce_adjoint_batch* b, const double* w, int max_steps, double* grad);
+int mce_adjoint_batch_num_params(mce_adjoint_batch* b);
+int mce_adjoint_batch_check(mce_adjoint_batch* b, double* max_table_rel_err, double* max_fz_rel_err);
+int mce_adjoint_batch_timing(mce_adjoint_batch* b, double* ms4);
+void mce_adjoint_batch_destroy(mce_adjoint_batch* b);
 
 /* Host wall time (ms) of the steps since the last mce_clear_profile: which = 0
  * whole steps, 1 input packing, 2 the moment checks after the device work. */

@@ -161,3 +161,47 @@ def test_windowed_gradient_with_fixed_checkpoints():
         fd = (vals[0] - vals[1]) / (2 * h)
         g = res["grad"][name][idx]
         assert abs(g - fd) <= 1e-4 * abs(fd) + 1e-7, (name, idx, g, fd)
+
+
+def test_batch_runs_match_their_own_runs():
+    """AdjointBatch (one batched handle for every run, the records and
+    reverses on several host threads) against an AdjointRun per run: the
+    window lives of a 4-state window-4 problem (runs of 1 to 4 steps, each
+    from its own start statistics and constants).  Re fz is the same doubles
+    (the batched step path is the single one); the gradients agree within
+    1e-12 (the reverse's atomic sums may add in another order)."""
+    _need_gpu()
+    import oracle
+    from cauchyfriendly_gb300 import workloads as W
+    from cauchyfriendly_gb300.adjoint import AdjointBatch, AdjointRun, loglik_weights, windowed_log_likelihood
+    prob = W.four_state_lti(seed=4, steps=10)
+    Wn = 4
+    ms = oracle.max_shape_of({"steps": Wn, "d": 4, "pncc": 1})
+    cs = [oracle.draw_reference_constants(60 + w, 4, ms) for w in range(Wn)]
+    rp = np.stack([c[0] for c in cs])
+    bp = np.stack([c[1] for c in cs])
+    starts = windowed_log_likelihood(prob, Wn, rp, bp, with_grad=False)["starts"]
+    lens = [min(Wn, 10 - st["step"]) for st in starts]
+    msm = [prob["msmts"][st["step"]:st["step"] + n].reshape(-1) for st, n in zip(starts, lens)]
+    P = _params(prob)
+    model = (P["Phi"], P["Gamma"], P["beta"], P["H"], P["gamma"])
+    batch = AdjointBatch(4, 1, 1, lens, [st["A0"] for st in starts], [st["p0"] for st in starts],
+                         [st["b0"] for st in starts], [rp[st["slot"]] for st in starts],
+                         [bp[st["slot"]] for st in starts])
+    fzb = batch.forward(msm, *model)
+    te, fe = batch.check()
+    assert te <= 1e-12 and fe <= 1e-12, (te, fe)
+    ws = [loglik_weights(f) for f in fzb]
+    ws[1] = np.zeros_like(ws[1])  # a run without seeds gets a zero gradient
+    gb = batch.backward(ws)
+    for r, st in enumerate(starts):
+        run = AdjointRun(4, 1, 1, lens[r], st["A0"], st["p0"], st["b0"], rp[st["slot"]], bp[st["slot"]])
+        fz = run.forward(msm[r], *model)
+        assert np.array_equal(fz, fzb[r]), (r, fz, fzb[r])
+        if r == 1:
+            assert np.all(_flat(gb[r]) == 0.0)
+        else:
+            g = _flat(run.backward(ws[r]))
+            assert np.allclose(_flat(gb[r]), g, rtol=1e-12, atol=1e-12 * np.max(np.abs(g))), r
+        run.close()
+    batch.close()
