@@ -12,7 +12,9 @@
 // scales held constant: the log-likelihood of a run is one seed, 1/Re fz_K, on
 // the last update's fz, and any sum of log fz over a range of updates is two.
 //
-// Layout of the computation (one estimator per object):
+// Layout of the computation (one run per mce_adjoint; an mce_adjoint_batch
+// steps its runs with one batched handle and records and reverses them on
+// several host threads, each thread with its own stream and buffers):
 //  * forward: the library's GPU step path runs the updates; after each one
 //    the object copies the kept terms and their g-tables (mce_dump_terms) and
 //    the update's G_SCALE_FACTOR.  On the host it re-derives, per update, the
