@@ -55,14 +55,20 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the one-estimator-per-handle comparison")
     ap.add_argument("--plain-stride", type=int, default=16)
     ap.add_argument("--adjoint-steps", type=int, default=100)
-    ap.add_argument("--workload", default="batched3", choices=["batched3", "windows5", "rel2d", "adjoint", "cpdfnd"],
+    ap.add_argument("--workload", default="batched3",
+                    choices=["batched3", "windows5", "rel2d", "adjoint", "cpdfnd", "window7"],
                     help="batched3: the batched 3-state configuration (default); windows5: the sliding-window "
                          "5-state LTV configuration for --window-steps steps; rel2d: the relative 2-D system of "
                          "two 5-state estimators; cpdfnd: the N-D conditional pdf of a 4-state estimator at "
-                         "--nd-points points")
+                         "--nd-points points; window7: one window of the 7-state LTV model (window 8, two "
+                         "measurements per step) as far as its g-tables stay below --max-cells cells")
     ap.add_argument("--nd-points", type=int, default=256)
     ap.add_argument("--window-steps", type=int, default=12)
     ap.add_argument("--rel-updates", type=int, default=6, help="rel2d: updates of both estimators (6: 12.2 M pairs)")
+    ap.add_argument("--max-cells", type=float, default=4e8,
+                    help="window7: stop before an update whose g-table cells, projected by the largest growth "
+                         "seen so far, would pass this")
+    ap.add_argument("--cpu-updates", type=int, default=6, help="window7: updates the CPU baseline runs")
     return ap.parse_args()
 
 
@@ -700,6 +706,114 @@ def _rel2d_cpu_share(job):
     return r["pairs"], t1
 
 
+def run_window7(args):
+    """One window of the 7-state LTV model of the batched 7-state
+    sliding-window configuration (workloads.seven_state_ltv_windows: Gamma
+    7x2, H 2x7, two measurements per step; a window of 8 steps is 16
+    updates, up to (8-1)*2+7 = 21 hyperplanes per term), one estimator from
+    the initial statistics, update by update while the g-tables fit: the run
+    stops before an update whose cells, projected with the largest growth
+    factor seen so far, would pass --max-cells.  Reports per update the
+    terms, g-table cells and device ms, and the memory the next updates would
+    need.  value: post-MU terms / device time over the updates run;
+    cpu_baseline: the reference's C++ (serial build; the oracle port where it
+    is not built) over the first --cpu-updates updates, with the GPU's terms/s
+    on the same updates beside it."""
+    import ctypes
+    import torch
+    import oracle
+    from cauchyfriendly_gb300 import CauchyEstimator, _lib
+    from cauchyfriendly_gb300 import workloads as W
+    torch.cuda.set_device(0)
+    lib = _lib.load()
+    Wn = 8
+    prob = W.seven_state_ltv_windows(seed=args.seed, steps=Wn)
+    ms = oracle.max_shape_of(prob)
+    have_ref = os.path.exists(os.path.join(oracle.REF_OUT, "libmce_ref_serial.so"))
+    if have_ref:
+        ref = oracle.Reference(prob, seed=500)
+        rp, bp = ref.constants()
+        ref.close()
+    else:
+        rp, bp = oracle.draw_reference_constants(500, prob["d"], ms)
+
+    def gpu_run():
+        est = CauchyEstimator(prob["A0"], prob["p0"], prob["b0"], Wn, 7, 0, 2, 2, root_point=rp, b_pert=bp)
+        rows, prev_cells, growth = [], None, 1.0
+        stop = None
+        for k in range(Wn):
+            for j in range(2):
+                if prev_cells is not None and prev_cells * growth > args.max_cells:
+                    stop = "next update projected at %.3g cells (growth %.1fx) > --max-cells %.3g" % (
+                        prev_cells * growth, growth, args.max_cells)
+                    break
+                pm0 = est.post_mu_terms()
+                est.step(prob["msmts"][k, j], prob["Phi"][k], prob["Gamma"], prob["beta"], prob["H"][j],
+                         prob["gamma"][j])
+                cells = int(lib.mce_total_cells(est._h, 0))
+                rows.append({"update": 2 * k + j, "terms": int(est.num_terms()),
+                             "post_mu_terms": int(est.post_mu_terms() - pm0), "cells": cells,
+                             "device_ms": round(float(est.last_step_ms()), 3), "errors": int(est.errors())})
+                if prev_cells:
+                    growth = max(growth, cells / prev_cells)
+                prev_cells = cells
+            if stop:
+                break
+        est.close()
+        return rows, stop, growth
+
+    for _ in range(max(0, args.warmup - 2)):
+        gpu_run()
+    rows, stop, growth = gpu_run()
+    terms = sum(r["post_mu_terms"] for r in rows)
+    dev_s = sum(r["device_ms"] for r in rows) / 1e3
+    # the memory the rest of the window would take (16 bytes per g-table cell;
+    # the terms' records are small beside it), each update grown by the last
+    # growth factor of its kind: a step's first update (time propagation adds
+    # the Gamma hyperplanes) or its second (measurement update only)
+    kind_growth = {}
+    for r0, r1 in zip(rows, rows[1:]):
+        if r0["cells"] > 0:
+            kind_growth[r1["update"] % 2] = r1["cells"] / r0["cells"]
+    proj, c = [], rows[-1]["cells"]
+    for u in range(len(rows), 2 * Wn):
+        c *= kind_growth.get(u % 2, growth)
+        proj.append({"update": u, "cells": float("%.3g" % c), "table_gb": float("%.3g" % (16 * c / 1e9))})
+    line = {"metric": METRIC, "value": terms / dev_s, "unit": UNIT, "n_gpus": 1, "steps": 1,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dev_s, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "one window of the 7-state LTV model (window 8, 2 msmts/step, up to 21 "
+                                   "hyperplanes per term), updates 0..%d" % (len(rows) - 1),
+                       "max_cells": args.max_cells},
+            "updates": rows, "stopped": stop,
+            "growth_per_update_kind": {"first_of_step": kind_growth.get(0), "second_of_step": kind_growth.get(1)},
+            "projected_rest_of_window": proj}
+    if not args.no_cpu_baseline:
+        nu = min(args.cpu_updates, len(rows))
+        if have_ref:
+            cpu = oracle.Reference(prob, seed=500)
+            kind = "reference"
+        else:
+            cpu = oracle.Oracle(prob, rp, bp)
+            kind = "port"
+        t0 = time.perf_counter()
+        n = 0
+        for k in range(Wn):
+            for j in range(2):
+                if n < nu:
+                    cpu.step(k, j)
+                    n += 1
+        t_cpu = time.perf_counter() - t0
+        cpu.close()
+        sub_terms = sum(r["post_mu_terms"] for r in rows[:nu])
+        sub_dev = sum(r["device_ms"] for r in rows[:nu]) / 1e3
+        line["cpu_baseline"] = {"value": sub_terms / t_cpu, "unit": UNIT, "cores": 1, "kind": kind,
+                                "sample": "updates 0..%d of the window, serial (%d post-MU terms, %.1f s)"
+                                          % (nu - 1, sub_terms, t_cpu),
+                                "gpu_same_updates": sub_terms / sub_dev}
+    print(json.dumps(line), flush=True)
+
+
 def autotune_summary(table, passes, off):
     """The autotuner's settled block sizes per kernel as {log2 items: block}."""
     if off:
@@ -726,6 +840,9 @@ def main():
         return
     if args.workload == "cpdfnd":
         run_cpdfnd(args)
+        return
+    if args.workload == "window7":
+        run_window7(args)
         return
     import torch
     rank = int(os.environ.get("RANK", "0"))

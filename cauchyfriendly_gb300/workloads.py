@@ -165,9 +165,20 @@ def five_state_ltv_windows(seed=0, steps=200, dt=0.1, outlier_frac=0.02, outlier
     0.05 in each entry, Gamma 5x2 = 0.1 N(0,1), H 2x5 = N(0,1), beta = gamma =
     [0.05, 0.05] / [0.1, 0.1], p0 = 0.1, two measurements per step, 2% of the
     noise samples replaced by outliers at 50x.  Phi has shape (steps, 5, 5)."""
+    return ltv_windows(5, seed, steps, dt, outlier_frac, outlier_scale)
+
+
+def seven_state_ltv_windows(seed=0, steps=150, dt=0.1, outlier_frac=0.02, outlier_scale=50.0):
+    """The 7-state version of five_state_ltv_windows (Gamma 7x2, H 2x7), the
+    model of the batched 7-state sliding-window estimators (window 8)."""
+    return ltv_windows(7, seed, steps, dt, outlier_frac, outlier_scale)
+
+
+def ltv_windows(d, seed=0, steps=200, dt=0.1, outlier_frac=0.02, outlier_scale=50.0):
+    """d-state LTV problem with two process-noise columns and two
+    measurements per step, seeded as five_state_ltv_windows describes."""
     from scipy.linalg import expm
     rng = np.random.Generator(np.random.PCG64(seed))
-    d = 5
     A = rng.normal(0.0, 0.3, (d, d))
     ph = rng.uniform(0, 2 * np.pi, (d, d))
     Phis = np.stack([expm(dt * (A + 0.05 * np.sin(0.05 * k + ph))) for k in range(steps)])

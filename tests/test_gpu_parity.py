@@ -341,3 +341,33 @@ def test_persistent_term_reduction_keeps_results_bit_identical():
                        cwd=root, env=env, capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]
     assert " passed" in r.stdout
+
+
+def test_seven_state_ltv_window_against_oracle():
+    """The 7-state LTV model of the batched 7-state sliding-window
+    configuration (two measurements per step): a window-8 estimator (room for
+    (8-1)*2+7 = 21 hyperplanes per term, above the shared-memory bitmap
+    limit) through its first 6 updates (3 steps, about 10,800 terms) against
+    the oracle on the same host: integer structure exact, moments within
+    1e-9.  (The sixth update holds a g value within an ulp of the term
+    approximation's threshold, where the host's hypot decides: 10,810 terms
+    with x86-64 glibc, 10,811 with aarch64 glibc.)"""
+    from cauchyfriendly_gb300 import workloads as W
+    prob = W.seven_state_ltv_windows(seed=0, steps=8)
+    rp, bp = oracle.draw_reference_constants(500, 7, oracle.max_shape_of(prob))
+    gpu = _GpuAdapter(prob, rp, bp)
+    orc = oracle.Oracle(prob, rp, bp)
+    got, want = [], []
+    for k in range(3):
+        for s in range(2):
+            for est, out in ((gpu, got), (orc, want)):
+                err = est.step(k, s)
+                rec = est.moments()
+                rec["err"] = int(err)
+                rec["Nt"] = est.num_terms()
+                rec["tps"] = est.terms_per_shape()
+                out.append(rec)
+    gpu.close()
+    orc.close()
+    assert [r["Nt"] for r in want][:5] == [8, 36, 192, 678, 3308]
+    G.compare_records(got, want, check_terms=False)
