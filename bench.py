@@ -380,6 +380,35 @@ def run_windows5(args):
 
 
 
+def _adjoint_ref_forward(job):
+    """One forward run of the adjoint workload's sliding-window problem
+    through the reference's own PySlidingWindowManager
+    (scripts/swig/cauchy/cauchy_estimator.py, the unmodified copy in
+    oracle/_ref) over its C++ (oracle/_ref, serial build); seconds, or None
+    where the copy is absent."""
+    seed, steps, Wn = job
+    # the reference's manager prints as it shuts windows down: keep it off
+    # this process's stdout, which the bench's one JSON line shares
+    devnull = os.open(os.devnull, os.O_WRONLY)
+    os.dup2(devnull, 1)
+    sys.stdout = open(os.devnull, "w")
+    import oracle
+    from oracle import ref_pycauchy
+    from cauchyfriendly_gb300 import workloads as W
+    ce = oracle.reference_python_api(ref_pycauchy)
+    if ce is None:
+        return None
+    prob = W.four_state_lti(seed=seed, steps=steps)
+    t0 = time.perf_counter()
+    mgr = ce.PySlidingWindowManager("lti", Wn, swm_debug_print=False, win_debug_print=False)
+    mgr.initialize_lti(prob["A0"], prob["p0"], prob["b0"], prob["Phi"], None, prob["Gamma"], prob["beta"],
+                       prob["H"], prob["gamma"])
+    for k in range(steps):
+        mgr.step(prob["msmts"][k], None)
+    mgr.shutdown()
+    return time.perf_counter() - t0
+
+
 def run_adjoint(args):
     """Adjoint workload (the 4-state LTI sliding-window configuration: Phi
     random with spectral radius 0.95, Gamma 4x1 and H 1x4 N(0,1), beta 0.1,
@@ -441,6 +470,23 @@ def run_adjoint(args):
                                   zip(("step_path", "forward_tape", "table_reverse", "record_chain"),
                                       r["timing_ms"])},
             "loglik": r["loglik"], "grad_norm": float(np.sqrt(sum(float(np.sum(v ** 2)) for v in r["grad"].values())))}
+    if not args.no_cpu_baseline:
+        # The reference has no derivatives: its gradient is central
+        # differences of its own forward run, 2 x 30 runs.  One run per host
+        # core, all at once; the gradient's time is 60 runs at that rate.
+        import multiprocessing as mp
+        cores = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        with mp.get_context("spawn").Pool(cores) as pool:
+            ts = pool.map(_adjoint_ref_forward, [(args.seed, steps, Wn)] * cores)
+        wall = time.perf_counter() - t0
+        if all(t is not None for t in ts):
+            runs_per_s = cores / wall
+            line["cpu_baseline"] = {"value": runs_per_s / 60.0, "unit": "gradients/s", "cores": cores,
+                                    "kind": "reference",
+                                    "sample": "the reference's PySlidingWindowManager forward run (serial C++), one "
+                                              "per core at once (%.1f s wall, %.1f s per run); a gradient = 2 x 30 "
+                                              "runs (central differences)" % (wall, max(ts))}
     print(json.dumps(line), flush=True)
 
 
