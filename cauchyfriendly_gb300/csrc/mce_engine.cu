@@ -415,14 +415,25 @@ public:
     std::vector<int> h_order;       // moment-chain launch order
     DevBuf<int> ftr_cnt;            // worklist lengths of the resolution rounds
     static constexpr int kFtrFirstBatch = 4, kFtrBatch = 2, kFtrCntSlots = 8, kFtrMaxRounds = 100000;
-    static bool ftr_persistent()
+    // How the resolution rounds after the first run: 0 queued in batches, the
+    // host reading the worklist length once per batch; 1 one persistent
+    // cooperative launch; 2 a device-side loop in a CUDA graph.  Chosen with
+    // MCE_FTR_ROUNDS=batched|persistent|graph (MCE_FTR_PERSISTENT=1 is
+    // persistent).
+    static int ftr_rounds_mode()
     {
-        static const bool on = [] {
-            const char* v = getenv("MCE_FTR_PERSISTENT");
-            return v && v[0] == '1';
+        static const int mode = [] {
+            const char* p = getenv("MCE_FTR_PERSISTENT");
+            if (p && p[0] == '1') return 1;
+            const char* v = getenv("MCE_FTR_ROUNDS");
+            if (v && !strcmp(v, "batched")) return 0;
+            if (v && !strcmp(v, "persistent")) return 1;
+            if (v && !strcmp(v, "graph")) return 2;
+            return 0;
         }();
-        return on;
+        return mode;
     }
+    void* ftr_graph = nullptr;  // the rounds' CUDA graph (mode 2), built on first use
     DevBuf<int> d_order;
     // combos per shape (lexicographic d-subsets)
     DevBuf<int> dcombo_off;
@@ -742,6 +753,7 @@ public:
     ~Engine() override
     {
         if (lc.stream) cudaStreamSynchronize(lc.stream);
+        if (ftr_graph) Kernels<D>::ftr_graph_destroy(ftr_graph);
         if (ndw) nd_work_destroy(ndw);
         if (mstream) cudaStreamSynchronize(mstream);
         if (ev0) cudaEventDestroy(ev0);
@@ -896,6 +908,7 @@ public:
     {
         MCE_CUDA(cudaGetLastError());
         MCE_CUDA(cudaStreamSynchronize(lc.stream));
+        if (ftr_graph) Kernels<D>::ftr_graph_collect(ftr_graph);
         int err = 0;
         MCE_CUDA(cudaMemcpy(&err, counters.ptr, sizeof(int), cudaMemcpyDeviceToHost));
         if (err) {
@@ -1324,20 +1337,35 @@ public:
         // the count once per batch
         if ((s = ftr_cnt.ensure(kFtrCntSlots))) return s;
         // the first round over every record as an ordinary (full-occupancy)
-        // launch; the rounds after it either queued in batches, the host
-        // reading the worklist length once per batch (the default, the faster
-        // here), or, with MCE_FTR_PERSISTENT=1, in one persistent cooperative
-        // launch over the device worklists with no host round trip
+        // launch; the rounds after it as ftr_rounds_mode() says: queued in
+        // batches, the host reading the worklist length once per batch; in one
+        // persistent cooperative launch over the device worklists; or as a
+        // device-side loop in a CUDA graph (neither of the last two has a host
+        // round trip).  The no-allocation step runs the batched rounds.
         MCE_CUDA(cudaMemsetAsync(ftr_cnt.ptr, 0, sizeof(int) * kFtrCntSlots, lc.stream));
         pbeg(KID_FTR);
         Kernels<D>::ftr_resolve(R, nR, cell_ent2.ptr, boff.ptr, H - 1, MC, status.ptr, owner.ptr, nullptr, nullptr,
                                 nR, ftr_wl[0].ptr, ftr_cnt.ptr, ftr_resume.ptr, lc);
-        const int pst = ftr_persistent()
-                            ? Kernels<D>::ftr_resolve_all(R, nR, cell_ent2.ptr, boff.ptr, H - 1, MC, status.ptr,
-                                                          owner.ptr, ftr_wl[0].ptr, ftr_wl[1].ptr, ftr_cnt.ptr,
-                                                          ftr_resume.ptr, reinterpret_cast<unsigned*>(ftr_cnt.ptr + 4),
-                                                          1, kFtrMaxRounds, err, lc)
-                            : MCE_ERR_ARG;
+        const int fmode = ftr_rounds_mode();
+        int pst = MCE_ERR_ARG;
+        if (fmode == 1)
+            pst = Kernels<D>::ftr_resolve_all(R, nR, cell_ent2.ptr, boff.ptr, H - 1, MC, status.ptr, owner.ptr,
+                                              ftr_wl[0].ptr, ftr_wl[1].ptr, ftr_cnt.ptr, ftr_resume.ptr,
+                                              reinterpret_cast<unsigned*>(ftr_cnt.ptr + 4), 1, kFtrMaxRounds, err,
+                                              lc);
+        else if (fmode == 2 && !g_device_alloc_forbidden) {
+            if (!ftr_graph && Kernels<D>::ftr_graph_create(&ftr_graph, lc) != MCE_OK) {
+                set_error("the CUDA graph of the term reduction's rounds could not be built");
+                return MCE_ERR_CUDA;
+            }
+            pst = Kernels<D>::ftr_graph_launch(ftr_graph, R, nR, cell_ent2.ptr, boff.ptr, H - 1, MC, status.ptr,
+                                               owner.ptr, ftr_wl[0].ptr, ftr_wl[1].ptr, ftr_cnt.ptr, ftr_resume.ptr,
+                                               kFtrMaxRounds, err, lc);
+            if (pst != MCE_OK) {
+                set_error("launching the CUDA graph of the term reduction's rounds failed");
+                return MCE_ERR_CUDA;
+            }
+        }
         pend();
         int unk = 0;
         long long bound = nR;

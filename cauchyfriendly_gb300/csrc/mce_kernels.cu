@@ -12,6 +12,8 @@
 #include <algorithm>
 #include <climits>
 #include <cstdlib>
+#include <cstring>
+#include <memory>
 #include <mutex>
 #include <vector>
 
@@ -1489,6 +1491,65 @@ __global__ void __launch_bounds__(128) k_ftr_resolve_all(TermRecs R, long long n
     }
 }
 
+// The resolution rounds after the first as a loop that runs on the device
+// inside a CUDA graph: a WHILE conditional node whose body is one round over
+// the previous round's worklist (k_ftr_graph_round) followed by a one-thread
+// kernel (k_ftr_graph_next) that advances the round, clears the next round's
+// count and sets the loop condition from the worklist just produced, so the
+// host neither launches nor waits for the rounds.  The graph is built once per
+// engine; its kernels read their pointers from a device argument block that
+// the host rewrites before each launch.  Round r reads worklist (r - 1) & 1
+// and count cnt[(r - 1) % 8] and writes worklist r & 1 and cnt[r % 8], as the
+// batched rounds do.  After max_rounds rounds the loop stops with
+// kErrResolveStalled.
+template <int D>
+struct FtrLoopArgs {
+    TermRecs R;
+    long long nR;
+    const CellEntry<D>* ent;
+    const long long* boff;
+    long long hmask;
+    int MC;
+    int* status;
+    int* owner;
+    int* wl0;
+    int* wl1;
+    int* cnt;
+    int* resume;
+    int* err;
+    int round;       // the round the body runs next (the device advances it)
+    int max_rounds;
+};
+
+template <int D>
+__global__ void __launch_bounds__(128) k_ftr_graph_round(const FtrLoopArgs<D>* a)
+{
+    const int r = *(volatile const int*)&a->round;
+    const TermRecs R = a->R;
+    const int* wl_in = ((r - 1) & 1) ? a->wl1 : a->wl0;
+    int* wl_out = (r & 1) ? a->wl1 : a->wl0;
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long nth = (long long)gridDim.x * blockDim.x;
+    ftr_round<D>(R, a->nR, a->ent, a->boff, a->hmask, a->MC, a->status, a->owner, wl_in, a->cnt + (r - 1) % 8, wl_out,
+                 a->cnt + r % 8, a->resume, tid, nth);
+}
+
+template <int D>
+__global__ void k_ftr_graph_next(FtrLoopArgs<D>* a, cudaGraphConditionalHandle h)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int r = a->round;
+    const int n = *(volatile int*)(a->cnt + r % 8);
+    a->cnt[(r + 1) % 8] = 0;
+    a->round = r + 1;
+    unsigned more = n > 0 ? 1u : 0u;
+    if (more && r + 1 >= a->max_rounds) {
+        atomicOr(a->err, kErrResolveStalled);
+        more = 0u;
+    }
+    cudaGraphSetConditional(h, more);
+}
+
 #if MCE_COMMON_UNIT
 __global__ void k_group_count(const int* status, const int* owner, long long nR, int* gcnt)
 {
@@ -2602,6 +2663,124 @@ int Kernels<D>::ftr_resolve_all(TermRecs R, long long nR, const void* ent, const
     }
     ++g_launches;
     return MCE_OK;
+}
+
+template <int D>
+struct FtrGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    FtrLoopArgs<D>* dargs = nullptr;
+    int* hround = nullptr;  // page-locked copy of the round counter after a launch
+    FtrLoopArgs<D> hargs;
+    bool pending = false;
+    ~FtrGraph()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (dargs) cudaFree(dargs);
+        if (hround) cudaFreeHost(hround);
+    }
+};
+
+template <int D>
+int Kernels<D>::ftr_graph_create(void** out, const LaunchCfg& c)
+{
+    *out = nullptr;
+    std::unique_ptr<FtrGraph<D>> g(new FtrGraph<D>());
+    auto fail = [&]() {
+        cudaGetLastError();
+        return MCE_ERR_CUDA;
+    };
+    if (cudaMalloc(&g->dargs, sizeof(FtrLoopArgs<D>)) != cudaSuccess) return fail();
+    if (cudaMallocHost(&g->hround, sizeof(int)) != cudaSuccess) {
+        g->hround = nullptr;
+        return fail();
+    }
+    int bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_ftr_graph_round<D>, 128, 0) != cudaSuccess || bps < 1)
+        return fail();
+    if (cudaGraphCreate(&g->graph, 0) != cudaSuccess) return fail();
+    cudaGraphConditionalHandle h;
+    if (cudaGraphConditionalHandleCreate(&h, g->graph, 1, cudaGraphCondAssignDefault) != cudaSuccess) return fail();
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cond;
+    if (cudaGraphAddNode(&cond, g->graph, nullptr, nullptr, 0, &cp) != cudaSuccess) return fail();
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    FtrLoopArgs<D>* a = g->dargs;
+    void* rargs[] = {&a};
+    cudaKernelNodeParams kr;
+    memset(&kr, 0, sizeof(kr));
+    kr.func = (void*)k_ftr_graph_round<D>;
+    kr.gridDim = dim3((unsigned)(bps * c.num_sms));
+    kr.blockDim = dim3(128);
+    kr.kernelParams = rargs;
+    cudaGraphNode_t nround, nnext;
+    if (cudaGraphAddKernelNode(&nround, body, nullptr, 0, &kr) != cudaSuccess) return fail();
+    void* nargs[] = {&a, &h};
+    cudaKernelNodeParams kn;
+    memset(&kn, 0, sizeof(kn));
+    kn.func = (void*)k_ftr_graph_next<D>;
+    kn.gridDim = dim3(1);
+    kn.blockDim = dim3(32);
+    kn.kernelParams = nargs;
+    if (cudaGraphAddKernelNode(&nnext, body, &nround, 1, &kn) != cudaSuccess) return fail();
+    if (cudaGraphInstantiate(&g->exec, g->graph, 0) != cudaSuccess) {
+        g->exec = nullptr;
+        return fail();
+    }
+    *out = g.release();
+    return MCE_OK;
+}
+
+template <int D>
+int Kernels<D>::ftr_graph_launch(void* gv, TermRecs R, long long nR, const void* ent, const long long* boff,
+                                 long long hmask, int MC, int* status, int* owner, int* wl0, int* wl1, int* cnt,
+                                 int* resume, int max_rounds, int* err, const LaunchCfg& c)
+{
+    FtrGraph<D>* g = static_cast<FtrGraph<D>*>(gv);
+    FtrLoopArgs<D>& h = g->hargs;
+    h.R = R;
+    h.nR = nR;
+    h.ent = static_cast<const CellEntry<D>*>(ent);
+    h.boff = boff;
+    h.hmask = hmask;
+    h.MC = MC;
+    h.status = status;
+    h.owner = owner;
+    h.wl0 = wl0;
+    h.wl1 = wl1;
+    h.cnt = cnt;
+    h.resume = resume;
+    h.err = err;
+    h.round = 1;
+    h.max_rounds = max_rounds;
+    // (a pageable source: staged before the call returns)
+    if (cudaMemcpyAsync(g->dargs, &h, sizeof(h), cudaMemcpyHostToDevice, c.stream) != cudaSuccess ||
+        cudaGraphLaunch(g->exec, c.stream) != cudaSuccess ||
+        cudaMemcpyAsync(g->hround, &g->dargs->round, sizeof(int), cudaMemcpyDeviceToHost, c.stream) != cudaSuccess) {
+        cudaGetLastError();
+        return MCE_ERR_CUDA;
+    }
+    g->pending = true;
+    return MCE_OK;
+}
+
+template <int D>
+void Kernels<D>::ftr_graph_collect(void* gv)
+{
+    FtrGraph<D>* g = static_cast<FtrGraph<D>*>(gv);
+    if (!g || !g->pending) return;
+    g->pending = false;
+    g_launches += 2LL * std::max(0, *g->hround - 1);  // a round and its loop step per iteration
+}
+
+template <int D>
+void Kernels<D>::ftr_graph_destroy(void* gv)
+{
+    delete static_cast<FtrGraph<D>*>(gv);
 }
 
 static inline size_t gtable_smem_per_warp(int MC, int capR)

@@ -188,6 +188,17 @@ struct Kernels {
     static int ftr_resolve_all(TermRecs R, long long nR, const void* ent, const long long* boff, long long hmask,
                                int MC, int* status, int* owner, int* wl0, int* wl1, int* cnt, int* resume,
                                unsigned* bar, int first_round, int max_rounds, int* err, const LaunchCfg& c);
+    // The rounds from round 1 on as a device-side WHILE loop of a CUDA graph
+    // (built once per engine by ftr_graph_create; its kernels read their
+    // pointers from a device argument block that ftr_graph_launch rewrites);
+    // ftr_graph_collect, after the stream has been synchronised, counts the
+    // rounds' launches.
+    static int ftr_graph_create(void** graph, const LaunchCfg& c);
+    static int ftr_graph_launch(void* graph, TermRecs R, long long nR, const void* ent, const long long* boff,
+                                long long hmask, int MC, int* status, int* owner, int* wl0, int* wl1, int* cnt,
+                                int* resume, int max_rounds, int* err, const LaunchCfg& c);
+    static void ftr_graph_collect(void* graph);
+    static void ftr_graph_destroy(void* graph);
     // g-tables of every reduction group (flattening.hpp:318-568).
     static void gtable(TermRecs R, const int* roots_list, long long nroots, const int* gcnt,
                        const long long* goff, const int* members, ParentList P, Tables Told, const int* Bkeys,

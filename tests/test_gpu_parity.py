@@ -325,19 +325,23 @@ def test_trim_memory_between_reset_and_step():
         assert np.array_equal(first[k], second[k]), k
 
 
-def test_persistent_term_reduction_keeps_results_bit_identical():
-    """MCE_FTR_PERSISTENT=1 runs the term reduction's rounds after the first
-    in one persistent cooperative launch over the device worklists: the
-    golden fixtures stay bit-identical and a random batch matches the oracle
-    (a subprocess: the switch is read once per process)."""
+@pytest.mark.parametrize("mode", ["batched", "persistent", "graph"])
+def test_term_reduction_round_modes_keep_results_bit_identical(mode):
+    """MCE_FTR_ROUNDS picks how the term reduction's rounds after the first
+    run: queued in batches (the host reading the worklist length once per
+    batch), in one persistent cooperative launch over the device worklists,
+    or as a device-side WHILE loop in a CUDA graph.  Under each, the golden
+    fixtures stay bit-identical and a random batch matches the oracle (a
+    subprocess: the switch is read once per process)."""
     _gpu()
     import os
     import subprocess
     import sys
-    env = dict(os.environ, MCE_FTR_PERSISTENT="1")
+    env = dict(os.environ, MCE_FTR_ROUNDS=mode)
+    env.pop("MCE_FTR_PERSISTENT", None)
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     r = subprocess.run([sys.executable, "-m", "pytest", os.path.join(root, "tests", "test_gpu_parity.py"), "-q",
-                        "-p", "no:cacheprovider", "-k", "(bit_identical or random_three_state) and not persistent"],
+                        "-p", "no:cacheprovider", "-k", "(bit_identical or random_three_state) and not round_modes"],
                        cwd=root, env=env, capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]
     assert " passed" in r.stdout
