@@ -411,6 +411,21 @@ class Oracle(_EstimatorBase):
         lowered child apart (no term reduction between the lowerings)."""
         return _cpdf_nd_call(self._l.lib.orc_cpdf_nd, self.h, x, "orc_cpdf_nd", 1 if reduce else 0)
 
+    def cpdf_marginal(self, xm, idx, nu_bar, reduce=True):
+        """The marginal pdf of the states idx (ascending, fewer than d) at xm
+        (complex; the reference's PointWiseNDimCauchyCPDF::evaluate_marginal_cpdf),
+        the last lookups at nu_bar (d - len(idx) values)."""
+        f = self._l.lib.orc_cpdf_marginal
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_void_p, _dp, _ip, ctypes.c_int, _dp, _dp, ctypes.c_int]
+        xx, nb = _arr(xm), _arr(nu_bar)
+        ii = np.ascontiguousarray(np.asarray(idx, dtype=np.int32))
+        out = np.zeros(2)
+        st = f(self.h, _ptr(xx), _ptr(ii, _ip), len(ii), _ptr(nb), _ptr(out), 1 if reduce else 0)
+        if st < 0:
+            raise RuntimeError("orc_cpdf_marginal returned %d" % st)
+        return complex(out[0], out[1])
+
 
 class OracleSlot:
     """A window slot of n_mgr oracle estimators with the batch interface the
@@ -514,6 +529,21 @@ class Reference(_EstimatorBase):
     def cpdf_nd(self, x):
         """The reference's own PointWiseNDimCauchyCPDF::evaluate_cpdf at x."""
         return _cpdf_nd_call(self._l.lib.ref_cpdf_nd, self.h, x, "ref_cpdf_nd", None)
+
+    def cpdf_marginal(self, xm, idx, seed):
+        """The reference's own evaluate_marginal_cpdf of the states idx at xm
+        after srand(seed); returns (value, nu_bar it drew)."""
+        f = self._l.lib.ref_cpdf_marginal
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_void_p, _dp, _ip, ctypes.c_int, ctypes.c_uint, _dp, _dp]
+        xx = _arr(xm)
+        ii = np.ascontiguousarray(np.asarray(idx, dtype=np.int32))
+        nb = np.zeros(self.d - len(ii))
+        out = np.zeros(2)
+        st = f(self.h, _ptr(xx), _ptr(ii, _ip), len(ii), int(seed), _ptr(nb), _ptr(out))
+        if st < 0:
+            raise RuntimeError("ref_cpdf_marginal returned %d" % st)
+        return complex(out[0], out[1]), nb
 
     def cpdf_1d_grid(self, marg, low, high, res, max_points=100000):
         """The reference's own marginal 1-D pdf grid; returns (x, y, bar_nu)."""

@@ -1570,6 +1570,91 @@ static int cpdf_nd_eval(Estimator& E, const double* xk, cplx* out, bool reduce =
     return 0;
 }
 
+// PointWiseNDimCauchyCPDF::evaluate_marginal_cpdf (cpdf_ndim.hpp:918-1230):
+// the marginal pdf of the states idx[0..nm) (ascending, 0 < nm < d) at
+// xm[nm].  Every term's A columns and b are reordered so that the states
+// integrated out come first and the kept states last, b less the point at
+// the kept states (construct_lowered_marginal_parent_elements :445-517); nm
+// lowerings as in evaluate_cpdf; then every term of the d - nm dimensions
+// left is looked up at the sign vector of A nu_bar (:1180-1212); the sum
+// / Re fz * (2 pi)^-nm.  Returns as cpdf_nd_eval.
+static int cpdf_marginal_eval(Estimator& E, const double* xm, const int* idx, int nm, const double* nu_bar,
+                              cplx* out, bool reduce = true)
+{
+    if (E.master_step < 1 || E.errors) return -1;
+    const int dim = E.d, nz = dim - nm;
+    if (nm < 1 || nm >= dim) return -2;
+    std::vector<int> reo(dim);
+    std::vector<char> F(dim, 1);
+    for (int i = 0; i < nm; i++) {
+        reo[nz + i] = idx[i];
+        F[idx[i]] = 0;
+    }
+    for (int i = 0, c = 0; i < dim; i++)
+        if (F[i]) reo[c++] = i;
+    int top = 0;
+    for (int i = 0; i < E.shape_range; i++)
+        if (E.terms_per_shape[i] > 0) top = i;
+    int shape_range = top + 1;
+    std::vector<std::vector<Term>> par(shape_range);
+    for (const Term& t : E.terms) {
+        if (t.m >= shape_range) continue;
+        Term r = t;
+        std::vector<double> tb(t.b);
+        for (int i = 0; i < nm; i++) tb[reo[nz + i]] -= xm[i];
+        for (int i = 0; i < t.m; i++)
+            for (int j = 0; j < dim; j++) r.A[i * dim + j] = t.A[i * dim + reo[j]];
+        for (int j = 0; j < dim; j++) r.b[j] = tb[reo[j]];
+        par[t.m].push_back(std::move(r));
+    }
+    for (int d = dim; d > nz; d--) {
+        const int dl = d - 1;
+        std::vector<Term> kids;
+        for (int m = d; m < shape_range; m++)
+            for (const Term& P : par[m]) {
+                const size_t k0 = kids.size();
+                lower_children(P, d, nullptr, kids);
+                for (size_t k = k0; k < kids.size(); k++) {
+                    const int pre = kids[k].m;
+                    const int ns = mu_coalign(kids[k], dl);
+                    if (ns < 0) return -3;
+                    kids[k].has_cmap = ns < pre;
+                }
+            }
+        std::vector<std::vector<Term*>> byshape(shape_range);
+        for (Term& c : kids) byshape[c.m].push_back(&c);
+        std::vector<std::vector<Term>> next(shape_range);
+        for (int m = 0; m < shape_range; m++) {
+            if (byshape[m].empty() || m < dl) continue;
+            std::vector<int> Fr;
+            if (reduce) ftr(byshape[m], dl, Fr);
+            else
+                for (size_t i = 0; i < byshape[m].size(); i++) Fr.push_back((int)i);
+            std::vector<Term*> roots;
+            make_gtables_shape(byshape[m], Fr, dl, 1.0, roots, true);
+            for (Term* r : roots) next[m].push_back(std::move(*r));
+        }
+        par.swap(next);
+        shape_range -= 1;
+    }
+    cplx f = mkc(0, 0);
+    for (int m = nz; m < shape_range; m++)
+        for (const Term& t : par[m]) {
+            int enc = 0;
+            for (int k = 0; k < m; k++) {
+                double w = 0;
+                for (int j = 0; j < nz; j++) w += t.A[k * nz + j] * nu_bar[j];
+                if (w < 0) enc |= 1 << k;
+            }
+            f += lookup_num(t.gp.get(), enc, m);
+        }
+    const double nf = __real__ E.fz;
+    f = mkc(__real__ f / nf, __imag__ f / nf);
+    const double s = pow(kTwoPiInv, nm);
+    *out = mkc(__real__ f * s, __imag__ f * s);
+    return 0;
+}
+
 static int cpdf_grid_points(double low, double high, double res)
 {
     return (int)((high - low + res - 1e-15) / res) + 1;
@@ -2223,6 +2308,16 @@ int orc_cpdf_nd(void* h, const double* x, double* out, int reduce)
         out[1] = __imag__ v;
     }
     return st;
+}
+
+int orc_cpdf_marginal(void* h, const double* xm, const int* idx, int nm, const double* nu_bar, double* out, int reduce)
+{
+    cplx v;
+    const int st = cpdf_marginal_eval(*(Estimator*)h, xm, idx, nm, nu_bar, &v, reduce != 0);
+    if (st) return st;
+    out[0] = __real__ v;
+    out[1] = __imag__ v;
+    return 0;
 }
 
 int orc_cpdf_1d_grid(void* h, int marg, const double* bar_nu, double low, double high, double res, int max_points,

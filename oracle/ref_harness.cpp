@@ -273,6 +273,37 @@ int ref_cpdf_nd(void* vh, const double* x, double* out)
     return 0;
 }
 
+// PointWiseNDimCauchyCPDF::evaluate_marginal_cpdf (include/cpdf_ndim.hpp:918-1230)
+// of the states idx[0..nm) at xm[nm] with the handle's pdf object, after
+// srand(seed).  The function draws from rand() as it goes: each lowering's
+// DiffCellEnumHelper::init draws one b_pert value per hyperplane of its
+// largest shape (cell_enumeration.hpp:466-469; the shape range starts at the
+// largest shape held + 1 and drops by one a lowering), then nu_bar[d - nm]
+// = 2 U - 1 (cpdf_ndim.hpp:1187-1188).  nu_bar receives those values,
+// reproduced from the same draws.  out[2] = (re, im); -5 where the reference
+// would assert.
+int ref_cpdf_marginal(void* vh, const double* xm, const int* idx, int nm, unsigned seed, double* nu_bar, double* out)
+{
+    RefHandle* h = (RefHandle*)vh;
+    if (h->est->master_step < 1 || h->est->numeric_moment_errors || nm < 1 || nm >= h->d) return -5;
+    if (!h->cpdf) h->cpdf = new PointWiseNDimCauchyCPDF(h->est);
+    int top = 0;
+    for (int i = 0; i < h->est->shape_range; i++)
+        if (h->est->terms_per_shape[i] > 0) top = i;
+    long long skip = 0;
+    for (int l = 0; l < nm; l++) skip += (top + 1 - l) - 1;
+    srand(seed);
+    for (long long i = 0; i < skip; i++) rand();
+    for (int i = 0; i < h->d - nm; i++) nu_bar[i] = 2 * random_uniform() - 1;
+    srand(seed);
+    std::vector<double> x(xm, xm + nm);
+    std::vector<int> id(idx, idx + nm);
+    const C_COMPLEX_TYPE v = h->cpdf->evaluate_marginal_cpdf(x.data(), id.data(), nm);
+    out[0] = __real__ v;
+    out[1] = __imag__ v;
+    return 0;
+}
+
 int ref_cpdf_1d_grid(void* vh, int marg, double low, double high, double res, int max_points, double* xs,
                      double* ys, double* bar_nu)
 {

@@ -15,7 +15,7 @@ REL_TOL = 1e-9
 def names():
     """The step-record fixtures (the marginal pdf ones are cpdf_names())."""
     return sorted(n for n in (os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
-                  if not n.startswith(("cpdf1d_", "cpdf2d_", "cpdfnd_", "ext_", "rel2d_", "win_", "speyer_",
+                  if not n.startswith(("cpdf1d_", "cpdf2d_", "cpdfnd_", "cpdfmarg_", "ext_", "rel2d_", "win_", "speyer_",
                                        "tr_ordering_", "adj_")))
 
 
@@ -50,6 +50,25 @@ def load_cpdfnd(name):
         prob[k] = int(z[k])
     prob["B"] = None
     return prob, (z["root_point"], z["b_pert"]), int(z["updates"]), z["x"], z["f"]
+
+
+def cpdfmarg_names():
+    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "cpdfmarg_*.npz")))
+
+
+def load_cpdfmarg(name):
+    """(problem, (root_point, b_pert), updates, [(idx, xm, nu_bar, complex value)])"""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    prob = {k: z[k] for k in ("Phi", "Gamma", "beta", "H", "gamma", "A0", "p0", "b0", "msmts")}
+    for k in ("d", "pncc", "cmcc", "p", "steps"):
+        prob[k] = int(z[k])
+    prob["B"] = None
+    d = prob["d"]
+    cases = []
+    for idx, xm, nu, f in zip(z["idx"], z["xm"], z["nu_bar"], z["f"]):
+        nm = int(np.sum(idx >= 0))
+        cases.append((idx[:nm].astype(np.int32), xm[:nm], nu[:d - nm], complex(f)))
+    return prob, (z["root_point"], z["b_pert"]), int(z["updates"]), cases
 
 
 def rel2d_names():

@@ -67,6 +67,20 @@ def test_oracle_nd_pdf_matches_reference_bitwise(name):
     assert G.bitwise_equal(got, F), (name, G.relerr(got, F))
 
 
+@pytest.mark.parametrize("name", G.cpdfmarg_names())
+def test_oracle_marginal_pdf_matches_reference_bitwise(name):
+    """The oracle's marginal pdf of every subset of the states
+    (PointWiseNDimCauchyCPDF::evaluate_marginal_cpdf: columns reordered, the
+    kept states lowered out, the rest looked up at nu_bar) gives the
+    reference's values bit for bit (tests/golden/cpdfmarg_*.npz)."""
+    prob, consts, updates, cases = G.load_cpdfmarg(name)
+    est = _stepped_oracle(prob, consts, updates)
+    got = np.array([est.cpdf_marginal(xm, idx, nu) for idx, xm, nu, _ in cases])
+    want = np.array([f for _, _, _, f in cases])
+    est.close()
+    assert G.bitwise_equal(got, want), (name, G.relerr(got, want))
+
+
 def test_oracle_nd_pdf_refuses_before_the_first_step():
     from cauchyfriendly_gb300 import workloads as W
     prob = W.four_state_lti(seed=0, steps=3)
