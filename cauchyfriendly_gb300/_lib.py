@@ -33,6 +33,7 @@ SIGNATURES = {
     "mce_cpdf_1d_grid": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_double, ctypes.c_int, _dp, _dp]),
     "mce_cpdf_nd": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.c_int, _dp]),
+    "mce_cpdf_marginal": (ctypes.c_int, [_vp, ctypes.c_int, _ip, ctypes.c_int, _dp, _dp, ctypes.c_int, _dp]),
     "mce_cpdf_2d_grid": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp] + [ctypes.c_double] * 6
                          + [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]),
     "mce_draw_bar_nu": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_int, _dp]),

@@ -328,6 +328,8 @@ public:
                              int max_points, double* xs, double* ys) = 0;
     // PointWiseNDimCauchyCPDF::evaluate_cpdf at npts points (csrc/mce_ndpdf.cu)
     virtual int cpdf_nd(int est, const double* x, int npts, double* out) = 0;
+    virtual int cpdf_marginal(int est, const int* idx, int nm, const double* nu_bar, const double* x, int npts,
+                              double* out) = 0;
     // waits for the work the engine queued (after a step that stopped early)
     virtual void drain() = 0;
     // Estimator e's current terms for the relative system: the device lists,
@@ -1820,6 +1822,30 @@ public:
     NdWork* ndw = nullptr;
     int cpdf_nd(int e, const double* x, int npts, double* out) override
     {
+        return cpdf_points(e, nullptr, 0, nullptr, x, npts, out);
+    }
+
+    // PointWiseNDimCauchyCPDF::evaluate_marginal_cpdf (cpdf_ndim.hpp:918-1230):
+    // the marginal pdf of the states idx[0..nm) (ascending, 0 < nm < d) at
+    // npts points x[npts][nm], the terms left after nm lowerings looked up
+    // at nu_bar[d - nm]
+    int cpdf_marginal(int e, const int* idx, int nm, const double* nu_bar, const double* x, int npts,
+                      double* out) override
+    {
+        if (!idx || !nu_bar || nm < 1 || nm >= D) {
+            set_error("marginal pdf: 0 < number of states < d, and nu_bar, are required");
+            return MCE_ERR_ARG;
+        }
+        for (int i = 0; i < nm; i++)
+            if (idx[i] < 0 || idx[i] >= D || (i > 0 && idx[i] <= idx[i - 1])) {
+                set_error("marginal pdf: the state indices must ascend within [0, d)");
+                return MCE_ERR_ARG;
+            }
+        return cpdf_points(e, idx, nm, nu_bar, x, npts, out);
+    }
+
+    int cpdf_points(int e, const int* idx, int nm, const double* nu_bar, const double* x, int npts, double* out)
+    {
         if (e < 0 || e >= E || !x || !out || npts < 1) return MCE_ERR_ARG;
         if (MC > 16) {
             set_error("N-D pdf: terms of more than 16 hyperplanes are not supported");
@@ -1855,6 +1881,19 @@ public:
         in.keys = Tb[cur].keys.ptr;
         in.vals = Tb[cur].vals.ptr;
         in.fz = est[e].fz[0];
+        if (nm > 0) {
+            // the states integrated out first, the kept states last
+            // (evaluate_marginal_cpdf, cpdf_ndim.hpp:950-968)
+            bool kept[kMaxDim] = {false};
+            for (int i = 0; i < nm; i++) {
+                in.reorient[D - nm + i] = idx[i];
+                kept[idx[i]] = true;
+            }
+            for (int i = 0, c = 0; i < D; i++)
+                if (!kept[i]) in.reorient[c++] = i;
+            in.nkeep = nm;
+            in.nu_bar = nu_bar;
+        }
         return nd_pdf_eval(in, x, npts, out, ndw, lc, &launches);
     }
 
@@ -2682,6 +2721,12 @@ int mce_cpdf_nd(mce_handle* h, int e, const double* x, int npts, double* out)
 {
     if (bad(h, e)) return MCE_ERR_ARG;
     return h->eng->cpdf_nd(e, x, npts, out);
+}
+int mce_cpdf_marginal(mce_handle* h, int e, const int* marg_idx, int n_marg, const double* nu_bar, const double* x,
+                      int npts, double* out)
+{
+    if (bad(h, e)) return MCE_ERR_ARG;
+    return h->eng->cpdf_marginal(e, marg_idx, n_marg, nu_bar, x, npts, out);
 }
 int mce_cpdf_2d_grid(mce_handle* h, int e, int marg_idx1, int marg_idx2, const double* bar_nu, double gridx_low,
                      double gridx_high, double gridx_res, double gridy_low, double gridy_high, double gridy_res,

@@ -82,12 +82,20 @@ struct NdInput {
     const int* keys = nullptr;
     const cd* vals = nullptr;
     double fz = 0;  // Re fz, the normaliser
+    // The marginal pdf of nkeep states (0: the pdf of the full state): the
+    // state order with the states integrated out first and the kept ones last
+    // (reorient[j] = the state in position j), and the point nu_bar[D - nkeep]
+    // at which the terms left after nkeep lowerings are looked up (host).
+    int nkeep = 0;
+    int reorient[kMaxDim] = {0};
+    const double* nu_bar = nullptr;
 };
 struct NdWork;
 NdWork* nd_work_create();
 void nd_work_destroy(NdWork* w);
-// The pdf at npts points x_host[npts][D] into out_host[2 * npts] (re, im);
-// kernels launched are added to *launches.
+// The pdf at npts points x_host[npts][D] (the marginal: [npts][nkeep], the
+// kept states in ascending order) into out_host[2 * npts] (re, im); kernels
+// launched are added to *launches.
 int nd_pdf_eval(const NdInput& in, const double* x_host, int npts, double* out_host, NdWork* w, const LaunchCfg& lc,
                 long long* launches);
 

@@ -692,6 +692,69 @@ __global__ void k_nd_final_combine(const cd* partial, const long long* coff, int
     out[2 * p + 1] = s.im / fz * scale;
 }
 
+// The marginal pdf's first level (construct_lowered_marginal_parent_elements,
+// cpdf_ndim.hpp:445-517): every term's A columns and b in the order
+// reo (the states integrated out first, the kept states last).
+struct NdReorient {
+    int r[kMaxDim];
+};
+__global__ void k_nd_reorient(const int* m, const double* A, const double* b, long long n, int MC, int D,
+                              NdReorient reo, double* Ao, double* bo)
+{
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int mt = m[t];
+        const double* Ai = A + t * MC * D;
+        double* Aw = Ao + t * MC * D;
+        for (int i = 0; i < mt; i++)
+            for (int j = 0; j < D; j++) Aw[i * D + j] = Ai[i * D + reo.r[j]];
+        for (int j = 0; j < D; j++) bo[t * D + j] = b[t * D + reo.r[j]];
+    }
+}
+
+// The marginal pdf's last stage (cpdf_ndim.hpp:1180-1212) summed over a
+// chunk of one point's terms (ld dimensions, A [MC][ld]): each term's g value
+// at the sign vector of A nu (bit k set where row k . nu < 0).  Chunks as in
+// k_nd_final_partial.
+__global__ void k_nd_final_marg_partial(NdTerms T, int MC, int ld, const double* nu, const int* keys, const cd* vals,
+                                        const long long* pstart, const long long* coff, int npts, cd* partial)
+{
+    __shared__ double sre[kNdFinalThreads], sim[kNdFinalThreads];
+    const long long b = blockIdx.x;
+    int lo = 0, hi = npts;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (coff[mid] <= b) lo = mid;
+        else hi = mid;
+    }
+    const int p = lo;
+    const long long a = pstart[p] + (b - coff[p]) * kNdFinalChunk;
+    const long long e = min(pstart[p + 1], a + kNdFinalChunk);
+    cd s = mkcd(0, 0);
+    for (long long i = a + threadIdx.x; i < e; i += kNdFinalThreads) {
+        const int m = T.m[i];
+        const double* Ai = T.A + i * MC * ld;
+        int enc = 0;
+        for (int k = 0; k < m; k++) {
+            double w = 0.0;
+            for (int j = 0; j < ld; j++) w += Ai[k * ld + j] * nu[j];
+            if (neg(w)) enc |= 1 << k;
+        }
+        s = cadd(s, lookup_num(keys + T.toff[i], vals + T.toff[i], T.tcnt[i], enc, m));
+    }
+    sre[threadIdx.x] = s.re;
+    sim[threadIdx.x] = s.im;
+    __syncthreads();
+    for (int o = kNdFinalThreads / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            sre[threadIdx.x] += sre[threadIdx.x + o];
+            sim[threadIdx.x] += sim[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[b] = mkcd(sre[0], sim[0]);
+}
+
 }  // namespace
 
 struct NdWork {
@@ -702,6 +765,8 @@ struct NdWork {
     NdBuf<cd> vals[2];
     NdBuf<long long> coff, cellof, kscan, scan_tmp;
     NdBuf<double> x, out;
+    NdBuf<double> rA, rb, nu;  // the marginal's reordered first level and nu_bar
+    std::vector<double> h_x;
     NdBuf<int> err;
     NdBuf<long long> pstart, pcoff;
     NdBuf<cd> partial;
@@ -850,17 +915,32 @@ int nd_pdf_eval(const NdInput& in, const double* x_host, int npts, double* out_h
         report_error("N-D pdf: one-dimensional estimators use the marginal 1-D pdf");
         return MCE_ERR_ARG;
     }
+    if (in.nkeep < 0 || in.nkeep >= D || (in.nkeep > 0 && !in.nu_bar)) return MCE_ERR_ARG;
+    // the marginal's points: the kept states' coordinates in the last nkeep
+    // places of a D-vector whose other places hold 0 (b - 0 is b, so the
+    // first lowering subtracts the point at the kept states only, as
+    // construct_lowered_marginal_parent_elements does)
+    const int xd = in.nkeep ? in.nkeep : D;
+    const double* xs = x_host;
+    if (in.nkeep) {
+        w->h_x.assign((size_t)npts * D, 0.0);
+        for (int p = 0; p < npts; p++)
+            for (int i = 0; i < in.nkeep; i++) w->h_x[(size_t)p * D + D - in.nkeep + i] = x_host[(size_t)p * in.nkeep + i];
+        xs = w->h_x.data();
+    }
     // points in chunks: every lowering multiplies the terms by their rows
     // (at most MC, MC - 1, ...), so the first level's (point, term) pairs are
     // bounded such that the last level stays under about 2^26 children
+    const int lowerings = in.nkeep ? in.nkeep : D - 1;
     double growth = 1.0;
-    for (int l = 0; l < D - 1; l++) growth *= std::max(1, MC - l);
+    for (int l = 0; l < lowerings; l++) growth *= std::max(1, MC - l);
     const double budget = (double)(1LL << 26) / growth;
     const long long per = std::max<long long>(1, (long long)(budget / (double)std::max<long long>(1, in.n)));
+    (void)xd;
     w->launches = 0;
     for (long long p0 = 0; p0 < npts; p0 += per) {
         const int np = (int)std::min<long long>(per, npts - p0);
-        const int s = nd_pdf_chunk(in, x_host + p0 * D, np, out_host + 2 * p0, *w, lc);
+        const int s = nd_pdf_chunk(in, xs + p0 * D, np, out_host + 2 * p0, *w, lc);
         if (s) return s;
     }
     if (launches) *launches += w->launches;
@@ -880,14 +960,27 @@ int nd_pdf_chunk(const NdInput& in, const double* x_host, int npts, double* out_
     ND_CUDA(cudaMemsetAsync(w->err.ptr, 0, sizeof(int), lc.stream));
     ND_CUDA(cudaMemsetAsync(w->out.ptr, 0, sizeof(double) * 2 * npts, lc.stream));
     // level 0: the estimator's own terms and tables, shared by every point
+    // (for the marginal, their A columns and b reordered)
     NdTerms P{nullptr, const_cast<int*>(in.m), const_cast<double*>(in.A), const_cast<double*>(in.p),
               const_cast<double*>(in.b), const_cast<long long*>(in.toff), const_cast<int*>(in.tcnt)};
     const int* pkeys = in.keys;
     const cd* pvals = in.vals;
     long long n = in.n;
+    const int stop = in.nkeep ? D - in.nkeep : 1;  // the dimension the lowerings end at
+    if (in.nkeep && n > 0) {
+        if ((s = w->rA.ensure((size_t)n * MC * D))) return s;
+        if ((s = w->rb.ensure((size_t)n * D))) return s;
+        NdReorient reo;
+        for (int j = 0; j < kMaxDim; j++) reo.r[j] = j < D ? in.reorient[j] : 0;
+        k_nd_reorient<<<nd_grid(n, 128, lc.num_sms), 128, 0, lc.stream>>>(in.m, in.A, in.b, n, MC, D, reo, w->rA.ptr,
+                                                                          w->rb.ptr);
+        w->launches += 1;
+        P.A = w->rA.ptr;
+        P.b = w->rb.ptr;
+    }
     int cur = 0;
     bool empty = n == 0;
-    for (int ld = D; ld > 1 && !empty; ld--) {
+    for (int ld = D; ld > stop && !empty; ld--) {
         const bool first = ld == D;
         long long nn = 0;
         NdTermBufs& next = w->lev[cur];
@@ -910,8 +1003,9 @@ int nd_pdf_chunk(const NdInput& in, const double* x_host, int npts, double* out_
         if (n == 0) empty = true;
     }
     if (!empty) {
-        // pow(RECIPRICAL_TWO_PI, dim) (cpdf_ndim.hpp:893)
-        const double sc = pow(1.0 / (2.0 * M_PI), (double)D);
+        // pow(RECIPRICAL_TWO_PI, dim) (cpdf_ndim.hpp:893), for the marginal
+        // pow(RECIPRICAL_TWO_PI, num_marg_state_idxs) (:1214)
+        const double sc = pow(1.0 / (2.0 * M_PI), (double)(in.nkeep ? in.nkeep : D));
         if ((s = w->pstart.ensure(npts + 1))) return s;
         if ((s = w->pcoff.ensure(npts + 1))) return s;
         k_nd_point_starts<<<(npts + 1 + 127) / 128, 128, 0, lc.stream>>>(P.pt, n, npts, w->pstart.ptr);
@@ -929,8 +1023,15 @@ int nd_pdf_chunk(const NdInput& in, const double* x_host, int npts, double* out_
                                 cudaMemcpyHostToDevice, lc.stream));
         if (nb > 0) {
             if ((s = w->partial.ensure(nb + 1))) return s;
-            k_nd_final_partial<<<(unsigned)nb, kNdFinalThreads, 0, lc.stream>>>(P, MC, pkeys, pvals, w->pstart.ptr,
-                                                                                 w->pcoff.ptr, npts, w->partial.ptr);
+            if (in.nkeep) {
+                if ((s = w->nu.ensure((size_t)stop))) return s;
+                ND_CUDA(cudaMemcpyAsync(w->nu.ptr, in.nu_bar, sizeof(double) * stop, cudaMemcpyHostToDevice,
+                                        lc.stream));
+                k_nd_final_marg_partial<<<(unsigned)nb, kNdFinalThreads, 0, lc.stream>>>(
+                    P, MC, stop, w->nu.ptr, pkeys, pvals, w->pstart.ptr, w->pcoff.ptr, npts, w->partial.ptr);
+            } else
+                k_nd_final_partial<<<(unsigned)nb, kNdFinalThreads, 0, lc.stream>>>(P, MC, pkeys, pvals, w->pstart.ptr,
+                                                                                     w->pcoff.ptr, npts, w->partial.ptr);
         }
         k_nd_final_combine<<<(npts + 127) / 128, 128, 0, lc.stream>>>(w->partial.ptr, w->pcoff.ptr, npts, in.fz, sc,
                                                                      w->out.ptr);

@@ -225,6 +225,25 @@ class BatchedCauchyEstimator:
         _lib.check(self._lib.mce_cpdf_nd(self._h, int(e), _p(X), X.shape[0], _p(out)), "mce_cpdf_nd")
         return out[0::2] + 1j * out[1::2]
 
+    def cpdf_marginal(self, x, marg_idxs, nu_bar=None, e=0):
+        """The marginal pdf of the states marg_idxs (ascending, fewer than d)
+        of estimator e at the points x ([n][len(marg_idxs)]):
+        PointWiseNDimCauchyCPDF::evaluate_marginal_cpdf
+        (include/cpdf_ndim.hpp:918-1230); complex values.  nu_bar
+        (d - len(marg_idxs) values) stands for the reference's rand() draws;
+        by default a fixed point off the hyperplanes (the value does not
+        depend on it beyond rounding)."""
+        idx = np.ascontiguousarray(np.asarray(marg_idxs, dtype=np.int32).reshape(-1))
+        nz = self.d - len(idx)
+        if nu_bar is None:
+            nu_bar = np.cos(1.0 + 2.3 * np.arange(max(nz, 0)))
+        nu = np.ascontiguousarray(np.asarray(nu_bar, dtype=np.float64).reshape(-1))
+        X = np.ascontiguousarray(np.asarray(x, dtype=np.float64).reshape(-1, len(idx)))
+        out = np.zeros(2 * X.shape[0])
+        _lib.check(self._lib.mce_cpdf_marginal(self._h, int(e), idx.ctypes.data_as(_lib._ip), len(idx), _p(nu), _p(X),
+                                               X.shape[0], _p(out)), "mce_cpdf_marginal")
+        return out[0::2] + 1j * out[1::2]
+
     def cpdf_1d_grid(self, e, marg_idx, gridx_low, gridx_high, gridx_resolution, bar_nu):
         """Marginal 1-D conditional pdf of estimator e on the grid
         gridx_low..gridx_high step gridx_resolution

@@ -174,6 +174,20 @@ int mce_cpdf_1d_grid(mce_handle* h, int est, int marg_idx, const double* bar_nu,
  * enter the integration). */
 int mce_cpdf_nd(mce_handle* h, int est, const double* x, int npts, double* out);
 
+/* The marginal pdf of the states marg_idx[n_marg] (ascending, 0 < n_marg <
+ * d) of estimator `est` at npts points x[npts*n_marg]:
+ * PointWiseNDimCauchyCPDF::evaluate_marginal_cpdf (include/cpdf_ndim.hpp:
+ * 918-1230).  Every term's columns are reordered so that the states
+ * integrated out come first, the kept states are lowered out one at a time
+ * as in mce_cpdf_nd, and the terms of the d - n_marg dimensions left are
+ * looked up at the sign vector of A nu_bar; nu_bar[d - n_marg] stands for
+ * the values the reference draws from rand() (any point off the
+ * hyperplanes gives the same value up to rounding).  out[2*npts]; the same
+ * errors as mce_cpdf_nd, MCE_ERR_ARG for indices that do not ascend within
+ * [0, d). */
+int mce_cpdf_marginal(mce_handle* h, int est, const int* marg_idx, int n_marg, const double* nu_bar, const double* x,
+                      int npts, double* out);
+
 /* Marginal 2-D conditional pdf of estimator `est` over states
  * marg_idx1 < marg_idx2 on the grid x = gridx_low ... gridx_high (step
  * gridx_res) by y = gridy_low ... gridy_high, x varying fastest, as

@@ -136,6 +136,39 @@ def test_gpu_nd_pdf_matches_reference(name):
     est.close()
 
 
+@pytest.mark.parametrize("name", G.cpdfmarg_names())
+def test_gpu_marginal_pdf_matches_reference(name):
+    """mce_cpdf_marginal for every subset of the states short of all of them
+    (one call per subset, all its points at once) against the reference's
+    PointWiseNDimCauchyCPDF::evaluate_marginal_cpdf (tests/golden/
+    cpdfmarg_*.npz), each case at the nu_bar the reference drew: within 1e-9
+    relative, with a floor of 1e-3 of the fixture's largest value (the GPU
+    lowers every (point, term) pair without the reference's term reduction
+    between the lowerings, as mce_cpdf_nd does).  A nu_bar other than the
+    reference's gives the same values within the same tolerance."""
+    _, CE, _ = _need_gpu()
+    prob, (rp, bp), updates, cases = G.load_cpdfmarg(name)
+    est = _stepped_gpu(CE, prob, rp, bp, updates)
+    want = np.array([f for _, _, _, f in cases])
+    got = np.zeros(len(cases), dtype=complex)
+    other = np.zeros(len(cases), dtype=complex)
+    groups = {}
+    for i, (idx, xm, nu, _) in enumerate(cases):
+        groups.setdefault((tuple(idx), tuple(nu)), []).append(i)
+    for (idx, nu), rows in groups.items():
+        X = np.array([cases[i][1] for i in rows])
+        got[rows] = est.cpdf_marginal(X, list(idx), nu_bar=np.array(nu))
+        other[rows] = est.cpdf_marginal(X, list(idx))
+    assert G.relerr(got, want, floor=1e-3) <= G.REL_TOL, (name, G.relerr(got, want, floor=1e-3))
+    assert G.relerr(other, want, floor=1e-3) <= G.REL_TOL, (name, G.relerr(other, want, floor=1e-3))
+    with pytest.raises(Exception):
+        est.cpdf_marginal(np.zeros((1, 2)), [1, 0])  # indices must ascend
+    with pytest.raises(Exception):
+        est.cpdf_marginal(np.zeros((1, prob["d"])), list(range(prob["d"])))  # fewer than d states
+    assert est.device_errors() == 0
+    est.close()
+
+
 def test_gpu_nd_pdf_against_oracle_on_larger_estimators():
     """Larger term sets than the fixtures (a 4-state estimator after 6 updates,
     a 5-state two-measurement one after 5, a 3-state one after 8): the GPU
