@@ -481,9 +481,20 @@ __device__ inline DD ddiv(DD a, DD b)
     const double q = a.v / b.v;
     return DD{q, (a.t - q * b.t) / b.v};
 }
+// a / b with rb = 1 / b.v: the value divides (the same double as the
+// forward run), the tangent multiplies by the shared reciprocal (a row
+// normalised by one norm divides d values by it)
+__device__ inline DD ddiv_r(DD a, DD b, double rb)
+{
+    const double q = a.v / b.v;
+    return DD{q, (a.t - q * b.t) * rb};
+}
 __device__ inline DD dabs(DD x) { return x.v < 0 ? dneg(x) : (x.v > 0 ? x : DD{0.0, 0.0}); }
 
-constexpr int kRows = 16, kDim = 8;  // the step path's limits (16 hyperplanes, 8 states)
+// The record chain's limits: at most kGammaMax process-noise columns; a
+// kernel instantiation per state dimension D and row capacity MR (16, or 32
+// for records of 17 to 31 rows), so a thread's arrays are sized to the run.
+constexpr int kGammaMax = 8;
 
 struct ChainArgs {
     int d, pncc, p, MS, N, first, last, with_tp, sub, nP;
@@ -516,17 +527,19 @@ __device__ inline int dgate(const DD* r, const DD* c, int d)
     return pos ? 1 : (ng ? -1 : 0);
 }
 
+template <int D, int MR>
 __global__ void __launch_bounds__(128) k_adj_chain(ChainArgs a)
 {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)a.nP * a.N) return;
     const int pi = (int)(idx % a.nP), dir = (int)(idx / a.nP);
-    const int d = a.d;
+    constexpr int d = D;
     const int offb = 0, offg = offb + a.pncc, offp = offg + a.p, offPhi = offp + d, offG = offPhi + d * d,
               offH = offG + d * a.pncc;
     auto par = [&](const double* v, int i, int off) { return DD{v[i], dir == off + i ? 1.0 : 0.0}; };
-    // the parent's record
-    DD A[kRows * kDim], P[kRows], B[kDim];
+    // the parent's record; A then holds the MU's mu rows (m + 1 of them) and
+    // P its rho values
+    DD A[(MR + 1) * D], P[MR + 1], B[D];
     int m;
     if (a.first) {
         m = d;
@@ -542,7 +555,7 @@ __global__ void __launch_bounds__(128) k_adj_chain(ChainArgs a)
     }
     if (a.with_tp) {
         // Gamma pre-coalignment
-        DD Gt[kDim * kDim], bt[kDim];
+        DD Gt[kGammaMax * D], bt[kGammaMax];
         const int pncc = a.pncc;
         for (int i = 0; i < pncc; i++) {
             for (int j = 0; j < d; j++) Gt[i * d + j] = par(a.Gamma, j * pncc + i, offG);
@@ -551,10 +564,11 @@ __global__ void __launch_bounds__(128) k_adj_chain(ChainArgs a)
         for (int i = 0; i < pncc; i++) {
             DD nf = dd(0.0);
             for (int j = 0; j < d; j++) nf = dadd(nf, dabs(Gt[i * d + j]));
-            for (int j = 0; j < d; j++) Gt[i * d + j] = ddiv(Gt[i * d + j], nf);
+            const double rnf = 1.0 / nf.v;
+            for (int j = 0; j < d; j++) Gt[i * d + j] = ddiv_r(Gt[i * d + j], nf, rnf);
             bt[i] = dmul(bt[i], nf);
         }
-        bool F[kDim];
+        bool F[kGammaMax];
         for (int i = 0; i < pncc; i++) F[i] = true;
         for (int i = 0; i < pncc - 1; i++)
             if (F[i])
@@ -576,16 +590,17 @@ __global__ void __launch_bounds__(128) k_adj_chain(ChainArgs a)
                     u++;
                 }
         }
-        // time_prop
-        DD w[kRows * kDim];
-        for (int i = 0; i < m * d; i++) w[i] = A[i];
-        for (int i = 0; i < m; i++)
+        // time_prop, a row at a time
+        for (int i = 0; i < m; i++) {
+            DD w[D];
+            for (int k = 0; k < d; k++) w[k] = A[i * d + k];
             for (int j = 0; j < d; j++) {
                 DD sum = dd(0.0);
-                for (int k = 0; k < d; k++) sum = dadd(sum, dmul(w[i * d + k], par(a.Phi, k + j * d, offPhi)));
+                for (int k = 0; k < d; k++) sum = dadd(sum, dmul(w[k], par(a.Phi, k + j * d, offPhi)));
                 A[i * d + j] = sum;
             }
-        DD wb[kDim];
+        }
+        DD wb[D];
         for (int i = 0; i < d; i++) wb[i] = B[i];
         for (int i = 0; i < d; i++) {
             DD sum = dd(0.0);
@@ -597,9 +612,10 @@ __global__ void __launch_bounds__(128) k_adj_chain(ChainArgs a)
             DD n1 = dd(0.0);
             for (int j = 0; j < d; j++) n1 = dadd(n1, dabs(A[i * d + j]));
             P[i] = dmul(P[i], n1);
-            for (int j = 0; j < d; j++) A[i * d + j] = ddiv(A[i * d + j], n1);
+            const double rn1 = 1.0 / n1.v;
+            for (int j = 0; j < d; j++) A[i * d + j] = ddiv_r(A[i * d + j], n1, rn1);
         }
-        bool Fg[kDim];
+        bool Fg[kGammaMax];
         for (int j = 0; j < cnt; j++) Fg[j] = true;
         for (int j = 0; j < cnt; j++)
             for (int k = 0; k < m; k++)
@@ -617,13 +633,12 @@ __global__ void __launch_bounds__(128) k_adj_chain(ChainArgs a)
     // measurement update
     const DD* H = nullptr;
     (void)H;
-    DD Hr[kDim];
+    DD Hr[D];
     for (int j = 0; j < d; j++) Hr[j] = par(a.H, a.sub * d + j, offH);
     const DD gam = par(a.gamma, a.sub, offg);
-    DD mu[(kRows + 1) * kDim], rho[kRows + 1];
-    bool Fi[kRows + 1];
-    for (int i = 0; i < m * d; i++) mu[i] = A[i];
-    for (int i = 0; i < m; i++) rho[i] = P[i];
+    DD* mu = A;   // the rows, scaled in place
+    DD* rho = P;  // rho_l from p_l, in place
+    bool Fi[MR + 1];
     rho[m] = gam;
     for (int j = 0; j < d; j++) mu[m * d + j] = dd(0.0);
     Fi[m] = true;
@@ -631,8 +646,7 @@ __global__ void __launch_bounds__(128) k_adj_chain(ChainArgs a)
         DD h = dd(0.0);
         for (int j = 0; j < d; j++) h = dadd(h, dmul(Hr[j], mu[l * d + j]));
         if (fabs(h.v) < kMuEps) {
-            rho[l] = P[l];
-            Fi[l] = false;
+            Fi[l] = false;  // rho_l = p_l
         } else {
             const DD r = ddiv(dd(1.0), h);
             for (int j = 0; j < d; j++) mu[l * d + j] = dmul(mu[l * d + j], r);
@@ -648,7 +662,7 @@ __global__ void __launch_bounds__(128) k_adj_chain(ChainArgs a)
     for (int tt = 0; tt <= m; tt++) {
         if (!Fi[tt]) continue;
         const int term = tt == m ? pi : a.kid_off[pi] + kid++;
-        DD cA[kRows * kDim], cp[kRows], cq[kRows], cb[kDim];
+        DD cA[MR * D], cp[MR], cq[MR], cb[D];
         const DD cc = zeta, cd_ = rho[tt];
         for (int j = 0; j < d; j++) cb[j] = dadd(B[j], dmul(zeta, mu[tt * d + j]));
         int l = 0;
@@ -681,10 +695,11 @@ __global__ void __launch_bounds__(128) k_adj_chain(ChainArgs a)
                 DD n1 = dd(0.0);
                 for (int j = 0; j < d; j++) n1 = dadd(n1, dabs(cA[i * d + j]));
                 cp[i] = dmul(cp[i], n1);
-                for (int j = 0; j < d; j++) cA[i * d + j] = ddiv(cA[i * d + j], n1);
+                const double rn1 = 1.0 / n1.v;
+                for (int j = 0; j < d; j++) cA[i * d + j] = ddiv_r(cA[i * d + j], n1, rn1);
             }
             if (tt != m) {
-                bool F[kRows], hflag[kRows];
+                bool F[MR], hflag[MR];
                 for (int j = 0; j < m; j++) {
                     F[j] = true;
                     hflag[j] = horth ? ((horth >> j) & 1) : false;
@@ -758,6 +773,28 @@ __global__ void __launch_bounds__(128) k_adj_chain(ChainArgs a)
         }
     }
     atomicAdd(&a.grad[dir], g);
+}
+
+template <int D>
+void launch_chain_d(const ChainArgs& ca, long long nthr, cudaStream_t s)
+{
+    const int grid = (int)((nthr + 127) / 128);
+    if (ca.MS <= 16) k_adj_chain<D, 16><<<grid, 128, 0, s>>>(ca);
+    else k_adj_chain<D, 32><<<grid, 128, 0, s>>>(ca);
+}
+
+// The record chain of one update: a thread per (parent, direction).
+void launch_chain(const ChainArgs& ca, long long nthr, cudaStream_t s)
+{
+    switch (ca.d) {
+    case 2: launch_chain_d<2>(ca, nthr, s); break;
+    case 3: launch_chain_d<3>(ca, nthr, s); break;
+    case 4: launch_chain_d<4>(ca, nthr, s); break;
+    case 5: launch_chain_d<5>(ca, nthr, s); break;
+    case 6: launch_chain_d<6>(ca, nthr, s); break;
+    case 7: launch_chain_d<7>(ca, nthr, s); break;
+    default: launch_chain_d<8>(ca, nthr, s); break;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1788,7 +1825,7 @@ int bwd_run(mce_adjoint* o, const double* w, double* grad, Workspace& W)
         ca.kept_of = W.dkept.ptr;
         ca.grad = W.dgrad.ptr;
         const long long nthr = (long long)nP * N;
-        k_adj_chain<<<(int)((nthr + 127) / 128), 128, 0, s>>>(ca);
+        launch_chain(ca, nthr, s);
         W.tin.swap(W.tout);
     }
     if ((st = download(grad, W.dgrad.ptr, N, s))) {
@@ -1867,8 +1904,9 @@ mce_adjoint* mce_adjoint_create(int d, int pncc, int p, int steps, const double*
         if (status) *status = st;
         return nullptr;
     };
-    if (d < 2 || d > 8 || pncc < 1 || p < 1 || steps < 1 || !A0 || !p0 || !b0 || !root_point || !b_pert)
-        return fail(MCE_ERR_ARG, "mce_adjoint_create: invalid arguments");
+    if (d < 2 || d > 8 || pncc < 1 || pncc > kGammaMax || p < 1 || steps < 1 || !A0 || !p0 || !b0 || !root_point ||
+        !b_pert)
+        return fail(MCE_ERR_ARG, "mce_adjoint_create: invalid arguments (2 <= d <= 8, 1 <= pncc <= 8)");
     std::unique_ptr<mce_adjoint> o(new mce_adjoint());
     o->d = d;
     o->pncc = pncc;
@@ -1954,9 +1992,9 @@ mce_adjoint_batch* mce_adjoint_batch_create(int n_runs, int d, int pncc, int p, 
         if (status) *status = st;
         return nullptr;
     };
-    if (n_runs < 1 || d < 2 || d > 8 || pncc < 1 || p < 1 || !steps || !A0 || !p0 || !b0 || !root_point ||
-        !b_pert || bpert_stride < 1)
-        return fail(MCE_ERR_ARG, "mce_adjoint_batch_create: invalid arguments");
+    if (n_runs < 1 || d < 2 || d > 8 || pncc < 1 || pncc > kGammaMax || p < 1 || !steps || !A0 || !p0 || !b0 ||
+        !root_point || !b_pert || bpert_stride < 1)
+        return fail(MCE_ERR_ARG, "mce_adjoint_batch_create: invalid arguments (2 <= d <= 8, 1 <= pncc <= 8)");
     std::unique_ptr<mce_adjoint_batch> b(new mce_adjoint_batch());
     b->n = n_runs;
     b->d = d;
