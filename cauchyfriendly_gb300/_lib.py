@@ -101,8 +101,11 @@ SIGNATURES = {
     "mce_adjoint_destroy": (None, [_vp]),
     "mce_adjoint_batch_create": (_vp, [ctypes.c_int] * 4 + [_ip] + [_dp] * 5 + [ctypes.c_int, _ip]),
     "mce_adjoint_batch_forward": (ctypes.c_int, [_vp, _dp, ctypes.c_int] + [_dp] * 6),
+    "mce_adjoint_batch_forward_ltv": (ctypes.c_int, [_vp, _dp, ctypes.c_int] + [_dp] * 6),
+    "mce_adjoint_forward_ltv": (ctypes.c_int, [_vp] + [_dp] * 7),
     "mce_adjoint_batch_backward": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp]),
     "mce_adjoint_batch_num_params": (ctypes.c_int, [_vp]),
+    "mce_adjoint_batch_set_first_sub": (ctypes.c_int, [_vp, ctypes.c_int]),
     "mce_adjoint_batch_check": (ctypes.c_int, [_vp, _dp, _dp]),
     "mce_adjoint_batch_timing": (ctypes.c_int, [_vp, _dp]),
     "mce_adjoint_batch_destroy": (None, [_vp]),

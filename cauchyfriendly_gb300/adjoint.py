@@ -54,14 +54,17 @@ class AdjointRun:
 
     def forward(self, msmts, Phi, Gamma, beta, H, gamma, p0=None):
         """Runs and records every update; returns Re fz of each.  p0 (or None:
-        the constructor's) is the initial scale vector of this run."""
+        the constructor's) is the initial scale vector of this run.  Phi is
+        (d, d), or (steps, d, d) for a time-varying model (the gradient's Phi
+        is then that of a perturbation common to every step's Phi)."""
         f = lambda a: np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(-1))
         if p0 is not None:
             self._recreate(f(p0))
+        ltv = np.asarray(Phi).ndim == 3
         self._model = [f(x) for x in (msmts, Phi, Gamma, beta, H, gamma)]
         fz = np.zeros(self.steps * self.p)
-        _lib.check(self._L.mce_adjoint_forward(self._h, *[_lib.dp(x) for x in self._model], _lib.dp(fz)),
-                   "mce_adjoint_forward")
+        fn = self._L.mce_adjoint_forward_ltv if ltv else self._L.mce_adjoint_forward
+        _lib.check(fn(self._h, *[_lib.dp(x) for x in self._model], _lib.dp(fz)), "mce_adjoint_forward")
         self.fz = fz
         return fz
 
@@ -117,16 +120,20 @@ class AdjointRun:
 
 
 class AdjointBatch:
-    """Adjoint runs of one LTI model (d states, pncc process-noise columns, p
-    measurements per step) stepped together: run r has steps[r] steps from
+    """Adjoint runs of d states, pncc process-noise columns and p
+    measurements per step, stepped together: run r has steps[r] steps from
     (A0[r], p0[r], b0[r]) with its own rand() constants (root_point[r],
-    b_pert[r]).  One batched handle steps every run (mce_adjoint_batch_*), and
-    the runs' records and reverses spread over the host's cores; each run's
-    gradient is the one an AdjointRun of its own gives."""
+    b_pert[r]); one LTI model for all, or (forward with per-run Phi
+    sequences) a time-varying model per run.  first_sub = p - 1 makes every
+    run a window restarted with the last measurement of its first step.  One
+    batched handle steps every run (mce_adjoint_batch_*), and the runs'
+    records and reverses spread over the host's cores; each run's gradient is
+    the one an AdjointRun of its own gives."""
 
-    def __init__(self, d, pncc, p, steps, A0, p0, b0, root_point, b_pert):
+    def __init__(self, d, pncc, p, steps, A0, p0, b0, root_point, b_pert, first_sub=0):
         self._L = _lib.load()
         self.d, self.pncc, self.p = int(d), int(pncc), int(p)
+        self.first_sub = int(first_sub)
         self.steps = np.ascontiguousarray(np.asarray(steps, dtype=np.int32).reshape(-1))
         self.n = len(self.steps)
         f = lambda a, *sh: np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(self.n, *sh))
@@ -139,9 +146,18 @@ class AdjointBatch:
         if not self._h:
             raise _lib.MceError("mce_adjoint_batch_create failed (%d): %s" % (st.value, _lib.last_error()))
         self.max_steps = int(self.steps.max())
+        if self.first_sub:
+            _lib.check(self._L.mce_adjoint_batch_set_first_sub(self._h, self.first_sub),
+                       "mce_adjoint_batch_set_first_sub")
+
+    def updates(self, r):
+        """Updates of run r: steps[r] * p less the first measurement index."""
+        return int(self.steps[r]) * self.p - self.first_sub
 
     def forward(self, msmts, Phi, Gamma, beta, H, gamma):
-        """msmts: run r's measurements (steps[r]*p values) for every r.
+        """msmts: run r's measurements (steps[r]*p values) for every r.  Phi:
+        one (d, d) matrix for every run, or for a time-varying model run r's
+        Phi of each of its steps (a list of (steps[r], d, d) arrays).
         Returns Re fz of every update of every run (a list of arrays)."""
         stride = self.max_steps * self.p
         M = np.zeros((self.n, stride))
@@ -150,10 +166,27 @@ class AdjointBatch:
             M[r, :len(m)] = m
         f = lambda a: np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(-1))
         fz = np.zeros((self.n, stride))
-        _lib.check(self._L.mce_adjoint_batch_forward(self._h, _lib.dp(M), self.max_steps,
-                                                     *[_lib.dp(f(x)) for x in (Phi, Gamma, beta, H, gamma)],
-                                                     _lib.dp(fz)), "mce_adjoint_batch_forward")
-        return [fz[r, :self.steps[r] * self.p].copy() for r in range(self.n)]
+        ltv = isinstance(Phi, (list, tuple)) or np.asarray(Phi).ndim == 3
+        if ltv:
+            # each run its own Phi sequence, Gamma and H (one of each given
+            # for all runs is repeated)
+            d, n = self.d, self.n
+            Ph = np.zeros((n, self.max_steps, d, d))
+            for r, q in enumerate(Phi):
+                q = np.asarray(q, dtype=np.float64).reshape(-1, d, d)
+                Ph[r, :len(q)] = q
+                Ph[r, len(q):] = q[-1]
+            per = lambda x, sz: (np.stack([np.asarray(v, dtype=np.float64).reshape(-1) for v in x])
+                                 if isinstance(x, (list, tuple)) else
+                                 np.tile(np.asarray(x, dtype=np.float64).reshape(1, -1), (n, 1)))
+            Gamma = per(Gamma, d * self.pncc)
+            H = per(H, self.p * d)
+            fn, Phi = self._L.mce_adjoint_batch_forward_ltv, Ph
+        else:
+            fn = self._L.mce_adjoint_batch_forward
+        _lib.check(fn(self._h, _lib.dp(M), self.max_steps, *[_lib.dp(f(x)) for x in (Phi, Gamma, beta, H, gamma)],
+                      _lib.dp(fz)), "mce_adjoint_batch_forward")
+        return [fz[r, :self.updates(r)].copy() for r in range(self.n)]
 
     def backward(self, ws):
         """ws: run r's seeds (steps[r]*p values) for every r.  Returns a list
@@ -312,6 +345,110 @@ def windowed_log_likelihood(prob, W, root_point, b_pert, p0=None, beta=None, gam
                     continue
                 grad[k] += g[k].reshape(grad[k].shape)
     return {"loglik": L, "grad": grad, "starts": starts, "best": best, "timing_ms": timing}
+
+
+def windowed_log_likelihood_batch(probs, W, root_point, b_pert, beta, gamma, p0, steps=None, checkpoints=None,
+                                  with_grad=True):
+    """Sliding-window log-likelihood of n estimators that share the scales
+    (beta, gamma, p0) and have each their own model (probs[i]: Phi (d, d) or
+    per step (steps, d, d), Gamma, H), measurements (steps, p) and step count
+    steps[i] (at most its measurement count): the sum over estimators, over
+    their steps k < steps[i] and the p updates of step k, of log fz of the
+    update in the window chosen at step k (PySlidingWindowManager's best
+    window), and its gradient with respect to beta, gamma and p0 with the
+    window-boundary checkpoints held fixed.  One window manager runs all n
+    estimators (to their longest step count); every window life of every
+    estimator is recomputed from its checkpoint in two AdjointBatch sets, the
+    first lives (from the initial statistics, where p0 enters) and the
+    restarted ones (which begin with the last measurement of their first
+    step).  The seeds are windowed_log_likelihood's, per update.
+
+    checkpoints: (starts, best) from a first call, to hold them fixed.
+    Returns a dict: loglik, grad (beta, gamma, p0), checkpoints, timing_ms."""
+    from .windows import SlidingWindowManager
+    n = len(probs)
+    d, pncc, p = probs[0]["d"], probs[0]["pncc"], probs[0]["p"]
+    beta = np.asarray(beta, dtype=np.float64).reshape(pncc)
+    gamma = np.asarray(gamma, dtype=np.float64).reshape(p)
+    p0 = np.asarray(p0, dtype=np.float64).reshape(d)
+    steps = [int(q["msmts"].shape[0]) for q in probs] if steps is None else [int(k) for k in steps]
+    K = max(steps)
+    rp = np.asarray(root_point, dtype=np.float64)
+    bp = np.asarray(b_pert, dtype=np.float64)
+    phi = lambda q, k: np.asarray(q["Phi"] if np.asarray(q["Phi"]).ndim == 2 else q["Phi"][k], dtype=np.float64)
+    if checkpoints is None:
+        mgr = SlidingWindowManager(W, np.stack([q["A0"] for q in probs]), np.tile(p0, (n, 1)),
+                                   np.stack([q["b0"] for q in probs]), d, pncc, p,
+                                   root_point=np.repeat(rp[:, None, :], n, axis=1),
+                                   b_pert=np.repeat(bp[:, None, :], n, axis=1))
+        best = []
+        try:
+            for k in range(K):
+                out = mgr.step(np.stack([q["msmts"][k] for q in probs]), np.stack([phi(q, k) for q in probs]),
+                               np.stack([np.asarray(q["Gamma"]).reshape(d, pncc) for q in probs]),
+                               np.tile(beta, (n, 1)), np.stack([np.asarray(q["H"]).reshape(p, d) for q in probs]),
+                               np.tile(gamma, (n, 1)))
+                best.append([o[2] for o in out])
+            starts = [{"slot": s_["slot"], "step": s_["step"], "A0": np.asarray(s_["A0"]), "p0": np.asarray(s_["p0"]),
+                       "b0": np.asarray(s_["b0"])} for s_ in mgr.starts]
+        finally:
+            mgr.close()
+    else:
+        starts, best = checkpoints
+    L = 0.0
+    grad = {"beta": np.zeros(pncc), "gamma": np.zeros(p), "p0": np.zeros(d)}
+    timing = np.zeros(4)
+    for first in (True, False):
+        # the runs: (estimator, life) with the life's first step before the
+        # estimator's step count
+        runs = []
+        for li, st in enumerate(starts):
+            if (li == 0) != first:
+                continue
+            for i in range(n):
+                if st["step"] < steps[i]:
+                    runs.append((i, li, min(W, steps[i] - st["step"])))
+        if not runs:
+            continue
+        fs = 0 if first else p - 1
+        A0 = [starts[li]["A0"][i] for i, li, _ in runs]
+        P0 = [p0 if first else starts[li]["p0"][i] for i, li, _ in runs]
+        B0 = [starts[li]["b0"][i] for i, li, _ in runs]
+        batch = AdjointBatch(d, pncc, p, [m for _, _, m in runs], A0, P0, B0,
+                             [rp[starts[li]["slot"]] for _, li, _ in runs],
+                             [bp[starts[li]["slot"]] for _, li, _ in runs], first_sub=fs)
+        try:
+            ms, Ph, Gs, Hs = [], [], [], []
+            for i, li, m in runs:
+                s0 = starts[li]["step"]
+                z = np.asarray(probs[i]["msmts"][s0:s0 + m], dtype=np.float64).reshape(-1)[fs:]
+                ms.append(z)
+                Ph.append(np.stack([phi(probs[i], s0 + k) for k in range(m)]))
+                Gs.append(probs[i]["Gamma"])
+                Hs.append(probs[i]["H"])
+            fzs = batch.forward(ms, Ph, Gs, beta, Hs, gamma)
+            ws = []
+            for (i, li, m), fz in zip(runs, fzs):
+                s0, slot = starts[li]["step"], starts[li]["slot"]
+                w = np.zeros(len(fz))
+                for u in range(len(fz)):
+                    k = s0 + (u + fs) // p
+                    if best[k][i] == slot:
+                        L += float(np.log(fz[u]))
+                        w[u] += 1.0 / fz[u]
+                        if u >= 1:
+                            w[u - 1] -= 1.0 / fz[u - 1]
+                ws.append(w)
+            if with_grad:
+                for g in batch.backward(ws):
+                    grad["beta"] += g["beta"]
+                    grad["gamma"] += g["gamma"]
+                    if first:
+                        grad["p0"] += g["p0"]
+            timing += batch.timing()
+        finally:
+            batch.close()
+    return {"loglik": L, "grad": grad, "checkpoints": (starts, best), "timing_ms": timing}
 
 
 _FN = None

@@ -956,8 +956,16 @@ struct mce_adjoint {
     mce_handle* h = nullptr;
     int est = 0;          // this run's estimator in h
     bool owns_h = true;   // false for the runs of an mce_adjoint_batch
-    // model (LTI) and measurements of the recorded run
+    // model and measurements of the recorded run; Phi is d x d, or with ltv
+    // one d x d matrix per step (the gradient's Phi entries are then those
+    // of a perturbation common to every step's Phi)
     std::vector<double> Phi, Gamma, beta, H, gamma, msmts;
+    bool ltv = false;
+    // measurement index of the first update (0; p - 1 for a window restarted
+    // with the last measurement of its step, whose master step then jumps to
+    // p): update u is measurement (u + first_sub) % p of step
+    // (u + first_sub) / p, and the run has steps * p - first_sub updates
+    int first_sub = 0;
     std::vector<Update> ups;
     double max_table_err = 0;
     double fz_check_err = 0;
@@ -999,6 +1007,12 @@ struct mce_adjoint {
 };
 
 namespace {
+
+// The Phi of update u's time propagation (of its step, u / p).
+const double* phi_of(const mce_adjoint& o, int u)
+{
+    return o.ltv ? o.Phi.data() + (size_t)((u + o.first_sub) / o.p) * o.d * o.d : o.Phi.data();
+}
 
 // Gamma pre-coalignment (cauchy_util.hpp:128-210): normalised columns as rows
 int precoalign(const mce_adjoint& o, const std::vector<double>& G, const std::vector<double>& beta,
@@ -1133,6 +1147,7 @@ void derive_update(const mce_adjoint& o, const Update& U, const RecSet& parents,
                    std::vector<TermInfo>& info)
 {
     const int d = o.d;
+    const double* Phi = phi_of(o, (int)(&U - &o.ups[0]));
     std::vector<double> Gt, bt;
     int gcnt = 0;
     if (U.with_tp) gcnt = precoalign(o, o.Gamma, o.beta, Gt, bt);
@@ -1161,13 +1176,13 @@ void derive_update(const mce_adjoint& o, const Update& U, const RecSet& parents,
             for (int i = 0; i < tm; i++)
                 for (int j = 0; j < d; j++) {
                     double s = 0.0;
-                    for (int k = 0; k < d; k++) s += w[i * d + k] * o.Phi[k + j * d];
+                    for (int k = 0; k < d; k++) s += w[i * d + k] * Phi[k + j * d];
                     tA[i * d + j] = s;
                 }
             memcpy(wb, tb, sizeof(double) * d);
             for (int i = 0; i < d; i++) {
                 double s = 0.0;
-                for (int j = 0; j < d; j++) s += o.Phi[i * d + j] * wb[j];
+                for (int j = 0; j < d; j++) s += Phi[i * d + j] * wb[j];
                 tb[i] = s;
             }
             // tp_coalign (cauchy_term.hpp:475-531)
@@ -1436,11 +1451,12 @@ int grid_of(long long n) { return (int)std::min<long long>((n + 255) / 256, 152 
 
 // Copies the model and measurements of a run and resets its records.
 int fwd_begin(mce_adjoint* o, const double* msmts, const double* Phi, const double* Gamma, const double* beta,
-              const double* H, const double* gamma)
+              const double* H, const double* gamma, bool ltv = false)
 {
-    const int d = o->d, nup = o->steps * o->p;
+    const int d = o->d, nup = o->steps * o->p - o->first_sub;
     o->msmts.assign(msmts, msmts + nup);
-    o->Phi.assign(Phi, Phi + d * d);
+    o->ltv = ltv;
+    o->Phi.assign(Phi, Phi + (size_t)(ltv ? o->steps : 1) * d * d);
     o->Gamma.assign(Gamma, Gamma + d * o->pncc);
     o->beta.assign(beta, beta + o->pncc);
     o->H.assign(H, H + o->p * d);
@@ -1486,8 +1502,8 @@ int fwd_record(mce_adjoint* o, int u, Workspace& W, double* fz_raw)
     Update& U = o->ups[u];
     U.first = u == 0;
     U.last = u == nup - 1;
-    U.sub = u % o->p;
-    U.with_tp = !U.first && (u % o->p) == 0;
+    U.sub = (u + o->first_sub) % o->p;
+    U.with_tp = !U.first && U.sub == 0;
     struct Lap {
         double* acc;
         std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
@@ -1800,7 +1816,7 @@ int bwd_run(mce_adjoint* o, const double* w, double* grad, Workspace& W)
         ca.beta = W.dpar[0].ptr;
         ca.gamma = W.dpar[1].ptr;
         ca.p0 = W.dpar[2].ptr;
-        ca.Phi = W.dpar[3].ptr;
+        ca.Phi = W.dpar[3].ptr + (o->ltv ? (size_t)((u + o->first_sub) / o->p) * d * d : 0);
         ca.Gamma = W.dpar[4].ptr;
         ca.H = W.dpar[5].ptr;
         ca.A0 = W.dpar[6].ptr;
@@ -1929,26 +1945,38 @@ mce_adjoint* mce_adjoint_create(int d, int pncc, int p, int steps, const double*
     return o.release();
 }
 
-int mce_adjoint_forward(mce_adjoint* o, const double* msmts, const double* Phi, const double* Gamma,
-                        const double* beta, const double* H, const double* gamma, double* fz_raw)
+static int forward_run(mce_adjoint* o, const double* msmts, const double* Phi, const double* Gamma,
+                       const double* beta, const double* H, const double* gamma, double* fz_raw, bool ltv)
 {
     if (!o || !msmts || !Phi || !Gamma || !beta || !H || !gamma) return MCE_ERR_ARG;
     int st;
     if (!o->ws) o->ws.reset(new Workspace());
     if ((st = o->ws->init())) return st;
     o->ws->owner = nullptr;
-    if ((st = fwd_begin(o, msmts, Phi, Gamma, beta, H, gamma))) return st;
+    if ((st = fwd_begin(o, msmts, Phi, Gamma, beta, H, gamma, ltv))) return st;
     if ((st = mce_reset(o->h)) < 0) return st;
     const int d = o->d, nup = (int)o->ups.size();
     for (int u = 0; u < nup; u++) {
         const int sub = u % o->p;
         auto t0 = std::chrono::steady_clock::now();
-        st = mce_step(o->h, msmts[u], Phi, Gamma, beta, H + (size_t)sub * d, gamma[sub], nullptr, nullptr);
+        st = mce_step(o->h, msmts[u], phi_of(*o, u), Gamma, beta, H + (size_t)sub * d, gamma[sub], nullptr, nullptr);
         if (st < 0) return st;
         o->ms[0] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         if ((st = fwd_record(o, u, *o->ws, fz_raw))) return st;
     }
     return MCE_OK;
+}
+
+int mce_adjoint_forward(mce_adjoint* o, const double* msmts, const double* Phi, const double* Gamma,
+                        const double* beta, const double* H, const double* gamma, double* fz_raw)
+{
+    return forward_run(o, msmts, Phi, Gamma, beta, H, gamma, fz_raw, false);
+}
+
+int mce_adjoint_forward_ltv(mce_adjoint* o, const double* msmts, const double* Phis, const double* Gamma,
+                            const double* beta, const double* H, const double* gamma, double* fz_raw)
+{
+    return forward_run(o, msmts, Phis, Gamma, beta, H, gamma, fz_raw, true);
 }
 
 int mce_adjoint_check(mce_adjoint* o, double* max_table_rel_err, double* max_fz_rel_err)
@@ -2042,37 +2070,64 @@ mce_adjoint_batch* mce_adjoint_batch_create(int n_runs, int d, int pncc, int p, 
     return b.release();
 }
 
-int mce_adjoint_batch_forward(mce_adjoint_batch* b, const double* msmts, int max_steps, const double* Phi,
-                              const double* Gamma, const double* beta, const double* H, const double* gamma,
-                              double* fz_raw)
+static int batch_forward(mce_adjoint_batch* b, const double* msmts, int max_steps, const double* Phi,
+                         const double* Gamma, const double* beta, const double* H, const double* gamma, double* fz_raw,
+                         bool ltv)
 {
     if (!b || !msmts || !Phi || !Gamma || !beta || !H || !gamma || max_steps < 1) return MCE_ERR_ARG;
-    const int n = b->n, d = b->d, p = b->p, stride = max_steps * p;
+    const int n = b->n, d = b->d, p = b->p, pncc = b->pncc, stride = max_steps * p;
     int st, max_up = 0;
+    // a time-varying batch carries each run's own Phi sequence, Gamma and H
+    auto Gam_of = [&](int r) { return ltv ? Gamma + (size_t)r * d * pncc : Gamma; };
+    auto H_of = [&](int r) { return ltv ? H + (size_t)r * p * d : H; };
     for (int r = 0; r < n; r++) {
         mce_adjoint* o = b->runs[r].get();
         if (o->steps > max_steps) return MCE_ERR_ARG;
-        if ((st = fwd_begin(o, msmts + (size_t)r * stride, Phi, Gamma, beta, H, gamma))) return st;
+        const double* Ph = ltv ? Phi + (size_t)r * max_steps * d * d : Phi;
+        if ((st = fwd_begin(o, msmts + (size_t)r * stride, Ph, Gam_of(r), beta, H_of(r), gamma, ltv))) return st;
         max_up = std::max(max_up, (int)o->ups.size());
     }
     for (auto& w : b->ws) w->owner = nullptr;
     if (fz_raw) std::fill(fz_raw, fz_raw + (size_t)n * stride, 0.0);
     if ((st = mce_reset(b->h)) < 0) return st;
     std::vector<double> z(n), Hr((size_t)n * d), gam(n);
+    // a time-varying batch is stepped with per-estimator model arrays: each
+    // run's Phi of its own step and its Gamma, beta repeated
+    std::vector<double> Phb, Gb, bb;
+    if (ltv) {
+        Phb.assign((size_t)n * d * d, 0.0);
+        Gb.assign((size_t)n * d * pncc, 0.0);
+        bb.assign((size_t)n * pncc, 0.0);
+        for (int r = 0; r < n; r++) {
+            std::copy(Gam_of(r), Gam_of(r) + d * pncc, Gb.begin() + (size_t)r * d * pncc);
+            std::copy(beta, beta + pncc, bb.begin() + (size_t)r * pncc);
+        }
+    }
     std::vector<int> act;
+    const int fsub = b->runs[0]->first_sub;
     for (int u = 0; u < max_up; u++) {
-        const int sub = u % p;
+        const int sub = (u + fsub) % p;
         act.clear();
         for (int r = 0; r < n; r++) {
-            const bool on = u < (int)b->runs[r]->ups.size();
+            const mce_adjoint* o = b->runs[r].get();
+            const bool on = u < (int)o->ups.size();
             z[r] = on ? msmts[(size_t)r * stride + u] : 0.0;
-            for (int j = 0; j < d; j++) Hr[(size_t)r * d + j] = H[(size_t)sub * d + j];
+            for (int j = 0; j < d; j++) Hr[(size_t)r * d + j] = H_of(r)[(size_t)sub * d + j];
             gam[r] = gamma[sub];
+            if (ltv) {
+                const double* Ph = phi_of(*o, on ? u : (int)o->ups.size() - 1);
+                std::copy(Ph, Ph + d * d, Phb.begin() + (size_t)r * d * d);
+            }
             if (on) act.push_back(r);
         }
         auto t0 = std::chrono::steady_clock::now();
-        st = mce_batch_step(b->h, z.data(), Phi, Gamma, beta, Hr.data(), gam.data(), nullptr, nullptr, 1, nullptr);
+        st = ltv ? mce_batch_step(b->h, z.data(), Phb.data(), Gb.data(), bb.data(), Hr.data(), gam.data(), nullptr,
+                                  nullptr, 0, nullptr)
+                 : mce_batch_step(b->h, z.data(), Phi, Gamma, beta, Hr.data(), gam.data(), nullptr, nullptr, 1,
+                                  nullptr);
         if (st < 0) return st;
+        // a restarted window's master step jumps to p after its first update
+        if (u == 0 && fsub > 0 && (st = mce_set_master_step(b->h, p)) < 0) return st;
         auto t1 = std::chrono::steady_clock::now();
         st = parallel_runs((int)act.size(), b->threads, b->dev, [&](int i, int w) {
             const int r = act[i];
@@ -2084,6 +2139,20 @@ int mce_adjoint_batch_forward(mce_adjoint_batch* b, const double* msmts, int max
         b->ms[1] += std::chrono::duration<double, std::milli>(t2 - t1).count();
     }
     return MCE_OK;
+}
+
+int mce_adjoint_batch_forward(mce_adjoint_batch* b, const double* msmts, int max_steps, const double* Phi,
+                              const double* Gamma, const double* beta, const double* H, const double* gamma,
+                              double* fz_raw)
+{
+    return batch_forward(b, msmts, max_steps, Phi, Gamma, beta, H, gamma, fz_raw, false);
+}
+
+int mce_adjoint_batch_forward_ltv(mce_adjoint_batch* b, const double* msmts, int max_steps, const double* Phis,
+                                  const double* Gamma, const double* beta, const double* H, const double* gamma,
+                                  double* fz_raw)
+{
+    return batch_forward(b, msmts, max_steps, Phis, Gamma, beta, H, gamma, fz_raw, true);
 }
 
 int mce_adjoint_batch_backward(mce_adjoint_batch* b, const double* w, int max_steps, double* grad)
@@ -2104,6 +2173,16 @@ int mce_adjoint_batch_backward(mce_adjoint_batch* b, const double* w, int max_st
     });
     b->ms[2] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return st;
+}
+
+int mce_adjoint_batch_set_first_sub(mce_adjoint_batch* b, int first_sub)
+{
+    if (!b || first_sub < 0 || first_sub >= b->p) return MCE_ERR_ARG;
+    for (auto& o : b->runs) {
+        o->first_sub = first_sub;
+        o->ups.clear();
+    }
+    return MCE_OK;
 }
 
 int mce_adjoint_batch_num_params(mce_adjoint_batch* b)

@@ -377,6 +377,11 @@ mce_adjoint* mce_adjoint_create(int d, int pncc, int p, int steps, const double*
                                 const double* b0, const double* root_point, const double* b_pert, int* status);
 int mce_adjoint_forward(mce_adjoint* a, const double* msmts, const double* Phi, const double* Gamma,
                         const double* beta, const double* H, const double* gamma, double* fz_raw);
+/* mce_adjoint_forward for a time-varying model: Phis[steps*d*d], the Phi of
+ * every step (step k's time propagation uses Phis[k]); the gradient's Phi
+ * entries are then those of a perturbation common to every step's Phi. */
+int mce_adjoint_forward_ltv(mce_adjoint* a, const double* msmts, const double* Phis, const double* Gamma,
+                            const double* beta, const double* H, const double* gamma, double* fz_raw);
 int mce_adjoint_num_params(mce_adjoint* a);
 int mce_adjoint_backward(mce_adjoint* a, const double* w, double* grad);
 int mce_adjoint_check(mce_adjoint* a, double* max_table_rel_err, double* max_fz_rel_err);
@@ -407,7 +412,22 @@ mce_adjoint_batch* mce_adjoint_batch_create(int n_runs, int d, int pncc, int p, 
 int mce_adjoint_batch_forward(mce_adjoint_batch* b, const double* msmts, int max_steps, const double* Phi,
                               const double* Gamma, const double* beta, const double* H, const double* gamma,
                               double* fz_raw);
+/* mce_adjoint_batch_forward for time-varying models, each run its own:
+ * Phis[n_runs*max_steps*d*d] (run r's Phi of its step k at
+ * (r*max_steps + k)*d*d), Gammas[n_runs*d*pncc], Hs[n_runs*p*d]; beta and
+ * gamma are shared.  Each run's gradient is with respect to its own Phi
+ * (a perturbation common to its steps), Gamma and H, and the shared scales. */
+int mce_adjoint_batch_forward_ltv(mce_adjoint_batch* b, const double* msmts, int max_steps, const double* Phis,
+                                  const double* Gammas, const double* beta, const double* Hs, const double* gamma,
+                                  double* fz_raw);
 int mce_adjoint_batch_backward(mce_adjoint_batch* b, const double* w, int max_steps, double* grad);
+/* Every run of the batch starts with measurement first_sub of its first
+ * step (0 by default): a sliding window restarted with the last measurement
+ * of a step (first_sub = p - 1) runs that one update, then its master step
+ * jumps to p (pycauchy_single_step_set_master_step), so its steps[r] steps
+ * are steps[r] * p - first_sub updates; msmts, fz_raw and w hold them from
+ * the run's offset on.  Clears the recorded runs. */
+int mce_adjoint_batch_set_first_sub(mce_adjoint_batch* b, int first_sub);
 int mce_adjoint_batch_num_params(mce_adjoint_batch* b);
 int mce_adjoint_batch_check(mce_adjoint_batch* b, double* max_table_rel_err, double* max_fz_rel_err);
 int mce_adjoint_batch_timing(mce_adjoint_batch* b, double* ms4);

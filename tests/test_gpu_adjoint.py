@@ -205,3 +205,74 @@ def test_batch_runs_match_their_own_runs():
             assert np.allclose(_flat(gb[r]), g, rtol=1e-12, atol=1e-12 * np.max(np.abs(g))), r
         run.close()
     batch.close()
+
+
+def test_adjoint_of_records_above_sixteen_rows():
+    """A 3-state run with seven process-noise columns over 3 steps (records
+    of 17 hyperplanes, 684 terms: the record chain's 32-row instantiation)
+    against central differences of the GPU forward run."""
+    _need_gpu()
+    import oracle
+    from cauchyfriendly_gb300 import workloads as W
+    from cauchyfriendly_gb300.adjoint import loglik_weights
+    prob = W.many_gamma(3, 7, 3, seed=1)
+    assert oracle.max_shape_of(prob) > 16
+    rp, bp = oracle.draw_reference_constants(78, 3, oracle.max_shape_of(prob))
+    z = dict(prob)
+    z["root_point"], z["b_pert"] = rp, bp
+    run = _run(z)
+    P = _params(z)
+    L, fz = _loglik(run, z, P)
+    assert np.isfinite(L)
+    te, fe = run.check()
+    assert te <= 1e-12 and fe <= 1e-12, (te, fe)
+    g = run.backward(loglik_weights(fz))
+    fd = {}
+    for n in NAMES:
+        a = P[n]
+        fd[n] = np.zeros_like(a)
+        for idx in np.ndindex(a.shape):
+            h = 1e-6 * max(abs(a[idx]), 1e-3)
+            Pp = {k: v.copy() for k, v in P.items()}
+            Pm = {k: v.copy() for k, v in P.items()}
+            Pp[n][idx] += h
+            Pm[n][idx] -= h
+            fd[n][idx] = (_loglik(run, z, Pp)[0] - _loglik(run, z, Pm)[0]) / (2 * h)
+    ok, err = _close(_flat(g), _flat(fd))
+    assert ok, err
+    run.close()
+
+
+def test_batched_windowed_gradient_of_time_varying_models():
+    """windowed_log_likelihood_batch: two 3-state LTV estimators (two
+    process-noise columns, two measurements per step, each its own model and
+    step count), window 2, sharing (beta, gamma, p0): the gradient with the
+    window checkpoints held fixed against central differences of the same
+    objective, on every shared scale."""
+    _need_gpu()
+    import oracle
+    from cauchyfriendly_gb300 import workloads as W
+    from cauchyfriendly_gb300.adjoint import windowed_log_likelihood_batch
+    probs = [W.ltv_windows(3, seed=s, steps=6) for s in (21, 22)]
+    Wn = 2
+    ms = oracle.max_shape_of({"steps": Wn, "d": 3, "pncc": 2})
+    cs = [oracle.draw_reference_constants(90 + w, 3, ms) for w in range(Wn)]
+    rp = np.stack([c[0] for c in cs])
+    bp = np.stack([c[1] for c in cs])
+    beta, gamma, p0 = probs[0]["beta"], probs[0]["gamma"], probs[0]["p0"]
+    res = windowed_log_likelihood_batch(probs, Wn, rp, bp, beta, gamma, p0, steps=[6, 5])
+    assert np.isfinite(res["loglik"])
+    scales = {"beta": beta, "gamma": gamma, "p0": p0}
+    for name, base in scales.items():
+        for idx in range(len(base)):
+            h = 1e-6 * max(abs(base[idx]), 1e-3)
+            vals = []
+            for sgn in (1, -1):
+                sc = {k: np.array(v, dtype=np.float64) for k, v in scales.items()}
+                sc[name][idx] += sgn * h
+                r = windowed_log_likelihood_batch(probs, Wn, rp, bp, sc["beta"], sc["gamma"], sc["p0"], steps=[6, 5],
+                                                  checkpoints=res["checkpoints"], with_grad=False)
+                vals.append(r["loglik"])
+            fd = (vals[0] - vals[1]) / (2 * h)
+            g = res["grad"][name][idx]
+            assert abs(g - fd) <= 1e-4 * abs(fd) + 1e-6, (name, idx, g, fd)
