@@ -56,12 +56,15 @@ def parse():
     ap.add_argument("--plain-stride", type=int, default=16)
     ap.add_argument("--adjoint-steps", type=int, default=100)
     ap.add_argument("--workload", default="batched3",
-                    choices=["batched3", "windows5", "rel2d", "adjoint", "cpdfnd", "window7"],
+                    choices=["batched3", "windows5", "rel2d", "adjoint", "cpdfnd", "window7", "mle"],
                     help="batched3: the batched 3-state configuration (default); windows5: the sliding-window "
                          "5-state LTV configuration for --window-steps steps; rel2d: the relative 2-D system of "
                          "two 5-state estimators; cpdfnd: the N-D conditional pdf of a 4-state estimator at "
                          "--nd-points points; window7: one window of the 7-state LTV model (window 8, two "
-                         "measurements per step) as far as its g-tables stay below --max-cells cells")
+                         "measurements per step) as far as its g-tables stay below --max-cells cells; mle: "
+                         "maximum-likelihood tuning of the shared scales of --mle-estimators LTV sliding-window "
+                         "estimators of --mle-states states (window --mle-window) with Adam on batched adjoint "
+                         "gradients")
     ap.add_argument("--nd-points", type=int, default=256)
     ap.add_argument("--window-steps", type=int, default=12)
     ap.add_argument("--rel-updates", type=int, default=6, help="rel2d: updates of both estimators (6: 12.2 M pairs)")
@@ -69,6 +72,10 @@ def parse():
                     help="window7: stop before an update whose g-table cells, projected by the largest growth "
                          "seen so far, would pass this")
     ap.add_argument("--cpu-updates", type=int, default=6, help="window7: updates the CPU baseline runs")
+    ap.add_argument("--mle-estimators", type=int, default=64)
+    ap.add_argument("--mle-states", type=int, default=3)
+    ap.add_argument("--mle-window", type=int, default=3)
+    ap.add_argument("--mle-iters", type=int, default=4, help="mle: Adam iterations (the configuration's is 50)")
     return ap.parse_args()
 
 
@@ -860,6 +867,80 @@ def run_window7(args):
     print(json.dumps(line), flush=True)
 
 
+def run_mle(args):
+    """Maximum-likelihood tuning of log(beta), log(gamma) and log(p0) shared
+    by --mle-estimators LTV sliding-window estimators of --mle-states states
+    (workloads.ltv_windows, seeds 0..n-1, each its own model and
+    measurements; Gamma d x 2, H 2 x d, two measurements per step), step
+    counts uniform in 100..150, window --mle-window, with Adam (lr 0.05) on
+    the gradient of the summed sliding-window log-likelihood
+    (adjoint.windowed_log_likelihood_batch: one window manager for all
+    estimators, every window life recomputed in batched adjoint runs),
+    starting from the generating scales times 3.  This is the batched 7-state
+    configuration's pipeline; at 7 states a window short enough to
+    recompute (at most 3 steps, 6 measurements) leaves the windows without a
+    covariance (the manager finds no usable window and stops, as the
+    reference's does), and a window of 8 does not fit in the GPU's memory
+    (--workload window7), so it runs at --mle-states.  Short windows meet
+    steps where every window of a manager has an error code (the reference
+    exits there); the manager takes the fullest window then and counts the
+    steps (no_window_steps per iteration).  value: gradients/s (each
+    gradient covers every estimator); the log-likelihood and scales per
+    iteration."""
+    import torch
+    from cauchyfriendly_gb300 import workloads as W
+    from cauchyfriendly_gb300.adjoint import windowed_log_likelihood_batch
+    import oracle
+    torch.cuda.set_device(0)
+    n, Wn, dd = args.mle_estimators, args.mle_window, args.mle_states
+    rng = np.random.Generator(np.random.PCG64(args.seed + 7))
+    steps = [int(k) for k in rng.integers(100, 151, size=n)]
+    probs = [W.ltv_windows(dd, seed=args.seed + i, steps=150) for i in range(n)]
+    ms = oracle.max_shape_of({"steps": Wn, "d": dd, "pncc": 2})
+    cs = [oracle.draw_reference_constants(700 + w, dd, ms) for w in range(Wn)]
+    rp = np.stack([c[0] for c in cs])
+    bp = np.stack([c[1] for c in cs])
+    true = {"beta": probs[0]["beta"], "gamma": probs[0]["gamma"], "p0": probs[0]["p0"]}
+    theta = {k: torch.tensor(np.log(3.0 * np.asarray(v)), dtype=torch.float64, requires_grad=True)
+             for k, v in true.items()}
+    opt = torch.optim.Adam(list(theta.values()), lr=0.05)
+    hist, tg = [], []
+    stopped = None
+    for it in range(args.mle_iters):
+        sc = {k: np.exp(v.detach().numpy()) for k, v in theta.items()}
+        t0 = time.perf_counter()
+        try:
+            r = windowed_log_likelihood_batch(probs, Wn, rp, bp, sc["beta"], sc["gamma"], sc["p0"], steps=steps,
+                                              no_window="fullest")
+        except RuntimeError as e:
+            stopped = "iteration %d: %s" % (it, e)
+            break
+        tg.append(time.perf_counter() - t0)
+        opt.zero_grad()
+        for k, v in theta.items():
+            # maximise the log-likelihood: minimise its negative; d/dlog s = s d/ds
+            v.grad = torch.as_tensor(-sc[k] * r["grad"][k], dtype=torch.float64)
+        opt.step()
+        hist.append({"iter": it, "loglik": r["loglik"], "seconds": round(tg[-1], 3),
+                     "no_window_steps": int(r["no_window_steps"]),
+                     "beta": [float(x) for x in sc["beta"]], "gamma": [float(x) for x in sc["gamma"]],
+                     "p0_mean": float(np.mean(sc["p0"]))})
+        print(json.dumps(hist[-1]), file=sys.stderr, flush=True)
+    timed = tg[1:] if len(tg) > 1 else tg
+    g_s = float(np.mean(timed)) if timed else float("nan")
+    line = {"metric": "MCE log-likelihood gradients/s (1 GB300, FP64; batched sliding-window adjoint)",
+            "value": 1.0 / g_s, "unit": "gradients/s", "n_gpus": 1, "steps": len(timed), "warmup": len(tg) - len(timed),
+            "ms_per_step": 1e3 * g_s, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "%d x %d-state LTV sliding-window MCE, window %d, 2 msmts/step, steps U{100..150}, "
+                                   "Adam on log(beta, gamma, p0)" % (n, dd, Wn),
+                       "estimators": n, "states": dd, "window": Wn, "iterations": args.mle_iters,
+                       "estimator_steps": int(sum(steps))},
+            "iterations": hist, "stopped": stopped,
+            "true_scales": {k: [float(x) for x in np.asarray(v).reshape(-1)] for k, v in true.items()}}
+    print(json.dumps(line), flush=True)
+
+
 def autotune_summary(table, passes, off):
     """The autotuner's settled block sizes per kernel as {log2 items: block}."""
     if off:
@@ -889,6 +970,9 @@ def main():
         return
     if args.workload == "window7":
         run_window7(args)
+        return
+    if args.workload == "mle":
+        run_mle(args)
         return
     import torch
     rank = int(os.environ.get("RANK", "0"))

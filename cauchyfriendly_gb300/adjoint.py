@@ -348,7 +348,7 @@ def windowed_log_likelihood(prob, W, root_point, b_pert, p0=None, beta=None, gam
 
 
 def windowed_log_likelihood_batch(probs, W, root_point, b_pert, beta, gamma, p0, steps=None, checkpoints=None,
-                                  with_grad=True):
+                                  with_grad=True, no_window="raise"):
     """Sliding-window log-likelihood of n estimators that share the scales
     (beta, gamma, p0) and have each their own model (probs[i]: Phi (d, d) or
     per step (steps, d, d), Gamma, H), measurements (steps, p) and step count
@@ -364,7 +364,10 @@ def windowed_log_likelihood_batch(probs, W, root_point, b_pert, beta, gamma, p0,
     step).  The seeds are windowed_log_likelihood's, per update.
 
     checkpoints: (starts, best) from a first call, to hold them fixed.
-    Returns a dict: loglik, grad (beta, gamma, p0), checkpoints, timing_ms."""
+    no_window: the manager's rule for a step where every window has an error
+    code (SlidingWindowManager: "raise" as the reference, or "fullest").
+    Returns a dict: loglik, grad (beta, gamma, p0), checkpoints, timing_ms,
+    no_window_steps."""
     from .windows import SlidingWindowManager
     n = len(probs)
     d, pncc, p = probs[0]["d"], probs[0]["pncc"], probs[0]["p"]
@@ -380,7 +383,7 @@ def windowed_log_likelihood_batch(probs, W, root_point, b_pert, beta, gamma, p0,
         mgr = SlidingWindowManager(W, np.stack([q["A0"] for q in probs]), np.tile(p0, (n, 1)),
                                    np.stack([q["b0"] for q in probs]), d, pncc, p,
                                    root_point=np.repeat(rp[:, None, :], n, axis=1),
-                                   b_pert=np.repeat(bp[:, None, :], n, axis=1))
+                                   b_pert=np.repeat(bp[:, None, :], n, axis=1), no_window=no_window)
         best = []
         try:
             for k in range(K):
@@ -391,10 +394,12 @@ def windowed_log_likelihood_batch(probs, W, root_point, b_pert, beta, gamma, p0,
                 best.append([o[2] for o in out])
             starts = [{"slot": s_["slot"], "step": s_["step"], "A0": np.asarray(s_["A0"]), "p0": np.asarray(s_["p0"]),
                        "b0": np.asarray(s_["b0"])} for s_ in mgr.starts]
+            no_window_steps = mgr.no_window_steps
         finally:
             mgr.close()
     else:
         starts, best = checkpoints
+        no_window_steps = 0
     L = 0.0
     grad = {"beta": np.zeros(pncc), "gamma": np.zeros(p), "p0": np.zeros(d)}
     timing = np.zeros(4)
@@ -448,7 +453,8 @@ def windowed_log_likelihood_batch(probs, W, root_point, b_pert, beta, gamma, p0,
             timing += batch.timing()
         finally:
             batch.close()
-    return {"loglik": L, "grad": grad, "checkpoints": (starts, best), "timing_ms": timing}
+    return {"loglik": L, "grad": grad, "checkpoints": (starts, best), "timing_ms": timing,
+            "no_window_steps": no_window_steps}
 
 
 _FN = None

@@ -124,8 +124,14 @@ class SlidingWindowManager:
     """
 
     def __init__(self, num_windows, A0, p0, b0, d, pncc, p, cmcc=0, slot_factory=None, root_point=None,
-                 b_pert=None):
+                 b_pert=None, no_window="raise"):
         assert num_windows >= 2
+        # a step where every window of a manager has an error code: "raise"
+        # as the reference does (it exits), or "fullest": take the fullest
+        # window anyway and count the step in no_window_steps
+        assert no_window in ("raise", "fullest")
+        self.no_window = no_window
+        self.no_window_steps = 0
         self.W = int(num_windows)
         self.d, self.pncc, self.p, self.cmcc = int(d), int(pncc), int(p), int(cmcc)
         A0 = np.asarray(A0, dtype=np.float64)
@@ -176,7 +182,10 @@ class SlidingWindowManager:
                 okay[m, 0] = True
                 continue
             if not cands:
-                raise RuntimeError("no window is available without an error code (manager %d)" % m)
+                if self.no_window == "raise":
+                    raise RuntimeError("no window is available without an error code (manager %d)" % m)
+                cands = [(w, self.win_counts[w]) for w in range(self.W) if self.win_counts[w] > 0]
+                self.no_window_steps += 1
             best[m] = list(reversed(sorted(cands, key=lambda x: x[1])))[0][0]
         return best, okay
 
