@@ -4,6 +4,7 @@ oracle estimators (no GPU)."""
 import os
 
 import numpy as np
+import pytest
 
 import oracle
 from cauchyfriendly_gb300 import windows, workloads as W
@@ -97,3 +98,46 @@ def test_window_bookkeeping_with_oracle_estimators():
     for c in seen_counts[Wn:]:
         assert sorted(c.tolist()) == list(range(Wn))
     mgr.close()
+
+
+def test_window_manager_without_a_usable_window():
+    """A step at which every window of a manager carries a covariance error
+    code: the manager raises, as the reference exits
+    (cauchy_estimator.py:1181-1216), unless built with no_window="fullest",
+    which takes the fullest window and counts the step.  The slots are
+    oracle estimators whose error codes are forced on from the third step."""
+    oracle.build(with_reference=False)
+    Wn, steps, n, d = 3, 6, 1, 4
+    probs = [W.four_state_lti(seed=s, steps=steps) for s in range(n)]
+    ms = oracle.max_shape_of({"steps": Wn, "d": d, "pncc": 1})
+    consts = [oracle.draw_reference_constants(7 + m, d, ms) for m in range(n)]
+
+    class Forced(oracle.OracleSlot):
+        step_no = [0]
+
+        def errors(self, i):
+            return (windows.COV_UNSTABLE if self.step_no[0] >= 3 else 0) | super().errors(i)
+
+    def run(rule):
+        Forced.step_no[0] = 0
+        factory = lambda A0_, p0_, b0_, st_, d_, cm_, pn_, p_: Forced(A0_, p0_, b0_, st_, d_, cm_, pn_, p_, consts)
+        mgr = windows.SlidingWindowManager(Wn, np.stack([p["A0"] for p in probs]), np.stack([p["p0"] for p in probs]),
+                                           np.stack([p["b0"] for p in probs]), d, 1, 1, slot_factory=factory,
+                                           no_window=rule)
+        try:
+            for k in range(steps):
+                Forced.step_no[0] = k
+                counts = mgr.win_counts.copy()
+                out = mgr.step(np.stack([p["msmts"][k] for p in probs]), np.stack([p["Phi"] for p in probs]),
+                               np.stack([p["Gamma"] for p in probs]), np.stack([p["beta"] for p in probs]),
+                               np.stack([p["H"] for p in probs]), np.stack([p["gamma"] for p in probs]))
+                if k >= 3:
+                    # the fullest window of the step (each stepped window's count grew by one)
+                    assert counts[out[0][2]] == max(counts)
+            return mgr.no_window_steps
+        finally:
+            mgr.close()
+
+    with pytest.raises(RuntimeError):
+        run("raise")
+    assert run("fullest") == steps - 3
