@@ -181,12 +181,15 @@ class SlidingWindowManager:
             if self.step_idx == 0:
                 okay[m, 0] = True
                 continue
-            if not cands:
+            forced = not cands
+            if forced:
                 if self.no_window == "raise":
                     raise RuntimeError("no window is available without an error code (manager %d)" % m)
                 cands = [(w, self.win_counts[w]) for w in range(self.W) if self.win_counts[w] > 0]
                 self.no_window_steps += 1
             best[m] = list(reversed(sorted(cands, key=lambda x: x[1])))[0][0]
+            if forced:
+                okay[m, best[m]] = True  # the weighted average is then that window's estimate
         return best, okay
 
     def _weighted_average(self, m, okay, moms):
