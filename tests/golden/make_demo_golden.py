@@ -3,7 +3,8 @@
 The reference ships no expected outputs for this path, but its demo program
 src/cauchy_estimator.cpp holds fixed problems with fixed measurement
 sequences (test_cauchy_2_state_moshe, _3_state_, _4_state_, _5_state_,
-_3_state_moshe_3msmts, _four_state_two_pnoise, _4_state_2_msmts_moshe).
+_3_state_moshe_3msmts, _four_state_two_pnoise, _4_state_2_msmts_moshe,
+test_no_proc_noise: no process noise, 30 steps).
 This script reads each demo's arrays (Phi, Gamma, H, beta, gamma, A0, p0, b0,
 zs) and sizes (n, cmcc, pncc, p, steps) out of that file's text, runs the
 reference estimator on them through oracle/ref_harness.cpp (serial build,
@@ -34,6 +35,8 @@ DEMOS = [
     ("demo_four_state_two_pnoise", "test_cauchy_four_state_two_pnoise", 305),
     ("demo_four_state_two_msmts", "test_cauchy_4_state_2_msmts_moshe", 306),
     ("demo_five_state_moshe", "test_cauchy_5_state_moshe", 307),
+    # srand(10) before the constructor, as the demo seeds it
+    ("demo_no_process_noise", "test_no_proc_noise", 10),
 ]
 
 
@@ -64,6 +67,8 @@ def _ints(body):
     out = {}
     for name in ("n", "cmcc", "pncc", "p", "steps"):
         m = re.search(r"const int %s\s*=\s*(\d+)\s*;" % name, body)
+        if m is None and name == "steps":  # test_no_proc_noise: int num_steps = 30;
+            m = re.search(r"int num_steps\s*=\s*(\d+)\s*;", body)
         out[name] = int(m.group(1))
     return out
 
@@ -83,9 +88,10 @@ def problem(src, fname):
     prob = {
         "d": n, "pncc": pncc, "cmcc": k["cmcc"], "p": p, "steps": steps, "B": None,
         "Phi": _array(body, "Phi", n * n).reshape(n, n),
-        "Gamma": _array(body, "Gamma", n * pncc).reshape(n, pncc),
+        # no process noise: Gamma and beta are NULL pointers in the demo
+        "Gamma": _array(body, "Gamma", n * pncc).reshape(n, pncc) if pncc else np.zeros((n, 0)),
         "H": _array(body, "H", p * n).reshape(p, n),
-        "beta": _array(body, "beta", pncc),
+        "beta": _array(body, "beta", pncc) if pncc else np.zeros(0),
         "gamma": _array(body, "gamma", p),
         "A0": _array(body, "A0", n * n).reshape(n, n),
         "p0": _array(body, "p0", n),
