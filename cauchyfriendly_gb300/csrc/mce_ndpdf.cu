@@ -52,10 +52,12 @@ struct NdBuf {
     int ensure(size_t n)
     {
         if (n <= cap && ptr) return MCE_OK;
+        // half again as large as the last size, so that a sequence of calls
+        // growing a little at a time does not reallocate at every call
+        const size_t want = std::max<size_t>(std::max(n, cap + cap / 2), 64);
         if (ptr) cudaFree(ptr);
         ptr = nullptr;
         cap = 0;
-        const size_t want = std::max<size_t>(std::max(n, cap + cap / 2), 64);
         if (cudaMalloc(&ptr, want * sizeof(T)) != cudaSuccess) {
             cudaGetLastError();
             report_error("cudaMalloc of " + std::to_string(want * sizeof(T)) + " bytes failed (N-D pdf)");

@@ -276,3 +276,46 @@ def test_batched_windowed_gradient_of_time_varying_models():
             fd = (vals[0] - vals[1]) / (2 * h)
             g = res["grad"][name][idx]
             assert abs(g - fd) <= 1e-4 * abs(fd) + 1e-6, (name, idx, g, fd)
+
+
+def test_adjoint_of_a_time_varying_model():
+    """AdjointRun with a Phi per step (a 3-state LTV model, two process-noise
+    columns, two measurements per step, 3 steps): the gradient with respect
+    to (beta, gamma, p0, a perturbation common to every step's Phi, Gamma,
+    H) against central differences of the GPU forward run."""
+    _need_gpu()
+    import oracle
+    from cauchyfriendly_gb300 import workloads as W
+    from cauchyfriendly_gb300.adjoint import loglik_weights
+    prob = W.ltv_windows(3, seed=31, steps=3)
+    assert prob["Phi"].ndim == 3
+    rp, bp = oracle.draw_reference_constants(79, 3, oracle.max_shape_of(prob))
+    z = dict(prob)
+    z["root_point"], z["b_pert"] = rp, bp
+    run = _run(z)
+    P = _params(z)
+    L, fz = _loglik(run, z, P)
+    te, fe = run.check()
+    assert te <= 1e-12 and fe <= 1e-12, (te, fe)
+    g = run.backward(loglik_weights(fz))
+    assert g["Phi"].shape == (3, 3)
+    fd = {}
+    for n in NAMES:
+        a = P[n]
+        shape = a.shape[1:] if n == "Phi" else a.shape
+        fd[n] = np.zeros(shape)
+        for idx in np.ndindex(shape):
+            ref = a[(0,) + idx] if n == "Phi" else a[idx]
+            h = 1e-6 * max(abs(ref), 1e-3)
+            vals = []
+            for sgn in (1, -1):
+                Q = {k: v.copy() for k, v in P.items()}
+                if n == "Phi":
+                    Q[n][(slice(None),) + idx] += sgn * h  # every step's Phi
+                else:
+                    Q[n][idx] += sgn * h
+                vals.append(_loglik(run, z, Q)[0])
+            fd[n][idx] = (vals[0] - vals[1]) / (2 * h)
+    ok, err = _close(_flat(g), _flat(fd))
+    assert ok, err
+    run.close()
