@@ -353,6 +353,33 @@ __device__ inline double cond1_from_lu(const double* A, const int* P, double nrm
     return nrm * inrm;
 }
 
+// cond1_from_lu(A, P, nrm) > eps, stopping at the first inverse column whose
+// 1-norm s already gives nrm * s > eps: the full value is nrm times the
+// largest column norm, and rounding is monotone, so that column settles the
+// comparison exactly as the full computation would (the columns are solved
+// in the same order and the same arithmetic).  Nearly singular subsets,
+// whose every inverse column is large, then cost one solve instead of D.
+template <int D>
+__device__ inline bool cond1_exceeds(const double* A, const int* P, double nrm, double eps)
+{
+    int PT[D];
+    inverse_perm<D>(P, PT);
+    double inrm = -1;
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+        double w[D];
+#pragma unroll
+        for (int j = 0; j < D; j++) w[j] = (j == PT[i]) ? 1.0 : 0.0;
+        lu_solve_inplace<D>(A, w);
+        double s = 0;
+#pragma unroll
+        for (int j = 0; j < D; j++) s += fabs(w[j]);
+        if (nrm * s > eps) return true;
+        if (dlt(inrm, s)) inrm = s;
+    }
+    return nrm * inrm > eps;
+}
+
 template <int D>
 __device__ inline void solve_lu(const double* LU, const int* P, const double* b, double* x)
 {

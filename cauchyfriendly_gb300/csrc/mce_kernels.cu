@@ -638,7 +638,7 @@ __global__ void k_build_B_vertices(ParentList P, long long nP, const long long* 
         }
         if (plu<D>(Ac, Pv)) {
             const double bound = nrm * (double)inv_norm1_bound<D>(Ac);
-            if ((bound <= 0.1 * kCondEps) || !(cond1_from_lu<D>(Ac, Pv, nrm) > kCondEps)) {
+            if ((bound <= 0.1 * kCondEps) || !cond1_exceeds<D>(Ac, Pv, nrm, kCondEps)) {
                 solve_lu<D>(Ac, Pv, bc, v);
                 unsigned inmask = 0;
                 for (int j = 0; j < D; j++) inmask |= 1u << c[j];
