@@ -19,6 +19,18 @@ counter) / time.
           measurement buffers, wall clock around the call
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Other workloads (--workload, one JSON line each; see their functions):
+  windows5  the 5-state LTV sliding-window configuration (window 6, two
+            measurements per step) for --window-steps steps
+  adjoint   one gradient of the 4-state window-7 sliding-window
+            log-likelihood against the manager's forward run, with the
+            reference's central-difference gradient as the CPU baseline
+  mle       Adam on the shared log-scales of 64 LTV sliding-window
+            estimators over batched adjoint gradients
+  window7   one window of the 7-state LTV model as far as its tables fit
+  rel2d     the relative-system 2-D pdf of two 5-state estimators
+  cpdfnd    the N-D conditional pdf of a 4-state estimator at many points
 """
 from __future__ import annotations
 
