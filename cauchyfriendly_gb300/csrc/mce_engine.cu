@@ -1847,7 +1847,12 @@ public:
     int cpdf_points(int e, const int* idx, int nm, const double* nu_bar, const double* x, int npts, double* out)
     {
         if (e < 0 || e >= E || !x || !out || npts < 1) return MCE_ERR_ARG;
-        if (MC > 16) {
+        // the largest shape the estimator's terms have now (the handle's
+        // capacity MC may be larger)
+        int MB = 0;
+        for (int m = 0; m < (int)est[e].tps.size(); m++)
+            if (est[e].tps[m] > 0) MB = m;
+        if (MB > 16) {
             set_error("N-D pdf: terms of more than 16 hyperplanes are not supported");
             return MCE_ERR_SHAPE;
         }
@@ -1871,6 +1876,7 @@ public:
         NdInput in;
         in.D = D;
         in.MC = MC;
+        in.MB = std::max(MB, 1);
         in.n = hpstart[e + 1] - a;
         in.m = P.m.ptr + a;
         in.A = P.A.ptr + a * MC * D;

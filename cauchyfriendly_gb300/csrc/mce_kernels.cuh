@@ -72,6 +72,7 @@ inline long long gtable_bitmap_words(int MC, int D, int cells_cap = 0)
 // contiguous range of a parent list) and tables.
 struct NdInput {
     int D = 0, MC = 0;
+    int MB = 0;  // the most rows any of the terms has (MC: the storage's row capacity)
     long long n = 0;
     const int* m = nullptr;
     const double* A = nullptr;  // [n][MC][D]

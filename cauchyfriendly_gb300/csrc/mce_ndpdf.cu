@@ -416,12 +416,13 @@ __global__ void k_nd_list(const int* big, const long long* bscan, long long nk, 
 // else the ascending keys from coff[c] on.
 template <int LC>
 __global__ void k_nd_cells(const long long* ptoff, const int* ptcnt, const int* pkeys, NdKids K,
-                           const long long* list, const long long* nlist, int MC, const long long* coff,
+                           const long long* list, const long long* nlist, int MC, int MB, const long long* coff,
                            int* keys_out)
 {
     extern __shared__ unsigned nd_smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
-    const int words = (1 << MC) > 32 ? (1 << MC) / 32 : 1;
+    // bitmaps of 2^MB bits: no parent or child has more than MB rows
+    const int words = (1 << MB) > 32 ? (1 << MB) / 32 : 1;
     unsigned* PB = nd_smem + (size_t)wib * (2 * words + 32);
     unsigned* RK = PB + words;
     int* bmk = reinterpret_cast<int*>(RK + words);
@@ -806,7 +807,7 @@ namespace {
 
 template <int LD>
 int nd_level(NdWork& w, NdTerms P, const int* pkeys, const cd* pvals, long long n, long long npairs, const double* x,
-             int D, int MC, NdTermBufs& next, int kb, long long* n_next, const LaunchCfg& lc)
+             int D, int MC, int MB, NdTermBufs& next, int kb, long long* n_next, const LaunchCfg& lc)
 {
     constexpr int LC = LD - 1;
     int s;
@@ -829,7 +830,7 @@ int nd_level(NdWork& w, NdTerms P, const int* pkeys, const cd* pvals, long long 
     k_nd_lower<LD><<<nd_grid(nk, thr, lc.num_sms), thr, 0, lc.stream>>>(P, n, npairs, x, D, w.coff.ptr, nk, MC, K,
                                                                       w.err.ptr);
     // cells: counts, offsets, keys
-    const int words = (1 << MC) > 32 ? (1 << MC) / 32 : 1;
+    const int words = (1 << MB) > 32 ? (1 << MB) / 32 : 1;
     const size_t pw = (size_t)(2 * words + 32) * 4;
     int warps = (int)(96 * 1024 / pw);
     if (warps > 4) warps = 4;
@@ -849,8 +850,8 @@ int nd_level(NdWork& w, NdTerms P, const int* pkeys, const cd* pvals, long long 
     scan_int_to_ll(w.big.ptr, w.kscan.ptr, nk, w.ss, lc);
     k_nd_list<<<nd_grid(nk, thr, lc.num_sms), thr, 0, lc.stream>>>(w.big.ptr, w.kscan.ptr, nk, w.blist.ptr);
     const long long* nlist = w.kscan.ptr + nk;
-    k_nd_cells<LC><<<cgrid, warps * 32, sm, lc.stream>>>(P.toff, P.tcnt, pkeys, K, w.blist.ptr, nlist, MC, nullptr,
-                                                         nullptr);
+    k_nd_cells<LC><<<cgrid, warps * 32, sm, lc.stream>>>(P.toff, P.tcnt, pkeys, K, w.blist.ptr, nlist, MC, MB,
+                                                         nullptr, nullptr);
     scan_int_to_ll(K.ccnt, w.cellof.ptr, nk, w.ss, lc);
     long long ncell = 0;
     ND_CUDA(cudaMemcpyAsync(&ncell, w.cellof.ptr + nk, sizeof(long long), cudaMemcpyDeviceToHost, lc.stream));
@@ -860,7 +861,7 @@ int nd_level(NdWork& w, NdTerms P, const int* pkeys, const cd* pvals, long long 
     if ((s = w.vals[kb].ensure(ncell + 1))) return s;
     k_nd_cells_small<LC><<<nd_grid(nk, thr, lc.num_sms), thr, 0, lc.stream>>>(K, nk, w.cellof.ptr, w.keys[kb].ptr,
                                                                             nullptr);
-    k_nd_cells<LC><<<cgrid, warps * 32, sm, lc.stream>>>(P.toff, P.tcnt, pkeys, K, w.blist.ptr, nlist, MC,
+    k_nd_cells<LC><<<cgrid, warps * 32, sm, lc.stream>>>(P.toff, P.tcnt, pkeys, K, w.blist.ptr, nlist, MC, MB,
                                                          w.cellof.ptr, w.keys[kb].ptr);
     if (ncell > 0)
         k_nd_gvals<LC><<<nd_grid(ncell, thr, lc.num_sms), thr, 0, lc.stream>>>(
@@ -884,17 +885,17 @@ int nd_level(NdWork& w, NdTerms P, const int* pkeys, const cd* pvals, long long 
 }
 
 int nd_level_dispatch(int LD, NdWork& w, NdTerms P, const int* pkeys, const cd* pvals, long long n,
-                      long long npairs, const double* x, int D, int MC, NdTermBufs& next, int kb, long long* n_next,
-                      const LaunchCfg& lc)
+                      long long npairs, const double* x, int D, int MC, int MB, NdTermBufs& next, int kb,
+                      long long* n_next, const LaunchCfg& lc)
 {
     switch (LD) {
-    case 2: return nd_level<2>(w, P, pkeys, pvals, n, npairs, x, D, MC, next, kb, n_next, lc);
-    case 3: return nd_level<3>(w, P, pkeys, pvals, n, npairs, x, D, MC, next, kb, n_next, lc);
-    case 4: return nd_level<4>(w, P, pkeys, pvals, n, npairs, x, D, MC, next, kb, n_next, lc);
-    case 5: return nd_level<5>(w, P, pkeys, pvals, n, npairs, x, D, MC, next, kb, n_next, lc);
-    case 6: return nd_level<6>(w, P, pkeys, pvals, n, npairs, x, D, MC, next, kb, n_next, lc);
-    case 7: return nd_level<7>(w, P, pkeys, pvals, n, npairs, x, D, MC, next, kb, n_next, lc);
-    case 8: return nd_level<8>(w, P, pkeys, pvals, n, npairs, x, D, MC, next, kb, n_next, lc);
+    case 2: return nd_level<2>(w, P, pkeys, pvals, n, npairs, x, D, MC, MB, next, kb, n_next, lc);
+    case 3: return nd_level<3>(w, P, pkeys, pvals, n, npairs, x, D, MC, MB, next, kb, n_next, lc);
+    case 4: return nd_level<4>(w, P, pkeys, pvals, n, npairs, x, D, MC, MB, next, kb, n_next, lc);
+    case 5: return nd_level<5>(w, P, pkeys, pvals, n, npairs, x, D, MC, MB, next, kb, n_next, lc);
+    case 6: return nd_level<6>(w, P, pkeys, pvals, n, npairs, x, D, MC, MB, next, kb, n_next, lc);
+    case 7: return nd_level<7>(w, P, pkeys, pvals, n, npairs, x, D, MC, MB, next, kb, n_next, lc);
+    case 8: return nd_level<8>(w, P, pkeys, pvals, n, npairs, x, D, MC, MB, next, kb, n_next, lc);
     default: return MCE_ERR_ARG;
     }
 }
@@ -908,7 +909,7 @@ int nd_pdf_eval(const NdInput& in, const double* x_host, int npts, double* out_h
                 long long* launches)
 {
     if (!w || npts < 1 || !x_host || !out_host || in.D < 1 || in.D > kMaxDim) return MCE_ERR_ARG;
-    if (in.MC > kNdMaxRows) {
+    if (in.MB > kNdMaxRows || in.MB > in.MC) {
         report_error("N-D pdf: terms of more than 16 hyperplanes are not supported");
         return MCE_ERR_SHAPE;
     }
@@ -987,7 +988,7 @@ int nd_pdf_chunk(const NdInput& in, const double* x_host, int npts, double* out_
         long long nn = 0;
         NdTermBufs& next = w->lev[cur];
         s = nd_level_dispatch(ld, *w, P, pkeys, pvals, n, first ? n * npts : n, first ? w->x.ptr : nullptr, D, MC,
-                              next, cur, &nn, lc);
+                              in.MB, next, cur, &nn, lc);
         if (s) return s;
         int err = 0;
         ND_CUDA(cudaMemcpyAsync(&err, w->err.ptr, sizeof(int), cudaMemcpyDeviceToHost, lc.stream));

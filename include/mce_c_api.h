@@ -169,8 +169,9 @@ int mce_cpdf_1d_grid(mce_handle* h, int est, int marg_idx, const double* bar_nu,
  * whose arrangements agree within 1e-8 between the lowerings): the same sum
  * up to rounding.  MCE_ERR_ARG before the first step or when the last step
  * reported moment errors (the reference asserts), MCE_ERR_DONE after the
- * last step, MCE_ERR_SHAPE above 16 hyperplanes per term (the N-D pdf keeps
- * its lowered terms' cell sets in shared memory), MCE_ERR_DEVICE
+ * last step, MCE_ERR_SHAPE when a current term has more than 16 hyperplanes
+ * (the N-D pdf keeps its lowered terms' cell sets in shared memory; the
+ * handle's capacity may be larger), MCE_ERR_DEVICE
  * where the reference exits (an anti-coaligned pair of rows that do not
  * enter the integration). */
 int mce_cpdf_nd(mce_handle* h, int est, const double* x, int npts, double* out);

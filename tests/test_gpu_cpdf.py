@@ -208,11 +208,24 @@ def test_gpu_nd_pdf_against_oracle_on_larger_estimators():
         assert close(got[pick[:2]], apart) <= G.REL_TOL, (prob["d"], close(got[pick[:2]], apart))
         est.close()
         orc.close()
-    # terms of more than 16 hyperplanes (here up to 3 + 7 * 2 = 17) are refused
-    prob = W.many_gamma(3, 2, 8, seed=14)
+    # a handle with room for 21 hyperplanes: its terms of at most 9 rows after
+    # 4 steps are evaluated (against the oracle, lowering every pair apart),
+    # its terms of 17 rows after 8 steps are refused
+    prob = W.many_gamma(3, 2, 10, seed=14)
     rp, bp = oracle.draw_reference_constants(23, 3, oracle.max_shape_of(prob))
-    est = CE(prob["A0"], prob["p0"], prob["b0"], 8, 3, 0, 2, 1, root_point=rp, b_pert=bp)
-    est.step(prob["msmts"][0, 0], prob["Phi"], prob["Gamma"], prob["beta"], prob["H"][0], prob["gamma"][0])
+    est = CE(prob["A0"], prob["p0"], prob["b0"], 10, 3, 0, 2, 1, root_point=rp, b_pert=bp)
+    orc = oracle.Oracle(prob, rp, bp)
+    for k in range(4):
+        est.step(prob["msmts"][k, 0], prob["Phi"], prob["Gamma"], prob["beta"], prob["H"][0], prob["gamma"][0])
+        orc.step(k, 0)
+    mu = orc.moments()["mean"].real
+    X = mu + np.array([[0.0, 0.0, 0.0], [0.3, -0.2, 0.1], [-1.0, 0.5, 2.0]])
+    got = est.cpdf_nd(X)
+    want = np.array([orc.cpdf_nd(x, reduce=False) for x in X])
+    assert G.relerr(got, want, floor=1e-3) <= G.REL_TOL, G.relerr(got, want, floor=1e-3)
+    orc.close()
+    for k in range(4, 8):
+        est.step(prob["msmts"][k, 0], prob["Phi"], prob["Gamma"], prob["beta"], prob["H"][0], prob["gamma"][0])
     with pytest.raises(_lib.MceError, match="16 hyperplanes"):
         est.cpdf_nd(np.zeros(3))
     est.close()
